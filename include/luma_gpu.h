@@ -1,0 +1,166 @@
+/*
+ * luma_gpu.h — C ABI of the GB300 lattice-Boltzmann time step.
+ *
+ * This is the drop-in boundary for LUMA's hot path.  The reference has no
+ * plugin or FFI layer: its seam is the C++ member functions
+ *   void GridObj::LBM_multi_opt(int subcycle = 0)      (LUMA inc/GridObj.h:188,
+ *        body src/GridObj_ops_lbm_optimised.cpp:36-193, called from
+ *        src/main_lbm.cpp:441 and recursively from :45-49)
+ *   void ObjectManager::ibm_apply(GridObj*, bool)      (LUMA inc/ObjectManager.h:142,
+ *        body src/ObjectManager_ops_ibm.cpp:33-54)
+ * whose state is the GridObj members f, fNew, u, rho, force_xyz, LatTyp,
+ * omega, dt, dh, ux_in/uy_in/uz_in, CoarseLims and the sub-grid tree
+ * (LUMA inc/GridObj.h:54-127).  A host shim compiled into those member
+ * functions forwards to the entry points below.
+ *
+ * Conventions
+ *  - Every entry point returns an int status: LUMA_OK (0) or a negative
+ *    LUMA_E_* code; none throws or exits.  luma_gpu_last_error_string()
+ *    describes the most recent failure on the calling thread.
+ *  - Host arrays passed in or out use the reference's layout: site index
+ *    id = k + j*K + i*K*M (src/GridObj_ops_lbm_optimised.cpp:79); per-site
+ *    vectors are interleaved, f[v + id*Q], u[d + id*dims]
+ *    (LUMA inc/IVector.h:94-101).  The device keeps its own layout
+ *    (structure of arrays, FP64 or shifted FP32) and converts on transfer.
+ *  - Plain C types only; handles are opaque.
+ */
+#ifndef LUMA_GPU_H
+#define LUMA_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define LUMA_GPU_ABI_VERSION 1
+
+/* Status codes. */
+#define LUMA_OK 0
+#define LUMA_E_INVALID (-1)     /* bad argument or unsupported configuration */
+#define LUMA_E_CUDA (-2)        /* a CUDA runtime call failed */
+#define LUMA_E_NOMEM (-3)       /* device or host allocation failed */
+#define LUMA_E_STATE (-4)       /* call not valid in the handle's current state */
+#define LUMA_E_TIMEOUT (-5)     /* a bounded device-side wait gave up */
+#define LUMA_E_NUMERIC (-6)     /* watchdog found a non-finite or drifting value */
+#define LUMA_E_DOMAIN (-7)      /* e.g. an IBM marker left the grid */
+
+/* Site labels: the values of the reference's eType
+ * (LUMA inc/Enumerations.h:84-96). */
+enum {
+    LUMA_SITE_SOLID = 0,
+    LUMA_SITE_FLUID = 1,
+    LUMA_SITE_REFINED = 2,
+    LUMA_SITE_TL_TO_COARSER = 3,
+    LUMA_SITE_TL_TO_FINER = 4,
+    LUMA_SITE_BFL = 5,
+    LUMA_SITE_VELOCITY = 6,
+    LUMA_SITE_PRESSURE = 7,
+    LUMA_SITE_SLIP = 8,
+    LUMA_SITE_EXTRAPOLATE_RIGHT = 9
+};
+
+/* Storage / arithmetic precision of the populations. */
+enum {
+    LUMA_PREC_FP64 = 0,          /* the reference's arithmetic */
+    LUMA_PREC_FP32_SHIFTED = 1   /* stores f_i - w_i*rho0 in FP32, collides in FP32 */
+};
+
+/* Collision operator (definitions.h L_USE_KBC_COLLISION / L_USE_BGKSMAG). */
+enum {
+    LUMA_COLL_BGK = 0,           /* _LBM_collide_opt, :765-790 */
+    LUMA_COLL_BGK_SMAG = 1,      /* _LBM_collide_opt with _LBM_smag, :717-756 */
+    LUMA_COLL_KBC = 2            /* _LBM_kbcCollide_opt, :1122-1305 */
+};
+
+/* Feature flags (compile-time switches of the reference's definitions.h). */
+#define LUMA_FLAG_REGULARISED 0x1   /* L_REGULARISED_BOUNDARIES */
+#define LUMA_FLAG_IBM 0x2           /* L_IBM_ON: split loop, Guo forcing, IBM pass */
+#define LUMA_FLAG_GRAVITY 0x4       /* L_GRAVITY_ON */
+#define LUMA_FLAG_FIX_MACRO3D 0x8   /* add 0.5*F_z to z-momentum (the reference adds it
+                                       to x, src/GridObj_ops_lbm_optimised.cpp:833) */
+#define LUMA_FLAG_FIX_KBC 0x10      /* KBC relaxes the streamed populations (the reference
+                                       relaxes the pre-stream f, :1147,1296) */
+
+/* Description of one grid (one level/region of the hierarchy).  Mirrors the
+ * GridObj members it is filled from; arrays are read during create only. */
+typedef struct luma_grid_desc {
+    int abi_version;            /* LUMA_GPU_ABI_VERSION */
+    int level, region;          /* GridObj::level, region_number */
+    int dims, Q;                /* L_DIMS, L_NUM_VELS: (2,9), (3,19) or (3,27) */
+    int N, M, K;                /* N_lim, M_lim, K_lim (K = 1 in 2D) */
+    int precision;              /* LUMA_PREC_* */
+    int collision;              /* LUMA_COLL_* */
+    int flags;                  /* LUMA_FLAG_* */
+    double omega, dt, dh;       /* GridObj::omega, dt, dh */
+    double refinement_ratio;    /* GridObj::refinement_ratio = 2^-level */
+    double rho_in;              /* L_RHOIN */
+    double velocity_ramp;       /* L_VELOCITY_RAMP (dimensionless time); 0 = no ramp */
+    double pressure_delta;      /* GridUnits::pd2dlbm(L_PRESSURE_DELTA) (lattice units) */
+    double gravity;             /* GridObj::gravity (lattice units) */
+    int gravity_dir;            /* L_GRAVITY_DIRECTION (0,1,2) */
+    double csmag;               /* L_CSMAG */
+    double global_edges[6];     /* GridManager global edges of L0: xmin,xmax,ymin,ymax,zmin,zmax */
+    double wall_thickness[6];   /* L_WALL_THICKNESS_{LEFT,RIGHT,BOTTOM,TOP,FRONT,BACK} */
+    int coarse_lims[6];         /* CoarseLimsX/Y/Z [min,max] on the parent (level > 0) */
+    const int32_t *lattyp;      /* N*M*K site labels (LUMA_SITE_*) */
+    const double *xpos, *ypos, *zpos;    /* XPos[N], YPos[M], ZPos[K] */
+    const double *ux_in, *uy_in, *uz_in; /* inlet profile, length M */
+} luma_grid_desc;
+
+typedef struct luma_gpu_grid luma_gpu_grid;
+
+/* Reductions over the fluid-updated sites of one grid, accumulated in FP64. */
+typedef struct luma_reduction {
+    double mass;                /* sum rho */
+    double momentum[3];         /* sum rho*u_d */
+    double kinetic_energy;      /* sum 0.5*rho*|u|^2 */
+    double max_speed;           /* max |u| */
+    int64_t nonfinite;          /* count of non-finite rho/u values */
+} luma_reduction;
+
+/* ---- version / errors -------------------------------------------------- */
+int luma_gpu_abi_version(void);
+const char *luma_gpu_last_error_string(void);
+
+/* ---- grid lifetime ------------------------------------------------------ */
+/* Replaces GridObj(int level) / GridObj(int region, GridObj& parent) and
+ * LBM_addSubGrid (LUMA src/GridObj.cpp:51-118): allocates device state for
+ * one grid; `parent` is NULL for level 0, else the parent's handle (the new
+ * grid becomes its next sub-grid, in region order). */
+int luma_gpu_grid_create(const luma_grid_desc *desc, luma_gpu_grid *parent, luma_gpu_grid **out);
+/* Destroys a grid and its sub-grids. */
+int luma_gpu_grid_destroy(luma_gpu_grid *grid);
+/* Selects the CUDA stream (a cudaStream_t, may be NULL for the legacy
+ * stream) used by every subsequent call on this grid tree. */
+int luma_gpu_set_stream(luma_gpu_grid *root, void *cuda_stream);
+
+/* ---- state transfer ------------------------------------------------------ */
+/* Host -> device: f (N*M*K*Q), u (N*M*K*dims), rho (N*M*K); force_xyz may be
+ * NULL.  Arrays in the reference layout (post-collision f, as GridObj::f
+ * holds between time steps).  Sets the grid's step counter to t. */
+int luma_gpu_upload_state(luma_gpu_grid *grid, const double *f, const double *u,
+                          const double *rho, const double *force_xyz, int t);
+/* Device -> host, same layout; any pointer may be NULL to skip it. */
+int luma_gpu_download_state(luma_gpu_grid *grid, double *f, double *u, double *rho,
+                            double *force_xyz);
+/* Step counter of a grid (GridObj::t). */
+int luma_gpu_get_time(const luma_gpu_grid *grid, int *t);
+
+/* ---- the time step ------------------------------------------------------ */
+/* Runs `nsteps` calls of GridObj::LBM_multi_opt() on the root grid: each
+ * recursively advances every sub-grid two sub-steps, then this grid one
+ * step (explode/coalesce, IBM pass and collision included).  Asynchronous
+ * on the grid's stream. */
+int luma_gpu_step(luma_gpu_grid *root, int nsteps);
+/* Blocks until all work queued on the grid's stream has finished. */
+int luma_gpu_synchronize(luma_gpu_grid *root);
+
+/* ---- reductions / watchdog ----------------------------------------------- */
+int luma_gpu_reduce(luma_gpu_grid *grid, luma_reduction *out);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* LUMA_GPU_H */

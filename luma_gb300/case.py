@@ -1,0 +1,319 @@
+"""Host-side case set-up: the definitions-driven initialisation of a level-0 grid.
+
+Mirrors the reference's compile-time configuration (LUMA ``inc/definitions.h``)
+and the L0 initialisation that consumes it, producing exactly the inputs the
+time step reads:
+
+* global edges ``dh * L_N`` etc. (``src/GridManager.cpp:45-51``);
+* site positions ``linspace(dh/2, edge - dh/2, n)`` (``src/GridObj_init_grids.cpp:237-245``,
+  ``inc/GridUtils.h:289-308``);
+* wall labels with the reference's precedence (``LBM_initBoundLab``,
+  ``src/GridObj_init_grids.cpp:983-1097``; ``LBM_setBCPrecedence`` :1372-1377);
+* the inlet profile (``_LBM_initSetInletProfile`` :1322-1360);
+* initial u, rho (``LBM_initVelocity``/``LBM_initRho`` :37-152) and
+  ``nu``/``omega`` (:336-344);
+* the Guo force field at t=0 under gravity (:284-291).
+
+Arithmetic follows the reference's expression order so the values are
+bit-identical to those the reference computes.
+"""
+from __future__ import annotations
+
+import math
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import _abi as A
+
+CS = 1.0 / math.sqrt(3.0)
+
+
+@dataclass
+class Definitions:
+    """The subset of ``definitions.h`` switches that shape the time step."""
+
+    dims: int = 2
+    resolution: int = 100          # L_RESOLUTION
+    timestep: float = 0.0001       # L_TIMESTEP
+    bx: float = 1.0                # L_BX
+    by: float = 1.0                # L_BY
+    bz: float = 1.0                # L_BZ
+    re: float | None = 100.0       # L_RE
+    nu: float | None = None        # L_NU (overrides L_RE when set)
+    ux0: float = 0.0               # L_UX0
+    uy0: float = 0.0               # L_UY0
+    uz0: float = 0.0               # L_UZ0
+    rho_in: float = 1.0            # L_RHOIN
+    parabolic_inlet: bool = False  # L_PARABOLIC_INLET
+    no_flow: bool = True           # L_NO_FLOW
+    velocity_ramp: float = 0.0     # L_VELOCITY_RAMP (0 = undefined)
+    regularised: bool = False      # L_REGULARISED_BOUNDARIES
+    kbc: bool = False              # L_USE_KBC_COLLISION
+    smagorinsky: bool = False      # L_USE_BGKSMAG
+    csmag: float = 0.3             # L_CSMAG
+    ibm: bool = False              # L_IBM_ON
+    gravity: bool = False          # L_GRAVITY_ON
+    gravity_force: float = 0.0     # L_GRAVITY_FORCE
+    gravity_dir: int = 0           # L_GRAVITY_DIRECTION
+    pressure_delta: float = 0.0    # L_PRESSURE_DELTA
+    physical_rho: float = 1000.0   # L_PHYSICAL_RHO
+    # L_WALL_LEFT, RIGHT, BOTTOM, TOP, FRONT, BACK
+    walls: tuple = (A.FLUID,) * 6
+    # L_WALL_THICKNESS_* in coarse cells
+    wall_cells: tuple = (1.0,) * 6
+
+    @property
+    def Q(self) -> int:
+        if self.dims == 2:
+            return 9
+        return 27 if self.kbc else 19
+
+    def sizes(self) -> tuple[int, int, int]:
+        n = int(self.bx * self.resolution)
+        m = int(self.by * self.resolution)
+        k = int(self.bz * self.resolution) if self.dims == 3 else 1
+        return n, m, k
+
+
+@dataclass
+class Level0:
+    defs: Definitions
+    N: int
+    M: int
+    K: int
+    dh: float
+    dt: float
+    nu: float
+    omega: float
+    gravity: float
+    global_edges: np.ndarray
+    wall_thickness: np.ndarray
+    xpos: np.ndarray
+    ypos: np.ndarray
+    zpos: np.ndarray
+    typ: np.ndarray
+    ux_in: np.ndarray
+    uy_in: np.ndarray
+    uz_in: np.ndarray
+    u: np.ndarray
+    rho: np.ndarray
+    force_xyz: np.ndarray = field(default=None)
+
+    @property
+    def ncell(self) -> int:
+        return self.N * self.M * self.K
+
+    def flags(self, fix_macro3d: bool = False, fix_kbc: bool = False) -> int:
+        d = self.defs
+        fl = 0
+        if d.regularised:
+            fl |= A.FLAG_REGULARISED
+        if d.ibm:
+            fl |= A.FLAG_IBM
+        if d.gravity:
+            fl |= A.FLAG_GRAVITY
+        if fix_macro3d:
+            fl |= A.FLAG_FIX_MACRO3D
+        if fix_kbc:
+            fl |= A.FLAG_FIX_KBC
+        return fl
+
+    def desc(self, precision: int = A.PREC_FP64, fix_macro3d: bool = False,
+             fix_kbc: bool = False) -> "A.GridDesc":
+        """A level-0 ``luma_grid_desc``; keeps the arrays it points to alive."""
+        d = self.defs
+        g = A.GridDesc()
+        g.abi_version = A.ABI_VERSION
+        g.level, g.region = 0, 0
+        g.dims, g.Q = d.dims, d.Q
+        g.N, g.M, g.K = self.N, self.M, self.K
+        g.precision = precision
+        g.collision = A.COLL_KBC if d.kbc else (A.COLL_BGK_SMAG if d.smagorinsky else A.COLL_BGK)
+        g.flags = self.flags(fix_macro3d, fix_kbc)
+        g.omega, g.dt, g.dh = self.omega, self.dt, self.dh
+        g.refinement_ratio = 1.0
+        g.rho_in = d.rho_in
+        g.velocity_ramp = d.velocity_ramp
+        g.pressure_delta = pd2dlbm(d.pressure_delta, self.dh, self.dt, self.dm)
+        g.gravity = self.gravity
+        g.gravity_dir = d.gravity_dir
+        g.csmag = d.csmag
+        for i in range(6):
+            g.global_edges[i] = float(self.global_edges[i])
+            g.wall_thickness[i] = float(self.wall_thickness[i])
+        keep = (np.ascontiguousarray(self.typ, dtype=np.int32),
+                np.ascontiguousarray(self.xpos), np.ascontiguousarray(self.ypos),
+                np.ascontiguousarray(self.zpos), np.ascontiguousarray(self.ux_in),
+                np.ascontiguousarray(self.uy_in), np.ascontiguousarray(self.uz_in))
+        g.lattyp = A.iptr(keep[0])
+        g.xpos, g.ypos, g.zpos = A.dptr(keep[1]), A.dptr(keep[2]), A.dptr(keep[3])
+        g.ux_in, g.uy_in, g.uz_in = A.dptr(keep[4]), A.dptr(keep[5]), A.dptr(keep[6])
+        g._keep = keep
+        return g
+
+    @property
+    def dm(self) -> float:
+        return (self.defs.physical_rho / self.defs.rho_in) * self.dh * self.dh * self.dh
+
+
+def pd2dlbm(p: float, dh: float, dt: float, dm: float) -> float:
+    """GridUnits::pd2dlbm (inc/GridUnits.h:171-174)."""
+    return (p * dh * (dt * dt) / dm) / (CS * CS)
+
+
+def linspace(lo: float, hi: float, n: int) -> np.ndarray:
+    """GridUtils::linspace (inc/GridUtils.h:289-308): lo + spacing*i."""
+    n = max(n, 2)
+    spacing = (hi - lo) / float(n - 1)
+    return np.array([lo + spacing * i for i in range(n)], dtype=np.float64)
+
+
+def ramp_coefficient(defs: Definitions, t: float) -> float:
+    """GridUtils::getVelocityRampCoefficient (src/GridUtils.cpp:1808-1816)."""
+    if defs.velocity_ramp > 0 and t <= defs.velocity_ramp:
+        return (1.0 - math.cos(math.pi * t / defs.velocity_ramp)) / 2.0
+    return 1.0
+
+
+def _precedence(cur: int, want: int) -> int:
+    """LBM_setBCPrecedence (src/GridObj_init_grids.cpp:1372-1377)."""
+    if cur == A.SOLID or want == A.SOLID:
+        return A.SOLID
+    if cur == A.VELOCITY:
+        return A.VELOCITY
+    return want
+
+
+def build_level0(defs: Definitions) -> Level0:
+    N, M, K = defs.sizes()
+    dh = 1.0 / float(defs.resolution)
+    dt = defs.timestep
+    edges = np.array([0.0, dh * N, 0.0, dh * M, 0.0, dh * K if defs.dims == 3 else 0.0])
+    wt = np.array([c * dh for c in defs.wall_cells], dtype=np.float64)
+    xpos = linspace(dh / 2.0, edges[1] - dh / 2.0, N)
+    ypos = linspace(dh / 2.0, edges[3] - dh / 2.0, M)
+    zpos = linspace(dh / 2.0, edges[5] - dh / 2.0, K) if defs.dims == 3 else np.zeros(1)
+
+    typ = np.full((N, M, K), A.FLUID, dtype=np.int32)
+    left, right, bottom, top, front, back = defs.walls
+
+    def label(sel, want):
+        sub = typ[sel]
+        flat = sub.reshape(-1)
+        for n_ in range(flat.size):
+            flat[n_] = _precedence(int(flat[n_]), want)
+        typ[sel] = flat.reshape(sub.shape)
+
+    for i in range(N):
+        if xpos[i] <= wt[0]:
+            label((slice(i, i + 1), slice(None), slice(None)), left)
+    for i in range(N):
+        if xpos[i] >= edges[1] - wt[1]:
+            label((slice(i, i + 1), slice(None), slice(None)), right)
+    if defs.dims == 3:
+        for k in range(K):
+            if zpos[k] <= wt[4]:
+                label((slice(None), slice(None), slice(k, k + 1)), front)
+        for k in range(K):
+            if zpos[k] >= edges[5] - wt[5]:
+                label((slice(None), slice(None), slice(k, k + 1)), back)
+    for j in range(M):
+        if ypos[j] <= wt[2]:
+            label((slice(None), slice(j, j + 1), slice(None)), bottom)
+    for j in range(M):
+        if ypos[j] >= edges[3] - wt[3]:
+            label((slice(None), slice(j, j + 1), slice(None)), top)
+
+    # Inlet profile.
+    if defs.parabolic_inlet:
+        b = edges[3] - wt[3]
+        p = (b + wt[2]) / 2.0
+        q = b - p
+        umax = (1.5 * defs.ux0 * dt) / dh
+        ux_in = np.array([umax * (1.0 - math.pow((ypos[j] - p) / q, 2.0)) for j in range(M)])
+        uy_in = np.zeros(M)
+        uz_in = np.zeros(M)
+    else:
+        ux_in = np.full(M, (defs.ux0 * dt) / dh)
+        uy_in = np.full(M, (defs.uy0 * dt) / dh)
+        uz_in = np.full(M, (defs.uz0 * dt) / dh)
+
+    # Initial velocity and density.
+    D = defs.dims
+    u = np.zeros((N, M, K, D))
+    rc = ramp_coefficient(defs, 0.0)
+    prof = np.stack([ux_in * rc, uy_in * rc, uz_in * rc], axis=1)[:, :D]
+    for i in range(N):
+        for j in range(M):
+            for k in range(K):
+                t_ = typ[i, j, k]
+                if defs.no_flow and t_ != A.VELOCITY:
+                    u[i, j, k] = 0.0
+                else:
+                    u[i, j, k] = prof[j]
+                if t_ == A.SOLID:
+                    u[i, j, k] = 0.0
+    rho = np.full((N, M, K), float(defs.rho_in))
+
+    nu_d = defs.nu if defs.nu is not None else 1.0 / float(defs.re)
+    nu = (nu_d * dt) / (dh * dh)
+    omega = 1.0 / ((nu / (CS * CS)) + 0.5)
+    gravity = (defs.gravity_force * (dt * dt)) / dh
+    force = np.zeros((N, M, K, D))
+    if defs.gravity:
+        force[..., defs.gravity_dir] = rho * gravity * 1.0
+    return Level0(defs=defs, N=N, M=M, K=K, dh=dh, dt=dt, nu=nu, omega=omega, gravity=gravity,
+                  global_edges=edges, wall_thickness=wt, xpos=xpos, ypos=ypos, zpos=zpos,
+                  typ=typ.reshape(-1), ux_in=ux_in, uy_in=uy_in, uz_in=uz_in,
+                  u=u.reshape(-1), rho=rho.reshape(-1), force_xyz=force.reshape(-1))
+
+
+# ---- lattice tables (src/stdafx.cpp:29-153) used by host-side helpers ----
+
+def lattice(dims: int, Q: int):
+    """Velocity set ``c`` (Q x 3 ints) and weights ``w`` in the reference's order."""
+    if (dims, Q) == (2, 9):
+        c = [(1, 0, 0), (-1, 0, 0), (0, 1, 0), (0, -1, 0), (1, 1, 0), (-1, -1, 0), (1, -1, 0),
+             (-1, 1, 0), (0, 0, 0)]
+        w = [1 / 9] * 4 + [1 / 36] * 4 + [4 / 9]
+    elif (dims, Q) == (3, 19):
+        c = [(1, 0, 0), (-1, 0, 0), (0, 1, 0), (0, -1, 0), (0, 0, 1), (0, 0, -1), (1, 1, 0),
+             (-1, -1, 0), (1, -1, 0), (-1, 1, 0), (0, 1, 1), (0, -1, -1), (0, 1, -1), (0, -1, 1),
+             (1, 0, 1), (-1, 0, -1), (-1, 0, 1), (1, 0, -1), (0, 0, 0)]
+        w = [1 / 18] * 6 + [1 / 36] * 12 + [1 / 3]
+    elif (dims, Q) == (3, 27):
+        c = [(1, 0, 0), (-1, 0, 0), (0, 1, 0), (0, -1, 0), (0, 0, 1), (0, 0, -1), (0, 1, 1),
+             (0, -1, -1), (0, 1, -1), (0, -1, 1), (1, 0, 1), (-1, 0, -1), (1, 0, -1), (-1, 0, 1),
+             (1, 1, 0), (-1, -1, 0), (1, -1, 0), (-1, 1, 0), (1, 1, 1), (-1, -1, -1), (-1, -1, 1),
+             (1, 1, -1), (-1, 1, 1), (1, -1, -1), (1, -1, 1), (-1, 1, -1), (0, 0, 0)]
+        w = [2 / 27] * 6 + [1 / 54] * 12 + [1 / 216] * 8 + [8 / 27]
+    else:
+        raise ValueError(f"no lattice D{dims}Q{Q}")
+    return np.array(c, dtype=np.int64), np.array(w, dtype=np.float64)
+
+
+def equilibrium(dims: int, Q: int, rho: np.ndarray, u: np.ndarray) -> np.ndarray:
+    """Vectorised _LBM_equilibrium_opt (src/GridObj_ops_lbm_optimised.cpp:674-705).
+
+    ``rho`` has shape (n,), ``u`` shape (n, dims); returns (n, Q) in the
+    reference's expression order (bit-identical for IEEE double)."""
+    c, w = lattice(dims, Q)
+    cs2 = CS * CS
+    u = u.reshape(-1, dims)
+    out = np.empty((u.shape[0], Q))
+    for v in range(Q):
+        cv = c[v]
+        if dims == 3:
+            A_ = (cv[0] * u[:, 0]) + (cv[1] * u[:, 1]) + (cv[2] * u[:, 2])
+            B_ = ((cv[0] * cv[0] - cs2) * (u[:, 0] * u[:, 0]) + (cv[1] * cv[1] - cs2) * (u[:, 1] * u[:, 1])
+                  + (cv[2] * cv[2] - cs2) * (u[:, 2] * u[:, 2])
+                  + float(2 * cv[0] * cv[1]) * u[:, 0] * u[:, 1]
+                  + float(2 * cv[0] * cv[2]) * u[:, 0] * u[:, 2]
+                  + float(2 * cv[1] * cv[2]) * u[:, 1] * u[:, 2])
+        else:
+            A_ = (cv[0] * u[:, 0]) + (cv[1] * u[:, 1])
+            B_ = ((cv[0] * cv[0] - cs2) * (u[:, 0] * u[:, 0]) + (cv[1] * cv[1] - cs2) * (u[:, 1] * u[:, 1])
+                  + float(2 * cv[0] * cv[1]) * u[:, 0] * u[:, 1])
+        out[:, v] = rho * w[v] * (1.0 + (A_ / cs2) + (B_ / (2.0 * cs2 * cs2)))
+    return out

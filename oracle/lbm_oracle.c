@@ -1,0 +1,753 @@
+/*
+ * ORACLE — test infrastructure only.  A plain-C restatement of the reference
+ * LUMA v1.7.12 lattice-Boltzmann time step (GridObj::LBM_multi_opt and its
+ * callees, src/GridObj_ops_lbm_optimised.cpp) used to check the CUDA path.
+ * Only tests, the smoke check and the benchmark's CPU-baseline leg use it;
+ * the product never links or calls it.
+ *
+ * It keeps the reference's arithmetic: FP64, the reference's operation
+ * order, the reference's array-of-structures layout (f[v + id*Q]), two
+ * population arrays swapped after every step, and the reference's quirks:
+ *  - the 3D macroscopic step adds 0.5*F_z to the x-momentum (:833) unless
+ *    LUMA_FLAG_FIX_MACRO3D is set;
+ *  - KBC relaxes the pre-stream f (:1147,1296) unless LUMA_FLAG_FIX_KBC;
+ *  - the forced-equilibrium velocity BC writes the current row's inlet
+ *    velocity into the source site's u (:255-269);
+ *  - transition-to-coarser sites are not collided (:144).
+ * Parity of this restatement with the reference itself is pinned by the
+ * golden fixtures in tests/golden (produced by the reference's own build).
+ *
+ * Build: gcc -O2 -ffp-contract=off -fPIC -shared [-fopenmp].
+ */
+#include <math.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+#include "../include/luma_gpu.h"
+
+/* ---------------- lattice tables (src/stdafx.cpp:29-153) ---------------- */
+
+static const int C9[9][3] = {{1, 0, 0}, {-1, 0, 0}, {0, 1, 0}, {0, -1, 0}, {1, 1, 0},
+                             {-1, -1, 0}, {1, -1, 0}, {-1, 1, 0}, {0, 0, 0}};
+static const double W9[9] = {1.0 / 9.0, 1.0 / 9.0, 1.0 / 9.0, 1.0 / 9.0, 1.0 / 36.0,
+                             1.0 / 36.0, 1.0 / 36.0, 1.0 / 36.0, 4.0 / 9.0};
+static const int C19[19][3] = {{1, 0, 0}, {-1, 0, 0}, {0, 1, 0}, {0, -1, 0}, {0, 0, 1},
+                               {0, 0, -1}, {1, 1, 0}, {-1, -1, 0}, {1, -1, 0}, {-1, 1, 0},
+                               {0, 1, 1}, {0, -1, -1}, {0, 1, -1}, {0, -1, 1}, {1, 0, 1},
+                               {-1, 0, -1}, {-1, 0, 1}, {1, 0, -1}, {0, 0, 0}};
+static const double W19[19] = {1.0 / 18.0, 1.0 / 18.0, 1.0 / 18.0, 1.0 / 18.0, 1.0 / 18.0,
+                               1.0 / 18.0, 1.0 / 36.0, 1.0 / 36.0, 1.0 / 36.0, 1.0 / 36.0,
+                               1.0 / 36.0, 1.0 / 36.0, 1.0 / 36.0, 1.0 / 36.0, 1.0 / 36.0,
+                               1.0 / 36.0, 1.0 / 36.0, 1.0 / 36.0, 1.0 / 3.0};
+static const int C27[27][3] = {{1, 0, 0}, {-1, 0, 0}, {0, 1, 0}, {0, -1, 0}, {0, 0, 1},
+                               {0, 0, -1}, {0, 1, 1}, {0, -1, -1}, {0, 1, -1}, {0, -1, 1},
+                               {1, 0, 1}, {-1, 0, -1}, {1, 0, -1}, {-1, 0, 1}, {1, 1, 0},
+                               {-1, -1, 0}, {1, -1, 0}, {-1, 1, 0}, {1, 1, 1}, {-1, -1, -1},
+                               {-1, -1, 1}, {1, 1, -1}, {-1, 1, 1}, {1, -1, -1}, {1, -1, 1},
+                               {-1, 1, -1}, {0, 0, 0}};
+static const double W27[27] = {
+    2.0 / 27.0,  2.0 / 27.0,  2.0 / 27.0,  2.0 / 27.0,  2.0 / 27.0,  2.0 / 27.0,  1.0 / 54.0,
+    1.0 / 54.0,  1.0 / 54.0,  1.0 / 54.0,  1.0 / 54.0,  1.0 / 54.0,  1.0 / 54.0,  1.0 / 54.0,
+    1.0 / 54.0,  1.0 / 54.0,  1.0 / 54.0,  1.0 / 54.0,  1.0 / 216.0, 1.0 / 216.0, 1.0 / 216.0,
+    1.0 / 216.0, 1.0 / 216.0, 1.0 / 216.0, 1.0 / 216.0, 1.0 / 216.0, 8.0 / 27.0};
+/* Opposites and specular reflections (src/GridUtils.cpp:31-69). */
+static const int OPP9[9] = {1, 0, 3, 2, 5, 4, 7, 6, 8};
+static const int OPP19[19] = {1, 0, 3, 2, 5, 4, 7, 6, 9, 8, 11, 10, 13, 12, 15, 14, 17, 16, 18};
+static const int OPP27[27] = {1,  0,  3,  2,  5,  4,  7,  6,  9,  8,  11, 10, 13, 12,
+                              15, 14, 17, 16, 19, 18, 21, 20, 23, 22, 25, 24, 26};
+static const int REF9[3][9] = {{1, 0, 2, 3, 7, 6, 5, 4, 8}, {0, 1, 3, 2, 6, 7, 4, 5, 8}, {0}};
+static const int REF19[3][19] = {
+    {1, 0, 2, 3, 4, 5, 9, 8, 7, 6, 10, 11, 12, 13, 16, 17, 14, 15, 18},
+    {0, 1, 3, 2, 4, 5, 8, 9, 6, 7, 13, 12, 11, 10, 14, 15, 16, 17, 18},
+    {0, 1, 2, 3, 5, 4, 6, 7, 8, 9, 12, 13, 10, 11, 17, 16, 15, 14, 18}};
+static const int REF27[3][27] = {
+    {1, 0, 2, 3, 4, 5, 6, 7, 8, 9, 13, 12, 11, 10, 17, 16, 15, 14, 22, 23, 24, 25, 18, 19, 20, 21, 26},
+    {0, 1, 3, 2, 4, 5, 9, 8, 7, 6, 10, 11, 12, 13, 16, 17, 14, 15, 24, 25, 22, 23, 20, 21, 18, 19, 26},
+    {0, 1, 2, 3, 5, 4, 8, 9, 6, 7, 12, 13, 10, 11, 14, 15, 16, 17, 21, 20, 19, 18, 25, 24, 23, 22, 26}};
+
+#define SQ(x) ((x) * (x))
+#define L_PI 3.14159265358979323846
+#define L_SQRT2 1.4142135623730950488016887242097
+
+typedef struct oracle_grid oracle_grid;
+struct oracle_grid {
+    luma_grid_desc d;
+    int ncell, Q, D;
+    const int (*c)[3];
+    const double *w;
+    const int *opp;
+    const int *refl; /* [3][Q] flattened */
+    int *typ;
+    double *xpos, *ypos, *zpos, *ux_in, *uy_in, *uz_in;
+    double *f, *fNew, *feq, *u, *rho, *force_xyz, *force_i, *u_n;
+    int t;
+    oracle_grid *parent;
+    oracle_grid *sub[8];
+    int nsub;
+    int has_ibm_bodies, has_flexible_bodies;
+    void (*ibm_hook)(oracle_grid *, void *); /* IBM pass (set by the IBM oracle) */
+    void *ibm_ctx;
+};
+
+static char g_err[512];
+static void set_err(const char *m) { snprintf(g_err, sizeof g_err, "%s", m); }
+const char *oracle_last_error(void) { return g_err; }
+
+static double cs_(void) { return 1.0 / sqrt(3.0); }
+
+/* ---- equilibrium: _LBM_equilibrium_opt, :674-705 ---- */
+static double feq_at(const oracle_grid *g, int id, int v) {
+    const double cs = cs_();
+    const int *c = g->c[v];
+    const double *u = g->u + (size_t)id * g->D;
+    double A, B;
+    if (g->D == 3) {
+        A = (c[0] * u[0]) + (c[1] * u[1]) + (c[2] * u[2]);
+        B = (SQ(c[0]) - SQ(cs)) * SQ(u[0]) + (SQ(c[1]) - SQ(cs)) * SQ(u[1]) +
+            (SQ(c[2]) - SQ(cs)) * SQ(u[2]) + 2 * c[0] * c[1] * u[0] * u[1] +
+            2 * c[0] * c[2] * u[0] * u[2] + 2 * c[1] * c[2] * u[1] * u[2];
+    } else {
+        A = (c[0] * u[0]) + (c[1] * u[1]);
+        B = (SQ(c[0]) - SQ(cs)) * SQ(u[0]) + (SQ(c[1]) - SQ(cs)) * SQ(u[1]) +
+            2 * c[0] * c[1] * u[0] * u[1];
+    }
+    return g->rho[id] * g->w[v] * (1.0 + (A / SQ(cs)) + (B / (2.0 * SQ(cs) * SQ(cs))));
+}
+
+/* ---- GridUtils::getVelocityRampCoefficient, src/GridUtils.cpp:1808-1816 ---- */
+static double ramp_coeff(const oracle_grid *g, double t) {
+    if (g->d.velocity_ramp > 0.0 && t <= g->d.velocity_ramp)
+        return (1.0 - cos(L_PI * t / g->d.velocity_ramp)) / 2.0;
+    return 1.0;
+}
+
+/* ---- GridUtils::isWithinDomainWall, src/GridUtils.cpp:1369-1430 ---- */
+static int within_domain_wall(const oracle_grid *g, double x, double y, double z, int nvec[3],
+                              int *ndir, int *edges) {
+    const double *E = g->d.global_edges, *T = g->d.wall_thickness;
+    nvec[0] = nvec[1] = nvec[2] = 0;
+    *ndir = -1;
+    *edges = 0;
+    if (x > 0.0 && x < T[0]) { *ndir = 0; nvec[0] = 1; (*edges)++; }
+    if (x < E[1] && x > E[1] - T[1]) { *ndir = 0; nvec[0] = -1; (*edges)++; }
+    if (y > 0.0 && y < T[2]) { *ndir = 1; nvec[1] = 1; (*edges)++; }
+    if (y < E[3] && y > E[3] - T[3]) { *ndir = 1; nvec[1] = -1; (*edges)++; }
+    if (g->D == 3) {
+        if (z > 0.0 && z < T[4]) { *ndir = 2; nvec[2] = 1; (*edges)++; }
+        if (z < E[5] && z > E[5] - T[5]) { *ndir = 2; nvec[2] = -1; (*edges)++; }
+    }
+    return *edges > 0;
+}
+
+/* ---- sub-grid lookup: GridUtils::getSubGrid, src/GridUtils.cpp:1761-1799.
+ * The reference tests L0 positions against each region's global edges; the
+ * region containing the site is the one whose coarse limits contain it. ---- */
+static oracle_grid *sub_grid_at(oracle_grid *g, int i, int j, int k) {
+    if (g->d.level > 0) return g->nsub ? g->sub[0] : NULL;
+    for (int s = 0; s < g->nsub; ++s) {
+        const int *L = g->sub[s]->d.coarse_lims;
+        if (i >= L[0] && i <= L[1] && j >= L[2] && j <= L[3] && (g->D == 2 || (k >= L[4] && k <= L[5])))
+            return g->sub[s];
+    }
+    return NULL;
+}
+
+static int stream_site(oracle_grid *g, int i, int j, int k, int id, int type, int subcycle);
+static void macro_site(oracle_grid *g, int i, int j, int k, int id, int type);
+
+/* ---- _LBM_coalesce_opt, :591-636 (getFineIndices, src/GridUtils.cpp:410-425) ---- */
+static int coalesce(oracle_grid *g, int i, int j, int k, int id, int v) {
+    oracle_grid *cg = sub_grid_at(g, i, j, k);
+    if (!cg) { set_err("coalesce: no sub-grid"); return -1; }
+    const int cM = cg->d.M, cK = cg->d.K, Q = g->Q;
+    const int ci = 2 * (i - cg->d.coarse_lims[0] + 1) - 2;
+    const int cj = 2 * (j - cg->d.coarse_lims[2] + 1) - 2;
+    const int ck = g->D == 3 ? 2 * (k - cg->d.coarse_lims[4] + 1) - 2 : 0;
+    double s = 0.0;
+    for (int ii = 0; ii < 2; ++ii)
+        for (int jj = 0; jj < 2; ++jj)
+            for (int kk = 0; kk < (g->D == 3 ? 2 : 1); ++kk)
+                s += cg->f[v + (ck + kk) * Q + (cj + jj) * Q * cK + (size_t)(ci + ii) * Q * cK * cM];
+    s /= (g->D == 3) ? 8.0 : 4.0;
+    g->fNew[v + (size_t)id * Q] = s;
+    return 0;
+}
+
+/* ---- _LBM_explode_opt, :646-663 (getCoarseIndices, src/GridUtils.cpp:440-466) ---- */
+static void explode(oracle_grid *g, int id, int v, int sx, int sy, int sz) {
+    oracle_grid *p = g->parent;
+    if (sx % 2 != 0) sx -= 1;
+    if (sy % 2 != 0) sy -= 1;
+    if (sz % 2 != 0) sz -= 1;
+    const int pi = sx / 2 + g->d.coarse_lims[0];
+    const int pj = sy / 2 + g->d.coarse_lims[2];
+    const int pk = g->D == 3 ? sz / 2 + g->d.coarse_lims[4] : 0;
+    const int Q = g->Q;
+    g->fNew[v + (size_t)id * Q] = p->f[v + pk * Q + pj * Q * p->d.K + (size_t)pi * Q * p->d.K * p->d.M];
+}
+
+/* ---- _LBM_applySpecReflect_opt, :527-581 ---- */
+static int spec_reflect(oracle_grid *g, int i, int j, int k, int id, int v, int *applied) {
+    int nv[3], nd, ne;
+    const int Q = g->Q;
+    const int *c = g->c[v];
+    *applied = 0;
+    if (!within_domain_wall(g, g->xpos[i], g->ypos[j], g->zpos[k], nv, &nd, &ne)) {
+        set_err("Slip wall not located inside a domain wall region");
+        return -1;
+    }
+    int plane = -1;
+    if (nv[0] == 1 && c[0] == 1) plane = 0;
+    else if (nv[0] == -1 && c[0] == -1) plane = 0;
+    else if (nv[1] == 1 && c[1] == 1) plane = 1;
+    else if (nv[1] == -1 && c[1] == -1) plane = 1;
+    else if (nv[2] == 1 && c[2] == 1) plane = 2;
+    else if (nv[2] == -1 && c[2] == -1) plane = 2;
+    if (plane >= 0) {
+        g->fNew[v + (size_t)id * Q] = g->f[g->refl[plane * Q + v] + (size_t)id * Q];
+        *applied = 1;
+    }
+    return 0;
+}
+
+/* ---- _LBM_stream_opt, :206-297 ---- */
+static int stream_site(oracle_grid *g, int i, int j, int k, int id, int type, int subcycle) {
+    const int N = g->d.N, M = g->d.M, K = g->d.K, Q = g->Q;
+    for (int v = 0; v < Q; ++v) {
+        const int sx = (i - g->c[v][0] + N) % N;
+        const int sy = (j - g->c[v][1] + M) % M;
+        const int sz = (k - g->c[v][2] + K) % K;
+        const int sid = sz + sy * K + sx * K * M;
+        const int st = g->typ[sid];
+        if (type == LUMA_SITE_BFL || st == LUMA_SITE_BFL) {
+            set_err("BFL bodies are outside the GPU path");
+            return -1;
+        }
+        if (type == LUMA_SITE_SLIP) {
+            int applied;
+            if (spec_reflect(g, i, j, k, id, v, &applied)) return -1;
+            if (applied) continue;
+        }
+        if (st == LUMA_SITE_SOLID) {
+            g->fNew[v + (size_t)id * Q] = g->f[g->opp[v] + (size_t)id * Q];
+        } else if (st == LUMA_SITE_EXTRAPOLATE_RIGHT) {
+            g->fNew[v + (size_t)id * Q] = g->f[v + (size_t)(sid - 2 * (K * M)) * Q];
+        } else if (st == LUMA_SITE_VELOCITY && !(g->d.flags & LUMA_FLAG_REGULARISED)) {
+            if (g->d.velocity_ramp > 0.0) {
+                const double rc = ramp_coeff(g, g->t * g->d.dt);
+                g->u[0 + (size_t)sid * g->D] = g->ux_in[j] * rc;
+                g->u[1 + (size_t)sid * g->D] = g->uy_in[j] * rc;
+                if (g->D == 3) g->u[2 + (size_t)sid * g->D] = g->uz_in[j] * rc;
+            }
+            g->fNew[v + (size_t)id * Q] = feq_at(g, sid, v);
+        } else if (g->parent && st == LUMA_SITE_TL_TO_COARSER && subcycle == 0) {
+            explode(g, id, v, sx, sy, sz);
+        } else if (g->nsub && st == LUMA_SITE_REFINED && type == LUMA_SITE_TL_TO_FINER) {
+            if (coalesce(g, i, j, k, id, v)) return -1;
+        } else {
+            g->fNew[v + (size_t)id * Q] = g->f[v + (size_t)sid * Q];
+        }
+    }
+    return 0;
+}
+
+/* ---- _LBM_macro_opt, :800-919 (time averages not restated) ---- */
+static void macro_site(oracle_grid *g, int i, int j, int k, int id, int type) {
+    const int Q = g->Q, D = g->D;
+    const int forcing = (g->d.flags & (LUMA_FLAG_IBM | LUMA_FLAG_GRAVITY)) != 0;
+    if (type == LUMA_SITE_FLUID || type == LUMA_SITE_BFL || type == LUMA_SITE_TL_TO_FINER ||
+        type == LUMA_SITE_SLIP) {
+        double r = 0.0, mx = 0.0, my = 0.0, mz = 0.0;
+        const double *fn = g->fNew + (size_t)id * Q;
+        for (int v = 0; v < Q; ++v) {
+            r += fn[v];
+            mx += g->c[v][0] * fn[v];
+            my += g->c[v][1] * fn[v];
+            if (D == 3) mz += g->c[v][2] * fn[v];
+        }
+        if (forcing) {
+            const double *F = g->force_xyz + (size_t)id * D;
+            mx += 0.5 * F[0];
+            my += 0.5 * F[1];
+            if (D == 3) {
+                if (g->d.flags & LUMA_FLAG_FIX_MACRO3D) mz += 0.5 * F[2];
+                else mx += 0.5 * F[2];
+            }
+        }
+        g->u[0 + (size_t)id * D] = mx / r;
+        g->u[1 + (size_t)id * D] = my / r;
+        if (D == 3) g->u[2 + (size_t)id * D] = mz / r;
+        g->rho[id] = r;
+    }
+    if (type == LUMA_SITE_TL_TO_FINER) {
+        oracle_grid *cg = sub_grid_at(g, i, j, k);
+        if (!cg) return;
+        const int cM = cg->d.M, cK = cg->d.K;
+        const int ci = 2 * (i - cg->d.coarse_lims[0] + 1) - 2;
+        const int cj = 2 * (j - cg->d.coarse_lims[2] + 1) - 2;
+        const int ck = D == 3 ? 2 * (k - cg->d.coarse_lims[4] + 1) - 2 : 0;
+        for (int ii = 0; ii < 2; ++ii)
+            for (int jj = 0; jj < 2; ++jj)
+                for (int kk = 0; kk < (D == 3 ? 2 : 1); ++kk) {
+                    const size_t cid = (size_t)(ck + kk) + (size_t)(cj + jj) * cK + (size_t)(ci + ii) * cK * cM;
+                    for (int dd = 0; dd < D; ++dd) cg->u[dd + cid * D] = g->u[dd + (size_t)id * D];
+                    cg->rho[cid] = g->rho[id];
+                }
+    }
+}
+
+/* ---- _LBM_updateAndExtrapolate (order 1), :1353-1412, and
+ *      GridUtils::extrapolate, inc/GridUtils.h:232-281 ---- */
+static int update_and_extrapolate(oracle_grid *g, int subcycle, const double *q, const int dir[3],
+                                  int i, int j, int k, int p, int max, double *out) {
+    const int N = g->d.N, M = g->d.M, K = g->d.K;
+    const int id = k + j * K + i * K * M;
+    const int i1 = i + dir[0], i2 = i1 + dir[0];
+    const int j1 = j + dir[1], j2 = j1 + dir[1];
+    const int k1 = k + dir[2], k2 = k1 + dir[2];
+    if (i1 < 0 || i1 >= N || j1 < 0 || j1 >= M || k1 < 0 || k1 >= K || i2 < 0 || i2 >= N ||
+        j2 < 0 || j2 >= M || k2 < 0 || k2 >= K) {
+        set_err("Extrapolation does not have enough available cells.");
+        return -1;
+    }
+    const int id1 = k1 + j1 * K + i1 * K * M;
+    const int id2 = k2 + j2 * K + i2 * K * M;
+    if (id1 > id) {
+        if (stream_site(g, i1, j1, k1, id1, g->typ[id1], subcycle)) return -1;
+        macro_site(g, i1, j1, k1, id1, g->typ[id1]);
+    }
+    if (id2 > id) {
+        if (stream_site(g, i2, j2, k2, id2, g->typ[id2], subcycle)) return -1;
+        macro_site(g, i2, j2, k2, id2, g->typ[id2]);
+    }
+    *out = 2.0 * q[p + (size_t)id1 * max] - q[p + (size_t)id2 * max];
+    return 0;
+}
+
+/* ---- _LBM_regularised_opt, :313-510 ---- */
+static int regularised(oracle_grid *g, int i, int j, int k, int id, int type, int subcycle) {
+    const int Q = g->Q, D = g->D;
+    const double cs = cs_();
+    double vel[3];
+    double dens = g->d.rho_in;
+    int nv[3], nd, ne;
+    double f_plus = 0.0, f_zero = 0.0;
+    double Sxx = 0, Syy = 0, Sxy = 0, Szz = 0, Sxz = 0, Syz = 0;
+    const double rc = ramp_coeff(g, (g->t + 1) * g->d.dt);
+    if (!within_domain_wall(g, g->xpos[i], g->ypos[j], g->zpos[k], nv, &nd, &ne)) {
+        set_err("Velocity site not outside domain walls is currently not supported.");
+        return -1;
+    }
+    vel[0] = g->ux_in[j] * rc;
+    vel[1] = g->uy_in[j] * rc;
+    vel[2] = g->uz_in[j] * rc;
+    dens += g->d.pressure_delta;
+    if (ne > 1) {
+        if (type == LUMA_SITE_PRESSURE) {
+            set_err("Pressure BC not supported at corner/edge site.");
+            return -1;
+        }
+        if (update_and_extrapolate(g, subcycle, g->rho, nv, i, j, k, 0, 1, &dens)) return -1;
+    } else {
+        for (int v = 0; v < Q; ++v) {
+            if (g->c[v][nd] == -nv[nd]) f_plus += g->fNew[v + (size_t)id * Q];
+            else if (g->c[v][nd] == 0) f_zero += g->fNew[v + (size_t)id * Q];
+        }
+        if (type == LUMA_SITE_PRESSURE) {
+            for (int dd = 0; dd < D; dd++)
+                if (dd != nd)
+                    if (update_and_extrapolate(g, subcycle, g->u, nv, i, j, k, dd, D, &vel[dd])) return -1;
+            vel[nd] = 1.0 - ((1.0 / dens) * (2.0 * f_plus + f_zero));
+            if (nv[nd] == -1) vel[nd] *= -1.0;
+        } else {
+            double nvel = vel[nd];
+            if (nv[nd] == -1) nvel *= -1.0;
+            dens = (1.0 / (1.0 - nvel)) * (2.0 * f_plus + f_zero);
+        }
+    }
+    g->rho[id] = dens;
+    g->u[0 + (size_t)id * D] = vel[0];
+    g->u[1 + (size_t)id * D] = vel[1];
+    if (D == 3) g->u[2 + (size_t)id * D] = vel[2];
+
+    double *fn = g->fNew + (size_t)id * Q;
+    for (int v = 0; v < Q; ++v) {
+        const int *c = g->c[v];
+        if (ne == 1 && c[nd] == nv[nd]) {
+            fn[v] = feq_at(g, id, v) + (fn[g->opp[v]] - feq_at(g, id, g->opp[v]));
+        } else if (ne > 1 && (c[0] == nv[0] || c[1] == nv[1] || (D == 3 && c[2] == nv[2]))) {
+            int dp = 0;
+            double mag = 0.0;
+            for (int dd = 0; dd < D; dd++) {
+                dp += c[dd] * nv[dd];
+                mag += ((double)c[dd] * (double)c[dd]);
+            }
+            mag = sqrt(mag);
+            if (dp == 0 && mag > 1.0) fn[v] = feq_at(g, id, v);
+            else fn[v] = feq_at(g, id, v) + (fn[g->opp[v]] - feq_at(g, id, g->opp[v]));
+        }
+        const double fneq = fn[v] - feq_at(g, id, v);
+        Sxx += c[0] * c[0] * fneq;
+        Syy += c[1] * c[1] * fneq;
+        Sxy += c[0] * c[1] * fneq;
+        if (D == 3) {
+            Szz += c[2] * c[2] * fneq;
+            Sxz += c[0] * c[2] * fneq;
+            Syz += c[1] * c[2] * fneq;
+        }
+    }
+    for (int v = 0; v < Q; v++) {
+        const int *c = g->c[v];
+        fn[v] = feq_at(g, id, v) +
+                (g->w[v] / (2.0 * SQ(cs) * SQ(cs))) *
+                    (((c[0] * c[0] - SQ(cs)) * Sxx) + ((c[1] * c[1] - SQ(cs)) * Syy) +
+                     ((c[2] * c[2] - SQ(cs)) * Szz) + (2.0 * c[0] * c[1] * Sxy) +
+                     (2.0 * c[0] * c[2] * Sxz) + (2.0 * c[1] * c[2] * Syz));
+    }
+    return 0;
+}
+
+/* ---- _LBM_forceGrid_opt, :928-990 ---- */
+static void force_grid(oracle_grid *g, int id) {
+    const int Q = g->Q, D = g->D;
+    const double cs = cs_();
+    double *fi = g->force_i + (size_t)id * Q;
+    const double *u = g->u + (size_t)id * D;
+    const double *F = g->force_xyz + (size_t)id * D;
+    memset(fi, 0, sizeof(double) * Q);
+    for (int v = 0; v < Q; v++) {
+        double beta = 0.0;
+        const double lambda = (1 - 0.5 * g->d.omega) * (g->w[v] / (cs * cs));
+        for (int dd = 0; dd < D; dd++) beta += (g->c[v][dd] * u[dd]);
+        beta = beta * (1 / (cs * cs));
+        for (int dd = 0; dd < D; dd++) fi[v] += F[dd] * (g->c[v][dd] * (1 + beta) - u[dd]);
+        fi[v] *= lambda;
+    }
+}
+
+/* ---- _LBM_smag, :717-756 ---- */
+static double smag(oracle_grid *g, int id, double omega) {
+    const int Q = g->Q, D = g->D;
+    const double cs = cs_();
+    double fneq[27], S[3][3];
+    for (int v = 0; v < Q; ++v) fneq[v] = g->fNew[v + (size_t)id * Q] - feq_at(g, id, v);
+    memset(S, 0, sizeof S);
+    for (int a = 0; a < D; ++a)
+        for (int b = a; b < D; ++b) {
+            S[a][b] = 0.0;
+            for (int v = 0; v < Q; ++v) S[a][b] += g->c[v][a] * g->c[v][b] * fneq[v];
+        }
+    for (int a = 1; a < D; ++a)
+        for (int b = 0; b < a; ++b) S[a][b] = S[b][a];
+    /* Matrix2D % (inc/Matrix.h:65-75): per-row sums of element-wise
+     * products over the 3x3 store, then the sum of the row sums. */
+    double ip = 0.0;
+    for (int a = 0; a < 3; ++a) {
+        double row = 0.0;
+        for (int b = 0; b < 3; ++b) row += S[a][b] * S[a][b];
+        ip += row;
+    }
+    const double Qs = sqrt(2.0 * ip);
+    const double tau = 1.0 / omega;
+    const double tau_t =
+        0.5 * (sqrt(SQ(tau) + 2.0 * L_SQRT2 * SQ(g->d.csmag) * g->d.rho_in * SQ(cs) * SQ(cs) * Qs) - tau);
+    return (1.0 / (tau + tau_t));
+}
+
+/* ---- _LBM_collide_opt, :765-790 ---- */
+static void collide_bgk(oracle_grid *g, int id) {
+    const int Q = g->Q;
+    const int forcing = (g->d.flags & (LUMA_FLAG_IBM | LUMA_FLAG_GRAVITY)) != 0;
+    const double om = g->d.collision == LUMA_COLL_BGK_SMAG ? smag(g, id, g->d.omega) : g->d.omega;
+    double *fn = g->fNew + (size_t)id * Q;
+    for (int v = 0; v < Q; ++v) {
+        if (forcing) fn[v] += om * (feq_at(g, id, v) - fn[v]) + g->force_i[v + (size_t)id * Q];
+        else fn[v] += om * (feq_at(g, id, v) - fn[v]);
+    }
+}
+
+/* ---- _LBM_kbcCollide_opt, :1122-1305 ---- */
+static void collide_kbc(oracle_grid *g, int id) {
+    const int Q = g->Q, D = g->D;
+    const int forcing = (g->d.flags & (LUMA_FLAG_IBM | LUMA_FLAG_GRAVITY)) != 0;
+    const double *src = (g->d.flags & LUMA_FLAG_FIX_KBC) ? g->fNew : g->f;
+    double ds[27], dh[27], fneq[27], Mneq[13];
+    int C[13 * 27];
+    const int nm = D == 3 ? 13 : 3;
+    for (int m = 0; m < nm; ++m) Mneq[m] = 0.0;
+    for (int m = 0; m < nm * Q; ++m) C[m] = 1;
+    double *fe = g->feq + (size_t)id * Q;
+    for (int v = 0; v < Q; v++) {
+        fe[v] = feq_at(g, id, v);
+        fneq[v] = src[v + (size_t)id * Q] - fe[v];
+        int idx = 0;
+        for (int s = 0; s < D; ++s)
+            for (int a = s; a < D; ++a) {
+                C[idx + v * nm] = g->c[v][s] * g->c[v][a];
+                Mneq[idx] += fneq[v] * C[idx + v * nm];
+                idx++;
+                if (D == 3)
+                    for (int b = a; b < D; ++b)
+                        if (s != a || a != b || s != b) {
+                            C[idx + v * nm] = g->c[v][s] * g->c[v][a] * g->c[v][b];
+                            Mneq[idx] += fneq[v] * C[idx + v * nm];
+                            idx++;
+                        }
+            }
+    }
+    for (int v = 0; v < Q; v++) {
+        const int *c = g->c[v];
+        if (D == 3) {
+            if (c[0] == 0) {
+                if (c[1] == 0) {
+                    if (c[2] == 0) ds[v] = (-(Mneq[0] + Mneq[8] + Mneq[12]));
+                    else
+                        ds[v] = ((-(Mneq[0] - Mneq[12]) - (Mneq[8] - Mneq[12])) / 6.0 +
+                                 (Mneq[0] + Mneq[8] + Mneq[12]) / 6.0 - c[2] * 0.5 * (Mneq[2] + Mneq[9]));
+                } else {
+                    if (c[2] == 0)
+                        ds[v] = ((-(Mneq[0] - Mneq[12]) + 2.0 * (Mneq[8] - Mneq[12])) / 6.0 +
+                                 (Mneq[0] + Mneq[8] + Mneq[12]) / 6.0 - c[1] * 0.5 * (Mneq[1] + Mneq[11]));
+                    else
+                        ds[v] = (C[10 + v * nm] * 0.25 * Mneq[10] +
+                                 (c[2] * 0.25 * Mneq[9] + c[1] * 0.25 * Mneq[11]));
+                }
+            } else {
+                if (c[1] == 0) {
+                    if (c[2] == 0)
+                        ds[v] = ((2.0 * (Mneq[0] - Mneq[12]) - (Mneq[8] - Mneq[12])) / 6.0 +
+                                 (Mneq[0] + Mneq[8] + Mneq[12]) / 6.0 - c[0] * 0.5 * (Mneq[4] + Mneq[7]));
+                    else
+                        ds[v] = (C[6 + v * nm] * 0.25 * Mneq[6] + (c[2] * 0.25 * Mneq[2] + c[0] * 0.25 * Mneq[7]));
+                } else {
+                    if (c[2] == 0)
+                        ds[v] = (C[3 + v * nm] * 0.25 * Mneq[3] + (c[1] * 0.25 * Mneq[1] + c[0] * 0.25 * Mneq[4]));
+                    else
+                        ds[v] = (C[5 + v * nm] * Mneq[5] / 8.0);
+                }
+            }
+        } else {
+            if (c[0] == 0) {
+                if (c[1] == 0) ds[v] = 0.0;
+                else ds[v] = -0.25 * (Mneq[0] - Mneq[2]);
+            } else {
+                if (c[1] == 0) ds[v] = 0.25 * (Mneq[0] - Mneq[2]);
+                else ds[v] = 0.25 * C[1 + v * nm] * Mneq[1];
+            }
+        }
+        dh[v] = fneq[v] - ds[v];
+    }
+    double top = 0.0, bot = 0.0;
+    for (int v = 0; v < Q; v++) {
+        top += ds[v] * dh[v] / fe[v];
+        bot += dh[v] * dh[v] / fe[v];
+    }
+    const double beta_m1 = 2.0 / g->d.omega;
+    double gamma;
+    if (bot == 0.0) gamma = 2.0;
+    else gamma = beta_m1 - (2.0 - beta_m1) * (top / bot);
+    double *fn = g->fNew + (size_t)id * Q;
+    for (int v = 0; v < Q; v++) {
+        const double base = src[v + (size_t)id * Q] - (1.0 / beta_m1) * (2.0 * ds[v] + gamma * dh[v]);
+        fn[v] = forcing ? base + g->force_i[v + (size_t)id * Q] : base;
+    }
+}
+
+static void collide_site(oracle_grid *g, int id) {
+    if (g->d.collision == LUMA_COLL_KBC) collide_kbc(g, id);
+    else collide_bgk(g, id);
+}
+
+/* ---- _LBM_resetForces, :1327-1337 ---- */
+static void reset_forces(oracle_grid *g) {
+    if (g->d.flags & LUMA_FLAG_GRAVITY) {
+        for (int id = 0; id < g->ncell; ++id)
+            g->force_xyz[g->d.gravity_dir + (size_t)id * g->D] = g->rho[id] * g->d.gravity * g->d.refinement_ratio;
+    } else {
+        memset(g->force_xyz, 0, sizeof(double) * (size_t)g->ncell * g->D);
+    }
+}
+
+/* Sites whose update touches only their own fNew/u/rho and read f: the
+ * loop can run in parallel (as the reference's optional OpenMP loop does,
+ * :69-71) when no site has a non-local side effect. */
+static int loop_is_local(const oracle_grid *g) {
+    if (g->d.velocity_ramp > 0.0 && !(g->d.flags & LUMA_FLAG_REGULARISED)) return 0;
+    if (g->d.flags & LUMA_FLAG_REGULARISED) return 0;
+    if (g->nsub) return 0;
+    return 1;
+}
+
+/* ---- GridObj::LBM_multi_opt, :36-193 ---- */
+static int multi_opt(oracle_grid *g, int subcycle) {
+    for (int s = 0; s < g->nsub; ++s)
+        for (int it = 0; it < 2; ++it)
+            if (multi_opt(g->sub[s], it)) return -1;
+    const int ibm = (g->d.flags & LUMA_FLAG_IBM) != 0;
+    const int gravity = (g->d.flags & LUMA_FLAG_GRAVITY) != 0;
+    const int N = g->d.N, M = g->d.M, K = g->d.K;
+    const int reg = (g->d.flags & LUMA_FLAG_REGULARISED) != 0;
+    if (ibm && g->has_ibm_bodies) reset_forces(g);
+    int err = 0;
+    const int par = loop_is_local(g);
+#pragma omp parallel for schedule(static) if (par) reduction(| : err)
+    for (int i = 0; i < N; ++i) {
+        for (int j = 0; j < M; ++j) {
+            for (int k = 0; k < K; ++k) {
+                const int id = k + j * K + i * K * M;
+                const int type = g->typ[id];
+                if (type == LUMA_SITE_REFINED || type == LUMA_SITE_SOLID || (!reg && type == LUMA_SITE_VELOCITY))
+                    continue;
+                if (stream_site(g, i, j, k, id, type, subcycle)) { err |= 1; continue; }
+                if (reg && (type == LUMA_SITE_VELOCITY || type == LUMA_SITE_PRESSURE))
+                    if (regularised(g, i, j, k, id, type, subcycle)) { err |= 1; continue; }
+                macro_site(g, i, j, k, id, type);
+                if (!ibm) {
+                    if (gravity && type != LUMA_SITE_SOLID) force_grid(g, id);
+                    if (type != LUMA_SITE_TL_TO_COARSER) collide_site(g, id);
+                }
+            }
+        }
+    }
+    if (err) return -1;
+    if (ibm) {
+        if (g->has_flexible_bodies) memcpy(g->u_n, g->u, sizeof(double) * (size_t)g->ncell * g->D);
+        if (g->has_ibm_bodies && g->ibm_hook) g->ibm_hook(g, g->ibm_ctx);
+#pragma omp parallel for schedule(static)
+        for (int id = 0; id < g->ncell; ++id) {
+            const int type = g->typ[id];
+            if (type != LUMA_SITE_SOLID) force_grid(g, id);
+            if (type != LUMA_SITE_TL_TO_COARSER) collide_site(g, id);
+        }
+    }
+    double *tmp = g->f;
+    g->f = g->fNew;
+    g->fNew = tmp;
+    ++g->t;
+    return 0;
+}
+
+/* ------------------------------ public API ------------------------------ */
+
+static double *dup_d(const double *p, size_t n) {
+    double *q = (double *)malloc(sizeof(double) * (n ? n : 1));
+    if (p) memcpy(q, p, sizeof(double) * n);
+    else memset(q, 0, sizeof(double) * (n ? n : 1));
+    return q;
+}
+
+oracle_grid *oracle_grid_create(const luma_grid_desc *d, oracle_grid *parent) {
+    if (!d || d->abi_version != LUMA_GPU_ABI_VERSION) { set_err("bad descriptor"); return NULL; }
+    oracle_grid *g = (oracle_grid *)calloc(1, sizeof(oracle_grid));
+    g->d = *d;
+    g->Q = d->Q;
+    g->D = d->dims;
+    if (d->Q == 9 && d->dims == 2) { g->c = C9; g->w = W9; g->opp = OPP9; g->refl = &REF9[0][0]; }
+    else if (d->Q == 19 && d->dims == 3) { g->c = C19; g->w = W19; g->opp = OPP19; g->refl = &REF19[0][0]; }
+    else if (d->Q == 27 && d->dims == 3) { g->c = C27; g->w = W27; g->opp = OPP27; g->refl = &REF27[0][0]; }
+    else { set_err("unsupported lattice"); free(g); return NULL; }
+    g->ncell = d->N * d->M * d->K;
+    const size_t n = (size_t)g->ncell;
+    g->typ = (int *)malloc(sizeof(int) * n);
+    for (size_t i = 0; i < n; ++i) g->typ[i] = d->lattyp ? d->lattyp[i] : LUMA_SITE_FLUID;
+    g->xpos = dup_d(d->xpos, d->N);
+    g->ypos = dup_d(d->ypos, d->M);
+    g->zpos = dup_d(d->zpos, d->K);
+    g->ux_in = dup_d(d->ux_in, d->M);
+    g->uy_in = dup_d(d->uy_in, d->M);
+    g->uz_in = dup_d(d->uz_in, d->M);
+    g->f = dup_d(NULL, n * g->Q);
+    g->fNew = dup_d(NULL, n * g->Q);
+    g->feq = dup_d(NULL, n * g->Q);
+    g->force_i = dup_d(NULL, n * g->Q);
+    g->u = dup_d(NULL, n * g->D);
+    g->u_n = dup_d(NULL, n * g->D);
+    g->force_xyz = dup_d(NULL, n * g->D);
+    g->rho = dup_d(NULL, n);
+    g->d.lattyp = NULL;
+    g->d.xpos = g->d.ypos = g->d.zpos = NULL;
+    g->d.ux_in = g->d.uy_in = g->d.uz_in = NULL;
+    g->parent = parent;
+    if (parent) {
+        if (parent->nsub >= 8) { set_err("too many sub-grids"); return NULL; }
+        parent->sub[parent->nsub++] = g;
+    }
+    return g;
+}
+
+void oracle_grid_destroy(oracle_grid *g) {
+    if (!g) return;
+    for (int s = 0; s < g->nsub; ++s) oracle_grid_destroy(g->sub[s]);
+    free(g->typ); free(g->xpos); free(g->ypos); free(g->zpos);
+    free(g->ux_in); free(g->uy_in); free(g->uz_in);
+    free(g->f); free(g->fNew); free(g->feq); free(g->force_i);
+    free(g->u); free(g->u_n); free(g->force_xyz); free(g->rho);
+    free(g);
+}
+
+/* Upload sets f, fNew and feq to the given populations, as LBM_initGrid
+ * does (src/GridObj_init_grids.cpp:331-332). */
+int oracle_upload_state(oracle_grid *g, const double *f, const double *u, const double *rho,
+                        const double *force_xyz, int t) {
+    const size_t n = (size_t)g->ncell;
+    if (f) {
+        memcpy(g->f, f, sizeof(double) * n * g->Q);
+        memcpy(g->fNew, f, sizeof(double) * n * g->Q);
+        memcpy(g->feq, f, sizeof(double) * n * g->Q);
+    }
+    if (u) { memcpy(g->u, u, sizeof(double) * n * g->D); memcpy(g->u_n, u, sizeof(double) * n * g->D); }
+    if (rho) memcpy(g->rho, rho, sizeof(double) * n);
+    if (force_xyz) memcpy(g->force_xyz, force_xyz, sizeof(double) * n * g->D);
+    g->t = t;
+    return 0;
+}
+
+int oracle_download_state(const oracle_grid *g, double *f, double *u, double *rho, double *force_xyz) {
+    const size_t n = (size_t)g->ncell;
+    if (f) memcpy(f, g->f, sizeof(double) * n * g->Q);
+    if (u) memcpy(u, g->u, sizeof(double) * n * g->D);
+    if (rho) memcpy(rho, g->rho, sizeof(double) * n);
+    if (force_xyz) memcpy(force_xyz, g->force_xyz, sizeof(double) * n * g->D);
+    return 0;
+}
+
+/* Equilibrium populations for the given rho/u fields (reference layout),
+ * exactly as LBM_initGrid computes f (src/GridObj_init_grids.cpp:316-333). */
+int oracle_equilibrium(oracle_grid *g, const double *u, const double *rho, double *f_out) {
+    const size_t n = (size_t)g->ncell;
+    memcpy(g->u, u, sizeof(double) * n * g->D);
+    memcpy(g->rho, rho, sizeof(double) * n);
+    for (size_t id = 0; id < n; ++id)
+        for (int v = 0; v < g->Q; ++v) f_out[v + id * g->Q] = feq_at(g, (int)id, v);
+    return 0;
+}
+
+int oracle_step(oracle_grid *root, int nsteps) {
+    for (int s = 0; s < nsteps; ++s)
+        if (multi_opt(root, 0)) return -1;
+    return 0;
+}
+
+int oracle_get_time(const oracle_grid *g) { return g->t; }
+
+int oracle_set_threads(int n) {
+#ifdef _OPENMP
+    if (n > 0) omp_set_num_threads(n);
+    return omp_get_max_threads();
+#else
+    (void)n;
+    return 1;
+#endif
+}
+
+/* Hooks for the IBM oracle (ibm_oracle.c). */
+void oracle_set_ibm(oracle_grid *g, int has_ibm, int has_flexible, void (*hook)(oracle_grid *, void *), void *ctx) {
+    g->has_ibm_bodies = has_ibm;
+    g->has_flexible_bodies = has_flexible;
+    g->ibm_hook = hook;
+    g->ibm_ctx = ctx;
+}

@@ -1,0 +1,122 @@
+"""ORACLE — test infrastructure only: loader for the CPU restatement.
+
+Builds ``oracle/_build/liboracle.so`` from ``lbm_oracle.c`` (and the IBM
+restatement) with gcc and exposes it through ctypes with the same shape as
+the GPU C ABI (create / upload / step / download).  Only tests, the smoke
+check and the benchmark's CPU-baseline leg import this module.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(HERE)
+BUILD = os.path.join(HERE, "_build")
+LIB = os.path.join(BUILD, "liboracle.so")
+SOURCES = ["lbm_oracle.c", "ibm_oracle.c"]
+
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+from luma_gb300 import _abi as A  # noqa: E402
+
+
+def build(force: bool = False) -> str:
+    srcs = [os.path.join(HERE, s) for s in SOURCES if os.path.exists(os.path.join(HERE, s))]
+    deps = srcs + [os.path.join(ROOT, "include", "luma_gpu.h")]
+    if not force and os.path.exists(LIB) and os.path.getmtime(LIB) >= max(map(os.path.getmtime, deps)):
+        return LIB
+    os.makedirs(BUILD, exist_ok=True)
+    tmp = LIB + f".tmp{os.getpid()}"
+    cmd = ["gcc", "-O2", "-ffp-contract=off", "-fPIC", "-shared", "-fopenmp", "-std=c11",
+           "-o", tmp, *srcs, "-lm"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("oracle build failed:\n" + r.stderr[-4000:])
+    os.replace(tmp, LIB)
+    return LIB
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        L = C.CDLL(build())
+        L.oracle_grid_create.restype = C.c_void_p
+        L.oracle_grid_create.argtypes = [C.POINTER(A.GridDesc), C.c_void_p]
+        L.oracle_grid_destroy.argtypes = [C.c_void_p]
+        L.oracle_upload_state.argtypes = [C.c_void_p] + [C.POINTER(C.c_double)] * 4 + [C.c_int]
+        L.oracle_download_state.argtypes = [C.c_void_p] + [C.POINTER(C.c_double)] * 4
+        L.oracle_equilibrium.argtypes = [C.c_void_p] + [C.POINTER(C.c_double)] * 3
+        L.oracle_step.argtypes = [C.c_void_p, C.c_int]
+        L.oracle_get_time.argtypes = [C.c_void_p]
+        L.oracle_set_threads.argtypes = [C.c_int]
+        L.oracle_last_error.restype = C.c_char_p
+        _lib = L
+    return _lib
+
+
+class OracleGrid:
+    """One grid of the CPU restatement (reference AoS layout on the host)."""
+
+    def __init__(self, desc: "A.GridDesc", parent: "OracleGrid | None" = None):
+        self.desc = desc
+        self.L = lib()
+        self.h = self.L.oracle_grid_create(C.byref(desc), parent.h if parent else None)
+        if not self.h:
+            raise RuntimeError(self.L.oracle_last_error().decode())
+        self.n = desc.N * desc.M * desc.K
+        self.children: list[OracleGrid] = []
+        self.parent = parent
+        if parent is not None:
+            parent.children.append(self)
+
+    def close(self):
+        if self.h and self.parent is None:
+            self.L.oracle_grid_destroy(self.h)
+        self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def upload(self, f=None, u=None, rho=None, force=None, t: int = 0):
+        arrs = [None if a is None else np.ascontiguousarray(a, dtype=np.float64) for a in (f, u, rho, force)]
+        self.L.oracle_upload_state(self.h, *[A.dptr(a) for a in arrs], t)
+
+    def download(self):
+        d = self.desc
+        f = np.empty(self.n * d.Q)
+        u = np.empty(self.n * d.dims)
+        rho = np.empty(self.n)
+        force = np.empty(self.n * d.dims)
+        self.L.oracle_download_state(self.h, A.dptr(f), A.dptr(u), A.dptr(rho), A.dptr(force))
+        return {"f": f, "u": u, "rho": rho, "force": force}
+
+    def equilibrium(self, u, rho):
+        d = self.desc
+        u = np.ascontiguousarray(u, dtype=np.float64)
+        rho = np.ascontiguousarray(rho, dtype=np.float64)
+        f = np.empty(self.n * d.Q)
+        self.L.oracle_equilibrium(self.h, A.dptr(u), A.dptr(rho), A.dptr(f))
+        return f
+
+    def step(self, nsteps: int = 1):
+        if self.L.oracle_step(self.h, nsteps) != 0:
+            raise RuntimeError(self.L.oracle_last_error().decode())
+
+    @property
+    def t(self) -> int:
+        return self.L.oracle_get_time(self.h)
+
+
+def set_threads(n: int) -> int:
+    return lib().oracle_set_threads(n)

@@ -1,0 +1,190 @@
+/* Oracle test infrastructure: a driver for the reference's own serial build.
+ *
+ * It performs the initialisation sequence of the reference's main()
+ * (src/main_lbm.cpp:170-291: GridManager, GridObj(0), LBM_addSubGrid per
+ * region, setGridHierarchy, ObjectManager, geometry read, ibm_initialise),
+ * optionally replaces the L0 velocity/density field with a field read from a
+ * raw binary file (and re-initialises f = feq(rho, u) exactly as
+ * LBM_initGrid does, src/GridObj_init_grids.cpp:316-333), then calls
+ * GridObj::LBM_multi_opt() the requested number of times
+ * (src/main_lbm.cpp:441) and dumps every grid of the hierarchy as raw
+ * little-endian arrays in the reference's AoS layout.
+ *
+ * Usage:
+ *   luma_ref --out DIR --steps N [--dump-every K] [--init-u FILE] [--init-rho FILE]
+ *            [--workdir DIR]
+ *
+ * Output, per dump step s and grid (level l, region r):
+ *   DIR/s<s>/L<l>R<r>_meta.txt   key value lines (sizes, omega, dt, dh, t, limits)
+ *   DIR/s<s>/L<l>R<r>_<name>.bin f, u, rho, typ (int32), force (if allocated)
+ * and, if IBM bodies exist, DIR/s<s>/markers.txt.
+ */
+#include <sys/stat.h>
+#include <unistd.h>
+
+#include <chrono>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../inc/stdafx.h"
+#include "../inc/GridObj.h"
+#include "../inc/GridManager.h"
+#include "../inc/ObjectManager.h"
+#include "../inc/IBBody.h"
+
+static void write_raw(const std::string &path, const void *data, size_t bytes) {
+    FILE *fp = std::fopen(path.c_str(), "wb");
+    if (!fp) { std::perror(path.c_str()); std::exit(2); }
+    if (bytes && std::fwrite(data, 1, bytes, fp) != bytes) { std::perror(path.c_str()); std::exit(2); }
+    std::fclose(fp);
+}
+
+static std::vector<double> read_raw(const std::string &path, size_t count) {
+    std::vector<double> v(count);
+    FILE *fp = std::fopen(path.c_str(), "rb");
+    if (!fp) { std::perror(path.c_str()); std::exit(2); }
+    if (std::fread(v.data(), sizeof(double), count, fp) != count) {
+        std::fprintf(stderr, "short read %s\n", path.c_str());
+        std::exit(2);
+    }
+    std::fclose(fp);
+    return v;
+}
+
+static void dump_grid(GridObj *g, const std::string &dir) {
+    char pre[64];
+    std::snprintf(pre, sizeof pre, "/L%dR%d_", g->level, g->region_number);
+    std::string p = dir + pre;
+    FILE *m = std::fopen((p + "meta.txt").c_str(), "w");
+    std::fprintf(m, "level %d\nregion %d\nN %d\nM %d\nK %d\nQ %d\ndims %d\nt %d\n", g->level,
+                 g->region_number, g->N_lim, g->M_lim, g->K_lim, L_NUM_VELS, L_DIMS, g->t);
+    std::fprintf(m, "omega %.17g\ndt %.17g\ndh %.17g\nnu %.17g\n", g->omega, g->dt, g->dh, g->nu);
+    if (g->level > 0)
+        std::fprintf(m, "coarse_lims %d %d %d %d %d %d\n", g->CoarseLimsX[0], g->CoarseLimsX[1],
+                     g->CoarseLimsY[0], g->CoarseLimsY[1], g->CoarseLimsZ[0], g->CoarseLimsZ[1]);
+    std::fclose(m);
+    write_raw(p + "f.bin", g->f.data(), g->f.size() * sizeof(double));
+    write_raw(p + "u.bin", g->u.data(), g->u.size() * sizeof(double));
+    write_raw(p + "rho.bin", g->rho.data(), g->rho.size() * sizeof(double));
+    std::vector<int> typ(g->LatTyp.size());
+    for (size_t i = 0; i < typ.size(); ++i) typ[i] = static_cast<int>(g->LatTyp[i]);
+    write_raw(p + "typ.bin", typ.data(), typ.size() * sizeof(int));
+    write_raw(p + "uxin.bin", g->ux_in.data(), g->ux_in.size() * sizeof(double));
+    write_raw(p + "xpos.bin", g->XPos.data(), g->XPos.size() * sizeof(double));
+    write_raw(p + "ypos.bin", g->YPos.data(), g->YPos.size() * sizeof(double));
+    write_raw(p + "zpos.bin", g->ZPos.data(), g->ZPos.size() * sizeof(double));
+    if (!g->force_xyz.empty())
+        write_raw(p + "force.bin", g->force_xyz.data(), g->force_xyz.size() * sizeof(double));
+    for (GridObj *sg : g->subGrid) dump_grid(sg, dir);
+}
+
+static void dump_markers(const std::string &dir) {
+#ifdef L_IBM_ON
+    ObjectManager *om = ObjectManager::getInstance();
+    FILE *fp = std::fopen((dir + "/markers.txt").c_str(), "w");
+    for (size_t b = 0; b < om->iBody.size(); ++b) {
+        IBBody &body = om->iBody[b];
+        for (size_t m = 0; m < body.markers.size(); ++m) {
+            IBMarker &mk = body.markers[m];
+            std::fprintf(fp, "%zu %zu %.17g %.17g %.17g %.17g %.17g %.17g %.17g %.17g %.17g %.17g %.17g %.17g %zu\n",
+                         b, m, mk.position[0], mk.position[1], mk.position[2], mk.force_xyz[0],
+                         mk.force_xyz[1], mk.force_xyz[2], mk.epsilon, mk.ds, mk.markerVel[0],
+                         mk.markerVel[1], mk.markerVel[2], mk.dilation, mk.supp_i.size());
+        }
+    }
+    std::fclose(fp);
+#else
+    (void)dir;
+#endif
+}
+
+static void dump_all(GridObj *root, const std::string &out, int step) {
+    std::string dir = out + "/s" + std::to_string(step);
+    mkdir(dir.c_str(), 0755);
+    dump_grid(root, dir);
+    dump_markers(dir);
+}
+
+static void reinit_equilibrium(GridObj *g) {
+    const int n = g->N_lim * g->M_lim * g->K_lim;
+    for (int id = 0; id < n; ++id)
+        for (int v = 0; v < L_NUM_VELS; ++v) g->f[v + id * L_NUM_VELS] = g->_LBM_equilibrium_opt(id, v);
+    g->feq = g->f;
+    g->fNew = g->f;
+}
+
+int main(int argc, char **argv) {
+    std::string out = ".", init_u, init_rho, workdir;
+    int steps = 0, dump_every = 0;
+    for (int a = 1; a < argc; ++a) {
+        std::string k = argv[a];
+        auto next = [&]() -> std::string {
+            if (a + 1 >= argc) { std::fprintf(stderr, "missing value for %s\n", k.c_str()); std::exit(2); }
+            return argv[++a];
+        };
+        if (k == "--out") out = next();
+        else if (k == "--steps") steps = std::atoi(next().c_str());
+        else if (k == "--dump-every") dump_every = std::atoi(next().c_str());
+        else if (k == "--init-u") init_u = next();
+        else if (k == "--init-rho") init_rho = next();
+        else if (k == "--workdir") workdir = next();
+        else { std::fprintf(stderr, "unknown argument %s\n", k.c_str()); return 2; }
+    }
+    mkdir(out.c_str(), 0755);
+    char outabs[4096];
+    if (!realpath(out.c_str(), outabs)) { std::perror("realpath"); return 2; }
+    out = outabs;
+    if (!workdir.empty() && chdir(workdir.c_str()) != 0) { std::perror("chdir"); return 2; }
+
+    GridUtils::path_str = out;
+    std::ofstream logfile((out + "/log.txt").c_str(), std::ios::out);
+    GridUtils::logfile = &logfile;
+
+    GridManager *gm = GridManager::getInstance();
+    GridObj *const grids = new GridObj(0);
+    if (L_NUM_LEVELS != 0)
+        for (int reg = 0; reg < L_NUM_REGIONS; ++reg) grids->LBM_addSubGrid(reg);
+    gm->setGridHierarchy(grids);
+
+    const size_t ncell = (size_t)grids->N_lim * grids->M_lim * grids->K_lim;
+    if (!init_u.empty()) {
+        std::vector<double> u = read_raw(init_u, ncell * L_DIMS);
+        for (size_t i = 0; i < u.size(); ++i) grids->u[i] = u[i];
+    }
+    if (!init_rho.empty()) {
+        std::vector<double> r = read_raw(init_rho, ncell);
+        for (size_t i = 0; i < r.size(); ++i) grids->rho[i] = r[i];
+    }
+    if (!init_u.empty() || !init_rho.empty()) {
+        reinit_equilibrium(grids);
+#ifdef L_IBM_ON
+        grids->u_n = grids->u;
+#endif
+    }
+
+    ObjectManager *om = ObjectManager::getInstance(grids);
+#ifdef L_GEOMETRY_FILE
+    om->io_readInGeomConfig();
+#endif
+#ifdef L_IBM_ON
+    om->ibm_initialise();
+#endif
+    (void)om;
+
+    dump_all(grids, out, 0);
+    auto t0 = std::chrono::steady_clock::now();
+    for (int s = 1; s <= steps; ++s) {
+        grids->LBM_multi_opt();
+        if ((dump_every > 0 && s % dump_every == 0) || s == steps) dump_all(grids, out, s);
+    }
+    auto t1 = std::chrono::steady_clock::now();
+    double sec = std::chrono::duration<double>(t1 - t0).count();
+    FILE *tf = std::fopen((out + "/timing.txt").c_str(), "w");
+    std::fprintf(tf, "steps %d\nseconds %.6f\ncells %zu\n", steps, sec, ncell);
+    std::fclose(tf);
+    logfile.close();
+    return 0;
+}

@@ -1,0 +1,126 @@
+"""Generate the golden fixtures in this directory from the reference itself.
+
+Runs the reference's own serial build (``oracle/build_ref.py`` compiles it
+from the reference checkout into ``oracle/_ref/<case>/luma_ref``) on each
+oracle case, with seeded injected initial fields where the case needs them,
+and stores the inputs the reference computed plus its outputs at chosen
+steps.  Large population arrays are stored as SHA-256 digests of their raw
+FP64 bytes (bit-exact checks need no copy of the data).
+
+Also extracts the one known-answer vector the reference's own test suite
+holds for the current algorithm: the t=0 D2Q9 equilibrium row of
+``cases/testsuite/base/case000/io_lite.Lev0.Reg0.Rnk0.0.dat``.
+
+Usage (needs the reference checkout; not run on the GPU machine):
+    python tests/golden/make_golden.py [--ref /root/reference/LUMA] [case ...]
+"""
+from __future__ import annotations
+
+import argparse
+import hashlib
+import json
+import os
+import subprocess
+import sys
+import tempfile
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+from oracle import build_ref  # noqa: E402
+from tests.golden import cases as CASES  # noqa: E402
+
+
+def sha(a: np.ndarray) -> str:
+    return hashlib.sha256(np.ascontiguousarray(a, dtype=np.float64).tobytes()).hexdigest()
+
+
+def read_grid(d: str, lev: int = 0, reg: int = 0) -> dict:
+    p = os.path.join(d, f"L{lev}R{reg}_")
+    meta = {}
+    with open(p + "meta.txt") as fp:
+        for line in fp:
+            k, *v = line.split()
+            meta[k] = [float(x) if "." in x or "e" in x else int(x) for x in v]
+            if len(meta[k]) == 1:
+                meta[k] = meta[k][0]
+    out = {"meta": meta}
+    for name in ("f", "u", "rho", "uxin", "xpos", "ypos", "zpos", "force"):
+        if os.path.exists(p + name + ".bin"):
+            out[name] = np.fromfile(p + name + ".bin", dtype=np.float64)
+    out["typ"] = np.fromfile(p + "typ.bin", dtype=np.int32)
+    return out
+
+
+def run_case(name: str, ref: str) -> str:
+    spec = CASES.CASES[name]
+    exe = build_ref.build_case(name, ref)
+    work = tempfile.mkdtemp(prefix=f"golden_{name}_")
+    args = [exe, "--out", work, "--steps", str(max(spec["steps"])), "--dump-every", "0"]
+    init = CASES.initial_fields(name)
+    if init is not None:
+        upath = os.path.join(work, "init_u.bin")
+        init["u"].astype(np.float64).tofile(upath)
+        args += ["--init-u", upath]
+    # Dump at each requested step: rerun with --dump-every = gcd is wasteful;
+    # the harness dumps every `dump-every` steps, so pick the gcd of steps.
+    g = 0
+    for s in spec["steps"]:
+        g = np.gcd(g, s)
+    args[args.index("--dump-every") + 1] = str(int(g))
+    subprocess.run(args, check=True)
+    out = {"case": name}
+    s0 = read_grid(os.path.join(work, "s0"))
+    out["omega"] = np.float64(s0["meta"]["omega"])
+    out["typ"] = s0["typ"]
+    out["ux_in"] = s0["uxin"]
+    out["ypos"] = s0["ypos"]
+    out["f0_sha"] = sha(s0["f"])
+    if init is not None:
+        out["init_u"] = init["u"]
+    for s in spec["steps"]:
+        gs = read_grid(os.path.join(work, f"s{s}"))
+        out[f"u_{s}"] = gs["u"]
+        out[f"rho_{s}"] = gs["rho"]
+        out[f"f_sha_{s}"] = sha(gs["f"])
+        if s in spec.get("store_f", ()):
+            out[f"f_{s}"] = gs["f"]
+    with open(os.path.join(work, "timing.txt")) as fp:
+        out["ref_timing"] = fp.read()
+    np.savez_compressed(os.path.join(HERE, f"{name}.npz"), **out)
+    return work
+
+
+def extract_kat(ref: str) -> None:
+    path = os.path.join(ref, "cases", "testsuite", "base", "case000", "io_lite.Lev0.Reg0.Rnk0.0.dat")
+    with open(path) as fp:
+        lines = fp.read().splitlines()
+    head = lines[2].split()
+    row = lines[3].split()
+    col = {h: i for i, h in enumerate(head)}
+    rec = {
+        "source": "LUMA cases/testsuite/base/case000/io_lite.Lev0.Reg0.Rnk0.0.dat, first data row",
+        "rho": float(row[col["RHO"]]),
+        "u": [float(row[col["UX"]]), float(row[col["UY"]])],
+        "f": [float(row[col[f"F{v}"]]) for v in range(9)],
+        "decimals": 8,
+    }
+    with open(os.path.join(HERE, "kat_feq_d2q9.json"), "w") as fp:
+        json.dump(rec, fp, indent=1)
+
+
+def main(argv=None) -> int:
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--ref", default=build_ref.DEFAULT_REF)
+    ap.add_argument("cases", nargs="*")
+    a = ap.parse_args(argv)
+    extract_kat(a.ref)
+    for c in a.cases or sorted(CASES.CASES):
+        print(c, run_case(c, a.ref))
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())
