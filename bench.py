@@ -1,0 +1,367 @@
+"""Benchmark: D3Q19 LBGK periodic box 256^3 (tau = 0.55, Taylor-Green
+u0 = 0.02 plus seeded 1e-4 noise), million lattice updates per second.
+
+One bench step is one LBM time step of the whole 256^3 grid (GridObj::
+LBM_multi_opt on an all-fluid periodic grid).  ``value`` is the shifted-FP32
+path (the chosen precision) with the state resident in HBM; the plain FP64
+path (the reference's arithmetic) is measured on the same workload and
+reported beside it with the FP32-vs-FP64 velocity error.  ``e2e`` goes
+through the C ABI with host buffers: upload of the reference-layout FP64
+state, the K steps, and download of u and rho, all inside the timed region.
+
+Multi-GPU: every rank runs an independent replica of the box (the path has no
+data exchange on one grid per GPU); value = sum over ranks.
+
+``--impl reference`` times the reference's CPU implementation of the path
+(the oracle restatement of GridObj::LBM_multi_opt, OpenMP over all host
+threads) on a bounded slab of the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "D3Q19 MLUPS & %HBM roofline, FP32-shifted vs FP64 at stated error; adjoint cost"
+SIZE = 256
+TAU = 0.55
+U0 = 0.02
+NOISE = 1e-4
+
+
+def workload_level0(n: int, nz: int | None = None):
+    """Level-0 grid of the periodic Taylor-Green box (n x n x nz)."""
+    from luma_gb300 import _abi as A
+    from luma_gb300 import case as hostcase
+    from tests.golden.cases import taylor_green
+    nz = nz or n
+    # dt = dh/16 keeps the reference's Mach check quiet; Re gives nu_lbm = (tau - 0.5)/3.
+    nu_lbm = (TAU - 0.5) / 3.0
+    dt = (1.0 / n) / 16.0
+    re = 1.0 / (nu_lbm * (1.0 / n) ** 2 / dt)
+    d = hostcase.Definitions(dims=3, resolution=n, timestep=dt, bx=1.0, by=1.0, bz=nz / n, re=re,
+                             walls=(A.FLUID,) * 6)
+    l0 = hostcase.build_level0(d)
+    l0.u = taylor_green(n, n, nz, U0, NOISE).reshape(-1)
+    return l0
+
+
+def equilibrium_f(l0):
+    from luma_gb300 import case as hostcase
+    return hostcase.equilibrium(3, 19, l0.rho, l0.u).reshape(-1)
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.samples = []
+        self.proc = None
+        self.thread = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits", "-lms", "100",
+                 "-i", str(self.gpu)], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except (OSError, ValueError):
+            self.proc = None
+            return
+        self.thread = threading.Thread(target=self._read, daemon=True)
+        self.thread.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) >= 9:
+                self.samples.append((time.monotonic(), parts))
+
+    def mark(self):
+        return time.monotonic()
+
+    def stop(self):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self, t0: float, t1: float) -> dict:
+        inside = [p for (t, p) in self.samples if t0 - 0.15 <= t <= t1 + 0.15] or [p for (_, p) in self.samples]
+        if not inside:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no nvidia-smi samples"], "samples": 0}
+
+        def num(x):
+            try:
+                return float(x)
+            except ValueError:
+                return None
+        sm = [num(p[1]) for p in inside if num(p[1]) is not None]
+        smax = [num(p[2]) for p in inside if num(p[2]) is not None]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for p in inside for i in range(4) if p[5 + i].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": reasons, "samples": len(inside),
+                "power_w_max": max((num(p[3]) or 0.0) for p in inside)}
+
+
+def read_peaks() -> dict:
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as fp:
+            d = json.load(fp)
+        return {"hbm_gbs": d["hbm_gbs"], "source": "measured"}
+    return {"hbm_gbs": 6800.0, "source": "fallback"}
+
+
+def read_profile_traffic(name: str):
+    """Per-launch DRAM bytes from a committed ncu summary (profiles/<name>.txt,
+    line 'dram_bytes_per_launch <bytes>'), or None."""
+    p = os.path.join(ROOT, "profiles", name + ".txt")
+    if not os.path.exists(p):
+        return None
+    with open(p) as fp:
+        for line in fp:
+            if line.startswith("dram_bytes_per_launch"):
+                try:
+                    return float(line.split()[1])
+                except (IndexError, ValueError):
+                    return None
+    return None
+
+
+def cpu_oracle_mlups(n: int, nz: int, steps: int, warmup: int, threads: int | None, min_seconds: float = 0.0):
+    """Time the oracle (OpenMP) on an n x n x nz slab: `steps` steps, or more
+    in chunks until at least `min_seconds` of CPU work has been timed."""
+    from oracle import oracle as O
+    l0 = workload_level0(n, nz)
+    f0 = equilibrium_f(l0)
+    g = O.OracleGrid(l0.desc())
+    used = O.set_threads(threads or os.cpu_count() or 1)
+    g.upload(f0, l0.u, l0.rho, None, 0)
+    if warmup:
+        g.step(warmup)
+    done = 0
+    t0 = time.perf_counter()
+    g.step(steps)
+    done += steps
+    while time.perf_counter() - t0 < min_seconds:
+        g.step(steps)
+        done += steps
+    dt = time.perf_counter() - t0
+    return l0.ncell * done / dt / 1e6, used, dt, done
+
+
+def run_reference(args, rank: int, world: int):
+    if rank != 0:
+        return 0
+    nz = 16
+    mlups, used, dt, _ = cpu_oracle_mlups(SIZE, nz, args.steps, args.warmup, None)
+    sample = (f"one LBM step of a {SIZE}x{SIZE}x{nz} periodic slab of the Taylor-Green box per bench step "
+              f"(oracle restatement of GridObj::LBM_multi_opt, FP64, OpenMP)")
+    line = {
+        "metric": METRIC, "value": round(mlups, 3), "unit": "MLUPS", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(dt / args.steps * 1e3, 4), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "impl": "reference",
+        "config": {"workload": f"D3Q19 LBGK periodic {SIZE}x{SIZE}x{nz} slab, tau={TAU}, TGV u0={U0} + noise {NOISE}",
+                   "precision": "fp64", "host_threads": used},
+        "cpu_baseline": {"value": round(mlups, 3), "unit": "MLUPS", "cores": used, "kind": "port",
+                         "sample": sample},
+        "e2e": {"value": round(mlups, 3), "unit": "MLUPS", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_ours(args, rank: int, world: int, local_rank: int):
+    import torch
+    from luma_gb300 import _abi as A
+    from luma_gb300.gpu import GpuGrid
+
+    torch.cuda.set_device(local_rank)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist_
+        dist_.init_process_group("nccl")
+        dist = dist_
+    dev = torch.device("cuda", local_rank)
+    stream = torch.cuda.current_stream(dev)
+    n = args.size
+    l0 = workload_level0(n)
+    f0 = equilibrium_f(l0)
+    ncell = l0.ncell
+    K, W = args.steps, args.warmup
+
+    def barrier():
+        if dist:
+            dist.barrier()
+        torch.cuda.synchronize(dev)
+
+    def max_over_ranks(x: float) -> float:
+        if not dist:
+            return x
+        t = torch.tensor([x], device=dev, dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        return float(t.item())
+
+    def timed_steps(grid, steps, sampler=None):
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        barrier()
+        t0 = time.monotonic()
+        e0.record(stream)
+        grid.step(steps)
+        e1.record(stream)
+        e1.synchronize()
+        t1 = time.monotonic()
+        barrier()
+        return e0.elapsed_time(e1) / 1e3, t0, t1
+
+    # ---- FP32 shifted (headline) ----
+    g32 = GpuGrid(l0.desc(precision=A.PREC_FP32_SHIFTED))
+    g32.set_stream(stream.cuda_stream)
+    g32.upload(f0, l0.u, l0.rho, None, 0)
+    g32.step(W)
+    sampler = ClockSampler(local_rank if "CUDA_VISIBLE_DEVICES" not in os.environ else 0)
+    sampler.start()
+    time.sleep(0.3)
+    sec32, t0, t1 = timed_steps(g32, K)
+    sampler_summary = sampler.summary(t0, t1)
+    sec32 = max_over_ranks(sec32)
+    mlups32 = world * ncell * K / sec32 / 1e6
+    g32.synchronize()
+
+    # ---- FP64 (the reference's arithmetic) on the same workload ----
+    K64 = max(K // 4, 20)
+    g64 = GpuGrid(l0.desc(precision=A.PREC_FP64))
+    g64.set_stream(stream.cuda_stream)
+    g64.upload(f0, l0.u, l0.rho, None, 0)
+    g64.step(W)
+    sec64, _, _ = timed_steps(g64, K64)
+    sampler.stop()
+    sec64 = max_over_ranks(sec64)
+    mlups64 = world * ncell * K64 / sec64 / 1e6
+    # accuracy at equal step counts: bring both to t = W + K
+    g64.step(K - K64)
+    g64.synchronize()
+    s32 = g32.download(f=False)
+    s64 = g64.download(f=False)
+    eu = float(np.linalg.norm(s32["u"] - s64["u"]) / np.linalg.norm(s64["u"]))
+    er = float(np.linalg.norm(s32["rho"] - s64["rho"]) / np.linalg.norm(s64["rho"]))
+    red64 = g64.reduce()
+    g64.close()
+
+    # ---- e2e through the C ABI with host buffers (pinned) ----
+    import torch as _t
+    hf = _t.from_numpy(f0).pin_memory()
+    hu = _t.from_numpy(l0.u).pin_memory()
+    hr = _t.from_numpy(l0.rho).pin_memory()
+    out_u = _t.empty(ncell * 3, dtype=_t.float64).pin_memory()
+    out_r = _t.empty(ncell, dtype=_t.float64).pin_memory()
+    import ctypes as C
+    from luma_gb300.gpu import check, lib
+    L = lib()
+    dp = C.POINTER(C.c_double)
+    ptr = lambda t: C.cast(t.data_ptr(), dp)  # noqa: E731
+    # warm the pool/paths once
+    check(L.luma_gpu_upload_state(C.c_void_p(g32.h), ptr(hf), ptr(hu), ptr(hr), None, 0))
+    barrier()
+    t_e0 = time.perf_counter()
+    check(L.luma_gpu_upload_state(C.c_void_p(g32.h), ptr(hf), ptr(hu), ptr(hr), None, 0))
+    check(L.luma_gpu_step(C.c_void_p(g32.h), K))
+    check(L.luma_gpu_download_state(C.c_void_p(g32.h), None, ptr(out_u), ptr(out_r), None))
+    barrier()
+    sec_e2e = max_over_ranks(time.perf_counter() - t_e0)
+    e2e = world * ncell * K / sec_e2e / 1e6
+    h2d = (f0.nbytes + l0.u.nbytes + l0.rho.nbytes) / K
+    d2h = (out_u.numel() + out_r.numel()) * 8 / K
+    g32.close()
+
+    # ---- roofline ----
+    peaks = read_peaks()
+    bytes32 = 2 * 19 * 4 * ncell
+    ach32 = bytes32 / (sec32 / K) / 1e9
+    traffic = read_profile_traffic("k_aa_d3q19_fp32_256")
+    bytes64 = 2 * 19 * 8 * ncell
+
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        mlc, used, dtc, nst = cpu_oracle_mlups(SIZE, 16, args.cpu_steps, 1, None, min_seconds=10.0)
+        cpu = {"value": round(mlc, 3), "unit": "MLUPS", "cores": used, "kind": "port",
+               "sample": f"{nst} LBM steps of a {SIZE}x{SIZE}x16 periodic slab of the same box "
+                         f"(oracle restatement, FP64, OpenMP), {dtc:.1f} s"}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": round(mlups32, 2), "unit": "MLUPS", "n_gpus": world, "steps": K,
+            "warmup": W, "ms_per_step": round(sec32 / K * 1e3, 5), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": f"D3Q19 LBGK periodic {n}^3 Taylor-Green u0={U0} + U(-{NOISE},{NOISE}) noise "
+                                   f"(seed 20261203), tau={TAU}",
+                       "precision": "fp32_shifted (f_i - w_i*rho0 stored in FP32, FP32 collision)",
+                       "streaming": "in-place AA pattern, SoA", "parallelism": f"replicas x{world}",
+                       "l2": "inputs larger than L2 (1.27 GB FP32 populations per grid)"},
+            "clocks": sampler_summary,
+            "e2e": {"value": round(e2e, 2), "unit": "MLUPS", "h2d_bytes_per_step": int(h2d),
+                    "d2h_bytes_per_step": int(d2h),
+                    "note": "C ABI with pinned host buffers: upload of FP64 reference-layout state, K steps, "
+                            "download of u and rho"},
+            "gpu_launches": K,
+            "roofline": {"bound": "hbm", "achieved": round(ach32, 1), "peak": peaks["hbm_gbs"], "unit": "GB/s",
+                         "frac": round(ach32 / peaks["hbm_gbs"], 4), "traffic": traffic,
+                         "peak_source": peaks["source"], "kernel": "k_aa<19,P32>",
+                         "bytes_per_launch": bytes32},
+            "fp64": {"value": round(mlups64, 2), "unit": "MLUPS", "steps": K64,
+                     "ms_per_step": round(sec64 / K64 * 1e3, 4),
+                     "hbm_gbs": round(bytes64 / (sec64 / K64) / 1e9, 1),
+                     "hbm_frac": round(bytes64 / (sec64 / K64) / 1e9 / peaks["hbm_gbs"], 4)},
+            "fp32_vs_fp64": {"speedup": round(mlups32 / mlups64, 3), "rel_l2_u": eu, "rel_l2_rho": er,
+                             "after_steps": W + K, "fp64_mass": red64["mass"]},
+            "cpu_baseline": cpu,
+        }
+        print(json.dumps(line), flush=True)
+    if dist:
+        dist.destroy_process_group()
+    return 0
+
+
+def main(argv=None) -> int:
+    ap = argparse.ArgumentParser(description=__doc__)
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=2000)
+    ap.add_argument("--warmup", type=int, default=20)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--size", type=int, default=SIZE)
+    ap.add_argument("--cpu-steps", type=int, default=20)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args(argv)
+    if args.warmup < 3:
+        args.warmup = 3
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.impl == "reference":
+        return run_reference(args, rank, world)
+    return run_ours(args, rank, world, local_rank)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,569 @@
+// C ABI of the GB300 LBM time step (include/luma_gpu.h): grid handles,
+// state transfer, the recursive multi-grid step and reductions.
+//
+// The step mirrors GridObj::LBM_multi_opt (LUMA src/GridObj_ops_lbm_optimised.cpp:36-193):
+// two sub-steps of every sub-grid, then this grid's stream/macro/[IBM]/
+// collide, then the buffer swap.  Grids whose sites are all fluid (periodic
+// box, BGK, no forcing, no refinement) run the in-place AA kernel instead of
+// the two-buffer general kernel; both give the reference's result.
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "device.cuh"
+#include "grid.hpp"
+#include "kernels.hpp"
+
+using namespace luma;
+
+static thread_local std::string g_last_error;
+
+int luma_set_error(int code, const char *fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    g_last_error = buf;
+    return code;
+}
+
+#define CK(call)                                                                                  \
+    do {                                                                                          \
+        cudaError_t e_ = (call);                                                                  \
+        if (e_ != cudaSuccess)                                                                    \
+            return luma_set_error(LUMA_E_CUDA, "%s failed: %s", #call, cudaGetErrorString(e_)); \
+    } while (0)
+
+namespace {
+
+template <class F>
+cudaError_t dispatch(int Q, int prec, F &&f) {
+    if (prec == LUMA_PREC_FP64) {
+        if (Q == 9) return f(std::integral_constant<int, 9>{}, P64{});
+        if (Q == 19) return f(std::integral_constant<int, 19>{}, P64{});
+        return f(std::integral_constant<int, 27>{}, P64{});
+    }
+    if (Q == 9) return f(std::integral_constant<int, 9>{}, P32{});
+    if (Q == 19) return f(std::integral_constant<int, 19>{}, P32{});
+    return f(std::integral_constant<int, 27>{}, P32{});
+}
+
+size_t real_size(const luma_gpu_grid *g) { return g->d.precision == LUMA_PREC_FP64 ? 8 : 4; }
+
+// GridUtils::isWithinDomainWall (src/GridUtils.cpp:1369-1430).
+bool within_domain_wall(const luma_grid_desc &d, double x, double y, double z, int nv[3], int *nd, int *edges) {
+    const double *E = d.global_edges, *T = d.wall_thickness;
+    nv[0] = nv[1] = nv[2] = 0;
+    *nd = -1;
+    *edges = 0;
+    if (x > 0.0 && x < T[0]) { *nd = 0; nv[0] = 1; ++*edges; }
+    if (x < E[1] && x > E[1] - T[1]) { *nd = 0; nv[0] = -1; ++*edges; }
+    if (y > 0.0 && y < T[2]) { *nd = 1; nv[1] = 1; ++*edges; }
+    if (y < E[3] && y > E[3] - T[3]) { *nd = 1; nv[1] = -1; ++*edges; }
+    if (d.dims == 3) {
+        if (z > 0.0 && z < T[4]) { *nd = 2; nv[2] = 1; ++*edges; }
+        if (z < E[5] && z > E[5] - T[5]) { *nd = 2; nv[2] = -1; ++*edges; }
+    }
+    return *edges > 0;
+}
+
+void host_c(int Q, int v, int c[3]) {
+    for (int d = 0; d < 3; ++d)
+        c[d] = Q == 9 ? Lattice<9>::c(v, d) : (Q == 19 ? Lattice<19>::c(v, d) : Lattice<27>::c(v, d));
+}
+
+double ramp(const luma_grid_desc &d, double t) {
+    if (d.velocity_ramp > 0.0 && t <= d.velocity_ramp) return (1.0 - std::cos(3.14159265358979323846 * t / d.velocity_ramp)) / 2.0;
+    return 1.0;
+}
+
+// Host pre-processing of the boundary sites: wall normals for slip and
+// regularised sites, and the last writer of each velocity site's u under a
+// velocity ramp.
+int build_site_tables(luma_gpu_grid *g, const int32_t *typ, const double *xpos, const double *ypos,
+                      const double *zpos) {
+    const luma_grid_desc &d = g->d;
+    const int N = d.N, M = d.M, K = d.K, Q = d.Q;
+    const bool reg = (d.flags & LUMA_FLAG_REGULARISED) != 0;
+    std::vector<int8_t> wall;
+    std::vector<RegSite> regs;
+    bool need_wall = false;
+    for (size_t id = 0; id < g->n; ++id)
+        if (typ[id] == LUMA_SITE_SLIP) need_wall = true;
+    if (need_wall) wall.assign(4 * g->n, 0);
+    for (int i = 0; i < N; ++i)
+        for (int j = 0; j < M; ++j)
+            for (int k = 0; k < K; ++k) {
+                const int id = k + j * K + i * K * M;
+                const int t = typ[id];
+                if (t == LUMA_SITE_BFL) return luma_set_error(LUMA_E_INVALID, "BFL sites are outside the GPU path");
+                // Pulling from an extrapolate-right site reads the population two
+                // sites to its left (:246-251): such sites need i >= 2.
+                if (t == LUMA_SITE_EXTRAPOLATE_RIGHT && i < 2)
+                    return luma_set_error(LUMA_E_INVALID, "extrapolate-right site at i=%d < 2", i);
+                if (t == LUMA_SITE_SLIP || (reg && (t == LUMA_SITE_VELOCITY || t == LUMA_SITE_PRESSURE))) {
+                    if (!xpos || !ypos || !zpos)
+                        return luma_set_error(LUMA_E_INVALID, "slip/regularised sites need site positions");
+                    int nv[3], nd, ne;
+                    if (!within_domain_wall(d, xpos[i], ypos[j], zpos[k], nv, &nd, &ne))
+                        return luma_set_error(LUMA_E_INVALID,
+                                              "site (%d,%d,%d): boundary site not located inside a domain wall", i, j, k);
+                    if (t == LUMA_SITE_SLIP) {
+                        wall[4 * (size_t)id + 0] = (int8_t)nv[0];
+                        wall[4 * (size_t)id + 1] = (int8_t)nv[1];
+                        wall[4 * (size_t)id + 2] = (int8_t)nv[2];
+                        wall[4 * (size_t)id + 3] = (int8_t)ne;
+                    } else {
+                        if (ne > 1 && t == LUMA_SITE_PRESSURE)
+                            return luma_set_error(LUMA_E_INVALID, "Pressure BC not supported at corner/edge site");
+                        RegSite r;
+                        r.id = id; r.i = i; r.j = j; r.k = k;
+                        r.nvec[0] = (int8_t)nv[0]; r.nvec[1] = (int8_t)nv[1]; r.nvec[2] = (int8_t)nv[2];
+                        r.ndir = (int8_t)nd;
+                        r.edges = (int8_t)ne;
+                        // extrapolation needs two inward neighbours on the grid
+                        const int i2 = i + 2 * nv[0], j2 = j + 2 * nv[1], k2 = k + 2 * nv[2];
+                        if (i2 < 0 || i2 >= N || j2 < 0 || j2 >= M || k2 < 0 || k2 >= K)
+                            return luma_set_error(LUMA_E_INVALID, "Extrapolation does not have enough available cells.");
+                        regs.push_back(r);
+                    }
+                }
+            }
+    // Velocity sites under a ramp without regularisation: row of the last
+    // (i,j,k,v)-ordered site that streams from them (:255-265).
+    std::vector<int2> velu;
+    if (d.velocity_ramp > 0.0 && !reg) {
+        for (int si = 0; si < N; ++si)
+            for (int sj = 0; sj < M; ++sj)
+                for (int sk = 0; sk < K; ++sk) {
+                    const int sid = sk + sj * K + si * K * M;
+                    if (typ[sid] != LUMA_SITE_VELOCITY) continue;
+                    long best = -1;
+                    int best_row = -1;
+                    for (int v = 0; v < Q; ++v) {
+                        int c[3];
+                        host_c(Q, v, c);
+                        const int x = (si + c[0] + N) % N, y = (sj + c[1] + M) % M, z = (sk + c[2] + K) % K;
+                        const int xid = z + y * K + x * K * M;
+                        const int xt = typ[xid];
+                        if (xt == LUMA_SITE_SOLID || xt == LUMA_SITE_REFINED || xt == LUMA_SITE_VELOCITY) continue;
+                        if (xt == LUMA_SITE_SLIP) continue;  // reflected links never reach the velocity branch
+                        const long key = (long)xid * Q + v;
+                        if (key > best) { best = key; best_row = y; }
+                    }
+                    if (best_row >= 0) velu.push_back(make_int2(sid, best_row));
+                }
+    }
+    if (need_wall) {
+        CK(cudaMalloc(&g->wall, wall.size()));
+        CK(cudaMemcpy(g->wall, wall.data(), wall.size(), cudaMemcpyHostToDevice));
+    }
+    g->nreg = (int)regs.size();
+    if (g->nreg) {
+        CK(cudaMalloc(&g->reg, regs.size() * sizeof(RegSite)));
+        CK(cudaMemcpy(g->reg, regs.data(), regs.size() * sizeof(RegSite), cudaMemcpyHostToDevice));
+    }
+    g->nvelu = (int)velu.size();
+    if (g->nvelu) {
+        CK(cudaMalloc(&g->velu, velu.size() * sizeof(int2)));
+        CK(cudaMemcpy(g->velu, velu.data(), velu.size() * sizeof(int2), cudaMemcpyHostToDevice));
+    }
+    return LUMA_OK;
+}
+
+StepArgs make_args(luma_gpu_grid *g, int subcycle) {
+    const luma_grid_desc &d = g->d;
+    StepArgs a;
+    memset(&a, 0, sizeof a);
+    a.N = d.N; a.M = d.M; a.K = d.K; a.ncell = (int)g->n;
+    a.typ = g->typ;
+    a.f = g->f[g->cur];
+    a.fNew = g->f[g->cur ^ 1];
+    a.u = g->u; a.rho = g->rho; a.force = g->force;
+    a.ux_in = g->uxin; a.uy_in = g->uyin; a.uz_in = g->uzin;
+    a.omega = d.omega; a.rho0 = d.rho_in; a.cs2 = g->cs2; a.csmag = d.csmag;
+    a.pdelta = d.pressure_delta;
+    a.has_ramp = d.velocity_ramp > 0.0;
+    a.ramp_stream = ramp(d, g->t * d.dt);
+    a.ramp_reg = ramp(d, (g->t + 1) * d.dt);
+    a.flags = d.flags; a.collision = d.collision; a.subcycle = subcycle;
+    a.forcing = (d.flags & (LUMA_FLAG_IBM | LUMA_FLAG_GRAVITY)) != 0;
+    a.ibm_split = (d.flags & LUMA_FLAG_IBM) != 0;
+    a.level = d.level;
+    if (g->parent) {
+        a.parent_f = g->parent->f[g->parent->cur];
+        a.pN = g->parent->d.N; a.pM = g->parent->d.M; a.pK = g->parent->d.K;
+        for (int q = 0; q < 6; ++q) a.lims[q] = d.coarse_lims[q];
+    }
+    a.nchild = (int)g->kids.size();
+    for (int s = 0; s < a.nchild && s < kMaxChildren; ++s) {
+        luma_gpu_grid *c = g->kids[s];
+        a.child[s].f = c->f[c->cur];
+        a.child[s].u = c->u;
+        a.child[s].rho = c->rho;
+        a.child[s].N = c->d.N; a.child[s].M = c->d.M; a.child[s].K = c->d.K;
+        for (int q = 0; q < 6; ++q) a.child[s].lims[q] = c->d.coarse_lims[q];
+    }
+    return a;
+}
+
+bool bulk_eligible(const luma_gpu_grid *g, const int32_t *typ) {
+    const luma_grid_desc &d = g->d;
+    if (g->parent || !g->kids.empty()) return false;
+    if (d.collision != LUMA_COLL_BGK) return false;
+    if (d.N > 65535 || d.M > 65535) return false;  // grid.y / grid.z launch limits
+    if (d.flags & (LUMA_FLAG_IBM | LUMA_FLAG_GRAVITY | LUMA_FLAG_REGULARISED)) return false;
+    for (size_t i = 0; i < g->n; ++i)
+        if (typ[i] != LUMA_SITE_FLUID) return false;
+    return true;
+}
+
+int step_grid(luma_gpu_grid *g, int subcycle, bool write_macro) {
+    for (luma_gpu_grid *c : g->kids)
+        for (int it = 0; it < 2; ++it) {
+            int rc = step_grid(c, it, true);
+            if (rc) return rc;
+        }
+    const luma_grid_desc &d = g->d;
+    cudaStream_t s = g->stream;
+    if (g->bulk) {
+        CK(dispatch(d.Q, d.precision, [&](auto q, auto p) {
+            return launch_aa<decltype(q)::value, decltype(p)>(g->f[0], g->u, g->rho, d.N, d.M, d.K, d.omega,
+                                                              d.rho_in, g->aa_odd == 0, write_macro, s);
+        }));
+        g->aa_odd ^= 1;
+        ++g->t;
+        return LUMA_OK;
+    }
+    StepArgs a = make_args(g, subcycle);
+    if (g->ibm && g->ibm->has_bodies) {
+        int rc = luma_ibm_reset_forces(g);
+        if (rc) return rc;
+    }
+    CK(dispatch(d.Q, d.precision, [&](auto q, auto p) {
+        return launch_general_phaseA<decltype(q)::value, decltype(p)>(a, g->wall, s);
+    }));
+    if (g->nreg)
+        CK(dispatch(d.Q, d.precision, [&](auto q, auto p) {
+            return launch_general_phaseB<decltype(q)::value, decltype(p)>(a, g->wall, g->reg, g->nreg, s);
+        }));
+    if (g->nvelu) {
+        if (d.precision == LUMA_PREC_FP64) CK(launch_velocity_u<P64>(a, d.dims, g->velu, g->nvelu, s));
+        else CK(launch_velocity_u<P32>(a, d.dims, g->velu, g->nvelu, s));
+    }
+    if (a.ibm_split) {
+        if (g->ibm && g->ibm->has_bodies) {
+            int rc = luma_ibm_apply(g, a);
+            if (rc) return rc;
+        }
+        CK(dispatch(d.Q, d.precision, [&](auto q, auto p) {
+            return launch_general_phaseC<decltype(q)::value, decltype(p)>(a, s);
+        }));
+    }
+    g->cur ^= 1;
+    ++g->t;
+    return LUMA_OK;
+}
+
+void free_grid(luma_gpu_grid *g) {
+    if (!g) return;
+    for (luma_gpu_grid *c : g->kids) free_grid(c);
+    luma_ibm_free(g);
+    cudaFree(g->typ);
+    cudaFree(g->f[0]);
+    cudaFree(g->f[1]);
+    cudaFree(g->u);
+    cudaFree(g->rho);
+    cudaFree(g->force);
+    cudaFree(g->uxin);
+    cudaFree(g->uyin);
+    cudaFree(g->uzin);
+    cudaFree(g->wall);
+    cudaFree(g->reg);
+    cudaFree(g->velu);
+    cudaFree(g->acc);
+    delete g;
+}
+
+}  // namespace
+
+extern "C" {
+
+int luma_gpu_abi_version(void) { return LUMA_GPU_ABI_VERSION; }
+
+const char *luma_gpu_last_error_string(void) { return g_last_error.c_str(); }
+
+int luma_gpu_grid_create(const luma_grid_desc *desc, luma_gpu_grid *parent, luma_gpu_grid **out) {
+    if (!desc || !out) return luma_set_error(LUMA_E_INVALID, "null argument");
+    *out = nullptr;
+    const luma_grid_desc &d = *desc;
+    if (d.abi_version != LUMA_GPU_ABI_VERSION)
+        return luma_set_error(LUMA_E_INVALID, "ABI version %d, library is %d", d.abi_version, LUMA_GPU_ABI_VERSION);
+    if (!((d.dims == 2 && d.Q == 9) || (d.dims == 3 && (d.Q == 19 || d.Q == 27))))
+        return luma_set_error(LUMA_E_INVALID, "unsupported lattice D%dQ%d", d.dims, d.Q);
+    if (d.N <= 0 || d.M <= 0 || d.K <= 0 || (d.dims == 2 && d.K != 1))
+        return luma_set_error(LUMA_E_INVALID, "bad grid size %dx%dx%d", d.N, d.M, d.K);
+    if ((double)d.N * d.M * d.K * d.Q >= 9.0e18) return luma_set_error(LUMA_E_INVALID, "grid too large");
+    if ((size_t)d.N * d.M * d.K > 0x7fffffffu)
+        return luma_set_error(LUMA_E_INVALID, "grid has more than 2^31-1 sites");
+    if (d.precision != LUMA_PREC_FP64 && d.precision != LUMA_PREC_FP32_SHIFTED)
+        return luma_set_error(LUMA_E_INVALID, "unknown precision %d", d.precision);
+    if (d.collision < LUMA_COLL_BGK || d.collision > LUMA_COLL_KBC)
+        return luma_set_error(LUMA_E_INVALID, "unknown collision %d", d.collision);
+    if (d.collision == LUMA_COLL_KBC && d.dims == 3 && d.Q != 27)
+        return luma_set_error(LUMA_E_INVALID, "3D KBC needs D3Q27 (the reference forces L_NUM_VELS 27)");
+    if (d.flags & LUMA_FLAG_REGULARISED && d.Q == 27)
+        return luma_set_error(LUMA_E_INVALID, "Cannot use regularised boundaries with D3Q27");
+    if (!(d.omega > 0.0) || (d.omega >= 2.0 && d.collision != LUMA_COLL_BGK_SMAG))
+        return luma_set_error(LUMA_E_INVALID, "relaxation frequency omega=%g out of range", d.omega);
+    if (!d.lattyp) return luma_set_error(LUMA_E_INVALID, "lattyp is required");
+    if (!d.ux_in || !d.uy_in || !d.uz_in) return luma_set_error(LUMA_E_INVALID, "inlet profile arrays are required");
+    if (parent) {
+        if (parent->bulk_fixed) return luma_set_error(LUMA_E_STATE, "parent grid already holds state");
+        if ((int)parent->kids.size() >= kMaxChildren) return luma_set_error(LUMA_E_INVALID, "too many sub-grids");
+        if (parent->d.dims != d.dims || parent->d.Q != d.Q || parent->d.precision != d.precision)
+            return luma_set_error(LUMA_E_INVALID, "sub-grid lattice/precision differs from its parent");
+        if (d.level != parent->d.level + 1) return luma_set_error(LUMA_E_INVALID, "sub-grid level must be parent+1");
+        // Explode reads parent site (fine/2 + lim) and coalesce reads the 2^d
+        // children of each covered coarse site: both stay inside the two grids
+        // when the limits lie on the parent and the child spans them exactly.
+        const int *L = d.coarse_lims;
+        const int pdim[3] = {parent->d.N, parent->d.M, parent->d.K};
+        const int cdim[3] = {d.N, d.M, d.K};
+        for (int a = 0; a < d.dims; ++a)
+            if (L[2 * a] < 0 || L[2 * a + 1] >= pdim[a] || L[2 * a] > L[2 * a + 1] ||
+                cdim[a] != 2 * (L[2 * a + 1] - L[2 * a] + 1))
+                return luma_set_error(LUMA_E_INVALID, "sub-grid coarse limits/size inconsistent on axis %d", a);
+    }
+    luma_gpu_grid *g = new (std::nothrow) luma_gpu_grid();
+    if (!g) return luma_set_error(LUMA_E_NOMEM, "host allocation failed");
+    g->d = d;
+    g->n = (size_t)d.N * d.M * d.K;
+    {
+        const double cs = 1.0 / std::sqrt(3.0);
+        g->cs2 = cs * cs;
+    }
+    g->parent = parent;
+    g->stream = parent ? parent->stream : nullptr;
+    int rc = LUMA_OK;
+    auto fail = [&](int code) {
+        free_grid(g);
+        return code;
+    };
+    std::vector<uint8_t> typ8(g->n);
+    for (size_t i = 0; i < g->n; ++i) {
+        if (d.lattyp[i] < 0 || d.lattyp[i] > LUMA_SITE_EXTRAPOLATE_RIGHT) {
+            luma_set_error(LUMA_E_INVALID, "site %zu has unknown label %d", i, d.lattyp[i]);
+            return fail(LUMA_E_INVALID);
+        }
+        typ8[i] = (uint8_t)d.lattyp[i];
+    }
+    const size_t rs = real_size(g);
+    const size_t popb = g->n * d.Q * rs;
+#define CKF(call)                                                                                 \
+    do {                                                                                          \
+        cudaError_t e_ = (call);                                                                  \
+        if (e_ != cudaSuccess) {                                                                  \
+            luma_set_error(e_ == cudaErrorMemoryAllocation ? LUMA_E_NOMEM : LUMA_E_CUDA, "%s: %s", #call, \
+                           cudaGetErrorString(e_));                                               \
+            return fail(e_ == cudaErrorMemoryAllocation ? LUMA_E_NOMEM : LUMA_E_CUDA);          \
+        }                                                                                         \
+    } while (0)
+    CKF(cudaMalloc(&g->typ, g->n));
+    CKF(cudaMemcpy(g->typ, typ8.data(), g->n, cudaMemcpyHostToDevice));
+    g->bulk = bulk_eligible(g, d.lattyp);
+    CKF(cudaMalloc(&g->f[0], popb));
+    if (!g->bulk) CKF(cudaMalloc(&g->f[1], popb));
+    CKF(cudaMalloc(&g->u, g->n * d.dims * rs));
+    CKF(cudaMalloc(&g->rho, g->n * rs));
+    CKF(cudaMemset(g->u, 0, g->n * d.dims * rs));
+    CKF(cudaMemset(g->rho, 0, g->n * rs));
+    if (d.flags & (LUMA_FLAG_IBM | LUMA_FLAG_GRAVITY)) {
+        CKF(cudaMalloc(&g->force, g->n * d.dims * rs));
+        CKF(cudaMemset(g->force, 0, g->n * d.dims * rs));
+    }
+    CKF(cudaMalloc(&g->uxin, d.M * sizeof(double)));
+    CKF(cudaMalloc(&g->uyin, d.M * sizeof(double)));
+    CKF(cudaMalloc(&g->uzin, d.M * sizeof(double)));
+    CKF(cudaMemcpy(g->uxin, d.ux_in, d.M * sizeof(double), cudaMemcpyHostToDevice));
+    CKF(cudaMemcpy(g->uyin, d.uy_in, d.M * sizeof(double), cudaMemcpyHostToDevice));
+    CKF(cudaMemcpy(g->uzin, d.uz_in, d.M * sizeof(double), cudaMemcpyHostToDevice));
+    CKF(cudaMalloc(&g->acc, 8 * sizeof(double)));
+    rc = build_site_tables(g, d.lattyp, d.xpos, d.ypos, d.zpos);
+    if (rc) return fail(rc);
+    g->d.lattyp = nullptr;
+    g->d.xpos = g->d.ypos = g->d.zpos = nullptr;
+    g->d.ux_in = g->d.uy_in = g->d.uz_in = nullptr;
+    if (parent) {
+        parent->kids.push_back(g);
+        if (parent->bulk) {
+            // A grid with sub-grids takes the general path; it holds no state yet.
+            parent->bulk = false;
+            if (!parent->f[1] && cudaMalloc(&parent->f[1], parent->n * parent->d.Q * real_size(parent)) != cudaSuccess) {
+                parent->kids.pop_back();
+                luma_set_error(LUMA_E_NOMEM, "second population buffer for parent");
+                return fail(LUMA_E_NOMEM);
+            }
+        }
+    }
+    *out = g;
+    return LUMA_OK;
+#undef CKF
+}
+
+int luma_gpu_grid_destroy(luma_gpu_grid *g) {
+    if (!g) return LUMA_OK;
+    if (g->parent) {
+        auto &k = g->parent->kids;
+        for (size_t i = 0; i < k.size(); ++i)
+            if (k[i] == g) { k.erase(k.begin() + i); break; }
+    }
+    free_grid(g);
+    return LUMA_OK;
+}
+
+static void set_stream_rec(luma_gpu_grid *g, cudaStream_t s) {
+    g->stream = s;
+    for (luma_gpu_grid *c : g->kids) set_stream_rec(c, s);
+}
+
+int luma_gpu_set_stream(luma_gpu_grid *root, void *cuda_stream) {
+    if (!root) return luma_set_error(LUMA_E_INVALID, "null grid");
+    set_stream_rec(root, static_cast<cudaStream_t>(cuda_stream));
+    return LUMA_OK;
+}
+
+int luma_gpu_upload_state(luma_gpu_grid *g, const double *f, const double *u, const double *rho,
+                          const double *force_xyz, int t) {
+    if (!g) return luma_set_error(LUMA_E_INVALID, "null grid");
+    const luma_grid_desc &d = g->d;
+    cudaStream_t s = g->stream;
+    const size_t rs = real_size(g);
+    double *stage = nullptr;
+    const size_t maxd = g->n * (size_t)(d.Q > d.dims ? d.Q : d.dims);
+    CK(cudaMallocAsync(&stage, maxd * sizeof(double), s));
+    int rc = LUMA_OK;
+    auto run = [&]() -> int {
+        if (f) {
+            CK(cudaMemcpyAsync(stage, f, g->n * d.Q * sizeof(double), cudaMemcpyHostToDevice, s));
+            const int layout = g->bulk ? kPopAAE : kPopPlain;
+            CK(dispatch(d.Q, d.precision, [&](auto q, auto p) {
+                return launch_pop_in<decltype(q)::value, decltype(p)>(stage, g->f[0], d.N, d.M, d.K, layout, d.rho_in, s);
+            }));
+            if (!g->bulk) CK(cudaMemcpyAsync(g->f[1], g->f[0], g->n * d.Q * rs, cudaMemcpyDeviceToDevice, s));
+            g->cur = 0;
+            g->aa_odd = 0;
+        }
+        auto vec_in = [&](const double *h, void *dst, int dims) -> int {
+            CK(cudaMemcpyAsync(stage, h, g->n * dims * sizeof(double), cudaMemcpyHostToDevice, s));
+            if (d.precision == LUMA_PREC_FP64) CK(launch_vec_in<P64>(stage, dst, g->n, dims, s));
+            else CK(launch_vec_in<P32>(stage, dst, g->n, dims, s));
+            return LUMA_OK;
+        };
+        if (u && (rc = vec_in(u, g->u, d.dims))) return rc;
+        if (rho && (rc = vec_in(rho, g->rho, 1))) return rc;
+        if (force_xyz) {
+            if (!g->force) return luma_set_error(LUMA_E_STATE, "grid has no force field (no IBM/gravity flag)");
+            if ((rc = vec_in(force_xyz, g->force, d.dims))) return rc;
+        }
+        return LUMA_OK;
+    };
+    rc = run();
+    cudaFreeAsync(stage, s);
+    CK(cudaStreamSynchronize(s));
+    if (rc) return rc;
+    g->t = t;
+    g->bulk_fixed = true;
+    return LUMA_OK;
+}
+
+int luma_gpu_download_state(luma_gpu_grid *g, double *f, double *u, double *rho, double *force_xyz) {
+    if (!g) return luma_set_error(LUMA_E_INVALID, "null grid");
+    const luma_grid_desc &d = g->d;
+    cudaStream_t s = g->stream;
+    double *stage = nullptr;
+    const size_t maxd = g->n * (size_t)(d.Q > d.dims ? d.Q : d.dims);
+    CK(cudaMallocAsync(&stage, maxd * sizeof(double), s));
+    int rc = LUMA_OK;
+    auto run = [&]() -> int {
+        if (f) {
+            const int layout = g->bulk ? (g->aa_odd ? kPopAAO : kPopAAE) : kPopPlain;
+            const void *src = g->bulk ? g->f[0] : g->f[g->cur];
+            CK(dispatch(d.Q, d.precision, [&](auto q, auto p) {
+                return launch_pop_out<decltype(q)::value, decltype(p)>(src, stage, d.N, d.M, d.K, layout, d.rho_in, s);
+            }));
+            CK(cudaMemcpyAsync(f, stage, g->n * d.Q * sizeof(double), cudaMemcpyDeviceToHost, s));
+            CK(cudaStreamSynchronize(s));
+        }
+        auto vec_out = [&](const void *src, double *h, int dims) -> int {
+            if (d.precision == LUMA_PREC_FP64) CK(launch_vec_out<P64>(src, stage, g->n, dims, s));
+            else CK(launch_vec_out<P32>(src, stage, g->n, dims, s));
+            CK(cudaMemcpyAsync(h, stage, g->n * dims * sizeof(double), cudaMemcpyDeviceToHost, s));
+            CK(cudaStreamSynchronize(s));
+            return LUMA_OK;
+        };
+        if (u && (rc = vec_out(g->u, u, d.dims))) return rc;
+        if (rho && (rc = vec_out(g->rho, rho, 1))) return rc;
+        if (force_xyz) {
+            if (!g->force) memset(force_xyz, 0, g->n * d.dims * sizeof(double));
+            else if ((rc = vec_out(g->force, force_xyz, d.dims))) return rc;
+        }
+        return LUMA_OK;
+    };
+    rc = run();
+    cudaFreeAsync(stage, s);
+    CK(cudaStreamSynchronize(s));
+    return rc;
+}
+
+int luma_gpu_get_time(const luma_gpu_grid *g, int *t) {
+    if (!g || !t) return luma_set_error(LUMA_E_INVALID, "null argument");
+    *t = g->t;
+    return LUMA_OK;
+}
+
+int luma_gpu_step(luma_gpu_grid *root, int nsteps) {
+    if (!root) return luma_set_error(LUMA_E_INVALID, "null grid");
+    if (root->parent) return luma_set_error(LUMA_E_INVALID, "luma_gpu_step takes the level-0 grid");
+    if (nsteps < 0) return luma_set_error(LUMA_E_INVALID, "negative step count");
+    for (int s = 0; s < nsteps; ++s) {
+        int rc = step_grid(root, 0, s == nsteps - 1);
+        if (rc) return rc;
+    }
+    return LUMA_OK;
+}
+
+int luma_gpu_synchronize(luma_gpu_grid *root) {
+    if (!root) return luma_set_error(LUMA_E_INVALID, "null grid");
+    CK(cudaStreamSynchronize(root->stream));
+    if (int u = read_unsupported_flag(root->stream))
+        return luma_set_error(LUMA_E_INVALID, "a site needed an operation outside the GPU path (code %d)", u);
+    return LUMA_OK;
+}
+
+int luma_gpu_reduce(luma_gpu_grid *g, luma_reduction *out) {
+    if (!g || !out) return luma_set_error(LUMA_E_INVALID, "null argument");
+    const luma_grid_desc &d = g->d;
+    if (d.precision == LUMA_PREC_FP64) CK(launch_reduce<P64>(g->typ, g->rho, g->u, g->n, d.dims, g->acc, g->stream));
+    else CK(launch_reduce<P32>(g->typ, g->rho, g->u, g->n, d.dims, g->acc, g->stream));
+    double h[7];
+    CK(cudaMemcpyAsync(h, g->acc, sizeof h, cudaMemcpyDeviceToHost, g->stream));
+    CK(cudaStreamSynchronize(g->stream));
+    out->mass = h[0];
+    out->momentum[0] = h[1];
+    out->momentum[1] = h[2];
+    out->momentum[2] = h[3];
+    out->kinetic_energy = h[4];
+    memcpy(&out->max_speed, &h[5], sizeof(double));
+    out->nonfinite = (int64_t)h[6];
+    return LUMA_OK;
+}
+
+}  // extern "C"

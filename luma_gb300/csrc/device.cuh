@@ -1,0 +1,148 @@
+// Device-side grid state, precision policies and the per-site physics shared
+// by the LBM kernels.
+//
+// Populations live on the device as structure-of-arrays, f[v*ncell + id],
+// with the reference's site index id = k + j*K + i*K*M (z fastest; LUMA
+// src/GridObj_ops_lbm_optimised.cpp:79), so consecutive threads touch
+// consecutive addresses for every direction.  Macroscopic fields are SoA too
+// (u[d*ncell + id]).
+//
+// Two precision policies:
+//  * P64: FP64 storage and arithmetic (the reference's arithmetic);
+//  * P32: shifted FP32 storage g_i = f_i - w_i*rho0 with FP32 arithmetic.
+//    Every operation of the step is linear in the populations with weights
+//    that respect w_i = w_opp(i), so it acts on g exactly as on f once the
+//    equilibrium is shifted the same way: g_eq_i = w_i*(rho - rho0) +
+//    w_i*rho*(c_i.u/cs^2 + ...).  Keeping rho - rho0 = sum_i g_i as the
+//    primary density variable removes the O(1) offset that costs FP32
+//    populations their significant bits.
+#pragma once
+
+#include <cstdint>
+
+#include "lattice.cuh"
+#include "../../include/luma_gpu.h"
+
+namespace luma {
+
+struct P64 {
+    using S = double;  // storage
+    using R = double;  // arithmetic
+    static constexpr bool shifted = false;
+};
+struct P32 {
+    using S = float;
+    using R = float;
+    static constexpr bool shifted = true;
+};
+
+constexpr int kMaxChildren = 4;
+
+// A sub-grid as seen by its parent (coalesce and the transition-layer
+// macroscopic copy, :591-636 and :850-891).
+struct ChildView {
+    const void *f;     // child's current population buffer (S*)
+    void *u, *rho;     // child's macroscopic fields (R*)
+    int N, M, K;
+    int lims[6];       // child's CoarseLims on this grid
+};
+
+// Everything a step kernel reads about one grid.  Passed by value.
+struct StepArgs {
+    int N, M, K, ncell;
+    const uint8_t *typ;
+    const void *f;          // populations before the step (S*)
+    void *fNew;             // populations after the step (S*)
+    void *u, *rho;          // R*, SoA
+    const void *force;      // R*, SoA force_xyz (null when no forcing)
+    const double *ux_in, *uy_in, *uz_in;
+    double omega, rho0, cs2, csmag;
+    double pdelta;          // GridUnits::pd2dlbm(L_PRESSURE_DELTA)
+    double ramp_stream;     // velocity-ramp coefficient at t*dt (0 => no ramp write)
+    double ramp_reg;        // ramp coefficient at (t+1)*dt (regularised BCs)
+    int has_ramp;
+    int flags, collision, subcycle;
+    int forcing;            // IBM or gravity forcing active
+    int ibm_split;          // reference compiled with L_IBM_ON: collide in a second pass
+    // explode source (parent grid), :646-663
+    const void *parent_f;
+    int pN, pM, pK;
+    int lims[6];            // this grid's CoarseLims on the parent
+    int level;
+    int nchild;
+    ChildView child[kMaxChildren];
+};
+
+// Per regularised site: inward normal, normal direction and edge count from
+// GridUtils::isWithinDomainWall (src/GridUtils.cpp:1369-1430), computed on
+// the host from the site positions.
+struct RegSite {
+    int id, i, j, k;
+    int8_t nvec[3];
+    int8_t ndir;
+    int8_t edges;
+};
+
+template <class P>
+__device__ __forceinline__ typename P::R ld(const void *p, size_t idx) {
+    return static_cast<typename P::R>(static_cast<const typename P::S *>(p)[idx]);
+}
+template <class P>
+__device__ __forceinline__ void st(void *p, size_t idx, typename P::R v) {
+    static_cast<typename P::S *>(p)[idx] = static_cast<typename P::S>(v);
+}
+template <class P>
+__device__ __forceinline__ typename P::R ldr(const void *p, size_t idx) {
+    return static_cast<const typename P::R *>(p)[idx];
+}
+template <class P>
+__device__ __forceinline__ void str(void *p, size_t idx, typename P::R v) {
+    static_cast<typename P::R *>(p)[idx] = v;
+}
+
+// The non-constant part of the equilibrium, A/cs^2 + B/(2 cs^4), in the
+// reference's expression order (_LBM_equilibrium_opt, :674-705).
+template <int Q, class R>
+__device__ __forceinline__ R eq_poly(int v, R ux, R uy, R uz, R cs2) {
+    using L = Lattice<Q>;
+    const R c0 = R(L::c(v, 0)), c1 = R(L::c(v, 1)), c2 = R(L::c(v, 2));
+    R A, B;
+    if (L::D == 3) {
+        A = (c0 * ux) + (c1 * uy) + (c2 * uz);
+        B = (R(L::c(v, 0) * L::c(v, 0)) - cs2) * (ux * ux) + (R(L::c(v, 1) * L::c(v, 1)) - cs2) * (uy * uy) +
+            (R(L::c(v, 2) * L::c(v, 2)) - cs2) * (uz * uz) + R(2 * L::c(v, 0) * L::c(v, 1)) * ux * uy +
+            R(2 * L::c(v, 0) * L::c(v, 2)) * ux * uz + R(2 * L::c(v, 1) * L::c(v, 2)) * uy * uz;
+    } else {
+        A = (c0 * ux) + (c1 * uy);
+        B = (R(L::c(v, 0) * L::c(v, 0)) - cs2) * (ux * ux) + (R(L::c(v, 1) * L::c(v, 1)) - cs2) * (uy * uy) +
+            R(2 * L::c(v, 0) * L::c(v, 1)) * ux * uy;
+    }
+    return (A / cs2) + (B / (R(2) * cs2 * cs2));
+}
+
+// Equilibrium in the stored representation: f_eq (P64) or g_eq = f_eq - w*rho0 (P32).
+template <int Q, class P>
+__device__ __forceinline__ typename P::R feq_s(int v, typename P::R rho, typename P::R drho, typename P::R ux,
+                                                typename P::R uy, typename P::R uz, typename P::R cs2) {
+    using R = typename P::R;
+    const R w = R(Lattice<Q>::w(v));
+    if (P::shifted) return w * drho + w * rho * eq_poly<Q, R>(v, ux, uy, uz, cs2);
+    return rho * w * (R(1) + eq_poly<Q, R>(v, ux, uy, uz, cs2));
+}
+
+// Guo forcing term of direction v (_LBM_forceGrid_opt, :928-990).
+template <int Q, class R>
+__device__ __forceinline__ R guo(int v, R omega, R cs2, R ux, R uy, R uz, R Fx, R Fy, R Fz) {
+    using L = Lattice<Q>;
+    const R lambda = (R(1) - R(0.5) * omega) * (R(L::w(v)) / cs2);
+    R beta = R(L::c(v, 0)) * ux + R(L::c(v, 1)) * uy;
+    if (L::D == 3) beta += R(L::c(v, 2)) * uz;
+    beta = beta * (R(1) / cs2);
+    R s = R(0);
+    s += Fx * (R(L::c(v, 0)) * (R(1) + beta) - ux);
+    s += Fy * (R(L::c(v, 1)) * (R(1) + beta) - uy);
+    if (L::D == 3) s += Fz * (R(L::c(v, 2)) * (R(1) + beta) - uz);
+    return s * lambda;
+}
+
+}  // namespace luma

@@ -1,0 +1,584 @@
+// General two-buffer LBM step: every site type of the reference's stream,
+// macroscopic, forcing and collision operators, with the reference's
+// update order.  Used for grids with boundaries, refinement or IBM; the
+// all-periodic fast path lives in k_bulk.cu.
+//
+// One step of a grid (GridObj::LBM_multi_opt, src/GridObj_ops_lbm_optimised.cpp:36-193):
+//   phase A  k_stream_macro   stream (:206-297) + macroscopic (:800-919)
+//                             [+ forcing and collision when the reference runs
+//                             a single loop, i.e. without L_IBM_ON]
+//   phase B  k_regularised    regularised velocity/pressure sites (:313-510);
+//                             they read the interior macroscopic values of
+//                             phase A (extrapolation, :1353-1412)
+//   phase V  k_velocity_u     the u written into velocity sites by the
+//                             forced-equilibrium BC under a velocity ramp (:255-265)
+//   [IBM pass]
+//   phase C  k_force_collide  forcing (:928-990) + collision (:765-790,
+//                             :1122-1305) when the reference splits the loop
+// followed by a swap of the two population buffers (:159).
+#include <cuda_runtime.h>
+
+#include "device.cuh"
+#include "kernels.hpp"
+
+namespace luma {
+
+namespace {
+
+__device__ int g_unsupported;  // set when a site needs a feature outside the GPU path
+
+template <int Q>
+__device__ __forceinline__ int child_at(const StepArgs &a, int i, int j, int k) {
+    constexpr int D = Lattice<Q>::D;
+    if (a.level > 0) return a.nchild ? 0 : -1;
+    for (int s = 0; s < a.nchild; ++s) {
+        const int *L = a.child[s].lims;
+        if (i >= L[0] && i <= L[1] && j >= L[2] && j <= L[3] && (D == 2 || (k >= L[4] && k <= L[5]))) return s;
+    }
+    return -1;
+}
+
+// _LBM_stream_opt (:206-297) for one site; fills fn[] with the streamed
+// populations in the stored representation.
+template <int Q, class P>
+__device__ __forceinline__ void stream_site(const StepArgs &a, const int8_t *wall, int i, int j, int k, int id,
+                                            int type, typename P::R *fn) {
+    using L = Lattice<Q>;
+    using R = typename P::R;
+    constexpr int D = L::D;
+    const int N = a.N, M = a.M, K = a.K;
+    const size_t n = (size_t)a.ncell;
+    int slip_plane_mask = 0;  // for slip sites: bit v set when direction v is reflected, plane in nibble
+    int8_t nv0 = 0, nv1 = 0, nv2 = 0;
+    if (type == LUMA_SITE_SLIP) {
+        nv0 = wall[4 * (size_t)id + 0];
+        nv1 = wall[4 * (size_t)id + 1];
+        nv2 = wall[4 * (size_t)id + 2];
+    }
+#pragma unroll
+    for (int v = 0; v < Q; ++v) {
+        const int cx = L::c(v, 0), cy = L::c(v, 1), cz = L::c(v, 2);
+        int sx = i - cx, sy = j - cy, sz = k - cz;
+        sx = sx < 0 ? sx + N : (sx >= N ? sx - N : sx);
+        sy = sy < 0 ? sy + M : (sy >= M ? sy - M : sy);
+        if (D == 3) sz = sz < 0 ? sz + K : (sz >= K ? sz - K : sz);
+        else sz = 0;
+        const int sid = sz + sy * K + sx * K * M;
+        const int stype = a.typ[sid];
+        if (type == LUMA_SITE_BFL || stype == LUMA_SITE_BFL) {
+            g_unsupported = 1;
+            fn[v] = R(0);
+            continue;
+        }
+        if (type == LUMA_SITE_SLIP) {
+            // _LBM_applySpecReflect_opt (:527-581): first matching wall wins.
+            int plane = -1;
+            if (nv0 == 1 && cx == 1) plane = 0;
+            else if (nv0 == -1 && cx == -1) plane = 0;
+            else if (nv1 == 1 && cy == 1) plane = 1;
+            else if (nv1 == -1 && cy == -1) plane = 1;
+            else if (nv2 == 1 && cz == 1) plane = 2;
+            else if (nv2 == -1 && cz == -1) plane = 2;
+            if (plane >= 0) {
+                int rv = plane == 0 ? L::reflect(0, v) : (plane == 1 ? L::reflect(1, v) : L::reflect(2, v));
+                fn[v] = ld<P>(a.f, (size_t)rv * n + id);
+                slip_plane_mask |= 1;
+                continue;
+            }
+        }
+        if (stype == LUMA_SITE_SOLID) {
+            fn[v] = ld<P>(a.f, (size_t)L::opp(v) * n + id);
+        } else if (stype == LUMA_SITE_EXTRAPOLATE_RIGHT) {
+            fn[v] = ld<P>(a.f, (size_t)v * n + (sid - 2 * (K * M)));
+        } else if (stype == LUMA_SITE_VELOCITY && !(a.flags & LUMA_FLAG_REGULARISED)) {
+            const R rs = ldr<P>(a.rho, sid);
+            R ux, uy, uz = R(0);
+            if (a.has_ramp) {
+                ux = R(a.ux_in[j] * a.ramp_stream);
+                uy = R(a.uy_in[j] * a.ramp_stream);
+                if (D == 3) uz = R(a.uz_in[j] * a.ramp_stream);
+            } else {
+                ux = ldr<P>(a.u, sid);
+                uy = ldr<P>(a.u, n + sid);
+                if (D == 3) uz = ldr<P>(a.u, 2 * n + sid);
+            }
+            fn[v] = feq_s<Q, P>(v, rs, rs - R(a.rho0), ux, uy, uz, R(a.cs2));
+        } else if (a.parent_f && stype == LUMA_SITE_TL_TO_COARSER && a.subcycle == 0) {
+            // _LBM_explode_opt (:646-663) with GridUtils::getCoarseIndices.
+            int fx = sx, fy = sy, fz = sz;
+            if (fx % 2 != 0) fx -= 1;
+            if (fy % 2 != 0) fy -= 1;
+            if (fz % 2 != 0) fz -= 1;
+            const int pi = fx / 2 + a.lims[0];
+            const int pj = fy / 2 + a.lims[2];
+            const int pk = D == 3 ? fz / 2 + a.lims[4] : 0;
+            const size_t pn = (size_t)a.pN * a.pM * a.pK;
+            fn[v] = ld<P>(a.parent_f, (size_t)v * pn + pk + (size_t)pj * a.pK + (size_t)pi * a.pK * a.pM);
+        } else if (a.nchild && stype == LUMA_SITE_REFINED && type == LUMA_SITE_TL_TO_FINER) {
+            // _LBM_coalesce_opt (:591-636) with GridUtils::getFineIndices.
+            const int s = child_at<Q>(a, i, j, k);
+            if (s < 0) {
+                g_unsupported = 2;
+                fn[v] = R(0);
+                continue;
+            }
+            const ChildView &cg = a.child[s];
+            const int ci = 2 * (i - cg.lims[0] + 1) - 2;
+            const int cj = 2 * (j - cg.lims[2] + 1) - 2;
+            const int ck = D == 3 ? 2 * (k - cg.lims[4] + 1) - 2 : 0;
+            const size_t cn = (size_t)cg.N * cg.M * cg.K;
+            R acc = R(0);
+#pragma unroll
+            for (int ii = 0; ii < 2; ++ii)
+#pragma unroll
+                for (int jj = 0; jj < 2; ++jj)
+#pragma unroll
+                    for (int kk = 0; kk < (D == 3 ? 2 : 1); ++kk)
+                        acc += ld<P>(cg.f, (size_t)v * cn + (ck + kk) + (size_t)(cj + jj) * cg.K +
+                                               (size_t)(ci + ii) * cg.K * cg.M);
+            fn[v] = acc / (D == 3 ? R(8) : R(4));
+        } else {
+            fn[v] = ld<P>(a.f, (size_t)v * n + sid);
+        }
+    }
+    (void)slip_plane_mask;
+}
+
+// _LBM_macro_opt (:800-891): density and velocity of fluid-like sites from
+// the streamed populations, + 0.5*F when forcing; the 3D reference adds the
+// z half-force to x (:833) unless LUMA_FLAG_FIX_MACRO3D.
+template <int Q, class P>
+__device__ __forceinline__ void macro_site(const StepArgs &a, int i, int j, int k, int id, int type,
+                                           const typename P::R *fn, typename P::R &rho, typename P::R &drho,
+                                           typename P::R &ux, typename P::R &uy, typename P::R &uz) {
+    using L = Lattice<Q>;
+    using R = typename P::R;
+    constexpr int D = L::D;
+    const size_t n = (size_t)a.ncell;
+    if (type == LUMA_SITE_FLUID || type == LUMA_SITE_BFL || type == LUMA_SITE_TL_TO_FINER ||
+        type == LUMA_SITE_SLIP) {
+        R r = R(0), mx = R(0), my = R(0), mz = R(0);
+#pragma unroll
+        for (int v = 0; v < Q; ++v) {
+            r += fn[v];
+            mx += R(L::c(v, 0)) * fn[v];
+            my += R(L::c(v, 1)) * fn[v];
+            if (D == 3) mz += R(L::c(v, 2)) * fn[v];
+        }
+        if (a.forcing) {
+            const R Fx = ldr<P>(a.force, id), Fy = ldr<P>(a.force, n + id);
+            mx += R(0.5) * Fx;
+            my += R(0.5) * Fy;
+            if (D == 3) {
+                const R Fz = ldr<P>(a.force, 2 * n + id);
+                if (a.flags & LUMA_FLAG_FIX_MACRO3D) mz += R(0.5) * Fz;
+                else mx += R(0.5) * Fz;
+            }
+        }
+        if (P::shifted) {
+            drho = r;
+            rho = R(a.rho0) + r;
+        } else {
+            rho = r;
+            drho = r - R(a.rho0);
+        }
+        ux = mx / rho;
+        uy = my / rho;
+        uz = D == 3 ? mz / rho : R(0);
+        str<P>(a.u, id, ux);
+        str<P>(a.u, n + id, uy);
+        if (D == 3) str<P>(a.u, 2 * n + id, uz);
+        str<P>(a.rho, id, rho);
+    } else {
+        rho = ldr<P>(a.rho, id);
+        drho = rho - R(a.rho0);
+        ux = ldr<P>(a.u, id);
+        uy = ldr<P>(a.u, n + id);
+        uz = D == 3 ? ldr<P>(a.u, 2 * n + id) : R(0);
+    }
+    if (type == LUMA_SITE_TL_TO_FINER) {
+        const int s = child_at<Q>(a, i, j, k);
+        if (s < 0) return;
+        const ChildView &cg = a.child[s];
+        const int ci = 2 * (i - cg.lims[0] + 1) - 2;
+        const int cj = 2 * (j - cg.lims[2] + 1) - 2;
+        const int ck = D == 3 ? 2 * (k - cg.lims[4] + 1) - 2 : 0;
+        const size_t cn = (size_t)cg.N * cg.M * cg.K;
+        for (int ii = 0; ii < 2; ++ii)
+            for (int jj = 0; jj < 2; ++jj)
+                for (int kk = 0; kk < (D == 3 ? 2 : 1); ++kk) {
+                    const size_t cid = (size_t)(ck + kk) + (size_t)(cj + jj) * cg.K + (size_t)(ci + ii) * cg.K * cg.M;
+                    str<P>(cg.u, cid, ux);
+                    str<P>(cg.u, cn + cid, uy);
+                    if (D == 3) str<P>(cg.u, 2 * cn + cid, uz);
+                    str<P>(cg.rho, cid, rho);
+                }
+    }
+}
+
+// _LBM_smag (:717-756): Smagorinsky-modified relaxation frequency.
+template <int Q, class P>
+__device__ __forceinline__ typename P::R smag_omega(const StepArgs &a, const typename P::R *fn, typename P::R rho,
+                                                    typename P::R drho, typename P::R ux, typename P::R uy,
+                                                    typename P::R uz) {
+    using L = Lattice<Q>;
+    using R = typename P::R;
+    constexpr int D = L::D;
+    R S00 = 0, S01 = 0, S02 = 0, S11 = 0, S12 = 0, S22 = 0;
+#pragma unroll
+    for (int v = 0; v < Q; ++v) {
+        const R fneq = fn[v] - feq_s<Q, P>(v, rho, drho, ux, uy, uz, R(a.cs2));
+        S00 += R(L::c(v, 0) * L::c(v, 0)) * fneq;
+        S01 += R(L::c(v, 0) * L::c(v, 1)) * fneq;
+        S11 += R(L::c(v, 1) * L::c(v, 1)) * fneq;
+        if (D == 3) {
+            S02 += R(L::c(v, 0) * L::c(v, 2)) * fneq;
+            S12 += R(L::c(v, 1) * L::c(v, 2)) * fneq;
+            S22 += R(L::c(v, 2) * L::c(v, 2)) * fneq;
+        }
+    }
+    const R r0 = S00 * S00 + S01 * S01 + S02 * S02;
+    const R r1 = S01 * S01 + S11 * S11 + S12 * S12;
+    const R r2 = S02 * S02 + S12 * S12 + S22 * S22;
+    const R Qs = sqrt(R(2) * (r0 + r1 + r2));
+    const R tau = R(1) / R(a.omega);
+    const R cs2 = R(a.cs2);
+    const R tau_t = R(0.5) * (sqrt(tau * tau + R(2) * R(1.4142135623730950488016887242097) * R(a.csmag * a.csmag) *
+                                                   R(a.rho0) * cs2 * cs2 * Qs) - tau);
+    return R(1) / (tau + tau_t);
+}
+
+// Collision of one site in place on fn (BGK / BGK-Smagorinsky / KBC), with
+// the Guo term when forcing.  `fpre` is the pre-stream f of the site, read by
+// the reference's KBC (:1147, :1296).
+template <int Q, class P>
+__device__ __forceinline__ void collide_site(const StepArgs &a, int id, typename P::R *fn, typename P::R rho,
+                                             typename P::R drho, typename P::R ux, typename P::R uy,
+                                             typename P::R uz) {
+    using L = Lattice<Q>;
+    using R = typename P::R;
+    constexpr int D = L::D;
+    const size_t n = (size_t)a.ncell;
+    const R cs2 = R(a.cs2);
+    R Fx = R(0), Fy = R(0), Fz = R(0);
+    if (a.forcing) {
+        Fx = ldr<P>(a.force, id);
+        Fy = ldr<P>(a.force, n + id);
+        if (D == 3) Fz = ldr<P>(a.force, 2 * n + id);
+    }
+    if (a.collision != LUMA_COLL_KBC) {
+        const R om = a.collision == LUMA_COLL_BGK_SMAG ? smag_omega<Q, P>(a, fn, rho, drho, ux, uy, uz) : R(a.omega);
+#pragma unroll
+        for (int v = 0; v < Q; ++v) {
+            const R eq = feq_s<Q, P>(v, rho, drho, ux, uy, uz, cs2);
+            if (a.forcing) fn[v] = fn[v] + (om * (eq - fn[v]) + guo<Q, R>(v, R(a.omega), cs2, ux, uy, uz, Fx, Fy, Fz));
+            else fn[v] = fn[v] + om * (eq - fn[v]);
+        }
+        return;
+    }
+    // KBC-N4 (3D) / KBC-D (2D), _LBM_kbcCollide_opt (:1122-1305).
+    const bool fixed = (a.flags & LUMA_FLAG_FIX_KBC) != 0;
+    R src[Q], fe[Q], fneq[Q];
+    R M[13];
+#pragma unroll
+    for (int m = 0; m < 13; ++m) M[m] = R(0);
+#pragma unroll
+    for (int v = 0; v < Q; ++v) {
+        src[v] = fixed ? fn[v] : ld<P>(a.f, (size_t)v * n + id);
+        fe[v] = feq_s<Q, P>(v, rho, drho, ux, uy, uz, cs2);
+        fneq[v] = src[v] - fe[v];
+        const int cx = L::c(v, 0), cy = L::c(v, 1), cz = L::c(v, 2);
+        if (D == 3) {
+            // moment order: xx, xxy, xxz, xy, xyy, xyz, xz, xzz, yy, yyz, yz, yzz, zz
+            M[0] += fneq[v] * R(cx * cx);
+            M[1] += fneq[v] * R(cx * cx * cy);
+            M[2] += fneq[v] * R(cx * cx * cz);
+            M[3] += fneq[v] * R(cx * cy);
+            M[4] += fneq[v] * R(cx * cy * cy);
+            M[5] += fneq[v] * R(cx * cy * cz);
+            M[6] += fneq[v] * R(cx * cz);
+            M[7] += fneq[v] * R(cx * cz * cz);
+            M[8] += fneq[v] * R(cy * cy);
+            M[9] += fneq[v] * R(cy * cy * cz);
+            M[10] += fneq[v] * R(cy * cz);
+            M[11] += fneq[v] * R(cy * cz * cz);
+            M[12] += fneq[v] * R(cz * cz);
+        } else {
+            M[0] += fneq[v] * R(cx * cx);
+            M[1] += fneq[v] * R(cx * cy);
+            M[2] += fneq[v] * R(cy * cy);
+        }
+    }
+    R ds[Q];
+    R top = R(0), bot = R(0);
+#pragma unroll
+    for (int v = 0; v < Q; ++v) {
+        const int cx = L::c(v, 0), cy = L::c(v, 1), cz = L::c(v, 2);
+        R s;
+        if (D == 3) {
+            if (cx == 0) {
+                if (cy == 0) {
+                    if (cz == 0) s = (-(M[0] + M[8] + M[12]));
+                    else
+                        s = ((-(M[0] - M[12]) - (M[8] - M[12])) / R(6) + (M[0] + M[8] + M[12]) / R(6) -
+                             R(cz) * R(0.5) * (M[2] + M[9]));
+                } else {
+                    if (cz == 0)
+                        s = ((-(M[0] - M[12]) + R(2) * (M[8] - M[12])) / R(6) + (M[0] + M[8] + M[12]) / R(6) -
+                             R(cy) * R(0.5) * (M[1] + M[11]));
+                    else
+                        s = (R(cy * cz) * R(0.25) * M[10] + (R(cz) * R(0.25) * M[9] + R(cy) * R(0.25) * M[11]));
+                }
+            } else {
+                if (cy == 0) {
+                    if (cz == 0)
+                        s = ((R(2) * (M[0] - M[12]) - (M[8] - M[12])) / R(6) + (M[0] + M[8] + M[12]) / R(6) -
+                             R(cx) * R(0.5) * (M[4] + M[7]));
+                    else
+                        s = (R(cx * cz) * R(0.25) * M[6] + (R(cz) * R(0.25) * M[2] + R(cx) * R(0.25) * M[7]));
+                } else {
+                    if (cz == 0)
+                        s = (R(cx * cy) * R(0.25) * M[3] + (R(cy) * R(0.25) * M[1] + R(cx) * R(0.25) * M[4]));
+                    else
+                        s = (R(cx * cy * cz) * M[5] / R(8));
+                }
+            }
+        } else {
+            if (cx == 0) s = cy == 0 ? R(0) : R(-0.25) * (M[0] - M[2]);
+            else s = cy == 0 ? R(0.25) * (M[0] - M[2]) : R(0.25) * R(cx * cy) * M[1];
+        }
+        ds[v] = s;
+        const R dh = fneq[v] - s;
+        const R feq_true = P::shifted ? fe[v] + R(L::w(v)) * R(a.rho0) : fe[v];
+        top += s * dh / feq_true;
+        bot += dh * dh / feq_true;
+    }
+    const R beta_m1 = R(2) / R(a.omega);
+    const R gamma = bot == R(0) ? R(2) : beta_m1 - (R(2) - beta_m1) * (top / bot);
+    const R inv_b = R(1) / beta_m1;
+#pragma unroll
+    for (int v = 0; v < Q; ++v) {
+        const R dh = fneq[v] - ds[v];
+        const R base = src[v] - inv_b * (R(2) * ds[v] + gamma * dh);
+        fn[v] = a.forcing ? base + guo<Q, R>(v, R(a.omega), cs2, ux, uy, uz, Fx, Fy, Fz) : base;
+    }
+}
+
+template <int Q, class P>
+__global__ void __launch_bounds__(128) k_stream_macro(StepArgs a, const int8_t *wall) {
+    using R = typename P::R;
+    const int id = blockIdx.x * blockDim.x + threadIdx.x;
+    if (id >= a.ncell) return;
+    const int type = a.typ[id];
+    const bool reg = (a.flags & LUMA_FLAG_REGULARISED) != 0;
+    if (type == LUMA_SITE_REFINED || type == LUMA_SITE_SOLID || type == LUMA_SITE_VELOCITY ||
+        (reg && type == LUMA_SITE_PRESSURE))
+        return;  // velocity/pressure sites of regularised grids are phase B
+    const int k = id % a.K;
+    const int j = (id / a.K) % a.M;
+    const int i = id / (a.K * a.M);
+    R fn[Q];
+    stream_site<Q, P>(a, wall, i, j, k, id, type, fn);
+    R rho, drho, ux, uy, uz;
+    macro_site<Q, P>(a, i, j, k, id, type, fn, rho, drho, ux, uy, uz);
+    const size_t n = (size_t)a.ncell;
+    if (!a.ibm_split && type != LUMA_SITE_TL_TO_COARSER) collide_site<Q, P>(a, id, fn, rho, drho, ux, uy, uz);
+#pragma unroll
+    for (int v = 0; v < Q; ++v) st<P>(a.fNew, (size_t)v * n + id, fn[v]);
+}
+
+// _LBM_regularised_opt (:313-510) for one velocity/pressure site of a
+// regularised grid, preceded by its stream and followed (single-loop
+// reference) by its collision.  Interior macroscopic values used for
+// extrapolation come from phase A.
+template <int Q, class P>
+__global__ void __launch_bounds__(128) k_regularised(StepArgs a, const int8_t *wall, const RegSite *sites, int nsites) {
+    using L = Lattice<Q>;
+    using R = typename P::R;
+    constexpr int D = L::D;
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= nsites) return;
+    const RegSite rs = sites[s];
+    const int id = rs.id, i = rs.i, j = rs.j, k = rs.k;
+    const int type = a.typ[id];
+    const size_t n = (size_t)a.ncell;
+    const R cs2 = R(a.cs2);
+    R fn[Q];
+    stream_site<Q, P>(a, wall, i, j, k, id, type, fn);
+    R vel[3] = {R(a.ux_in[j] * a.ramp_reg), R(a.uy_in[j] * a.ramp_reg), R(a.uz_in[j] * a.ramp_reg)};
+    const int nd = rs.ndir;
+    const int nv[3] = {rs.nvec[0], rs.nvec[1], rs.nvec[2]};
+    R dens = R(a.rho0) + R(a.pdelta);
+    R drho;
+    if (rs.edges > 1) {
+        // First-order extrapolation of rho along the inward normal.
+        const int i1 = i + nv[0], j1 = j + nv[1], k1 = k + nv[2];
+        const int i2 = i1 + nv[0], j2 = j1 + nv[1], k2 = k1 + nv[2];
+        const int id1 = k1 + j1 * a.K + i1 * a.K * a.M;
+        const int id2 = k2 + j2 * a.K + i2 * a.K * a.M;
+        dens = R(2) * ldr<P>(a.rho, id1) - ldr<P>(a.rho, id2);
+        drho = dens - R(a.rho0);
+    } else {
+        R fp = R(0), f0 = R(0);
+        R wp = R(0), w0 = R(0);
+#pragma unroll
+        for (int v = 0; v < Q; ++v) {
+            const int cn = nd == 0 ? L::c(v, 0) : (nd == 1 ? L::c(v, 1) : L::c(v, 2));
+            if (cn == -nv[nd]) { fp += fn[v]; wp += R(L::w(v)); }
+            else if (cn == 0) { f0 += fn[v]; w0 += R(L::w(v)); }
+        }
+        if (P::shifted) {  // true sums from shifted ones
+            fp += wp * R(a.rho0);
+            f0 += w0 * R(a.rho0);
+        }
+        if (type == LUMA_SITE_PRESSURE) {
+            for (int d = 0; d < D; d++)
+                if (d != nd) {
+                    const int i1 = i + nv[0], j1 = j + nv[1], k1 = k + nv[2];
+                    const int i2 = i1 + nv[0], j2 = j1 + nv[1], k2 = k1 + nv[2];
+                    const int id1 = k1 + j1 * a.K + i1 * a.K * a.M;
+                    const int id2 = k2 + j2 * a.K + i2 * a.K * a.M;
+                    vel[d] = R(2) * ldr<P>(a.u, (size_t)d * n + id1) - ldr<P>(a.u, (size_t)d * n + id2);
+                }
+            vel[nd] = R(1) - ((R(1) / dens) * (R(2) * fp + f0));
+            if (nv[nd] == -1) vel[nd] *= R(-1);
+        } else {
+            R nvel = vel[nd];
+            if (nv[nd] == -1) nvel *= R(-1);
+            dens = (R(1) / (R(1) - nvel)) * (R(2) * fp + f0);
+        }
+        drho = dens - R(a.rho0);
+    }
+    const R ux = vel[0], uy = vel[1], uz = D == 3 ? vel[2] : R(0);
+    str<P>(a.rho, id, dens);
+    str<P>(a.u, id, ux);
+    str<P>(a.u, n + id, uy);
+    if (D == 3) str<P>(a.u, 2 * n + id, uz);
+    R Sxx = 0, Syy = 0, Sxy = 0, Szz = 0, Sxz = 0, Syz = 0;
+#pragma unroll
+    for (int v = 0; v < Q; ++v) {
+        const int c0 = L::c(v, 0), c1 = L::c(v, 1), c2 = L::c(v, 2);
+        const int cn = nd == 0 ? c0 : (nd == 1 ? c1 : c2);
+        const R eqv = feq_s<Q, P>(v, dens, drho, ux, uy, uz, cs2);
+        if (rs.edges == 1 && cn == nv[nd]) {
+            fn[v] = eqv + (fn[L::opp(v)] - feq_s<Q, P>(L::opp(v), dens, drho, ux, uy, uz, cs2));
+        } else if (rs.edges > 1 && (c0 == nv[0] || c1 == nv[1] || (D == 3 && c2 == nv[2]))) {
+            const int dp = c0 * nv[0] + c1 * nv[1] + (D == 3 ? c2 * nv[2] : 0);
+            const int mag2 = c0 * c0 + c1 * c1 + (D == 3 ? c2 * c2 : 0);
+            if (dp == 0 && mag2 > 1) fn[v] = eqv;
+            else fn[v] = eqv + (fn[L::opp(v)] - feq_s<Q, P>(L::opp(v), dens, drho, ux, uy, uz, cs2));
+        }
+        const R fneq = fn[v] - eqv;
+        Sxx += R(c0 * c0) * fneq;
+        Syy += R(c1 * c1) * fneq;
+        Sxy += R(c0 * c1) * fneq;
+        if (D == 3) {
+            Szz += R(c2 * c2) * fneq;
+            Sxz += R(c0 * c2) * fneq;
+            Syz += R(c1 * c2) * fneq;
+        }
+    }
+#pragma unroll
+    for (int v = 0; v < Q; v++) {
+        const int c0 = L::c(v, 0), c1 = L::c(v, 1), c2 = L::c(v, 2);
+        fn[v] = feq_s<Q, P>(v, dens, drho, ux, uy, uz, cs2) +
+                (R(L::w(v)) / (R(2) * cs2 * cs2)) *
+                    (((R(c0 * c0) - cs2) * Sxx) + ((R(c1 * c1) - cs2) * Syy) + ((R(c2 * c2) - cs2) * Szz) +
+                     (R(2 * c0 * c1) * Sxy) + (R(2 * c0 * c2) * Sxz) + (R(2 * c1 * c2) * Syz));
+    }
+    if (!a.ibm_split) collide_site<Q, P>(a, id, fn, dens, drho, ux, uy, uz);
+#pragma unroll
+    for (int v = 0; v < Q; ++v) st<P>(a.fNew, (size_t)v * n + id, fn[v]);
+}
+
+// The velocity that the forced-equilibrium BC leaves in a velocity site's u
+// under a velocity ramp: the inlet value of the row of the last site (in the
+// reference's loop order) that pulled from it (:258-265).
+template <class P>
+__global__ void k_velocity_u(StepArgs a, int dims, const int2 *sites, int nsites) {
+    using R = typename P::R;
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= nsites) return;
+    const int2 e = sites[s];  // (site id, row of its last writer)
+    const size_t n = (size_t)a.ncell;
+    str<P>(a.u, e.x, R(a.ux_in[e.y] * a.ramp_stream));
+    str<P>(a.u, n + e.x, R(a.uy_in[e.y] * a.ramp_stream));
+    if (dims == 3) str<P>(a.u, 2 * n + e.x, R(a.uz_in[e.y] * a.ramp_stream));
+}
+
+// Second loop of the reference under L_IBM_ON (:125-156): forcing at every
+// non-solid site and collision at every site but transition-to-coarser,
+// using the macroscopic values after the IBM pass.
+template <int Q, class P>
+__global__ void __launch_bounds__(128) k_force_collide(StepArgs a) {
+    using R = typename P::R;
+    constexpr int D = Lattice<Q>::D;
+    const int id = blockIdx.x * blockDim.x + threadIdx.x;
+    if (id >= a.ncell) return;
+    const int type = a.typ[id];
+    if (type == LUMA_SITE_TL_TO_COARSER) return;
+    const size_t n = (size_t)a.ncell;
+    R fn[Q];
+#pragma unroll
+    for (int v = 0; v < Q; ++v) fn[v] = ld<P>(a.fNew, (size_t)v * n + id);
+    const R rho = ldr<P>(a.rho, id);
+    const R ux = ldr<P>(a.u, id), uy = ldr<P>(a.u, n + id);
+    const R uz = D == 3 ? ldr<P>(a.u, 2 * n + id) : R(0);
+    StepArgs b = a;
+    if (type == LUMA_SITE_SOLID) b.forcing = 0;  // solid sites are collided without the Guo term
+    collide_site<Q, P>(b, id, fn, rho, rho - R(a.rho0), ux, uy, uz);
+#pragma unroll
+    for (int v = 0; v < Q; ++v) st<P>(a.fNew, (size_t)v * n + id, fn[v]);
+}
+
+}  // namespace
+
+template <int Q, class P>
+cudaError_t launch_general_phaseA(const StepArgs &a, const int8_t *wall, cudaStream_t s) {
+    const int bs = 128;
+    k_stream_macro<Q, P><<<(a.ncell + bs - 1) / bs, bs, 0, s>>>(a, wall);
+    return cudaGetLastError();
+}
+template <int Q, class P>
+cudaError_t launch_general_phaseB(const StepArgs &a, const int8_t *wall, const RegSite *sites, int nsites,
+                                  cudaStream_t s) {
+    if (nsites <= 0) return cudaSuccess;
+    const int bs = 128;
+    k_regularised<Q, P><<<(nsites + bs - 1) / bs, bs, 0, s>>>(a, wall, sites, nsites);
+    return cudaGetLastError();
+}
+template <class P>
+cudaError_t launch_velocity_u(const StepArgs &a, int dims, const int2 *sites, int nsites, cudaStream_t s) {
+    if (nsites <= 0) return cudaSuccess;
+    k_velocity_u<P><<<(nsites + 127) / 128, 128, 0, s>>>(a, dims, sites, nsites);
+    return cudaGetLastError();
+}
+template <int Q, class P>
+cudaError_t launch_general_phaseC(const StepArgs &a, cudaStream_t s) {
+    const int bs = 128;
+    k_force_collide<Q, P><<<(a.ncell + bs - 1) / bs, bs, 0, s>>>(a);
+    return cudaGetLastError();
+}
+
+int read_unsupported_flag(cudaStream_t s) {
+    int h = 0;
+    cudaMemcpyFromSymbolAsync(&h, g_unsupported, sizeof(int), 0, cudaMemcpyDeviceToHost, s);
+    cudaStreamSynchronize(s);
+    return h;
+}
+
+#define LUMA_INST(Q, P)                                                                                        \
+    template cudaError_t launch_general_phaseA<Q, P>(const StepArgs &, const int8_t *, cudaStream_t);         \
+    template cudaError_t launch_general_phaseB<Q, P>(const StepArgs &, const int8_t *, const RegSite *, int,   \
+                                                     cudaStream_t);                                            \
+    template cudaError_t launch_general_phaseC<Q, P>(const StepArgs &, cudaStream_t);
+LUMA_INST(9, P64)
+LUMA_INST(19, P64)
+LUMA_INST(27, P64)
+LUMA_INST(9, P32)
+LUMA_INST(19, P32)
+LUMA_INST(27, P32)
+template cudaError_t launch_velocity_u<P64>(const StepArgs &, int, const int2 *, int, cudaStream_t);
+template cudaError_t launch_velocity_u<P32>(const StepArgs &, int, const int2 *, int, cudaStream_t);
+
+}  // namespace luma

@@ -1,0 +1,44 @@
+// Launch entry points of the device kernels (host-callable, stream-ordered).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "device.cuh"
+
+namespace luma {
+
+// k_general.cu
+template <int Q, class P>
+cudaError_t launch_general_phaseA(const StepArgs &a, const int8_t *wall, cudaStream_t s);
+template <int Q, class P>
+cudaError_t launch_general_phaseB(const StepArgs &a, const int8_t *wall, const RegSite *sites, int nsites,
+                                  cudaStream_t s);
+template <class P>
+cudaError_t launch_velocity_u(const StepArgs &a, int dims, const int2 *sites, int nsites, cudaStream_t s);
+template <int Q, class P>
+cudaError_t launch_general_phaseC(const StepArgs &a, cudaStream_t s);
+int read_unsupported_flag(cudaStream_t s);
+
+// k_bulk.cu
+template <int Q, class P>
+cudaError_t launch_aa(void *A, void *u, void *rho, int N, int M, int K, double omega, double rho0, bool from_e,
+                      bool write_macro, cudaStream_t s);
+
+// k_transfer.cu
+enum PopLayout { kPopPlain = 0, kPopAAE = 1, kPopAAO = 2 };
+template <int Q, class P>
+cudaError_t launch_pop_in(const double *aos, void *soa, int N, int M, int K, int layout, double rho0,
+                          cudaStream_t s);
+template <int Q, class P>
+cudaError_t launch_pop_out(const void *soa, double *aos, int N, int M, int K, int layout, double rho0,
+                           cudaStream_t s);
+template <class P>
+cudaError_t launch_vec_in(const double *aos, void *soa, size_t n, int dims, cudaStream_t s);
+template <class P>
+cudaError_t launch_vec_out(const void *soa, double *aos, size_t n, int dims, cudaStream_t s);
+template <class P>
+cudaError_t launch_reduce(const uint8_t *typ, const void *rho, const void *u, size_t n, int dims,
+                          double *acc /* device: mass, mx, my, mz, ke, maxspeed(bits), nonfinite */,
+                          cudaStream_t s);
+
+}  // namespace luma

@@ -1,0 +1,128 @@
+"""ctypes binding of the GB300 C ABI (``include/luma_gpu.h``).
+
+``GpuGrid`` mirrors one GridObj of the reference's hierarchy on the device:
+create from a ``luma_grid_desc``, upload/download state in the reference's
+host layout, and ``step`` = ``GridObj::LBM_multi_opt`` (LUMA
+src/GridObj_ops_lbm_optimised.cpp:36-193) on the level-0 grid.
+
+There is no CPU fallback: if the CUDA library is missing or no GPU is
+present, construction raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import _abi as A
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "libluma_gpu.so")
+
+_lib = None
+
+
+class LumaError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"luma_gpu error {code}: {msg}")
+        self.code = code
+
+
+def lib() -> C.CDLL:
+    """Load the in-tree CUDA library (build it with ``luma_gb300.build``)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise RuntimeError(f"luma_gb300 CUDA library not built: {LIB_PATH} missing "
+                               "(run __graft_entry__.build() or python -m luma_gb300.build)")
+        L = C.CDLL(LIB_PATH)
+        vp = C.c_void_p
+        dp = C.POINTER(C.c_double)
+        L.luma_gpu_abi_version.restype = C.c_int
+        L.luma_gpu_last_error_string.restype = C.c_char_p
+        L.luma_gpu_grid_create.argtypes = [C.POINTER(A.GridDesc), vp, C.POINTER(vp)]
+        L.luma_gpu_grid_destroy.argtypes = [vp]
+        L.luma_gpu_set_stream.argtypes = [vp, vp]
+        L.luma_gpu_upload_state.argtypes = [vp, dp, dp, dp, dp, C.c_int]
+        L.luma_gpu_download_state.argtypes = [vp, dp, dp, dp, dp]
+        L.luma_gpu_get_time.argtypes = [vp, C.POINTER(C.c_int)]
+        L.luma_gpu_step.argtypes = [vp, C.c_int]
+        L.luma_gpu_synchronize.argtypes = [vp]
+        L.luma_gpu_reduce.argtypes = [vp, C.POINTER(A.Reduction)]
+        if L.luma_gpu_abi_version() != A.ABI_VERSION:
+            raise RuntimeError("luma_gb300 library ABI version mismatch")
+        _lib = L
+    return _lib
+
+
+def check(rc: int) -> None:
+    if rc != A.LUMA_OK:
+        raise LumaError(rc, lib().luma_gpu_last_error_string().decode(errors="replace"))
+
+
+class GpuGrid:
+    """One grid of the device hierarchy.  Sub-grids are created with
+    ``parent=``; only the level-0 grid is stepped, and destroying it frees
+    the whole tree."""
+
+    def __init__(self, desc: "A.GridDesc", parent: "GpuGrid | None" = None):
+        self.L = lib()
+        self.desc = desc
+        h = C.c_void_p()
+        check(self.L.luma_gpu_grid_create(C.byref(desc), parent.h if parent else None, C.byref(h)))
+        self.h = h.value
+        self.n = desc.N * desc.M * desc.K
+        self.parent = parent
+        self.children: list[GpuGrid] = []
+        if parent is not None:
+            parent.children.append(self)
+
+    def close(self):
+        if self.h and self.parent is None:
+            self.L.luma_gpu_grid_destroy(self.h)
+        self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_stream(self, stream_ptr: int | None):
+        check(self.L.luma_gpu_set_stream(self.h, stream_ptr))
+
+    def upload(self, f=None, u=None, rho=None, force=None, t: int = 0):
+        arrs = [None if a is None else np.ascontiguousarray(a, dtype=np.float64) for a in (f, u, rho, force)]
+        check(self.L.luma_gpu_upload_state(self.h, *[A.dptr(a) for a in arrs], t))
+
+    def download(self, f=True, u=True, rho=True, force=False) -> dict:
+        d = self.desc
+        out = {}
+        bufs = []
+        for name, want, size in (("f", f, self.n * d.Q), ("u", u, self.n * d.dims), ("rho", rho, self.n),
+                                 ("force", force, self.n * d.dims)):
+            arr = np.empty(size) if want else None
+            if want:
+                out[name] = arr
+            bufs.append(A.dptr(arr))
+        check(self.L.luma_gpu_download_state(self.h, *bufs))
+        return out
+
+    def step(self, nsteps: int = 1):
+        check(self.L.luma_gpu_step(self.h, nsteps))
+
+    def synchronize(self):
+        check(self.L.luma_gpu_synchronize(self.h))
+
+    @property
+    def t(self) -> int:
+        v = C.c_int()
+        check(self.L.luma_gpu_get_time(self.h, C.byref(v)))
+        return v.value
+
+    def reduce(self) -> dict:
+        r = A.Reduction()
+        check(self.L.luma_gpu_reduce(self.h, C.byref(r)))
+        return {"mass": r.mass, "momentum": tuple(r.momentum), "kinetic_energy": r.kinetic_energy,
+                "max_speed": r.max_speed, "nonfinite": r.nonfinite}

@@ -1,0 +1,106 @@
+"""CUDA path against the oracle and the reference's golden outputs.
+
+FP64: relative L2 of u and rho <= 1e-10 against the oracle (which is
+bit-exact with the reference), at every stored step of each oracle case.
+FP32 shifted: relative L2 of u <= 2e-4 (rho - 1 within 1e-6 absolute) on the
+same cases.  The KBC cases are compared over the early steps the reference
+stays finite on.
+"""
+import numpy as np
+import pytest
+
+from luma_gb300 import _abi as A
+from oracle import oracle as O
+from tests.golden import cases as CASES
+from tests.golden import runner as R
+
+pytestmark = pytest.mark.gpu
+
+
+def rel_l2(a, b):
+    den = np.linalg.norm(b)
+    return np.linalg.norm(a - b) / (den if den > 0 else 1.0)
+
+
+def gpu_grid(desc):
+    from luma_gb300.gpu import GpuGrid
+    return GpuGrid(desc)
+
+
+@pytest.mark.parametrize("name", sorted(CASES.CASES))
+def test_fp64_matches_oracle_and_reference(name):
+    spec = CASES.CASES[name]
+    fx = R.fixture(name)
+    l0 = R.level0(name)
+    desc = l0.desc(precision=A.PREC_FP64)
+    g = gpu_grid(desc)
+    o = O.OracleGrid(l0.desc())
+    init = R.initial_state(l0)
+    g.upload(*init, t=0)
+    o.upload(*init, t=0)
+    done = 0
+    for s in spec["steps"]:
+        g.step(s - done)
+        o.step(s - done)
+        done = s
+        g.synchronize()
+        gs, os_ = g.download(force=False), o.download()
+        assert g.t == s
+        eu = rel_l2(gs["u"], os_["u"])
+        er = rel_l2(gs["rho"], os_["rho"])
+        ef = rel_l2(gs["f"], os_["f"])
+        assert eu <= 1e-10 and er <= 1e-10 and ef <= 1e-10, (name, s, eu, er, ef)
+        # and the reference's own fields
+        assert rel_l2(gs["u"], fx[f"u_{s}"]) <= 1e-10
+        assert rel_l2(gs["rho"], fx[f"rho_{s}"]) <= 1e-10
+
+
+@pytest.mark.parametrize("name", sorted(CASES.CASES))
+def test_fp32_shifted_close_to_fp64(name):
+    spec = CASES.CASES[name]
+    l0 = R.level0(name)
+    g = gpu_grid(l0.desc(precision=A.PREC_FP32_SHIFTED))
+    o = O.OracleGrid(l0.desc())
+    init = R.initial_state(l0)
+    g.upload(*init, t=0)
+    o.upload(*init, t=0)
+    s = spec["steps"][0]
+    g.step(s)
+    o.step(s)
+    gs, os_ = g.download(), o.download()
+    eu = rel_l2(gs["u"], os_["u"])
+    dr = np.max(np.abs(gs["rho"] - os_["rho"]))
+    assert eu <= 2e-4, (name, s, eu)
+    assert dr <= 1e-6, (name, s, dr)
+
+
+def test_aa_odd_and_even_step_counts():
+    """The in-place path stores populations in two alternating layouts; f, u,
+    rho must come back identical to the oracle after odd and even counts."""
+    l0 = R.level0("tgv_d3q19")
+    g = gpu_grid(l0.desc())
+    o = O.OracleGrid(l0.desc())
+    init = R.initial_state(l0)
+    g.upload(*init, t=0)
+    o.upload(*init, t=0)
+    for n in (1, 2, 3, 5):
+        g.step(n)
+        o.step(n)
+        gs, os_ = g.download(), o.download()
+        assert rel_l2(gs["f"], os_["f"]) <= 1e-12
+        assert rel_l2(gs["u"], os_["u"]) <= 1e-12
+        assert rel_l2(gs["rho"], os_["rho"]) <= 1e-13
+
+
+def test_reduce_mass_momentum():
+    l0 = R.level0("tgv_d3q19")
+    g = gpu_grid(l0.desc())
+    g.upload(*R.initial_state(l0), t=0)
+    g.step(4)
+    st = g.download()
+    red = g.reduce()
+    assert red["nonfinite"] == 0
+    assert abs(red["mass"] - st["rho"].sum()) <= 1e-9 * l0.ncell
+    u = st["u"].reshape(-1, 3)
+    mom = (st["rho"][:, None] * u).sum(axis=0)
+    assert np.allclose(red["momentum"], mom, rtol=0, atol=1e-12 * l0.ncell)
