@@ -138,7 +138,7 @@ int luma_gpu_set_stream(luma_gpu_grid *root, void *cuda_stream);
 
 /* ---- state transfer ------------------------------------------------------ */
 /* Host -> device: f (N*M*K*Q), u (N*M*K*dims), rho (N*M*K); force_xyz may be
- * NULL.  Arrays in the reference layout (post-collision f, as GridObj::f
+ * NULL and is ignored on grids without IBM or gravity forcing.  Arrays in the reference layout (post-collision f, as GridObj::f
  * holds between time steps).  Sets the grid's step counter to t. */
 int luma_gpu_upload_state(luma_gpu_grid *grid, const double *f, const double *u,
                           const double *rho, const double *force_xyz, int t);

@@ -469,10 +469,9 @@ int luma_gpu_upload_state(luma_gpu_grid *g, const double *f, const double *u, co
         };
         if (u && (rc = vec_in(u, g->u, d.dims))) return rc;
         if (rho && (rc = vec_in(rho, g->rho, 1))) return rc;
-        if (force_xyz) {
-            if (!g->force) return luma_set_error(LUMA_E_STATE, "grid has no force field (no IBM/gravity flag)");
-            if ((rc = vec_in(force_xyz, g->force, d.dims))) return rc;
-        }
+        // force_xyz is ignored on grids without a force field (the reference
+        // allocates it only under L_IBM_ON or L_GRAVITY_ON).
+        if (force_xyz && g->force && (rc = vec_in(force_xyz, g->force, d.dims))) return rc;
         return LUMA_OK;
     };
     rc = run();

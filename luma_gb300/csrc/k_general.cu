@@ -427,11 +427,35 @@ __global__ void __launch_bounds__(128) k_regularised(StepArgs a, const int8_t *w
             if (cn == -nv[nd]) { fp += fn[v]; wp += R(L::w(v)); }
             else if (cn == 0) { f0 += fn[v]; w0 += R(L::w(v)); }
         }
-        if (P::shifted) {  // true sums from shifted ones
-            fp += wp * R(a.rho0);
-            f0 += w0 * R(a.rho0);
-        }
-        if (type == LUMA_SITE_PRESSURE) {
+        if (P::shifted) {
+            // On a face the weights satisfy 2*sum(w_plus) + sum(w_zero) = 1, so
+            // 2 f+ + f0 = rho0 + (2 g+ + g0): work with the small shifted sum X
+            // and the density offset directly, as the unshifted formulas would
+            // lose it to cancellation in FP32.
+            (void)wp;
+            (void)w0;
+            const R X = R(2) * fp + f0;
+            if (type == LUMA_SITE_PRESSURE) {
+                for (int d = 0; d < D; d++)
+                    if (d != nd) {
+                        const int i1 = i + nv[0], j1 = j + nv[1], k1 = k + nv[2];
+                        const int i2 = i1 + nv[0], j2 = j1 + nv[1], k2 = k1 + nv[2];
+                        const int id1 = k1 + j1 * a.K + i1 * a.K * a.M;
+                        const int id2 = k2 + j2 * a.K + i2 * a.K * a.M;
+                        vel[d] = R(2) * ldr<P>(a.u, (size_t)d * n + id1) - ldr<P>(a.u, (size_t)d * n + id2);
+                    }
+                drho = R(a.pdelta);
+                // u_n = 1 - (rho0 + X)/dens = (drho - X)/dens
+                vel[nd] = (drho - X) / dens;
+                if (nv[nd] == -1) vel[nd] *= R(-1);
+            } else {
+                R nvel = vel[nd];
+                if (nv[nd] == -1) nvel *= R(-1);
+                // dens = (rho0 + X)/(1 - un)  =>  dens - rho0 = (X + rho0*un)/(1 - un)
+                drho = (X + R(a.rho0) * nvel) / (R(1) - nvel);
+                dens = R(a.rho0) + drho;
+            }
+        } else if (type == LUMA_SITE_PRESSURE) {
             for (int d = 0; d < D; d++)
                 if (d != nd) {
                     const int i1 = i + nv[0], j1 = j + nv[1], k1 = k + nv[2];
@@ -447,7 +471,7 @@ __global__ void __launch_bounds__(128) k_regularised(StepArgs a, const int8_t *w
             if (nv[nd] == -1) nvel *= R(-1);
             dens = (R(1) / (R(1) - nvel)) * (R(2) * fp + f0);
         }
-        drho = dens - R(a.rho0);
+        if (!P::shifted) drho = dens - R(a.rho0);
     }
     const R ux = vel[0], uy = vel[1], uz = D == 3 ? vel[2] : R(0);
     str<P>(a.rho, id, dens);
