@@ -82,6 +82,8 @@ enum {
                                        to x, src/GridObj_ops_lbm_optimised.cpp:833) */
 #define LUMA_FLAG_FIX_KBC 0x10      /* KBC relaxes the streamed populations (the reference
                                        relaxes the pre-stream f, :1147,1296) */
+#define LUMA_FLAG_TWO_BUFFER 0x20   /* keep the two-buffer step even where the in-place
+                                       (AA-pattern) step applies */
 
 /* Description of one grid (one level/region of the hierarchy).  Mirrors the
  * GridObj members it is filled from; arrays are read during create only. */

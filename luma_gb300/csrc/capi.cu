@@ -219,7 +219,7 @@ bool bulk_eligible(const luma_gpu_grid *g, const int32_t *typ) {
     if (g->parent || !g->kids.empty()) return false;
     if (d.collision != LUMA_COLL_BGK) return false;
     if (d.N > 65535 || d.M > 65535) return false;  // grid.y / grid.z launch limits
-    if (d.flags & (LUMA_FLAG_IBM | LUMA_FLAG_GRAVITY | LUMA_FLAG_REGULARISED)) return false;
+    if (d.flags & (LUMA_FLAG_IBM | LUMA_FLAG_GRAVITY | LUMA_FLAG_REGULARISED | LUMA_FLAG_TWO_BUFFER)) return false;
     for (size_t i = 0; i < g->n; ++i)
         if (typ[i] != LUMA_SITE_FLUID) return false;
     return true;

@@ -120,29 +120,81 @@ __device__ __forceinline__ R eq_poly(int v, R ux, R uy, R uz, R cs2) {
     return (A / cs2) + (B / (R(2) * cs2 * cs2));
 }
 
-// Equilibrium in the stored representation: f_eq (P64) or g_eq = f_eq - w*rho0 (P32).
+// x * w_v for FP32 with the exact (FP64) lattice weight: w = hi + lo with hi
+// the nearest float, so fma(x, hi, x*lo) is x*w to within an ulp.  The
+// weights 1/18, 1/36, 1/3 ... are not floats; rounding them once biases every
+// equilibrium the same way each step (sum_v w_v != 1 and sum_v w_v c_v c_v !=
+// cs^2 I in FP32), which drifts mass and momentum.  With the split weight
+// only unbiased rounding of the product remains.
+template <int Q>
+__device__ __forceinline__ float wmul(int v, float x) {
+    const double w = Lattice<Q>::w(v);
+    const float hi = float(w);
+    const float lo = float(w - double(hi));
+    return fmaf(x, hi, x * lo);
+}
+
+// The FP32 equilibrium polynomial with the exact constants of cs^2 = 1/3:
+// 3 c.u + 4.5 (c.u)^2 - 1.5 u.u (the reference's A/cs^2 + B/(2 cs^4)).
+template <int Q>
+__device__ __forceinline__ float eq_poly32(int v, float ux, float uy, float uz) {
+    using L = Lattice<Q>;
+    float cu = 0.f;
+    if (L::c(v, 0)) cu += L::c(v, 0) > 0 ? ux : -ux;
+    if (L::c(v, 1)) cu += L::c(v, 1) > 0 ? uy : -uy;
+    if (L::D == 3 && L::c(v, 2)) cu += L::c(v, 2) > 0 ? uz : -uz;
+    const float usq = ux * ux + uy * uy + (L::D == 3 ? uz * uz : 0.f);
+    return 3.f * cu + 4.5f * cu * cu - 1.5f * usq;
+}
+
+// Equilibrium in the stored representation: f_eq (P64, the reference's
+// expression) or g_eq = f_eq - w*rho0 = w*(drho + rho*poly) (P32).
 template <int Q, class P>
 __device__ __forceinline__ typename P::R feq_s(int v, typename P::R rho, typename P::R drho, typename P::R ux,
                                                 typename P::R uy, typename P::R uz, typename P::R cs2) {
     using R = typename P::R;
-    const R w = R(Lattice<Q>::w(v));
-    if (P::shifted) return w * drho + w * rho * eq_poly<Q, R>(v, ux, uy, uz, cs2);
-    return rho * w * (R(1) + eq_poly<Q, R>(v, ux, uy, uz, cs2));
+    if constexpr (P::shifted) {
+        (void)cs2;
+        return wmul<Q>(v, drho + rho * eq_poly32<Q>(v, ux, uy, uz));
+    } else {
+        const R w = R(Lattice<Q>::w(v));
+        return rho * w * (R(1) + eq_poly<Q, R>(v, ux, uy, uz, cs2));
+    }
 }
 
-// Guo forcing term of direction v (_LBM_forceGrid_opt, :928-990).
+// w_v * X in the arithmetic of the policy (exact-weight product in FP32).
+template <int Q, class P>
+__device__ __forceinline__ typename P::R wtimes(int v, typename P::R x) {
+    if constexpr (P::shifted) return wmul<Q>(v, x);
+    else return typename P::R(Lattice<Q>::w(v)) * x;
+}
+
+// Guo forcing term of direction v (_LBM_forceGrid_opt, :928-990).  FP64
+// keeps the reference's expression; FP32 uses 1/cs^2 = 3 and the
+// exact-weight product.
 template <int Q, class R>
 __device__ __forceinline__ R guo(int v, R omega, R cs2, R ux, R uy, R uz, R Fx, R Fy, R Fz) {
     using L = Lattice<Q>;
-    const R lambda = (R(1) - R(0.5) * omega) * (R(L::w(v)) / cs2);
-    R beta = R(L::c(v, 0)) * ux + R(L::c(v, 1)) * uy;
-    if (L::D == 3) beta += R(L::c(v, 2)) * uz;
-    beta = beta * (R(1) / cs2);
-    R s = R(0);
-    s += Fx * (R(L::c(v, 0)) * (R(1) + beta) - ux);
-    s += Fy * (R(L::c(v, 1)) * (R(1) + beta) - uy);
-    if (L::D == 3) s += Fz * (R(L::c(v, 2)) * (R(1) + beta) - uz);
-    return s * lambda;
+    if constexpr (sizeof(R) == 4) {
+        R beta = R(L::c(v, 0)) * ux + R(L::c(v, 1)) * uy;
+        if (L::D == 3) beta += R(L::c(v, 2)) * uz;
+        beta = R(3) * beta;
+        R s = R(0);
+        s += Fx * (R(L::c(v, 0)) * (R(1) + beta) - ux);
+        s += Fy * (R(L::c(v, 1)) * (R(1) + beta) - uy);
+        if (L::D == 3) s += Fz * (R(L::c(v, 2)) * (R(1) + beta) - uz);
+        return wmul<Q>(v, R(3) * (R(1) - R(0.5) * omega) * s);
+    } else {
+        const R lambda = (R(1) - R(0.5) * omega) * (R(L::w(v)) / cs2);
+        R beta = R(L::c(v, 0)) * ux + R(L::c(v, 1)) * uy;
+        if (L::D == 3) beta += R(L::c(v, 2)) * uz;
+        beta = beta * (R(1) / cs2);
+        R s = R(0);
+        s += Fx * (R(L::c(v, 0)) * (R(1) + beta) - ux);
+        s += Fy * (R(L::c(v, 1)) * (R(1) + beta) - uy);
+        if (L::D == 3) s += Fz * (R(L::c(v, 2)) * (R(1) + beta) - uz);
+        return s * lambda;
+    }
 }
 
 }  // namespace luma

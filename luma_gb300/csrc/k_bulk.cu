@@ -95,16 +95,23 @@ __global__ void __launch_bounds__(256) k_aa(typename P::S *__restrict__ A, typen
         rho_out[x] = rho;
     }
     const R usq15 = R(1.5) * (ux * ux + uy * uy + uz * uz);
-    // Equilibrium base: shifted  g_eq = w*drho + w*rho*(3cu + 4.5cu^2 - 1.5u^2)
-    //                   plain    f_eq = w*rho*(1 + 3cu + 4.5cu^2 - 1.5u^2)
-    const R base = P::shifted ? R(0) : R(1);
+    // rho*u.u from the momentum itself: 1.5 j.u
+    const R ju15 = R(1.5) * (jx * ux + jy * uy + jz * uz);
+    // Equilibrium, (v, opp(v)) pairs sharing their even part:
+    //   shifted  g_eq = w*(drho + 3 c.j + 4.5 (c.j)(c.u) - 1.5 j.u), exact-weight product
+    //   plain    f_eq = w*rho*(1 + 3cu + 4.5cu^2 - 1.5u^2)
+    // The shifted form takes the odd part 3 w c.j from the momentum sums
+    // directly, not as rho * (j/rho): in FP32 the rounded quotient times rho
+    // differs from j by a bias fixed by the (nearly steady) density field,
+    // which the collision would turn into a steady momentum leak.
 #pragma unroll
     for (int v = 0; v < Q; ++v) {
         const int o = L::opp(v);
         if (o < v) continue;  // handled with its partner
-        const R w = R(L::w(v));
         if (o == v) {  // rest population
-            const R eq = P::shifted ? w * drho - w * rho * usq15 : w * rho * (base - usq15);
+            R eq;
+            if constexpr (P::shifted) eq = wmul<Q>(v, drho - ju15);
+            else eq = R(L::w(v)) * rho * (R(1) - usq15);
             g[v] = g[v] + omega * (eq - g[v]);
             continue;
         }
@@ -112,10 +119,23 @@ __global__ void __launch_bounds__(256) k_aa(typename P::S *__restrict__ A, typen
         if (L::c(v, 0)) cu += L::c(v, 0) > 0 ? ux : -ux;
         if (L::c(v, 1)) cu += L::c(v, 1) > 0 ? uy : -uy;
         if (D == 3 && L::c(v, 2)) cu += L::c(v, 2) > 0 ? uz : -uz;
-        const R wr = w * rho;
-        const R sym = (P::shifted ? w * drho : R(0)) + wr * (base + R(4.5) * cu * cu - usq15);
-        const R asym = R(3) * wr * cu;
-        const R eqv = sym + asym, eqo = sym - asym;
+        R eqv, eqo;
+        if constexpr (P::shifted) {
+            R cj = R(0);
+            if (L::c(v, 0)) cj += L::c(v, 0) > 0 ? jx : -jx;
+            if (L::c(v, 1)) cj += L::c(v, 1) > 0 ? jy : -jy;
+            if (D == 3 && L::c(v, 2)) cj += L::c(v, 2) > 0 ? jz : -jz;
+            const R even = drho + (R(4.5) * cj * cu - ju15);
+            const R odd = R(3) * cj;
+            eqv = wmul<Q>(v, even + odd);
+            eqo = wmul<Q>(v, even - odd);
+        } else {
+            const R wr = R(L::w(v)) * rho;
+            const R sym = wr * (R(1) + R(4.5) * cu * cu - usq15);
+            const R asym = R(3) * wr * cu;
+            eqv = sym + asym;
+            eqo = sym - asym;
+        }
         g[v] = g[v] + omega * (eqv - g[v]);
         g[o] = g[o] + omega * (eqo - g[o]);
     }

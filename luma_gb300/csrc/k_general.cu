@@ -505,10 +505,18 @@ __global__ void __launch_bounds__(128) k_regularised(StepArgs a, const int8_t *w
 #pragma unroll
     for (int v = 0; v < Q; v++) {
         const int c0 = L::c(v, 0), c1 = L::c(v, 1), c2 = L::c(v, 2);
-        fn[v] = feq_s<Q, P>(v, dens, drho, ux, uy, uz, cs2) +
-                (R(L::w(v)) / (R(2) * cs2 * cs2)) *
-                    (((R(c0 * c0) - cs2) * Sxx) + ((R(c1 * c1) - cs2) * Syy) + ((R(c2 * c2) - cs2) * Szz) +
-                     (R(2 * c0 * c1) * Sxy) + (R(2 * c0 * c2) * Sxz) + (R(2 * c1 * c2) * Syz));
+        if constexpr (P::shifted) {
+            // w/(2 cs^4) (c_a c_b - cs^2 delta_ab) S_ab with cs^2 = 1/3 and integer coefficients
+            fn[v] = feq_s<Q, P>(v, dens, drho, ux, uy, uz, cs2) +
+                    wmul<Q>(v, R(1.5) * (R(3 * c0 * c0 - 1) * Sxx + R(3 * c1 * c1 - 1) * Syy +
+                                         R(3 * c2 * c2 - 1) * Szz + R(6 * c0 * c1) * Sxy + R(6 * c0 * c2) * Sxz +
+                                         R(6 * c1 * c2) * Syz));
+        } else {
+            fn[v] = feq_s<Q, P>(v, dens, drho, ux, uy, uz, cs2) +
+                    (R(L::w(v)) / (R(2) * cs2 * cs2)) *
+                        (((R(c0 * c0) - cs2) * Sxx) + ((R(c1 * c1) - cs2) * Syy) + ((R(c2 * c2) - cs2) * Szz) +
+                         (R(2 * c0 * c1) * Sxy) + (R(2 * c0 * c2) * Sxz) + (R(2 * c1 * c2) * Syz));
+        }
     }
     if (!a.ibm_split) collide_site<Q, P>(a, id, fn, dens, drho, ux, uy, uz);
 #pragma unroll
