@@ -250,7 +250,7 @@ def run_ours(args, rank: int, world: int, local_rank: int):
     g32.synchronize()
 
     # ---- FP64 (the reference's arithmetic) on the same workload ----
-    K64 = max(K // 4, 20)
+    K64 = min(K, max(K // 4, 20))
     g64 = GpuGrid(l0.desc(precision=A.PREC_FP64))
     g64.set_stream(stream.cuda_stream)
     g64.upload(f0, l0.u, l0.rho, None, 0)

@@ -99,6 +99,11 @@ class Level0:
     u: np.ndarray
     rho: np.ndarray
     force_xyz: np.ndarray = field(default=None)
+    level: int = 0
+    region: int = 0
+    coarse_lims: tuple = (0, 0, 0, 0, 0, 0)
+    refinement_ratio: float = 1.0
+    edges: tuple = None          # this grid's global edges (x/y/z min,max)
 
     @property
     def ncell(self) -> int:
@@ -125,14 +130,16 @@ class Level0:
         d = self.defs
         g = A.GridDesc()
         g.abi_version = A.ABI_VERSION
-        g.level, g.region = 0, 0
+        g.level, g.region = self.level, self.region
         g.dims, g.Q = d.dims, d.Q
         g.N, g.M, g.K = self.N, self.M, self.K
         g.precision = precision
         g.collision = A.COLL_KBC if d.kbc else (A.COLL_BGK_SMAG if d.smagorinsky else A.COLL_BGK)
         g.flags = self.flags(fix_macro3d, fix_kbc)
         g.omega, g.dt, g.dh = self.omega, self.dt, self.dh
-        g.refinement_ratio = 1.0
+        g.refinement_ratio = self.refinement_ratio
+        for q in range(6):
+            g.coarse_lims[q] = int(self.coarse_lims[q])
         g.rho_in = d.rho_in
         g.velocity_ramp = d.velocity_ramp
         g.pressure_delta = pd2dlbm(d.pressure_delta, self.dh, self.dt, self.dm)
@@ -155,6 +162,9 @@ class Level0:
     @property
     def dm(self) -> float:
         return (self.defs.physical_rho / self.defs.rho_in) * self.dh * self.dh * self.dh
+
+
+GridLevel = Level0
 
 
 def pd2dlbm(p: float, dh: float, dt: float, dm: float) -> float:
@@ -266,7 +276,131 @@ def build_level0(defs: Definitions) -> Level0:
     return Level0(defs=defs, N=N, M=M, K=K, dh=dh, dt=dt, nu=nu, omega=omega, gravity=gravity,
                   global_edges=edges, wall_thickness=wt, xpos=xpos, ypos=ypos, zpos=zpos,
                   typ=typ.reshape(-1), ux_in=ux_in, uy_in=uy_in, uz_in=uz_in,
-                  u=u.reshape(-1), rho=rho.reshape(-1), force_xyz=force.reshape(-1))
+                  u=u.reshape(-1), rho=rho.reshape(-1), force_xyz=force.reshape(-1),
+                  edges=tuple(edges))
+
+
+def _inlet_profile(defs: Definitions, ypos: np.ndarray, dt: float, dh: float, edges0) -> tuple:
+    """_LBM_initSetInletProfile (src/GridObj_init_grids.cpp:1322-1360) on any grid."""
+    M = ypos.size
+    if defs.parabolic_inlet:
+        wt_top = defs.wall_cells[3] / float(defs.resolution)
+        wt_bot = defs.wall_cells[2] / float(defs.resolution)
+        b = edges0[3] - wt_top
+        p = (b + wt_bot) / 2.0
+        q = b - p
+        umax = (1.5 * defs.ux0 * dt) / dh
+        return (np.array([umax * (1.0 - math.pow((ypos[j] - p) / q, 2.0)) for j in range(M)]),
+                np.zeros(M), np.zeros(M))
+    return (np.full(M, (defs.ux0 * dt) / dh), np.full(M, (defs.uy0 * dt) / dh),
+            np.full(M, (defs.uz0 * dt) / dh))
+
+
+def build_subgrid(parent: "Level0", start: tuple, end: tuple, region: int = 0,
+                  coarse_dh_for_edges: float | None = None) -> "Level0":
+    """One embedded refined grid (factor 2) inside `parent`, mirroring the
+    reference's serial set-up: GridManager edges rounded to the grid spacing
+    (src/GridManager.cpp:85-90), coarse limits from the enclosing parent
+    voxels of the first/last fine voxel centres (LBM_initGridToGridMappings,
+    src/GridObj_init_grids.cpp:547-888; GridUtils::getEnclosingVoxel,
+    src/GridUtils.cpp:1625-1719), fine positions (LBM_initPositionVector,
+    :902-975), parent relabelling to transition-to-finer / refined and child
+    labels from the parent (LBM_initRefinedLab, :1106-1224), and the fine
+    relaxation frequency (:527).  `parent.typ` is relabelled in place."""
+    defs = parent.defs
+    D = defs.dims
+    dh_p = parent.dh
+    dh = dh_p / 2.0
+    dt = parent.dt / 2.0
+    rdh = coarse_dh_for_edges if coarse_dh_for_edges is not None else dh_p
+    edges = []
+    for a_ in range(3):
+        if a_ == 2 and D == 2:
+            edges += [0.0, 0.0]
+            continue
+        lo = round(start[a_] / rdh) * rdh
+        hi = round(end[a_] / rdh) * rdh
+        edges += [lo, hi]
+    pstart = [parent.edges[0], parent.edges[2], parent.edges[4]]
+    ppos = [parent.xpos, parent.ypos, parent.zpos]
+    lims = [0, 0, 0, 0, 0, 0]
+    sizes = [1, 1, 1]
+    pos = [None, None, np.zeros(1)]
+    for a_ in range(D):
+        lo = int(math.floor(((edges[2 * a_] + dh / 2.0) - pstart[a_]) / dh_p))
+        hi = int(math.floor(((edges[2 * a_ + 1] - dh / 2.0) - pstart[a_]) / dh_p))
+        lims[2 * a_], lims[2 * a_ + 1] = lo, hi
+        sizes[a_] = int((hi - lo + .5) * 2) + 1
+        p0 = ppos[a_][lo] - dh / 2.0
+        arr = [p0]
+        while len(arr) < sizes[a_]:
+            arr.append(arr[-1] + dh)
+        pos[a_] = np.array(arr)
+    N, M, K = sizes
+    # Parent relabelling.
+    Np, Mp, Kp = parent.N, parent.M, parent.K
+    ptyp = parent.typ.reshape(Np, Mp, Kp)
+    for i in range(Np):
+        xi = parent.xpos[i]
+        if not (xi > edges[0] and xi < edges[1]):
+            continue
+        for j in range(Mp):
+            yj = parent.ypos[j]
+            if not (yj > edges[2] and yj < edges[3]):
+                continue
+            for k in range(Kp):
+                zk = parent.zpos[k]
+                if D == 3 and not (zk > edges[4] and zk < edges[5]):
+                    continue
+                tl = ((xi > edges[0] and xi < edges[0] + dh_p) or (xi < edges[1] and xi > edges[1] - dh_p) or
+                      (yj > edges[2] and yj < edges[2] + dh_p) or (yj < edges[3] and yj > edges[3] - dh_p))
+                if D == 3:
+                    tl = tl or (zk > edges[4] and zk < edges[4] + dh_p) or (zk < edges[5] and zk > edges[5] - dh_p)
+                if tl:
+                    if ptyp[i, j, k] == A.FLUID:
+                        ptyp[i, j, k] = A.TL_TO_FINER
+                elif ptyp[i, j, k] == A.FLUID:
+                    ptyp[i, j, k] = A.REFINED
+    parent.typ = ptyp.reshape(-1)
+    # Child labels.
+    typ = np.empty((N, M, K), dtype=np.int32)
+    for i in range(N):
+        pi = (i - (i % 2)) // 2 + lims[0]
+        for j in range(M):
+            pj = (j - (j % 2)) // 2 + lims[2]
+            for k in range(K):
+                pk = ((k - (k % 2)) // 2 + lims[4]) if D == 3 else 0
+                pl = ptyp[pi, pj, pk]
+                typ[i, j, k] = A.TL_TO_COARSER if pl == A.TL_TO_FINER else (A.FLUID if pl == A.REFINED else pl)
+    ux_in, uy_in, uz_in = _inlet_profile(defs, pos[1], dt, dh, parent_root_edges(parent))
+    u = np.zeros((N, M, K, D))
+    rc = ramp_coefficient(defs, 0.0)
+    prof = np.stack([ux_in * rc, uy_in * rc, uz_in * rc], axis=1)[:, :D]
+    for i in range(N):
+        for j in range(M):
+            for k in range(K):
+                t_ = typ[i, j, k]
+                if not (defs.no_flow and t_ != A.VELOCITY):
+                    u[i, j, k] = prof[j]
+                if t_ == A.SOLID:
+                    u[i, j, k] = 0.0
+    rho = np.full((N, M, K), float(defs.rho_in))
+    omega = 1.0 / (((1.0 / parent.omega - 0.5) * 2.0) + 0.5)
+    level = parent.level + 1
+    rr = 1.0 / (2 ** level)
+    force = np.zeros((N, M, K, D))
+    if defs.gravity:
+        force[..., defs.gravity_dir] = rho * parent.gravity * rr
+    return Level0(defs=defs, N=N, M=M, K=K, dh=dh, dt=dt, nu=parent.nu, omega=omega, gravity=parent.gravity,
+                  global_edges=parent.global_edges, wall_thickness=parent.wall_thickness,
+                  xpos=pos[0], ypos=pos[1], zpos=pos[2], typ=typ.reshape(-1), ux_in=ux_in, uy_in=uy_in,
+                  uz_in=uz_in, u=u.reshape(-1), rho=rho.reshape(-1), force_xyz=force.reshape(-1),
+                  level=level, region=region, coarse_lims=tuple(lims), refinement_ratio=rr, edges=tuple(edges))
+
+
+def parent_root_edges(g: "Level0"):
+    """Global edges of level 0 (every grid keeps them in global_edges)."""
+    return g.global_edges
 
 
 # ---- lattice tables (src/stdafx.cpp:29-153) used by host-side helpers ----

@@ -54,6 +54,18 @@ CASES = {
                          re=60, gravity=True, gravity_force=0.04, gravity_dir=2,
                          walls=(SL, SL, S, S, F, F)),
         steps=(300,), store_f=()),
+    # D2Q9 channel with one embedded refined region (explode/coalesce).
+    "refine_d2q9": dict(
+        defs=Definitions(dims=2, resolution=40, timestep=1.0 / 800.0, bx=2.0, by=1.0, re=50, ux0=1.0,
+                         walls=(V, X, S, S, F, F)),
+        regions=[((0.5, 0.25, 0.0), (1.0, 0.75, 0.0))],
+        steps=(10, 200), store_f=(10,)),
+    # D3Q19 periodic box with two nested refined regions.
+    "refine_d3q19": dict(
+        defs=Definitions(dims=3, resolution=32, timestep=1.0 / 512.0, bx=1.0, by=1.0, bz=1.0,
+                         re=120, walls=(F,) * 6),
+        regions=[((0.25, 0.25, 0.25), (0.75, 0.75, 0.75)), ((0.375, 0.375, 0.375), (0.625, 0.625, 0.625))],
+        steps=(5, 40), store_f=(), store_fields=False),
     # D2Q9 BGK-Smagorinsky channel.
     "smag_d2q9": dict(
         defs=Definitions(dims=2, resolution=32, timestep=1.0 / 320.0, bx=2.0, by=1.0, re=2000,
@@ -101,7 +113,7 @@ def initial_fields(name: str):
     """Injected initial velocity (reference layout, flattened) or None."""
     d: Definitions = CASES[name]["defs"]
     N, M, K = d.sizes()
-    if name == "tgv_d3q19":
+    if name in ("tgv_d3q19", "refine_d3q19"):
         return {"u": taylor_green(N, M, K, 0.02, 1e-4).reshape(-1)}
     if name == "kbc_d3q27":
         return {"u": taylor_green(N, M, K, 0.05, 1e-3).reshape(-1)}

@@ -72,21 +72,45 @@ def run_case(name: str, ref: str) -> str:
     args[args.index("--dump-every") + 1] = str(int(g))
     subprocess.run(args, check=True)
     out = {"case": name}
+    levels = [(0, 0)] + [(l + 1, 0) for l in range(len(spec.get("regions", [])))]
     s0 = read_grid(os.path.join(work, "s0"))
     out["omega"] = np.float64(s0["meta"]["omega"])
     out["typ"] = s0["typ"]
     out["ux_in"] = s0["uxin"]
     out["ypos"] = s0["ypos"]
     out["f0_sha"] = sha(s0["f"])
-    if init is not None:
+    for (lev, reg) in levels[1:]:
+        gl = read_grid(os.path.join(work, "s0"), lev, reg)
+        k = f"L{lev}R{reg}"
+        out[f"{k}_typ"] = gl["typ"]
+        out[f"{k}_omega"] = np.float64(gl["meta"]["omega"])
+        out[f"{k}_coarse_lims"] = np.array(gl["meta"]["coarse_lims"], dtype=np.int64)
+        out[f"{k}_xpos"] = gl["xpos"]
+        out[f"{k}_ypos"] = gl["ypos"]
+        out[f"{k}_zpos"] = gl["zpos"]
+        out[f"{k}_ux_in"] = gl["uxin"]
+        out[f"{k}_f0_sha"] = sha(gl["f"])
+    if init is not None and spec.get("store_fields", True):
         out["init_u"] = init["u"]
     for s in spec["steps"]:
         gs = read_grid(os.path.join(work, f"s{s}"))
-        out[f"u_{s}"] = gs["u"]
-        out[f"rho_{s}"] = gs["rho"]
+        if spec.get("store_fields", True):
+            out[f"u_{s}"] = gs["u"]
+            out[f"rho_{s}"] = gs["rho"]
+        out[f"u_sha_{s}"] = sha(gs["u"])
+        out[f"rho_sha_{s}"] = sha(gs["rho"])
         out[f"f_sha_{s}"] = sha(gs["f"])
         if s in spec.get("store_f", ()):
             out[f"f_{s}"] = gs["f"]
+        for (lev, reg) in levels[1:]:
+            gl = read_grid(os.path.join(work, f"s{s}"), lev, reg)
+            k = f"L{lev}R{reg}"
+            if spec.get("store_fields", True):
+                out[f"{k}_u_{s}"] = gl["u"]
+                out[f"{k}_rho_{s}"] = gl["rho"]
+            out[f"{k}_u_sha_{s}"] = sha(gl["u"])
+            out[f"{k}_rho_sha_{s}"] = sha(gl["rho"])
+            out[f"{k}_f_sha_{s}"] = sha(gl["f"])
     with open(os.path.join(work, "timing.txt")) as fp:
         out["ref_timing"] = fp.read()
     np.savez_compressed(os.path.join(HERE, f"{name}.npz"), **out)

@@ -35,3 +35,40 @@ def initial_state(l0: hostcase.Level0):
     d = l0.defs
     f0 = hostcase.equilibrium(d.dims, d.Q, l0.rho, l0.u).reshape(-1)
     return f0, l0.u.copy(), l0.rho.copy(), l0.force_xyz.copy()
+
+
+def hierarchy(name: str) -> list:
+    """[level0, level1, ...] of an oracle case (one region per level), built
+    by the host set-up; parents are relabelled as children are added."""
+    spec = CASES.CASES[name]
+    grids = [level0(name)]
+    for r in spec.get("regions", []):
+        grids.append(hostcase.build_subgrid(grids[-1], r[0], r[1]))
+    return grids
+
+
+def grid_key(g) -> str:
+    return f"L{g.level}R{g.region}"
+
+
+def build_backend(name: str, make, precision=None):
+    """Create the grid tree of an oracle case on a backend.
+
+    `make(desc, parent)` builds one grid (OracleGrid or GpuGrid); returns
+    (grids, levels) with each grid's initial state uploaded."""
+    levels = hierarchy(name)
+    grids = []
+    for lv in levels:
+        desc = lv.desc() if precision is None else lv.desc(precision=precision)
+        g = make(desc, grids[-1] if grids else None)
+        grids.append(g)
+    for g, lv in zip(grids, levels):
+        g.upload(*initial_state(lv), t=0)
+    return grids, levels
+
+
+def fields_at(fx: dict, key: str, s: int, name: str):
+    """(u, rho, u_sha, rho_sha, f_sha) of grid `key` at step s from a fixture."""
+    pre = "" if key == "L0R0" else key + "_"
+    return (fx.get(f"{pre}u_{s}"), fx.get(f"{pre}rho_{s}"), str(fx[f"{pre}u_sha_{s}"]),
+            str(fx[f"{pre}rho_sha_{s}"]), str(fx[f"{pre}f_sha_{s}"]))

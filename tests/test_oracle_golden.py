@@ -17,7 +17,7 @@ def test_host_setup_matches_reference(name):
     """Labels, inlet profile, positions and omega computed by the host set-up
     equal the values the reference computed at initialisation."""
     fx = R.fixture(name)
-    l0 = R.level0(name)
+    l0 = R.hierarchy(name)[0]
     assert np.array_equal(l0.typ, fx["typ"])
     assert np.array_equal(l0.ux_in, fx["ux_in"])
     assert np.array_equal(l0.ypos, fx["ypos"])
@@ -26,25 +26,47 @@ def test_host_setup_matches_reference(name):
     assert R.sha(f0) == str(fx["f0_sha"])
 
 
+@pytest.mark.parametrize("name", sorted(n for n in CASES.CASES if CASES.CASES[n].get("regions")))
+def test_host_subgrid_setup_matches_reference(name):
+    """Sub-grid labels, coarse limits, positions, inlet profile and omega of
+    every refined level, and the parent relabelling, equal the reference's."""
+    fx = R.fixture(name)
+    levels = R.hierarchy(name)
+    assert np.array_equal(levels[0].typ, fx["typ"])
+    for lv in levels[1:]:
+        k = R.grid_key(lv)
+        assert np.array_equal(lv.typ, fx[f"{k}_typ"]), k
+        assert lv.omega == float(fx[f"{k}_omega"]), k
+        assert tuple(lv.coarse_lims) == tuple(int(x) for x in fx[f"{k}_coarse_lims"]), k
+        assert np.array_equal(lv.xpos, fx[f"{k}_xpos"]) and np.array_equal(lv.ypos, fx[f"{k}_ypos"]), k
+        assert np.array_equal(lv.ux_in, fx[f"{k}_ux_in"]), k
+        f0, *_ = R.initial_state(lv)
+        assert R.sha(f0) == str(fx[f"{k}_f0_sha"]), k
+
+
 @pytest.mark.parametrize("name", sorted(CASES.CASES))
 def test_oracle_bit_exact_vs_reference(name):
     """The restatement reproduces the reference bit for bit (FP64, same
-    operation order, no contraction) at every stored step."""
+    operation order, no contraction) at every stored step, on every grid."""
     spec = CASES.CASES[name]
     fx = R.fixture(name)
-    l0 = R.level0(name)
-    g = O.OracleGrid(l0.desc())
-    g.upload(*R.initial_state(l0), t=0)
+    grids, levels = R.build_backend(name, lambda d, p: O.OracleGrid(d, p))
     done = 0
     for s in spec["steps"]:
-        g.step(s - done)
+        grids[0].step(s - done)
         done = s
-        st = g.download()
-        assert np.array_equal(st["u"], fx[f"u_{s}"]), f"u differs at step {s}"
-        assert np.array_equal(st["rho"], fx[f"rho_{s}"]), f"rho differs at step {s}"
-        assert R.sha(st["f"]) == str(fx[f"f_sha_{s}"]), f"f differs at step {s}"
-        if f"f_{s}" in fx:
-            assert np.array_equal(st["f"], fx[f"f_{s}"])
+        for g, lv in zip(grids, levels):
+            key = R.grid_key(lv)
+            st = g.download()
+            u, rho, u_sha, rho_sha, f_sha = R.fields_at(fx, key, s, name)
+            if u is not None:
+                assert np.array_equal(st["u"], u), f"{key} u differs at step {s}"
+                assert np.array_equal(st["rho"], rho), f"{key} rho differs at step {s}"
+            assert R.sha(st["u"]) == u_sha, f"{key} u differs at step {s}"
+            assert R.sha(st["rho"]) == rho_sha, f"{key} rho differs at step {s}"
+            assert R.sha(st["f"]) == f_sha, f"{key} f differs at step {s}"
+            if key == "L0R0" and f"f_{s}" in fx:
+                assert np.array_equal(st["f"], fx[f"f_{s}"])
 
 
 def test_known_answer_equilibrium_d2q9():
