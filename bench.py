@@ -299,7 +299,7 @@ def run_ours(args, rank: int, world: int, local_rank: int):
     peaks = read_peaks()
     bytes32 = 2 * 19 * 4 * ncell
     ach32 = bytes32 / (sec32 / K) / 1e9
-    traffic = read_profile_traffic("k_aa_d3q19_fp32_256")
+    traffic = read_profile_traffic("k_aa_d3q19_fp32_256") if n == SIZE else None
     bytes64 = 2 * 19 * 8 * ncell
 
     cpu = None

@@ -1,0 +1,84 @@
+"""CPU checks of the C ABI library: it loads, exports every entry point the
+header declares, and its struct layout matches the ctypes mirror.  No
+compute call is made (no GPU here)."""
+import ctypes as C
+import os
+import re
+
+import pytest
+
+from luma_gb300 import _abi as A
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+HEADER = os.path.join(ROOT, "include", "luma_gpu.h")
+LIB = os.path.join(ROOT, "luma_gb300", "_build", "libluma_gpu.so")
+
+
+def declared_functions():
+    src = open(HEADER).read()
+    return sorted(set(re.findall(r"^\s*(?:int|const char \*)\s*(luma_gpu_\w+)\s*\(", src, re.M)))
+
+
+@pytest.fixture(scope="module")
+def lib():
+    if not os.path.exists(LIB):
+        from luma_gb300 import build
+        build.build()
+    try:
+        return C.CDLL(LIB)
+    except OSError as e:  # libcudart missing on a host without the toolkit
+        pytest.skip(f"cannot load CUDA library here: {e}")
+
+
+def test_header_declares_entry_points():
+    names = declared_functions()
+    assert "luma_gpu_step" in names and "luma_gpu_grid_create" in names
+    assert len(names) >= 11
+
+
+def test_library_exports_every_declared_symbol(lib):
+    for name in declared_functions():
+        assert hasattr(lib, name), name
+
+
+def test_abi_version_and_error_string(lib):
+    lib.luma_gpu_abi_version.restype = C.c_int
+    assert lib.luma_gpu_abi_version() == A.ABI_VERSION
+    lib.luma_gpu_last_error_string.restype = C.c_char_p
+    assert isinstance(lib.luma_gpu_last_error_string(), bytes)
+
+
+def test_invalid_descriptor_rejected_without_gpu(lib):
+    """Descriptor validation runs before any CUDA call: a wrong ABI version
+    and an unsupported lattice come back as LUMA_E_INVALID."""
+    lib.luma_gpu_grid_create.argtypes = [C.POINTER(A.GridDesc), C.c_void_p, C.POINTER(C.c_void_p)]
+    lib.luma_gpu_last_error_string.restype = C.c_char_p
+    d = A.GridDesc()
+    d.abi_version = 999
+    h = C.c_void_p()
+    assert lib.luma_gpu_grid_create(C.byref(d), None, C.byref(h)) == A.LUMA_E_INVALID
+    assert b"ABI" in lib.luma_gpu_last_error_string()
+    d.abi_version = A.ABI_VERSION
+    d.dims, d.Q, d.N, d.M, d.K = 3, 15, 4, 4, 4
+    assert lib.luma_gpu_grid_create(C.byref(d), None, C.byref(h)) == A.LUMA_E_INVALID
+    assert b"lattice" in lib.luma_gpu_last_error_string()
+    d.Q = 19
+    d.collision = A.COLL_KBC
+    d.omega = 1.5
+    assert lib.luma_gpu_grid_create(C.byref(d), None, C.byref(h)) == A.LUMA_E_INVALID
+    assert b"D3Q27" in lib.luma_gpu_last_error_string()
+
+
+def test_desc_struct_size_matches_header():
+    """sizeof(luma_grid_desc) from a C compile of the header equals ctypes'."""
+    import subprocess
+    import tempfile
+    src = '#include "luma_gpu.h"\n#include <stdio.h>\nint main(){printf("%zu %zu\\n", sizeof(luma_grid_desc), sizeof(luma_reduction));return 0;}\n'
+    with tempfile.TemporaryDirectory() as td:
+        c = os.path.join(td, "s.c")
+        open(c, "w").write(src)
+        exe = os.path.join(td, "s")
+        subprocess.run(["gcc", "-I", os.path.join(ROOT, "include"), c, "-o", exe], check=True)
+        out = subprocess.run([exe], capture_output=True, text=True, check=True).stdout.split()
+    assert int(out[0]) == C.sizeof(A.GridDesc)
+    assert int(out[1]) == C.sizeof(A.Reduction)
