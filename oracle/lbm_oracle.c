@@ -751,3 +751,318 @@ void oracle_set_ibm(oracle_grid *g, int has_ibm, int has_flexible, void (*hook)(
     g->ibm_hook = hook;
     g->ibm_ctx = ctx;
 }
+
+/* =========================== immersed boundary ===========================
+ * Restatement of ObjectManager's IBM operator for rigid bodies
+ * (src/ObjectManager_ops_ibm.cpp): Roma delta kernel (:255-272), support
+ * search (:279-453) with delta values (:462-491), marker spacing ds
+ * (:927-981), epsilon from the dense support-overlap system (:773-920) solved
+ * with the partial-pivot LU the oracle build links in place of LAPACK, then
+ * per step interpolate (:498-591), force (:598-614), spread (:621-689) and
+ * macroscopic update at the supports (:696-766). */
+
+typedef struct ibm_body {
+    oracle_grid *owner;
+    int nm;
+    double *pos, *vel, *eps, *ds, *dil, *area, *F, *irho, *imom;
+    int *off;        /* CSR offsets into the support arrays, nm + 1 */
+    int *si, *sj, *sk;
+    double *sx, *sy, *sz, *delta;
+} ibm_body;
+
+typedef struct ibm_ctx {
+    int nb;
+    ibm_body *b;
+    double global_edges[6];
+} ibm_ctx;
+
+static double delta_kernel(double radius, double dilation) {
+    const double mag_r = fabs(radius) / dilation;
+    if (mag_r > 1.5) return 0.0;
+    if (mag_r > 0.5) return (5.0 - (3.0 * mag_r) - sqrt(-3.0 * pow(1.0 - mag_r, 2) + 1.0)) / 6.0;
+    return (1.0 + sqrt(1.0 - 3.0 * pow(mag_r, 2))) / 3.0;
+}
+
+/* Enclosing voxel of a position on a grid (GridUtils::getEnclosingVoxel,
+ * serial form): floor((x - grid start) / dh). */
+static int enclosing(double x, double start, double dh) { return (int)floor((x - start) / dh); }
+
+static double grid_start(const oracle_grid *g, int axis) {
+    /* Level 0 starts at 0; a sub-grid starts half a fine cell before its first site. */
+    const double *p = axis == 0 ? g->xpos : (axis == 1 ? g->ypos : g->zpos);
+    return g->d.level == 0 ? 0.0 : p[0] - g->d.dh / 2.0;
+}
+
+static int within_domain(const ibm_ctx *c, const double p[3], int D) {
+    const double *E = c->global_edges;
+    if (p[0] < E[0] || p[0] > E[1] || p[1] < E[2] || p[1] > E[3]) return 0;
+    if (D == 3 && (p[2] < E[4] || p[2] > E[5])) return 0;
+    return 1;
+}
+
+static void support_delta(const ibm_body *b, int m, const double est[3], int D, double *out) {
+    const double dh = b->owner->d.dh;
+    const double *x = b->pos + 3 * m;
+    const double dx = (est[0] - x[0]) / dh, dy = (est[1] - x[1]) / dh;
+    double v = delta_kernel(dx, b->dil[m]) * delta_kernel(dy, b->dil[m]);
+    if (D == 3) v = v * delta_kernel((est[2] - x[2]) / dh, b->dil[m]);
+    *out = v;
+}
+
+/* ibm_findSupport (:279-453) for one body; two passes (count, fill). */
+static int find_support(ibm_ctx *c, ibm_body *b) {
+    oracle_grid *g = b->owner;
+    const int D = g->D;
+    const double dh = g->d.dh;
+    int total = 0;
+    for (int pass = 0; pass < 2; ++pass) {
+        int n = 0;
+        for (int m = 0; m < b->nm; ++m) {
+            if (pass == 1) b->off[m] = n;
+            const double *x = b->pos + 3 * m;
+            const int in = enclosing(x[0], grid_start(g, 0), dh);
+            const int jn = enclosing(x[1], grid_start(g, 1), dh);
+            const int kn = D == 3 ? enclosing(x[2], grid_start(g, 2), dh) : 0;
+            if (in < 0 || jn < 0 || kn < 0 || in >= g->d.N || jn >= g->d.M || kn >= g->d.K) {
+                set_err("Body is no-longer inside the domain! Simulation has likely crashed.");
+                return -1;
+            }
+            double nearpos[3] = {g->xpos[in], g->ypos[jn], D == 3 ? g->zpos[kn] : 0.0};
+            if (pass == 1) {
+                b->si[n] = in; b->sj[n] = jn; b->sk[n] = kn;
+                b->sx[n] = nearpos[0]; b->sy[n] = nearpos[1]; b->sz[n] = nearpos[2];
+                support_delta(b, m, nearpos, D, &b->delta[n]);
+            }
+            ++n;
+            for (int i = in - 5; i <= in + 5; i++)
+                for (int j = jn - 5; j <= jn + 5; j++)
+                    for (int k = (D == 3 ? kn - 5 : 0); k <= (D == 3 ? kn + 5 : 0); k++) {
+                        double est[3] = {nearpos[0] + (i - in) * dh, nearpos[1] + (j - jn) * dh, nearpos[2]};
+                        if (D == 3) est[2] = nearpos[2] + (k - kn) * dh;
+                        if ((fabs(x[0] - est[0]) / dh < 1.5 * b->dil[m]) && (fabs(x[1] - est[1]) / dh < 1.5 * b->dil[m]) &&
+                            (D == 2 || fabs(x[2] - est[2]) / dh < 1.5 * b->dil[m]) && within_domain(c, est, D)) {
+                            if (i != in || j != jn || (D == 3 && k != kn)) {
+                                if (pass == 1) {
+                                    b->si[n] = i; b->sj[n] = j; b->sk[n] = k;
+                                    b->sx[n] = est[0]; b->sy[n] = est[1]; b->sz[n] = est[2];
+                                    support_delta(b, m, est, D, &b->delta[n]);
+                                }
+                                ++n;
+                            }
+                        }
+                    }
+        }
+        if (pass == 0) {
+            total = n;
+            free(b->si); free(b->sj); free(b->sk); free(b->sx); free(b->sy); free(b->sz); free(b->delta);
+            b->si = (int *)malloc(sizeof(int) * (total + 1));
+            b->sj = (int *)malloc(sizeof(int) * (total + 1));
+            b->sk = (int *)malloc(sizeof(int) * (total + 1));
+            b->sx = (double *)malloc(sizeof(double) * (total + 1));
+            b->sy = (double *)malloc(sizeof(double) * (total + 1));
+            b->sz = (double *)malloc(sizeof(double) * (total + 1));
+            b->delta = (double *)malloc(sizeof(double) * (total + 1));
+        } else {
+            b->off[b->nm] = n;
+        }
+    }
+    return 0;
+}
+
+/* ibm_computeDs (:927-981). */
+static void compute_ds(ibm_body *b) {
+    const double dh = b->owner->d.dh;
+    for (int m = 0; m < b->nm; ++m) {
+        double ds = 10.0;
+        for (int n = 0; n < b->nm; ++n) {
+            if (n == m) continue;
+            double r = 0.0;
+            for (int d = 0; d < 3; ++d) r += pow(b->pos[3 * m + d] - b->pos[3 * n + d], 2);
+            const double dist = sqrt(r) / dh;
+            if (dist < ds) ds = dist;
+        }
+        b->ds[m] = ds;
+    }
+}
+
+/* Partial-pivot LU (column-major, 1-based pivots) and the transposed solve:
+ * the algorithm the oracle build of the reference links for dgetrf_/dgetrs_. */
+static int lu_factor(int n, double *a, int lda, int *ipiv) {
+#define A_(r, c) a[(size_t)(c) * lda + (r)]
+    for (int k = 0; k < n; ++k) {
+        int p = k;
+        double best = fabs(A_(k, k));
+        for (int r = k + 1; r < n; ++r) {
+            double v = fabs(A_(r, k));
+            if (v > best) { best = v; p = r; }
+        }
+        ipiv[k] = p + 1;
+        if (A_(p, k) == 0.0) continue;
+        if (p != k)
+            for (int cc = 0; cc < n; ++cc) { double t = A_(k, cc); A_(k, cc) = A_(p, cc); A_(p, cc) = t; }
+        const double inv = 1.0 / A_(k, k);
+        for (int r = k + 1; r < n; ++r) A_(r, k) *= inv;
+        for (int cc = k + 1; cc < n; ++cc) {
+            const double akc = A_(k, cc);
+            if (akc == 0.0) continue;
+            for (int r = k + 1; r < n; ++r) A_(r, cc) -= A_(r, k) * akc;
+        }
+    }
+    return 0;
+}
+static void lu_solve_t(int n, const double *a, int lda, const int *ipiv, double *x) {
+    for (int r = 0; r < n; ++r) { double s = x[r]; for (int cc = 0; cc < r; ++cc) s -= A_(cc, r) * x[cc]; x[r] = s / A_(r, r); }
+    for (int r = n - 1; r >= 0; --r) { double s = x[r]; for (int cc = r + 1; cc < n; ++cc) s -= A_(cc, r) * x[cc]; x[r] = s; }
+    for (int k = n - 1; k >= 0; --k) { int p = ipiv[k] - 1; if (p != k) { double t = x[k]; x[k] = x[p]; x[p] = t; } }
+#undef A_
+}
+
+/* ibm_findEpsilon (:773-920) + GridUtils::solveLinearSystem (src/GridUtils.cpp:356-395). */
+static void find_epsilon(ibm_body *b) {
+    const int n = b->nm, D = b->owner->D;
+    const double dh = b->owner->d.dh;
+    double *A = (double *)calloc((size_t)n * n, sizeof(double));  /* row-major A[I][J] */
+    for (int I = 0; I < n; ++I)
+        for (int J = 0; J < n; ++J) {
+            double aij = 0.0;
+            for (int s = b->off[I]; s < b->off[I + 1]; ++s) {
+                const double dI = b->delta[s];
+                double dJ = delta_kernel((b->pos[3 * J + 0] - b->sx[s]) / dh, b->dil[J]) *
+                            delta_kernel((b->pos[3 * J + 1] - b->sy[s]) / dh, b->dil[J]);
+                if (D == 3) dJ = dJ * delta_kernel((b->pos[3 * J + 2] - b->sz[s]) / dh, b->dil[J]);
+                aij += dI * dJ * b->area[I];
+            }
+            A[(size_t)I * n + J] = aij * b->ds[J];
+        }
+    /* The row-major copy read column-major is A^T; the transposed solve
+     * then solves A x = 1. */
+    int *ipiv = (int *)malloc(sizeof(int) * n);
+    double *x = (double *)malloc(sizeof(double) * n);
+    for (int i = 0; i < n; ++i) x[i] = 1.0;
+    lu_factor(n, A, n, ipiv);
+    lu_solve_t(n, A, n, ipiv, x);
+    for (int m = 0; m < n; ++m) b->eps[m] = x[m];
+    free(A); free(ipiv); free(x);
+}
+
+static void ibm_pass(oracle_grid *g, void *vctx) {
+    ibm_ctx *c = (ibm_ctx *)vctx;
+    const int D = g->D;
+    const int K = g->d.K, M = g->d.M;
+    for (int ib = 0; ib < c->nb; ++ib) {
+        ibm_body *b = &c->b[ib];
+        if (b->owner != g) continue;
+        /* interpolate + force */
+        for (int m = 0; m < b->nm; ++m) {
+            double r = 0.0, mom[3] = {0.0, 0.0, 0.0};
+            for (int s = b->off[m]; s < b->off[m + 1]; ++s) {
+                const size_t id = (size_t)b->sk[s] + (size_t)b->sj[s] * K + (size_t)b->si[s] * K * M;
+                r += g->rho[id] * b->delta[s] * b->area[m];
+                for (int d = 0; d < D; d++) mom[d] += g->rho[id] * g->u[d + id * D] * b->delta[s] * b->area[m];
+            }
+            b->irho[m] = r;
+            for (int d = 0; d < D; d++) {
+                b->imom[3 * m + d] = mom[d];
+                b->F[3 * m + d] = 2.0 * (mom[d] - r * b->vel[3 * m + d]) / 1.0;
+            }
+        }
+        /* spread */
+        for (int m = 0; m < b->nm; ++m)
+            for (int s = b->off[m]; s < b->off[m + 1]; ++s) {
+                const size_t id = (size_t)b->sk[s] + (size_t)b->sj[s] * K + (size_t)b->si[s] * K * M;
+                const double volWidth = b->eps[m];
+                const double volDepth = D == 3 ? b->ds[m] : 1.0;
+                for (int d = 0; d < D; d++)
+                    g->force_xyz[d + id * D] -= b->delta[s] * b->F[3 * m + d] * volWidth * volDepth * b->ds[m];
+            }
+        /* macroscopic update at the supports */
+        for (int m = 0; m < b->nm; ++m)
+            for (int s = b->off[m]; s < b->off[m + 1]; ++s) {
+                const int id = b->sk[s] + b->sj[s] * K + b->si[s] * K * M;
+                macro_site(g, b->si[s], b->sj[s], b->sk[s], id, g->typ[id]);
+            }
+    }
+}
+
+static ibm_ctx *g_ibm = NULL;
+
+/* Adds a rigid body of nm markers (positions xyz[3*nm]) owned by grid g.
+ * Returns the body index. */
+int oracle_ibm_add_body(oracle_grid *g, int nm, const double *xyz) {
+    if (!g_ibm) {
+        g_ibm = (ibm_ctx *)calloc(1, sizeof(ibm_ctx));
+    }
+    oracle_grid *root = g;
+    while (root->parent) root = root->parent;
+    memcpy(g_ibm->global_edges, root->d.global_edges, sizeof(double) * 6);
+    g_ibm->b = (ibm_body *)realloc(g_ibm->b, sizeof(ibm_body) * (g_ibm->nb + 1));
+    ibm_body *b = &g_ibm->b[g_ibm->nb];
+    memset(b, 0, sizeof *b);
+    b->owner = g;
+    b->nm = nm;
+    b->pos = dup_d(xyz, 3 * (size_t)nm);
+    b->vel = dup_d(NULL, 3 * (size_t)nm);
+    b->eps = dup_d(NULL, nm);
+    b->ds = dup_d(NULL, nm);
+    b->dil = dup_d(NULL, nm);
+    b->area = dup_d(NULL, nm);
+    b->F = dup_d(NULL, 3 * (size_t)nm);
+    b->irho = dup_d(NULL, nm);
+    b->imom = dup_d(NULL, 3 * (size_t)nm);
+    for (int m = 0; m < nm; ++m) { b->eps[m] = 0.0; b->dil[m] = 1.0; b->area[m] = 1.0; b->ds[m] = 1.0; }
+    b->off = (int *)calloc(nm + 1, sizeof(int));
+    g->has_ibm_bodies = 1;
+    g->ibm_hook = ibm_pass;
+    g->ibm_ctx = g_ibm;
+    return g_ibm->nb++;
+}
+
+/* ObjectManager::ibm_initialise (:190-246): supports, then ds, then epsilon. */
+int oracle_ibm_initialise(void) {
+    if (!g_ibm) return 0;
+    for (int ib = 0; ib < g_ibm->nb; ++ib)
+        if (find_support(g_ibm, &g_ibm->b[ib])) return -1;
+    for (int ib = 0; ib < g_ibm->nb; ++ib) compute_ds(&g_ibm->b[ib]);
+    for (int ib = 0; ib < g_ibm->nb; ++ib) find_epsilon(&g_ibm->b[ib]);
+    return 0;
+}
+
+/* Per-marker state: rows of (x y z Fx Fy Fz eps ds nsupp). */
+int oracle_ibm_markers(int ib, double *out) {
+    if (!g_ibm || ib >= g_ibm->nb) return -1;
+    ibm_body *b = &g_ibm->b[ib];
+    for (int m = 0; m < b->nm; ++m) {
+        double *o = out + 9 * (size_t)m;
+        o[0] = b->pos[3 * m]; o[1] = b->pos[3 * m + 1]; o[2] = b->pos[3 * m + 2];
+        o[3] = b->F[3 * m]; o[4] = b->F[3 * m + 1]; o[5] = b->owner->D == 3 ? b->F[3 * m + 2] : 0.0;
+        o[6] = b->eps[m]; o[7] = b->ds[m]; o[8] = (double)(b->off[m + 1] - b->off[m]);
+    }
+    return 0;
+}
+
+/* Support lists: rows of (marker i j k delta), total count returned. */
+int oracle_ibm_supports(int ib, double *out, int cap) {
+    if (!g_ibm || ib >= g_ibm->nb) return -1;
+    ibm_body *b = &g_ibm->b[ib];
+    const int n = b->off[b->nm];
+    if (out && cap >= n)
+        for (int m = 0; m < b->nm; ++m)
+            for (int s = b->off[m]; s < b->off[m + 1]; ++s) {
+                double *o = out + 5 * (size_t)s;
+                o[0] = m; o[1] = b->si[s]; o[2] = b->sj[s]; o[3] = b->sk[s]; o[4] = b->delta[s];
+            }
+    return n;
+}
+
+void oracle_ibm_reset(void) {
+    if (!g_ibm) return;
+    for (int ib = 0; ib < g_ibm->nb; ++ib) {
+        ibm_body *b = &g_ibm->b[ib];
+        free(b->pos); free(b->vel); free(b->eps); free(b->ds); free(b->dil); free(b->area); free(b->F);
+        free(b->irho); free(b->imom); free(b->off); free(b->si); free(b->sj); free(b->sk); free(b->sx);
+        free(b->sy); free(b->sz); free(b->delta);
+    }
+    free(g_ibm->b);
+    free(g_ibm);
+    g_ibm = NULL;
+}

@@ -18,7 +18,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(HERE)
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD, "liboracle.so")
-SOURCES = ["lbm_oracle.c", "ibm_oracle.c"]
+SOURCES = ["lbm_oracle.c"]
 
 if ROOT not in sys.path:
     sys.path.insert(0, ROOT)
@@ -58,6 +58,11 @@ def lib():
         L.oracle_get_time.argtypes = [C.c_void_p]
         L.oracle_set_threads.argtypes = [C.c_int]
         L.oracle_last_error.restype = C.c_char_p
+        L.oracle_ibm_add_body.argtypes = [C.c_void_p, C.c_int, C.POINTER(C.c_double)]
+        L.oracle_ibm_initialise.argtypes = []
+        L.oracle_ibm_markers.argtypes = [C.c_int, C.POINTER(C.c_double)]
+        L.oracle_ibm_supports.argtypes = [C.c_int, C.POINTER(C.c_double), C.c_int]
+        L.oracle_ibm_reset.argtypes = []
         _lib = L
     return _lib
 
@@ -120,3 +125,33 @@ class OracleGrid:
 
 def set_threads(n: int) -> int:
     return lib().oracle_set_threads(n)
+
+
+class OracleIBM:
+    """Rigid IB bodies of the oracle (one process-wide set)."""
+
+    def __init__(self):
+        self.L = lib()
+        self.L.oracle_ibm_reset()
+        self.nm = []
+
+    def add_body(self, grid: OracleGrid, positions) -> int:
+        pos = np.ascontiguousarray(positions, dtype=np.float64).reshape(-1, 3)
+        ib = self.L.oracle_ibm_add_body(grid.h, pos.shape[0], A.dptr(pos))
+        self.nm.append(pos.shape[0])
+        return ib
+
+    def initialise(self):
+        if self.L.oracle_ibm_initialise() != 0:
+            raise RuntimeError(self.L.oracle_last_error().decode())
+
+    def markers(self, ib: int) -> np.ndarray:
+        out = np.empty((self.nm[ib], 9))
+        self.L.oracle_ibm_markers(ib, A.dptr(out))
+        return out
+
+    def supports(self, ib: int) -> np.ndarray:
+        n = self.L.oracle_ibm_supports(ib, None, 0)
+        out = np.empty((n, 5))
+        self.L.oracle_ibm_supports(ib, A.dptr(out), n)
+        return out

@@ -89,10 +89,22 @@ static void dump_markers(const std::string &dir) {
         IBBody &body = om->iBody[b];
         for (size_t m = 0; m < body.markers.size(); ++m) {
             IBMarker &mk = body.markers[m];
+            const double fz = mk.force_xyz.size() > 2 ? mk.force_xyz[2] : 0.0;
             std::fprintf(fp, "%zu %zu %.17g %.17g %.17g %.17g %.17g %.17g %.17g %.17g %.17g %.17g %.17g %.17g %zu\n",
                          b, m, mk.position[0], mk.position[1], mk.position[2], mk.force_xyz[0],
-                         mk.force_xyz[1], mk.force_xyz[2], mk.epsilon, mk.ds, mk.markerVel[0],
+                         mk.force_xyz[1], fz, mk.epsilon, mk.ds, mk.markerVel[0],
                          mk.markerVel[1], mk.markerVel[2], mk.dilation, mk.supp_i.size());
+        }
+    }
+    std::fclose(fp);
+    fp = std::fopen((dir + "/supports.txt").c_str(), "w");
+    for (size_t b = 0; b < om->iBody.size(); ++b) {
+        IBBody &body = om->iBody[b];
+        for (size_t m = 0; m < body.markers.size(); ++m) {
+            IBMarker &mk = body.markers[m];
+            for (size_t q = 0; q < mk.supp_i.size(); ++q)
+                std::fprintf(fp, "%zu %zu %zu %d %d %d %.17g\n", b, m, q, mk.supp_i[q], mk.supp_j[q], mk.supp_k[q],
+                             mk.deltaval[q]);
         }
     }
     std::fclose(fp);
@@ -108,6 +120,42 @@ static void dump_all(GridObj *root, const std::string &out, int step) {
     dump_markers(dir);
 }
 
+#ifdef L_IBM_ON
+/* Rigid IB bodies with explicit marker positions (the case's marker layout
+ * is not one of the reference's prefab formulas).  File format:
+ *   nbodies
+ *   level region nmarkers      (per body, followed by nmarkers lines "x y z")
+ * Each body is built as the reference's constructors build one
+ * (inc/Body.h:197-255 then IBBody::initialise, src/IBBody.cpp:58-91). */
+static void inject_markers(ObjectManager *om, GridObj *root, const std::string &path) {
+    std::ifstream in(path.c_str());
+    int nb = 0;
+    in >> nb;
+    for (int b = 0; b < nb; ++b) {
+        int lev, reg, nm;
+        in >> lev >> reg >> nm;
+        GridObj *g = nullptr;
+        GridUtils::getGrid(root, lev, reg, g);
+        if (!g) { std::fprintf(stderr, "no grid L%d R%d\n", lev, reg); std::exit(2); }
+        IBBody body;
+        body._Owner = g;
+        body.id = b;
+        body.closed_surface = true;
+        body.level = lev;
+        body.owningRank = 0;
+        for (int m = 0; m < nm; ++m) {
+            double x, y, z;
+            in >> x >> y >> z;
+            body.markers.emplace_back(x, y, z, m, g);
+        }
+        body.initialise(eRigid);
+        om->iBody.push_back(body);
+        om->hasIBMBodies[lev] = true;
+    }
+    om->ibm_finaliseReadIn(nb);
+}
+#endif
+
 static void reinit_equilibrium(GridObj *g) {
     const int n = g->N_lim * g->M_lim * g->K_lim;
     for (int id = 0; id < n; ++id)
@@ -117,7 +165,7 @@ static void reinit_equilibrium(GridObj *g) {
 }
 
 int main(int argc, char **argv) {
-    std::string out = ".", init_u, init_rho, workdir;
+    std::string out = ".", init_u, init_rho, workdir, markers;
     int steps = 0, dump_every = 0;
     for (int a = 1; a < argc; ++a) {
         std::string k = argv[a];
@@ -131,6 +179,7 @@ int main(int argc, char **argv) {
         else if (k == "--init-u") init_u = next();
         else if (k == "--init-rho") init_rho = next();
         else if (k == "--workdir") workdir = next();
+        else if (k == "--markers") markers = next();
         else { std::fprintf(stderr, "unknown argument %s\n", k.c_str()); return 2; }
     }
     mkdir(out.c_str(), 0755);
@@ -168,6 +217,9 @@ int main(int argc, char **argv) {
     ObjectManager *om = ObjectManager::getInstance(grids);
 #ifdef L_GEOMETRY_FILE
     om->io_readInGeomConfig();
+#endif
+#ifdef L_IBM_ON
+    if (!markers.empty()) inject_markers(om, grids, markers);
 #endif
 #ifdef L_IBM_ON
     om->ibm_initialise();

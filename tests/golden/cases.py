@@ -66,6 +66,16 @@ CASES = {
                          re=120, walls=(F,) * 6),
         regions=[((0.25, 0.25, 0.25), (0.75, 0.75, 0.75)), ((0.375, 0.375, 0.375), (0.625, 0.625, 0.625))],
         steps=(5, 40), store_f=(), store_fields=False),
+    # D2Q9 channel with a rigid IBM cylinder: 64 markers, seeded radii.
+    "ibm_cyl_d2q9": dict(
+        defs=Definitions(dims=2, resolution=32, timestep=1.0 / 800.0, bx=5.0, by=2.0, re=160, ux0=1.0,
+                         ibm=True, walls=(V, X, S, S, F, F)),
+        bodies="cylinder", steps=(5, 100), store_f=(5,)),
+    # D3Q19 channel with a rigid IBM sphere (Fibonacci markers).
+    "ibm_sphere_d3q19": dict(
+        defs=Definitions(dims=3, resolution=16, timestep=1.0 / 400.0, bx=3.0, by=1.5, bz=1.5, re=40, ux0=1.0,
+                         ibm=True, walls=(V, X, S, S, F, F)),
+        bodies="sphere", steps=(5, 50), store_f=()),
     # D2Q9 BGK-Smagorinsky channel.
     "smag_d2q9": dict(
         defs=Definitions(dims=2, resolution=32, timestep=1.0 / 320.0, bx=2.0, by=1.0, re=2000,
@@ -120,3 +130,47 @@ def initial_fields(name: str):
     if name == "kbc_d2q9":
         return {"u": double_shear(N, M, 0.05, 1e-4).reshape(-1)}
     return None
+
+
+def cylinder_markers(cx: float, cy: float, r_lu: float, dh: float, n: int = 64, sigma: float = 0.1,
+                     seed: int = SEED) -> np.ndarray:
+    """n markers at uniform angles 2 pi i / n on radii r_lu + N(0, sigma^2)
+    lattice units (seeded), positions in the reference's length units."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    radii = (r_lu + rng.normal(0.0, sigma, size=n)) * dh
+    th = 2.0 * math.pi * np.arange(n) / n
+    return np.stack([cx + radii * np.cos(th), cy + radii * np.sin(th), np.zeros(n)], axis=1)
+
+
+def fibonacci_sphere(cx: float, cy: float, cz: float, radius: float, n: int) -> np.ndarray:
+    """Fibonacci (golden-angle) layout of n points on a sphere."""
+    inc = math.pi * (3.0 - math.sqrt(5.0))
+    off = 2.0 / n
+    k = np.arange(n)
+    y = k * off - 1.0 + off / 2.0
+    r = np.sqrt(1.0 - y * y)
+    phi = k * inc
+    return np.stack([cx + np.cos(phi) * r * radius, cy + y * radius, cz + np.sin(phi) * r * radius], axis=1)
+
+
+def bodies(name: str):
+    """[(level, region, positions (n, 3))] of the case's rigid IB bodies."""
+    spec = CASES[name]
+    kind = spec.get("bodies")
+    d: Definitions = spec["defs"]
+    dh = 1.0 / d.resolution
+    if kind == "cylinder":
+        return [(0, 0, cylinder_markers(2.0, 1.0, 10.0, dh))]
+    if kind == "sphere":
+        n = int(math.floor(4.0 * math.pi * 0.25 ** 2 / dh ** 2))
+        return [(0, 0, fibonacci_sphere(1.0, 0.75, 0.75, 0.25, n))]
+    return []
+
+
+def write_marker_file(path: str, body_list) -> None:
+    with open(path, "w") as fp:
+        fp.write(f"{len(body_list)}\n")
+        for lev, reg, pos in body_list:
+            fp.write(f"{lev} {reg} {len(pos)}\n")
+            for x, y, z in pos:
+                fp.write(f"{float(x)!r} {float(y)!r} {float(z)!r}\n")

@@ -64,6 +64,11 @@ def run_case(name: str, ref: str) -> str:
         upath = os.path.join(work, "init_u.bin")
         init["u"].astype(np.float64).tofile(upath)
         args += ["--init-u", upath]
+    blist = CASES.bodies(name)
+    if blist:
+        mpath = os.path.join(work, "markers.in")
+        CASES.write_marker_file(mpath, blist)
+        args += ["--markers", mpath]
     # Dump at each requested step: rerun with --dump-every = gcd is wasteful;
     # the harness dumps every `dump-every` steps, so pick the gcd of steps.
     g = 0
@@ -111,6 +116,12 @@ def run_case(name: str, ref: str) -> str:
             out[f"{k}_u_sha_{s}"] = sha(gl["u"])
             out[f"{k}_rho_sha_{s}"] = sha(gl["rho"])
             out[f"{k}_f_sha_{s}"] = sha(gl["f"])
+    if blist:
+        for s in (0,) + tuple(spec["steps"]):
+            mk = np.loadtxt(os.path.join(work, f"s{s}", "markers.txt"), ndmin=2)
+            out[f"markers_{s}"] = mk
+        sup = np.loadtxt(os.path.join(work, "s0", "supports.txt"), ndmin=2)
+        out["supports"] = sup
     with open(os.path.join(work, "timing.txt")) as fp:
         out["ref_timing"] = fp.read()
     np.savez_compressed(os.path.join(HERE, f"{name}.npz"), **out)

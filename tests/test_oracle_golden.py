@@ -83,3 +83,35 @@ def test_known_answer_equilibrium_d2q9():
     n = d.ncell
     f = g.equilibrium(np.tile(u, (n, 1)).reshape(-1), np.full(n, kat["rho"]))
     assert np.allclose(f.reshape(n, 9), np.array(kat["f"])[None, :], atol=0.5e-8, rtol=0)
+
+
+@pytest.mark.parametrize("name", sorted(n for n in CASES.CASES if CASES.CASES[n].get("bodies")))
+def test_oracle_ibm_bit_exact_vs_reference(name):
+    """IBM restatement against the reference: support lists and delta values,
+    marker spacing ds, epsilon (same LU as the reference's oracle build),
+    marker forces and the flow field at every stored step."""
+    spec = CASES.CASES[name]
+    fx = R.fixture(name)
+    grids, levels = R.build_backend(name, lambda d, p: O.OracleGrid(d, p))
+    ibm = O.OracleIBM()
+    for lev, reg, pos in CASES.bodies(name):
+        ibm.add_body(grids[lev], pos)
+    ibm.initialise()
+    mk = ibm.markers(0)
+    ref0 = fx["markers_0"]
+    assert np.array_equal(mk[:, 7], ref0[:, 9]), "ds"
+    assert np.array_equal(mk[:, 6], ref0[:, 8]), "epsilon"
+    assert np.array_equal(mk[:, 8], ref0[:, 14]), "support counts"
+    sup = ibm.supports(0)
+    assert np.array_equal(sup[:, 1:4], fx["supports"][:, 3:6])
+    assert np.array_equal(sup[:, 4], fx["supports"][:, 6])
+    done = 0
+    D = levels[0].defs.dims
+    for s in spec["steps"]:
+        grids[0].step(s - done)
+        done = s
+        st = grids[0].download()
+        assert np.array_equal(st["u"], fx[f"u_{s}"]) and np.array_equal(st["rho"], fx[f"rho_{s}"])
+        assert R.sha(st["f"]) == str(fx[f"f_sha_{s}"])
+        mk = ibm.markers(0)
+        assert np.array_equal(mk[:, 3:3 + D], fx[f"markers_{s}"][:, 5:5 + D]), f"marker force at step {s}"
