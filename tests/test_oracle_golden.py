@@ -44,7 +44,7 @@ def test_host_subgrid_setup_matches_reference(name):
         assert R.sha(f0) == str(fx[f"{k}_f0_sha"]), k
 
 
-@pytest.mark.parametrize("name", sorted(CASES.CASES))
+@pytest.mark.parametrize("name", sorted(n for n in CASES.CASES if not CASES.CASES[n].get("bodies")))
 def test_oracle_bit_exact_vs_reference(name):
     """The restatement reproduces the reference bit for bit (FP64, same
     operation order, no contraction) at every stored step, on every grid."""
