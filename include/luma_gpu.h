@@ -162,6 +162,26 @@ int luma_gpu_synchronize(luma_gpu_grid *root);
 /* ---- reductions / watchdog ----------------------------------------------- */
 int luma_gpu_reduce(luma_gpu_grid *grid, luma_reduction *out);
 
+/* ---- immersed-boundary bodies (grids created with LUMA_FLAG_IBM) -------- */
+/* Adds a rigid body of `nmarkers` Lagrangian markers to the grid that owns
+ * it: positions[3*m + d] in the reference's length units, optional marker
+ * velocities (lattice units, NULL = stationary).  Replaces the body
+ * construction of ObjectManager::io_readInGeomConfig / IBBody
+ * (LUMA src/ObjectManager_ops_io.cpp:322-800, src/IBBody.cpp:58-91). */
+int luma_gpu_ibm_add_body(luma_gpu_grid *grid, int nmarkers, const double *positions,
+                          const double *velocities, int *body_index);
+/* Support stencils, marker spacing and epsilon for every body of the tree:
+ * ObjectManager::ibm_initialise (src/ObjectManager_ops_ibm.cpp:190-246).
+ * Call after all bodies are added and before stepping. */
+int luma_gpu_ibm_initialise(luma_gpu_grid *root);
+/* Per-marker state, 9 doubles per marker: x y z Fx Fy Fz epsilon ds nsupport
+ * (F = the last IBM force of ibm_computeForce, lattice units). */
+int luma_gpu_ibm_get_markers(luma_gpu_grid *grid, int body, double *out);
+/* FP64 sum over a body's markers of F*epsilon*ds (*ds in 3D): the force the
+ * body exerts in lattice units, as io_writeLiftDrag scales it per marker
+ * (src/ObjectManager_ops_io.cpp:65-128) before its physical scaling. */
+int luma_gpu_ibm_body_force(luma_gpu_grid *grid, int body, double force[3]);
+
 #ifdef __cplusplus
 }
 #endif

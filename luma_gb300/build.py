@@ -30,7 +30,7 @@ def nvcc() -> str:
 
 
 def _flags(debug: bool) -> list[str]:
-    f = ["-std=c++17", "-O3", "-lineinfo", *ARCH, "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
+    f = ["-std=c++17", "-O3", "-lineinfo", *ARCH, "-Xcompiler", "-fPIC,-fopenmp", "--expt-relaxed-constexpr",
          "-I", os.path.join(ROOT, "include")]
     if debug:
         f += ["-DLUMA_GPU_CHECKS=1"]
@@ -66,7 +66,7 @@ def build(force: bool = False, debug: bool = False, jobs: int | None = None, ver
     objs = [o for o, _ in res]
     if force or not os.path.exists(LIB) or os.path.getmtime(LIB) < max(os.path.getmtime(o) for o in objs):
         tmp = LIB + f".tmp{os.getpid()}"
-        cmd = [cc, "-shared", *ARCH, "-o", tmp, *objs, "-lcudart"]
+        cmd = [cc, "-shared", *ARCH, "-o", tmp, *objs, "-lcudart", "-lgomp"]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError("luma_gb300 link failed:\n" + r.stderr[-4000:])

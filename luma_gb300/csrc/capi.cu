@@ -17,6 +17,7 @@
 #include <vector>
 
 #include "device.cuh"
+#include "dispatch.hpp"
 #include "grid.hpp"
 #include "kernels.hpp"
 
@@ -42,18 +43,6 @@ int luma_set_error(int code, const char *fmt, ...) {
     } while (0)
 
 namespace {
-
-template <class F>
-cudaError_t dispatch(int Q, int prec, F &&f) {
-    if (prec == LUMA_PREC_FP64) {
-        if (Q == 9) return f(std::integral_constant<int, 9>{}, P64{});
-        if (Q == 19) return f(std::integral_constant<int, 19>{}, P64{});
-        return f(std::integral_constant<int, 27>{}, P64{});
-    }
-    if (Q == 9) return f(std::integral_constant<int, 9>{}, P32{});
-    if (Q == 19) return f(std::integral_constant<int, 19>{}, P32{});
-    return f(std::integral_constant<int, 27>{}, P32{});
-}
 
 size_t real_size(const luma_gpu_grid *g) { return g->d.precision == LUMA_PREC_FP64 ? 8 : 4; }
 
@@ -244,7 +233,7 @@ int step_grid(luma_gpu_grid *g, int subcycle, bool write_macro) {
     }
     StepArgs a = make_args(g, subcycle);
     if (g->ibm && g->ibm->has_bodies) {
-        int rc = luma_ibm_reset_forces(g);
+        int rc = luma_ibm_reset_forces(g, a);
         if (rc) return rc;
     }
     CK(dispatch(d.Q, d.precision, [&](auto q, auto p) {
@@ -398,6 +387,9 @@ int luma_gpu_grid_create(const luma_grid_desc *desc, luma_gpu_grid *parent, luma
     CKF(cudaMalloc(&g->acc, 8 * sizeof(double)));
     rc = build_site_tables(g, d.lattyp, d.xpos, d.ypos, d.zpos);
     if (rc) return fail(rc);
+    if (d.xpos) g->hx.assign(d.xpos, d.xpos + d.N);
+    if (d.ypos) g->hy.assign(d.ypos, d.ypos + d.M);
+    if (d.zpos) g->hz.assign(d.zpos, d.zpos + d.K);
     g->d.lattyp = nullptr;
     g->d.xpos = g->d.ypos = g->d.zpos = nullptr;
     g->d.ux_in = g->d.uy_in = g->d.uz_in = nullptr;

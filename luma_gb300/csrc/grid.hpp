@@ -14,6 +14,8 @@ namespace luma {
 struct IbmState;
 }
 
+struct luma_gpu_grid;
+
 struct luma_gpu_grid {
     luma_grid_desc d{};         // copy of the descriptor (array pointers cleared)
     size_t n = 0;               // sites
@@ -37,18 +39,52 @@ struct luma_gpu_grid {
     std::vector<luma_gpu_grid *> kids;
     cudaStream_t stream = nullptr;
     luma::IbmState *ibm = nullptr;
+    std::vector<double> hx, hy, hz;  // site positions (host copy, for IB support search)
 };
 
 int luma_set_error(int code, const char *fmt, ...);
 
 // ibm.cu
-int luma_ibm_reset_forces(luma_gpu_grid *g);
+int luma_ibm_reset_forces(luma_gpu_grid *g, const luma::StepArgs &a);
 int luma_ibm_apply(luma_gpu_grid *g, const luma::StepArgs &a);
 void luma_ibm_free(luma_gpu_grid *g);
 
 namespace luma {
+
+// One rigid immersed-boundary body on the host: marker state and the
+// support lists built by ibm_findSupport (FP64, reference order).
+struct IbmBody {
+    int nm = 0;
+    std::vector<double> pos, vel, eps, ds, dil, area;  // per marker (pos/vel: 3 per marker)
+    std::vector<int> off;                               // CSR offsets, nm + 1
+    std::vector<int> si, sj, sk;                        // support site indices
+    std::vector<double> sx, sy, sz, delta;              // support positions and delta values
+};
+
+// Device arrays of all bodies owned by one grid, concatenated in body order.
+struct IbmDevice {
+    int nm = 0, nsup = 0, nu = 0;
+    double *vel = nullptr, *eps = nullptr, *ds = nullptr, *area = nullptr;
+    double *F = nullptr, *irho = nullptr, *imom = nullptr;   // per marker (F, imom: 3 per marker)
+    int *moff = nullptr, *msite = nullptr, *smarker = nullptr;
+    double *mdelta = nullptr;
+    int *usite = nullptr, *uoff = nullptr, *uref = nullptr;  // unique support sites -> supports in order
+};
+
 struct IbmState {
     bool has_bodies = false;
     bool has_flexible = false;
+    bool ready = false;
+    std::vector<IbmBody> bodies;
+    IbmDevice dev;
 };
+
+// Marker-side arguments of the IBM kernels.
+struct IbmArgs {
+    int nm, nu, dims;
+    const int *moff, *msite, *smarker, *usite, *uoff, *uref;
+    const double *mdelta, *vel, *eps, *ds, *area;
+    double *F, *irho, *imom;
+};
+
 }

@@ -1,21 +1,375 @@
-// Immersed-boundary pass on a grid (ObjectManager::ibm_apply,
-// LUMA src/ObjectManager_ops_ibm.cpp:33-54).
+// Immersed-boundary bodies and the IBM pass of a grid
+// (ObjectManager::ibm_apply, LUMA src/ObjectManager_ops_ibm.cpp:33-54).
+//
+// Set-up runs once on the host in FP64 for rigid bodies, with the
+// reference's algorithms and order: support search around the enclosing
+// voxel (ibm_findSupport, :279-453) with tensor-product Roma delta values
+// (:255-272, :462-491), marker spacing (ibm_computeDs, :927-981) and the
+// epsilon system (ibm_findEpsilon, :773-920) solved by partial-pivot LU.
+// The per-step pass runs on the device (k_general.cu): one thread per
+// marker interpolates and forms the force; one thread per distinct support
+// site gathers the spread contributions in the reference's order (no
+// atomics) and recomputes the macroscopic values there.
 #include <cuda_runtime.h>
 
-#include "grid.hpp"
+#include <cmath>
+#include <cstring>
+#include <vector>
 
-int luma_ibm_reset_forces(luma_gpu_grid *g) {
-    (void)g;
+#include "dispatch.hpp"
+#include "grid.hpp"
+#include "kernels.hpp"
+
+using namespace luma;
+
+namespace {
+
+double delta_kernel(double radius, double dilation) {
+    const double mag_r = std::fabs(radius) / dilation;
+    if (mag_r > 1.5) return 0.0;
+    if (mag_r > 0.5) return (5.0 - (3.0 * mag_r) - std::sqrt(-3.0 * std::pow(1.0 - mag_r, 2) + 1.0)) / 6.0;
+    return (1.0 + std::sqrt(1.0 - 3.0 * std::pow(mag_r, 2))) / 3.0;
+}
+
+const luma_gpu_grid *root_of(const luma_gpu_grid *g) {
+    while (g->parent) g = g->parent;
+    return g;
+}
+
+double grid_start(const luma_gpu_grid *g, int axis) {
+    const std::vector<double> &p = axis == 0 ? g->hx : (axis == 1 ? g->hy : g->hz);
+    return g->d.level == 0 ? 0.0 : p[0] - g->d.dh / 2.0;
+}
+
+void support_delta(const luma_gpu_grid *g, const IbmBody &b, int m, const double est[3], double *out) {
+    const double dh = g->d.dh;
+    const double *x = &b.pos[3 * m];
+    double v = delta_kernel((est[0] - x[0]) / dh, b.dil[m]) * delta_kernel((est[1] - x[1]) / dh, b.dil[m]);
+    if (g->d.dims == 3) v = v * delta_kernel((est[2] - x[2]) / dh, b.dil[m]);
+    *out = v;
+}
+
+int find_support(const luma_gpu_grid *g, IbmBody &b) {
+    const int D = g->d.dims;
+    const double dh = g->d.dh;
+    const double *E = root_of(g)->d.global_edges;
+    b.off.assign(b.nm + 1, 0);
+    b.si.clear(); b.sj.clear(); b.sk.clear();
+    b.sx.clear(); b.sy.clear(); b.sz.clear(); b.delta.clear();
+    auto push = [&](int i, int j, int k, const double p[3], int m) {
+        b.si.push_back(i); b.sj.push_back(j); b.sk.push_back(k);
+        b.sx.push_back(p[0]); b.sy.push_back(p[1]); b.sz.push_back(p[2]);
+        double dv;
+        support_delta(g, b, m, p, &dv);
+        b.delta.push_back(dv);
+    };
+    for (int m = 0; m < b.nm; ++m) {
+        b.off[m] = (int)b.si.size();
+        const double *x = &b.pos[3 * m];
+        const int in = (int)std::floor((x[0] - grid_start(g, 0)) / dh);
+        const int jn = (int)std::floor((x[1] - grid_start(g, 1)) / dh);
+        const int kn = D == 3 ? (int)std::floor((x[2] - grid_start(g, 2)) / dh) : 0;
+        if (in < 0 || jn < 0 || kn < 0 || in >= g->d.N || jn >= g->d.M || kn >= g->d.K)
+            return luma_set_error(LUMA_E_DOMAIN, "IB marker %d is no longer inside its grid", m);
+        const double near[3] = {g->hx[in], g->hy[jn], D == 3 ? g->hz[kn] : 0.0};
+        push(in, jn, kn, near, m);
+        for (int i = in - 5; i <= in + 5; i++)
+            for (int j = jn - 5; j <= jn + 5; j++)
+                for (int k = (D == 3 ? kn - 5 : 0); k <= (D == 3 ? kn + 5 : 0); k++) {
+                    double est[3] = {near[0] + (i - in) * dh, near[1] + (j - jn) * dh, near[2]};
+                    if (D == 3) est[2] = near[2] + (k - kn) * dh;
+                    const bool in_cage = (std::fabs(x[0] - est[0]) / dh < 1.5 * b.dil[m]) &&
+                                         (std::fabs(x[1] - est[1]) / dh < 1.5 * b.dil[m]) &&
+                                         (D == 2 || std::fabs(x[2] - est[2]) / dh < 1.5 * b.dil[m]);
+                    const bool in_domain = !(est[0] < E[0] || est[0] > E[1] || est[1] < E[2] || est[1] > E[3] ||
+                                             (D == 3 && (est[2] < E[4] || est[2] > E[5])));
+                    if (in_cage && in_domain && (i != in || j != jn || (D == 3 && k != kn))) {
+                        if (i < 0 || j < 0 || k < 0 || i >= g->d.N || j >= g->d.M || k >= g->d.K)
+                            return luma_set_error(LUMA_E_DOMAIN, "IB marker %d has supports off its grid", m);
+                        push(i, j, k, est, m);
+                    }
+                }
+    }
+    b.off[b.nm] = (int)b.si.size();
     return LUMA_OK;
 }
 
-int luma_ibm_apply(luma_gpu_grid *g, const luma::StepArgs &a) {
-    (void)g;
-    (void)a;
+void compute_ds(const luma_gpu_grid *g, IbmBody &b) {
+    const double dh = g->d.dh;
+    for (int m = 0; m < b.nm; ++m) {
+        double ds = 10.0;
+        for (int n = 0; n < b.nm; ++n) {
+            if (n == m) continue;
+            double r = 0.0;
+            for (int d = 0; d < 3; ++d) r += std::pow(b.pos[3 * m + d] - b.pos[3 * n + d], 2);
+            const double dist = std::sqrt(r) / dh;
+            if (dist < ds) ds = dist;
+        }
+        b.ds[m] = ds;
+    }
+}
+
+// Dense LU with partial pivoting, column-major, then the transposed solve
+// (the reference calls dgetrf_/dgetrs_ with trans='T' on a row-major copy,
+// which solves A x = b).  The column updates of one elimination step are
+// independent, so they run on all host threads without changing a single
+// floating-point operation.
+void lu_solve_transposed(int n, std::vector<double> &a, std::vector<double> &x) {
+    std::vector<int> ipiv(n);
+#define A_(r, c) a[(size_t)(c) * n + (r)]
+    for (int k = 0; k < n; ++k) {
+        int p = k;
+        double best = std::fabs(A_(k, k));
+        for (int r = k + 1; r < n; ++r) {
+            const double v = std::fabs(A_(r, k));
+            if (v > best) { best = v; p = r; }
+        }
+        ipiv[k] = p + 1;
+        if (A_(p, k) == 0.0) continue;
+        if (p != k)
+            for (int c = 0; c < n; ++c) std::swap(A_(k, c), A_(p, c));
+        const double inv = 1.0 / A_(k, k);
+        for (int r = k + 1; r < n; ++r) A_(r, k) *= inv;
+#pragma omp parallel for schedule(static) if (n - k > 256)
+        for (int c = k + 1; c < n; ++c) {
+            const double akc = A_(k, c);
+            if (akc == 0.0) continue;
+            for (int r = k + 1; r < n; ++r) A_(r, c) -= A_(r, k) * akc;
+        }
+    }
+    for (int r = 0; r < n; ++r) { double s = x[r]; for (int c = 0; c < r; ++c) s -= A_(c, r) * x[c]; x[r] = s / A_(r, r); }
+    for (int r = n - 1; r >= 0; --r) { double s = x[r]; for (int c = r + 1; c < n; ++c) s -= A_(c, r) * x[c]; x[r] = s; }
+    for (int k = n - 1; k >= 0; --k) { const int p = ipiv[k] - 1; if (p != k) std::swap(x[k], x[p]); }
+#undef A_
+}
+
+void find_epsilon(const luma_gpu_grid *g, IbmBody &b) {
+    const int n = b.nm, D = g->d.dims;
+    const double dh = g->d.dh;
+    std::vector<double> A((size_t)n * n, 0.0);  // row-major A[I][J]
+#pragma omp parallel for schedule(dynamic, 16) if (n > 256)
+    for (int I = 0; I < n; ++I)
+        for (int J = 0; J < n; ++J) {
+            double aij = 0.0;
+            for (int s = b.off[I]; s < b.off[I + 1]; ++s) {
+                const double dI = b.delta[s];
+                double dJ = delta_kernel((b.pos[3 * J + 0] - b.sx[s]) / dh, b.dil[J]) *
+                            delta_kernel((b.pos[3 * J + 1] - b.sy[s]) / dh, b.dil[J]);
+                if (D == 3) dJ = dJ * delta_kernel((b.pos[3 * J + 2] - b.sz[s]) / dh, b.dil[J]);
+                aij += dI * dJ * b.area[I];
+            }
+            A[(size_t)I * n + J] = aij * b.ds[J];
+        }
+    std::vector<double> x(n, 1.0);
+    lu_solve_transposed(n, A, x);
+    for (int m = 0; m < n; ++m) b.eps[m] = x[m];
+}
+
+template <class T>
+int dalloc_copy(T **dst, const std::vector<T> &src) {
+    cudaFree(*dst);
+    *dst = nullptr;
+    const size_t bytes = std::max<size_t>(1, src.size()) * sizeof(T);
+    if (cudaMalloc(dst, bytes) != cudaSuccess) return luma_set_error(LUMA_E_NOMEM, "IBM device allocation failed");
+    if (!src.empty() && cudaMemcpy(*dst, src.data(), src.size() * sizeof(T), cudaMemcpyHostToDevice) != cudaSuccess)
+        return luma_set_error(LUMA_E_CUDA, "IBM upload failed");
+    return LUMA_OK;
+}
+
+void free_device(IbmDevice &d) {
+    cudaFree(d.vel); cudaFree(d.eps); cudaFree(d.ds); cudaFree(d.area);
+    cudaFree(d.F); cudaFree(d.irho); cudaFree(d.imom);
+    cudaFree(d.moff); cudaFree(d.msite); cudaFree(d.smarker); cudaFree(d.mdelta);
+    cudaFree(d.usite); cudaFree(d.uoff); cudaFree(d.uref);
+    d = IbmDevice();
+}
+
+// Concatenate the grid's bodies and build the site-major view of the supports.
+int upload_bodies(luma_gpu_grid *g) {
+    IbmState &st = *g->ibm;
+    std::vector<double> vel, eps, ds, area, mdelta;
+    std::vector<int> moff(1, 0), msite, smarker;
+    int mbase = 0;
+    for (const IbmBody &b : st.bodies) {
+        for (int m = 0; m < b.nm; ++m) {
+            for (int d = 0; d < 3; ++d) vel.push_back(b.vel[3 * m + d]);
+            eps.push_back(b.eps[m]);
+            ds.push_back(b.ds[m]);
+            area.push_back(b.area[m]);
+            for (int s = b.off[m]; s < b.off[m + 1]; ++s) {
+                msite.push_back(b.sk[s] + b.sj[s] * g->d.K + b.si[s] * g->d.K * g->d.M);
+                mdelta.push_back(b.delta[s]);
+                smarker.push_back(mbase + m);
+            }
+            moff.push_back((int)msite.size());
+        }
+        mbase += b.nm;
+    }
+    const int nsup = (int)msite.size();
+    // distinct sites in first-appearance order, each with its supports in order
+    std::vector<int> usite, uoff, uref, first(g->n, -1), count;
+    for (int s = 0; s < nsup; ++s) {
+        const int id = msite[s];
+        if (first[id] < 0) {
+            first[id] = (int)usite.size();
+            usite.push_back(id);
+            count.push_back(0);
+        }
+        count[first[id]]++;
+    }
+    uoff.assign(usite.size() + 1, 0);
+    for (size_t u = 0; u < usite.size(); ++u) uoff[u + 1] = uoff[u] + count[u];
+    uref.assign(nsup, 0);
+    std::vector<int> fill(usite.size(), 0);
+    for (int s = 0; s < nsup; ++s) {
+        const int u = first[msite[s]];
+        uref[uoff[u] + fill[u]++] = s;
+    }
+    IbmDevice &dv = st.dev;
+    free_device(dv);
+    int rc;
+    if ((rc = dalloc_copy(&dv.vel, vel)) || (rc = dalloc_copy(&dv.eps, eps)) || (rc = dalloc_copy(&dv.ds, ds)) ||
+        (rc = dalloc_copy(&dv.area, area)) || (rc = dalloc_copy(&dv.mdelta, mdelta)) ||
+        (rc = dalloc_copy(&dv.moff, moff)) || (rc = dalloc_copy(&dv.msite, msite)) ||
+        (rc = dalloc_copy(&dv.smarker, smarker)) || (rc = dalloc_copy(&dv.usite, usite)) ||
+        (rc = dalloc_copy(&dv.uoff, uoff)) || (rc = dalloc_copy(&dv.uref, uref)))
+        return rc;
+    std::vector<double> zeros3(3 * (size_t)mbase, 0.0), zeros1(mbase, 0.0);
+    if ((rc = dalloc_copy(&dv.F, zeros3)) || (rc = dalloc_copy(&dv.imom, zeros3)) || (rc = dalloc_copy(&dv.irho, zeros1)))
+        return rc;
+    dv.nm = mbase;
+    dv.nsup = nsup;
+    dv.nu = (int)usite.size();
+    return LUMA_OK;
+}
+
+IbmArgs make_ibm_args(const luma_gpu_grid *g) {
+    const IbmDevice &d = g->ibm->dev;
+    IbmArgs b;
+    b.nm = d.nm; b.nu = d.nu; b.dims = g->d.dims;
+    b.moff = d.moff; b.msite = d.msite; b.smarker = d.smarker;
+    b.usite = d.usite; b.uoff = d.uoff; b.uref = d.uref;
+    b.mdelta = d.mdelta; b.vel = d.vel; b.eps = d.eps; b.ds = d.ds; b.area = d.area;
+    b.F = d.F; b.irho = d.irho; b.imom = d.imom;
+    return b;
+}
+
+int init_tree(luma_gpu_grid *g) {
+    if (g->ibm && g->ibm->has_bodies) {
+        IbmState &st = *g->ibm;
+        for (IbmBody &b : st.bodies) {
+            int rc = find_support(g, b);
+            if (rc) return rc;
+        }
+        for (IbmBody &b : st.bodies) compute_ds(g, b);
+        for (IbmBody &b : st.bodies) find_epsilon(g, b);
+        int rc = upload_bodies(g);
+        if (rc) return rc;
+        st.ready = true;
+    }
+    for (luma_gpu_grid *c : g->kids) {
+        int rc = init_tree(c);
+        if (rc) return rc;
+    }
+    return LUMA_OK;
+}
+
+}  // namespace
+
+int luma_ibm_reset_forces(luma_gpu_grid *g, const StepArgs &a) {
+    if (!g->force) return luma_set_error(LUMA_E_STATE, "IB bodies on a grid without a force field");
+    const luma_grid_desc &d = g->d;
+    cudaError_t e = d.precision == LUMA_PREC_FP64
+                        ? launch_reset_forces<P64>(a, d.dims, d.gravity, d.gravity_dir, d.refinement_ratio, g->stream)
+                        : launch_reset_forces<P32>(a, d.dims, d.gravity, d.gravity_dir, d.refinement_ratio, g->stream);
+    if (e != cudaSuccess) return luma_set_error(LUMA_E_CUDA, "reset forces: %s", cudaGetErrorString(e));
+    return LUMA_OK;
+}
+
+int luma_ibm_apply(luma_gpu_grid *g, const StepArgs &a) {
+    if (!g->ibm->ready) return luma_set_error(LUMA_E_STATE, "luma_gpu_ibm_initialise was not called");
+    const IbmArgs b = make_ibm_args(g);
+    cudaError_t e = dispatch(g->d.Q, g->d.precision, [&](auto q, auto p) {
+        return launch_ibm_pass<decltype(q)::value, decltype(p)>(a, b, g->stream);
+    });
+    if (e != cudaSuccess) return luma_set_error(LUMA_E_CUDA, "IBM pass: %s", cudaGetErrorString(e));
     return LUMA_OK;
 }
 
 void luma_ibm_free(luma_gpu_grid *g) {
+    if (g->ibm) free_device(g->ibm->dev);
     delete g->ibm;
     g->ibm = nullptr;
 }
+
+extern "C" {
+
+int luma_gpu_ibm_add_body(luma_gpu_grid *g, int nmarkers, const double *positions, const double *velocities,
+                          int *body_index) {
+    if (!g || !positions || nmarkers <= 0) return luma_set_error(LUMA_E_INVALID, "bad IB body arguments");
+    if (!(g->d.flags & LUMA_FLAG_IBM))
+        return luma_set_error(LUMA_E_INVALID, "IB bodies need a grid created with LUMA_FLAG_IBM");
+    if (g->hx.empty() || g->hy.empty() || g->hz.empty())
+        return luma_set_error(LUMA_E_INVALID, "IB bodies need the grid's site positions");
+    if (!g->ibm) g->ibm = new IbmState();
+    IbmBody b;
+    b.nm = nmarkers;
+    b.pos.assign(positions, positions + 3 * (size_t)nmarkers);
+    if (velocities) b.vel.assign(velocities, velocities + 3 * (size_t)nmarkers);
+    else b.vel.assign(3 * (size_t)nmarkers, 0.0);
+    b.eps.assign(nmarkers, 0.0);
+    b.ds.assign(nmarkers, 1.0);
+    b.dil.assign(nmarkers, 1.0);
+    b.area.assign(nmarkers, 1.0);
+    g->ibm->bodies.push_back(b);
+    g->ibm->has_bodies = true;
+    g->ibm->ready = false;
+    if (body_index) *body_index = (int)g->ibm->bodies.size() - 1;
+    return LUMA_OK;
+}
+
+int luma_gpu_ibm_initialise(luma_gpu_grid *root) {
+    if (!root) return luma_set_error(LUMA_E_INVALID, "null grid");
+    return init_tree(root);
+}
+
+int luma_gpu_ibm_get_markers(luma_gpu_grid *g, int body, double *out) {
+    if (!g || !out) return luma_set_error(LUMA_E_INVALID, "null argument");
+    if (!g->ibm || body < 0 || body >= (int)g->ibm->bodies.size())
+        return luma_set_error(LUMA_E_INVALID, "no IB body %d on this grid", body);
+    const IbmState &st = *g->ibm;
+    int base = 0;
+    for (int b = 0; b < body; ++b) base += st.bodies[b].nm;
+    const IbmBody &bd = st.bodies[body];
+    std::vector<double> F(3 * (size_t)bd.nm, 0.0);
+    if (st.ready && cudaMemcpy(F.data(), st.dev.F + 3 * (size_t)base, F.size() * sizeof(double),
+                               cudaMemcpyDeviceToHost) != cudaSuccess)
+        return luma_set_error(LUMA_E_CUDA, "marker force download failed");
+    for (int m = 0; m < bd.nm; ++m) {
+        double *o = out + 9 * (size_t)m;
+        o[0] = bd.pos[3 * m]; o[1] = bd.pos[3 * m + 1]; o[2] = bd.pos[3 * m + 2];
+        o[3] = F[3 * m]; o[4] = F[3 * m + 1]; o[5] = g->d.dims == 3 ? F[3 * m + 2] : 0.0;
+        o[6] = bd.eps[m]; o[7] = bd.ds[m];
+        o[8] = bd.off.empty() ? 0.0 : double(bd.off[m + 1] - bd.off[m]);
+    }
+    return LUMA_OK;
+}
+
+int luma_gpu_ibm_body_force(luma_gpu_grid *g, int body, double force[3]) {
+    if (!g || !force) return luma_set_error(LUMA_E_INVALID, "null argument");
+    if (!g->ibm || body < 0 || body >= (int)g->ibm->bodies.size())
+        return luma_set_error(LUMA_E_INVALID, "no IB body %d on this grid", body);
+    const IbmBody &bd = g->ibm->bodies[body];
+    std::vector<double> m(9 * (size_t)bd.nm);
+    int rc = luma_gpu_ibm_get_markers(g, body, m.data());
+    if (rc) return rc;
+    force[0] = force[1] = force[2] = 0.0;
+    for (int k = 0; k < bd.nm; ++k) {
+        const double *o = &m[9 * (size_t)k];
+        const double volDepth = g->d.dims == 3 ? o[7] : 1.0;
+        for (int d = 0; d < g->d.dims; ++d) force[d] += o[3 + d] * o[6] * volDepth * o[7];
+    }
+    return LUMA_OK;
+}
+
+}  // extern "C"

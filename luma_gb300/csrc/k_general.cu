@@ -19,6 +19,7 @@
 #include <cuda_runtime.h>
 
 #include "device.cuh"
+#include "grid.hpp"
 #include "kernels.hpp"
 
 namespace luma {
@@ -563,7 +564,103 @@ __global__ void __launch_bounds__(128) k_force_collide(StepArgs a) {
     for (int v = 0; v < Q; ++v) st<P>(a.fNew, (size_t)v * n + id, fn[v]);
 }
 
+// ---- immersed boundary pass (ObjectManager::ibm_apply, src/ObjectManager_ops_ibm.cpp:33-54) ----
+
+// ibm_interpolate (:498-591) + ibm_computeForce (:598-614), one thread per
+// marker, FP64 marker arithmetic in the reference's order.
+template <int Q, class P>
+__global__ void k_ibm_interp_force(StepArgs a, IbmArgs b) {
+    constexpr int D = Lattice<Q>::D;
+    const int m = blockIdx.x * blockDim.x + threadIdx.x;
+    if (m >= b.nm) return;
+    const size_t n = (size_t)a.ncell;
+    double r = 0.0, mom[3] = {0.0, 0.0, 0.0};
+    const double A = b.area[m];
+    for (int s = b.moff[m]; s < b.moff[m + 1]; ++s) {
+        const int id = b.msite[s];
+        const double rs = double(ldr<P>(a.rho, id));
+        const double dl = b.mdelta[s];
+        r += rs * dl * A;
+        for (int d = 0; d < D; ++d) mom[d] += rs * double(ldr<P>(a.u, (size_t)d * n + id)) * dl * A;
+    }
+    b.irho[m] = r;
+    for (int d = 0; d < D; ++d) {
+        b.imom[3 * m + d] = mom[d];
+        b.F[3 * m + d] = 2.0 * (mom[d] - r * b.vel[3 * m + d]) / 1.0;
+    }
+}
+
+// ibm_spread (:621-689) as a gather: one thread per distinct support site
+// applies every (marker, support) contribution to it in the reference's
+// (body, marker, support) order, so no atomics and a deterministic sum.
+template <int Q, class P>
+__global__ void k_ibm_spread(StepArgs a, IbmArgs b) {
+    constexpr int D = Lattice<Q>::D;
+    const int u = blockIdx.x * blockDim.x + threadIdx.x;
+    if (u >= b.nu) return;
+    const size_t n = (size_t)a.ncell;
+    const int id = b.usite[u];
+    double f[3];
+    for (int d = 0; d < D; ++d) f[d] = double(ldr<P>(a.force, (size_t)d * n + id));
+    for (int q = b.uoff[u]; q < b.uoff[u + 1]; ++q) {
+        const int s = b.uref[q];
+        const int m = b.smarker[s];
+        const double volWidth = b.eps[m];
+        const double volDepth = D == 3 ? b.ds[m] : 1.0;
+        for (int d = 0; d < D; ++d) f[d] -= b.mdelta[s] * b.F[3 * m + d] * volWidth * volDepth * b.ds[m];
+    }
+    for (int d = 0; d < D; ++d) str<P>(const_cast<void *>(a.force), (size_t)d * n + id, typename P::R(f[d]));
+}
+
+// ibm_updateMacroscopic (:696-766): the macroscopic step again at every
+// support site, now with the spread force.
+template <int Q, class P>
+__global__ void k_ibm_remacro(StepArgs a, IbmArgs b) {
+    using R = typename P::R;
+    const int u = blockIdx.x * blockDim.x + threadIdx.x;
+    if (u >= b.nu) return;
+    const size_t n = (size_t)a.ncell;
+    const int id = b.usite[u];
+    const int k = id % a.K, j = (id / a.K) % a.M, i = id / (a.K * a.M);
+    const int type = a.typ[id];
+    R fn[Q];
+#pragma unroll
+    for (int v = 0; v < Q; ++v) fn[v] = ld<P>(a.fNew, (size_t)v * n + id);
+    R rho, drho, ux, uy, uz;
+    macro_site<Q, P>(a, i, j, k, id, type, fn, rho, drho, ux, uy, uz);
+}
+
+// _LBM_resetForces (:1327-1337): zero the force field, or, under gravity,
+// set only the gravity component to rho*g*refinement_ratio (the other
+// components keep their values, as in the reference).
+template <class P>
+__global__ void k_reset_forces(StepArgs a, int dims, double gravity, int gdir, double rr) {
+    const size_t id = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (id >= (size_t)a.ncell) return;
+    const size_t n = (size_t)a.ncell;
+    if (a.flags & LUMA_FLAG_GRAVITY) {
+        str<P>(const_cast<void *>(a.force), (size_t)gdir * n + id,
+               typename P::R(double(ldr<P>(a.rho, id)) * gravity * rr));
+    } else {
+        for (int d = 0; d < dims; ++d) str<P>(const_cast<void *>(a.force), (size_t)d * n + id, typename P::R(0));
+    }
+}
+
 }  // namespace
+
+template <int Q, class P>
+cudaError_t launch_ibm_pass(const StepArgs &a, const IbmArgs &b, cudaStream_t s) {
+    if (b.nm <= 0) return cudaSuccess;
+    k_ibm_interp_force<Q, P><<<(b.nm + 127) / 128, 128, 0, s>>>(a, b);
+    k_ibm_spread<Q, P><<<(b.nu + 127) / 128, 128, 0, s>>>(a, b);
+    k_ibm_remacro<Q, P><<<(b.nu + 127) / 128, 128, 0, s>>>(a, b);
+    return cudaGetLastError();
+}
+template <class P>
+cudaError_t launch_reset_forces(const StepArgs &a, int dims, double gravity, int gdir, double rr, cudaStream_t s) {
+    k_reset_forces<P><<<(a.ncell + 255) / 256, 256, 0, s>>>(a, dims, gravity, gdir, rr);
+    return cudaGetLastError();
+}
 
 template <int Q, class P>
 cudaError_t launch_general_phaseA(const StepArgs &a, const int8_t *wall, cudaStream_t s) {
@@ -610,6 +707,15 @@ LUMA_INST(27, P64)
 LUMA_INST(9, P32)
 LUMA_INST(19, P32)
 LUMA_INST(27, P32)
+#define LUMA_INST_IBM(Q, P) template cudaError_t launch_ibm_pass<Q, P>(const StepArgs &, const IbmArgs &, cudaStream_t);
+LUMA_INST_IBM(9, P64)
+LUMA_INST_IBM(19, P64)
+LUMA_INST_IBM(27, P64)
+LUMA_INST_IBM(9, P32)
+LUMA_INST_IBM(19, P32)
+LUMA_INST_IBM(27, P32)
+template cudaError_t launch_reset_forces<P64>(const StepArgs &, int, double, int, double, cudaStream_t);
+template cudaError_t launch_reset_forces<P32>(const StepArgs &, int, double, int, double, cudaStream_t);
 template cudaError_t launch_velocity_u<P64>(const StepArgs &, int, const int2 *, int, cudaStream_t);
 template cudaError_t launch_velocity_u<P32>(const StepArgs &, int, const int2 *, int, cudaStream_t);
 

@@ -50,6 +50,10 @@ def lib() -> C.CDLL:
         L.luma_gpu_step.argtypes = [vp, C.c_int]
         L.luma_gpu_synchronize.argtypes = [vp]
         L.luma_gpu_reduce.argtypes = [vp, C.POINTER(A.Reduction)]
+        L.luma_gpu_ibm_add_body.argtypes = [vp, C.c_int, dp, dp, C.POINTER(C.c_int)]
+        L.luma_gpu_ibm_initialise.argtypes = [vp]
+        L.luma_gpu_ibm_get_markers.argtypes = [vp, C.c_int, dp]
+        L.luma_gpu_ibm_body_force.argtypes = [vp, C.c_int, dp]
         if L.luma_gpu_abi_version() != A.ABI_VERSION:
             raise RuntimeError("luma_gb300 library ABI version mismatch")
         _lib = L
@@ -126,3 +130,25 @@ class GpuGrid:
         check(self.L.luma_gpu_reduce(self.h, C.byref(r)))
         return {"mass": r.mass, "momentum": tuple(r.momentum), "kinetic_energy": r.kinetic_energy,
                 "max_speed": r.max_speed, "nonfinite": r.nonfinite}
+
+    # ---- immersed-boundary bodies ----
+    def ibm_add_body(self, positions, velocities=None) -> int:
+        pos = np.ascontiguousarray(positions, dtype=np.float64).reshape(-1, 3)
+        vel = None if velocities is None else np.ascontiguousarray(velocities, dtype=np.float64).reshape(-1, 3)
+        idx = C.c_int()
+        check(self.L.luma_gpu_ibm_add_body(self.h, pos.shape[0], A.dptr(pos), A.dptr(vel), C.byref(idx)))
+        self._nm = getattr(self, "_nm", []) + [pos.shape[0]]
+        return idx.value
+
+    def ibm_initialise(self):
+        check(self.L.luma_gpu_ibm_initialise(self.h))
+
+    def ibm_markers(self, body: int) -> np.ndarray:
+        out = np.empty((self._nm[body], 9))
+        check(self.L.luma_gpu_ibm_get_markers(self.h, body, A.dptr(out)))
+        return out
+
+    def ibm_body_force(self, body: int) -> np.ndarray:
+        out = np.zeros(3)
+        check(self.L.luma_gpu_ibm_body_force(self.h, body, A.dptr(out)))
+        return out

@@ -110,3 +110,46 @@ def test_reduce_mass_momentum():
     u = st["u"].reshape(-1, 3)
     mom = (st["rho"][:, None] * u).sum(axis=0)
     assert np.allclose(red["momentum"], mom, rtol=0, atol=1e-12 * l0.ncell)
+
+
+@pytest.mark.parametrize("name", sorted(n for n in CASES.CASES if CASES.CASES[n].get("bodies")))
+@pytest.mark.parametrize("prec", [A.PREC_FP64, A.PREC_FP32_SHIFTED])
+def test_ibm_matches_oracle(name, prec):
+    """Rigid IB bodies: supports/epsilon/ds from the host set-up equal the
+    oracle's (bit-exact); marker forces and fields after the stored steps
+    match at 1e-10 (FP64) or within the FP32 bounds."""
+    spec = CASES.CASES[name]
+    fx = R.fixture(name)
+    gg, levels = R.build_backend(name, make_gpu, prec)
+    oo, _ = R.build_backend(name, make_oracle)
+    oibm = O.OracleIBM()
+    for lev, reg, pos in CASES.bodies(name):
+        gg[lev].ibm_add_body(pos)
+        oibm.add_body(oo[lev], pos)
+    gg[0].ibm_initialise()
+    oibm.initialise()
+    gm, om = gg[0].ibm_markers(0), oibm.markers(0)
+    assert np.array_equal(gm[:, 6:9], om[:, 6:9])
+    assert np.array_equal(gm[:, 6], fx["markers_0"][:, 8])
+    done = 0
+    D = levels[0].defs.dims
+    for s in spec["steps"]:
+        gg[0].step(s - done)
+        oo[0].step(s - done)
+        done = s
+        gs, os_ = gg[0].download(), oo[0].download()
+        gm, om = gg[0].ibm_markers(0), oibm.markers(0)
+        ef = rel_l2(gm[:, 3:3 + D], om[:, 3:3 + D])
+        eu = rel_l2(gs["u"], os_["u"])
+        if prec == A.PREC_FP64:
+            assert eu <= 1e-10 and rel_l2(gs["f"], os_["f"]) <= 1e-10, (name, s, eu)
+            assert ef <= 1e-9, (name, s, ef)
+            assert rel_l2(gs["u"], fx[f"u_{s}"]) <= 1e-10
+        else:
+            assert eu <= 2e-4, (name, s, eu)
+            assert ef <= 1e-3, (name, s, ef)
+    tot = gg[0].ibm_body_force(0)
+    mk = gg[0].ibm_markers(0)
+    vd = mk[:, 7] if D == 3 else 1.0
+    ref = (mk[:, 3:3 + D] * (mk[:, 6] * vd * mk[:, 7])[:, None]).sum(axis=0)
+    assert np.allclose(tot[:D], ref, rtol=1e-12, atol=0)
