@@ -30,7 +30,7 @@ def nvcc() -> str:
 
 
 def _flags(debug: bool) -> list[str]:
-    f = ["-std=c++17", "-O3", "-lineinfo", *ARCH, "-Xcompiler", "-fPIC,-fopenmp", "--expt-relaxed-constexpr",
+    f = ["-std=c++17", "-O3", "-lineinfo", *ARCH, "-Xcompiler", "-fPIC,-fopenmp,-ffp-contract=off", "--expt-relaxed-constexpr",
          "-I", os.path.join(ROOT, "include")]
     if debug:
         f += ["-DLUMA_GPU_CHECKS=1"]
