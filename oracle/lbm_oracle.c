@@ -945,14 +945,24 @@ static void find_epsilon(ibm_body *b) {
     free(A); free(ipiv); free(x);
 }
 
-static void ibm_pass(oracle_grid *g, void *vctx) {
-    ibm_ctx *c = (ibm_ctx *)vctx;
+static void fem_move_bodies(oracle_grid *g, ibm_ctx *c);
+static void fem_free_all(void);
+static double fem_check_vel_diff(oracle_grid *g);
+static void fem_commit_start_of_step(oracle_grid *g);
+static int grid_has_flexible(oracle_grid *g);
+
+static void ibm_apply(oracle_grid *g, ibm_ctx *c, int dosub);
+
+static void ibm_pass(oracle_grid *g, void *vctx) { ibm_apply(g, (ibm_ctx *)vctx, 1); }
+
+static void ibm_apply(oracle_grid *g, ibm_ctx *c, int dosub) {
     const int D = g->D;
     const int K = g->d.K, M = g->d.M;
+    /* interpolate (all bodies), then force, then spread, then macro: the
+     * four passes of ibm_apply each run over every body of the grid. */
     for (int ib = 0; ib < c->nb; ++ib) {
         ibm_body *b = &c->b[ib];
         if (b->owner != g) continue;
-        /* interpolate + force */
         for (int m = 0; m < b->nm; ++m) {
             double r = 0.0, mom[3] = {0.0, 0.0, 0.0};
             for (int s = b->off[m]; s < b->off[m + 1]; ++s) {
@@ -963,10 +973,19 @@ static void ibm_pass(oracle_grid *g, void *vctx) {
             b->irho[m] = r;
             for (int d = 0; d < D; d++) {
                 b->imom[3 * m + d] = mom[d];
-                b->F[3 * m + d] = 2.0 * (mom[d] - r * b->vel[3 * m + d]) / 1.0;
             }
         }
-        /* spread */
+    }
+    for (int ib = 0; ib < c->nb; ++ib) {
+        ibm_body *b = &c->b[ib];
+        if (b->owner != g) continue;
+        for (int m = 0; m < b->nm; ++m)
+            for (int d = 0; d < D; d++)
+                b->F[3 * m + d] = 2.0 * (b->imom[3 * m + d] - b->irho[m] * b->vel[3 * m + d]) / 1.0;
+    }
+    for (int ib = 0; ib < c->nb; ++ib) {
+        ibm_body *b = &c->b[ib];
+        if (b->owner != g) continue;
         for (int m = 0; m < b->nm; ++m)
             for (int s = b->off[m]; s < b->off[m + 1]; ++s) {
                 const size_t id = (size_t)b->sk[s] + (size_t)b->sj[s] * K + (size_t)b->si[s] * K * M;
@@ -975,12 +994,29 @@ static void ibm_pass(oracle_grid *g, void *vctx) {
                 for (int d = 0; d < D; d++)
                     g->force_xyz[d + id * D] -= b->delta[s] * b->F[3 * m + d] * volWidth * volDepth * b->ds[m];
             }
-        /* macroscopic update at the supports */
+    }
+    for (int ib = 0; ib < c->nb; ++ib) {
+        ibm_body *b = &c->b[ib];
+        if (b->owner != g) continue;
         for (int m = 0; m < b->nm; ++m)
             for (int s = b->off[m]; s < b->off[m + 1]; ++s) {
                 const int id = b->sk[s] + b->sj[s] * K + b->si[s] * K * M;
                 macro_site(g, b->si[s], b->sj[s], b->sk[s], id, g->typ[id]);
             }
+    }
+    if (grid_has_flexible(g)) fem_move_bodies(g, c);
+    if (dosub && grid_has_flexible(g)) {
+        /* ObjectManager::ibm_subIterate (:111-185) */
+        double res;
+        int it = 0;
+        do {
+            memcpy(g->u, g->u_n, sizeof(double) * (size_t)g->ncell * g->D);
+            reset_forces(g);
+            ibm_apply(g, c, 0);
+            res = fem_check_vel_diff(g);
+            it++;
+        } while (res > 1e-4 && it < 10);
+        fem_commit_start_of_step(g);
     }
 }
 
@@ -1055,6 +1091,7 @@ int oracle_ibm_supports(int ib, double *out, int cap) {
 }
 
 void oracle_ibm_reset(void) {
+    fem_free_all();
     if (!g_ibm) return;
     for (int ib = 0; ib < g_ibm->nb; ++ib) {
         ibm_body *b = &g_ibm->b[ib];
@@ -1065,4 +1102,476 @@ void oracle_ibm_reset(void) {
     free(g_ibm->b);
     free(g_ibm);
     g_ibm = NULL;
+}
+
+/* ============================ FEM filaments ==============================
+ * Restatement of FEMBody / FEMElement (src/FEMBody.cpp, src/FEMElement.cpp)
+ * for a planar co-rotational Euler-Bernoulli beam with 3 DOFs per node,
+ * Newmark-beta (alpha 0.25, delta 0.5) and Newton-Raphson (tol 1e-10, 20
+ * iterations), coupled to the IB markers of its body; and the FSI
+ * sub-iteration loop of ObjectManager (:61-185, :988-1032). */
+
+#define NB_ALPHA 0.25
+#define NB_DELTA 0.5
+#define FSI_RELAX 0.5
+
+typedef struct fem_el {
+    double length0, length, area, I, E, density, angles;
+    double T[6][6], F[6];
+    int nchild;
+    int child_node[64];
+    double child_z1[64], child_z2[64];
+} fem_el;
+
+typedef struct fem_body {
+    int ib;              /* IB body index */
+    int nel, ndof, bc;
+    double *pos0, *pos, *ang0, *ang;   /* nodes: pos 3 per node */
+    fem_el *el;
+    double *M, *K, *R, *F, *U, *U_n, *delU, *Ud, *Ud_n, *Udd, *Udd_n;  /* dense M,K row-major */
+    int *parent_el;
+    double *parent_zeta;
+    double *mpos0;       /* marker initial positions (3 per marker) */
+    double *mvel_km1;    /* previous marker velocities */
+    double fsi_vel_scale; /* L_UX0 * dt / dh */
+    double dm;           /* GridObj::dm of the owning grid */
+    int it;
+    double res;
+} fem_body;
+
+static fem_body *g_fem = NULL;
+static int g_nfem = 0;
+
+static void mat6_mul(const double A[6][6], const double B[6][6], double C[6][6]) {
+    for (int r = 0; r < 6; ++r)
+        for (int c = 0; c < 6; ++c) {
+            double s = 0.0;
+            for (int k = 0; k < 6; ++k) s += A[r][k] * B[k][c];
+            C[r][c] = s;
+        }
+}
+static void mat6_T(const double A[6][6], double B[6][6]) {
+    for (int r = 0; r < 6; ++r)
+        for (int c = 0; c < 6; ++c) B[c][r] = A[r][c];
+}
+/* GridUtils::matrix_multiply(A, x) for square A (:257-279). */
+static void matvec(int n, const double *A, const double *x, double *y) {
+    for (int r = 0; r < n; ++r) {
+        double s = 0.0;
+        for (int c = 0; c < n; ++c) s += A[(size_t)r * n + c] * x[c];
+        y[r] = s;
+    }
+}
+
+static void set_T(fem_el *e) {
+    memset(e->T, 0, sizeof e->T);
+    e->T[0][0] = e->T[1][1] = e->T[3][3] = e->T[4][4] = cos(e->angles);
+    e->T[0][1] = e->T[3][4] = sin(e->angles);
+    e->T[1][0] = e->T[4][3] = -sin(e->angles);
+    e->T[2][2] = e->T[5][5] = 1.0;
+}
+
+/* FEMBody::updateFEMValues (:297-325). */
+static void fem_update_values(fem_body *f) {
+    const int D = 2;
+    for (int n = 0; n <= f->nel; ++n) {
+        for (int d = 0; d < D; d++) f->pos[3 * n + d] = f->pos0[3 * n + d] + f->U[n * 3 + d];
+        f->ang[n] = f->ang0[n] + f->U[n * 3 + D];
+    }
+    for (int e = 0; e < f->nel; ++e) {
+        double v[3];
+        for (int d = 0; d < 3; ++d) v[d] = f->pos[3 * (e + 1) + d] - f->pos[3 * e + d];
+        f->el[e].angles = atan2(v[1], v[0]);
+        double r = 0.0;
+        for (int d = 0; d < 3; ++d) r += pow(v[d], 2);
+        f->el[e].length = sqrt(r);
+        set_T(&f->el[e]);
+    }
+}
+
+static void assemble_vec(const fem_body *f, int e, const double *loc, double *glob) {
+    for (int i = 0; i < 6; ++i) glob[e * 3 + i] += loc[i];
+}
+static void assemble_mat(const fem_body *f, int e, const double L[6][6], double *G) {
+    for (int i = 0; i < 6; ++i)
+        for (int j = 0; j < 6; ++j) G[(size_t)(e * 3 + i) * f->ndof + (e * 3 + j)] += L[i][j];
+}
+
+/* FEMElement::loadVector (:133-173). */
+static void fem_load_vector(fem_body *f, int e, const ibm_body *b, double forceScale) {
+    fem_el *E = &f->el[e];
+    for (int q = 0; q < E->nchild; ++q) {
+        const int node = E->child_node[q];
+        const double a = E->child_z1[q], bb = E->child_z2[q];
+        const double Ts[2][2] = {{E->T[0][0], E->T[0][1]}, {E->T[1][0], E->T[1][1]}};
+        double fv[2];
+        const double sc = b->eps[node] * 1.0 * forceScale;
+        const double fx[2] = {b->F[3 * node] * sc, b->F[3 * node + 1] * sc};
+        for (int r = 0; r < 2; ++r) {
+            double s = 0.0;
+            for (int c = 0; c < 2; ++c) s += Ts[r][c] * fx[c];
+            fv[r] = s;
+        }
+        const double L = E->length;
+        double R[6];
+        R[0] = fv[0] * 0.5 * L * (0.5 * bb - 0.5 * a + 0.25 * SQ(a) - 0.25 * SQ(bb));
+        R[1] = fv[1] * 0.5 * L * (0.5 * bb - 0.5 * a - SQ(a) * SQ(a) / 16.0 + SQ(bb) * SQ(bb) / 16.0 + 3.0 * SQ(a) / 8.0 - 3.0 * SQ(bb) / 8.0);
+        R[2] = fv[1] * 0.5 * L * (L * (-SQ(a) * SQ(a) + SQ(bb) * SQ(bb)) / 32.0 - L * (-(a * a * a) + (bb * bb * bb)) / 24.0 - L * (-SQ(a) + SQ(bb)) / 16.0 + L * (bb - a) / 8.0);
+        R[3] = fv[0] * 0.5 * L * (-0.25 * SQ(a) + 0.25 * SQ(bb) + 0.5 * bb - 0.5 * a);
+        R[4] = fv[1] * 0.5 * L * (0.5 * bb - 0.5 * a + SQ(a) * SQ(a) / 16.0 - SQ(bb) * SQ(bb) / 16.0 - 3.0 * SQ(a) / 8.0 + 3.0 * SQ(bb) / 8.0);
+        R[5] = fv[1] * 0.5 * L * (L * (-SQ(a) * SQ(a) + SQ(bb) * SQ(bb)) / 32.0 + L * (-(a * a * a) + (bb * bb * bb)) / 24.0 - L * (-SQ(a) + SQ(bb)) / 16.0 - L * (bb - a) / 8.0);
+        double Tt[6][6], RG[6];
+        mat6_T(E->T, Tt);
+        for (int r = 0; r < 6; ++r) {
+            double s = 0.0;
+            for (int c = 0; c < 6; ++c) s += Tt[r][c] * R[c];
+            RG[r] = s;
+        }
+        assemble_vec(f, e, RG, f->R);
+    }
+}
+
+/* FEMElement::massMatrix (:178-213). */
+static void fem_mass(fem_body *f, int e) {
+    fem_el *E = &f->el[e];
+    double Ml[6][6];
+    memset(Ml, 0, sizeof Ml);
+    const double C1 = E->density * E->area * E->length0 / 420.0, L0 = E->length0;
+    Ml[0][0] = C1 * 140.0; Ml[0][3] = C1 * 70.0; Ml[1][1] = C1 * 156.0; Ml[1][2] = C1 * 22.0 * L0;
+    Ml[1][4] = C1 * 54; Ml[1][5] = C1 * (-13.0 * L0); Ml[2][2] = C1 * 4.0 * SQ(L0); Ml[2][4] = C1 * 13.0 * L0;
+    Ml[2][5] = C1 * (-3.0 * SQ(L0)); Ml[3][3] = C1 * 140.0; Ml[4][4] = C1 * 156.0; Ml[4][5] = C1 * (-22.0 * L0);
+    Ml[5][5] = C1 * 4.0 * SQ(L0);
+    for (int i = 1; i < 6; i++)
+        for (int j = 0; j < i; j++) Ml[i][j] = Ml[j][i];
+    double Tt[6][6], A[6][6], G[6][6];
+    mat6_T(E->T, Tt);
+    mat6_mul(Tt, Ml, A);
+    mat6_mul(A, E->T, G);
+    assemble_mat(f, e, G, f->M);
+}
+
+/* FEMElement::stiffMatrix (:218-268). */
+static void fem_stiff(fem_body *f, int e) {
+    fem_el *E = &f->el[e];
+    double Kl[6][6];
+    memset(Kl, 0, sizeof Kl);
+    const double EE = E->E, A = E->area, I = E->I, L0 = E->length0;
+    Kl[0][0] = EE * A / L0; Kl[0][3] = -EE * A / L0;
+    Kl[1][1] = 12.0 * EE * I / (L0 * L0 * L0); Kl[1][2] = 6.0 * EE * I / SQ(L0);
+    Kl[1][4] = -12.0 * EE * I / (L0 * L0 * L0); Kl[1][5] = 6.0 * EE * I / SQ(L0);
+    Kl[2][2] = 4.0 * EE * I / L0; Kl[2][4] = -6.0 * EE * I / SQ(L0); Kl[2][5] = 2.0 * EE * I / L0;
+    Kl[3][3] = EE * A / L0; Kl[4][4] = 12.0 * EE * I / (L0 * L0 * L0); Kl[4][5] = -6.0 * EE * I / SQ(L0);
+    Kl[5][5] = 4.0 * EE * I / L0;
+    for (int i = 1; i < 6; i++)
+        for (int j = 0; j < i; j++) Kl[i][j] = Kl[j][i];
+    const double F0 = -E->F[0], V0 = E->F[4];
+    Kl[0][1] += -V0 / L0; Kl[0][4] += V0 / L0; Kl[1][0] += -V0 / L0; Kl[1][1] += F0 / L0;
+    Kl[1][3] += V0 / L0; Kl[1][4] += -F0 / L0; Kl[3][1] += V0 / L0; Kl[3][4] += -V0 / L0;
+    Kl[4][0] += V0 / L0; Kl[4][1] += -F0 / L0; Kl[4][3] += -V0 / L0; Kl[4][4] += F0 / L0;
+    double Tt[6][6], B[6][6], G[6][6];
+    mat6_T(E->T, Tt);
+    mat6_mul(Tt, Kl, B);
+    mat6_mul(B, E->T, G);
+    assemble_mat(f, e, G, f->K);
+}
+
+/* FEMElement::forceVector (:273-302). */
+static void fem_force(fem_body *f, int e) {
+    fem_el *E = &f->el[e];
+    const double a1 = f->ang[e], a2 = f->ang[e + 1];
+    const double L = E->length, L0 = E->length0;
+    const double u = (SQ(L) - SQ(L0)) / (L + L0);
+    const double t1 = atan2(cos(E->angles) * sin(a1) - sin(E->angles) * cos(a1), cos(E->angles) * cos(a1) + sin(E->angles) * sin(a1));
+    const double t2 = atan2(cos(E->angles) * sin(a2) - sin(E->angles) * cos(a2), cos(E->angles) * cos(a2) + sin(E->angles) * sin(a2));
+    const double F0 = (E->E * E->area / L0) * u;
+    const double M1 = (2 * E->E * E->I / L0) * (2.0 * t1 + t2);
+    const double M2 = (2 * E->E * E->I / L0) * (t1 + 2.0 * t2);
+    E->F[0] = -F0; E->F[1] = (1.0 / L0) * (M1 + M2); E->F[2] = M1;
+    E->F[3] = F0; E->F[4] = -(1.0 / L0) * (M1 + M2); E->F[5] = M2;
+    double Tt[6][6], FG[6];
+    mat6_T(E->T, Tt);
+    for (int r = 0; r < 6; ++r) {
+        double s = 0.0;
+        for (int c = 0; c < 6; ++c) s += Tt[r][c] * E->F[c];
+        FG[r] = s;
+    }
+    assemble_vec(f, e, FG, f->F);
+}
+
+/* GridUtils::solveLinearSystem (src/GridUtils.cpp:356-395) with BC offset. */
+static void solve_bc(int dim, const double *Arow, const double *b, int BC, double *out) {
+    const int n = dim - BC;
+    double *a = (double *)malloc(sizeof(double) * (size_t)dim * dim);
+    memcpy(a, Arow, sizeof(double) * (size_t)dim * dim);
+    for (int i = 0; i < dim; ++i) out[i] = b[i];
+    int *ipiv = (int *)malloc(sizeof(int) * (n > 0 ? n : 1));
+    /* row-major a read column-major from offset BC*dim+BC with lda = dim */
+    double *sub = a + (size_t)BC * dim + BC;
+    lu_factor(n, sub, dim, ipiv);
+    lu_solve_t(n, sub, dim, ipiv, out + BC);
+    for (int i = 0; i < BC; ++i) out[i] = 0.0;
+    free(a);
+    free(ipiv);
+}
+
+static void fem_newmark_set(fem_body *f, double Dt) {
+    const int n = f->ndof;
+    const double a0 = 1.0 / (NB_ALPHA * SQ(Dt)), a2 = 1.0 / (NB_ALPHA * Dt), a3 = 1.0 / (2.0 * NB_ALPHA) - 1.0;
+    double *Meff = (double *)malloc(sizeof(double) * n), *MF = (double *)malloc(sizeof(double) * n);
+    for (int i = 0; i < n; i++) Meff[i] = a0 * (f->U_n[i] - f->U[i]) + a2 * f->Ud[i] + a3 * f->Udd[i];
+    matvec(n, f->M, Meff, MF);
+    for (int i = 0; i < n; i++) {
+        f->F[i] = f->R[i] - f->F[i] + MF[i];
+        for (int j = 0; j < n; j++) f->K[(size_t)i * n + j] += a0 * f->M[(size_t)i * n + j];
+    }
+    free(Meff);
+    free(MF);
+}
+
+/* FEMBody::dynamicFEM (:136-179) with newtonRaphsonIterator (:183-218),
+ * checkNRConvergence (:224-231), finishNewmark (:236-255). */
+static void fem_dynamic(fem_body *f, ibm_body *b) {
+    oracle_grid *g = b->owner;
+    const int n = f->ndof;
+    const double Dt = g->d.dt;
+    memcpy(f->U, f->U_n, sizeof(double) * n);
+    memcpy(f->Ud, f->Ud_n, sizeof(double) * n);
+    memcpy(f->Udd, f->Udd_n, sizeof(double) * n);
+    fem_update_values(f);
+    memset(f->R, 0, sizeof(double) * n);
+    const double forceScale = f->dm / SQ(Dt);
+    for (int e = 0; e < f->nel; ++e) fem_load_vector(f, e, b, forceScale);
+    f->it = 0;
+    do {
+        memset(f->F, 0, sizeof(double) * n);
+        memset(f->M, 0, sizeof(double) * (size_t)n * n);
+        memset(f->K, 0, sizeof(double) * (size_t)n * n);
+        for (int e = 0; e < f->nel; ++e) {
+            fem_force(f, e);
+            fem_mass(f, e);
+            fem_stiff(f, e);
+        }
+        fem_newmark_set(f, Dt);
+        solve_bc(n, f->K, f->F, f->bc, f->delU);
+        for (int i = 0; i < n; i++) f->U[i] = f->U[i] + f->delU[i];
+        fem_update_values(f);
+        double dp = 0.0;
+        for (int i = 0; i < n; i++) dp += f->delU[i] * f->delU[i];
+        const double L = f->el[0].length0 * f->nel;
+        f->res = sqrt(dp / (double)n) / L;
+        f->it++;
+    } while (f->res > 1e-10 && f->it < 20);
+    const double a6 = 1.0 / (NB_ALPHA * SQ(Dt)), a7 = -1.0 / (NB_ALPHA * Dt), a8 = -(1.0 / (2.0 * NB_ALPHA) - 1.0);
+    const double a9 = Dt * (1.0 - NB_DELTA), a10 = NB_DELTA * Dt;
+    for (int i = 0; i < n; i++) {
+        const double s = a6 * (f->U[i] - f->U_n[i]) + a7 * f->Ud[i] + a8 * f->Udd[i];
+        f->Ud[i] = f->Ud[i] + a9 * f->Udd[i] + a10 * s;
+        f->Udd[i] = s;
+    }
+    /* FEMBody::updateIBMarkers (:329-370) */
+    for (int m = 0; m < b->nm; ++m) {
+        const fem_el *E = &f->el[f->parent_el[m]];
+        const double z = f->parent_zeta[m];
+        double dU[6], dV[6], lU[6], lV[6];
+        const int e = f->parent_el[m];
+        for (int i = 0; i < 6; ++i) { dU[i] = f->U[e * 3 + i]; dV[i] = f->Ud[e * 3 + i]; }
+        for (int r = 0; r < 6; ++r) {
+            double s1 = 0.0, s2 = 0.0;
+            for (int c = 0; c < 6; ++c) { s1 += E->T[r][c] * dU[c]; s2 += E->T[r][c] * dV[c]; }
+            lU[r] = s1; lV[r] = s2;
+        }
+        const double zz = (z + 1.0) / 2.0, L = E->length;
+        const double N0 = 1.0 - (z + 1.0) / 2.0;
+        const double N1 = 1.0 - 3.0 * SQ(zz) + 2.0 * (zz * zz * zz);
+        const double N2 = (zz - 2.0 * SQ(zz) + (zz * zz * zz)) * L;
+        const double N3 = (z + 1.0) / 2.0;
+        const double N4 = 3.0 * SQ(zz) - 2.0 * (zz * zz * zz);
+        const double N5 = (-SQ(zz) + (zz * zz * zz)) * L;
+        const double su[2] = {lU[0] * N0 + lU[3] * N3, lU[1] * N1 + lU[2] * N2 + lU[4] * N4 + lU[5] * N5};
+        const double sv[2] = {lV[0] * N0 + lV[3] * N3, lV[1] * N1 + lV[2] * N2 + lV[4] * N4 + lV[5] * N5};
+        const double Tt[2][2] = {{E->T[0][0], E->T[1][0]}, {E->T[0][1], E->T[1][1]}};
+        double gu[2], gv[2];
+        for (int r = 0; r < 2; ++r) {
+            double s1 = 0.0, s2 = 0.0;
+            for (int c = 0; c < 2; ++c) { s1 += Tt[r][c] * su[c]; s2 += Tt[r][c] * sv[c]; }
+            gu[r] = s1;
+            gv[r] = s2 * (g->d.dt / g->d.dh);
+        }
+        for (int d = 0; d < 2; d++) {
+            b->pos[3 * m + d] = f->mpos0[3 * m + d] + gu[d];
+            f->mvel_km1[3 * m + d] = b->vel[3 * m + d];
+            b->vel[3 * m + d] = FSI_RELAX * gv[d] + (1.0 - FSI_RELAX) * f->mvel_km1[3 * m + d];
+        }
+    }
+}
+
+static int grid_has_flexible(oracle_grid *g) {
+    for (int k = 0; k < g_nfem; ++k)
+        if (g_ibm->b[g_fem[k].ib].owner == g) return 1;
+    return 0;
+}
+
+/* ObjectManager::ibm_moveBodies (:61-104): FEM for every flexible body on
+ * the grid, new supports for them, then ds and epsilon for all bodies of
+ * the grid. */
+static void fem_move_bodies(oracle_grid *g, ibm_ctx *c) {
+    for (int k = 0; k < g_nfem; ++k)
+        if (c->b[g_fem[k].ib].owner == g) fem_dynamic(&g_fem[k], &c->b[g_fem[k].ib]);
+    for (int k = 0; k < g_nfem; ++k)
+        if (c->b[g_fem[k].ib].owner == g) find_support(c, &c->b[g_fem[k].ib]);
+    for (int ib = 0; ib < c->nb; ++ib)
+        if (c->b[ib].owner == g) compute_ds(&c->b[ib]);
+    for (int ib = 0; ib < c->nb; ++ib)
+        if (c->b[ib].owner == g) find_epsilon(&c->b[ib]);
+}
+
+/* ObjectManager::ibm_checkVelDiff (:988-1032). */
+static double fem_check_vel_diff(oracle_grid *g) {
+    double res = 0.0;
+    for (int k = 0; k < g_nfem; ++k) {
+        fem_body *f = &g_fem[k];
+        ibm_body *b = &g_ibm->b[f->ib];
+        if (b->owner != g) continue;
+        for (int m = 0; m < b->nm; ++m) {
+            double r = 0.0;
+            for (int d = 0; d < 3; ++d) r += pow(b->vel[3 * m + d] - f->mvel_km1[3 * m + d], 2);
+            const double v = sqrt(r) / f->fsi_vel_scale;
+            if (fabs(v) > res) res = fabs(v);
+        }
+    }
+    return res;
+}
+
+static void fem_commit_start_of_step(oracle_grid *g) {
+    for (int k = 0; k < g_nfem; ++k) {
+        fem_body *f = &g_fem[k];
+        if (g_ibm->b[f->ib].owner != g) continue;
+        memcpy(f->U_n, f->U, sizeof(double) * f->ndof);
+        memcpy(f->Ud_n, f->Ud, sizeof(double) * f->ndof);
+        memcpy(f->Udd_n, f->Udd, sizeof(double) * f->ndof);
+    }
+}
+
+/* A flexible filament: the markers of Body's filament builder
+ * (inc/Body.h:143-187) and its FEMBody (src/FEMBody.cpp:48-130) with the
+ * IB <-> FEM node mapping (:378-424).  angle_v in degrees; 2D only (the
+ * reference's FEM is planar).  Returns the IB body index. */
+int oracle_ibm_add_filament(oracle_grid *g, const double start[3], double length, double height, double depth,
+                            double angle_v, int nel, int clamped, double density, double E, double dm,
+                            double fsi_vel_scale) {
+    if (g->D != 2) { set_err("FEM filaments are planar (2D) in the reference"); return -1; }
+    const double dh = g->d.dh;
+    const int nmk = (int)floor(length / dh) + 1;
+    const double spacing = length / (nmk - 1);
+    const double spacing_h = spacing * cos(angle_v * L_PI / 180);
+    double *xyz = (double *)malloc(sizeof(double) * 3 * nmk);
+    for (int i = 0; i < nmk; i++) {
+        xyz[3 * i + 0] = start[0] + i * spacing_h * cos(0.0 * L_PI / 180.0);
+        xyz[3 * i + 1] = start[1] + i * spacing * sin(angle_v * L_PI / 180.0);
+        xyz[3 * i + 2] = start[2] + i * spacing_h * sin(0.0 * L_PI / 180.0);
+    }
+    const int ib = oracle_ibm_add_body(g, nmk, xyz);
+    free(xyz);
+    g->has_flexible_bodies = 1;
+    g_fem = (fem_body *)realloc(g_fem, sizeof(fem_body) * (g_nfem + 1));
+    fem_body *f = &g_fem[g_nfem++];
+    memset(f, 0, sizeof *f);
+    f->ib = ib;
+    f->nel = nel;
+    f->ndof = (nel + 1) * 3;
+    f->bc = clamped ? 3 : 2;
+    f->dm = dm;
+    f->fsi_vel_scale = fsi_vel_scale;
+    const double fspacing = length / nel;
+    const double fspacing_h = fspacing * cos(angle_v * L_PI / 180);
+    f->pos0 = dup_d(NULL, 3 * (size_t)(nel + 1));
+    f->pos = dup_d(NULL, 3 * (size_t)(nel + 1));
+    f->ang0 = dup_d(NULL, nel + 1);
+    f->ang = dup_d(NULL, nel + 1);
+    for (int i = 0; i < nel + 1; i++) {
+        f->pos0[3 * i + 0] = start[0] + i * fspacing_h * cos(0.0 * L_PI / 180.0);
+        f->pos0[3 * i + 1] = start[1] + i * fspacing * sin(angle_v * L_PI / 180.0);
+        f->pos0[3 * i + 2] = start[2] + i * fspacing_h * sin(0.0 * L_PI / 180.0);
+        f->ang0[i] = angle_v * L_PI / 180.0;
+        f->ang[i] = f->ang0[i];
+    }
+    memcpy(f->pos, f->pos0, sizeof(double) * 3 * (nel + 1));
+    depth = dh; /* 2D: unit lattice depth (src/FEMBody.cpp:103-105) */
+    f->el = (fem_el *)calloc(nel, sizeof(fem_el));
+    for (int e = 0; e < nel; ++e) {
+        fem_el *el = &f->el[e];
+        el->length0 = fspacing;
+        el->length = fspacing;
+        el->area = height * depth;
+        el->angles = angle_v * L_PI / 180.0;
+        el->I = depth * (height * height * height) / 12.0;
+        el->E = E;
+        el->density = density;
+        set_T(el);
+    }
+    /* computeNodeMapping */
+    const int nI = nmk, nF = nel + 1;
+    f->parent_el = (int *)malloc(sizeof(int) * nI);
+    f->parent_zeta = (double *)malloc(sizeof(double) * nI);
+    f->parent_el[0] = 0;
+    f->parent_zeta[0] = -1.0;
+    for (int i = 1; i < nI; i++) {
+        const double q = i * ((nF - 1.0) / (nI - 1.0));
+        if (fmod(q, 1.0) == 0.0) {
+            f->parent_el[i] = (int)floor(q) - 1;
+            f->parent_zeta[i] = 1.0;
+        } else {
+            f->parent_el[i] = (int)floor(q);
+            f->parent_zeta[i] = fmod(q, 1.0) * 2.0 - 1.0;
+        }
+    }
+    for (int e = 0; e < nel; ++e)
+        for (int node = 0; node < nI; ++node) {
+            double n1 = -1 + 2.0 * ((node - 0.5) * ((nF - 1.0) / (nI - 1.0)) - e) / 1.0;
+            double n2 = -1 + 2.0 * ((node + 0.5) * ((nF - 1.0) / (nI - 1.0)) - e) / 1.0;
+            if ((n1 > -1.0 && n1 < 1.0) || (n2 > -1.0 && n2 < 1.0)) {
+                if (n1 < -1.0) n1 = -1.0;
+                if (n2 > 1.0) n2 = 1.0;
+                fem_el *el = &f->el[e];
+                if (el->nchild >= 64) { set_err("too many IB nodes per element"); return -1; }
+                el->child_node[el->nchild] = node;
+                el->child_z1[el->nchild] = n1;
+                el->child_z2[el->nchild] = n2;
+                el->nchild++;
+            }
+        }
+    const int n = f->ndof;
+    f->M = dup_d(NULL, (size_t)n * n);
+    f->K = dup_d(NULL, (size_t)n * n);
+    f->R = dup_d(NULL, n); f->F = dup_d(NULL, n); f->U = dup_d(NULL, n); f->U_n = dup_d(NULL, n);
+    f->delU = dup_d(NULL, n); f->Ud = dup_d(NULL, n); f->Ud_n = dup_d(NULL, n);
+    f->Udd = dup_d(NULL, n); f->Udd_n = dup_d(NULL, n);
+    ibm_body *b = &g_ibm->b[ib];
+    f->mpos0 = dup_d(b->pos, 3 * (size_t)nmk);
+    f->mvel_km1 = dup_d(NULL, 3 * (size_t)nmk);
+    return ib;
+}
+
+/* FEM state of filament k: U (ndof values) and node positions. */
+int oracle_fem_state(int k, double *U, int *ndof, int *it, double *res) {
+    if (k < 0 || k >= g_nfem) return -1;
+    fem_body *f = &g_fem[k];
+    if (ndof) *ndof = f->ndof;
+    if (U) memcpy(U, f->U_n, sizeof(double) * f->ndof);
+    if (it) *it = f->it;
+    if (res) *res = f->res;
+    return 0;
+}
+
+static void fem_free_all(void) {
+    for (int k = 0; k < g_nfem; ++k) {
+        fem_body *f = &g_fem[k];
+        free(f->pos0); free(f->pos); free(f->ang0); free(f->ang); free(f->el);
+        free(f->M); free(f->K); free(f->R); free(f->F); free(f->U); free(f->U_n); free(f->delU);
+        free(f->Ud); free(f->Ud_n); free(f->Udd); free(f->Udd_n); free(f->parent_el); free(f->parent_zeta);
+        free(f->mpos0); free(f->mvel_km1);
+    }
+    free(g_fem);
+    g_fem = NULL;
+    g_nfem = 0;
 }

@@ -63,6 +63,11 @@ def lib():
         L.oracle_ibm_markers.argtypes = [C.c_int, C.POINTER(C.c_double)]
         L.oracle_ibm_supports.argtypes = [C.c_int, C.POINTER(C.c_double), C.c_int]
         L.oracle_ibm_reset.argtypes = []
+        L.oracle_ibm_add_filament.argtypes = [C.c_void_p, C.POINTER(C.c_double), C.c_double, C.c_double,
+                                              C.c_double, C.c_double, C.c_int, C.c_int, C.c_double,
+                                              C.c_double, C.c_double, C.c_double]
+        L.oracle_fem_state.argtypes = [C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_int),
+                                       C.POINTER(C.c_int), C.POINTER(C.c_double)]
         _lib = L
     return _lib
 
@@ -155,3 +160,23 @@ class OracleIBM:
         out = np.empty((n, 5))
         self.L.oracle_ibm_supports(ib, A.dptr(out), n)
         return out
+
+    def add_filament(self, grid: OracleGrid, start, length, height, depth, angle_v, nel, clamped, density, E,
+                     dm, fsi_vel_scale) -> int:
+        st = np.ascontiguousarray(start, dtype=np.float64)
+        ib = self.L.oracle_ibm_add_filament(grid.h, A.dptr(st), length, height, depth, angle_v, nel,
+                                            int(clamped), density, E, dm, fsi_vel_scale)
+        if ib < 0:
+            raise RuntimeError(self.L.oracle_last_error().decode())
+        import math
+        self.nm.append(int(math.floor(length / grid.desc.dh)) + 1)
+        return ib
+
+    def fem_state(self, k: int):
+        nd = C.c_int()
+        self.L.oracle_fem_state(k, None, C.byref(nd), None, None)
+        U = np.empty(nd.value)
+        it = C.c_int()
+        res = C.c_double()
+        self.L.oracle_fem_state(k, A.dptr(U), C.byref(nd), C.byref(it), C.byref(res))
+        return U, it.value, res.value

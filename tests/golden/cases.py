@@ -76,6 +76,13 @@ CASES = {
         defs=Definitions(dims=3, resolution=16, timestep=1.0 / 400.0, bx=3.0, by=1.5, bz=1.5, re=40, ux0=1.0,
                          ibm=True, walls=(V, X, S, S, F, F)),
         bodies="sphere", steps=(5, 50), store_f=()),
+    # D2Q9 channel with a flexible FEM filament (FSI sub-iterations).
+    "fem_filament_d2q9": dict(
+        defs=Definitions(dims=2, resolution=40, timestep=1.0 / 1000.0, bx=2.0, by=1.0, re=100, ux0=1.0,
+                         ibm=True, walls=(V, X, S, S, F, F)),
+        filaments=[dict(start=(0.5, 0.0, 0.0), length=0.4, height=0.02, depth=0.0, angle_v=90.0,
+                        nel=10, clamped=True, density=1000.0, E=1.0e8)],
+        steps=(2, 30), store_f=(2,)),
     # D2Q9 BGK-Smagorinsky channel.
     "smag_d2q9": dict(
         defs=Definitions(dims=2, resolution=32, timestep=1.0 / 320.0, bx=2.0, by=1.0, re=2000,
@@ -174,3 +181,26 @@ def write_marker_file(path: str, body_list) -> None:
             fp.write(f"{lev} {reg} {len(pos)}\n")
             for x, y, z in pos:
                 fp.write(f"{float(x)!r} {float(y)!r} {float(z)!r}\n")
+
+
+def geometry_config(name: str) -> str:
+    """input/geometry.config text for the case's filaments (reference format)."""
+    lines = []
+    for fl in CASES[name].get("filaments", []):
+        x, y, z = fl["start"]
+        lines.append("FILAMENT_ARRAY IBM 0 0 1 %r %r %r 0.0 0.0 0.0 %r %r %r %r 0 FLEXIBLE %d %s %r %r" % (
+            x, y, z, fl["length"], fl["height"], fl["depth"], fl["angle_v"], fl["nel"],
+            "CLAMPED" if fl["clamped"] else "SUPPORTED", fl["density"], fl["E"]))
+    return "\n".join(lines) + "\n"
+
+
+def filament_start(name: str, fl: dict) -> tuple:
+    """Start position after the geometry reader's wall shift
+    (src/ObjectManager_ops_io.cpp:481-488): + wall thickness where the
+    left/bottom/front wall is solid."""
+    d: Definitions = CASES[name]["defs"]
+    dh = 1.0 / d.resolution
+    sx = d.wall_cells[0] * dh if d.walls[0] == A.SOLID else 0.0
+    sy = d.wall_cells[2] * dh if d.walls[2] == A.SOLID else 0.0
+    sz = d.wall_cells[4] * dh if d.walls[4] == A.SOLID else 0.0
+    return (fl["start"][0] + sx, fl["start"][1] + sy, fl["start"][2] + sz)

@@ -64,8 +64,13 @@ def run_case(name: str, ref: str) -> str:
         upath = os.path.join(work, "init_u.bin")
         init["u"].astype(np.float64).tofile(upath)
         args += ["--init-u", upath]
-    blist = CASES.bodies(name)
-    if blist:
+    if spec.get("filaments"):
+        os.makedirs(os.path.join(work, "input"), exist_ok=True)
+        with open(os.path.join(work, "input", "geometry.config"), "w") as fp:
+            fp.write(CASES.geometry_config(name))
+        args += ["--workdir", work]
+    blist = CASES.bodies(name) or (["filament"] if spec.get("filaments") else [])
+    if blist and not spec.get("filaments"):
         mpath = os.path.join(work, "markers.in")
         CASES.write_marker_file(mpath, blist)
         args += ["--markers", mpath]

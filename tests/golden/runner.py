@@ -72,3 +72,21 @@ def fields_at(fx: dict, key: str, s: int, name: str):
     pre = "" if key == "L0R0" else key + "_"
     return (fx.get(f"{pre}u_{s}"), fx.get(f"{pre}rho_{s}"), str(fx[f"{pre}u_sha_{s}"]),
             str(fx[f"{pre}rho_sha_{s}"]), str(fx[f"{pre}f_sha_{s}"]))
+
+
+def grid_dm(lv) -> float:
+    """GridObj::dm: (L_PHYSICAL_RHO / L_RHOIN) * dh^3 on L0, /8 per level."""
+    d = lv.defs
+    return (d.physical_rho / d.rho_in) * lv.dh * lv.dh * lv.dh
+
+
+def attach_filaments(name, grids, levels, add):
+    """Add the case's filaments with `add(grid, **params)` on level 0."""
+    out = []
+    for fl in CASES.CASES[name].get("filaments", []):
+        lv = levels[0]
+        out.append(add(grids[0], start=CASES.filament_start(name, fl), length=fl["length"], height=fl["height"],
+                       depth=fl["depth"], angle_v=fl["angle_v"], nel=fl["nel"], clamped=fl["clamped"],
+                       density=fl["density"], E=fl["E"], dm=grid_dm(lv),
+                       fsi_vel_scale=lv.defs.ux0 * lv.dt / lv.dh))
+    return out

@@ -38,7 +38,8 @@ def make_oracle(desc, parent):
     return O.OracleGrid(desc, parent)
 
 
-NO_BODIES = sorted(n for n in CASES.CASES if not CASES.CASES[n].get("bodies"))
+NO_BODIES = sorted(n for n in CASES.CASES
+                   if not CASES.CASES[n].get("bodies") and not CASES.CASES[n].get("filaments"))
 
 
 @pytest.mark.parametrize("name", NO_BODIES)

@@ -44,7 +44,8 @@ def test_host_subgrid_setup_matches_reference(name):
         assert R.sha(f0) == str(fx[f"{k}_f0_sha"]), k
 
 
-@pytest.mark.parametrize("name", sorted(n for n in CASES.CASES if not CASES.CASES[n].get("bodies")))
+@pytest.mark.parametrize("name", sorted(n for n in CASES.CASES
+                                        if not CASES.CASES[n].get("bodies") and not CASES.CASES[n].get("filaments")))
 def test_oracle_bit_exact_vs_reference(name):
     """The restatement reproduces the reference bit for bit (FP64, same
     operation order, no contraction) at every stored step, on every grid."""
@@ -115,3 +116,31 @@ def test_oracle_ibm_bit_exact_vs_reference(name):
         assert R.sha(st["f"]) == str(fx[f"f_sha_{s}"])
         mk = ibm.markers(0)
         assert np.array_equal(mk[:, 3:3 + D], fx[f"markers_{s}"][:, 5:5 + D]), f"marker force at step {s}"
+
+
+@pytest.mark.parametrize("name", sorted(n for n in CASES.CASES if CASES.CASES[n].get("filaments")))
+def test_oracle_fem_fsi_bit_exact_vs_reference(name):
+    """Flexible filament (co-rotational FEM beam, Newmark/Newton-Raphson,
+    FSI sub-iterations) built as the reference's FILAMENT_ARRAY reader builds
+    it: marker positions, forces, epsilon and the flow field match the
+    reference bit for bit."""
+    spec = CASES.CASES[name]
+    fx = R.fixture(name)
+    grids, levels = R.build_backend(name, lambda d, p: O.OracleGrid(d, p))
+    ibm = O.OracleIBM()
+    R.attach_filaments(name, grids, levels, lambda g, **k: ibm.add_filament(g, **k))
+    ibm.initialise()
+    mk = ibm.markers(0)
+    assert np.array_equal(mk[:, 0:3], fx["markers_0"][:, 2:5])
+    assert np.array_equal(mk[:, 6], fx["markers_0"][:, 8])
+    done = 0
+    for s in spec["steps"]:
+        grids[0].step(s - done)
+        done = s
+        st = grids[0].download()
+        mk = ibm.markers(0)
+        rm = fx[f"markers_{s}"]
+        assert np.array_equal(st["u"], fx[f"u_{s}"]) and np.array_equal(st["rho"], fx[f"rho_{s}"])
+        assert np.array_equal(mk[:, 0:2], rm[:, 2:4]), "marker positions"
+        assert np.array_equal(mk[:, 3:5], rm[:, 5:7]), "marker forces"
+        assert np.array_equal(mk[:, 6], rm[:, 8]), "epsilon"
