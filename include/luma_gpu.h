@@ -174,6 +174,19 @@ int luma_gpu_ibm_add_body(luma_gpu_grid *grid, int nmarkers, const double *posit
  * ObjectManager::ibm_initialise (src/ObjectManager_ops_ibm.cpp:190-246).
  * Call after all bodies are added and before stepping. */
 int luma_gpu_ibm_initialise(luma_gpu_grid *root);
+/* Adds a flexible filament as the reference's FILAMENT_ARRAY geometry
+ * reader builds one (LUMA src/ObjectManager_ops_io.cpp:455-567): IB markers
+ * every dh along the filament (inc/Body.h:143-187) and a co-rotational
+ * Euler-Bernoulli FEM beam of `nel` elements (src/FEMBody.cpp:48-130),
+ * clamped or simply supported at `start` (already shifted by the wall
+ * thickness where the reader shifts it); angle_v in degrees; dm =
+ * GridObj::dm; fsi_vel_scale = L_UX0*dt/dh (the FSI residual's scale,
+ * src/ObjectManager_ops_ibm.cpp:1007).  2D grids only: the reference's FEM
+ * is planar and aborts in 3D.  The FEM (Newmark-beta + Newton-Raphson) and
+ * the FSI sub-iterations run on the device. */
+int luma_gpu_ibm_add_filament(luma_gpu_grid *grid, const double start[3], double length, double height,
+                              double depth, double angle_v, int nel, int clamped, double density,
+                              double youngs_modulus, double dm, double fsi_vel_scale, int *body_index);
 /* Per-marker state, 9 doubles per marker: x y z Fx Fy Fz epsilon ds nsupport
  * (F = the last IBM force of ibm_computeForce, lattice units). */
 int luma_gpu_ibm_get_markers(luma_gpu_grid *grid, int body, double *out);

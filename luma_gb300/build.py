@@ -20,6 +20,8 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD, "libluma_gpu.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+# Units whose FP64 operation sequence must be the reference's (no FMA contraction).
+FMAD_OFF = {"fem.cu"}
 
 
 def nvcc() -> str:
@@ -50,7 +52,8 @@ def build(force: bool = False, debug: bool = False, jobs: int | None = None, ver
         obj = os.path.join(BUILD, os.path.basename(src)[:-3] + ".o")
         if not force and os.path.exists(obj) and os.path.getmtime(obj) >= max(os.path.getmtime(src), newest_hdr):
             return obj, None
-        cmd = [cc, *flags, "-c", src, "-o", obj]
+        extra = ["-fmad=false"] if os.path.basename(src) in FMAD_OFF else []
+        cmd = [cc, *flags, *extra, "-c", src, "-o", obj]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             return obj, " ".join(cmd) + "\n" + r.stdout[-3000:] + r.stderr[-6000:]

@@ -1,0 +1,798 @@
+// Flexible filaments on the device: the co-rotational Euler-Bernoulli beam
+// of FEMBody/FEMElement (LUMA src/FEMBody.cpp:136-424,
+// src/FEMElement.cpp:109-302) and the FSI coupling of ObjectManager
+// (src/ObjectManager_ops_ibm.cpp:61-185, :988-1032).
+//
+// One CTA per filament runs dynamicFEM: Newmark-beta (alpha 0.25, delta
+// 0.5) with Newton-Raphson (tol 1e-10, <= 20 iterations); each iteration
+// assembles the element force vectors and the mass and stiffness matrices
+// with the reference's summation order (every global entry sums its element
+// contributions in element order), forms the effective system and solves it
+// with partial-pivot LU.  A second per-filament kernel rebuilds the moving
+// markers' supports, spacing and epsilon.  This translation unit is built
+// with FMA contraction off so the FP64 operation sequence is the
+// reference's.
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "dispatch.hpp"
+#include "grid.hpp"
+#include "kernels.hpp"
+
+using namespace luma;
+
+namespace {
+
+constexpr double kNbAlpha = 0.25;
+constexpr double kNbDelta = 0.5;
+constexpr double kRelax = 0.5;
+constexpr double kPi = 3.14159265358979323846;
+
+struct FemKernelArgs {
+    int nfil, maxdof, maxmk;
+    const int *node_off, *el_off, *dof_off, *mk_off, *bc;
+    const double *dm, *velscale;
+    const double *pos0, *ang0;
+    const double *len0, *area, *I, *E, *rho;
+    const int *child_off, *child_node;
+    const double *child_z1, *child_z2;
+    double *U, *U_n, *Ud, *Ud_n, *Udd, *Udd_n, *R, *Fv, *delU;
+    double *M, *K, *epsA;
+    double *elF, *elM, *elK, *elang, *ellen, *npos, *nang, *tmp;
+    const int *parent_el;
+    const double *parent_zeta, *mpos0;
+    int *it;
+    double *res, *fsi_res;
+    double dt, dh;
+    FlexArgs flex;
+    // grid for the support search
+    int N, M_, K_, dims, level;
+    const double *hx, *hy, *hz;
+    double gstart[3];
+    double edges[6];
+    int *error;
+};
+
+__device__ __forceinline__ void Tmat(double ang, double T[6][6]) {
+    for (int i = 0; i < 6; ++i)
+        for (int j = 0; j < 6; ++j) T[i][j] = 0.0;
+    const double c = cos(ang), s = sin(ang);
+    T[0][0] = T[1][1] = T[3][3] = T[4][4] = c;
+    T[0][1] = T[3][4] = s;
+    T[1][0] = T[4][3] = -s;
+    T[2][2] = T[5][5] = 1.0;
+}
+
+// FEMBody::updateFEMValues (:297-325) for filament f.
+__device__ void update_values(const FemKernelArgs &a, int f) {
+    const int n0 = a.node_off[f], nn = a.node_off[f + 1] - n0;
+    const int e0 = a.el_off[f], ne = a.el_off[f + 1] - e0;
+    const int d0 = a.dof_off[f];
+    for (int n = threadIdx.x; n < nn; n += blockDim.x) {
+        for (int d = 0; d < 2; d++) a.npos[3 * (n0 + n) + d] = a.pos0[3 * (n0 + n) + d] + a.U[d0 + n * 3 + d];
+        a.npos[3 * (n0 + n) + 2] = a.pos0[3 * (n0 + n) + 2];
+        a.nang[n0 + n] = a.ang0[n0 + n] + a.U[d0 + n * 3 + 2];
+    }
+    __syncthreads();
+    for (int e = threadIdx.x; e < ne; e += blockDim.x) {
+        double v[3];
+        for (int d = 0; d < 3; ++d) v[d] = a.npos[3 * (n0 + e + 1) + d] - a.npos[3 * (n0 + e) + d];
+        a.elang[e0 + e] = atan2(v[1], v[0]);
+        double r = 0.0;
+        for (int d = 0; d < 3; ++d) r += v[d] * v[d];
+        a.ellen[e0 + e] = sqrt(r);
+    }
+    __syncthreads();
+}
+
+// Partial-pivot LU of the n x n block whose column-major element (r, c)
+// is A[(off + c) * lda + (off + r)] (a row-major matrix read column-major,
+// as GridUtils::solveLinearSystem hands it to dgetrf_), then the transposed
+// solve for x (length n).  Pivot search and the triangular solves are
+// sequential (the reference's summation order); column updates run across
+// the block.
+__device__ void lu_solve_block(double *A, int lda, int off, int n, int *ipiv, double *x) {
+#define AC(r, c) A[(size_t)(off + (c)) * lda + (off + (r))]
+    __shared__ int piv;
+    for (int k = 0; k < n; ++k) {
+        if (threadIdx.x == 0) {
+            int p = k;
+            double best = fabs(AC(k, k));
+            for (int r = k + 1; r < n; ++r) {
+                const double v = fabs(AC(r, k));
+                if (v > best) { best = v; p = r; }
+            }
+            ipiv[k] = p + 1;
+            piv = p;
+        }
+        __syncthreads();
+        const int p = piv;
+        const bool zero = AC(p, k) == 0.0;
+        __syncthreads();
+        if (zero) continue;
+        if (p != k)
+            for (int c = threadIdx.x; c < n; c += blockDim.x) {
+                const double t = AC(k, c);
+                AC(k, c) = AC(p, c);
+                AC(p, c) = t;
+            }
+        __syncthreads();
+        const double inv = 1.0 / AC(k, k);
+        for (int r = k + 1 + threadIdx.x; r < n; r += blockDim.x) AC(r, k) *= inv;
+        __syncthreads();
+        for (int c = k + 1 + threadIdx.x; c < n; c += blockDim.x) {
+            const double akc = AC(k, c);
+            if (akc == 0.0) continue;
+            for (int r = k + 1; r < n; ++r) AC(r, c) -= AC(r, k) * akc;
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        for (int r = 0; r < n; ++r) { double s = x[r]; for (int c = 0; c < r; ++c) s -= AC(c, r) * x[c]; x[r] = s / AC(r, r); }
+        for (int r = n - 1; r >= 0; --r) { double s = x[r]; for (int c = r + 1; c < n; ++c) s -= AC(c, r) * x[c]; x[r] = s; }
+        for (int k = n - 1; k >= 0; --k) { const int p = ipiv[k] - 1; if (p != k) { const double t = x[k]; x[k] = x[p]; x[p] = t; } }
+    }
+    __syncthreads();
+#undef AC
+}
+
+// Element matrices of FEMElement::forceVector/massMatrix/stiffMatrix
+// (:273-302, :178-213, :218-268), in global coordinates.
+__device__ void element_matrices(const FemKernelArgs &a, int f, int e) {
+    const int e0 = a.el_off[f], n0 = a.node_off[f];
+    const int ge = e0 + e;
+    const double ang = a.elang[ge], L = a.ellen[ge], L0 = a.len0[ge];
+    const double EE = a.E[ge], A = a.area[ge], I = a.I[ge];
+    const double a1 = a.nang[n0 + e], a2 = a.nang[n0 + e + 1];
+    const double u = (L * L - L0 * L0) / (L + L0);
+    const double t1 = atan2(cos(ang) * sin(a1) - sin(ang) * cos(a1), cos(ang) * cos(a1) + sin(ang) * sin(a1));
+    const double t2 = atan2(cos(ang) * sin(a2) - sin(ang) * cos(a2), cos(ang) * cos(a2) + sin(ang) * sin(a2));
+    const double F0 = (EE * A / L0) * u;
+    const double M1 = (2 * EE * I / L0) * (2.0 * t1 + t2);
+    const double M2 = (2 * EE * I / L0) * (t1 + 2.0 * t2);
+    double F[6] = {-F0, (1.0 / L0) * (M1 + M2), M1, F0, -(1.0 / L0) * (M1 + M2), M2};
+    for (int i = 0; i < 6; ++i) a.elF[6 * ge + i] = F[i];
+    double T[6][6];
+    Tmat(ang, T);
+    // mass
+    double Ml[6][6] = {};
+    const double C1 = a.rho[ge] * A * L0 / 420.0;
+    Ml[0][0] = C1 * 140.0; Ml[0][3] = C1 * 70.0; Ml[1][1] = C1 * 156.0; Ml[1][2] = C1 * 22.0 * L0;
+    Ml[1][4] = C1 * 54; Ml[1][5] = C1 * (-13.0 * L0); Ml[2][2] = C1 * 4.0 * (L0 * L0); Ml[2][4] = C1 * 13.0 * L0;
+    Ml[2][5] = C1 * (-3.0 * (L0 * L0)); Ml[3][3] = C1 * 140.0; Ml[4][4] = C1 * 156.0; Ml[4][5] = C1 * (-22.0 * L0);
+    Ml[5][5] = C1 * 4.0 * (L0 * L0);
+    for (int i = 1; i < 6; i++)
+        for (int j = 0; j < i; j++) Ml[i][j] = Ml[j][i];
+    // stiffness (linear + geometric)
+    double Kl[6][6] = {};
+    Kl[0][0] = EE * A / L0; Kl[0][3] = -EE * A / L0;
+    Kl[1][1] = 12.0 * EE * I / (L0 * L0 * L0); Kl[1][2] = 6.0 * EE * I / (L0 * L0);
+    Kl[1][4] = -12.0 * EE * I / (L0 * L0 * L0); Kl[1][5] = 6.0 * EE * I / (L0 * L0);
+    Kl[2][2] = 4.0 * EE * I / L0; Kl[2][4] = -6.0 * EE * I / (L0 * L0); Kl[2][5] = 2.0 * EE * I / L0;
+    Kl[3][3] = EE * A / L0; Kl[4][4] = 12.0 * EE * I / (L0 * L0 * L0); Kl[4][5] = -6.0 * EE * I / (L0 * L0);
+    Kl[5][5] = 4.0 * EE * I / L0;
+    for (int i = 1; i < 6; i++)
+        for (int j = 0; j < i; j++) Kl[i][j] = Kl[j][i];
+    const double Fa = -F[0], V0 = F[4];
+    Kl[0][1] += -V0 / L0; Kl[0][4] += V0 / L0; Kl[1][0] += -V0 / L0; Kl[1][1] += Fa / L0;
+    Kl[1][3] += V0 / L0; Kl[1][4] += -Fa / L0; Kl[3][1] += V0 / L0; Kl[3][4] += -V0 / L0;
+    Kl[4][0] += V0 / L0; Kl[4][1] += -Fa / L0; Kl[4][3] += -V0 / L0; Kl[4][4] += Fa / L0;
+    // T^T X T with the reference's k-ordered products
+    for (int which = 0; which < 2; ++which) {
+        double (*X)[6] = which == 0 ? Ml : Kl;
+        double P[6][6];
+        for (int r = 0; r < 6; ++r)
+            for (int c = 0; c < 6; ++c) {
+                double s = 0.0;
+                for (int k = 0; k < 6; ++k) s += T[k][r] * X[k][c];
+                P[r][c] = s;
+            }
+        double *out = which == 0 ? a.elM + 36 * (size_t)ge : a.elK + 36 * (size_t)ge;
+        for (int r = 0; r < 6; ++r)
+            for (int c = 0; c < 6; ++c) {
+                double s = 0.0;
+                for (int k = 0; k < 6; ++k) s += P[r][k] * T[k][c];
+                out[6 * r + c] = s;
+            }
+    }
+}
+
+// Load vector entry of DOF d (FEMElement::loadVector, :133-173), summing the
+// (element, IB child) contributions in the reference's order.
+__device__ double load_entry(const FemKernelArgs &a, int f, int d, double forceScale) {
+    const int e0 = a.el_off[f], ne = a.el_off[f + 1] - e0, mk0 = a.mk_off[f];
+    double val = 0.0;
+    const int elo = d / 3 - 1 < 0 ? 0 : d / 3 - 1;
+    const int ehi = d / 3 > ne - 1 ? ne - 1 : d / 3;
+    for (int e = elo; e <= ehi; ++e) {
+        const int i = d - 3 * e;
+        if (i < 0 || i > 5) continue;
+        const int ge = e0 + e;
+        double T[6][6];
+        Tmat(a.elang[ge], T);
+        const double L = a.ellen[ge];
+        for (int q = a.child_off[ge]; q < a.child_off[ge + 1]; ++q) {
+            const int node = a.child_node[q];
+            const double za = a.child_z1[q], zb = a.child_z2[q];
+            const double sc = a.flex.eps[mk0 + node] * 1.0 * forceScale;
+            const double fx[2] = {a.flex.F[3 * (mk0 + node)] * sc, a.flex.F[3 * (mk0 + node) + 1] * sc};
+            double fv[2];
+            for (int r = 0; r < 2; ++r) {
+                double s = 0.0;
+                for (int c = 0; c < 2; ++c) s += T[r][c] * fx[c];
+                fv[r] = s;
+            }
+            double Rl[6];
+            const double a2 = za * za, b2 = zb * zb;
+            Rl[0] = fv[0] * 0.5 * L * (0.5 * zb - 0.5 * za + 0.25 * a2 - 0.25 * b2);
+            Rl[1] = fv[1] * 0.5 * L * (0.5 * zb - 0.5 * za - a2 * a2 / 16.0 + b2 * b2 / 16.0 + 3.0 * a2 / 8.0 - 3.0 * b2 / 8.0);
+            Rl[2] = fv[1] * 0.5 * L * (L * (-a2 * a2 + b2 * b2) / 32.0 - L * (-(za * za * za) + (zb * zb * zb)) / 24.0 - L * (-a2 + b2) / 16.0 + L * (zb - za) / 8.0);
+            Rl[3] = fv[0] * 0.5 * L * (-0.25 * a2 + 0.25 * b2 + 0.5 * zb - 0.5 * za);
+            Rl[4] = fv[1] * 0.5 * L * (0.5 * zb - 0.5 * za + a2 * a2 / 16.0 - b2 * b2 / 16.0 - 3.0 * a2 / 8.0 + 3.0 * b2 / 8.0);
+            Rl[5] = fv[1] * 0.5 * L * (L * (-a2 * a2 + b2 * b2) / 32.0 + L * (-(za * za * za) + (zb * zb * zb)) / 24.0 - L * (-a2 + b2) / 16.0 - L * (zb - za) / 8.0);
+            double s = 0.0;
+            for (int c = 0; c < 6; ++c) s += T[c][i] * Rl[c];
+            val += s;
+        }
+    }
+    return val;
+}
+
+__global__ void k_fem_dynamic(FemKernelArgs a) {
+    const int f = blockIdx.x;
+    if (f >= a.nfil) return;
+    const int d0 = a.dof_off[f], nd = a.dof_off[f + 1] - d0;
+    const int e0 = a.el_off[f], ne = a.el_off[f + 1] - e0;
+    const int mk0 = a.mk_off[f], nmk = a.mk_off[f + 1] - mk0;
+    const int bc = a.bc[f];
+    double *M = a.M + (size_t)f * a.maxdof * a.maxdof;
+    double *K = a.K + (size_t)f * a.maxdof * a.maxdof;
+    double *Meff = a.tmp + 2 * (size_t)d0, *MF = a.tmp + 2 * (size_t)d0 + nd;
+    __shared__ int ipiv[512];
+    __shared__ int go;
+    const double Dt = a.dt;
+    for (int i = threadIdx.x; i < nd; i += blockDim.x) {
+        a.U[d0 + i] = a.U_n[d0 + i];
+        a.Ud[d0 + i] = a.Ud_n[d0 + i];
+        a.Udd[d0 + i] = a.Udd_n[d0 + i];
+    }
+    __syncthreads();
+    update_values(a, f);
+    const double forceScale = a.dm[f] / (Dt * Dt);
+    for (int d = threadIdx.x; d < nd; d += blockDim.x) a.R[d0 + d] = load_entry(a, f, d, forceScale);
+    __syncthreads();
+    const double a0 = 1.0 / (kNbAlpha * (Dt * Dt)), a2 = 1.0 / (kNbAlpha * Dt), a3 = 1.0 / (2.0 * kNbAlpha) - 1.0;
+    int it = 0;
+    double res = 0.0;
+    do {
+        for (int e = threadIdx.x; e < ne; e += blockDim.x) element_matrices(a, f, e);
+        __syncthreads();
+        // F, M, K assembly: each entry sums its elements in order starting from 0
+        for (int d = threadIdx.x; d < nd; d += blockDim.x) {
+            double s = 0.0;
+            for (int e = (d / 3 - 1 < 0 ? 0 : d / 3 - 1); e <= (d / 3 > ne - 1 ? ne - 1 : d / 3); ++e) {
+                const int i = d - 3 * e;
+                if (i < 0 || i > 5) continue;
+                double T[6][6];
+                Tmat(a.elang[e0 + e], T);
+                double fg = 0.0;
+                for (int c = 0; c < 6; ++c) fg += T[c][i] * a.elF[6 * (e0 + e) + c];
+                s += fg;
+            }
+            a.Fv[d0 + d] = s;
+        }
+        for (int q = threadIdx.x; q < nd * nd; q += blockDim.x) {
+            const int r = q / nd, c = q % nd;
+            double sm = 0.0, sk = 0.0;
+            const int lo = (r > c ? r : c) / 3 - 1, hi = (r < c ? r : c) / 3;
+            for (int e = (lo < 0 ? 0 : lo); e <= (hi > ne - 1 ? ne - 1 : hi); ++e) {
+                const int i = r - 3 * e, j = c - 3 * e;
+                if (i < 0 || i > 5 || j < 0 || j > 5) continue;
+                sm += a.elM[36 * (size_t)(e0 + e) + 6 * i + j];
+                sk += a.elK[36 * (size_t)(e0 + e) + 6 * i + j];
+            }
+            M[(size_t)r * nd + c] = sm;
+            K[(size_t)r * nd + c] = sk;
+        }
+        __syncthreads();
+        // FEMBody::setNewmark (:264-293)
+        for (int i = threadIdx.x; i < nd; i += blockDim.x)
+            Meff[i] = a0 * (a.U_n[d0 + i] - a.U[d0 + i]) + a2 * a.Ud[d0 + i] + a3 * a.Udd[d0 + i];
+        __syncthreads();
+        for (int i = threadIdx.x; i < nd; i += blockDim.x) {
+            double s = 0.0;
+            for (int j = 0; j < nd; ++j) s += M[(size_t)i * nd + j] * Meff[j];
+            MF[i] = s;
+        }
+        __syncthreads();
+        for (int i = threadIdx.x; i < nd; i += blockDim.x) a.Fv[d0 + i] = a.R[d0 + i] - a.Fv[d0 + i] + MF[i];
+        for (int q = threadIdx.x; q < nd * nd; q += blockDim.x) K[q] += a0 * M[q];
+        for (int i = threadIdx.x; i < nd; i += blockDim.x) a.delU[d0 + i] = a.Fv[d0 + i];
+        __syncthreads();
+        lu_solve_block(K, nd, bc, nd - bc, ipiv, a.delU + d0 + bc);
+        for (int i = threadIdx.x; i < bc; i += blockDim.x) a.delU[d0 + i] = 0.0;
+        __syncthreads();
+        for (int i = threadIdx.x; i < nd; i += blockDim.x) a.U[d0 + i] = a.U[d0 + i] + a.delU[d0 + i];
+        __syncthreads();
+        update_values(a, f);
+        if (threadIdx.x == 0) {
+            double dp = 0.0;
+            for (int i = 0; i < nd; i++) dp += a.delU[d0 + i] * a.delU[d0 + i];
+            const double L = a.len0[e0] * ne;
+            res = sqrt(dp / (double)nd) / L;
+            go = (res > 1e-10 && it + 1 < 20) ? 1 : 0;
+        }
+        __syncthreads();
+        ++it;
+    } while (go);
+    // FEMBody::finishNewmark (:236-255)
+    const double a6 = 1.0 / (kNbAlpha * (Dt * Dt)), a7 = -1.0 / (kNbAlpha * Dt), a8 = -(1.0 / (2.0 * kNbAlpha) - 1.0);
+    const double a9 = Dt * (1.0 - kNbDelta), a10 = kNbDelta * Dt;
+    for (int i = threadIdx.x; i < nd; i += blockDim.x) {
+        const double s = a6 * (a.U[d0 + i] - a.U_n[d0 + i]) + a7 * a.Ud[d0 + i] + a8 * a.Udd[d0 + i];
+        a.Ud[d0 + i] = a.Ud[d0 + i] + a9 * a.Udd[d0 + i] + a10 * s;
+        a.Udd[d0 + i] = s;
+    }
+    if (threadIdx.x == 0) {
+        a.it[f] = it;
+        a.res[f] = res;
+    }
+    __syncthreads();
+    // FEMBody::updateIBMarkers (:329-370)
+    for (int m = threadIdx.x; m < nmk; m += blockDim.x) {
+        const int e = a.parent_el[mk0 + m];
+        const int ge = e0 + e;
+        const double z = a.parent_zeta[mk0 + m];
+        double T[6][6];
+        Tmat(a.elang[ge], T);
+        double lU[6], lV[6];
+        for (int r = 0; r < 6; ++r) {
+            double s1 = 0.0, s2 = 0.0;
+            for (int c = 0; c < 6; ++c) {
+                s1 += T[r][c] * a.U[d0 + e * 3 + c];
+                s2 += T[r][c] * a.Ud[d0 + e * 3 + c];
+            }
+            lU[r] = s1;
+            lV[r] = s2;
+        }
+        const double zz = (z + 1.0) / 2.0, L = a.ellen[ge];
+        const double N0 = 1.0 - (z + 1.0) / 2.0;
+        const double N1 = 1.0 - 3.0 * (zz * zz) + 2.0 * (zz * zz * zz);
+        const double N2 = (zz - 2.0 * (zz * zz) + (zz * zz * zz)) * L;
+        const double N3 = (z + 1.0) / 2.0;
+        const double N4 = 3.0 * (zz * zz) - 2.0 * (zz * zz * zz);
+        const double N5 = (-(zz * zz) + (zz * zz * zz)) * L;
+        const double su[2] = {lU[0] * N0 + lU[3] * N3, lU[1] * N1 + lU[2] * N2 + lU[4] * N4 + lU[5] * N5};
+        const double sv[2] = {lV[0] * N0 + lV[3] * N3, lV[1] * N1 + lV[2] * N2 + lV[4] * N4 + lV[5] * N5};
+        const double Tt[2][2] = {{T[0][0], T[1][0]}, {T[0][1], T[1][1]}};
+        const int g = mk0 + m;
+        for (int r = 0; r < 2; ++r) {
+            double s1 = 0.0, s2 = 0.0;
+            for (int c = 0; c < 2; ++c) { s1 += Tt[r][c] * su[c]; s2 += Tt[r][c] * sv[c]; }
+            const double gv = s2 * (a.dt / a.dh);
+            a.flex.pos[3 * g + r] = a.mpos0[3 * g + r] + s1;
+            a.flex.vel_km1[3 * g + r] = a.flex.vel[3 * g + r];
+            a.flex.vel[3 * g + r] = kRelax * gv + (1.0 - kRelax) * a.flex.vel_km1[3 * g + r];
+        }
+    }
+}
+
+__device__ double delta_kernel_d(double radius, double dilation) {
+    const double mag_r = fabs(radius) / dilation;
+    if (mag_r > 1.5) return 0.0;
+    if (mag_r > 0.5) return (5.0 - (3.0 * mag_r) - sqrt(-3.0 * ((1.0 - mag_r) * (1.0 - mag_r)) + 1.0)) / 6.0;
+    return (1.0 + sqrt(1.0 - 3.0 * (mag_r * mag_r))) / 3.0;
+}
+
+// Supports, ds and epsilon of one filament's markers (ibm_findSupport,
+// ibm_computeDs, ibm_findEpsilon for a moving body).
+__global__ void k_flex_support(FemKernelArgs a) {
+    const int f = blockIdx.x;
+    if (f >= a.nfil) return;
+    const int mk0 = a.mk_off[f], nmk = a.mk_off[f + 1] - mk0;
+    const int D = a.dims;
+    const double dh = a.dh;
+    const FlexArgs &x = a.flex;
+    for (int m = threadIdx.x; m < nmk; m += blockDim.x) {
+        const int g = mk0 + m;
+        const double *p = &x.pos[3 * g];
+        const int in = (int)floor((p[0] - a.gstart[0]) / dh);
+        const int jn = (int)floor((p[1] - a.gstart[1]) / dh);
+        const int kn = D == 3 ? (int)floor((p[2] - a.gstart[2]) / dh) : 0;
+        int ns = 0;
+        if (in < 0 || jn < 0 || kn < 0 || in >= a.N || jn >= a.M_ || kn >= a.K_) {
+            atomicExch(a.error, 1);
+            x.nsupp[g] = 0;
+            continue;
+        }
+        const double nearp[3] = {a.hx[in], a.hy[jn], D == 3 ? a.hz[kn] : 0.0};
+        auto add = [&](int i, int j, int k, const double e[3]) {
+            if (ns >= kFlexMaxSupp) { atomicExch(a.error, 2); return; }
+            const int s = g * kFlexMaxSupp + ns;
+            x.supp[s] = k + j * a.K_ + i * a.K_ * a.M_;
+            x.sx[s] = e[0]; x.sy[s] = e[1]; x.sz[s] = e[2];
+            double v = delta_kernel_d((e[0] - p[0]) / dh, 1.0) * delta_kernel_d((e[1] - p[1]) / dh, 1.0);
+            if (D == 3) v = v * delta_kernel_d((e[2] - p[2]) / dh, 1.0);
+            x.delta[s] = v;
+            ++ns;
+        };
+        add(in, jn, kn, nearp);
+        for (int i = in - 5; i <= in + 5; i++)
+            for (int j = jn - 5; j <= jn + 5; j++)
+                for (int k = (D == 3 ? kn - 5 : 0); k <= (D == 3 ? kn + 5 : 0); k++) {
+                    double e[3] = {nearp[0] + (i - in) * dh, nearp[1] + (j - jn) * dh, nearp[2]};
+                    if (D == 3) e[2] = nearp[2] + (k - kn) * dh;
+                    const bool cage = (fabs(p[0] - e[0]) / dh < 1.5) && (fabs(p[1] - e[1]) / dh < 1.5) &&
+                                      (D == 2 || fabs(p[2] - e[2]) / dh < 1.5);
+                    const bool dom = !(e[0] < a.edges[0] || e[0] > a.edges[1] || e[1] < a.edges[2] || e[1] > a.edges[3] ||
+                                       (D == 3 && (e[2] < a.edges[4] || e[2] > a.edges[5])));
+                    if (cage && dom && (i != in || j != jn || (D == 3 && k != kn))) {
+                        if (i < 0 || j < 0 || k < 0 || i >= a.N || j >= a.M_ || k >= a.K_) {
+                            atomicExch(a.error, 1);
+                            continue;
+                        }
+                        add(i, j, k, e);
+                    }
+                }
+        x.nsupp[g] = ns;
+    }
+    __syncthreads();
+    for (int m = threadIdx.x; m < nmk; m += blockDim.x) {
+        const int g = mk0 + m;
+        double ds = 10.0;
+        for (int q = 0; q < nmk; ++q) {
+            if (q == m) continue;
+            double r = 0.0;
+            for (int d = 0; d < 3; ++d) {
+                const double v = x.pos[3 * g + d] - x.pos[3 * (mk0 + q) + d];
+                r += v * v;
+            }
+            const double dist = sqrt(r) / dh;
+            if (dist < ds) ds = dist;
+        }
+        x.ds[g] = ds;
+    }
+    __syncthreads();
+    double *A = a.epsA + (size_t)f * a.maxmk * a.maxmk;
+    for (int q = threadIdx.x; q < nmk * nmk; q += blockDim.x) {
+        const int I = q / nmk, J = q % nmk;
+        const int gI = mk0 + I, gJ = mk0 + J;
+        double aij = 0.0;
+        for (int s = 0; s < x.nsupp[gI]; ++s) {
+            const int si = gI * kFlexMaxSupp + s;
+            double dJ = delta_kernel_d((x.pos[3 * gJ + 0] - x.sx[si]) / dh, 1.0) *
+                        delta_kernel_d((x.pos[3 * gJ + 1] - x.sy[si]) / dh, 1.0);
+            if (D == 3) dJ = dJ * delta_kernel_d((x.pos[3 * gJ + 2] - x.sz[si]) / dh, 1.0);
+            aij += x.delta[si] * dJ * 1.0;
+        }
+        A[(size_t)I * nmk + J] = aij * x.ds[gJ];
+    }
+    __shared__ int ipiv[512];
+    for (int m = threadIdx.x; m < nmk; m += blockDim.x) x.eps[mk0 + m] = 1.0;
+    __syncthreads();
+    lu_solve_block(A, nmk, 0, nmk, ipiv, x.eps + mk0);
+}
+
+// max over flexible markers of |U - U_km1| / (L_UX0 dt/dh)  (ibm_checkVelDiff)
+__global__ void k_fsi_residual(FemKernelArgs a) {
+    const int f = blockIdx.x;
+    if (f >= a.nfil) return;
+    const int mk0 = a.mk_off[f], nmk = a.mk_off[f + 1] - mk0;
+    for (int m = threadIdx.x; m < nmk; m += blockDim.x) {
+        const int g = mk0 + m;
+        double r = 0.0;
+        for (int d = 0; d < 3; ++d) {
+            const double v = a.flex.vel[3 * g + d] - a.flex.vel_km1[3 * g + d];
+            r += v * v;
+        }
+        const double v = fabs(sqrt(r) / a.velscale[f]);
+        atomicMax(reinterpret_cast<unsigned long long *>(a.fsi_res), (unsigned long long)__double_as_longlong(v));
+    }
+}
+
+__global__ void k_fem_commit(FemKernelArgs a, int ndof_total) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= ndof_total) return;
+    a.U_n[i] = a.U[i];
+    a.Ud_n[i] = a.Ud[i];
+    a.Udd_n[i] = a.Udd[i];
+}
+
+FemKernelArgs make_fem_args(luma_gpu_grid *g) {
+    FemDevice &d = g->ibm->fem;
+    FemKernelArgs a;
+    memset(&a, 0, sizeof a);
+    a.nfil = d.nfil; a.maxdof = d.maxdof; a.maxmk = d.maxmk;
+    a.node_off = d.node_off; a.el_off = d.el_off; a.dof_off = d.dof_off; a.mk_off = d.mk_off; a.bc = d.bc;
+    a.dm = d.dm; a.velscale = d.velscale;
+    a.pos0 = d.pos0; a.ang0 = d.ang0;
+    a.len0 = d.len0; a.area = d.area; a.I = d.I; a.E = d.E; a.rho = d.rho;
+    a.child_off = d.child_off; a.child_node = d.child_node; a.child_z1 = d.child_z1; a.child_z2 = d.child_z2;
+    a.U = d.U; a.U_n = d.U_n; a.Ud = d.Ud; a.Ud_n = d.Ud_n; a.Udd = d.Udd; a.Udd_n = d.Udd_n;
+    a.R = d.R; a.Fv = d.Fv; a.delU = d.delU;
+    a.M = d.M; a.K = d.K; a.epsA = d.epsA;
+    a.parent_el = d.parent_el; a.parent_zeta = d.parent_zeta; a.mpos0 = d.mpos0;
+    a.it = d.it; a.res = d.res; a.fsi_res = d.fsi_res;
+    a.dt = g->d.dt; a.dh = g->d.dh;
+    a.flex = d.flex;
+    a.N = g->d.N; a.M_ = g->d.M; a.K_ = g->d.K; a.dims = g->d.dims; a.level = g->d.level;
+    return a;
+}
+
+}  // namespace
+
+// ---- host side -------------------------------------------------------------
+
+struct FemScratch {
+    double *elF = nullptr, *elM = nullptr, *elK = nullptr, *elang = nullptr, *ellen = nullptr;
+    double *npos = nullptr, *nang = nullptr, *tmp = nullptr;
+    double *hx = nullptr, *hy = nullptr, *hz = nullptr;
+    int *error = nullptr;
+};
+static std::vector<std::pair<luma_gpu_grid *, FemScratch>> g_scratch;
+
+static FemScratch *scratch_of(luma_gpu_grid *g) {
+    for (auto &p : g_scratch)
+        if (p.first == g) return &p.second;
+    return nullptr;
+}
+
+template <class T>
+static int up(T **dst, const std::vector<T> &src) {
+    cudaFree(*dst);
+    *dst = nullptr;
+    if (cudaMalloc(dst, std::max<size_t>(1, src.size()) * sizeof(T)) != cudaSuccess)
+        return luma_set_error(LUMA_E_NOMEM, "FEM device allocation failed");
+    if (!src.empty() && cudaMemcpy(*dst, src.data(), src.size() * sizeof(T), cudaMemcpyHostToDevice) != cudaSuccess)
+        return luma_set_error(LUMA_E_CUDA, "FEM upload failed");
+    return LUMA_OK;
+}
+template <class T>
+static int zeros(T **dst, size_t n) {
+    return up(dst, std::vector<T>(n, T(0)));
+}
+
+// Upload every filament of the grid (called once by luma_gpu_ibm_initialise).
+int luma_fem_upload(luma_gpu_grid *g) {
+    IbmState &st = *g->ibm;
+    FemDevice &d = st.fem;
+    std::vector<int> node_off(1, 0), el_off(1, 0), dof_off(1, 0), mk_off(1, 0), bc, child_off(1, 0), child_node,
+        parent_el;
+    std::vector<double> dm, vs, pos0, ang0, len0, area, I, E, rho, cz1, cz2, pz, mpos0, mvel, mpos;
+    int maxdof = 0, maxmk = 0;
+    for (size_t k = 0; k < st.flex.size(); ++k) {
+        const FlexBody &fb = st.flex[k];
+        const IbmBody &ib = st.bodies[st.flex_body[k]];
+        bc.push_back(fb.bc);
+        dm.push_back(fb.dm);
+        vs.push_back(fb.velscale);
+        pos0.insert(pos0.end(), fb.pos0.begin(), fb.pos0.end());
+        ang0.insert(ang0.end(), fb.ang0.begin(), fb.ang0.end());
+        for (int e = 0; e < fb.nel; ++e) {
+            len0.push_back(fb.len0[e]); area.push_back(fb.area[e]); I.push_back(fb.I[e]); E.push_back(fb.E[e]);
+            rho.push_back(fb.rho[e]);
+            for (int q = fb.child_off[e]; q < fb.child_off[e + 1]; ++q) {
+                child_node.push_back(fb.child_node[q]);
+                cz1.push_back(fb.child_z1[q]);
+                cz2.push_back(fb.child_z2[q]);
+            }
+            child_off.push_back((int)child_node.size());
+        }
+        parent_el.insert(parent_el.end(), fb.parent_el.begin(), fb.parent_el.end());
+        pz.insert(pz.end(), fb.parent_zeta.begin(), fb.parent_zeta.end());
+        mpos0.insert(mpos0.end(), fb.mpos0.begin(), fb.mpos0.end());
+        mpos.insert(mpos.end(), ib.pos.begin(), ib.pos.end());
+        mvel.insert(mvel.end(), ib.vel.begin(), ib.vel.end());
+        node_off.push_back(node_off.back() + fb.nel + 1);
+        el_off.push_back(el_off.back() + fb.nel);
+        dof_off.push_back(dof_off.back() + 3 * (fb.nel + 1));
+        mk_off.push_back(mk_off.back() + fb.nm);
+        maxdof = std::max(maxdof, 3 * (fb.nel + 1));
+        maxmk = std::max(maxmk, fb.nm);
+    }
+    if (maxdof > 512 || maxmk > 512) return luma_set_error(LUMA_E_INVALID, "filament too large for the device solver");
+    d.nfil = (int)st.flex.size();
+    d.maxdof = maxdof;
+    d.maxmk = maxmk;
+    const int ndof = dof_off.back(), nmk = mk_off.back(), nel = el_off.back(), nnode = node_off.back();
+    int rc;
+    if ((rc = up(&d.node_off, node_off)) || (rc = up(&d.el_off, el_off)) || (rc = up(&d.dof_off, dof_off)) ||
+        (rc = up(&d.mk_off, mk_off)) || (rc = up(&d.bc, bc)) || (rc = up(&d.dm, dm)) || (rc = up(&d.velscale, vs)) ||
+        (rc = up(&d.pos0, pos0)) || (rc = up(&d.ang0, ang0)) || (rc = up(&d.len0, len0)) || (rc = up(&d.area, area)) ||
+        (rc = up(&d.I, I)) || (rc = up(&d.E, E)) || (rc = up(&d.rho, rho)) || (rc = up(&d.child_off, child_off)) ||
+        (rc = up(&d.child_node, child_node)) || (rc = up(&d.child_z1, cz1)) || (rc = up(&d.child_z2, cz2)) ||
+        (rc = up(&d.parent_el, parent_el)) || (rc = up(&d.parent_zeta, pz)) || (rc = up(&d.mpos0, mpos0)))
+        return rc;
+    if ((rc = zeros(&d.U, ndof)) || (rc = zeros(&d.U_n, ndof)) || (rc = zeros(&d.Ud, ndof)) ||
+        (rc = zeros(&d.Ud_n, ndof)) || (rc = zeros(&d.Udd, ndof)) || (rc = zeros(&d.Udd_n, ndof)) ||
+        (rc = zeros(&d.R, ndof)) || (rc = zeros(&d.Fv, ndof)) || (rc = zeros(&d.delU, ndof)) ||
+        (rc = zeros(&d.M, (size_t)d.nfil * maxdof * maxdof)) || (rc = zeros(&d.K, (size_t)d.nfil * maxdof * maxdof)) ||
+        (rc = zeros(&d.epsA, (size_t)d.nfil * maxmk * maxmk)) || (rc = zeros(&d.it, d.nfil)) ||
+        (rc = zeros(&d.res, d.nfil)) || (rc = zeros(&d.fsi_res, 1)))
+        return rc;
+    FlexArgs &x = d.flex;
+    x.nm = nmk;
+    x.dims = g->d.dims;
+    if ((rc = up(&x.pos, mpos)) || (rc = up(&x.vel, mvel)) || (rc = zeros(&x.vel_km1, 3 * (size_t)nmk)) ||
+        (rc = zeros(&x.F, 3 * (size_t)nmk)) || (rc = zeros(&x.eps, nmk)) || (rc = zeros(&x.ds, nmk)) ||
+        (rc = zeros(&x.irho, nmk)) || (rc = zeros(&x.imom, 3 * (size_t)nmk)) || (rc = zeros(&x.nsupp, nmk)) ||
+        (rc = zeros(&x.supp, (size_t)nmk * kFlexMaxSupp)) || (rc = zeros(&x.delta, (size_t)nmk * kFlexMaxSupp)) ||
+        (rc = zeros(&x.sx, (size_t)nmk * kFlexMaxSupp)) || (rc = zeros(&x.sy, (size_t)nmk * kFlexMaxSupp)) ||
+        (rc = zeros(&x.sz, (size_t)nmk * kFlexMaxSupp)))
+        return rc;
+    FemScratch sc;
+    if ((rc = zeros(&sc.elF, 6 * (size_t)nel)) || (rc = zeros(&sc.elM, 36 * (size_t)nel)) ||
+        (rc = zeros(&sc.elK, 36 * (size_t)nel)) || (rc = zeros(&sc.elang, nel)) || (rc = zeros(&sc.ellen, nel)) ||
+        (rc = zeros(&sc.npos, 3 * (size_t)nnode)) || (rc = zeros(&sc.nang, nnode)) ||
+        (rc = zeros(&sc.tmp, 2 * (size_t)ndof)) || (rc = up(&sc.hx, g->hx)) || (rc = up(&sc.hy, g->hy)) ||
+        (rc = up(&sc.hz, g->hz)) || (rc = zeros(&sc.error, 1)))
+        return rc;
+    g_scratch.push_back({g, sc});
+    st.u_n = nullptr;
+    const size_t rs = g->d.precision == LUMA_PREC_FP64 ? 8 : 4;
+    if (cudaMalloc(&st.u_n, g->n * g->d.dims * rs) != cudaSuccess)
+        return luma_set_error(LUMA_E_NOMEM, "u_n allocation failed");
+    return LUMA_OK;
+}
+
+static FemKernelArgs full_args(luma_gpu_grid *g) {
+    FemKernelArgs a = make_fem_args(g);
+    FemScratch *sc = scratch_of(g);
+    a.elF = sc->elF; a.elM = sc->elM; a.elK = sc->elK; a.elang = sc->elang; a.ellen = sc->ellen;
+    a.npos = sc->npos; a.nang = sc->nang; a.tmp = sc->tmp;
+    a.hx = sc->hx; a.hy = sc->hy; a.hz = sc->hz; a.error = sc->error;
+    const luma_gpu_grid *r = g;
+    while (r->parent) r = r->parent;
+    for (int q = 0; q < 6; ++q) a.edges[q] = r->d.global_edges[q];
+    for (int ax = 0; ax < 3; ++ax) {
+        const std::vector<double> &p = ax == 0 ? g->hx : (ax == 1 ? g->hy : g->hz);
+        a.gstart[ax] = g->d.level == 0 ? 0.0 : p[0] - g->d.dh / 2.0;
+    }
+    return a;
+}
+
+// Supports/ds/epsilon of the filaments' markers (initialise and after FEM).
+int luma_fem_supports(luma_gpu_grid *g) {
+    FemKernelArgs a = full_args(g);
+    k_flex_support<<<a.nfil, 128, 0, g->stream>>>(a);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return luma_set_error(LUMA_E_CUDA, "flex support: %s", cudaGetErrorString(e));
+    return LUMA_OK;
+}
+
+// ObjectManager::ibm_moveBodies (:61-104) for the filaments of a grid.
+int luma_fem_move_bodies(luma_gpu_grid *g) {
+    FemKernelArgs a = full_args(g);
+    k_fem_dynamic<<<a.nfil, 128, 0, g->stream>>>(a);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return luma_set_error(LUMA_E_CUDA, "FEM: %s", cudaGetErrorString(e));
+    return luma_fem_supports(g);
+}
+
+int luma_fem_residual(luma_gpu_grid *g, double *res) {
+    FemKernelArgs a = full_args(g);
+    cudaMemsetAsync(a.fsi_res, 0, sizeof(double), g->stream);
+    k_fsi_residual<<<a.nfil, 128, 0, g->stream>>>(a);
+    int err = 0;
+    cudaMemcpyAsync(res, a.fsi_res, sizeof(double), cudaMemcpyDeviceToHost, g->stream);
+    cudaMemcpyAsync(&err, a.error, sizeof(int), cudaMemcpyDeviceToHost, g->stream);
+    cudaError_t e = cudaStreamSynchronize(g->stream);
+    if (e != cudaSuccess) return luma_set_error(LUMA_E_CUDA, "FSI residual: %s", cudaGetErrorString(e));
+    if (err) return luma_set_error(LUMA_E_DOMAIN, "a filament marker left its grid (code %d)", err);
+    return LUMA_OK;
+}
+
+int luma_fem_commit(luma_gpu_grid *g) {
+    FemKernelArgs a = full_args(g);
+    int ndof = 0;
+    for (const FlexBody &fb : g->ibm->flex) ndof += 3 * (fb.nel + 1);
+    k_fem_commit<<<(ndof + 127) / 128, 128, 0, g->stream>>>(a, ndof);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return luma_set_error(LUMA_E_CUDA, "FEM commit: %s", cudaGetErrorString(e));
+    return LUMA_OK;
+}
+
+void luma_fem_free(luma_gpu_grid *g) {
+    for (size_t i = 0; i < g_scratch.size(); ++i)
+        if (g_scratch[i].first == g) {
+            FemScratch &s = g_scratch[i].second;
+            cudaFree(s.elF); cudaFree(s.elM); cudaFree(s.elK); cudaFree(s.elang); cudaFree(s.ellen);
+            cudaFree(s.npos); cudaFree(s.nang); cudaFree(s.tmp); cudaFree(s.hx); cudaFree(s.hy); cudaFree(s.hz);
+            cudaFree(s.error);
+            g_scratch.erase(g_scratch.begin() + i);
+            break;
+        }
+    if (!g->ibm) return;
+    FemDevice &d = g->ibm->fem;
+    void *ptrs[] = {d.node_off, d.el_off, d.dof_off, d.mk_off, d.bc, d.dm, d.velscale, d.pos0, d.ang0, d.len0,
+                    d.area, d.I, d.E, d.rho, d.child_off, d.child_node, d.child_z1, d.child_z2, d.U, d.U_n, d.Ud,
+                    d.Ud_n, d.Udd, d.Udd_n, d.R, d.Fv, d.delU, d.M, d.K, d.epsA, d.parent_el, d.parent_zeta,
+                    d.mpos0, d.it, d.res, d.fsi_res, d.flex.pos, d.flex.vel, d.flex.vel_km1, d.flex.F, d.flex.eps,
+                    d.flex.ds, d.flex.irho, d.flex.imom, d.flex.nsupp, d.flex.supp, d.flex.delta, d.flex.sx,
+                    d.flex.sy, d.flex.sz, g->ibm->u_n};
+    for (void *p : ptrs) cudaFree(p);
+    d = FemDevice();
+    g->ibm->u_n = nullptr;
+}
+
+// A flexible filament as the reference's FILAMENT_ARRAY reader builds it
+// (inc/Body.h:143-187 markers, src/FEMBody.cpp:48-130 beam,
+// :378-424 IB <-> FEM mapping).  2D only, as the reference's FEM is planar.
+extern "C" int luma_gpu_ibm_add_filament(luma_gpu_grid *g, const double start[3], double length, double height,
+                                         double depth, double angle_v, int nel, int clamped, double density,
+                                         double E, double dm, double fsi_vel_scale, int *body_index) {
+    if (!g || !start || nel <= 0 || length <= 0) return luma_set_error(LUMA_E_INVALID, "bad filament arguments");
+    if (g->d.dims != 2)
+        return luma_set_error(LUMA_E_INVALID, "FEM filaments are planar: the reference's FEM aborts in 3D");
+    const double dh = g->d.dh;
+    const int nmk = (int)std::floor(length / dh) + 1;
+    const double spacing = length / (nmk - 1);
+    const double spacing_h = spacing * std::cos(angle_v * kPi / 180);
+    std::vector<double> xyz(3 * (size_t)nmk);
+    for (int i = 0; i < nmk; i++) {
+        xyz[3 * i + 0] = start[0] + i * spacing_h * std::cos(0.0 * kPi / 180.0);
+        xyz[3 * i + 1] = start[1] + i * spacing * std::sin(angle_v * kPi / 180.0);
+        xyz[3 * i + 2] = start[2] + i * spacing_h * std::sin(0.0 * kPi / 180.0);
+    }
+    int ib = -1;
+    int rc = luma_gpu_ibm_add_body(g, nmk, xyz.data(), nullptr, &ib);
+    if (rc) return rc;
+    FlexBody fb;
+    fb.nel = nel;
+    fb.nm = nmk;
+    fb.bc = clamped ? 3 : 2;
+    fb.dm = dm;
+    fb.velscale = fsi_vel_scale;
+    const double fs = length / nel, fs_h = fs * std::cos(angle_v * kPi / 180);
+    for (int i = 0; i < nel + 1; i++) {
+        fb.pos0.push_back(start[0] + i * fs_h * std::cos(0.0 * kPi / 180.0));
+        fb.pos0.push_back(start[1] + i * fs * std::sin(angle_v * kPi / 180.0));
+        fb.pos0.push_back(start[2] + i * fs_h * std::sin(0.0 * kPi / 180.0));
+        fb.ang0.push_back(angle_v * kPi / 180.0);
+    }
+    depth = dh;  // 2D: unit lattice depth (src/FEMBody.cpp:103-105)
+    for (int e = 0; e < nel; ++e) {
+        fb.len0.push_back(fs);
+        fb.area.push_back(height * depth);
+        fb.I.push_back(depth * (height * height * height) / 12.0);
+        fb.E.push_back(E);
+        fb.rho.push_back(density);
+    }
+    const int nI = nmk, nF = nel + 1;
+    fb.parent_el.assign(nI, 0);
+    fb.parent_zeta.assign(nI, -1.0);
+    for (int i = 1; i < nI; i++) {
+        const double q = i * ((nF - 1.0) / (nI - 1.0));
+        if (std::fmod(q, 1.0) == 0.0) {
+            fb.parent_el[i] = (int)std::floor(q) - 1;
+            fb.parent_zeta[i] = 1.0;
+        } else {
+            fb.parent_el[i] = (int)std::floor(q);
+            fb.parent_zeta[i] = std::fmod(q, 1.0) * 2.0 - 1.0;
+        }
+    }
+    fb.child_off.assign(1, 0);
+    for (int e = 0; e < nel; ++e) {
+        for (int node = 0; node < nI; ++node) {
+            double n1 = -1 + 2.0 * ((node - 0.5) * ((nF - 1.0) / (nI - 1.0)) - e) / 1.0;
+            double n2 = -1 + 2.0 * ((node + 0.5) * ((nF - 1.0) / (nI - 1.0)) - e) / 1.0;
+            if ((n1 > -1.0 && n1 < 1.0) || (n2 > -1.0 && n2 < 1.0)) {
+                if (n1 < -1.0) n1 = -1.0;
+                if (n2 > 1.0) n2 = 1.0;
+                fb.child_node.push_back(node);
+                fb.child_z1.push_back(n1);
+                fb.child_z2.push_back(n2);
+            }
+        }
+        fb.child_off.push_back((int)fb.child_node.size());
+    }
+    fb.mpos0 = xyz;
+    g->ibm->flex.push_back(fb);
+    g->ibm->flex_body.push_back(ib);
+    g->ibm->has_flexible = true;
+    if (body_index) *body_index = ib;
+    return LUMA_OK;
+}

@@ -48,6 +48,13 @@ int luma_set_error(int code, const char *fmt, ...);
 int luma_ibm_reset_forces(luma_gpu_grid *g, const luma::StepArgs &a);
 int luma_ibm_apply(luma_gpu_grid *g, const luma::StepArgs &a);
 void luma_ibm_free(luma_gpu_grid *g);
+// fem.cu
+int luma_fem_upload(luma_gpu_grid *g);
+int luma_fem_supports(luma_gpu_grid *g);
+int luma_fem_move_bodies(luma_gpu_grid *g);
+int luma_fem_residual(luma_gpu_grid *g, double *res);
+int luma_fem_commit(luma_gpu_grid *g);
+void luma_fem_free(luma_gpu_grid *g);
 
 namespace luma {
 
@@ -71,12 +78,67 @@ struct IbmDevice {
     int *usite = nullptr, *uoff = nullptr, *uref = nullptr;  // unique support sites -> supports in order
 };
 
+// Flexible filaments: markers with fixed-capacity support slots (supports
+// move every FSI iteration) and the FEM beam state, all device resident.
+constexpr int kFlexMaxSupp = 27;
+
+struct FlexArgs {
+    int nm;                     // flexible markers on this grid (all filaments)
+    int dims;
+    double *pos, *vel, *vel_km1, *F, *eps, *ds, *irho, *imom;  // per marker (3 for pos/vel/F/imom)
+    int *nsupp, *supp;          // supp[m*kFlexMaxSupp + s] = site id
+    double *delta, *sx, *sy, *sz;
+};
+
+struct FemDevice {
+    int nfil = 0, maxdof = 0, maxmk = 0;
+    // per filament offsets
+    int *node_off = nullptr, *el_off = nullptr, *dof_off = nullptr, *mk_off = nullptr, *bc = nullptr;
+    double *dm = nullptr, *velscale = nullptr;
+    // nodes
+    double *pos0 = nullptr, *ang0 = nullptr;
+    // elements
+    double *len0 = nullptr, *area = nullptr, *I = nullptr, *E = nullptr, *rho = nullptr;
+    int *child_off = nullptr, *child_node = nullptr;
+    double *child_z1 = nullptr, *child_z2 = nullptr;
+    // state per DOF
+    double *U = nullptr, *U_n = nullptr, *Ud = nullptr, *Ud_n = nullptr, *Udd = nullptr, *Udd_n = nullptr;
+    double *R = nullptr, *Fv = nullptr, *delU = nullptr;
+    // scratch: dense M, K per filament (maxdof^2 each), element matrices
+    double *M = nullptr, *K = nullptr, *epsA = nullptr;
+    // markers
+    int *parent_el = nullptr;
+    double *parent_zeta = nullptr, *mpos0 = nullptr;
+    // outputs
+    int *it = nullptr;
+    double *res = nullptr, *fsi_res = nullptr;
+    // flexible IB marker arrays
+    FlexArgs flex{};
+};
+
+struct FlexBody {                // host description of one filament
+    int nel = 0, nm = 0, bc = 3;
+    double dm = 0, velscale = 1;
+    std::vector<double> pos0, ang0;          // nodes
+    std::vector<double> len0, area, I, E, rho;  // elements
+    std::vector<int> child_off, child_node;
+    std::vector<double> child_z1, child_z2;
+    std::vector<int> parent_el;
+    std::vector<double> parent_zeta, mpos0;  // markers
+};
+
 struct IbmState {
     bool has_bodies = false;
     bool has_flexible = false;
     bool ready = false;
     std::vector<IbmBody> bodies;
     IbmDevice dev;
+    std::vector<FlexBody> flex;      // filaments (their markers are bodies too, in order)
+    std::vector<int> flex_body;      // IB body index of each filament
+    FemDevice fem;
+    double *u_n = nullptr;           // start-of-step velocity (R*), for FSI resets
+    int fsi_iterations = 0;
+    double fsi_residual = 0;
 };
 
 // Marker-side arguments of the IBM kernels.

@@ -190,7 +190,11 @@ int upload_bodies(luma_gpu_grid *g) {
     std::vector<double> vel, eps, ds, area, mdelta;
     std::vector<int> moff(1, 0), msite, smarker;
     int mbase = 0;
-    for (const IbmBody &b : st.bodies) {
+    for (size_t bi = 0; bi < st.bodies.size(); ++bi) {
+        const IbmBody &b = st.bodies[bi];
+        bool flexible = false;
+        for (int fbi : st.flex_body) flexible |= (fbi == (int)bi);
+        if (flexible) continue;  // moving markers live in the FEM/flex arrays
         for (int m = 0; m < b.nm; ++m) {
             for (int d = 0; d < 3; ++d) vel.push_back(b.vel[3 * m + d]);
             eps.push_back(b.eps[m]);
@@ -265,6 +269,10 @@ int init_tree(luma_gpu_grid *g) {
         for (IbmBody &b : st.bodies) find_epsilon(g, b);
         int rc = upload_bodies(g);
         if (rc) return rc;
+        if (st.has_flexible) {
+            if ((rc = luma_fem_upload(g))) return rc;
+            if ((rc = luma_fem_supports(g))) return rc;
+        }
         st.ready = true;
     }
     for (luma_gpu_grid *c : g->kids) {
@@ -286,17 +294,50 @@ int luma_ibm_reset_forces(luma_gpu_grid *g, const StepArgs &a) {
     return LUMA_OK;
 }
 
-int luma_ibm_apply(luma_gpu_grid *g, const StepArgs &a) {
-    if (!g->ibm->ready) return luma_set_error(LUMA_E_STATE, "luma_gpu_ibm_initialise was not called");
+static int ibm_pass(luma_gpu_grid *g, const StepArgs &a) {
     const IbmArgs b = make_ibm_args(g);
+    FlexArgs f{};
+    if (g->ibm->has_flexible) f = g->ibm->fem.flex;
     cudaError_t e = dispatch(g->d.Q, g->d.precision, [&](auto q, auto p) {
-        return launch_ibm_pass<decltype(q)::value, decltype(p)>(a, b, g->stream);
+        return launch_ibm_pass<decltype(q)::value, decltype(p)>(a, b, f, g->stream);
     });
     if (e != cudaSuccess) return luma_set_error(LUMA_E_CUDA, "IBM pass: %s", cudaGetErrorString(e));
     return LUMA_OK;
 }
 
+// ObjectManager::ibm_apply(g, true) (:33-54) with ibm_moveBodies (:61-104)
+// and the FSI sub-iterations (:111-185): u_n, the start-of-step velocity,
+// was saved by the caller's first loop; each sub-iteration restores it,
+// resets the forces, re-runs the pass and the FEM, and checks the marker
+// velocity change against 1e-4 (at most 10 iterations).
+int luma_ibm_apply(luma_gpu_grid *g, const StepArgs &a) {
+    IbmState &st = *g->ibm;
+    if (!st.ready) return luma_set_error(LUMA_E_STATE, "luma_gpu_ibm_initialise was not called");
+    int rc;
+    const size_t ubytes = g->n * g->d.dims * (g->d.precision == LUMA_PREC_FP64 ? 8 : 4);
+    if (st.has_flexible && cudaMemcpyAsync(st.u_n, g->u, ubytes, cudaMemcpyDeviceToDevice, g->stream) != cudaSuccess)
+        return luma_set_error(LUMA_E_CUDA, "u_n copy failed");
+    if ((rc = ibm_pass(g, a))) return rc;
+    if (!st.has_flexible) return LUMA_OK;
+    if ((rc = luma_fem_move_bodies(g))) return rc;
+    double res = 0.0;
+    int it = 0;
+    do {
+        if (cudaMemcpyAsync(g->u, st.u_n, ubytes, cudaMemcpyDeviceToDevice, g->stream) != cudaSuccess)
+            return luma_set_error(LUMA_E_CUDA, "u reset failed");
+        if ((rc = luma_ibm_reset_forces(g, a))) return rc;
+        if ((rc = ibm_pass(g, a))) return rc;
+        if ((rc = luma_fem_move_bodies(g))) return rc;
+        if ((rc = luma_fem_residual(g, &res))) return rc;
+        it++;
+    } while (res > 1e-4 && it < 10);
+    st.fsi_iterations = it;
+    st.fsi_residual = res;
+    return luma_fem_commit(g);
+}
+
 void luma_ibm_free(luma_gpu_grid *g) {
+    if (g->ibm && g->ibm->has_flexible) luma_fem_free(g);
     if (g->ibm) free_device(g->ibm->dev);
     delete g->ibm;
     g->ibm = nullptr;
@@ -341,8 +382,37 @@ int luma_gpu_ibm_get_markers(luma_gpu_grid *g, int body, double *out) {
     int base = 0;
     for (int b = 0; b < body; ++b) base += st.bodies[b].nm;
     const IbmBody &bd = st.bodies[body];
+    int flex_index = -1, flex_base = 0, rigid_base = 0;
+    for (size_t k = 0; k < st.flex_body.size(); ++k)
+        if (st.flex_body[k] == body) flex_index = (int)k;
+    for (int b = 0; b < body; ++b) {
+        bool fl = false;
+        for (int fbi : st.flex_body) fl |= (fbi == b);
+        if (!fl) rigid_base += st.bodies[b].nm;
+    }
+    for (int k = 0; k < flex_index; ++k) flex_base += st.flex[k].nm;
+    (void)base;
     std::vector<double> F(3 * (size_t)bd.nm, 0.0);
-    if (st.ready && cudaMemcpy(F.data(), st.dev.F + 3 * (size_t)base, F.size() * sizeof(double),
+    if (flex_index >= 0 && st.ready) {
+        const FlexArgs &x = st.fem.flex;
+        std::vector<double> pos(3 * (size_t)bd.nm), eps(bd.nm), ds(bd.nm);
+        std::vector<int> ns(bd.nm);
+        cudaStreamSynchronize(g->stream);
+        if (cudaMemcpy(F.data(), x.F + 3 * (size_t)flex_base, F.size() * 8, cudaMemcpyDeviceToHost) ||
+            cudaMemcpy(pos.data(), x.pos + 3 * (size_t)flex_base, pos.size() * 8, cudaMemcpyDeviceToHost) ||
+            cudaMemcpy(eps.data(), x.eps + flex_base, eps.size() * 8, cudaMemcpyDeviceToHost) ||
+            cudaMemcpy(ds.data(), x.ds + flex_base, ds.size() * 8, cudaMemcpyDeviceToHost) ||
+            cudaMemcpy(ns.data(), x.nsupp + flex_base, ns.size() * 4, cudaMemcpyDeviceToHost))
+            return luma_set_error(LUMA_E_CUDA, "filament marker download failed");
+        for (int m = 0; m < bd.nm; ++m) {
+            double *o = out + 9 * (size_t)m;
+            o[0] = pos[3 * m]; o[1] = pos[3 * m + 1]; o[2] = pos[3 * m + 2];
+            o[3] = F[3 * m]; o[4] = F[3 * m + 1]; o[5] = g->d.dims == 3 ? F[3 * m + 2] : 0.0;
+            o[6] = eps[m]; o[7] = ds[m]; o[8] = ns[m];
+        }
+        return LUMA_OK;
+    }
+    if (st.ready && cudaMemcpy(F.data(), st.dev.F + 3 * (size_t)rigid_base, F.size() * sizeof(double),
                                cudaMemcpyDeviceToHost) != cudaSuccess)
         return luma_set_error(LUMA_E_CUDA, "marker force download failed");
     for (int m = 0; m < bd.nm; ++m) {

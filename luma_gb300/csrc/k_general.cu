@@ -646,14 +646,77 @@ __global__ void k_reset_forces(StepArgs a, int dims, double gravity, int gdir, d
     }
 }
 
-}  // namespace
+// ---- flexible (moving) markers: fixed-capacity supports, atomic spread ----
 
 template <int Q, class P>
-cudaError_t launch_ibm_pass(const StepArgs &a, const IbmArgs &b, cudaStream_t s) {
-    if (b.nm <= 0) return cudaSuccess;
-    k_ibm_interp_force<Q, P><<<(b.nm + 127) / 128, 128, 0, s>>>(a, b);
-    k_ibm_spread<Q, P><<<(b.nu + 127) / 128, 128, 0, s>>>(a, b);
-    k_ibm_remacro<Q, P><<<(b.nu + 127) / 128, 128, 0, s>>>(a, b);
+__global__ void k_flex_interp_force(StepArgs a, FlexArgs f) {
+    constexpr int D = Lattice<Q>::D;
+    const int m = blockIdx.x * blockDim.x + threadIdx.x;
+    if (m >= f.nm) return;
+    const size_t n = (size_t)a.ncell;
+    double r = 0.0, mom[3] = {0.0, 0.0, 0.0};
+    for (int s = 0; s < f.nsupp[m]; ++s) {
+        const int id = f.supp[m * kFlexMaxSupp + s];
+        const double rs = double(ldr<P>(a.rho, id));
+        const double dl = f.delta[m * kFlexMaxSupp + s];
+        r += rs * dl * 1.0;
+        for (int d = 0; d < D; ++d) mom[d] += rs * double(ldr<P>(a.u, (size_t)d * n + id)) * dl * 1.0;
+    }
+    f.irho[m] = r;
+    for (int d = 0; d < D; ++d) {
+        f.imom[3 * m + d] = mom[d];
+        f.F[3 * m + d] = 2.0 * (mom[d] - r * f.vel[3 * m + d]) / 1.0;
+    }
+}
+
+// Spread of moving markers: supports change every FSI iteration, so the
+// contributions are added with atomics (summation order differs from the
+// reference's serial loop at the level of FP64 rounding).
+template <int Q, class P>
+__global__ void k_flex_spread(StepArgs a, FlexArgs f) {
+    constexpr int D = Lattice<Q>::D;
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    const int m = t / kFlexMaxSupp, s = t % kFlexMaxSupp;
+    if (m >= f.nm || s >= f.nsupp[m]) return;
+    const size_t n = (size_t)a.ncell;
+    const int id = f.supp[m * kFlexMaxSupp + s];
+    const double volDepth = D == 3 ? f.ds[m] : 1.0;
+    for (int d = 0; d < D; ++d) {
+        const double c = f.delta[m * kFlexMaxSupp + s] * f.F[3 * m + d] * f.eps[m] * volDepth * f.ds[m];
+        atomicAdd(static_cast<typename P::R *>(const_cast<void *>(a.force)) + (size_t)d * n + id,
+                  typename P::R(-c));
+    }
+}
+
+template <int Q, class P>
+__global__ void k_flex_remacro(StepArgs a, FlexArgs f) {
+    using R = typename P::R;
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    const int m = t / kFlexMaxSupp, s = t % kFlexMaxSupp;
+    if (m >= f.nm || s >= f.nsupp[m]) return;
+    const size_t n = (size_t)a.ncell;
+    const int id = f.supp[m * kFlexMaxSupp + s];
+    const int k = id % a.K, j = (id / a.K) % a.M, i = id / (a.K * a.M);
+    R fn[Q];
+#pragma unroll
+    for (int v = 0; v < Q; ++v) fn[v] = ld<P>(a.fNew, (size_t)v * n + id);
+    R rho, drho, ux, uy, uz;
+    macro_site<Q, P>(a, i, j, k, id, a.typ[id], fn, rho, drho, ux, uy, uz);
+}
+
+}  // namespace
+
+// The four passes of ibm_apply, each over every body of the grid: rigid
+// bodies (ordered gather) and flexible markers (fixed slots, atomics).
+template <int Q, class P>
+cudaError_t launch_ibm_pass(const StepArgs &a, const IbmArgs &b, const FlexArgs &f, cudaStream_t s) {
+    const int nt = f.nm * kFlexMaxSupp;
+    if (b.nm > 0) k_ibm_interp_force<Q, P><<<(b.nm + 127) / 128, 128, 0, s>>>(a, b);
+    if (f.nm > 0) k_flex_interp_force<Q, P><<<(f.nm + 127) / 128, 128, 0, s>>>(a, f);
+    if (b.nm > 0) k_ibm_spread<Q, P><<<(b.nu + 127) / 128, 128, 0, s>>>(a, b);
+    if (f.nm > 0) k_flex_spread<Q, P><<<(nt + 127) / 128, 128, 0, s>>>(a, f);
+    if (b.nm > 0) k_ibm_remacro<Q, P><<<(b.nu + 127) / 128, 128, 0, s>>>(a, b);
+    if (f.nm > 0) k_flex_remacro<Q, P><<<(nt + 127) / 128, 128, 0, s>>>(a, f);
     return cudaGetLastError();
 }
 template <class P>
@@ -707,7 +770,8 @@ LUMA_INST(27, P64)
 LUMA_INST(9, P32)
 LUMA_INST(19, P32)
 LUMA_INST(27, P32)
-#define LUMA_INST_IBM(Q, P) template cudaError_t launch_ibm_pass<Q, P>(const StepArgs &, const IbmArgs &, cudaStream_t);
+#define LUMA_INST_IBM(Q, P) \
+    template cudaError_t launch_ibm_pass<Q, P>(const StepArgs &, const IbmArgs &, const FlexArgs &, cudaStream_t);
 LUMA_INST_IBM(9, P64)
 LUMA_INST_IBM(19, P64)
 LUMA_INST_IBM(27, P64)

@@ -19,10 +19,12 @@ template <int Q, class P>
 cudaError_t launch_general_phaseC(const StepArgs &a, cudaStream_t s);
 int read_unsupported_flag(cudaStream_t s);
 struct IbmArgs;
+struct FlexArgs;
 template <int Q, class P>
-cudaError_t launch_ibm_pass(const StepArgs &a, const IbmArgs &b, cudaStream_t s);
+cudaError_t launch_ibm_pass(const StepArgs &a, const IbmArgs &b, const FlexArgs &f, cudaStream_t s);
 template <class P>
 cudaError_t launch_reset_forces(const StepArgs &a, int dims, double gravity, int gdir, double rr, cudaStream_t s);
+
 
 // k_bulk.cu
 template <int Q, class P>

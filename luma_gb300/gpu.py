@@ -54,6 +54,9 @@ def lib() -> C.CDLL:
         L.luma_gpu_ibm_initialise.argtypes = [vp]
         L.luma_gpu_ibm_get_markers.argtypes = [vp, C.c_int, dp]
         L.luma_gpu_ibm_body_force.argtypes = [vp, C.c_int, dp]
+        L.luma_gpu_ibm_add_filament.argtypes = [vp, dp, C.c_double, C.c_double, C.c_double, C.c_double, C.c_int,
+                                                C.c_int, C.c_double, C.c_double, C.c_double, C.c_double,
+                                                C.POINTER(C.c_int)]
         if L.luma_gpu_abi_version() != A.ABI_VERSION:
             raise RuntimeError("luma_gb300 library ABI version mismatch")
         _lib = L
@@ -152,3 +155,13 @@ class GpuGrid:
         out = np.zeros(3)
         check(self.L.luma_gpu_ibm_body_force(self.h, body, A.dptr(out)))
         return out
+
+    def ibm_add_filament(self, start, length, height, depth, angle_v, nel, clamped, density, E, dm,
+                         fsi_vel_scale) -> int:
+        import math
+        st = np.ascontiguousarray(start, dtype=np.float64)
+        idx = C.c_int()
+        check(self.L.luma_gpu_ibm_add_filament(self.h, A.dptr(st), length, height, depth, angle_v, nel,
+                                               int(clamped), density, E, dm, fsi_vel_scale, C.byref(idx)))
+        self._nm = getattr(self, "_nm", []) + [int(math.floor(length / self.desc.dh)) + 1]
+        return idx.value

@@ -157,3 +157,31 @@ def test_ibm_matches_oracle(name, prec):
     vd = mk[:, 7] if D == 3 else 1.0
     ref = (mk[:, 3:3 + D] * (mk[:, 6] * vd * mk[:, 7])[:, None]).sum(axis=0)
     assert np.allclose(tot[:D], ref, rtol=1e-12, atol=0)
+
+
+@pytest.mark.parametrize("name", sorted(n for n in CASES.CASES if CASES.CASES[n].get("filaments")))
+def test_filament_fsi_matches_oracle(name):
+    """Flexible filament with the FEM and the FSI sub-iterations on the
+    device, FP64, against the oracle (bit-exact with the reference): flow
+    field rel L2 <= 1e-10, marker positions within 1e-12, marker forces rel
+    L2 <= 1e-8 after the stored steps."""
+    spec = CASES.CASES[name]
+    fx = R.fixture(name)
+    gg, levels = R.build_backend(name, make_gpu, A.PREC_FP64)
+    oo, _ = R.build_backend(name, make_oracle)
+    oibm = O.OracleIBM()
+    R.attach_filaments(name, gg, levels, lambda g, **k: g.ibm_add_filament(**k))
+    R.attach_filaments(name, oo, levels, lambda g, **k: oibm.add_filament(g, **k))
+    gg[0].ibm_initialise()
+    oibm.initialise()
+    done = 0
+    for s in spec["steps"]:
+        gg[0].step(s - done)
+        oo[0].step(s - done)
+        done = s
+        gs, os_ = gg[0].download(), oo[0].download()
+        gm, om = gg[0].ibm_markers(0), oibm.markers(0)
+        assert rel_l2(gs["u"], os_["u"]) <= 1e-10, (s, rel_l2(gs["u"], os_["u"]))
+        assert np.max(np.abs(gm[:, 0:2] - om[:, 0:2])) <= 1e-12
+        assert rel_l2(gm[:, 3:5], om[:, 3:5]) <= 1e-8, (s, rel_l2(gm[:, 3:5], om[:, 3:5]))
+        assert rel_l2(gs["u"], fx[f"u_{s}"]) <= 1e-10
