@@ -162,6 +162,20 @@ int luma_gpu_synchronize(luma_gpu_grid *root);
 /* ---- reductions / watchdog ----------------------------------------------- */
 int luma_gpu_reduce(luma_gpu_grid *grid, luma_reduction *out);
 
+/* No counterpart in the reference.  The FP64 reduction of luma_gpu_reduce
+ * for callers that cannot allocate device memory — code running inside a
+ * CUDA-graph stream capture, hosts that give the GPU's memory to a fixed
+ * pool at start-up, real-time loops — over SoA device arrays they own:
+ * typ[n] site labels (uint8, LUMA_SITE_*), rho[n], u[d*n + id] (FP64).
+ * It allocates nothing: its scratch is a fixed 64 KiB device array held by
+ * every GPU that loads the library.  At most 16,777,216 sites (larger n is
+ * rejected with LUMA_E_INVALID).  The first call on a device sets up that
+ * device's scratch address, so make it before any stream capture.  Calls
+ * share the scratch: calls whose kernels overlap on the GPU race.
+ * Blocks until the result is on the host. */
+int luma_gpu_reduce_fields_noalloc(const uint8_t *typ, const double *rho, const double *u, int64_t n,
+                                   int dims, void *cuda_stream, luma_reduction *out);
+
 /* ---- immersed-boundary bodies (grids created with LUMA_FLAG_IBM) -------- */
 /* Adds a rigid body of `nmarkers` Lagrangian markers to the grid that owns
  * it: positions[3*m + d] in the reference's length units, optional marker
