@@ -209,6 +209,26 @@ int luma_gpu_ibm_get_markers(luma_gpu_grid *grid, int body, double *out);
  * (src/ObjectManager_ops_io.cpp:65-128) before its physical scaling. */
 int luma_gpu_ibm_body_force(luma_gpu_grid *grid, int body, double force[3]);
 
+/* ---- discrete adjoint of the time-averaged drag ------------------------- */
+/* No counterpart in the reference (its objective is the drag that
+ * io_writeLiftDrag writes, src/ObjectManager_ops_io.cpp:105-121).
+ * Forward: runs `nsteps` ordinary steps from the current state, saving the
+ * population state every `checkpoint_every` steps, and returns
+ * J = (1/nsteps) sum over the steps of sum over the body's markers of
+ * F_x * epsilon * ds (* ds in 3D), lattice units.  Single grid, BGK, rigid
+ * bodies; site types fluid, solid, velocity, extrapolate-right; no
+ * regularised BCs, gravity or ramp (LUMA_E_INVALID otherwise). */
+int luma_gpu_adj_forward(luma_gpu_grid *grid, int nsteps, int checkpoint_every, int body, double *J);
+/* Backward: once per forward.  Recomputes each checkpoint segment, runs the
+ * reverse steps and returns dJ * dJ/ds for the scale s of the velocity of
+ * every velocity site (u = s * u_uploaded, at s = 1) and dJ * dJ/dX for the
+ * body's marker positions (dims doubles per marker, reference length
+ * units; through the supports' delta values, epsilon and ds).  Either
+ * output may be NULL.  The grid is left in the state after the forward. */
+int luma_gpu_adj_backward(luma_gpu_grid *grid, double dJ, double *grad_inlet_scale, double *grad_markers);
+/* Device bytes held by the checkpoints and the tape of the last forward. */
+int luma_gpu_adj_memory(const luma_gpu_grid *grid, size_t *bytes);
+
 #ifdef __cplusplus
 }
 #endif

@@ -252,6 +252,10 @@ int step_grid(luma_gpu_grid *g, int subcycle, bool write_macro) {
             int rc = luma_ibm_apply(g, a);
             if (rc) return rc;
         }
+        if (g->adj) {
+            int rc = luma_adj_step_hook(g, a);
+            if (rc) return rc;
+        }
         CK(dispatch(d.Q, d.precision, [&](auto q, auto p) {
             return launch_general_phaseC<decltype(q)::value, decltype(p)>(a, s);
         }));
@@ -265,6 +269,7 @@ void free_grid(luma_gpu_grid *g) {
     if (!g) return;
     for (luma_gpu_grid *c : g->kids) free_grid(c);
     luma_ibm_free(g);
+    luma_adj_free(g);
     cudaFree(g->typ);
     cudaFree(g->f[0]);
     cudaFree(g->f[1]);

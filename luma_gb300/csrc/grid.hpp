@@ -12,6 +12,7 @@
 
 namespace luma {
 struct IbmState;
+struct AdjState;
 }
 
 struct luma_gpu_grid;
@@ -39,6 +40,7 @@ struct luma_gpu_grid {
     std::vector<luma_gpu_grid *> kids;
     cudaStream_t stream = nullptr;
     luma::IbmState *ibm = nullptr;
+    luma::AdjState *adj = nullptr;   // discrete-adjoint tape (adjoint.cu)
     std::vector<double> hx, hy, hz;  // site positions (host copy, for IB support search)
 };
 
@@ -48,6 +50,9 @@ int luma_set_error(int code, const char *fmt, ...);
 int luma_ibm_reset_forces(luma_gpu_grid *g, const luma::StepArgs &a);
 int luma_ibm_apply(luma_gpu_grid *g, const luma::StepArgs &a);
 void luma_ibm_free(luma_gpu_grid *g);
+// adjoint.cu
+int luma_adj_step_hook(luma_gpu_grid *g, const luma::StepArgs &a);
+void luma_adj_free(luma_gpu_grid *g);
 // fem.cu
 int luma_fem_upload(luma_gpu_grid *g);
 int luma_fem_supports(luma_gpu_grid *g);

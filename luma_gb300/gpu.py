@@ -57,6 +57,9 @@ def lib() -> C.CDLL:
         L.luma_gpu_ibm_add_filament.argtypes = [vp, dp, C.c_double, C.c_double, C.c_double, C.c_double, C.c_int,
                                                 C.c_int, C.c_double, C.c_double, C.c_double, C.c_double,
                                                 C.POINTER(C.c_int)]
+        L.luma_gpu_adj_forward.argtypes = [vp, C.c_int, C.c_int, C.c_int, dp]
+        L.luma_gpu_adj_backward.argtypes = [vp, C.c_double, dp, dp]
+        L.luma_gpu_adj_memory.argtypes = [vp, C.POINTER(C.c_size_t)]
         if L.luma_gpu_abi_version() != A.ABI_VERSION:
             raise RuntimeError("luma_gb300 library ABI version mismatch")
         _lib = L
@@ -165,3 +168,25 @@ class GpuGrid:
                                                int(clamped), density, E, dm, fsi_vel_scale, C.byref(idx)))
         self._nm = getattr(self, "_nm", []) + [int(math.floor(length / self.desc.dh)) + 1]
         return idx.value
+
+    # ---- discrete adjoint of the time-averaged drag ----
+    def adj_forward(self, nsteps: int, checkpoint_every: int, body: int = 0) -> float:
+        """Runs nsteps steps, checkpointing every checkpoint_every, and returns
+        the time-averaged drag J of `body` (lattice units)."""
+        J = C.c_double()
+        check(self.L.luma_gpu_adj_forward(self.h, nsteps, checkpoint_every, body, C.byref(J)))
+        self._adj_body = body
+        return J.value
+
+    def adj_backward(self, dJ: float = 1.0):
+        """Returns (dJ/ds of the inlet velocity scale, dJ/dX as (markers, dims))."""
+        gs = C.c_double()
+        body = getattr(self, "_adj_body", 0)
+        gx = np.zeros((self._nm[body], self.desc.dims))
+        check(self.L.luma_gpu_adj_backward(self.h, dJ, C.byref(gs), A.dptr(gx)))
+        return gs.value, gx
+
+    def adj_memory(self) -> int:
+        b = C.c_size_t()
+        check(self.L.luma_gpu_adj_memory(self.h, C.byref(b)))
+        return b.value
