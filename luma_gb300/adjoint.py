@@ -45,25 +45,29 @@ def cylinder_markers(cx: float, cy: float, radius_lu: float, dh: float, n: int, 
 
 
 def cylinder_channel(nx: int = 400, ny: int = 160, diameter_lu: float = 20.0, n_markers: int = 64,
-                     sigma_lu: float = 0.1, u_max: float = 0.05, re: float = 100.0, nsteps: int = 4000,
-                     checkpoint_every: int = 100, seed: int = SEED) -> DragCase:
-    """D2Q9 BGK channel nx x ny: parabolic velocity inlet of centre-line
-    speed u_max (lattice units), extrapolate-right outlet, bounce-back walls
-    top and bottom, fluid at rest initially; a rigid cylinder centred ny/2
-    lattice units from the inlet on the channel's centre line.  The length
-    unit is half the channel height (resolution ny/2); `re` is L_RE over
-    that unit."""
+                     sigma_lu: float = 0.1, timestep: float = 1.0 / 2400.0, re: float = 100.0,
+                     nsteps: int = 4000, checkpoint_every: int = 100, seed: int = SEED) -> DragCase:
+    """D2Q9 BGK channel nx x ny: parabolic velocity inlet, extrapolate-right
+    outlet, bounce-back walls top and bottom, fluid at rest initially; a
+    rigid cylinder centred ny/2 lattice units from the inlet on the channel's
+    centre line.  The length unit is half the channel height (resolution
+    ny/2) and L_UX0 = 1, so the inlet's centre-line speed is
+    u_max = 1.5 * timestep * resolution lattice units (0.05 by default);
+    `re` is L_RE over that unit."""
     resolution = ny // 2                      # channel height = 2 length units
     bx, by = nx / resolution, ny / resolution
-    ux0 = 1.0
-    dt = u_max / (1.5 * ux0) / resolution     # parabolic centre-line speed 1.5 ux0 dt / dh = u_max
     V, X, S = A.VELOCITY, A.EXTRAPOLATE_RIGHT, A.SOLID
-    defs = hostcase.Definitions(dims=2, resolution=resolution, timestep=dt, bx=bx, by=by, re=re, ux0=ux0,
+    defs = hostcase.Definitions(dims=2, resolution=resolution, timestep=timestep, bx=bx, by=by, re=re, ux0=1.0,
                                 parabolic_inlet=True, ibm=True, walls=(V, X, S, S, A.FLUID, A.FLUID))
     dh = 1.0 / resolution
     cx, cy = by / 2.0, by / 2.0
     mk = cylinder_markers(cx, cy, diameter_lu / 2.0, dh, n_markers, sigma_lu, seed)
     return DragCase(defs, mk, nsteps, checkpoint_every)
+
+
+def inlet_u_max(c: DragCase) -> float:
+    """Centre-line speed of the parabolic inlet profile (lattice units)."""
+    return 1.5 * c.defs.ux0 * c.defs.timestep * c.defs.resolution
 
 
 def initial_state(defs: hostcase.Definitions, inlet_scale: float = 1.0):

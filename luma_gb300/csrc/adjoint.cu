@@ -11,9 +11,10 @@
 // population state saved every K steps and J accumulated in FP64.
 // Backward (luma_gpu_adj_backward): for each K-step segment, last first,
 // restore its checkpoint, re-run the segment once while taping the
-// post-stream populations, the force field and the marker forces of each
-// step (one segment of K states resident), then apply the reverse of each
-// step, newest first.  One step of the forward is
+// post-stream populations and the marker forces of each step (one segment
+// of K states resident; the force field is rebuilt from the marker forces),
+// then apply the reverse of each step, newest first.  Full segments run as
+// CUDA graphs captured once.  One step of the forward is
 //   stream   g = S f          periodic pull, half-way bounce-back,
 //                             extrapolate-right, forced-equilibrium inlet
 //                             feq(rho_v, s u_v)
@@ -58,13 +59,18 @@ struct AdjState {
     void *fin_f[2] = {nullptr, nullptr};
     void *fin_u = nullptr, *fin_rho = nullptr;
     int fin_cur = 0, fin_t = 0;
-    void *tape_g = nullptr, *tape_force = nullptr;
+    void *tape_g = nullptr;
     double *tape_Fm = nullptr;
     int tape_pos = 0;
+    int *site_u = nullptr;  // per site: index of the distinct support site, or -1
     void *lam[2] = {nullptr, nullptr};
     void *lamg = nullptr, *lamF = nullptr;
     double *mu = nullptr, *Gw = nullptr, *Gd = nullptr, *w = nullptr;
     size_t bytes = 0;
+    // full K-step segments run as CUDA graphs captured once (K even)
+    cudaStream_t own = nullptr;
+    cudaGraphExec_t seg_fwd = nullptr, seg_bwd = nullptr;
+    bool graphs = true;
 };
 
 }  // namespace luma
@@ -76,8 +82,8 @@ struct AdjArgs {
     int quirk;                 // 3D: F_z/2 enters u_x
     double omega, rho0, invT;
     const uint8_t *typ;
+    const int *site_u;         // per site: distinct support index or -1
     const void *g;             // taped post-stream populations (S)
-    const void *force;         // taped force field (R)
     const double *Fm;          // taped marker forces (3 per marker)
     const void *lam_in;        // adjoint of the post-collision f (R)
     void *lam_out;             // adjoint of the pre-stream f (R)
@@ -116,9 +122,19 @@ __global__ void __launch_bounds__(128) k_adj_collide(AdjArgs a) {
         for (int d = 0; d < D; ++d) j[d] += R(L::c(v, d)) * gv;
     }
     if (P::shifted) rho += R(a.rho0);
-    const R *Ff = static_cast<const R *>(a.force);
+    // the force field of the step: zero after the reset, the spread marker
+    // forces at support sites
     R F[3] = {R(0), R(0), R(0)};
-    for (int d = 0; d < D; ++d) F[d] = Ff[(size_t)d * n + id];
+    const int su = a.site_u[id];
+    if (su >= 0) {
+        double fs[3] = {0.0, 0.0, 0.0};
+        for (int q = a.uoff[su]; q < a.uoff[su + 1]; ++q) {
+            const int s = a.uref[q];
+            const int m = a.smarker[s];
+            for (int d = 0; d < D; ++d) fs[d] -= a.mdelta[s] * a.Fm[3 * m + d] * a.w[m];
+        }
+        for (int d = 0; d < D; ++d) F[d] = R(fs[d]);
+    }
     R u[3] = {R(0), R(0), R(0)};
     u[0] = (j[0] + R(0.5) * F[0] + (a.quirk ? R(0.5) * F[2] : R(0))) / rho;
     u[1] = (j[1] + R(0.5) * F[1]) / rho;
@@ -183,15 +199,13 @@ __device__ __forceinline__ void support_moments(const AdjArgs &a, int id, double
     }
 }
 
-// Reverse of the marker force and the spread, one thread per marker:
+// Reverse of the marker force and the spread for marker m:
 // mu_m = dJ/dF_m, and the sensitivities to the spreading weight w_m and to
 // each support's delta value.
 template <int Q, class P>
-__global__ void k_adj_marker(AdjArgs a) {
+__device__ __forceinline__ void adj_marker(const AdjArgs &a, int m) {
     using R = typename P::R;
     constexpr int D = Lattice<Q>::D;
-    const int m = blockIdx.x * blockDim.x + threadIdx.x;
-    if (m >= a.nm) return;
     const size_t n = (size_t)a.ncell;
     const R *lF = static_cast<const R *>(a.lamF);
     const bool inbody = m >= a.body_base && m < a.body_base + a.body_nm;
@@ -224,15 +238,13 @@ __global__ void k_adj_marker(AdjArgs a) {
     }
 }
 
-// Adjoint of the interpolated density and momentum, gathered per distinct
-// support site in the forward's order and added to lam_g through
+// Adjoint of the interpolated density and momentum at distinct support
+// site u, gathered in the forward's order and added to lam_g through
 // rho = sum_v g_v and j = sum_v c_v g_v.
 template <int Q, class P>
-__global__ void k_adj_support(AdjArgs a) {
+__device__ __forceinline__ void adj_support(const AdjArgs &a, int u) {
     using R = typename P::R;
     constexpr int D = Lattice<Q>::D;
-    const int u = blockIdx.x * blockDim.x + threadIdx.x;
-    if (u >= a.nu) return;
     const size_t n = (size_t)a.ncell;
     const int id = a.usite[u];
     if (a.typ[id] != LUMA_SITE_FLUID) return;  // moments of other sites are constants
@@ -253,6 +265,31 @@ __global__ void k_adj_support(AdjArgs a) {
         for (int d = 0; d < D; ++d) c += Lattice<Q>::c(v, d) * lj[d];
         lg[(size_t)v * n + id] += R(c);
     }
+}
+
+template <int Q, class P>
+__global__ void k_adj_marker(AdjArgs a) {
+    const int m = blockIdx.x * blockDim.x + threadIdx.x;
+    if (m < a.nm) adj_marker<Q, P>(a, m);
+}
+
+template <int Q, class P>
+__global__ void k_adj_support(AdjArgs a) {
+    const int u = blockIdx.x * blockDim.x + threadIdx.x;
+    if (u < a.nu) adj_support<Q, P>(a, u);
+}
+
+// Both IBM reverse passes in one block, for bodies small enough that one
+// block covers them: the block barrier orders the mu writes before the
+// support gathers read them.
+constexpr int kIbmBlock = 512;
+constexpr int kIbmBlockMaxMarkers = 4 * kIbmBlock;
+
+template <int Q, class P>
+__global__ void __launch_bounds__(kIbmBlock) k_adj_ibm_block(AdjArgs a) {
+    for (int m = threadIdx.x; m < a.nm; m += blockDim.x) adj_marker<Q, P>(a, m);
+    __syncthreads();
+    for (int u = threadIdx.x; u < a.nu; u += blockDim.x) adj_support<Q, P>(a, u);
 }
 
 __device__ __forceinline__ bool pulls(int t) {
@@ -360,7 +397,10 @@ void free_state(AdjState *st) {
     if (!st) return;
     for (void *p : st->ckpt) cudaFree(p);
     cudaFree(st->fin_f[0]); cudaFree(st->fin_f[1]); cudaFree(st->fin_u); cudaFree(st->fin_rho);
-    cudaFree(st->tape_g); cudaFree(st->tape_force); cudaFree(st->tape_Fm);
+    cudaFree(st->tape_g); cudaFree(st->tape_Fm); cudaFree(st->site_u);
+    if (st->seg_fwd) cudaGraphExecDestroy(st->seg_fwd);
+    if (st->seg_bwd) cudaGraphExecDestroy(st->seg_bwd);
+    if (st->own) cudaStreamDestroy(st->own);
     cudaFree(st->lam[0]); cudaFree(st->lam[1]); cudaFree(st->lamg); cudaFree(st->lamF); cudaFree(st->mu);
     cudaFree(st->Gw); cudaFree(st->Gd); cudaFree(st->w); cudaFree(st->d_J); cudaFree(st->d_gs);
     delete st;
@@ -398,9 +438,9 @@ AdjArgs make_adj_args(luma_gpu_grid *g, AdjState &st, int slot, int lin) {
     a.quirk = g->d.dims == 3 && !(g->d.flags & LUMA_FLAG_FIX_MACRO3D);
     a.omega = g->d.omega; a.rho0 = g->d.rho_in; a.invT = 1.0 / st.T;
     a.typ = g->typ;
+    a.site_u = st.site_u;
     const size_t rs = rsize(g);
     a.g = static_cast<char *>(st.tape_g) + (size_t)slot * g->n * g->d.Q * rs;
-    a.force = static_cast<char *>(st.tape_force) + (size_t)slot * g->n * g->d.dims * rs;
     a.Fm = st.tape_Fm + (size_t)slot * 3 * dv.nm;
     a.lam_in = st.lam[lin];
     a.lam_out = st.lam[lin ^ 1];
@@ -417,7 +457,9 @@ AdjArgs make_adj_args(luma_gpu_grid *g, AdjState &st, int slot, int lin) {
 template <int Q, class P>
 cudaError_t launch_adj_step(const AdjArgs &a, cudaStream_t s) {
     k_adj_collide<Q, P><<<(a.ncell + 127) / 128, 128, 0, s>>>(a);
-    if (a.nm > 0) {
+    if (a.nm > 0 && a.nm <= kIbmBlockMaxMarkers) {
+        k_adj_ibm_block<Q, P><<<1, kIbmBlock, 0, s>>>(a);
+    } else if (a.nm > 0) {
         k_adj_marker<Q, P><<<(a.nm + 63) / 64, 64, 0, s>>>(a);
         k_adj_support<Q, P><<<(a.nu + 127) / 128, 128, 0, s>>>(a);
     }
@@ -575,11 +617,8 @@ int luma_adj_step_hook(luma_gpu_grid *g, const StepArgs &a) {
     if (st.mode == 1) {
         k_drag<<<1, 256, 0, s>>>(dv.F, st.w, st.body_base, st.body_nm, 1.0 / st.T, st.d_J);
     } else if (st.mode == 2) {
-        const size_t rs = rsize(g);
-        const size_t gb = g->n * g->d.Q * rs, fb = g->n * g->d.dims * rs;
-        if (cudaMemcpyAsync(static_cast<char *>(st.tape_g) + st.tape_pos * gb, a.fNew, gb, cudaMemcpyDeviceToDevice, s) ||
-            cudaMemcpyAsync(static_cast<char *>(st.tape_force) + st.tape_pos * fb, a.force, fb, cudaMemcpyDeviceToDevice, s) ||
-            cudaMemcpyAsync(st.tape_Fm + (size_t)st.tape_pos * 3 * dv.nm, dv.F, 3 * dv.nm * sizeof(double),
+        // the populations are on the tape already (luma_adj_redirect)
+        if (cudaMemcpyAsync(st.tape_Fm + (size_t)st.tape_pos * 3 * dv.nm, dv.F, 3 * dv.nm * sizeof(double),
                             cudaMemcpyDeviceToDevice, s))
             return luma_set_error(LUMA_E_CUDA, "adjoint: tape copy failed");
         st.tape_pos++;
@@ -589,10 +628,87 @@ int luma_adj_step_hook(luma_gpu_grid *g, const StepArgs &a) {
     return LUMA_OK;
 }
 
+// While taping, the step streams into the tape slot of the step and its
+// collision writes the next state to the usual buffer, so the post-stream
+// populations stay on the tape without a copy.
+void luma_adj_redirect(luma_gpu_grid *g, StepArgs &a) {
+    const AdjState &st = *g->adj;
+    if (st.mode != 2) return;
+    a.fNew = static_cast<char *>(st.tape_g) + (size_t)st.tape_pos * g->n * g->d.Q * rsize(g);
+}
+
 void luma_adj_free(luma_gpu_grid *g) {
     free_state(g->adj);
     g->adj = nullptr;
 }
+
+namespace {
+
+// The adjoint's work runs on its own stream (capturable, unlike the legacy
+// default stream); the caller's stream is drained first and put back after.
+struct OwnStream {
+    luma_gpu_grid *g;
+    cudaStream_t saved;
+    OwnStream(luma_gpu_grid *g_, AdjState &st) : g(g_), saved(g_->stream) {
+        cudaStreamSynchronize(saved);
+        g->stream = st.own;
+    }
+    ~OwnStream() { g->stream = saved; }
+};
+
+// Enqueues fn()'s work as a CUDA graph: captured and instantiated on first
+// use, replayed after.  fn's host-side effects happen at capture only;
+// `replay_effects` repeats the ones that matter on each later replay.  On a
+// capture failure the work runs uncaptured and graphs are switched off.
+template <class F, class H>
+int run_graph(luma_gpu_grid *g, AdjState &st, cudaGraphExec_t *exec, F &&fn, H &&replay_effects) {
+    cudaStream_t s = g->stream;
+    if (!st.graphs) return fn();
+    if (*exec) {
+        if (cudaGraphLaunch(*exec, s) != cudaSuccess) return luma_set_error(LUMA_E_CUDA, "adjoint: graph launch failed");
+        replay_effects();
+        return LUMA_OK;
+    }
+    const int t0 = g->t, cur0 = g->cur;
+    if (cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+        cudaGetLastError();
+        st.graphs = false;
+        return fn();
+    }
+    const int rc = fn();
+    cudaGraph_t graph = nullptr;
+    const cudaError_t e = cudaStreamEndCapture(s, &graph);
+    cudaError_t ei = cudaErrorUnknown;
+    if (rc == LUMA_OK && e == cudaSuccess && graph) ei = cudaGraphInstantiate(exec, graph, 0);
+    if (graph) cudaGraphDestroy(graph);
+    if (ei != cudaSuccess) {
+        cudaGetLastError();
+        *exec = nullptr;
+        st.graphs = false;
+        g->t = t0;
+        g->cur = cur0;
+        return fn();
+    }
+    if (cudaGraphLaunch(*exec, s) != cudaSuccess) return luma_set_error(LUMA_E_CUDA, "adjoint: graph launch failed");
+    return LUMA_OK;
+}
+
+// Per-site index of the distinct support site (or -1), for the force-field
+// reconstruction in the reverse collide.
+int build_site_map(luma_gpu_grid *g, AdjState &st) {
+    const IbmDevice &dv = g->ibm->dev;
+    std::vector<int> usite(dv.nu), map(g->n, -1);
+    if (dv.nu && cudaMemcpy(usite.data(), dv.usite, dv.nu * sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess)
+        return luma_set_error(LUMA_E_CUDA, "adjoint: support sites");
+    for (int u = 0; u < dv.nu; ++u) map[usite[u]] = u;
+    int rc = dmalloc(&st.site_u, g->n * sizeof(int), st);
+    if (rc) return rc;
+    if (cudaMemcpy(st.site_u, map.data(), g->n * sizeof(int), cudaMemcpyHostToDevice) != cudaSuccess)
+        return luma_set_error(LUMA_E_CUDA, "adjoint: site map upload");
+    return LUMA_OK;
+}
+
+}  // namespace
 
 extern "C" {
 
@@ -604,6 +720,9 @@ int luma_gpu_adj_forward(luma_gpu_grid *g, int nsteps, int checkpoint_every, int
     luma_adj_free(g);
     AdjState *st = new AdjState();
     g->adj = st;
+    auto fail = [&](int code) { luma_adj_free(g); return code; };
+    if (cudaStreamCreateWithFlags(&st->own, cudaStreamNonBlocking) != cudaSuccess)
+        return fail(luma_set_error(LUMA_E_CUDA, "adjoint: stream creation failed"));
     st->body = body;
     st->T = nsteps;
     st->K = std::min(checkpoint_every, nsteps);
@@ -624,13 +743,11 @@ int luma_gpu_adj_forward(luma_gpu_grid *g, int nsteps, int checkpoint_every, int
     }
     const size_t rs = rsize(g);
     const size_t fbytes = g->n * g->d.Q * rs;
-    auto fail = [&](int code) { luma_adj_free(g); return code; };
     if ((rc = dmalloc(&st->w, w.size() * 8, *st)) || (rc = dmalloc(&st->d_J, 8, *st)) ||
-        (rc = dmalloc(&st->d_gs, 8, *st)))
+        (rc = dmalloc(&st->d_gs, 8, *st)) || (rc = build_site_map(g, *st)))
         return fail(rc);
-    cudaStream_t s = g->stream;
-    cudaMemcpyAsync(st->w, w.data(), w.size() * 8, cudaMemcpyHostToDevice, s);
-    cudaMemsetAsync(st->d_J, 0, 8, s);
+    if (cudaMemcpy(st->w, w.data(), w.size() * 8, cudaMemcpyHostToDevice) != cudaSuccess)
+        return fail(luma_set_error(LUMA_E_CUDA, "adjoint: weights upload"));
     st->ckpt.assign(st->nseg, nullptr);
     for (int k = 0; k < st->nseg; ++k)
         if ((rc = dmalloc(&st->ckpt[k], fbytes, *st))) return fail(rc);
@@ -638,25 +755,39 @@ int luma_gpu_adj_forward(luma_gpu_grid *g, int nsteps, int checkpoint_every, int
     if ((rc = dmalloc(&st->fin_f[0], fbytes, *st)) || (rc = dmalloc(&st->fin_f[1], fbytes, *st)) ||
         (rc = dmalloc(&st->fin_u, ub, *st)) || (rc = dmalloc(&st->fin_rho, rb, *st)))
         return fail(rc);
-    st->t0 = g->t;
-    st->mode = 1;
-    for (int k = 0; k < st->nseg; ++k) {
-        if (cudaMemcpyAsync(st->ckpt[k], g->f[g->cur], fbytes, cudaMemcpyDeviceToDevice, s) != cudaSuccess)
-            return fail(luma_set_error(LUMA_E_CUDA, "adjoint: checkpoint copy failed"));
-        if ((rc = luma_gpu_step(g, std::min(st->K, st->T - k * st->K)))) return fail(rc);
-    }
-    st->mode = 0;
-    // the state after the forward, put back after the backward sweep
-    cudaMemcpyAsync(st->fin_f[0], g->f[0], fbytes, cudaMemcpyDeviceToDevice, s);
-    cudaMemcpyAsync(st->fin_f[1], g->f[1], fbytes, cudaMemcpyDeviceToDevice, s);
-    cudaMemcpyAsync(st->fin_u, g->u, ub, cudaMemcpyDeviceToDevice, s);
-    cudaMemcpyAsync(st->fin_rho, g->rho, rb, cudaMemcpyDeviceToDevice, s);
-    st->fin_cur = g->cur;
-    st->fin_t = g->t;
+    st->graphs = (st->K % 2) == 0;  // a graph replays a fixed buffer parity
     double h = 0.0;
-    cudaMemcpyAsync(&h, st->d_J, 8, cudaMemcpyDeviceToHost, s);
-    cudaError_t e = cudaStreamSynchronize(s);
-    if (e != cudaSuccess) return fail(luma_set_error(LUMA_E_CUDA, "adjoint forward: %s", cudaGetErrorString(e)));
+    {
+        OwnStream guard(g, *st);
+        cudaStream_t s = g->stream;
+        cudaMemsetAsync(st->d_J, 0, 8, s);
+        st->t0 = g->t;
+        st->mode = 1;
+        for (int k = 0; k < st->nseg; ++k) {
+            if (cudaMemcpyAsync(st->ckpt[k], g->f[g->cur], fbytes, cudaMemcpyDeviceToDevice, s) != cudaSuccess)
+                return fail(luma_set_error(LUMA_E_CUDA, "adjoint: checkpoint copy failed"));
+            const int steps = std::min(st->K, st->T - k * st->K);
+            if (steps == st->K)
+                rc = run_graph(g, *st, &st->seg_fwd, [&] { return luma_gpu_step(g, steps); }, [&] { g->t += steps; });
+            else
+                rc = luma_gpu_step(g, steps);
+            if (rc) {
+                st->mode = 0;
+                return fail(rc);
+            }
+        }
+        st->mode = 0;
+        // the state after the forward, put back after the backward sweep
+        cudaMemcpyAsync(st->fin_f[0], g->f[0], fbytes, cudaMemcpyDeviceToDevice, s);
+        cudaMemcpyAsync(st->fin_f[1], g->f[1], fbytes, cudaMemcpyDeviceToDevice, s);
+        cudaMemcpyAsync(st->fin_u, g->u, ub, cudaMemcpyDeviceToDevice, s);
+        cudaMemcpyAsync(st->fin_rho, g->rho, rb, cudaMemcpyDeviceToDevice, s);
+        st->fin_cur = g->cur;
+        st->fin_t = g->t;
+        cudaMemcpyAsync(&h, st->d_J, 8, cudaMemcpyDeviceToHost, s);
+        cudaError_t e = cudaStreamSynchronize(s);
+        if (e != cudaSuccess) return fail(luma_set_error(LUMA_E_CUDA, "adjoint forward: %s", cudaGetErrorString(e)));
+    }
     *J = h;
     st->valid = true;
     return LUMA_OK;
@@ -670,52 +801,65 @@ int luma_gpu_adj_backward(luma_gpu_grid *g, double dJ, double *grad_inlet_scale,
     const int D = g->d.dims, Q = g->d.Q;
     const size_t rs = rsize(g);
     const size_t fbytes = g->n * Q * rs;
-    cudaStream_t s = g->stream;
     int rc;
     if (!st.tape_g) {
         if ((rc = dmalloc(&st.tape_g, (size_t)st.K * fbytes, st)) ||
-            (rc = dmalloc(&st.tape_force, (size_t)st.K * g->n * D * rs, st)) ||
             (rc = dmalloc(&st.tape_Fm, (size_t)st.K * 3 * dv.nm * 8, st)) || (rc = dmalloc(&st.lam[0], fbytes, st)) ||
             (rc = dmalloc(&st.lam[1], fbytes, st)) || (rc = dmalloc(&st.lamg, fbytes, st)) ||
             (rc = dmalloc(&st.lamF, g->n * D * rs, st)) || (rc = dmalloc(&st.mu, 3 * (size_t)dv.nm * 8, st)) ||
             (rc = dmalloc(&st.Gw, (size_t)dv.nm * 8, st)) || (rc = dmalloc(&st.Gd, (size_t)dv.nsup * 8, st)))
             return rc;
     }
-    cudaMemsetAsync(st.lam[0], 0, fbytes, s);
-    cudaMemsetAsync(st.Gw, 0, (size_t)dv.nm * 8, s);
-    cudaMemsetAsync(st.Gd, 0, (size_t)dv.nsup * 8, s);
-    cudaMemsetAsync(st.d_gs, 0, 8, s);
-    int lin = 0;
-    for (int k = st.nseg - 1; k >= 0; --k) {
-        const int steps = std::min(st.K, st.T - k * st.K);
-        cudaMemcpyAsync(g->f[g->cur], st.ckpt[k], fbytes, cudaMemcpyDeviceToDevice, s);
-        g->t = st.t0 + k * st.K;
-        st.mode = 2;
-        st.tape_pos = 0;
-        rc = luma_gpu_step(g, steps);
-        st.mode = 0;
-        if (rc) return rc;
-        for (int t = steps - 1; t >= 0; --t) {
-            const AdjArgs a = make_adj_args(g, st, t, lin);
-            cudaError_t e = dispatch(Q, g->d.precision, [&](auto q, auto p) {
-                return launch_adj_step<decltype(q)::value, decltype(p)>(a, s);
-            });
-            if (e != cudaSuccess) return luma_set_error(LUMA_E_CUDA, "adjoint step: %s", cudaGetErrorString(e));
-            lin ^= 1;
-        }
-    }
     std::vector<double> Gw(dv.nm), Gd(dv.nsup);
     double gs = 0.0;
-    cudaMemcpyAsync(Gw.data(), st.Gw, (size_t)dv.nm * 8, cudaMemcpyDeviceToHost, s);
-    cudaMemcpyAsync(Gd.data(), st.Gd, (size_t)dv.nsup * 8, cudaMemcpyDeviceToHost, s);
-    cudaMemcpyAsync(&gs, st.d_gs, 8, cudaMemcpyDeviceToHost, s);
-    // put back the state after the forward
-    cudaMemcpyAsync(g->f[0], st.fin_f[0], fbytes, cudaMemcpyDeviceToDevice, s);
-    cudaMemcpyAsync(g->f[1], st.fin_f[1], fbytes, cudaMemcpyDeviceToDevice, s);
-    cudaMemcpyAsync(g->u, st.fin_u, g->n * D * rs, cudaMemcpyDeviceToDevice, s);
-    cudaMemcpyAsync(g->rho, st.fin_rho, g->n * rs, cudaMemcpyDeviceToDevice, s);
-    cudaError_t e = cudaStreamSynchronize(s);
-    if (e != cudaSuccess) return luma_set_error(LUMA_E_CUDA, "adjoint backward: %s", cudaGetErrorString(e));
+    {
+        OwnStream guard(g, st);
+        cudaStream_t s = g->stream;
+        cudaMemsetAsync(st.lam[0], 0, fbytes, s);
+        cudaMemsetAsync(st.Gw, 0, (size_t)dv.nm * 8, s);
+        cudaMemsetAsync(st.Gd, 0, (size_t)dv.nsup * 8, s);
+        cudaMemsetAsync(st.d_gs, 0, 8, s);
+        int lin = 0;
+        // one segment: recompute with the tape on, then the reverse steps
+        auto segment = [&](int steps) -> int {
+            st.mode = 2;
+            st.tape_pos = 0;
+            int r = luma_gpu_step(g, steps);
+            st.mode = 0;
+            if (r) return r;
+            int l = lin;
+            for (int t = steps - 1; t >= 0; --t) {
+                const AdjArgs a = make_adj_args(g, st, t, l);
+                cudaError_t e = dispatch(Q, g->d.precision, [&](auto q, auto p) {
+                    return launch_adj_step<decltype(q)::value, decltype(p)>(a, s);
+                });
+                if (e != cudaSuccess) return luma_set_error(LUMA_E_CUDA, "adjoint step: %s", cudaGetErrorString(e));
+                l ^= 1;
+            }
+            return LUMA_OK;
+        };
+        for (int k = st.nseg - 1; k >= 0; --k) {
+            const int steps = std::min(st.K, st.T - k * st.K);
+            cudaMemcpyAsync(g->f[g->cur], st.ckpt[k], fbytes, cudaMemcpyDeviceToDevice, s);
+            g->t = st.t0 + k * st.K;
+            if (steps == st.K)
+                rc = run_graph(g, st, &st.seg_bwd, [&] { return segment(steps); }, [&] { g->t += steps; });
+            else
+                rc = segment(steps);
+            if (rc) return rc;
+            lin ^= steps & 1;
+        }
+        cudaMemcpyAsync(Gw.data(), st.Gw, (size_t)dv.nm * 8, cudaMemcpyDeviceToHost, s);
+        cudaMemcpyAsync(Gd.data(), st.Gd, (size_t)dv.nsup * 8, cudaMemcpyDeviceToHost, s);
+        cudaMemcpyAsync(&gs, st.d_gs, 8, cudaMemcpyDeviceToHost, s);
+        // put back the state after the forward
+        cudaMemcpyAsync(g->f[0], st.fin_f[0], fbytes, cudaMemcpyDeviceToDevice, s);
+        cudaMemcpyAsync(g->f[1], st.fin_f[1], fbytes, cudaMemcpyDeviceToDevice, s);
+        cudaMemcpyAsync(g->u, st.fin_u, g->n * D * rs, cudaMemcpyDeviceToDevice, s);
+        cudaMemcpyAsync(g->rho, st.fin_rho, g->n * rs, cudaMemcpyDeviceToDevice, s);
+        cudaError_t e = cudaStreamSynchronize(s);
+        if (e != cudaSuccess) return luma_set_error(LUMA_E_CUDA, "adjoint backward: %s", cudaGetErrorString(e));
+    }
     g->cur = st.fin_cur;
     g->t = st.fin_t;
     st.valid = false;

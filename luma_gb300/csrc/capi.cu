@@ -175,6 +175,7 @@ StepArgs make_args(luma_gpu_grid *g, int subcycle) {
     a.typ = g->typ;
     a.f = g->f[g->cur];
     a.fNew = g->f[g->cur ^ 1];
+    a.fOut = a.fNew;
     a.u = g->u; a.rho = g->rho; a.force = g->force;
     a.ux_in = g->uxin; a.uy_in = g->uyin; a.uz_in = g->uzin;
     a.omega = d.omega; a.rho0 = d.rho_in; a.cs2 = g->cs2; a.csmag = d.csmag;
@@ -232,6 +233,7 @@ int step_grid(luma_gpu_grid *g, int subcycle, bool write_macro) {
         return LUMA_OK;
     }
     StepArgs a = make_args(g, subcycle);
+    if (g->adj) luma_adj_redirect(g, a);
     if (g->ibm && g->ibm->has_bodies) {
         int rc = luma_ibm_reset_forces(g, a);
         if (rc) return rc;

@@ -53,6 +53,7 @@ struct StepArgs {
     const uint8_t *typ;
     const void *f;          // populations before the step (S*)
     void *fNew;             // populations after the step (S*)
+    void *fOut;             // where the split collision writes: fNew, or another buffer when fNew is kept
     void *u, *rho;          // R*, SoA
     const void *force;      // R*, SoA force_xyz (null when no forcing)
     const double *ux_in, *uy_in, *uz_in;

@@ -52,6 +52,7 @@ int luma_ibm_apply(luma_gpu_grid *g, const luma::StepArgs &a);
 void luma_ibm_free(luma_gpu_grid *g);
 // adjoint.cu
 int luma_adj_step_hook(luma_gpu_grid *g, const luma::StepArgs &a);
+void luma_adj_redirect(luma_gpu_grid *g, luma::StepArgs &a);
 void luma_adj_free(luma_gpu_grid *g);
 // fem.cu
 int luma_fem_upload(luma_gpu_grid *g);

@@ -561,7 +561,7 @@ __global__ void __launch_bounds__(128) k_force_collide(StepArgs a) {
     if (type == LUMA_SITE_SOLID) b.forcing = 0;  // solid sites are collided without the Guo term
     collide_site<Q, P>(b, id, fn, rho, rho - R(a.rho0), ux, uy, uz);
 #pragma unroll
-    for (int v = 0; v < Q; ++v) st<P>(a.fNew, (size_t)v * n + id, fn[v]);
+    for (int v = 0; v < Q; ++v) st<P>(a.fOut, (size_t)v * n + id, fn[v]);
 }
 
 // ---- immersed boundary pass (ObjectManager::ibm_apply, src/ObjectManager_ops_ibm.cpp:33-54) ----

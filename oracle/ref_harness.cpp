@@ -12,7 +12,10 @@
  *
  * Usage:
  *   luma_ref --out DIR --steps N [--dump-every K] [--init-u FILE] [--init-rho FILE]
- *            [--workdir DIR]
+ *            [--workdir DIR] [--markers FILE] [--drag-out FILE]
+ *
+ * With --drag-out nothing is dumped; FILE gets the time average over the N
+ * steps of body 0's lattice-unit drag and N.
  *
  * Output, per dump step s and grid (level l, region r):
  *   DIR/s<s>/L<l>R<r>_meta.txt   key value lines (sizes, omega, dt, dh, t, limits)
@@ -113,6 +116,25 @@ static void dump_markers(const std::string &dir) {
 #endif
 }
 
+/* Lattice-unit drag of body 0 as io_writeLiftDrag sums it per marker
+ * (src/ObjectManager_ops_io.cpp:105-121, before its physical scaling). */
+static double body_drag() {
+#ifdef L_IBM_ON
+    ObjectManager *om = ObjectManager::getInstance();
+    if (om->iBody.empty()) return 0.0;
+    IBBody &body = om->iBody[0];
+    double s = 0.0;
+    for (size_t m = 0; m < body.markers.size(); ++m) {
+        IBMarker &mk = body.markers[m];
+        const double volDepth = L_DIMS == 3 ? mk.ds : 1.0;
+        s += mk.force_xyz[0] * mk.epsilon * volDepth * mk.ds;
+    }
+    return s;
+#else
+    return 0.0;
+#endif
+}
+
 static void dump_all(GridObj *root, const std::string &out, int step) {
     std::string dir = out + "/s" + std::to_string(step);
     mkdir(dir.c_str(), 0755);
@@ -165,7 +187,7 @@ static void reinit_equilibrium(GridObj *g) {
 }
 
 int main(int argc, char **argv) {
-    std::string out = ".", init_u, init_rho, workdir, markers;
+    std::string out = ".", init_u, init_rho, workdir, markers, drag_out;
     int steps = 0, dump_every = 0;
     for (int a = 1; a < argc; ++a) {
         std::string k = argv[a];
@@ -180,6 +202,7 @@ int main(int argc, char **argv) {
         else if (k == "--init-rho") init_rho = next();
         else if (k == "--workdir") workdir = next();
         else if (k == "--markers") markers = next();
+        else if (k == "--drag-out") drag_out = next();
         else { std::fprintf(stderr, "unknown argument %s\n", k.c_str()); return 2; }
     }
     mkdir(out.c_str(), 0755);
@@ -226,11 +249,18 @@ int main(int argc, char **argv) {
 #endif
     (void)om;
 
-    dump_all(grids, out, 0);
+    if (drag_out.empty()) dump_all(grids, out, 0);
+    double drag_sum = 0.0;
     auto t0 = std::chrono::steady_clock::now();
     for (int s = 1; s <= steps; ++s) {
         grids->LBM_multi_opt();
-        if ((dump_every > 0 && s % dump_every == 0) || s == steps) dump_all(grids, out, s);
+        if (!drag_out.empty()) drag_sum += body_drag();
+        else if ((dump_every > 0 && s % dump_every == 0) || s == steps) dump_all(grids, out, s);
+    }
+    if (!drag_out.empty()) {
+        FILE *df = std::fopen(drag_out.c_str(), "w");
+        std::fprintf(df, "%.17g %d\n", steps > 0 ? drag_sum / steps : 0.0, steps);
+        std::fclose(df);
     }
     auto t1 = std::chrono::steady_clock::now();
     double sec = std::chrono::duration<double>(t1 - t0).count();
