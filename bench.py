@@ -191,6 +191,61 @@ def run_reference(args, rank: int, world: int):
     return 0
 
 
+def measure_adjoint() -> dict:
+    """Cost and memory of the drag gradient on the adjoint workload (D2Q9
+    400x160 channel, IB cylinder of 64 markers, 4000 steps, checkpoints every
+    100), FP32-shifted as the workload runs and FP64; wall clock around the
+    C-ABI calls (each blocks until its result is on the host)."""
+    from luma_gb300 import _abi as A
+    from luma_gb300 import adjoint as ADJ
+
+    c = ADJ.cylinder_channel()
+    umax = ADJ.inlet_u_max(c)
+    out = {"workload": "D2Q9 BGK channel 400x160, parabolic inlet u_max=0.05 lu, IB cylinder D=20 lu with 64 "
+                       "markers on radii 10+N(0,0.1^2) lu (seeded), 4000 steps, checkpoints every 100; "
+                       "J = time-averaged drag; gradient w.r.t. u_max and 128 marker coordinates",
+           "cost_definition": "(adjoint forward + backward) / plain forward (luma_gpu_step over the same steps)"}
+    grads = {}
+    for prec, name in ((A.PREC_FP32_SHIFTED, "fp32_shifted"), (A.PREC_FP64, "fp64")):
+        warm = ADJ.DragCase(c.defs, c.markers, 200, 100)
+        ADJ.drag_and_gradient(warm, prec)
+        g, _ = ADJ.make_grid(c, prec)
+        g.step(10)
+        g.synchronize()
+        t = time.perf_counter()
+        g.step(c.nsteps)
+        g.synchronize()
+        plain = time.perf_counter() - t
+        g.close()
+        g, _ = ADJ.make_grid(c, prec)
+        t = time.perf_counter()
+        J = g.adj_forward(c.nsteps, c.checkpoint_every, 0)
+        fwd = time.perf_counter() - t
+        t = time.perf_counter()
+        gs, gx = g.adj_backward(1.0)
+        bwd = time.perf_counter() - t
+        mem = g.adj_memory()
+        g.close()
+        grads[name] = (gs, gx)
+        out[name] = {"J": J, "dJ_du_max": gs / umax, "forward_s": round(fwd, 4), "backward_s": round(bwd, 4),
+                     "plain_forward_s": round(plain, 4), "cost_vs_forward": round((fwd + bwd) / plain, 3),
+                     "backward_vs_adjoint_forward": round(bwd / fwd, 3), "device_bytes": int(mem)}
+    g32, g64 = grads["fp32_shifted"], grads["fp64"]
+    out["fp32_vs_fp64"] = {"dJ_ds_rel": abs(g32[0] - g64[0]) / abs(g64[0]),
+                           "dJ_dX_rel_max": float(np.max(np.abs(g32[1] - g64[1])) / np.max(np.abs(g64[1])))}
+    fdp = os.path.join(ROOT, "tests", "golden", "adjoint_fd_cyl400.json")
+    if os.path.exists(fdp):
+        ref = json.load(open(fdp))
+        fd = np.array([r["fd"] for r in ref["markers"]])
+        chk = {"source": "central differences of the reference's own FP64 build (h=1e-4)"}
+        for name, (gs, gx) in grads.items():
+            ad = np.array([gx[r["marker"], r["dim"]] for r in ref["markers"]])
+            chk[name] = {"inlet_rel": abs(gs - ref["fd_inlet"]) / abs(ref["fd_inlet"]),
+                         "markers_rel_max": float(np.max(np.abs(ad - fd)) / np.max(np.abs(fd)))}
+        out["fd_check"] = chk
+    return out
+
+
 def run_ours(args, rank: int, world: int, local_rank: int):
     import torch
     from luma_gb300 import _abi as A
@@ -302,6 +357,8 @@ def run_ours(args, rank: int, world: int, local_rank: int):
     traffic = read_profile_traffic("k_aa_d3q19_fp32_256") if n == SIZE else None
     bytes64 = 2 * 19 * 8 * ncell
 
+    adjoint = measure_adjoint() if rank == 0 and not args.no_adjoint else None
+
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         mlc, used, dtc, nst = cpu_oracle_mlups(SIZE, 16, args.cpu_steps, 1, None, min_seconds=10.0)
@@ -336,6 +393,7 @@ def run_ours(args, rank: int, world: int, local_rank: int):
             "fp32_vs_fp64": {"speedup": round(mlups32 / mlups64, 3), "rel_l2_u": eu, "rel_l2_rho": er,
                              "after_steps": W + K, "fp64_mass": red64["mass"]},
             "cpu_baseline": cpu,
+            "adjoint": adjoint,
         }
         print(json.dumps(line), flush=True)
     if dist:
@@ -352,6 +410,7 @@ def main(argv=None) -> int:
     ap.add_argument("--size", type=int, default=SIZE)
     ap.add_argument("--cpu-steps", type=int, default=20)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint workload measurement")
     args = ap.parse_args(argv)
     if args.warmup < 3:
         args.warmup = 3

@@ -195,6 +195,30 @@ def _precedence(cur: int, want: int) -> int:
     return want
 
 
+def _precedence_array(cur: np.ndarray, want: int) -> np.ndarray:
+    """_precedence over an array of current labels."""
+    out = np.full(cur.shape, want, dtype=cur.dtype)
+    out[cur == A.VELOCITY] = A.VELOCITY
+    out[cur == A.SOLID] = A.SOLID
+    if want == A.SOLID:
+        out[...] = A.SOLID
+    return out
+
+
+def _initial_velocity(defs: Definitions, typ: np.ndarray, prof: np.ndarray) -> np.ndarray:
+    """LBM_initVelocity (src/GridObj_init_grids.cpp:37-152): the inlet
+    profile of each row (velocity sites only under L_NO_FLOW), zero at solid
+    sites.  typ has shape (N, M, K), prof (M, D)."""
+    N, M, K = typ.shape
+    D = prof.shape[1]
+    u = np.zeros((N, M, K, D))
+    use = np.ones(typ.shape, dtype=bool) if not defs.no_flow else (typ == A.VELOCITY)
+    prof_b = np.broadcast_to(prof[None, :, None, :], (N, M, K, D))
+    u[use] = prof_b[use]
+    u[typ == A.SOLID] = 0.0
+    return u
+
+
 def build_level0(defs: Definitions) -> Level0:
     N, M, K = defs.sizes()
     dh = 1.0 / float(defs.resolution)
@@ -209,11 +233,7 @@ def build_level0(defs: Definitions) -> Level0:
     left, right, bottom, top, front, back = defs.walls
 
     def label(sel, want):
-        sub = typ[sel]
-        flat = sub.reshape(-1)
-        for n_ in range(flat.size):
-            flat[n_] = _precedence(int(flat[n_]), want)
-        typ[sel] = flat.reshape(sub.shape)
+        typ[sel] = _precedence_array(typ[sel], want)
 
     for i in range(N):
         if xpos[i] <= wt[0]:
@@ -251,19 +271,9 @@ def build_level0(defs: Definitions) -> Level0:
 
     # Initial velocity and density.
     D = defs.dims
-    u = np.zeros((N, M, K, D))
     rc = ramp_coefficient(defs, 0.0)
     prof = np.stack([ux_in * rc, uy_in * rc, uz_in * rc], axis=1)[:, :D]
-    for i in range(N):
-        for j in range(M):
-            for k in range(K):
-                t_ = typ[i, j, k]
-                if defs.no_flow and t_ != A.VELOCITY:
-                    u[i, j, k] = 0.0
-                else:
-                    u[i, j, k] = prof[j]
-                if t_ == A.SOLID:
-                    u[i, j, k] = 0.0
+    u = _initial_velocity(defs, typ, prof)
     rho = np.full((N, M, K), float(defs.rho_in))
 
     nu_d = defs.nu if defs.nu is not None else 1.0 / float(defs.re)
@@ -340,50 +350,30 @@ def build_subgrid(parent: "Level0", start: tuple, end: tuple, region: int = 0,
     # Parent relabelling.
     Np, Mp, Kp = parent.N, parent.M, parent.K
     ptyp = parent.typ.reshape(Np, Mp, Kp)
-    for i in range(Np):
-        xi = parent.xpos[i]
-        if not (xi > edges[0] and xi < edges[1]):
-            continue
-        for j in range(Mp):
-            yj = parent.ypos[j]
-            if not (yj > edges[2] and yj < edges[3]):
-                continue
-            for k in range(Kp):
-                zk = parent.zpos[k]
-                if D == 3 and not (zk > edges[4] and zk < edges[5]):
-                    continue
-                tl = ((xi > edges[0] and xi < edges[0] + dh_p) or (xi < edges[1] and xi > edges[1] - dh_p) or
-                      (yj > edges[2] and yj < edges[2] + dh_p) or (yj < edges[3] and yj > edges[3] - dh_p))
-                if D == 3:
-                    tl = tl or (zk > edges[4] and zk < edges[4] + dh_p) or (zk < edges[5] and zk > edges[5] - dh_p)
-                if tl:
-                    if ptyp[i, j, k] == A.FLUID:
-                        ptyp[i, j, k] = A.TL_TO_FINER
-                elif ptyp[i, j, k] == A.FLUID:
-                    ptyp[i, j, k] = A.REFINED
+    xp, yp, zp = np.asarray(parent.xpos), np.asarray(parent.ypos), np.asarray(parent.zpos)
+    inx = (xp > edges[0]) & (xp < edges[1])
+    iny = (yp > edges[2]) & (yp < edges[3])
+    inz = ((zp > edges[4]) & (zp < edges[5])) if D == 3 else np.ones(Kp, dtype=bool)
+    tlx = ((xp > edges[0]) & (xp < edges[0] + dh_p)) | ((xp < edges[1]) & (xp > edges[1] - dh_p))
+    tly = ((yp > edges[2]) & (yp < edges[2] + dh_p)) | ((yp < edges[3]) & (yp > edges[3] - dh_p))
+    tlz = (((zp > edges[4]) & (zp < edges[4] + dh_p)) | ((zp < edges[5]) & (zp > edges[5] - dh_p))) if D == 3 \
+        else np.zeros(Kp, dtype=bool)
+    inside = inx[:, None, None] & iny[None, :, None] & inz[None, None, :]
+    tl = tlx[:, None, None] | tly[None, :, None] | tlz[None, None, :]
+    fluid = ptyp == A.FLUID
+    ptyp[inside & tl & fluid] = A.TL_TO_FINER
+    ptyp[inside & ~tl & fluid] = A.REFINED
     parent.typ = ptyp.reshape(-1)
     # Child labels.
-    typ = np.empty((N, M, K), dtype=np.int32)
-    for i in range(N):
-        pi = (i - (i % 2)) // 2 + lims[0]
-        for j in range(M):
-            pj = (j - (j % 2)) // 2 + lims[2]
-            for k in range(K):
-                pk = ((k - (k % 2)) // 2 + lims[4]) if D == 3 else 0
-                pl = ptyp[pi, pj, pk]
-                typ[i, j, k] = A.TL_TO_COARSER if pl == A.TL_TO_FINER else (A.FLUID if pl == A.REFINED else pl)
+    pi = np.arange(N) // 2 + lims[0]
+    pj = np.arange(M) // 2 + lims[2]
+    pk = (np.arange(K) // 2 + lims[4]) if D == 3 else np.zeros(K, dtype=np.int64)
+    pl = ptyp[pi[:, None, None], pj[None, :, None], pk[None, None, :]]
+    typ = np.where(pl == A.TL_TO_FINER, A.TL_TO_COARSER, np.where(pl == A.REFINED, A.FLUID, pl)).astype(np.int32)
     ux_in, uy_in, uz_in = _inlet_profile(defs, pos[1], dt, dh, parent_root_edges(parent))
-    u = np.zeros((N, M, K, D))
     rc = ramp_coefficient(defs, 0.0)
     prof = np.stack([ux_in * rc, uy_in * rc, uz_in * rc], axis=1)[:, :D]
-    for i in range(N):
-        for j in range(M):
-            for k in range(K):
-                t_ = typ[i, j, k]
-                if not (defs.no_flow and t_ != A.VELOCITY):
-                    u[i, j, k] = prof[j]
-                if t_ == A.SOLID:
-                    u[i, j, k] = 0.0
+    u = _initial_velocity(defs, typ, prof)
     rho = np.full((N, M, K), float(defs.rho_in))
     omega = 1.0 / (((1.0 / parent.omega - 0.5) * 2.0) + 0.5)
     level = parent.level + 1

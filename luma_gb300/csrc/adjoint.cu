@@ -809,6 +809,10 @@ int luma_gpu_adj_backward(luma_gpu_grid *g, double dJ, double *grad_inlet_scale,
             (rc = dmalloc(&st.lamF, g->n * D * rs, st)) || (rc = dmalloc(&st.mu, 3 * (size_t)dv.nm * 8, st)) ||
             (rc = dmalloc(&st.Gw, (size_t)dv.nm * 8, st)) || (rc = dmalloc(&st.Gd, (size_t)dv.nsup * 8, st)))
             return rc;
+        // the recompute's second loop also collides sites the stream skips
+        // (solid, velocity) from the tape: keep that memory defined
+        if (cudaMemset(st.tape_g, 0, (size_t)st.K * fbytes) != cudaSuccess)
+            return luma_set_error(LUMA_E_CUDA, "adjoint: tape clear");
     }
     std::vector<double> Gw(dv.nm), Gd(dv.nsup);
     double gs = 0.0;

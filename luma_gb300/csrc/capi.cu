@@ -8,6 +8,7 @@
 // the two-buffer general kernel; both give the reference's result.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
@@ -167,6 +168,101 @@ int build_site_tables(luma_gpu_grid *g, const int32_t *typ, const double *xpos, 
     return LUMA_OK;
 }
 
+}  // namespace
+
+// Sites of an IBM grid whose collision waits for the IBM pass: the distinct
+// support sites of rigid bodies, and the sites phase A does not stream
+// (solid, refined, velocity; the regularised boundary sites phase B
+// streams), which the reference's second loop collides as well.  Every
+// other site carries the zero force of the reset through the step, so
+// phase A collides it at once with the same arithmetic (the Guo term adds
+// exact zeros), saving a pass over the populations.  Not used under
+// gravity (non-zero force everywhere) or with flexible bodies (supports
+// move within the step).
+int luma_update_defer(luma_gpu_grid *g) {
+    cudaFree(g->defer);
+    cudaFree(g->defer_ids);
+    g->defer = nullptr;
+    g->defer_ids = nullptr;
+    g->ndefer = 0;
+    g->fuse = false;
+    const luma_grid_desc &d = g->d;
+    if (!(d.flags & LUMA_FLAG_IBM) || (d.flags & LUMA_FLAG_GRAVITY) || g->bulk) return LUMA_OK;
+    if (g->ibm && g->ibm->has_flexible) return LUMA_OK;
+    const bool reg = (d.flags & LUMA_FLAG_REGULARISED) != 0;
+    std::vector<uint8_t> mask(g->n, 0);
+    for (size_t id = 0; id < g->n; ++id) {
+        const int t = g->htyp[id];
+        if (t == LUMA_SITE_SOLID || t == LUMA_SITE_REFINED || t == LUMA_SITE_VELOCITY ||
+            (reg && t == LUMA_SITE_PRESSURE))
+            mask[id] = 1;
+    }
+    if (g->ibm && g->ibm->has_bodies && g->ibm->dev.nu > 0) {
+        std::vector<int> us(g->ibm->dev.nu);
+        CK(cudaMemcpy(us.data(), g->ibm->dev.usite, us.size() * sizeof(int), cudaMemcpyDeviceToHost));
+        for (int id : us) mask[id] = 1;
+    }
+    std::vector<int> ids;
+    for (size_t id = 0; id < g->n; ++id)
+        if (mask[id]) ids.push_back((int)id);
+    CK(cudaMalloc(&g->defer, g->n));
+    CK(cudaMemcpy(g->defer, mask.data(), g->n, cudaMemcpyHostToDevice));
+    CK(cudaMalloc(&g->defer_ids, std::max<size_t>(1, ids.size()) * sizeof(int)));
+    if (!ids.empty()) CK(cudaMemcpy(g->defer_ids, ids.data(), ids.size() * sizeof(int), cudaMemcpyHostToDevice));
+    g->ndefer = (int)ids.size();
+    g->fuse = true;
+    return LUMA_OK;
+}
+
+// Sites of a general-path grid split between the interior kernel (fluid
+// sites whose every pull source, wrapped periodically, is a fluid site) and
+// the full site logic (the rest, less the sites the stream skips).  Grids
+// below kInteriorMinSites keep the single full-logic launch: there the step
+// is bound by launch latency, not by the full kernel's register budget.
+constexpr size_t kInteriorMinSites = 1u << 20;
+
+int luma_build_interior(luma_gpu_grid *g) {
+    cudaFree(g->fast);
+    cudaFree(g->gen_ids);
+    g->fast = nullptr;
+    g->gen_ids = nullptr;
+    g->ngen = 0;
+    if (g->bulk || (g->n < kInteriorMinSites && !(g->d.flags & LUMA_FLAG_SPLIT_INTERIOR))) return LUMA_OK;
+    const luma_grid_desc &d = g->d;
+    const int N = d.N, M = d.M, K = d.K, Q = d.Q;
+    const bool reg = (d.flags & LUMA_FLAG_REGULARISED) != 0;
+    std::vector<int> cs(3 * Q);
+    for (int v = 0; v < Q; ++v) host_c(Q, v, &cs[3 * v]);
+    std::vector<uint8_t> fast(g->n, 0);
+    std::vector<int> gen;
+    const uint8_t *t = g->htyp.data();
+    for (int i = 0; i < N; ++i)
+        for (int j = 0; j < M; ++j)
+            for (int k = 0; k < K; ++k) {
+                const int id = k + j * K + i * K * M;
+                const int ty = t[id];
+                if (ty == LUMA_SITE_REFINED || ty == LUMA_SITE_SOLID || ty == LUMA_SITE_VELOCITY ||
+                    (reg && ty == LUMA_SITE_PRESSURE))
+                    continue;  // the stream skips these
+                bool plain = ty == LUMA_SITE_FLUID;
+                for (int v = 0; plain && v < Q; ++v) {
+                    const int x = (i - cs[3 * v] + N) % N, y = (j - cs[3 * v + 1] + M) % M;
+                    const int z = d.dims == 3 ? (k - cs[3 * v + 2] + K) % K : 0;
+                    plain = t[z + y * K + x * K * M] == LUMA_SITE_FLUID;
+                }
+                if (plain) fast[id] = 1;
+                else gen.push_back(id);
+            }
+    CK(cudaMalloc(&g->fast, g->n));
+    CK(cudaMemcpy(g->fast, fast.data(), g->n, cudaMemcpyHostToDevice));
+    CK(cudaMalloc(&g->gen_ids, std::max<size_t>(1, gen.size()) * sizeof(int)));
+    if (!gen.empty()) CK(cudaMemcpy(g->gen_ids, gen.data(), gen.size() * sizeof(int), cudaMemcpyHostToDevice));
+    g->ngen = (int)gen.size();
+    return LUMA_OK;
+}
+
+namespace {
+
 StepArgs make_args(luma_gpu_grid *g, int subcycle) {
     const luma_grid_desc &d = g->d;
     StepArgs a;
@@ -176,6 +272,7 @@ StepArgs make_args(luma_gpu_grid *g, int subcycle) {
     a.f = g->f[g->cur];
     a.fNew = g->f[g->cur ^ 1];
     a.fOut = a.fNew;
+    a.defer = g->fuse ? g->defer : nullptr;
     a.u = g->u; a.rho = g->rho; a.force = g->force;
     a.ux_in = g->uxin; a.uy_in = g->uyin; a.uz_in = g->uzin;
     a.omega = d.omega; a.rho0 = d.rho_in; a.cs2 = g->cs2; a.csmag = d.csmag;
@@ -239,7 +336,7 @@ int step_grid(luma_gpu_grid *g, int subcycle, bool write_macro) {
         if (rc) return rc;
     }
     CK(dispatch(d.Q, d.precision, [&](auto q, auto p) {
-        return launch_general_phaseA<decltype(q)::value, decltype(p)>(a, g->wall, s);
+        return launch_general_phaseA<decltype(q)::value, decltype(p)>(a, g->wall, g->fast, g->gen_ids, g->ngen, s);
     }));
     if (g->nreg)
         CK(dispatch(d.Q, d.precision, [&](auto q, auto p) {
@@ -259,7 +356,8 @@ int step_grid(luma_gpu_grid *g, int subcycle, bool write_macro) {
             if (rc) return rc;
         }
         CK(dispatch(d.Q, d.precision, [&](auto q, auto p) {
-            return launch_general_phaseC<decltype(q)::value, decltype(p)>(a, s);
+            return launch_general_phaseC<decltype(q)::value, decltype(p)>(a, g->fuse ? g->defer_ids : nullptr,
+                                                                          g->ndefer, s);
         }));
     }
     g->cur ^= 1;
@@ -285,6 +383,10 @@ void free_grid(luma_gpu_grid *g) {
     cudaFree(g->reg);
     cudaFree(g->velu);
     cudaFree(g->acc);
+    cudaFree(g->defer);
+    cudaFree(g->defer_ids);
+    cudaFree(g->fast);
+    cudaFree(g->gen_ids);
     delete g;
 }
 
@@ -394,6 +496,9 @@ int luma_gpu_grid_create(const luma_grid_desc *desc, luma_gpu_grid *parent, luma
     CKF(cudaMalloc(&g->acc, 8 * sizeof(double)));
     rc = build_site_tables(g, d.lattyp, d.xpos, d.ypos, d.zpos);
     if (rc) return fail(rc);
+    g->htyp.assign(d.lattyp, d.lattyp + g->n);
+    if ((rc = luma_update_defer(g))) return fail(rc);
+    if ((rc = luma_build_interior(g))) return fail(rc);
     if (d.xpos) g->hx.assign(d.xpos, d.xpos + d.N);
     if (d.ypos) g->hy.assign(d.ypos, d.ypos + d.M);
     if (d.zpos) g->hz.assign(d.zpos, d.zpos + d.K);
@@ -409,6 +514,10 @@ int luma_gpu_grid_create(const luma_grid_desc *desc, luma_gpu_grid *parent, luma
                 parent->kids.pop_back();
                 luma_set_error(LUMA_E_NOMEM, "second population buffer for parent");
                 return fail(LUMA_E_NOMEM);
+            }
+            if ((rc = luma_build_interior(parent))) {
+                parent->kids.pop_back();
+                return fail(rc);
             }
         }
     }

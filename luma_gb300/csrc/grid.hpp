@@ -36,6 +36,18 @@ struct luma_gpu_grid {
     bool bulk = false;          // in-place AA path
     bool bulk_fixed = false;    // state uploaded: path can no longer change
     int aa_odd = 0;             // AA storage state: 0 = E, 1 = O
+    // IBM grids: sites whose collision waits for the IBM pass (phase C);
+    // every other site is collided in phase A (fuse = true)
+    bool fuse = false;
+    uint8_t *defer = nullptr;   // per-site flag
+    int *defer_ids = nullptr;   // the flagged sites
+    int ndefer = 0;
+    std::vector<uint8_t> htyp;  // site labels (host copy)
+    // general path: interior fluid sites (plain pulls only) run a lean
+    // kernel; the listed others run the full site logic
+    uint8_t *fast = nullptr;
+    int *gen_ids = nullptr;
+    int ngen = 0;
     luma_gpu_grid *parent = nullptr;
     std::vector<luma_gpu_grid *> kids;
     cudaStream_t stream = nullptr;
@@ -46,6 +58,9 @@ struct luma_gpu_grid {
 
 int luma_set_error(int code, const char *fmt, ...);
 
+// capi.cu
+int luma_update_defer(luma_gpu_grid *g);
+int luma_build_interior(luma_gpu_grid *g);
 // ibm.cu
 int luma_ibm_reset_forces(luma_gpu_grid *g, const luma::StepArgs &a);
 int luma_ibm_apply(luma_gpu_grid *g, const luma::StepArgs &a);

@@ -274,6 +274,7 @@ int init_tree(luma_gpu_grid *g) {
             if ((rc = luma_fem_supports(g))) return rc;
         }
         st.ready = true;
+        if ((rc = luma_update_defer(g))) return rc;
     }
     for (luma_gpu_grid *c : g->kids) {
         int rc = init_tree(c);

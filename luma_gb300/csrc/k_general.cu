@@ -250,9 +250,10 @@ __device__ __forceinline__ typename P::R smag_omega(const StepArgs &a, const typ
 }
 
 // Collision of one site in place on fn (BGK / BGK-Smagorinsky / KBC), with
-// the Guo term when forcing.  `fpre` is the pre-stream f of the site, read by
-// the reference's KBC (:1147, :1296).
-template <int Q, class P>
+// the Guo term when forcing.  The reference's KBC reads the pre-stream f of
+// the site (:1147, :1296).  COLL fixes the operator at compile time (-1:
+// a.collision at run time).
+template <int Q, class P, int COLL = -1>
 __device__ __forceinline__ void collide_site(const StepArgs &a, int id, typename P::R *fn, typename P::R rho,
                                              typename P::R drho, typename P::R ux, typename P::R uy,
                                              typename P::R uz) {
@@ -267,8 +268,9 @@ __device__ __forceinline__ void collide_site(const StepArgs &a, int id, typename
         Fy = ldr<P>(a.force, n + id);
         if (D == 3) Fz = ldr<P>(a.force, 2 * n + id);
     }
-    if (a.collision != LUMA_COLL_KBC) {
-        const R om = a.collision == LUMA_COLL_BGK_SMAG ? smag_omega<Q, P>(a, fn, rho, drho, ux, uy, uz) : R(a.omega);
+    const int coll = COLL >= 0 ? COLL : a.collision;
+    if (coll != LUMA_COLL_KBC) {
+        const R om = coll == LUMA_COLL_BGK_SMAG ? smag_omega<Q, P>(a, fn, rho, drho, ux, uy, uz) : R(a.omega);
 #pragma unroll
         for (int v = 0; v < Q; ++v) {
             const R eq = feq_s<Q, P>(v, rho, drho, ux, uy, uz, cs2);
@@ -366,10 +368,8 @@ __device__ __forceinline__ void collide_site(const StepArgs &a, int id, typename
 }
 
 template <int Q, class P>
-__global__ void __launch_bounds__(128) k_stream_macro(StepArgs a, const int8_t *wall) {
+__device__ __forceinline__ void stream_macro_site(const StepArgs &a, const int8_t *wall, int id) {
     using R = typename P::R;
-    const int id = blockIdx.x * blockDim.x + threadIdx.x;
-    if (id >= a.ncell) return;
     const int type = a.typ[id];
     const bool reg = (a.flags & LUMA_FLAG_REGULARISED) != 0;
     if (type == LUMA_SITE_REFINED || type == LUMA_SITE_SOLID || type == LUMA_SITE_VELOCITY ||
@@ -383,9 +383,78 @@ __global__ void __launch_bounds__(128) k_stream_macro(StepArgs a, const int8_t *
     R rho, drho, ux, uy, uz;
     macro_site<Q, P>(a, i, j, k, id, type, fn, rho, drho, ux, uy, uz);
     const size_t n = (size_t)a.ncell;
+    if (a.ibm_split && a.defer && !a.defer[id] && type != LUMA_SITE_TL_TO_COARSER) {
+        // IBM grid, site outside every support: its force is the reset's zero,
+        // so its second-loop collision happens here (fOut != fNew keeps the
+        // streamed values in fNew as well)
+        if (a.fOut != a.fNew) {
+#pragma unroll
+            for (int v = 0; v < Q; ++v) st<P>(a.fNew, (size_t)v * n + id, fn[v]);
+        }
+        collide_site<Q, P>(a, id, fn, rho, drho, ux, uy, uz);
+#pragma unroll
+        for (int v = 0; v < Q; ++v) st<P>(a.fOut, (size_t)v * n + id, fn[v]);
+        return;
+    }
     if (!a.ibm_split && type != LUMA_SITE_TL_TO_COARSER) collide_site<Q, P>(a, id, fn, rho, drho, ux, uy, uz);
 #pragma unroll
     for (int v = 0; v < Q; ++v) st<P>(a.fNew, (size_t)v * n + id, fn[v]);
+}
+
+template <int Q, class P>
+__global__ void __launch_bounds__(128) k_stream_macro(StepArgs a, const int8_t *wall) {
+    const int id = blockIdx.x * blockDim.x + threadIdx.x;
+    if (id < a.ncell) stream_macro_site<Q, P>(a, wall, id);
+}
+
+// The same over the listed sites (those the interior kernel leaves).
+template <int Q, class P>
+__global__ void __launch_bounds__(128) k_stream_macro_list(StepArgs a, const int8_t *wall, const int *ids, int nids) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t < nids) stream_macro_site<Q, P>(a, wall, ids[t]);
+}
+
+// Interior fluid sites (every pull source a fluid site, so every direction
+// is a plain pull): stream, macroscopic and collision of the same operators
+// as stream_macro_site with the branches resolved at compile time, for a
+// lean register budget and all Q loads in flight at once.  Under the IBM
+// split, deferred sites stop after the macroscopic step (phase C collides
+// them); the others carry the reset's zero force, whose Guo term and half
+// force add exact zeros, so their force is not read.
+template <int Q, class P, int COLL>
+__global__ void __launch_bounds__(128) k_interior(StepArgs a, const uint8_t *fast) {
+    using L = Lattice<Q>;
+    using R = typename P::R;
+    constexpr int D = L::D;
+    const int id = blockIdx.x * blockDim.x + threadIdx.x;
+    if (id >= a.ncell || !fast[id]) return;
+    const int N = a.N, M = a.M, K = a.K;
+    const int k = id % K, j = (id / K) % M, i = id / (K * M);
+    const size_t n = (size_t)a.ncell;
+    R fn[Q];
+#pragma unroll
+    for (int v = 0; v < Q; ++v) {
+        int sx = i - L::c(v, 0), sy = j - L::c(v, 1), sz = k - L::c(v, 2);
+        sx = sx < 0 ? sx + N : (sx >= N ? sx - N : sx);
+        sy = sy < 0 ? sy + M : (sy >= M ? sy - M : sy);
+        if (D == 3) sz = sz < 0 ? sz + K : (sz >= K ? sz - K : sz);
+        else sz = 0;
+        fn[v] = ld<P>(a.f, (size_t)v * n + (sz + sy * K + sx * K * M));
+    }
+    const bool deferred = a.ibm_split && (!a.defer || a.defer[id]);
+    StepArgs b = a;
+    if (a.ibm_split && !deferred) b.forcing = 0;  // zero force: exact same sums
+    R rho, drho, ux, uy, uz;
+    macro_site<Q, P>(b, i, j, k, id, LUMA_SITE_FLUID, fn, rho, drho, ux, uy, uz);
+    if (deferred || (a.ibm_split && a.fOut != a.fNew)) {
+#pragma unroll
+        for (int v = 0; v < Q; ++v) st<P>(a.fNew, (size_t)v * n + id, fn[v]);
+        if (deferred) return;
+    }
+    collide_site<Q, P, COLL>(b, id, fn, rho, drho, ux, uy, uz);
+    void *out = a.ibm_split ? a.fOut : a.fNew;
+#pragma unroll
+    for (int v = 0; v < Q; ++v) st<P>(out, (size_t)v * n + id, fn[v]);
 }
 
 // _LBM_regularised_opt (:313-510) for one velocity/pressure site of a
@@ -543,11 +612,9 @@ __global__ void k_velocity_u(StepArgs a, int dims, const int2 *sites, int nsites
 // non-solid site and collision at every site but transition-to-coarser,
 // using the macroscopic values after the IBM pass.
 template <int Q, class P>
-__global__ void __launch_bounds__(128) k_force_collide(StepArgs a) {
+__device__ __forceinline__ void force_collide_site(const StepArgs &a, int id) {
     using R = typename P::R;
     constexpr int D = Lattice<Q>::D;
-    const int id = blockIdx.x * blockDim.x + threadIdx.x;
-    if (id >= a.ncell) return;
     const int type = a.typ[id];
     if (type == LUMA_SITE_TL_TO_COARSER) return;
     const size_t n = (size_t)a.ncell;
@@ -562,6 +629,19 @@ __global__ void __launch_bounds__(128) k_force_collide(StepArgs a) {
     collide_site<Q, P>(b, id, fn, rho, rho - R(a.rho0), ux, uy, uz);
 #pragma unroll
     for (int v = 0; v < Q; ++v) st<P>(a.fOut, (size_t)v * n + id, fn[v]);
+}
+
+template <int Q, class P>
+__global__ void __launch_bounds__(128) k_force_collide(StepArgs a) {
+    const int id = blockIdx.x * blockDim.x + threadIdx.x;
+    if (id < a.ncell) force_collide_site<Q, P>(a, id);
+}
+
+// The same over the listed sites only (the sites phase A left uncollided).
+template <int Q, class P>
+__global__ void __launch_bounds__(128) k_force_collide_list(StepArgs a, const int *ids, int nids) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t < nids) force_collide_site<Q, P>(a, ids[t]);
 }
 
 // ---- immersed boundary pass (ObjectManager::ibm_apply, src/ObjectManager_ops_ibm.cpp:33-54) ----
@@ -726,9 +806,18 @@ cudaError_t launch_reset_forces(const StepArgs &a, int dims, double gravity, int
 }
 
 template <int Q, class P>
-cudaError_t launch_general_phaseA(const StepArgs &a, const int8_t *wall, cudaStream_t s) {
+cudaError_t launch_general_phaseA(const StepArgs &a, const int8_t *wall, const uint8_t *fast, const int *gen_ids,
+                                  int ngen, cudaStream_t s) {
     const int bs = 128;
-    k_stream_macro<Q, P><<<(a.ncell + bs - 1) / bs, bs, 0, s>>>(a, wall);
+    if (!fast) {
+        k_stream_macro<Q, P><<<(a.ncell + bs - 1) / bs, bs, 0, s>>>(a, wall);
+        return cudaGetLastError();
+    }
+    const int nb = (a.ncell + bs - 1) / bs;
+    if (a.collision == LUMA_COLL_KBC) k_interior<Q, P, LUMA_COLL_KBC><<<nb, bs, 0, s>>>(a, fast);
+    else if (a.collision == LUMA_COLL_BGK_SMAG) k_interior<Q, P, LUMA_COLL_BGK_SMAG><<<nb, bs, 0, s>>>(a, fast);
+    else k_interior<Q, P, LUMA_COLL_BGK><<<nb, bs, 0, s>>>(a, fast);
+    if (ngen > 0) k_stream_macro_list<Q, P><<<(ngen + bs - 1) / bs, bs, 0, s>>>(a, wall, gen_ids, ngen);
     return cudaGetLastError();
 }
 template <int Q, class P>
@@ -746,9 +835,13 @@ cudaError_t launch_velocity_u(const StepArgs &a, int dims, const int2 *sites, in
     return cudaGetLastError();
 }
 template <int Q, class P>
-cudaError_t launch_general_phaseC(const StepArgs &a, cudaStream_t s) {
+cudaError_t launch_general_phaseC(const StepArgs &a, const int *ids, int nids, cudaStream_t s) {
     const int bs = 128;
-    k_force_collide<Q, P><<<(a.ncell + bs - 1) / bs, bs, 0, s>>>(a);
+    if (ids) {
+        if (nids > 0) k_force_collide_list<Q, P><<<(nids + bs - 1) / bs, bs, 0, s>>>(a, ids, nids);
+    } else {
+        k_force_collide<Q, P><<<(a.ncell + bs - 1) / bs, bs, 0, s>>>(a);
+    }
     return cudaGetLastError();
 }
 
@@ -760,10 +853,11 @@ int read_unsupported_flag(cudaStream_t s) {
 }
 
 #define LUMA_INST(Q, P)                                                                                        \
-    template cudaError_t launch_general_phaseA<Q, P>(const StepArgs &, const int8_t *, cudaStream_t);         \
+    template cudaError_t launch_general_phaseA<Q, P>(const StepArgs &, const int8_t *, const uint8_t *, const int *, \
+                                                     int, cudaStream_t);                                       \
     template cudaError_t launch_general_phaseB<Q, P>(const StepArgs &, const int8_t *, const RegSite *, int,   \
                                                      cudaStream_t);                                            \
-    template cudaError_t launch_general_phaseC<Q, P>(const StepArgs &, cudaStream_t);
+    template cudaError_t launch_general_phaseC<Q, P>(const StepArgs &, const int *, int, cudaStream_t);
 LUMA_INST(9, P64)
 LUMA_INST(19, P64)
 LUMA_INST(27, P64)

@@ -9,14 +9,15 @@ namespace luma {
 
 // k_general.cu
 template <int Q, class P>
-cudaError_t launch_general_phaseA(const StepArgs &a, const int8_t *wall, cudaStream_t s);
+cudaError_t launch_general_phaseA(const StepArgs &a, const int8_t *wall, const uint8_t *fast, const int *gen_ids,
+                                  int ngen, cudaStream_t s);
 template <int Q, class P>
 cudaError_t launch_general_phaseB(const StepArgs &a, const int8_t *wall, const RegSite *sites, int nsites,
                                   cudaStream_t s);
 template <class P>
 cudaError_t launch_velocity_u(const StepArgs &a, int dims, const int2 *sites, int nsites, cudaStream_t s);
 template <int Q, class P>
-cudaError_t launch_general_phaseC(const StepArgs &a, cudaStream_t s);
+cudaError_t launch_general_phaseC(const StepArgs &a, const int *ids, int nids, cudaStream_t s);
 int read_unsupported_flag(cudaStream_t s);
 struct IbmArgs;
 struct FlexArgs;

@@ -1,0 +1,115 @@
+"""Synthetic workloads of the named shapes, built through the host set-up.
+
+``sphere_refined``: D3Q19 BGK flow past a rigid IB sphere, base grid
+384 x 192 x 192 with two embedded refinement levels (factor 2 each) in boxes
+centred on the sphere; sphere diameter 24 base lattice units with a
+Fibonacci (golden-angle) layout of 5000 markers; uniform inlet u = 0.04 lu,
+Re = 100 on the diameter (nu = 0.04 * 24 / 100 in base lattice units).
+Inlet: forced-equilibrium velocity face; outlet: extrapolate-right; lateral
+faces periodic.
+
+Where the body lives: 5000 markers on the sphere of 96 level-2 lattice
+units (diameter) sit 2.4 lu apart, and the direct-forcing IBM (epsilon near
+3.5) diverges within a few steps there, in the reference's arithmetic as in
+this path (the oracle shows it on a scaled copy).  So the body is on level 1
+(diameter 48 lu, markers 1.2 lu apart; the reference's geometry reader would
+place 7238 there), and the level-2 box sits inside the sphere, centred on
+it, clear of the markers' supports.
+
+``run_sphere`` steps it on the GPU and reports MLUPS (fine updates counted
+2^level times per base step, as the reference's activeCellOps counts them),
+the drag coefficient from the FP64 marker-force sum, and the FP64/FP32
+field difference when both are run.
+"""
+from __future__ import annotations
+
+import math
+import time
+
+import numpy as np
+
+from . import _abi as A
+from . import case as hostcase
+
+
+def fibonacci_sphere(cx: float, cy: float, cz: float, radius: float, n: int) -> np.ndarray:
+    """Golden-angle layout of n points on a sphere, (n, 3)."""
+    inc = math.pi * (3.0 - math.sqrt(5.0))
+    off = 2.0 / n
+    k = np.arange(n)
+    y = k * off - 1.0 + off / 2.0
+    r = np.sqrt(1.0 - y * y)
+    phi = k * inc
+    return np.stack([cx + np.cos(phi) * r * radius, cy + y * radius, cz + np.sin(phi) * r * radius], axis=1)
+
+
+def sphere_refined(nx: int = 384, ny: int = 192, nz: int = 192, diameter_lu: float = 24.0, n_markers: int = 5000,
+                   u_lu: float = 0.04, re: float = 100.0, resolution: int = 16, l1_half: int = 24,
+                   l2_half: int = 4, body_level: int = 1):
+    """(levels [L0, L1, L2], markers (n, 3)) of the sphere workload.  The
+    sphere centre is nx/4 base cells from the inlet on the lateral centre
+    line; the level-1 box spans +-l1_half base cells around it, the level-2
+    box +-l2_half.  The body lives on `body_level`."""
+    dh = 1.0 / resolution
+    dt = u_lu * dh                    # ux0 = 1: ux0 * dt / dh = u_lu
+    nu_lbm = u_lu * diameter_lu / re
+    nu = nu_lbm * dh * dh / dt        # L_NU: nu_lbm = nu * dt / dh^2
+    V, X, F = A.VELOCITY, A.EXTRAPOLATE_RIGHT, A.FLUID
+    defs = hostcase.Definitions(dims=3, resolution=resolution, timestep=dt, bx=nx / resolution, by=ny / resolution,
+                                bz=nz / resolution, re=None, nu=nu, ux0=1.0, no_flow=False, ibm=True,
+                                walls=(V, X, F, F, F, F))
+    l0 = hostcase.build_level0(defs)
+    c = np.array([nx / 4.0, ny / 2.0, nz / 2.0]) * dh
+    lo1, hi1 = tuple(c - l1_half * dh), tuple(c + l1_half * dh)
+    l1 = hostcase.build_subgrid(l0, lo1, hi1)
+    lo2, hi2 = tuple(c - l2_half * dh), tuple(c + l2_half * dh)
+    l2 = hostcase.build_subgrid(l1, lo2, hi2)
+    mk = fibonacci_sphere(c[0], c[1], c[2], 0.5 * diameter_lu * dh, n_markers)
+    return [l0, l1, l2], mk
+
+
+BODY_LEVEL = 1
+
+
+def upload_level(g, lv) -> None:
+    f0 = hostcase.equilibrium(lv.defs.dims, lv.defs.Q, lv.rho, lv.u).reshape(-1)
+    g.upload(f0, lv.u, lv.rho, lv.force_xyz, 0)
+
+
+def run_sphere(precision: int, steps: int, warmup: int = 5, stream=None, levels=None, markers=None,
+               diameter_lu: float = 24.0, u_lu: float = 0.04, body_level: int = BODY_LEVEL) -> dict:
+    """Steps the sphere workload; returns timing, Cd and the L0 fields."""
+    from .gpu import GpuGrid
+    if levels is None:
+        levels, markers = sphere_refined(diameter_lu=diameter_lu, u_lu=u_lu)
+    grids = []
+    for lv in levels:
+        g = GpuGrid(lv.desc(precision=precision), grids[-1] if grids else None)
+        if stream is not None:
+            g.set_stream(stream)
+        grids.append(g)
+    for g, lv in zip(grids, levels):
+        upload_level(g, lv)
+    fine = grids[body_level]
+    fine.ibm_add_body(markers)
+    t = time.perf_counter()
+    grids[0].ibm_initialise()
+    t_init = time.perf_counter() - t
+    grids[0].step(warmup)
+    grids[0].synchronize()
+    t = time.perf_counter()
+    grids[0].step(steps)
+    grids[0].synchronize()
+    sec = time.perf_counter() - t
+    lu = sum(lv.ncell * (2 ** lv.level) for lv in levels)
+    F = fine.ibm_body_force(0)
+    Dl = diameter_lu * 2 ** body_level             # diameter in the body level's lattice units
+    cd = 2.0 * F[0] / (1.0 * u_lu * u_lu * math.pi * Dl * Dl / 4.0)
+    st = grids[0].download(f=False)
+    out = {"steps": steps, "warmup": warmup, "seconds": sec, "ms_per_step": sec / steps * 1e3,
+           "mlups": lu * steps / sec / 1e6, "lattice_updates_per_step": lu, "cd": cd, "force": F.tolist(),
+           "ibm_init_s": t_init, "u0": st["u"], "rho0": st["rho"],
+           "sites": [lv.ncell for lv in levels], "markers": int(len(markers))}
+    for g in reversed(grids):
+        g.close()
+    return out

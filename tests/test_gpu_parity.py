@@ -34,6 +34,13 @@ def make_gpu(desc, parent):
     return GpuGrid(desc, parent)
 
 
+def make_gpu_split(desc, parent):
+    """Interior fluid sites in their own kernel at any grid size."""
+    from luma_gb300.gpu import GpuGrid
+    desc.flags |= A.FLAG_SPLIT_INTERIOR
+    return GpuGrid(desc, parent)
+
+
 def make_oracle(desc, parent):
     return O.OracleGrid(desc, parent)
 
@@ -42,11 +49,12 @@ NO_BODIES = sorted(n for n in CASES.CASES
                    if not CASES.CASES[n].get("bodies") and not CASES.CASES[n].get("filaments"))
 
 
+@pytest.mark.parametrize("split", [False, True], ids=["one_kernel", "split_interior"])
 @pytest.mark.parametrize("name", NO_BODIES)
-def test_fp64_matches_oracle_and_reference(name):
+def test_fp64_matches_oracle_and_reference(name, split):
     spec = CASES.CASES[name]
     fx = R.fixture(name)
-    gg, levels = R.build_backend(name, make_gpu, A.PREC_FP64)
+    gg, levels = R.build_backend(name, make_gpu_split if split else make_gpu, A.PREC_FP64)
     oo, _ = R.build_backend(name, make_oracle)
     done = 0
     for s in spec["steps"]:
@@ -68,10 +76,11 @@ def test_fp64_matches_oracle_and_reference(name):
                 assert rel_l2(gs["rho"], rho) <= 1e-10
 
 
+@pytest.mark.parametrize("split", [False, True], ids=["one_kernel", "split_interior"])
 @pytest.mark.parametrize("name", NO_BODIES)
-def test_fp32_shifted_close_to_fp64(name):
+def test_fp32_shifted_close_to_fp64(name, split):
     spec = CASES.CASES[name]
-    gg, levels = R.build_backend(name, make_gpu, A.PREC_FP32_SHIFTED)
+    gg, levels = R.build_backend(name, make_gpu_split if split else make_gpu, A.PREC_FP32_SHIFTED)
     oo, _ = R.build_backend(name, make_oracle)
     s = spec["steps"][0] if name.startswith("kbc") else spec["steps"][-1]
     gg[0].step(s)
@@ -116,15 +125,16 @@ def test_reduce_mass_momentum():
     assert np.allclose(red["momentum"], mom, rtol=0, atol=1e-12 * l0.ncell)
 
 
+@pytest.mark.parametrize("split", [False, True], ids=["one_kernel", "split_interior"])
 @pytest.mark.parametrize("name", sorted(n for n in CASES.CASES if CASES.CASES[n].get("bodies")))
 @pytest.mark.parametrize("prec", [A.PREC_FP64, A.PREC_FP32_SHIFTED])
-def test_ibm_matches_oracle(name, prec):
+def test_ibm_matches_oracle(name, prec, split):
     """Rigid IB bodies: supports/epsilon/ds from the host set-up equal the
     oracle's (bit-exact); marker forces and fields after the stored steps
     match at 1e-10 (FP64) or within the FP32 bounds."""
     spec = CASES.CASES[name]
     fx = R.fixture(name)
-    gg, levels = R.build_backend(name, make_gpu, prec)
+    gg, levels = R.build_backend(name, make_gpu_split if split else make_gpu, prec)
     oo, _ = R.build_backend(name, make_oracle)
     oibm = O.OracleIBM()
     for lev, reg, pos in CASES.bodies(name):
