@@ -219,7 +219,7 @@ int luma_update_defer(luma_gpu_grid *g) {
 // the full site logic (the rest, less the sites the stream skips).  Grids
 // below kInteriorMinSites keep the single full-logic launch: there the step
 // is bound by launch latency, not by the full kernel's register budget.
-constexpr size_t kInteriorMinSites = 1u << 20;
+constexpr size_t kInteriorMinSites = 1u << 18;
 
 int luma_build_interior(luma_gpu_grid *g) {
     cudaFree(g->fast);

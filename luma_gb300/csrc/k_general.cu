@@ -451,7 +451,38 @@ __global__ void __launch_bounds__(128) k_interior(StepArgs a, const uint8_t *fas
         for (int v = 0; v < Q; ++v) st<P>(a.fNew, (size_t)v * n + id, fn[v]);
         if (deferred) return;
     }
-    collide_site<Q, P, COLL>(b, id, fn, rho, drho, ux, uy, uz);
+    if constexpr (!P::shifted && COLL == LUMA_COLL_BGK) {
+        // FP64 BGK with the constants of cs^2 = 1/3 written out (3, 4.5,
+        // 1.5) instead of the reference's divisions by cs^2: FP64 division
+        // is the costliest operation of the step on this part, and the
+        // results differ from the reference's expression by rounding only.
+        const R om = R(a.omega);
+        const R usq15 = R(1.5) * (ux * ux + uy * uy + uz * uz);
+        R Fx = R(0), Fy = R(0), Fz = R(0);
+        if (b.forcing) {
+            Fx = ldr<P>(a.force, id);
+            Fy = ldr<P>(a.force, n + id);
+            if (D == 3) Fz = ldr<P>(a.force, 2 * n + id);
+        }
+        const R g3 = R(3) * (R(1) - R(0.5) * om);
+#pragma unroll
+        for (int v = 0; v < Q; ++v) {
+            const R c0 = R(L::c(v, 0)), c1 = R(L::c(v, 1)), c2 = R(L::c(v, 2));
+            const R cu = c0 * ux + c1 * uy + (D == 3 ? c2 * uz : R(0));
+            const R w = R(L::w(v));
+            const R eq = w * rho * (R(1) + R(3) * cu + R(4.5) * cu * cu - usq15);
+            R f = fn[v] + om * (eq - fn[v]);
+            if (b.forcing) {
+                const R b1 = R(1) + R(3) * cu;
+                R s = Fx * (c0 * b1 - ux) + Fy * (c1 * b1 - uy);
+                if (D == 3) s += Fz * (c2 * b1 - uz);
+                f += w * (g3 * s);
+            }
+            fn[v] = f;
+        }
+    } else {
+        collide_site<Q, P, COLL>(b, id, fn, rho, drho, ux, uy, uz);
+    }
     void *out = a.ibm_split ? a.fOut : a.fNew;
 #pragma unroll
     for (int v = 0; v < Q; ++v) st<P>(out, (size_t)v * n + id, fn[v]);
