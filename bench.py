@@ -191,7 +191,7 @@ def run_reference(args, rank: int, world: int):
     return 0
 
 
-def measure_adjoint() -> dict:
+def measure_adjoint(nsteps: int = 4000, precisions=("fp32_shifted", "fp64")) -> dict:
     """Cost and memory of the drag gradient on the adjoint workload (D2Q9
     400x160 channel, IB cylinder of 64 markers, 4000 steps, checkpoints every
     100), FP32-shifted as the workload runs and FP64; wall clock around the
@@ -199,7 +199,7 @@ def measure_adjoint() -> dict:
     from luma_gb300 import _abi as A
     from luma_gb300 import adjoint as ADJ
 
-    c = ADJ.cylinder_channel()
+    c = ADJ.cylinder_channel(nsteps=nsteps)
     umax = ADJ.inlet_u_max(c)
     out = {"workload": "D2Q9 BGK channel 400x160, parabolic inlet u_max=0.05 lu, IB cylinder D=20 lu with 64 "
                        "markers on radii 10+N(0,0.1^2) lu (seeded), 4000 steps, checkpoints every 100; "
@@ -207,6 +207,8 @@ def measure_adjoint() -> dict:
            "cost_definition": "(adjoint forward + backward) / plain forward (luma_gpu_step over the same steps)"}
     grads = {}
     for prec, name in ((A.PREC_FP32_SHIFTED, "fp32_shifted"), (A.PREC_FP64, "fp64")):
+        if name not in precisions:
+            continue
         warm = ADJ.DragCase(c.defs, c.markers, 200, 100)
         ADJ.drag_and_gradient(warm, prec)
         g, _ = ADJ.make_grid(c, prec)
@@ -230,11 +232,12 @@ def measure_adjoint() -> dict:
         out[name] = {"J": J, "dJ_du_max": gs / umax, "forward_s": round(fwd, 4), "backward_s": round(bwd, 4),
                      "plain_forward_s": round(plain, 4), "cost_vs_forward": round((fwd + bwd) / plain, 3),
                      "backward_vs_adjoint_forward": round(bwd / fwd, 3), "device_bytes": int(mem)}
-    g32, g64 = grads["fp32_shifted"], grads["fp64"]
-    out["fp32_vs_fp64"] = {"dJ_ds_rel": abs(g32[0] - g64[0]) / abs(g64[0]),
-                           "dJ_dX_rel_max": float(np.max(np.abs(g32[1] - g64[1])) / np.max(np.abs(g64[1])))}
+    if len(grads) == 2:
+        g32, g64 = grads["fp32_shifted"], grads["fp64"]
+        out["fp32_vs_fp64"] = {"dJ_ds_rel": abs(g32[0] - g64[0]) / abs(g64[0]),
+                               "dJ_dX_rel_max": float(np.max(np.abs(g32[1] - g64[1])) / np.max(np.abs(g64[1])))}
     fdp = os.path.join(ROOT, "tests", "golden", "adjoint_fd_cyl400.json")
-    if os.path.exists(fdp):
+    if os.path.exists(fdp) and nsteps == 4000:
         ref = json.load(open(fdp))
         fd = np.array([r["fd"] for r in ref["markers"]])
         chk = {"source": "central differences of the reference's own FP64 build (h=1e-4)"}
@@ -244,6 +247,58 @@ def measure_adjoint() -> dict:
                          "markers_rel_max": float(np.max(np.abs(ad - fd)) / np.max(np.abs(fd)))}
         out["fd_check"] = chk
     return out
+
+
+def run_sphere_workload(args) -> int:
+    """D3Q19 flow past an IB sphere with two refinement levels (384x192x192
+    base; ``--size`` scales the base x extent and everything with it):
+    fine-weighted MLUPS, drag coefficient, FP32-vs-FP64 fields."""
+    from luma_gb300 import _abi as A
+    from luma_gb300 import workloads as WL
+
+    nx = args.size or 384
+    sc = nx / 384.0
+    kw = dict(nx=nx, ny=nx // 2, nz=nx // 2, diameter_lu=24.0 * sc, n_markers=int(round(5000 * sc * sc)),
+              l1_half=max(6, int(round(24 * sc))), l2_half=max(1, int(round(4 * sc))))
+    res = {}
+    sampler = ClockSampler(0)
+    sampler.start()
+    time.sleep(0.3)
+    t0 = time.monotonic()
+    for name, prec in (("fp32_shifted", A.PREC_FP32_SHIFTED), ("fp64", A.PREC_FP64)):
+        if args.precision not in ("both", name.split("_")[0]):
+            continue
+        levels, markers = WL.sphere_refined(**kw)
+        res[name] = WL.run_sphere(prec, args.steps, warmup=args.warmup, levels=levels, markers=markers,
+                                  diameter_lu=kw["diameter_lu"])
+    t1 = time.monotonic()
+    clocks = sampler.summary(t0, t1)
+    head = res.get("fp32_shifted") or res.get("fp64")
+    line = {"metric": "D3Q19 IBM sphere, two refinement levels: lattice updates per second (fine levels "
+                      "counted 2^level times per base step)",
+            "value": round(head["mlups"], 2), "unit": "MLUPS", "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": round(head["ms_per_step"], 4), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32" if "fp32_shifted" in res else "f64",
+            "data": "synthetic",
+            "config": {"workload": f"D3Q19 LBGK {nx}x{nx // 2}x{nx // 2} base grid, level-1 box "
+                                   f"+-{kw['l1_half']} and level-2 box +-{kw['l2_half']} base cells around the "
+                                   f"sphere (D={kw['diameter_lu']:g} base lu, {kw['n_markers']} Fibonacci markers "
+                                   f"on level 1), inlet u=0.04 lu, Re=100, lateral faces periodic",
+                       "sites_per_level": head["sites"], "lattice_updates_per_base_step":
+                           head["lattice_updates_per_step"]},
+            "clocks": clocks}
+    for name, r in res.items():
+        line[name] = {"mlups": round(r["mlups"], 2), "ms_per_step": round(r["ms_per_step"], 4), "cd": r["cd"],
+                      "force": r["force"], "ibm_init_s": round(r["ibm_init_s"], 3)}
+    if len(res) == 2:
+        u32, u64 = res["fp32_shifted"]["u0"], res["fp64"]["u0"]
+        r32, r64 = res["fp32_shifted"]["rho0"], res["fp64"]["rho0"]
+        line["fp32_vs_fp64"] = {"rel_l2_u_level0": float(np.linalg.norm(u32 - u64) / np.linalg.norm(u64)),
+                                "max_abs_rho_level0": float(np.max(np.abs(r32 - r64))),
+                                "cd_rel": abs(res["fp32_shifted"]["cd"] - res["fp64"]["cd"]) / abs(res["fp64"]["cd"]),
+                                "speedup": round(res["fp32_shifted"]["mlups"] / res["fp64"]["mlups"], 3)}
+    print(json.dumps(line), flush=True)
+    return 0
 
 
 def run_ours(args, rank: int, world: int, local_rank: int):
@@ -259,7 +314,7 @@ def run_ours(args, rank: int, world: int, local_rank: int):
         dist = dist_
     dev = torch.device("cuda", local_rank)
     stream = torch.cuda.current_stream(dev)
-    n = args.size
+    n = args.size or SIZE
     l0 = workload_level0(n)
     f0 = equilibrium_f(l0)
     ncell = l0.ncell
@@ -407,7 +462,13 @@ def main(argv=None) -> int:
     ap.add_argument("--steps", type=int, default=2000)
     ap.add_argument("--warmup", type=int, default=20)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--size", type=int, default=SIZE)
+    ap.add_argument("--size", type=int, default=None,
+                    help="box edge (default 256) or, for --workload sphere, base x extent (default 384)")
+    ap.add_argument("--workload", default="box", choices=["box", "sphere", "cylinder_adjoint"],
+                    help="box: the headline 256^3 line (default); sphere: IB sphere with two refinement "
+                         "levels; cylinder_adjoint: the drag-gradient workload alone")
+    ap.add_argument("--precision", default="both", choices=["both", "fp32", "fp64"],
+                    help="sphere / cylinder_adjoint workloads: which precisions to run")
     ap.add_argument("--cpu-steps", type=int, default=20)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint workload measurement")
@@ -419,6 +480,14 @@ def main(argv=None) -> int:
     local_rank = int(os.environ.get("LOCAL_RANK", "0"))
     if args.impl == "reference":
         return run_reference(args, rank, world)
+    if args.workload == "sphere":
+        return run_sphere_workload(args) if rank == 0 else 0
+    if args.workload == "cylinder_adjoint":
+        if rank == 0:
+            prec = {"both": ("fp32_shifted", "fp64"), "fp32": ("fp32_shifted",), "fp64": ("fp64",)}[args.precision]
+            steps = args.steps if args.steps != 2000 else 4000
+            print(json.dumps({"workload": "cylinder_adjoint", "adjoint": measure_adjoint(steps, prec)}), flush=True)
+        return 0
     return run_ours(args, rank, world, local_rank)
 
 
