@@ -301,6 +301,66 @@ def run_sphere_workload(args) -> int:
     return 0
 
 
+def run_filaments_workload(args) -> int:
+    """D3Q27 KBC (streamed-population form) 512x256x256 with one refinement
+    level around 64 FEM filaments: MLUPS, HBM fraction, tip displacement of
+    FP32 vs FP64 after the same steps."""
+    from luma_gb300 import _abi as A
+    from luma_gb300 import workloads as WL
+
+    nx = args.size or 512
+    sc = nx / 512.0
+    kw = dict(nx=nx, ny=nx // 2, nz=nx // 2, box=(max(8, int(96 * sc)), max(8, int(64 * sc)), max(8, int(96 * sc))),
+              resolution=max(4, int(32 * sc)), n_fil=64 if sc >= 0.5 else 4, nel=32 if sc >= 0.5 else 8)
+    res = {}
+    sampler = ClockSampler(0)
+    sampler.start()
+    time.sleep(0.3)
+    t0 = time.monotonic()
+    for name, prec in (("fp32_shifted", A.PREC_FP32_SHIFTED), ("fp64", A.PREC_FP64)):
+        if args.precision not in ("both", name.split("_")[0]):
+            continue
+        levels, fils = WL.kbc_filaments(**kw)
+        res[name] = WL.run_filaments(prec, args.steps, warmup=args.warmup, levels=levels, fils=fils)
+    t1 = time.monotonic()
+    clocks = sampler.summary(t0, t1)
+    peaks = read_peaks()
+    head = res.get("fp32_shifted") or res.get("fp64")
+    s = 4 if "fp32_shifted" in res else 8
+    bpl = 2 * 27 * s + 1
+    line = {"metric": "D3Q27 KBC + refinement + 64 FEM filaments: lattice updates per second (level 1 counted "
+                      "twice per base step)",
+            "value": round(head["mlups"], 2), "unit": "MLUPS", "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": round(head["ms_per_step"], 4), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32" if s == 4 else "f64", "data": "synthetic",
+            "config": {"workload": f"D3Q27 KBC (streamed-population form) {nx}x{nx // 2}x{nx // 2}, level-1 box "
+                                   f"{kw['box']} base cells, {kw['n_fil']} filaments x {kw['nel']} elements "
+                                   f"(one marker per node), EI log-uniform [1e-3,1e-1] (EI/(rho U^2 L^3)), "
+                                   f"structure/fluid density 100, inlet u=0.03 lu, Re=1000 on the filament length",
+                       "sites_per_level": head["sites"], "lattice_updates_per_base_step":
+                           head["lattice_updates_per_step"]},
+            "roofline": {"bound": "hbm", "bytes_per_lu": bpl,
+                         "achieved": round(head["mlups"] * 1e6 * bpl / 1e9, 1), "peak": peaks["hbm_gbs"],
+                         "unit": "GB/s", "frac": round(head["mlups"] * 1e6 * bpl / 1e9 / peaks["hbm_gbs"], 4),
+                         "note": "whole step (all kernels) against 2*Q*s+1 bytes per lattice update"},
+            "clocks": clocks}
+    for name, r in res.items():
+        disp = r["tips"] - r["tip0"]
+        line[name] = {"mlups": round(r["mlups"], 2), "ms_per_step": round(r["ms_per_step"], 4),
+                      "finite": r["finite"], "ibm_init_s": round(r["ibm_init_s"], 3),
+                      "tip_displacement_max": float(np.max(np.linalg.norm(disp, axis=1)))}
+    if len(res) == 2:
+        d32 = res["fp32_shifted"]["tips"] - res["fp32_shifted"]["tip0"]
+        d64 = res["fp64"]["tips"] - res["fp64"]["tip0"]
+        line["fp32_vs_fp64"] = {
+            "tip_displacement_rel_err": float(np.linalg.norm(d32 - d64) / np.linalg.norm(d64)),
+            "rel_l2_u_level0": float(np.linalg.norm(res["fp32_shifted"]["u0"] - res["fp64"]["u0"]) /
+                                     np.linalg.norm(res["fp64"]["u0"])),
+            "speedup": round(res["fp32_shifted"]["mlups"] / res["fp64"]["mlups"], 3)}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def run_ours(args, rank: int, world: int, local_rank: int):
     import torch
     from luma_gb300 import _abi as A
@@ -464,9 +524,10 @@ def main(argv=None) -> int:
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--size", type=int, default=None,
                     help="box edge (default 256) or, for --workload sphere, base x extent (default 384)")
-    ap.add_argument("--workload", default="box", choices=["box", "sphere", "cylinder_adjoint"],
+    ap.add_argument("--workload", default="box", choices=["box", "sphere", "cylinder_adjoint", "filaments"],
                     help="box: the headline 256^3 line (default); sphere: IB sphere with two refinement "
-                         "levels; cylinder_adjoint: the drag-gradient workload alone")
+                         "levels; cylinder_adjoint: the drag-gradient workload alone; filaments: D3Q27 KBC with "
+                         "one refinement level and 64 FEM filaments")
     ap.add_argument("--precision", default="both", choices=["both", "fp32", "fp64"],
                     help="sphere / cylinder_adjoint workloads: which precisions to run")
     ap.add_argument("--cpu-steps", type=int, default=20)
@@ -482,6 +543,8 @@ def main(argv=None) -> int:
         return run_reference(args, rank, world)
     if args.workload == "sphere":
         return run_sphere_workload(args) if rank == 0 else 0
+    if args.workload == "filaments":
+        return run_filaments_workload(args) if rank == 0 else 0
     if args.workload == "cylinder_adjoint":
         if rank == 0:
             prec = {"both": ("fp32_shifted", "fp64"), "fp32": ("fp32_shifted",), "fp64": ("fp64",)}[args.precision]

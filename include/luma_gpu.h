@@ -198,8 +198,13 @@ int luma_gpu_ibm_initialise(luma_gpu_grid *root);
  * clamped or simply supported at `start` (already shifted by the wall
  * thickness where the reader shifts it); angle_v in degrees; dm =
  * GridObj::dm; fsi_vel_scale = L_UX0*dt/dh (the FSI residual's scale,
- * src/ObjectManager_ops_ibm.cpp:1007).  2D grids only: the reference's FEM
- * is planar and aborts in 3D.  The FEM (Newmark-beta + Newton-Raphson) and
+ * src/ObjectManager_ops_ibm.cpp:1007).  The beam is planar (x-y plane, 3
+ * DOF per node) as the reference's FEM is; on a 3D grid the reference aborts
+ * on a matrix-size mismatch in FEMElement::loadVector and
+ * FEMBody::updateIBMarkers (src/FEMElement.cpp:153-157,
+ * src/FEMBody.cpp:356-361), which here take the x and y components and keep
+ * the markers' z (the only change), with the element depth `depth` (2D: dh,
+ * src/FEMBody.cpp:103-105).  The FEM (Newmark-beta + Newton-Raphson) and
  * the FSI sub-iterations run on the device. */
 int luma_gpu_ibm_add_filament(luma_gpu_grid *grid, const double start[3], double length, double height,
                               double depth, double angle_v, int nel, int clamped, double density,

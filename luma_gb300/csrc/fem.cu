@@ -31,8 +31,13 @@ constexpr double kNbDelta = 0.5;
 constexpr double kRelax = 0.5;
 constexpr double kPi = 3.14159265358979323846;
 
+// Shared memory budget for a filament's stiffness matrix (static shared
+// arrays of the kernel take the rest of the 227 KB).
+constexpr size_t kFemSmemMax = 200 * 1024;
+
 struct FemKernelArgs {
     int nfil, maxdof, maxmk;
+    int k_in_smem;              // K of the filament in dynamic shared memory
     const int *node_off, *el_off, *dof_off, *mk_off, *bc;
     const double *dm, *velscale;
     const double *pos0, *ang0;
@@ -91,49 +96,96 @@ __device__ void update_values(const FemKernelArgs &a, int f) {
 // Partial-pivot LU of the n x n block whose column-major element (r, c)
 // is A[(off + c) * lda + (off + r)] (a row-major matrix read column-major,
 // as GridUtils::solveLinearSystem hands it to dgetrf_), then the transposed
-// solve for x (length n).  Pivot search and the triangular solves are
-// sequential (the reference's summation order); column updates run across
-// the block.
+// solve for x (length n), n <= 512.  Every element sees the operations of
+// the dense serial algorithm in the same order; the ones that are exact
+// no-ops (a zero multiplier, a zero matrix entry in the triangular sums) are
+// skipped, which is what makes the banded beam and epsilon systems cheap.
+// One warp does the work (lanes over rows / columns, warp barriers only);
+// the pivot is the first row of largest magnitude (ties to the lower row).
+// Called by the whole block; returns after a block barrier.
 __device__ void lu_solve_block(double *A, int lda, int off, int n, int *ipiv, double *x) {
 #define AC(r, c) A[(size_t)(off + (c)) * lda + (off + (r))]
-    __shared__ int piv;
-    for (int k = 0; k < n; ++k) {
-        if (threadIdx.x == 0) {
-            int p = k;
-            double best = fabs(AC(k, k));
-            for (int r = k + 1; r < n; ++r) {
+    __shared__ int nnz;
+    __shared__ int nzr[512];
+    __shared__ int lim[512];
+    if (threadIdx.x < 32) {
+        const int lane = threadIdx.x;
+        for (int k = 0; k < n; ++k) {
+            double best = 0.0;
+            int p = n;
+            for (int r = k + lane; r < n; r += 32) {
                 const double v = fabs(AC(r, k));
-                if (v > best) { best = v; p = r; }
+                if (p == n || v > best) { best = v; p = r; }
             }
-            ipiv[k] = p + 1;
-            piv = p;
-        }
-        __syncthreads();
-        const int p = piv;
-        const bool zero = AC(p, k) == 0.0;
-        __syncthreads();
-        if (zero) continue;
-        if (p != k)
-            for (int c = threadIdx.x; c < n; c += blockDim.x) {
-                const double t = AC(k, c);
-                AC(k, c) = AC(p, c);
-                AC(p, c) = t;
+            for (int o = 16; o > 0; o >>= 1) {
+                const double ob = __shfl_xor_sync(0xffffffffu, best, o);
+                const int op = __shfl_xor_sync(0xffffffffu, p, o);
+                if (op < n && (p == n || ob > best || (ob == best && op < p))) { best = ob; p = op; }
             }
-        __syncthreads();
-        const double inv = 1.0 / AC(k, k);
-        for (int r = k + 1 + threadIdx.x; r < n; r += blockDim.x) AC(r, k) *= inv;
-        __syncthreads();
-        for (int c = k + 1 + threadIdx.x; c < n; c += blockDim.x) {
-            const double akc = AC(k, c);
-            if (akc == 0.0) continue;
-            for (int r = k + 1; r < n; ++r) AC(r, c) -= AC(r, k) * akc;
+            if (lane == 0) ipiv[k] = p + 1;
+            if (AC(p, k) == 0.0) continue;  // same value on every lane
+            __syncwarp();
+            if (p != k)
+                for (int c = lane; c < n; c += 32) {
+                    const double t = AC(k, c);
+                    AC(k, c) = AC(p, c);
+                    AC(p, c) = t;
+                }
+            if (lane == 0) nnz = 0;
+            __syncwarp();
+            const double inv = 1.0 / AC(k, k);
+            for (int r = k + 1 + lane; r < n; r += 32) {
+                const double m = AC(r, k) * inv;
+                AC(r, k) = m;
+                if (m != 0.0) nzr[atomicAdd(&nnz, 1)] = r;
+            }
+            __syncwarp();
+            const int cnt = nnz;
+            for (int c = k + 1 + lane; c < n; c += 32) {
+                const double akc = AC(k, c);
+                if (akc == 0.0) continue;
+                for (int q = 0; q < cnt; ++q) {
+                    const int r = nzr[q];
+                    AC(r, c) -= AC(r, k) * akc;
+                }
+            }
+            __syncwarp();
         }
-        __syncthreads();
-    }
-    if (threadIdx.x == 0) {
-        for (int r = 0; r < n; ++r) { double s = x[r]; for (int c = 0; c < r; ++c) s -= AC(c, r) * x[c]; x[r] = s / AC(r, r); }
-        for (int r = n - 1; r >= 0; --r) { double s = x[r]; for (int c = r + 1; c < n; ++c) s -= AC(c, r) * x[c]; x[r] = s; }
-        for (int k = n - 1; k >= 0; --k) { const int p = ipiv[k] - 1; if (p != k) { const double t = x[k]; x[k] = x[p]; x[p] = t; } }
+        // forward sums start at the first non-zero of each row's range
+        for (int r = lane; r < n; r += 32) {
+            int c = 0;
+            while (c < r && AC(c, r) == 0.0) ++c;
+            lim[r] = c;
+        }
+        __syncwarp();
+        if (lane == 0)
+            for (int r = 0; r < n; ++r) {
+                double s = x[r];
+                for (int c = lim[r]; c < r; ++c) {
+                    const double v = AC(c, r);
+                    if (v != 0.0) s -= v * x[c];
+                }
+                x[r] = s / AC(r, r);
+            }
+        __syncwarp();
+        // backward sums end at the last non-zero
+        for (int r = lane; r < n; r += 32) {
+            int c = n - 1;
+            while (c > r && AC(c, r) == 0.0) --c;
+            lim[r] = c;
+        }
+        __syncwarp();
+        if (lane == 0) {
+            for (int r = n - 1; r >= 0; --r) {
+                double s = x[r];
+                for (int c = r + 1; c <= lim[r]; ++c) {
+                    const double v = AC(c, r);
+                    if (v != 0.0) s -= v * x[c];
+                }
+                x[r] = s;
+            }
+            for (int k = n - 1; k >= 0; --k) { const int p = ipiv[k] - 1; if (p != k) { const double t = x[k]; x[k] = x[p]; x[p] = t; } }
+        }
     }
     __syncthreads();
 #undef AC
@@ -248,8 +300,9 @@ __global__ void k_fem_dynamic(FemKernelArgs a) {
     const int e0 = a.el_off[f], ne = a.el_off[f + 1] - e0;
     const int mk0 = a.mk_off[f], nmk = a.mk_off[f + 1] - mk0;
     const int bc = a.bc[f];
+    extern __shared__ double fem_smem[];
     double *M = a.M + (size_t)f * a.maxdof * a.maxdof;
-    double *K = a.K + (size_t)f * a.maxdof * a.maxdof;
+    double *K = a.k_in_smem ? fem_smem : a.K + (size_t)f * a.maxdof * a.maxdof;
     double *Meff = a.tmp + 2 * (size_t)d0, *MF = a.tmp + 2 * (size_t)d0 + nd;
     __shared__ int ipiv[512];
     __shared__ int go;
@@ -420,9 +473,12 @@ __global__ void k_flex_support(FemKernelArgs a) {
             ++ns;
         };
         add(in, jn, kn, nearp);
-        for (int i = in - 5; i <= in + 5; i++)
-            for (int j = jn - 5; j <= jn + 5; j++)
-                for (int k = (D == 3 ? kn - 5 : 0); k <= (D == 3 ? kn + 5 : 0); k++) {
+        // the reference scans +-5 nodes; every cage node (< 1.5 dh from the
+        // marker, which is < 1 dh from the near node) lies within +-2, met
+        // in the same (i, j, k) order
+        for (int i = in - 2; i <= in + 2; i++)
+            for (int j = jn - 2; j <= jn + 2; j++)
+                for (int k = (D == 3 ? kn - 2 : 0); k <= (D == 3 ? kn + 2 : 0); k++) {
                     double e[3] = {nearp[0] + (i - in) * dh, nearp[1] + (j - jn) * dh, nearp[2]};
                     if (D == 3) e[2] = nearp[2] + (k - kn) * dh;
                     const bool cage = (fabs(p[0] - e[0]) / dh < 1.5) && (fabs(p[1] - e[1]) / dh < 1.5) &&
@@ -666,7 +722,12 @@ int luma_fem_supports(luma_gpu_grid *g) {
 // ObjectManager::ibm_moveBodies (:61-104) for the filaments of a grid.
 int luma_fem_move_bodies(luma_gpu_grid *g) {
     FemKernelArgs a = full_args(g);
-    k_fem_dynamic<<<a.nfil, 128, 0, g->stream>>>(a);
+    // the stiffness matrix of a filament in shared memory when it fits
+    const size_t kb = (size_t)a.maxdof * a.maxdof * sizeof(double);
+    a.k_in_smem = kb <= kFemSmemMax &&
+                  cudaFuncSetAttribute(k_fem_dynamic, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kb) == cudaSuccess;
+    if (!a.k_in_smem) cudaGetLastError();
+    k_fem_dynamic<<<a.nfil, 128, a.k_in_smem ? kb : 0, g->stream>>>(a);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return luma_set_error(LUMA_E_CUDA, "FEM: %s", cudaGetErrorString(e));
     return luma_fem_supports(g);
@@ -720,13 +781,15 @@ void luma_fem_free(luma_gpu_grid *g) {
 
 // A flexible filament as the reference's FILAMENT_ARRAY reader builds it
 // (inc/Body.h:143-187 markers, src/FEMBody.cpp:48-130 beam,
-// :378-424 IB <-> FEM mapping).  2D only, as the reference's FEM is planar.
+// :378-424 IB <-> FEM mapping).  The beam is planar (x-y) as the
+// reference's; on a 3D grid its load and marker update use the x and y
+// components and markers keep their z.
 extern "C" int luma_gpu_ibm_add_filament(luma_gpu_grid *g, const double start[3], double length, double height,
                                          double depth, double angle_v, int nel, int clamped, double density,
                                          double E, double dm, double fsi_vel_scale, int *body_index) {
     if (!g || !start || nel <= 0 || length <= 0) return luma_set_error(LUMA_E_INVALID, "bad filament arguments");
-    if (g->d.dims != 2)
-        return luma_set_error(LUMA_E_INVALID, "FEM filaments are planar: the reference's FEM aborts in 3D");
+    if (g->d.dims == 3 && !(depth > 0))
+        return luma_set_error(LUMA_E_INVALID, "a filament on a 3D grid needs a positive depth");
     const double dh = g->d.dh;
     const int nmk = (int)std::floor(length / dh) + 1;
     const double spacing = length / (nmk - 1);
@@ -753,7 +816,7 @@ extern "C" int luma_gpu_ibm_add_filament(luma_gpu_grid *g, const double start[3]
         fb.pos0.push_back(start[2] + i * fs_h * std::sin(0.0 * kPi / 180.0));
         fb.ang0.push_back(angle_v * kPi / 180.0);
     }
-    depth = dh;  // 2D: unit lattice depth (src/FEMBody.cpp:103-105)
+    if (g->d.dims == 2) depth = dh;  // 2D: unit lattice depth (src/FEMBody.cpp:103-105)
     for (int e = 0; e < nel; ++e) {
         fb.len0.push_back(fs);
         fb.area.push_back(height * depth);

@@ -101,7 +101,10 @@ struct IbmDevice {
 
 // Flexible filaments: markers with fixed-capacity support slots (supports
 // move every FSI iteration) and the FEM beam state, all device resident.
-constexpr int kFlexMaxSupp = 27;
+// The support cage |x - X|/dh < 1.5 holds 3 nodes per axis, but a marker
+// within rounding of a half-node offset can pass the test on 4 (both ends
+// at 1.5 minus an ulp): 4^3 slots cover every case in 3D.
+constexpr int kFlexMaxSupp = 64;
 
 struct FlexArgs {
     int nm;                     // flexible markers on this grid (all filaments)

@@ -20,6 +20,14 @@ it, clear of the markers' supports.
 2^level times per base step, as the reference's activeCellOps counts them),
 the drag coefficient from the FP64 marker-force sum, and the FP64/FP32
 field difference when both are run.
+
+``kbc_filaments``: D3Q27 KBC 512 x 256 x 256 with one refinement level
+around an array of 64 FEM filaments (32 elements, one marker per node), the
+filament-array workload; ``run_filaments`` steps it and reports MLUPS and
+the filament tips.  The reference cannot run it (its FEM aborts in 3D); the
+structure density is 100x the fluid's, since lighter filaments in the
+reference's 3D coupling diverge within a few dozen steps (oracle, scaled
+copy).
 """
 from __future__ import annotations
 
@@ -110,6 +118,93 @@ def run_sphere(precision: int, steps: int, warmup: int = 5, stream=None, levels=
            "mlups": lu * steps / sec / 1e6, "lattice_updates_per_step": lu, "cd": cd, "force": F.tolist(),
            "ibm_init_s": t_init, "u0": st["u"], "rho0": st["rho"],
            "sites": [lv.ncell for lv in levels], "markers": int(len(markers))}
+    for g in reversed(grids):
+        g.close()
+    return out
+
+
+def kbc_filaments(nx: int = 512, ny: int = 256, nz: int = 256, n_fil: int = 64, nel: int = 32, u_lu: float = 0.03,
+                  re: float = 1000.0, resolution: int = 32, box=(96, 64, 96), ei_range=(1e-3, 1e-1),
+                  density_ratio: float = 100.0, seed: int = 20261204):
+    """(levels [L0, L1], filaments [dict of luma_gpu_ibm_add_filament
+    arguments]) of the filament-array workload: D3Q27 KBC (streamed-population
+    form), base grid nx x ny x nz, one refinement level in a box of `box` base
+    cells centred in y and z and starting nx/4 from the inlet; n_fil
+    filaments on level 1 on an 8 x 8 array over x-z with seeded jitter, each
+    clamped at the box's lower third and pointing +y, nel elements, one
+    marker per node (length nel level-1 lattice units), thickness and depth
+    one level-1 lattice unit, structure density density_ratio x fluid.
+    Bending rigidity EI log-uniform in ei_range, non-dimensional
+    (EI / (rho U^2 L^3), L the filament length).  Uniform inlet u = u_lu,
+    Re = u L / nu = re on the filament length; outlet extrapolate-right,
+    bottom/top solid, front/back periodic."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    dh = 1.0 / resolution
+    dt = u_lu * dh
+    dh1 = dh / 2.0
+    L = nel * dh1                             # filament length (one marker per node)
+    nu = 1.0 * L / re                         # L_NU with ux0 = 1
+    V, X, S, F = A.VELOCITY, A.EXTRAPOLATE_RIGHT, A.SOLID, A.FLUID
+    defs = hostcase.Definitions(dims=3, resolution=resolution, timestep=dt, bx=nx / resolution, by=ny / resolution,
+                                bz=nz / resolution, re=None, nu=nu, ux0=1.0, no_flow=False, ibm=True, kbc=True,
+                                walls=(V, X, S, S, F, F))
+    l0 = hostcase.build_level0(defs)
+    bx, by, bz = box
+    x0 = (nx // 4) * dh
+    y0 = (ny // 2 - by // 2) * dh
+    z0 = (nz // 2 - bz // 2) * dh
+    l1 = hostcase.build_subgrid(l0, (x0, y0, z0), (x0 + bx * dh, y0 + by * dh, z0 + bz * dh))
+    side = int(round(math.sqrt(n_fil)))
+    fils = []
+    rho_f = defs.physical_rho
+    dm = (rho_f / defs.rho_in) * dh1 ** 3
+    h = dh1
+    depth = dh1
+    I = depth * h ** 3 / 12.0
+    for q in range(n_fil):
+        ix, iz = q % side, q // side
+        px = x0 + (ix + 0.5 + rng.uniform(-0.25, 0.25)) * (bx * dh) / side
+        pz = z0 + (iz + 0.5 + rng.uniform(-0.25, 0.25)) * (bz * dh) / side
+        py = y0 + by * dh / 3.0
+        ei = math.exp(rng.uniform(math.log(ei_range[0]), math.log(ei_range[1])))
+        E = ei * rho_f * 1.0 * L ** 3 / I
+        fils.append(dict(start=(px, py, pz), length=L, height=h, depth=depth, angle_v=90.0, nel=nel, clamped=True,
+                         density=density_ratio * rho_f, E=E, dm=dm, fsi_vel_scale=1.0 * dt / dh1))
+    return [l0, l1], fils
+
+
+def run_filaments(precision: int, steps: int, warmup: int = 2, levels=None, fils=None, fix_kbc: bool = True) -> dict:
+    """Steps the filament-array workload; returns timing and tip positions."""
+    from .gpu import GpuGrid
+    if levels is None:
+        levels, fils = kbc_filaments()
+    grids = []
+    for lv in levels:
+        desc = lv.desc(precision=precision, fix_kbc=fix_kbc)
+        g = GpuGrid(desc, grids[-1] if grids else None)
+        grids.append(g)
+    for g, lv in zip(grids, levels):
+        upload_level(g, lv)
+    fine = grids[-1]
+    for fl in fils:
+        fine.ibm_add_filament(**fl)
+    t = time.perf_counter()
+    grids[0].ibm_initialise()
+    t_init = time.perf_counter() - t
+    tip0 = np.array([fine.ibm_markers(b)[-1, :3] for b in range(len(fils))])
+    grids[0].step(warmup)
+    grids[0].synchronize()
+    t = time.perf_counter()
+    grids[0].step(steps)
+    grids[0].synchronize()
+    sec = time.perf_counter() - t
+    lu = sum(lv.ncell * (2 ** lv.level) for lv in levels)
+    tips = np.array([fine.ibm_markers(b)[-1, :3] for b in range(len(fils))])
+    st = grids[0].download(f=False)
+    out = {"steps": steps, "warmup": warmup, "seconds": sec, "ms_per_step": sec / steps * 1e3,
+           "mlups": lu * steps / sec / 1e6, "lattice_updates_per_step": lu, "ibm_init_s": t_init,
+           "tip0": tip0, "tips": tips, "u0": st["u"], "sites": [lv.ncell for lv in levels],
+           "finite": bool(np.isfinite(st["u"]).all())}
     for g in reversed(grids):
         g.close()
     return out

@@ -1454,12 +1454,15 @@ static void fem_commit_start_of_step(oracle_grid *g) {
 
 /* A flexible filament: the markers of Body's filament builder
  * (inc/Body.h:143-187) and its FEMBody (src/FEMBody.cpp:48-130) with the
- * IB <-> FEM node mapping (:378-424).  angle_v in degrees; 2D only (the
- * reference's FEM is planar).  Returns the IB body index. */
+ * IB <-> FEM node mapping (:378-424).  angle_v in degrees.  The beam is
+ * planar (x-y); on a 3D grid the load and the marker update take the x and
+ * y components and markers keep their z, the one change that lets the
+ * reference's planar FEM run in 3D (where it aborts on a matrix-size
+ * mismatch).  Returns the IB body index. */
 int oracle_ibm_add_filament(oracle_grid *g, const double start[3], double length, double height, double depth,
                             double angle_v, int nel, int clamped, double density, double E, double dm,
                             double fsi_vel_scale) {
-    if (g->D != 2) { set_err("FEM filaments are planar (2D) in the reference"); return -1; }
+    if (g->D == 3 && !(depth > 0)) { set_err("a filament on a 3D grid needs a positive depth"); return -1; }
     const double dh = g->d.dh;
     const int nmk = (int)floor(length / dh) + 1;
     const double spacing = length / (nmk - 1);
@@ -1496,7 +1499,7 @@ int oracle_ibm_add_filament(oracle_grid *g, const double start[3], double length
         f->ang[i] = f->ang0[i];
     }
     memcpy(f->pos, f->pos0, sizeof(double) * 3 * (nel + 1));
-    depth = dh; /* 2D: unit lattice depth (src/FEMBody.cpp:103-105) */
+    if (g->D == 2) depth = dh; /* 2D: unit lattice depth (src/FEMBody.cpp:103-105) */
     f->el = (fem_el *)calloc(nel, sizeof(fem_el));
     for (int e = 0; e < nel; ++e) {
         fem_el *el = &f->el[e];

@@ -195,3 +195,46 @@ def test_filament_fsi_matches_oracle(name):
         assert np.max(np.abs(gm[:, 0:2] - om[:, 0:2])) <= 1e-12
         assert rel_l2(gm[:, 3:5], om[:, 3:5]) <= 1e-8, (s, rel_l2(gm[:, 3:5], om[:, 3:5]))
         assert rel_l2(gs["u"], fx[f"u_{s}"]) <= 1e-10
+
+
+@pytest.mark.parametrize("split", [False, True], ids=["one_kernel", "split_interior"])
+def test_filament_3d_matches_oracle(split):
+    """A filament on a 3D grid (D3Q19 channel 40x20x10): the planar beam
+    with the one change that lets it run in 3D (x-y load and marker update,
+    markers keep z).  The reference aborts there, so parity is against the
+    oracle only (3D FEM parity unpinned by the reference): FP64 flow field
+    rel L2 <= 1e-10, marker positions within 1e-11, marker forces rel L2
+    <= 1e-8 after 40 steps."""
+    from luma_gb300 import case as hc
+    V, X, S, F = A.VELOCITY, A.EXTRAPOLATE_RIGHT, A.SOLID, A.FLUID
+    d = hc.Definitions(dims=3, resolution=20, timestep=1.0 / 500.0, bx=2.0, by=1.0, bz=0.5, re=100, ux0=1.0,
+                       ibm=True, walls=(V, X, S, S, F, F))
+    l0 = hc.build_level0(d)
+    dh = 1.0 / d.resolution
+    fil = dict(start=(0.513, dh, 0.261), length=0.4, height=0.02, depth=0.05, angle_v=90.0, nel=10,
+               clamped=True, density=1.0e4, E=1.0e8, dm=(d.physical_rho / d.rho_in) * dh ** 3,
+               fsi_vel_scale=d.ux0 * d.timestep / dh)
+    desc = l0.desc(precision=A.PREC_FP64)
+    if split:
+        desc.flags |= A.FLAG_SPLIT_INTERIOR
+    from luma_gb300.gpu import GpuGrid
+    g = GpuGrid(desc)
+    o = O.OracleGrid(l0.desc())
+    f0 = hc.equilibrium(3, 19, l0.rho, l0.u).reshape(-1)
+    for x in (g, o):
+        x.upload(f0, l0.u, l0.rho, l0.force_xyz, 0)
+    oibm = O.OracleIBM()
+    g.ibm_add_filament(**fil)
+    oibm.add_filament(o, **fil)
+    g.ibm_initialise()
+    oibm.initialise()
+    for _ in range(4):
+        g.step(10)
+        o.step(10)
+        gs, os_ = g.download(), o.download()
+        gm, om = g.ibm_markers(0), oibm.markers(0)
+        assert rel_l2(gs["u"], os_["u"]) <= 1e-10, rel_l2(gs["u"], os_["u"])
+        assert np.max(np.abs(gm[:, 0:3] - om[:, 0:3])) <= 1e-11
+        assert np.all(gm[:, 2] == fil["start"][2])
+        assert rel_l2(gm[:, 3:6], om[:, 3:6]) <= 1e-8, rel_l2(gm[:, 3:6], om[:, 3:6])
+    assert np.max(np.abs(gm[:, 0] - fil["start"][0])) > 1e-3   # the filament bent
