@@ -38,6 +38,7 @@ constexpr size_t kFemSmemMax = 200 * 1024;
 struct FemKernelArgs {
     int nfil, maxdof, maxmk;
     int k_in_smem;              // K of the filament in dynamic shared memory
+    int eps_in_smem;            // the epsilon matrix of the filament in dynamic shared memory
     const int *node_off, *el_off, *dof_off, *mk_off, *bc;
     const double *dm, *velscale;
     const double *pos0, *ang0;
@@ -103,27 +104,36 @@ __device__ void update_values(const FemKernelArgs &a, int f) {
 // One warp does the work (lanes over rows / columns, warp barriers only);
 // the pivot is the first row of largest magnitude (ties to the lower row).
 // Called by the whole block; returns after a block barrier.
+// Zero tests and magnitude order on the bit patterns (integer pipe): +-0
+// are the only doubles whose bits shifted left by one are 0, and |x| of
+// non-NaN doubles orders like its bits read as unsigned.
+__device__ __forceinline__ bool is_zero(double v) { return (__double_as_longlong(v) << 1) == 0; }
+__device__ __forceinline__ unsigned long long mag_bits(double v) {
+    return (unsigned long long)__double_as_longlong(v) & 0x7fffffffffffffffull;
+}
+
 __device__ void lu_solve_block(double *A, int lda, int off, int n, int *ipiv, double *x) {
 #define AC(r, c) A[(size_t)(off + (c)) * lda + (off + (r))]
-    __shared__ int nnz;
-    __shared__ int nzr[512];
+    __shared__ int nnz, nnc;
+    __shared__ int nzr[512], nzc[512];
     __shared__ int lim[512];
+    __shared__ double xs[512];
     if (threadIdx.x < 32) {
         const int lane = threadIdx.x;
         for (int k = 0; k < n; ++k) {
-            double best = 0.0;
+            unsigned long long best = 0;
             int p = n;
             for (int r = k + lane; r < n; r += 32) {
-                const double v = fabs(AC(r, k));
+                const unsigned long long v = mag_bits(AC(r, k));
                 if (p == n || v > best) { best = v; p = r; }
             }
             for (int o = 16; o > 0; o >>= 1) {
-                const double ob = __shfl_xor_sync(0xffffffffu, best, o);
+                const unsigned long long ob = __shfl_xor_sync(0xffffffffu, best, o);
                 const int op = __shfl_xor_sync(0xffffffffu, p, o);
                 if (op < n && (p == n || ob > best || (ob == best && op < p))) { best = ob; p = op; }
             }
             if (lane == 0) ipiv[k] = p + 1;
-            if (AC(p, k) == 0.0) continue;  // same value on every lane
+            if (is_zero(AC(p, k))) continue;  // same value on every lane
             __syncwarp();
             if (p != k)
                 for (int c = lane; c < n; c += 32) {
@@ -131,61 +141,67 @@ __device__ void lu_solve_block(double *A, int lda, int off, int n, int *ipiv, do
                     AC(k, c) = AC(p, c);
                     AC(p, c) = t;
                 }
-            if (lane == 0) nnz = 0;
+            if (lane == 0) {
+                nnz = 0;
+                nnc = 0;
+            }
             __syncwarp();
             const double inv = 1.0 / AC(k, k);
             for (int r = k + 1 + lane; r < n; r += 32) {
                 const double m = AC(r, k) * inv;
                 AC(r, k) = m;
-                if (m != 0.0) nzr[atomicAdd(&nnz, 1)] = r;
+                if (!is_zero(m)) nzr[atomicAdd(&nnz, 1)] = r;
             }
+            for (int c = k + 1 + lane; c < n; c += 32)
+                if (!is_zero(AC(k, c))) nzc[atomicAdd(&nnc, 1)] = c;
             __syncwarp();
-            const int cnt = nnz;
-            for (int c = k + 1 + lane; c < n; c += 32) {
-                const double akc = AC(k, c);
-                if (akc == 0.0) continue;
-                for (int q = 0; q < cnt; ++q) {
-                    const int r = nzr[q];
-                    AC(r, c) -= AC(r, k) * akc;
-                }
+            // the rank-1 update over (row, column) pairs with a non-zero
+            // multiplier and a non-zero pivot-row entry, one pair per lane
+            const int cr = nnz, cc = nnc;
+            for (int t = lane; t < cr * cc; t += 32) {
+                const int r = nzr[t % cr], c = nzc[t / cr];
+                AC(r, c) -= AC(r, k) * AC(k, c);
             }
             __syncwarp();
         }
+        for (int r = lane; r < n; r += 32) xs[r] = x[r];
         // forward sums start at the first non-zero of each row's range
         for (int r = lane; r < n; r += 32) {
             int c = 0;
-            while (c < r && AC(c, r) == 0.0) ++c;
+            while (c < r && is_zero(AC(c, r))) ++c;
             lim[r] = c;
         }
         __syncwarp();
         if (lane == 0)
             for (int r = 0; r < n; ++r) {
-                double s = x[r];
+                double s = xs[r];
                 for (int c = lim[r]; c < r; ++c) {
                     const double v = AC(c, r);
-                    if (v != 0.0) s -= v * x[c];
+                    if (!is_zero(v)) s -= v * xs[c];
                 }
-                x[r] = s / AC(r, r);
+                xs[r] = s / AC(r, r);
             }
         __syncwarp();
         // backward sums end at the last non-zero
         for (int r = lane; r < n; r += 32) {
             int c = n - 1;
-            while (c > r && AC(c, r) == 0.0) --c;
+            while (c > r && is_zero(AC(c, r))) --c;
             lim[r] = c;
         }
         __syncwarp();
         if (lane == 0) {
             for (int r = n - 1; r >= 0; --r) {
-                double s = x[r];
+                double s = xs[r];
                 for (int c = r + 1; c <= lim[r]; ++c) {
                     const double v = AC(c, r);
-                    if (v != 0.0) s -= v * x[c];
+                    if (!is_zero(v)) s -= v * xs[c];
                 }
-                x[r] = s;
+                xs[r] = s;
             }
-            for (int k = n - 1; k >= 0; --k) { const int p = ipiv[k] - 1; if (p != k) { const double t = x[k]; x[k] = x[p]; x[p] = t; } }
+            for (int k = n - 1; k >= 0; --k) { const int p = ipiv[k] - 1; if (p != k) { const double t = xs[k]; xs[k] = xs[p]; xs[p] = t; } }
         }
+        __syncwarp();
+        for (int r = lane; r < n; r += 32) x[r] = xs[r];
     }
     __syncthreads();
 #undef AC
@@ -206,9 +222,14 @@ __device__ void element_matrices(const FemKernelArgs &a, int f, int e) {
     const double M1 = (2 * EE * I / L0) * (2.0 * t1 + t2);
     const double M2 = (2 * EE * I / L0) * (t1 + 2.0 * t2);
     double F[6] = {-F0, (1.0 / L0) * (M1 + M2), M1, F0, -(1.0 / L0) * (M1 + M2), M2};
-    for (int i = 0; i < 6; ++i) a.elF[6 * ge + i] = F[i];
     double T[6][6];
     Tmat(ang, T);
+    // internal force in global coordinates, T^T F (the assembly's product)
+    for (int i = 0; i < 6; ++i) {
+        double fg = 0.0;
+        for (int c = 0; c < 6; ++c) fg += T[c][i] * F[c];
+        a.elF[6 * ge + i] = fg;
+    }
     // mass
     double Ml[6][6] = {};
     const double C1 = a.rho[ge] * A * L0 / 420.0;
@@ -322,47 +343,53 @@ __global__ void k_fem_dynamic(FemKernelArgs a) {
     double res = 0.0;
     do {
         for (int e = threadIdx.x; e < ne; e += blockDim.x) element_matrices(a, f, e);
+        for (int q = threadIdx.x; q < nd * nd; q += blockDim.x) {
+            M[q] = 0.0;
+            K[q] = 0.0;
+        }
         __syncthreads();
-        // F, M, K assembly: each entry sums its elements in order starting from 0
+        // F, M, K assembly (assembleGlobalMat into zeroed arrays): an entry
+        // gets at most two element terms (adjacent elements share one node),
+        // and a sum of two terms does not depend on their order, so the
+        // element blocks are added even elements first, then odd ones
         for (int d = threadIdx.x; d < nd; d += blockDim.x) {
             double s = 0.0;
             for (int e = (d / 3 - 1 < 0 ? 0 : d / 3 - 1); e <= (d / 3 > ne - 1 ? ne - 1 : d / 3); ++e) {
                 const int i = d - 3 * e;
                 if (i < 0 || i > 5) continue;
-                double T[6][6];
-                Tmat(a.elang[e0 + e], T);
-                double fg = 0.0;
-                for (int c = 0; c < 6; ++c) fg += T[c][i] * a.elF[6 * (e0 + e) + c];
-                s += fg;
+                s += a.elF[6 * (e0 + e) + i];
             }
             a.Fv[d0 + d] = s;
         }
-        for (int q = threadIdx.x; q < nd * nd; q += blockDim.x) {
-            const int r = q / nd, c = q % nd;
-            double sm = 0.0, sk = 0.0;
-            const int lo = (r > c ? r : c) / 3 - 1, hi = (r < c ? r : c) / 3;
-            for (int e = (lo < 0 ? 0 : lo); e <= (hi > ne - 1 ? ne - 1 : hi); ++e) {
-                const int i = r - 3 * e, j = c - 3 * e;
-                if (i < 0 || i > 5 || j < 0 || j > 5) continue;
-                sm += a.elM[36 * (size_t)(e0 + e) + 6 * i + j];
-                sk += a.elK[36 * (size_t)(e0 + e) + 6 * i + j];
+        for (int pass = 0; pass < 2; ++pass) {
+            const int nb = (ne + 1 - pass) / 2;
+            for (int t = threadIdx.x; t < nb * 36; t += blockDim.x) {
+                const int e = 2 * (t / 36) + pass, ij = t % 36;
+                const size_t q = (size_t)(3 * e + ij / 6) * nd + (3 * e + ij % 6);
+                M[q] += a.elM[36 * (size_t)(e0 + e) + ij];
+                K[q] += a.elK[36 * (size_t)(e0 + e) + ij];
             }
-            M[(size_t)r * nd + c] = sm;
-            K[(size_t)r * nd + c] = sk;
+            __syncthreads();
         }
-        __syncthreads();
         // FEMBody::setNewmark (:264-293)
         for (int i = threadIdx.x; i < nd; i += blockDim.x)
             Meff[i] = a0 * (a.U_n[d0 + i] - a.U[d0 + i]) + a2 * a.Ud[d0 + i] + a3 * a.Udd[d0 + i];
         __syncthreads();
+        // M is zero outside the three node columns around row i's node
         for (int i = threadIdx.x; i < nd; i += blockDim.x) {
+            const int jlo = 3 * (i / 3) - 3 < 0 ? 0 : 3 * (i / 3) - 3;
+            const int jhi = 3 * (i / 3) + 6 > nd ? nd : 3 * (i / 3) + 6;
             double s = 0.0;
-            for (int j = 0; j < nd; ++j) s += M[(size_t)i * nd + j] * Meff[j];
+            for (int j = jlo; j < jhi; ++j) s += M[(size_t)i * nd + j] * Meff[j];
             MF[i] = s;
         }
         __syncthreads();
         for (int i = threadIdx.x; i < nd; i += blockDim.x) a.Fv[d0 + i] = a.R[d0 + i] - a.Fv[d0 + i] + MF[i];
-        for (int q = threadIdx.x; q < nd * nd; q += blockDim.x) K[q] += a0 * M[q];
+        for (int t = threadIdx.x; t < nd * 9; t += blockDim.x) {
+            const int i = t / 9, j = 3 * (i / 3) - 3 + t % 9;
+            if (j < 0 || j >= nd) continue;
+            K[(size_t)i * nd + j] += a0 * M[(size_t)i * nd + j];
+        }
         for (int i = threadIdx.x; i < nd; i += blockDim.x) a.delU[d0 + i] = a.Fv[d0 + i];
         __syncthreads();
         lu_solve_block(K, nd, bc, nd - bc, ipiv, a.delU + d0 + bc);
@@ -462,35 +489,46 @@ __global__ void k_flex_support(FemKernelArgs a) {
             continue;
         }
         const double nearp[3] = {a.hx[in], a.hy[jn], D == 3 ? a.hz[kn] : 0.0};
-        auto add = [&](int i, int j, int k, const double e[3]) {
+        // Per axis, the five candidate node coordinates around the near node
+        // (offsets -2..2), their cage and domain tests and their kernel
+        // values: every support's test and delta is a combination of these,
+        // evaluated with the same expressions as node by node.
+        double ec[3][5], ph[3][5];
+        bool cage[3][5], dom[3][5];
+        for (int d = 0; d < 3; ++d)
+            for (int o = 0; o < 5; ++o) {
+                const bool act = d < D;
+                const double e = act ? nearp[d] + (o - 2) * dh : nearp[d];
+                ec[d][o] = e;
+                cage[d][o] = !act || fabs(p[d] - e) / dh < 1.5;
+                dom[d][o] = !act || !(e < a.edges[2 * d] || e > a.edges[2 * d + 1]);
+                ph[d][o] = act ? delta_kernel_d((e - p[d]) / dh, 1.0) : 1.0;
+            }
+        auto add = [&](int i, int j, int k, int oi, int oj, int ok) {
             if (ns >= kFlexMaxSupp) { atomicExch(a.error, 2); return; }
             const int s = g * kFlexMaxSupp + ns;
             x.supp[s] = k + j * a.K_ + i * a.K_ * a.M_;
-            x.sx[s] = e[0]; x.sy[s] = e[1]; x.sz[s] = e[2];
-            double v = delta_kernel_d((e[0] - p[0]) / dh, 1.0) * delta_kernel_d((e[1] - p[1]) / dh, 1.0);
-            if (D == 3) v = v * delta_kernel_d((e[2] - p[2]) / dh, 1.0);
+            x.sx[s] = ec[0][oi]; x.sy[s] = ec[1][oj]; x.sz[s] = ec[2][ok];
+            double v = ph[0][oi] * ph[1][oj];
+            if (D == 3) v = v * ph[2][ok];
             x.delta[s] = v;
             ++ns;
         };
-        add(in, jn, kn, nearp);
+        add(in, jn, kn, 2, 2, 2);
         // the reference scans +-5 nodes; every cage node (< 1.5 dh from the
         // marker, which is < 1 dh from the near node) lies within +-2, met
         // in the same (i, j, k) order
-        for (int i = in - 2; i <= in + 2; i++)
-            for (int j = jn - 2; j <= jn + 2; j++)
-                for (int k = (D == 3 ? kn - 2 : 0); k <= (D == 3 ? kn + 2 : 0); k++) {
-                    double e[3] = {nearp[0] + (i - in) * dh, nearp[1] + (j - jn) * dh, nearp[2]};
-                    if (D == 3) e[2] = nearp[2] + (k - kn) * dh;
-                    const bool cage = (fabs(p[0] - e[0]) / dh < 1.5) && (fabs(p[1] - e[1]) / dh < 1.5) &&
-                                      (D == 2 || fabs(p[2] - e[2]) / dh < 1.5);
-                    const bool dom = !(e[0] < a.edges[0] || e[0] > a.edges[1] || e[1] < a.edges[2] || e[1] > a.edges[3] ||
-                                       (D == 3 && (e[2] < a.edges[4] || e[2] > a.edges[5])));
-                    if (cage && dom && (i != in || j != jn || (D == 3 && k != kn))) {
+        for (int oi = 0; oi < 5; oi++)
+            for (int oj = 0; oj < 5; oj++)
+                for (int ok = (D == 3 ? 0 : 2); ok <= (D == 3 ? 4 : 2); ok++) {
+                    const int i = in + oi - 2, j = jn + oj - 2, k = kn + ok - 2;
+                    if (cage[0][oi] && cage[1][oj] && cage[2][ok] && dom[0][oi] && dom[1][oj] && dom[2][ok] &&
+                        (oi != 2 || oj != 2 || ok != 2)) {
                         if (i < 0 || j < 0 || k < 0 || i >= a.N || j >= a.M_ || k >= a.K_) {
                             atomicExch(a.error, 1);
                             continue;
                         }
-                        add(i, j, k, e);
+                        add(i, j, k, oi, oj, ok);
                     }
                 }
         x.nsupp[g] = ns;
@@ -512,16 +550,38 @@ __global__ void k_flex_support(FemKernelArgs a) {
         x.ds[g] = ds;
     }
     __syncthreads();
-    double *A = a.epsA + (size_t)f * a.maxmk * a.maxmk;
+    extern __shared__ double flex_smem[];
+    double *A = a.eps_in_smem ? flex_smem : a.epsA + (size_t)f * a.maxmk * a.maxmk;
     for (int q = threadIdx.x; q < nmk * nmk; q += blockDim.x) {
         const int I = q / nmk, J = q % nmk;
         const int gI = mk0 + I, gJ = mk0 + J;
         double aij = 0.0;
-        for (int s = 0; s < x.nsupp[gI]; ++s) {
+        // markers more than 3 dh apart on an axis share no support node: every
+        // term is an exact zero and the entry stays +0
+        bool near = true;
+        for (int d = 0; d < D; ++d) near = near && fabs(x.pos[3 * gI + d] - x.pos[3 * gJ + d]) <= 3.01 * dh;
+        // I's support nodes take a few coordinates per axis: the kernel of J
+        // at each distinct coordinate is evaluated once and reused (the same
+        // expression on the same operands, so the same value)
+        double cv[3][6], fv[3][6];
+        int nc[3] = {0, 0, 0};
+        const double XJ[3] = {x.pos[3 * gJ + 0], x.pos[3 * gJ + 1], x.pos[3 * gJ + 2]};
+        auto phi_at = [&](int d, double v) -> double {
+            const long long b = __double_as_longlong(v);
+            for (int t = 0; t < nc[d]; ++t)
+                if (__double_as_longlong(cv[d][t]) == b) return fv[d][t];
+            const double r = delta_kernel_d((XJ[d] - v) / dh, 1.0);
+            if (nc[d] < 6) {
+                cv[d][nc[d]] = v;
+                fv[d][nc[d]] = r;
+                ++nc[d];
+            }
+            return r;
+        };
+        for (int s = 0; near && s < x.nsupp[gI]; ++s) {
             const int si = gI * kFlexMaxSupp + s;
-            double dJ = delta_kernel_d((x.pos[3 * gJ + 0] - x.sx[si]) / dh, 1.0) *
-                        delta_kernel_d((x.pos[3 * gJ + 1] - x.sy[si]) / dh, 1.0);
-            if (D == 3) dJ = dJ * delta_kernel_d((x.pos[3 * gJ + 2] - x.sz[si]) / dh, 1.0);
+            double dJ = phi_at(0, x.sx[si]) * phi_at(1, x.sy[si]);
+            if (D == 3) dJ = dJ * phi_at(2, x.sz[si]);
             aij += x.delta[si] * dJ * 1.0;
         }
         A[(size_t)I * nmk + J] = aij * x.ds[gJ];
@@ -713,7 +773,11 @@ static FemKernelArgs full_args(luma_gpu_grid *g) {
 // Supports/ds/epsilon of the filaments' markers (initialise and after FEM).
 int luma_fem_supports(luma_gpu_grid *g) {
     FemKernelArgs a = full_args(g);
-    k_flex_support<<<a.nfil, 128, 0, g->stream>>>(a);
+    const size_t eb = (size_t)a.maxmk * a.maxmk * sizeof(double);
+    a.eps_in_smem = eb <= kFemSmemMax &&
+                    cudaFuncSetAttribute(k_flex_support, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)eb) == cudaSuccess;
+    if (!a.eps_in_smem) cudaGetLastError();
+    k_flex_support<<<a.nfil, 128, a.eps_in_smem ? eb : 0, g->stream>>>(a);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return luma_set_error(LUMA_E_CUDA, "flex support: %s", cudaGetErrorString(e));
     return LUMA_OK;
