@@ -217,6 +217,16 @@ int luma_gpu_ibm_get_markers(luma_gpu_grid *grid, int body, double *out);
  * (src/ObjectManager_ops_io.cpp:65-128) before its physical scaling. */
 int luma_gpu_ibm_body_force(luma_gpu_grid *grid, int body, double force[3]);
 
+/* ---- bounce-back bodies ---------------------------------------------------- */
+/* Momentum-exchange force of the grid's solid sites (bounce-back bodies and,
+ * as in the reference, walls): ObjectManager::computeLiftDrag
+ * (src/ObjectManager.cpp:93-165), which the reference accumulates during a
+ * step under L_LD_OUT from the populations that step streams; here it is
+ * computed from the grid's current state (the populations the next step
+ * streams), in FP64, in lattice units.  Blocks until the result is on the
+ * host. */
+int luma_gpu_momex_force(luma_gpu_grid *grid, double force[3]);
+
 /* ---- discrete adjoint of the time-averaged drag ------------------------- */
 /* No counterpart in the reference (its objective is the drag that
  * io_writeLiftDrag writes, src/ObjectManager_ops_io.cpp:105-121).

@@ -60,6 +60,7 @@ def lib() -> C.CDLL:
         L.luma_gpu_adj_forward.argtypes = [vp, C.c_int, C.c_int, C.c_int, dp]
         L.luma_gpu_adj_backward.argtypes = [vp, C.c_double, dp, dp]
         L.luma_gpu_adj_memory.argtypes = [vp, C.POINTER(C.c_size_t)]
+        L.luma_gpu_momex_force.argtypes = [vp, dp]
         if L.luma_gpu_abi_version() != A.ABI_VERSION:
             raise RuntimeError("luma_gb300 library ABI version mismatch")
         _lib = L
@@ -168,6 +169,12 @@ class GpuGrid:
                                                int(clamped), density, E, dm, fsi_vel_scale, C.byref(idx)))
         self._nm = getattr(self, "_nm", []) + [int(math.floor(length / self.desc.dh)) + 1]
         return idx.value
+
+    def momex_force(self) -> np.ndarray:
+        """Momentum-exchange force of the solid sites (lattice units)."""
+        out = np.zeros(3)
+        check(self.L.luma_gpu_momex_force(self.h, A.dptr(out)))
+        return out
 
     # ---- discrete adjoint of the time-averaged drag ----
     def adj_forward(self, nsteps: int, checkpoint_every: int, body: int = 0) -> float:

@@ -734,6 +734,42 @@ int oracle_step(oracle_grid *root, int nsteps) {
 
 int oracle_get_time(const oracle_grid *g) { return g->t; }
 
+/* ObjectManager::computeLiftDrag for bounce-back bodies
+ * (src/ObjectManager.cpp:93-165): over every solid site in (i, j, k) order
+ * and every direction n, the fluid neighbour x_dest = x - c_opp(n) (no
+ * periodic wrap) adds 2 c_opp(n) f_opp(n)(x_dest), from the populations the
+ * next step streams (GridObj::f between steps). */
+void oracle_momex_force(const oracle_grid *g, double out[3]) {
+    const int N = g->d.N, M = g->d.M, K = g->d.K, Q = g->Q;
+    double fx = 0.0, fy = 0.0, fz = 0.0;
+    for (int i = 0; i < N; ++i)
+        for (int j = 0; j < M; ++j)
+            for (int k = 0; k < K; ++k) {
+                const int id = k + j * K + i * K * M;
+                if (g->typ[id] != LUMA_SITE_SOLID) continue;
+                for (int n = 0; n < Q; ++n) {
+                    const int no = g->opp[n];
+                    double cx = 0.0, cy = 0.0, cz = 0.0;
+                    const int xd = i - g->c[no][0], yd = j - g->c[no][1], zd = k - g->c[no][2];
+                    if (xd >= 0 && xd < N && yd >= 0 && yd < M && zd >= 0 && zd < K) {
+                        const int did = zd + yd * K + xd * K * M;
+                        if (g->typ[did] == LUMA_SITE_FLUID) {
+                            const double fv = g->f[no + (size_t)did * Q];
+                            cx = 2.0 * g->c[no][0] * fv;
+                            cy = 2.0 * g->c[no][1] * fv;
+                            cz = 2.0 * g->c[no][2] * fv;
+                        }
+                    }
+                    fx += cx;
+                    fy += cy;
+                    fz += cz;
+                }
+            }
+    out[0] = fx;
+    out[1] = fy;
+    out[2] = fz;
+}
+
 int oracle_set_threads(int n) {
 #ifdef _OPENMP
     if (n > 0) omp_set_num_threads(n);

@@ -68,6 +68,7 @@ def lib():
                                               C.c_double, C.c_double, C.c_double]
         L.oracle_fem_state.argtypes = [C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_int),
                                        C.POINTER(C.c_int), C.POINTER(C.c_double)]
+        L.oracle_momex_force.argtypes = [C.c_void_p, C.POINTER(C.c_double)]
         _lib = L
     return _lib
 
@@ -110,6 +111,12 @@ class OracleGrid:
         force = np.empty(self.n * d.dims)
         self.L.oracle_download_state(self.h, A.dptr(f), A.dptr(u), A.dptr(rho), A.dptr(force))
         return {"f": f, "u": u, "rho": rho, "force": force}
+
+    def momex_force(self) -> np.ndarray:
+        """Momentum-exchange force of the solid sites (computeLiftDrag)."""
+        out = np.zeros(3)
+        self.L.oracle_momex_force(self.h, A.dptr(out))
+        return out
 
     def equilibrium(self, u, rho):
         d = self.desc

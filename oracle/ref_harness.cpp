@@ -12,7 +12,11 @@
  *
  * Usage:
  *   luma_ref --out DIR --steps N [--dump-every K] [--init-u FILE] [--init-rho FILE]
- *            [--workdir DIR] [--markers FILE] [--drag-out FILE]
+ *            [--workdir DIR] [--markers FILE] [--drag-out FILE] [--momex-out FILE]
+ *
+ * With --momex-out (cases compiled with L_LD_OUT) FILE gets, per step s, the
+ * momentum-exchange force ObjectManager::computeLiftDrag accumulated over
+ * the solid sites during step s (from the populations before it).
  *
  * With --drag-out nothing is dumped; FILE gets the time average over the N
  * steps of body 0's lattice-unit drag and N.
@@ -187,7 +191,7 @@ static void reinit_equilibrium(GridObj *g) {
 }
 
 int main(int argc, char **argv) {
-    std::string out = ".", init_u, init_rho, workdir, markers, drag_out;
+    std::string out = ".", init_u, init_rho, workdir, markers, drag_out, momex_out;
     int steps = 0, dump_every = 0;
     for (int a = 1; a < argc; ++a) {
         std::string k = argv[a];
@@ -203,6 +207,7 @@ int main(int argc, char **argv) {
         else if (k == "--workdir") workdir = next();
         else if (k == "--markers") markers = next();
         else if (k == "--drag-out") drag_out = next();
+        else if (k == "--momex-out") momex_out = next();
         else { std::fprintf(stderr, "unknown argument %s\n", k.c_str()); return 2; }
     }
     mkdir(out.c_str(), 0755);
@@ -249,14 +254,32 @@ int main(int argc, char **argv) {
 #endif
     (void)om;
 
+#ifdef L_LD_OUT
+    // Momentum-exchange force of the solid sites of L0, reset every step
+    // (resetMomexBodyForces resets only the grid a bounce-back body was
+    // read onto).
+    FILE *mf = momex_out.empty() ? nullptr : std::fopen(momex_out.c_str(), "w");
+    if (mf) {
+        om->bbbOnGridLevel = 0;
+        om->bbbOnGridReg = 0;
+    }
+#endif
     if (drag_out.empty()) dump_all(grids, out, 0);
     double drag_sum = 0.0;
     auto t0 = std::chrono::steady_clock::now();
     for (int s = 1; s <= steps; ++s) {
         grids->LBM_multi_opt();
+#ifdef L_LD_OUT
+        if (mf)
+            std::fprintf(mf, "%d %.17g %.17g %.17g\n", s, om->bbbForceOnObjectX, om->bbbForceOnObjectY,
+                         om->bbbForceOnObjectZ);
+#endif
         if (!drag_out.empty()) drag_sum += body_drag();
         else if ((dump_every > 0 && s % dump_every == 0) || s == steps) dump_all(grids, out, s);
     }
+#ifdef L_LD_OUT
+    if (mf) std::fclose(mf);
+#endif
     if (!drag_out.empty()) {
         FILE *df = std::fopen(drag_out.c_str(), "w");
         std::fprintf(df, "%.17g %d\n", steps > 0 ? drag_sum / steps : 0.0, steps);

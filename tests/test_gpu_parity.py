@@ -238,3 +238,41 @@ def test_filament_3d_matches_oracle(split):
         assert np.all(gm[:, 2] == fil["start"][2])
         assert rel_l2(gm[:, 3:6], om[:, 3:6]) <= 1e-8, rel_l2(gm[:, 3:6], om[:, 3:6])
     assert np.max(np.abs(gm[:, 0] - fil["start"][0])) > 1e-3   # the filament bent
+
+
+@pytest.mark.parametrize("prec", [A.PREC_FP64, A.PREC_FP32_SHIFTED])
+def test_momentum_exchange_force(prec):
+    """Momentum exchange over the solid sites: the Poiseuille channel's walls
+    against the reference build's own L_LD_OUT force (tests/golden/
+    make_momex.py) after 0..300 steps, and a channel with a bounce-back block
+    against the oracle.  FP64: rel 1e-12 of the force magnitude; shifted
+    FP32: 1e-5."""
+    import json
+    import os
+    tol = 1e-12 if prec == A.PREC_FP64 else 1e-5
+    ref = json.load(open(os.path.join(os.path.dirname(__file__), "golden", "momex_d2q9.json")))
+    gg, _ = R.build_backend(ref["like"], make_gpu, prec)
+    for s in (1, 2, 50, 300):
+        gg[0].step(s - 1 - gg[0].t)
+        got, want = gg[0].momex_force(), np.array(ref["forces"][str(s)])
+        scale = max(np.max(np.abs(want)), 1e-3)
+        assert np.max(np.abs(got - want)) <= tol * scale, (s, got, want)
+    # a bounce-back block in the channel (solid sites labelled on the host)
+    from luma_gb300 import case as hc
+    l0 = R.level0("poiseuille_d2q9")
+    typ = l0.typ.reshape(l0.N, l0.M, l0.K).copy()
+    typ[60:70, 45:55, :] = A.SOLID
+    l0.typ = typ.reshape(-1)
+    u = l0.u.reshape(l0.N, l0.M, l0.K, -1).copy()
+    u[60:70, 45:55] = 0.0
+    l0.u = u.reshape(-1)
+    f0 = hc.equilibrium(2, 9, l0.rho, l0.u).reshape(-1)
+    g = gpu_grid(l0.desc(precision=prec))
+    o = O.OracleGrid(l0.desc())
+    for x in (g, o):
+        x.upload(f0, l0.u, l0.rho, None, 0)
+    g.step(400)
+    o.step(400)
+    got, want = g.momex_force(), o.momex_force()
+    assert abs(want[0]) > 1e-3
+    assert np.max(np.abs(got - want)) <= tol * np.max(np.abs(want)), (got, want)

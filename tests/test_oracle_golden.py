@@ -144,3 +144,16 @@ def test_oracle_fem_fsi_bit_exact_vs_reference(name):
         assert np.array_equal(mk[:, 0:2], rm[:, 2:4]), "marker positions"
         assert np.array_equal(mk[:, 3:5], rm[:, 5:7]), "marker forces"
         assert np.array_equal(mk[:, 6], rm[:, 8]), "epsilon"
+
+
+def test_oracle_momentum_exchange_bit_exact_vs_reference():
+    """computeLiftDrag over the solid sites (the Poiseuille channel's walls),
+    restated in the oracle: bit-exact with the reference build's force for
+    every step (the reference accumulates it during step s from the state
+    after step s-1)."""
+    ref = json.load(open(os.path.join(os.path.dirname(__file__), "golden", "momex_d2q9.json")))
+    oo, _ = R.build_backend(ref["like"], lambda d, p: O.OracleGrid(d, p))
+    for s in range(1, ref["steps"] + 1):
+        got = oo[0].momex_force()
+        assert got.tolist() == ref["forces"][str(s)], (s, got, ref["forces"][str(s)])
+        oo[0].step(1)
