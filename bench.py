@@ -169,6 +169,23 @@ def cpu_oracle_mlups(n: int, nz: int, steps: int, warmup: int, threads: int | No
     return l0.ncell * done / dt / 1e6, used, dt, done
 
 
+def max_over_ranks(x: float, dist=None, device=None) -> float:
+    """The largest of the ranks' values (the job's time is its slowest
+    rank's); x itself without a process group."""
+    if dist is None:
+        return x
+    import torch
+    t = torch.tensor([x], device=device, dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_mlups(world: int, sites_per_rank: int, steps: int, seconds: float) -> float:
+    """Whole-job throughput of `world` replicas that each update
+    sites_per_rank sites `steps` times, timed by the slowest rank."""
+    return world * sites_per_rank * steps / seconds / 1e6
+
+
 def run_reference(args, rank: int, world: int):
     if rank != 0:
         return 0
@@ -385,12 +402,8 @@ def run_ours(args, rank: int, world: int, local_rank: int):
             dist.barrier()
         torch.cuda.synchronize(dev)
 
-    def max_over_ranks(x: float) -> float:
-        if not dist:
-            return x
-        t = torch.tensor([x], device=dev, dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        return float(t.item())
+    def max_over_ranks_(x: float) -> float:
+        return max_over_ranks(x, dist, dev)
 
     def timed_steps(grid, steps, sampler=None):
         e0 = torch.cuda.Event(enable_timing=True)
@@ -415,8 +428,8 @@ def run_ours(args, rank: int, world: int, local_rank: int):
     time.sleep(0.3)
     sec32, t0, t1 = timed_steps(g32, K)
     sampler_summary = sampler.summary(t0, t1)
-    sec32 = max_over_ranks(sec32)
-    mlups32 = world * ncell * K / sec32 / 1e6
+    sec32 = max_over_ranks_(sec32)
+    mlups32 = replica_mlups(world, ncell, K, sec32)
     g32.synchronize()
 
     # ---- FP64 (the reference's arithmetic) on the same workload ----
@@ -427,8 +440,8 @@ def run_ours(args, rank: int, world: int, local_rank: int):
     g64.step(W)
     sec64, _, _ = timed_steps(g64, K64)
     sampler.stop()
-    sec64 = max_over_ranks(sec64)
-    mlups64 = world * ncell * K64 / sec64 / 1e6
+    sec64 = max_over_ranks_(sec64)
+    mlups64 = replica_mlups(world, ncell, K64, sec64)
     # accuracy at equal step counts: bring both to t = W + K
     g64.step(K - K64)
     g64.synchronize()
@@ -459,8 +472,8 @@ def run_ours(args, rank: int, world: int, local_rank: int):
     check(L.luma_gpu_step(C.c_void_p(g32.h), K))
     check(L.luma_gpu_download_state(C.c_void_p(g32.h), None, ptr(out_u), ptr(out_r), None))
     barrier()
-    sec_e2e = max_over_ranks(time.perf_counter() - t_e0)
-    e2e = world * ncell * K / sec_e2e / 1e6
+    sec_e2e = max_over_ranks_(time.perf_counter() - t_e0)
+    e2e = replica_mlups(world, ncell, K, sec_e2e)
     h2d = (f0.nbytes + l0.u.nbytes + l0.rho.nbytes) / K
     d2h = (out_u.numel() + out_r.numel()) * 8 / K
     g32.close()
