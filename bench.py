@@ -36,6 +36,11 @@ sys.path.insert(0, ROOT)
 METRIC = "D3Q19 MLUPS & %HBM roofline, FP32-shifted vs FP64 at stated error; adjoint cost"
 SIZE = 256
 TAU = 0.55
+# FP64 operations per lattice update of the D3Q19 in-place FP64 kernel
+# (dadd + dmul + 2 dfma SASS thread-instruction counters of one launch at
+# 128^3, divided by the sites); the FP64 path is bound by the FP64 pipe.
+FP64_FLOP_PER_LU_D3Q19 = 231
+FP64_NOMINAL_TFLOPS = 1.25
 U0 = 0.02
 NOISE = 1e-4
 
@@ -517,7 +522,11 @@ def run_ours(args, rank: int, world: int, local_rank: int):
             "fp64": {"value": round(mlups64, 2), "unit": "MLUPS", "steps": K64,
                      "ms_per_step": round(sec64 / K64 * 1e3, 4),
                      "hbm_gbs": round(bytes64 / (sec64 / K64) / 1e9, 1),
-                     "hbm_frac": round(bytes64 / (sec64 / K64) / 1e9 / peaks["hbm_gbs"], 4)},
+                     "hbm_frac": round(bytes64 / (sec64 / K64) / 1e9 / peaks["hbm_gbs"], 4),
+                     "fp64_tflops": round(mlups64 * 1e6 * FP64_FLOP_PER_LU_D3Q19 / 1e12, 3),
+                     "fp64_frac_of_nominal": round(mlups64 * 1e6 * FP64_FLOP_PER_LU_D3Q19 / 1e12 /
+                                                   FP64_NOMINAL_TFLOPS, 3),
+                     "bound": "FP64 pipe (231 FP64 FLOP per update, counted with ncu)"},
             "fp32_vs_fp64": {"speedup": round(mlups32 / mlups64, 3), "rel_l2_u": eu, "rel_l2_rho": er,
                              "after_steps": W + K, "fp64_mass": red64["mass"]},
             "cpu_baseline": cpu,
