@@ -410,6 +410,15 @@ def run_ours(args, rank: int, world: int, local_rank: int):
     def max_over_ranks_(x: float) -> float:
         return max_over_ranks(x, dist, dev)
 
+    def warm(grid, steps):
+        # the in-place kernel has four variants (two storage parities, with
+        # and without the macroscopic write, which the last step of a call
+        # does): two single-step calls after the rest reach all four, so no
+        # kernel is first loaded inside the timed region
+        grid.step(steps - 2)
+        grid.step(1)
+        grid.step(1)
+
     def timed_steps(grid, steps, sampler=None):
         e0 = torch.cuda.Event(enable_timing=True)
         e1 = torch.cuda.Event(enable_timing=True)
@@ -427,7 +436,7 @@ def run_ours(args, rank: int, world: int, local_rank: int):
     g32 = GpuGrid(l0.desc(precision=A.PREC_FP32_SHIFTED))
     g32.set_stream(stream.cuda_stream)
     g32.upload(f0, l0.u, l0.rho, None, 0)
-    g32.step(W)
+    warm(g32, W)
     sampler = ClockSampler(local_rank if "CUDA_VISIBLE_DEVICES" not in os.environ else 0)
     sampler.start()
     time.sleep(0.3)
@@ -442,7 +451,7 @@ def run_ours(args, rank: int, world: int, local_rank: int):
     g64 = GpuGrid(l0.desc(precision=A.PREC_FP64))
     g64.set_stream(stream.cuda_stream)
     g64.upload(f0, l0.u, l0.rho, None, 0)
-    g64.step(W)
+    warm(g64, W)
     sec64, _, _ = timed_steps(g64, K64)
     sampler.stop()
     sec64 = max_over_ranks_(sec64)
