@@ -330,6 +330,11 @@ int step_grid(luma_gpu_grid *g, int subcycle, bool write_macro) {
         return LUMA_OK;
     }
     StepArgs a = make_args(g, subcycle);
+    // Interior u and rho are read after the step (the caller's download or
+    // reduction after its last step), by the reset of a gravity force (the
+    // old rho) and by the regularised BCs' extrapolation; otherwise the
+    // step that follows recomputes them before any use.
+    a.macro_out = write_macro || (d.flags & (LUMA_FLAG_GRAVITY | LUMA_FLAG_REGULARISED)) ? 1 : 0;
     if (g->adj) luma_adj_redirect(g, a);
     if (g->ibm && g->ibm->has_bodies) {
         int rc = luma_ibm_reset_forces(g, a);

@@ -55,6 +55,7 @@ struct StepArgs {
     void *fNew;             // populations after the step (S*)
     void *fOut;             // where the split collision writes: fNew, or another buffer when fNew is kept
     const uint8_t *defer;   // IBM grids: per-site "collide in phase C" flag (null: phase C collides all)
+    int macro_out;          // interior sites store u and rho (0: nothing reads them before the next step)
     void *u, *rho;          // R*, SoA
     const void *force;      // R*, SoA force_xyz (null when no forcing)
     const double *ux_in, *uy_in, *uz_in;

@@ -148,7 +148,7 @@ __device__ __forceinline__ void stream_site(const StepArgs &a, const int8_t *wal
 // _LBM_macro_opt (:800-891): density and velocity of fluid-like sites from
 // the streamed populations, + 0.5*F when forcing; the 3D reference adds the
 // z half-force to x (:833) unless LUMA_FLAG_FIX_MACRO3D.
-template <int Q, class P>
+template <int Q, class P, bool STORE = true>
 __device__ __forceinline__ void macro_site(const StepArgs &a, int i, int j, int k, int id, int type,
                                            const typename P::R *fn, typename P::R &rho, typename P::R &drho,
                                            typename P::R &ux, typename P::R &uy, typename P::R &uz) {
@@ -186,10 +186,12 @@ __device__ __forceinline__ void macro_site(const StepArgs &a, int i, int j, int 
         ux = mx / rho;
         uy = my / rho;
         uz = D == 3 ? mz / rho : R(0);
-        str<P>(a.u, id, ux);
-        str<P>(a.u, n + id, uy);
-        if (D == 3) str<P>(a.u, 2 * n + id, uz);
-        str<P>(a.rho, id, rho);
+        if (STORE) {
+            str<P>(a.u, id, ux);
+            str<P>(a.u, n + id, uy);
+            if (D == 3) str<P>(a.u, 2 * n + id, uz);
+            str<P>(a.rho, id, rho);
+        }
     } else {
         rho = ldr<P>(a.rho, id);
         drho = rho - R(a.rho0);
@@ -445,7 +447,10 @@ __global__ void __launch_bounds__(128) k_interior(StepArgs a, const uint8_t *fas
     StepArgs b = a;
     if (a.ibm_split && !deferred) b.forcing = 0;  // zero force: exact same sums
     R rho, drho, ux, uy, uz;
-    macro_site<Q, P>(b, i, j, k, id, LUMA_SITE_FLUID, fn, rho, drho, ux, uy, uz);
+    // u and rho go to memory where something reads them later in the step
+    // or after it (macro_out) or the IBM pass needs them (deferred sites)
+    if (a.macro_out || deferred) macro_site<Q, P, true>(b, i, j, k, id, LUMA_SITE_FLUID, fn, rho, drho, ux, uy, uz);
+    else macro_site<Q, P, false>(b, i, j, k, id, LUMA_SITE_FLUID, fn, rho, drho, ux, uy, uz);
     if (deferred || (a.ibm_split && a.fOut != a.fNew)) {
 #pragma unroll
         for (int v = 0; v < Q; ++v) st<P>(a.fNew, (size_t)v * n + id, fn[v]);
