@@ -370,9 +370,153 @@ int step_grid(luma_gpu_grid *g, int subcycle, bool write_macro) {
     return LUMA_OK;
 }
 
+}  // namespace
+
+// ---- two steps of the tree as a CUDA graph ----------------------------------
+//
+// On grids of modest size a step is a handful of short kernels, and the host
+// launch gaps between them cost as much as the kernels.  luma_gpu_step then
+// runs pairs of steps as one CUDA graph: captured once (on a private stream,
+// then launched on the caller's), replayed while everything it baked in is
+// unchanged.  Two steps bring every grid's buffer and storage parity back,
+// so one graph serves every pair.  The signature below lists what a capture
+// bakes in (device pointers, parities, sizes, paths); any change recaptures.
+// Not used when a step carries host logic between its kernels (velocity
+// ramp: arguments change every step; moving bodies: the FSI loop reads a
+// residual on the host; a recorded adjoint), or while the caller's stream is
+// itself being captured.
+
+namespace luma {
+struct StepGraph {
+    cudaStream_t cap = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    std::vector<uintptr_t> sig;
+    bool broken = false;  // a capture failed: steps run one launch at a time
+};
+}  // namespace luma
+
+namespace {
+
+constexpr int kGraphMinSteps = 8;
+
+void tree_signature(const luma_gpu_grid *g, std::vector<uintptr_t> &s) {
+    auto P = [&](const void *p) { s.push_back((uintptr_t)p); };
+    auto V = [&](long long v) { s.push_back((uintptr_t)v); };
+    P(g); P(g->f[0]); P(g->f[1]); P(g->u); P(g->rho); P(g->force); P(g->typ); P(g->wall); P(g->reg); P(g->velu);
+    P(g->uxin); P(g->defer); P(g->defer_ids); P(g->fast); P(g->gen_ids); P(g->adj);
+    V(g->cur); V(g->aa_odd); V(g->bulk); V(g->fuse); V(g->ngen); V(g->ndefer); V(g->nreg); V(g->nvelu);
+    V(g->d.flags);
+    if (g->ibm) {
+        const IbmDevice &d = g->ibm->dev;
+        P(d.vel); P(d.eps); P(d.ds); P(d.area); P(d.F); P(d.irho); P(d.imom); P(d.moff); P(d.msite);
+        P(d.smarker); P(d.mdelta); P(d.usite); P(d.uoff); P(d.uref);
+        V(d.nm); V(d.nsup); V(d.nu); V(g->ibm->has_bodies); V(g->ibm->ready); V(g->ibm->has_flexible);
+    }
+    V((long long)g->kids.size());
+    for (const luma_gpu_grid *c : g->kids) tree_signature(c, s);
+}
+
+bool graph_safe(const luma_gpu_grid *g) {
+    if (g->d.velocity_ramp > 0.0 || g->adj || (g->ibm && g->ibm->has_flexible)) return false;
+    for (const luma_gpu_grid *c : g->kids)
+        if (!graph_safe(c)) return false;
+    return true;
+}
+
+void tree_stream(luma_gpu_grid *g, cudaStream_t s) {
+    g->stream = s;
+    for (luma_gpu_grid *c : g->kids) tree_stream(c, s);
+}
+
+void save_clocks(const luma_gpu_grid *g, std::vector<int> &v) {
+    v.push_back(g->t); v.push_back(g->cur); v.push_back(g->aa_odd);
+    for (const luma_gpu_grid *c : g->kids) save_clocks(c, v);
+}
+void restore_clocks(luma_gpu_grid *g, const std::vector<int> &v, size_t &i) {
+    g->t = v[i++]; g->cur = v[i++]; g->aa_odd = v[i++];
+    for (luma_gpu_grid *c : g->kids) restore_clocks(c, v, i);
+}
+// A replayed pair of root steps: every grid's counter advances by its own
+// steps (two per parent step on a child); parities are back where they were.
+void advance_t(luma_gpu_grid *g, int steps) {
+    g->t += steps;
+    for (luma_gpu_grid *c : g->kids) advance_t(c, 2 * steps);
+}
+
+void free_graph(luma_gpu_grid *g) {
+    if (!g->graph) return;
+    if (g->graph->exec) cudaGraphExecDestroy(g->graph->exec);
+    if (g->graph->cap) cudaStreamDestroy(g->graph->cap);
+    delete g->graph;
+    g->graph = nullptr;
+}
+
+int step_grid(luma_gpu_grid *g, int subcycle, bool write_macro);
+
+// Runs `pairs` pairs of root steps as graph launches; returns the pairs run
+// (0 when the tree cannot be captured: the caller steps directly).
+int run_step_pairs(luma_gpu_grid *root, int pairs, int *done) {
+    *done = 0;
+    if (pairs <= 0 || !graph_safe(root)) return LUMA_OK;
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(root->stream, &cs) != cudaSuccess || cs != cudaStreamCaptureStatusNone) {
+        cudaGetLastError();
+        return LUMA_OK;
+    }
+    if (!root->graph) root->graph = new StepGraph();
+    StepGraph &G = *root->graph;
+    if (G.broken) return LUMA_OK;
+    std::vector<uintptr_t> sig;
+    tree_signature(root, sig);
+    if (!G.exec || sig != G.sig) {
+        if (G.exec) cudaGraphExecDestroy(G.exec);
+        G.exec = nullptr;
+        if (!G.cap && cudaStreamCreateWithFlags(&G.cap, cudaStreamNonBlocking) != cudaSuccess) {
+            cudaGetLastError();
+            G.broken = true;
+            return LUMA_OK;
+        }
+        std::vector<int> clocks;
+        save_clocks(root, clocks);
+        const cudaStream_t user = root->stream;
+        tree_stream(root, G.cap);
+        int rc = LUMA_OK;
+        cudaGraph_t graph = nullptr;
+        if (cudaStreamBeginCapture(G.cap, cudaStreamCaptureModeThreadLocal) == cudaSuccess) {
+            rc = step_grid(root, 0, false);
+            if (rc == LUMA_OK) rc = step_grid(root, 0, false);
+            if (cudaStreamEndCapture(G.cap, &graph) != cudaSuccess) rc = LUMA_E_CUDA;
+        } else {
+            rc = LUMA_E_CUDA;
+        }
+        tree_stream(root, user);
+        if (rc == LUMA_OK && graph && cudaGraphInstantiate(&G.exec, graph, 0) != cudaSuccess) rc = LUMA_E_CUDA;
+        if (graph) cudaGraphDestroy(graph);
+        if (rc != LUMA_OK) {
+            // nothing ran: put the host-side clocks back and step directly
+            cudaGetLastError();
+            size_t i = 0;
+            restore_clocks(root, clocks, i);
+            G.exec = nullptr;
+            G.broken = true;
+            return LUMA_OK;
+        }
+        G.sig = sig;
+        // the capture advanced the host-side clocks by one pair: run it
+        CK(cudaGraphLaunch(G.exec, root->stream));
+        *done = 1;
+    }
+    for (; *done < pairs; ++*done) {
+        CK(cudaGraphLaunch(G.exec, root->stream));
+        advance_t(root, 2);
+    }
+    return LUMA_OK;
+}
+
 void free_grid(luma_gpu_grid *g) {
     if (!g) return;
     for (luma_gpu_grid *c : g->kids) free_grid(c);
+    free_graph(g);
     luma_ibm_free(g);
     luma_adj_free(g);
     cudaFree(g->typ);
@@ -645,6 +789,13 @@ int luma_gpu_step(luma_gpu_grid *root, int nsteps) {
     if (!root) return luma_set_error(LUMA_E_INVALID, "null grid");
     if (root->parent) return luma_set_error(LUMA_E_INVALID, "luma_gpu_step takes the level-0 grid");
     if (nsteps < 0) return luma_set_error(LUMA_E_INVALID, "negative step count");
+    if (nsteps >= kGraphMinSteps) {
+        // pairs as graph launches; the last step runs directly (it writes u, rho)
+        int done = 0;
+        const int rc = run_step_pairs(root, (nsteps - 1) / 2, &done);
+        if (rc) return rc;
+        nsteps -= 2 * done;
+    }
     for (int s = 0; s < nsteps; ++s) {
         int rc = step_grid(root, 0, s == nsteps - 1);
         if (rc) return rc;

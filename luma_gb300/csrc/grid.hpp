@@ -13,6 +13,7 @@
 namespace luma {
 struct IbmState;
 struct AdjState;
+struct StepGraph;
 }
 
 struct luma_gpu_grid;
@@ -53,6 +54,7 @@ struct luma_gpu_grid {
     cudaStream_t stream = nullptr;
     luma::IbmState *ibm = nullptr;
     luma::AdjState *adj = nullptr;   // discrete-adjoint tape (adjoint.cu)
+    luma::StepGraph *graph = nullptr;  // level 0: two steps of the tree as a CUDA graph (capi.cu)
     std::vector<double> hx, hy, hz;  // site positions (host copy, for IB support search)
 };
 
