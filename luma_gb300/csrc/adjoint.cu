@@ -63,8 +63,9 @@ struct AdjState {
     double *tape_Fm = nullptr;
     int tape_pos = 0;
     int *site_u = nullptr;  // per site: index of the distinct support site, or -1
-    void *lam[2] = {nullptr, nullptr};
-    void *lamg = nullptr, *lamF = nullptr;
+    void *lam = nullptr;                       // adjoint of f at segment boundaries
+    void *lamg[2] = {nullptr, nullptr};       // adjoint of the post-stream f, steps t and t-1
+    void *lamF = nullptr;
     double *mu = nullptr, *Gw = nullptr, *Gd = nullptr, *w = nullptr;
     size_t bytes = 0;
     // full K-step segments run as CUDA graphs captured once (K even)
@@ -78,7 +79,7 @@ struct AdjState {
 namespace {
 
 struct AdjArgs {
-    int N, M, K, ncell, nm, nu, body_base, body_nm;
+    int N, M, K, ncell, nm, nu, nsup, body_base, body_nm;
     int quirk;                 // 3D: F_z/2 enters u_x
     double omega, rho0, invT;
     const uint8_t *typ;
@@ -95,25 +96,16 @@ struct AdjArgs {
     double *mu, *Gw, *Gd, *gs;
 };
 
-// Reverse of macroscopic + forcing + collision at one site:
-// lam_g = d(lam'.f')/dg and lam_F = d(lam'.f')/dF.
+// Reverse of macroscopic + forcing + collision at fluid site id, given the
+// adjoint lam' of the collided populations (registers): writes
+// lam_g = d(lam'.f')/dg and lam_F = d(lam'.f')/dF of the site.
 template <int Q, class P>
-__global__ void __launch_bounds__(128) k_adj_collide(AdjArgs a) {
+__device__ __forceinline__ void adj_collide_at(const AdjArgs &a, int id, const typename P::R *lam, typename P::R *lg,
+                                               typename P::R *lF) {
     using L = Lattice<Q>;
     using R = typename P::R;
     constexpr int D = L::D;
-    const int id = blockIdx.x * blockDim.x + threadIdx.x;
-    if (id >= a.ncell) return;
     const size_t n = (size_t)a.ncell;
-    R *lg = static_cast<R *>(a.lamg);
-    R *lF = static_cast<R *>(a.lamF);
-    if (a.typ[id] != LUMA_SITE_FLUID) {
-        // collided values of other sites never reach a fluid site
-        for (int v = 0; v < Q; ++v) lg[(size_t)v * n + id] = R(0);
-        for (int d = 0; d < D; ++d) lF[(size_t)d * n + id] = R(0);
-        return;
-    }
-    const R *lam = static_cast<const R *>(a.lam_in);
     R rho = R(0), j[3] = {R(0), R(0), R(0)};
 #pragma unroll
     for (int v = 0; v < Q; ++v) {
@@ -150,7 +142,7 @@ __global__ void __launch_bounds__(128) k_adj_collide(AdjArgs a) {
             cu += R(L::c(v, d)) * u[d];
             Fc += R(L::c(v, d)) * F[d];
         }
-        const R lv = lam[(size_t)v * n + id];
+        const R lv = lam[v];
         arho += lv * om * w * (R(1) + R(3) * cu + R(4.5) * cu * cu - R(1.5) * usq);
         for (int d = 0; d < D; ++d) {
             const R c = R(L::c(v, d));
@@ -169,10 +161,39 @@ __global__ void __launch_bounds__(128) k_adj_collide(AdjArgs a) {
     if (D == 3) lF[2 * n + id] = aF[2] + (a.quirk ? au[0] : au[2]) * h;
 #pragma unroll
     for (int v = 0; v < Q; ++v) {
-        R s = (R(1) - om) * lam[(size_t)v * n + id] + lrho;
+        R s = (R(1) - om) * lam[v] + lrho;
         for (int d = 0; d < D; ++d) s += R(L::c(v, d)) * lj[d];
         lg[(size_t)v * n + id] = s;
     }
+}
+
+// Collided values of sites other than fluid ones never reach a fluid site.
+template <int Q, class P>
+__device__ __forceinline__ void adj_collide_zero(const AdjArgs &a, int id, typename P::R *lg, typename P::R *lF) {
+    using R = typename P::R;
+    const size_t n = (size_t)a.ncell;
+    for (int v = 0; v < Q; ++v) lg[(size_t)v * n + id] = R(0);
+    for (int d = 0; d < Lattice<Q>::D; ++d) lF[(size_t)d * n + id] = R(0);
+}
+
+// The reverse collision of a step from the adjoint in memory (lam_in).
+template <int Q, class P>
+__global__ void __launch_bounds__(128) k_adj_collide(AdjArgs a) {
+    using R = typename P::R;
+    const int id = blockIdx.x * blockDim.x + threadIdx.x;
+    if (id >= a.ncell) return;
+    R *lg = static_cast<R *>(a.lamg);
+    R *lF = static_cast<R *>(a.lamF);
+    if (a.typ[id] != LUMA_SITE_FLUID) {
+        adj_collide_zero<Q, P>(a, id, lg, lF);
+        return;
+    }
+    const size_t n = (size_t)a.ncell;
+    const R *lin = static_cast<const R *>(a.lam_in);
+    R lam[Q];
+#pragma unroll
+    for (int v = 0; v < Q; ++v) lam[v] = lin[(size_t)v * n + id];
+    adj_collide_at<Q, P>(a, id, lam, lg, lF);
 }
 
 // Density and momentum at a support site as the IBM interpolation saw them:
@@ -280,15 +301,83 @@ __global__ void k_adj_support(AdjArgs a) {
 }
 
 // Both IBM reverse passes in one block, for bodies small enough that one
-// block covers them: the block barrier orders the mu writes before the
-// support gathers read them.
+// block covers them, parallel over supports: the delta-weighted lam_F of
+// every support (shared memory), the per-marker sums in support order (the
+// same sums as adj_marker), then the per-support delta sensitivities and the
+// per-site gathers.  Block barriers order the phases.
 constexpr int kIbmBlock = 512;
 constexpr int kIbmBlockMaxMarkers = 4 * kIbmBlock;
+constexpr size_t kIbmBlockMaxSmem = 160 * 1024;
+
+// Density and momentum at a support site in the policy's arithmetic (the
+// FP32 path sums its shifted populations in FP32).
+template <int Q, class P>
+__device__ __forceinline__ void support_moments_r(const AdjArgs &a, int id, double &rho, double j[3]) {
+    using R = typename P::R;
+    constexpr int D = Lattice<Q>::D;
+    const size_t n = (size_t)a.ncell;
+    j[0] = j[1] = j[2] = 0.0;
+    if (a.typ[id] == LUMA_SITE_FLUID) {
+        R r = R(0), jr[3] = {R(0), R(0), R(0)};
+#pragma unroll
+        for (int v = 0; v < Q; ++v) {
+            const R gv = ld<P>(a.g, (size_t)v * n + id);
+            r += gv;
+            for (int d = 0; d < D; ++d) jr[d] += R(Lattice<Q>::c(v, d)) * gv;
+        }
+        rho = P::shifted ? double(r) + a.rho0 : double(r);
+        for (int d = 0; d < D; ++d) j[d] = double(jr[d]);
+    } else {
+        rho = double(static_cast<const R *>(a.rho_field)[id]);
+        for (int d = 0; d < D; ++d) j[d] = rho * double(static_cast<const R *>(a.u_field)[(size_t)d * n + id]);
+    }
+}
 
 template <int Q, class P>
 __global__ void __launch_bounds__(kIbmBlock) k_adj_ibm_block(AdjArgs a) {
-    for (int m = threadIdx.x; m < a.nm; m += blockDim.x) adj_marker<Q, P>(a, m);
+    using R = typename P::R;
+    constexpr int D = Lattice<Q>::D;
+    extern __shared__ double dlf[];  // 3 per support: delta * lam_F at its site
+    const size_t n = (size_t)a.ncell;
+    const R *lF = static_cast<const R *>(a.lamF);
+    for (int s = threadIdx.x; s < a.nsup; s += blockDim.x) {
+        const int id = a.msite[s];
+        const double dl = a.mdelta[s];
+        for (int d = 0; d < 3; ++d) dlf[3 * s + d] = d < D ? dl * double(lF[(size_t)d * n + id]) : 0.0;
+    }
     __syncthreads();
+    for (int m = threadIdx.x; m < a.nm; m += blockDim.x) {
+        const bool inbody = m >= a.body_base && m < a.body_base + a.body_nm;
+        double sl[3] = {0, 0, 0};
+        for (int s = a.moff[m]; s < a.moff[m + 1]; ++s)
+            for (int d = 0; d < D; ++d) sl[d] += dlf[3 * s + d];
+        const double wm = a.w[m];
+        const double *Fm = a.Fm + 3 * m;
+        double mu[3] = {0, 0, 0}, gw = 0.0;
+        for (int d = 0; d < D; ++d) {
+            mu[d] = -wm * sl[d];
+            gw -= Fm[d] * sl[d];
+        }
+        if (inbody) {
+            mu[0] += a.invT * wm;
+            gw += a.invT * Fm[0];
+        }
+        a.Gw[m] += gw;
+        for (int d = 0; d < 3; ++d) a.mu[3 * m + d] = mu[d];
+    }
+    __syncthreads();
+    for (int s = threadIdx.x; s < a.nsup; s += blockDim.x) {
+        const int m = a.smarker[s], id = a.msite[s];
+        const double wm = a.w[m], A2 = 2.0 * a.area[m];
+        const double *Fm = a.Fm + 3 * m;
+        double Vmu = 0.0;
+        for (int d = 0; d < D; ++d) Vmu += a.vel[3 * m + d] * a.mu[3 * m + d];
+        double rho, j[3];
+        support_moments_r<Q, P>(a, id, rho, j);
+        double t = -A2 * rho * Vmu;
+        for (int d = 0; d < D; ++d) t += A2 * a.mu[3 * m + d] * j[d] - wm * Fm[d] * double(lF[(size_t)d * n + id]);
+        a.Gd[s] += t;
+    }
     for (int u = threadIdx.x; u < a.nu; u += blockDim.x) adj_support<Q, P>(a, u);
 }
 
@@ -298,8 +387,11 @@ __device__ __forceinline__ bool pulls(int t) {
 
 // Reverse of the stream (the transpose of the pull, gathered per source
 // site) and the inlet-scale sensitivity of the forced-equilibrium inflow.
-template <int Q, class P>
-__global__ void __launch_bounds__(256) k_adj_stream(AdjArgs a) {
+// FUSE: the adjoint of the pre-stream populations of step t stays in
+// registers and feeds the reverse collision of step t-1 at the same site
+// (arguments b); otherwise it goes to a.lam_out.
+template <int Q, class P, bool FUSE>
+__global__ void __launch_bounds__(256) k_adj_stream(AdjArgs a, AdjArgs b) {
     using L = Lattice<Q>;
     using R = typename P::R;
     constexpr int D = L::D;
@@ -321,21 +413,23 @@ __global__ void __launch_bounds__(256) k_adj_stream(AdjArgs a) {
         const int yt = a.typ[id];
         const bool regular_source = yt == LUMA_SITE_FLUID;  // solid, velocity, extrapolate sources are replaced
         const bool extrap_source = i + 2 < N && a.typ[wrapid(i + 2, j, k)] == LUMA_SITE_EXTRAPOLATE_RIGHT;
+        R lam[Q];
 #pragma unroll
         for (int v = 0; v < Q; ++v) {
             const int cx = L::c(v, 0), cy = L::c(v, 1), cz = L::c(v, 2);
-            double s = 0.0;
+            R s = R(0);
             // x = y + c_v pulls f_v(y)
             const int xid = wrapid(i + cx, j + cy, k + cz);
-            if (regular_source && pulls(a.typ[xid])) s += double(lg[(size_t)v * n + xid]);
+            if (regular_source && pulls(a.typ[xid])) s += lg[(size_t)v * n + xid];
             // bounce-back at y: g_opp(v)(y) = f_v(y) when y + c_v is solid
-            if (pulls(yt) && a.typ[xid] == LUMA_SITE_SOLID) s += double(lg[(size_t)L::opp(v) * n + id]);
+            if (pulls(yt) && a.typ[xid] == LUMA_SITE_SOLID) s += lg[(size_t)L::opp(v) * n + id];
             // extrapolate-right: x pulls f_v(e - 2 e_x) from the outlet site e = y + 2 e_x
             if (extrap_source) {
                 const int x2 = wrapid(i + 2 + cx, j + cy, k + cz);
-                if (pulls(a.typ[x2])) s += double(lg[(size_t)v * n + x2]);
+                if (pulls(a.typ[x2])) s += lg[(size_t)v * n + x2];
             }
-            out[(size_t)v * n + id] = R(s);
+            if (FUSE) lam[v] = s;
+            else out[(size_t)v * n + id] = s;
             // inflow: y pulls feq_v(rho_e, s u_e) from the velocity site e = y - c_v
             if (yt == LUMA_SITE_FLUID) {
                 const int sid = wrapid(i - cx, j - cy, k - cz);
@@ -353,6 +447,12 @@ __global__ void __launch_bounds__(256) k_adj_stream(AdjArgs a) {
                     gs_local += double(lg[(size_t)v * n + id]) * dfeq;
                 }
             }
+        }
+        if (FUSE) {
+            R *lgb = static_cast<R *>(b.lamg);
+            R *lFb = static_cast<R *>(b.lamF);
+            if (yt == LUMA_SITE_FLUID) adj_collide_at<Q, P>(b, id, lam, lgb, lFb);
+            else adj_collide_zero<Q, P>(b, id, lgb, lFb);
         }
     }
     __shared__ double red[8];
@@ -401,7 +501,7 @@ void free_state(AdjState *st) {
     if (st->seg_fwd) cudaGraphExecDestroy(st->seg_fwd);
     if (st->seg_bwd) cudaGraphExecDestroy(st->seg_bwd);
     if (st->own) cudaStreamDestroy(st->own);
-    cudaFree(st->lam[0]); cudaFree(st->lam[1]); cudaFree(st->lamg); cudaFree(st->lamF); cudaFree(st->mu);
+    cudaFree(st->lam); cudaFree(st->lamg[0]); cudaFree(st->lamg[1]); cudaFree(st->lamF); cudaFree(st->mu);
     cudaFree(st->Gw); cudaFree(st->Gd); cudaFree(st->w); cudaFree(st->d_J); cudaFree(st->d_gs);
     delete st;
 }
@@ -429,11 +529,11 @@ int check_scope(const luma_gpu_grid *g, int body) {
     return LUMA_OK;
 }
 
-AdjArgs make_adj_args(luma_gpu_grid *g, AdjState &st, int slot, int lin) {
+AdjArgs make_adj_args(luma_gpu_grid *g, AdjState &st, int slot, int gbuf) {
     const IbmDevice &dv = g->ibm->dev;
     AdjArgs a;
     memset(&a, 0, sizeof a);
-    a.N = g->d.N; a.M = g->d.M; a.K = g->d.K; a.ncell = (int)g->n; a.nm = dv.nm; a.nu = dv.nu;
+    a.N = g->d.N; a.M = g->d.M; a.K = g->d.K; a.ncell = (int)g->n; a.nm = dv.nm; a.nu = dv.nu; a.nsup = dv.nsup;
     a.body_base = st.body_base; a.body_nm = st.body_nm;
     a.quirk = g->d.dims == 3 && !(g->d.flags & LUMA_FLAG_FIX_MACRO3D);
     a.omega = g->d.omega; a.rho0 = g->d.rho_in; a.invT = 1.0 / st.T;
@@ -442,9 +542,9 @@ AdjArgs make_adj_args(luma_gpu_grid *g, AdjState &st, int slot, int lin) {
     const size_t rs = rsize(g);
     a.g = static_cast<char *>(st.tape_g) + (size_t)slot * g->n * g->d.Q * rs;
     a.Fm = st.tape_Fm + (size_t)slot * 3 * dv.nm;
-    a.lam_in = st.lam[lin];
-    a.lam_out = st.lam[lin ^ 1];
-    a.lamg = st.lamg;
+    a.lam_in = st.lam;
+    a.lam_out = st.lam;
+    a.lamg = st.lamg[gbuf];
     a.lamF = st.lamF;
     a.rho_field = g->rho;
     a.u_field = g->u;
@@ -455,15 +555,27 @@ AdjArgs make_adj_args(luma_gpu_grid *g, AdjState &st, int slot, int lin) {
 }
 
 template <int Q, class P>
-cudaError_t launch_adj_step(const AdjArgs &a, cudaStream_t s) {
+cudaError_t launch_adj_collide(const AdjArgs &a, cudaStream_t s) {
     k_adj_collide<Q, P><<<(a.ncell + 127) / 128, 128, 0, s>>>(a);
-    if (a.nm > 0 && a.nm <= kIbmBlockMaxMarkers) {
-        k_adj_ibm_block<Q, P><<<1, kIbmBlock, 0, s>>>(a);
+    return cudaGetLastError();
+}
+
+// The reverse IBM pass and the reverse stream of step t (a); with a
+// previous step (b, prev) the reverse collision of step t-1 rides on the
+// reverse stream.
+template <int Q, class P>
+cudaError_t launch_adj_step(const AdjArgs &a, const AdjArgs &b, bool prev, cudaStream_t s) {
+    const size_t smem = (size_t)a.nsup * 3 * sizeof(double);
+    if (a.nm > 0 && a.nm <= kIbmBlockMaxMarkers && smem <= kIbmBlockMaxSmem) {
+        if (smem > 48 * 1024)
+            cudaFuncSetAttribute(k_adj_ibm_block<Q, P>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        k_adj_ibm_block<Q, P><<<1, kIbmBlock, smem, s>>>(a);
     } else if (a.nm > 0) {
         k_adj_marker<Q, P><<<(a.nm + 63) / 64, 64, 0, s>>>(a);
         k_adj_support<Q, P><<<(a.nu + 127) / 128, 128, 0, s>>>(a);
     }
-    k_adj_stream<Q, P><<<(a.ncell + 255) / 256, 256, 0, s>>>(a);
+    if (prev) k_adj_stream<Q, P, true><<<(a.ncell + 255) / 256, 256, 0, s>>>(a, b);
+    else k_adj_stream<Q, P, false><<<(a.ncell + 255) / 256, 256, 0, s>>>(a, b);
     return cudaGetLastError();
 }
 
@@ -804,8 +916,8 @@ int luma_gpu_adj_backward(luma_gpu_grid *g, double dJ, double *grad_inlet_scale,
     int rc;
     if (!st.tape_g) {
         if ((rc = dmalloc(&st.tape_g, (size_t)st.K * fbytes, st)) ||
-            (rc = dmalloc(&st.tape_Fm, (size_t)st.K * 3 * dv.nm * 8, st)) || (rc = dmalloc(&st.lam[0], fbytes, st)) ||
-            (rc = dmalloc(&st.lam[1], fbytes, st)) || (rc = dmalloc(&st.lamg, fbytes, st)) ||
+            (rc = dmalloc(&st.tape_Fm, (size_t)st.K * 3 * dv.nm * 8, st)) || (rc = dmalloc(&st.lam, fbytes, st)) ||
+            (rc = dmalloc(&st.lamg[0], fbytes, st)) || (rc = dmalloc(&st.lamg[1], fbytes, st)) ||
             (rc = dmalloc(&st.lamF, g->n * D * rs, st)) || (rc = dmalloc(&st.mu, 3 * (size_t)dv.nm * 8, st)) ||
             (rc = dmalloc(&st.Gw, (size_t)dv.nm * 8, st)) || (rc = dmalloc(&st.Gd, (size_t)dv.nsup * 8, st)))
             return rc;
@@ -819,27 +931,34 @@ int luma_gpu_adj_backward(luma_gpu_grid *g, double dJ, double *grad_inlet_scale,
     {
         OwnStream guard(g, st);
         cudaStream_t s = g->stream;
-        cudaMemsetAsync(st.lam[0], 0, fbytes, s);
+        cudaMemsetAsync(st.lam, 0, fbytes, s);
         cudaMemsetAsync(st.Gw, 0, (size_t)dv.nm * 8, s);
         cudaMemsetAsync(st.Gd, 0, (size_t)dv.nsup * 8, s);
         cudaMemsetAsync(st.d_gs, 0, 8, s);
-        int lin = 0;
-        // one segment: recompute with the tape on, then the reverse steps
+        // one segment: recompute with the tape on, then the reverse steps:
+        // the reverse collision of the last step from the adjoint in
+        // memory, then per step the reverse IBM pass and the reverse stream,
+        // which carries the reverse collision of the step before it; the
+        // segment's first step leaves the adjoint of its start in memory
         auto segment = [&](int steps) -> int {
             st.mode = 2;
             st.tape_pos = 0;
             int r = luma_gpu_step(g, steps);
             st.mode = 0;
             if (r) return r;
-            int l = lin;
-            for (int t = steps - 1; t >= 0; --t) {
-                const AdjArgs a = make_adj_args(g, st, t, l);
-                cudaError_t e = dispatch(Q, g->d.precision, [&](auto q, auto p) {
-                    return launch_adj_step<decltype(q)::value, decltype(p)>(a, s);
+            int gb = 0;
+            cudaError_t e = dispatch(Q, g->d.precision, [&](auto q, auto p) {
+                return launch_adj_collide<decltype(q)::value, decltype(p)>(make_adj_args(g, st, steps - 1, gb), s);
+            });
+            for (int t = steps - 1; t >= 0 && e == cudaSuccess; --t) {
+                const AdjArgs a = make_adj_args(g, st, t, gb);
+                const AdjArgs b = make_adj_args(g, st, t > 0 ? t - 1 : 0, gb ^ 1);
+                e = dispatch(Q, g->d.precision, [&](auto q, auto p) {
+                    return launch_adj_step<decltype(q)::value, decltype(p)>(a, b, t > 0, s);
                 });
-                if (e != cudaSuccess) return luma_set_error(LUMA_E_CUDA, "adjoint step: %s", cudaGetErrorString(e));
-                l ^= 1;
+                gb ^= 1;
             }
+            if (e != cudaSuccess) return luma_set_error(LUMA_E_CUDA, "adjoint step: %s", cudaGetErrorString(e));
             return LUMA_OK;
         };
         for (int k = st.nseg - 1; k >= 0; --k) {
@@ -851,7 +970,6 @@ int luma_gpu_adj_backward(luma_gpu_grid *g, double dJ, double *grad_inlet_scale,
             else
                 rc = segment(steps);
             if (rc) return rc;
-            lin ^= steps & 1;
         }
         cudaMemcpyAsync(Gw.data(), st.Gw, (size_t)dv.nm * 8, cudaMemcpyDeviceToHost, s);
         cudaMemcpyAsync(Gd.data(), st.Gd, (size_t)dv.nsup * 8, cudaMemcpyDeviceToHost, s);
