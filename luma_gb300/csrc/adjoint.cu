@@ -61,6 +61,7 @@ struct AdjState {
     int fin_cur = 0, fin_t = 0;
     void *tape_g = nullptr;
     double *tape_Fm = nullptr;
+    double *drag_terms = nullptr;  // per step of a forward segment: the body's F_x w per marker
     int tape_pos = 0;
     int *site_u = nullptr;  // per site: index of the distinct support site, or -1
     void *lam = nullptr;                       // adjoint of f at segment boundaries
@@ -466,18 +467,26 @@ __global__ void __launch_bounds__(256) k_adj_stream(AdjArgs a, AdjArgs b) {
     }
 }
 
-// J_t of the body, reduced in a fixed order by one block.
-__global__ void k_drag(const double *F, const double *w, int base, int nm, double invT, double *J) {
+// J over one forward segment: per step the body's drag terms (recorded by
+// the IBM interpolation), reduced in a fixed order by one block, scaled by
+// 1/T and added to J step after step.
+__global__ void k_drag_segment(const double *terms, int steps, int nm, double invT, double *J) {
     __shared__ double sh[256];
-    double s = 0.0;
-    for (int m = threadIdx.x; m < nm; m += blockDim.x) s += F[3 * (base + m)] * w[base + m];
-    sh[threadIdx.x] = s;
-    __syncthreads();
-    for (int o = blockDim.x / 2; o > 0; o >>= 1) {
-        if ((int)threadIdx.x < o) sh[threadIdx.x] += sh[threadIdx.x + o];
+    // J gains one term per step, in step order, whatever the segmentation
+    double acc = *J;
+    for (int t = 0; t < steps; ++t) {
+        double s = 0.0;
+        for (int m = threadIdx.x; m < nm; m += blockDim.x) s += terms[(size_t)t * nm + m];
+        sh[threadIdx.x] = s;
+        __syncthreads();
+        for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+            if ((int)threadIdx.x < o) sh[threadIdx.x] += sh[threadIdx.x + o];
+            __syncthreads();
+        }
+        if (threadIdx.x == 0) acc += sh[0] * invT;
         __syncthreads();
     }
-    if (threadIdx.x == 0) *J += sh[0] * invT;
+    if (threadIdx.x == 0) *J = acc;
 }
 
 template <class T>
@@ -497,7 +506,7 @@ void free_state(AdjState *st) {
     if (!st) return;
     for (void *p : st->ckpt) cudaFree(p);
     cudaFree(st->fin_f[0]); cudaFree(st->fin_f[1]); cudaFree(st->fin_u); cudaFree(st->fin_rho);
-    cudaFree(st->tape_g); cudaFree(st->tape_Fm); cudaFree(st->site_u);
+    cudaFree(st->tape_g); cudaFree(st->tape_Fm); cudaFree(st->site_u); cudaFree(st->drag_terms);
     if (st->seg_fwd) cudaGraphExecDestroy(st->seg_fwd);
     if (st->seg_bwd) cudaGraphExecDestroy(st->seg_bwd);
     if (st->own) cudaStreamDestroy(st->own);
@@ -726,15 +735,11 @@ int luma_adj_step_hook(luma_gpu_grid *g, const StepArgs &a) {
     AdjState &st = *g->adj;
     cudaStream_t s = g->stream;
     const IbmDevice &dv = g->ibm->dev;
-    if (st.mode == 1) {
-        k_drag<<<1, 256, 0, s>>>(dv.F, st.w, st.body_base, st.body_nm, 1.0 / st.T, st.d_J);
-    } else if (st.mode == 2) {
-        // the populations are on the tape already (luma_adj_redirect)
-        if (cudaMemcpyAsync(st.tape_Fm + (size_t)st.tape_pos * 3 * dv.nm, dv.F, 3 * dv.nm * sizeof(double),
-                            cudaMemcpyDeviceToDevice, s))
-            return luma_set_error(LUMA_E_CUDA, "adjoint: tape copy failed");
-        st.tape_pos++;
-    }
+    (void)a;
+    (void)s;
+    (void)dv;
+    // the step's records went where luma_adj_redirect pointed them
+    if (st.mode == 1 || st.mode == 2) st.tape_pos++;
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return luma_set_error(LUMA_E_CUDA, "adjoint hook: %s", cudaGetErrorString(e));
     return LUMA_OK;
@@ -743,10 +748,19 @@ int luma_adj_step_hook(luma_gpu_grid *g, const StepArgs &a) {
 // While taping, the step streams into the tape slot of the step and its
 // collision writes the next state to the usual buffer, so the post-stream
 // populations stay on the tape without a copy.
+// The forward's step records its body's drag terms for the segment's J
+// reduction; the taping step also records the marker forces.
 void luma_adj_redirect(luma_gpu_grid *g, StepArgs &a) {
     const AdjState &st = *g->adj;
-    if (st.mode != 2) return;
-    a.fNew = static_cast<char *>(st.tape_g) + (size_t)st.tape_pos * g->n * g->d.Q * rsize(g);
+    if (st.mode == 1) {
+        a.ibm_drag_out = st.drag_terms + (size_t)st.tape_pos * st.body_nm;
+        a.ibm_drag_w = st.w;
+        a.ibm_drag_base = st.body_base;
+        a.ibm_drag_nm = st.body_nm;
+    } else if (st.mode == 2) {
+        a.fNew = static_cast<char *>(st.tape_g) + (size_t)st.tape_pos * g->n * g->d.Q * rsize(g);
+        a.ibm_f_out = st.tape_Fm + (size_t)st.tape_pos * 3 * g->ibm->dev.nm;
+    }
 }
 
 void luma_adj_free(luma_gpu_grid *g) {
@@ -856,7 +870,8 @@ int luma_gpu_adj_forward(luma_gpu_grid *g, int nsteps, int checkpoint_every, int
     const size_t rs = rsize(g);
     const size_t fbytes = g->n * g->d.Q * rs;
     if ((rc = dmalloc(&st->w, w.size() * 8, *st)) || (rc = dmalloc(&st->d_J, 8, *st)) ||
-        (rc = dmalloc(&st->d_gs, 8, *st)) || (rc = build_site_map(g, *st)))
+        (rc = dmalloc(&st->d_gs, 8, *st)) || (rc = build_site_map(g, *st)) ||
+        (rc = dmalloc(&st->drag_terms, (size_t)st->K * std::max(1, st->body_nm) * 8, *st)))
         return fail(rc);
     if (cudaMemcpy(st->w, w.data(), w.size() * 8, cudaMemcpyHostToDevice) != cudaSuccess)
         return fail(luma_set_error(LUMA_E_CUDA, "adjoint: weights upload"));
@@ -875,14 +890,24 @@ int luma_gpu_adj_forward(luma_gpu_grid *g, int nsteps, int checkpoint_every, int
         cudaMemsetAsync(st->d_J, 0, 8, s);
         st->t0 = g->t;
         st->mode = 1;
+        // one forward segment: its steps record the drag terms, one block
+        // folds them into J
+        auto segment = [&](int steps) -> int {
+            st->tape_pos = 0;
+            int r = luma_gpu_step(g, steps);
+            if (r) return r;
+            k_drag_segment<<<1, 256, 0, g->stream>>>(st->drag_terms, steps, st->body_nm, 1.0 / st->T, st->d_J);
+            const cudaError_t e = cudaGetLastError();
+            return e == cudaSuccess ? LUMA_OK : luma_set_error(LUMA_E_CUDA, "adjoint drag: %s", cudaGetErrorString(e));
+        };
         for (int k = 0; k < st->nseg; ++k) {
             if (cudaMemcpyAsync(st->ckpt[k], g->f[g->cur], fbytes, cudaMemcpyDeviceToDevice, s) != cudaSuccess)
                 return fail(luma_set_error(LUMA_E_CUDA, "adjoint: checkpoint copy failed"));
             const int steps = std::min(st->K, st->T - k * st->K);
             if (steps == st->K)
-                rc = run_graph(g, *st, &st->seg_fwd, [&] { return luma_gpu_step(g, steps); }, [&] { g->t += steps; });
+                rc = run_graph(g, *st, &st->seg_fwd, [&] { return segment(steps); }, [&] { g->t += steps; });
             else
-                rc = luma_gpu_step(g, steps);
+                rc = segment(steps);
             if (rc) {
                 st->mode = 0;
                 return fail(rc);

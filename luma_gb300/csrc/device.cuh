@@ -56,6 +56,11 @@ struct StepArgs {
     void *fOut;             // where the split collision writes: fNew, or another buffer when fNew is kept
     const uint8_t *defer;   // IBM grids: per-site "collide in phase C" flag (null: phase C collides all)
     int macro_out;          // interior sites store u and rho (0: nothing reads them before the next step)
+    // recording for the adjoint (null when off): the rigid markers' forces
+    // (3 per marker) and one body's per-marker drag terms F_x w of the step
+    double *ibm_f_out, *ibm_drag_out;
+    const double *ibm_drag_w;
+    int ibm_drag_base, ibm_drag_nm;
     void *u, *rho;          // R*, SoA
     const void *force;      // R*, SoA force_xyz (null when no forcing)
     const double *ux_in, *uy_in, *uz_in;

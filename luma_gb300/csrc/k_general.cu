@@ -704,6 +704,10 @@ __global__ void k_ibm_interp_force(StepArgs a, IbmArgs b) {
         b.imom[3 * m + d] = mom[d];
         b.F[3 * m + d] = 2.0 * (mom[d] - r * b.vel[3 * m + d]) / 1.0;
     }
+    if (a.ibm_f_out)
+        for (int d = 0; d < 3; ++d) a.ibm_f_out[3 * m + d] = b.F[3 * m + d];
+    if (a.ibm_drag_out && m >= a.ibm_drag_base && m < a.ibm_drag_base + a.ibm_drag_nm)
+        a.ibm_drag_out[m - a.ibm_drag_base] = b.F[3 * m] * a.ibm_drag_w[m];
 }
 
 // ibm_spread (:621-689) as a gather: one thread per distinct support site
