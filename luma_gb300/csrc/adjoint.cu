@@ -61,6 +61,7 @@ struct AdjState {
     int fin_cur = 0, fin_t = 0;
     void *tape_g = nullptr;
     double *tape_Fm = nullptr;
+    void *tape_Fs = nullptr;  // per step: the spread force at the distinct support sites (R)
     double *drag_terms = nullptr;  // per step of a forward segment: the body's F_x w per marker
     int tape_pos = 0;
     int *site_u = nullptr;  // per site: index of the distinct support site, or -1
@@ -72,6 +73,19 @@ struct AdjState {
     // full K-step segments run as CUDA graphs captured once (K even)
     cudaStream_t own = nullptr;
     cudaGraphExec_t seg_fwd = nullptr, seg_bwd = nullptr;
+    // the reverse IBM pass runs on `side`, beside the reverse stream of the
+    // sites whose gathers touch no support site (`near` marks the others,
+    // listed in near_ids, which follow once both are done)
+    cudaStream_t side = nullptr;
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+    uint8_t *near = nullptr;
+    int *near_ids = nullptr;
+    int nnear = 0;
+    // kept for the next forward of the same length, segments and body while
+    // the grid's launch signature and its support sites stay the same: the
+    // buffers and the captured segment graphs are reused
+    std::vector<uintptr_t> sig;
+    std::vector<int> usite_host;
     bool graphs = true;
 };
 
@@ -85,8 +99,12 @@ struct AdjArgs {
     double omega, rho0, invT;
     const uint8_t *typ;
     const int *site_u;         // per site: distinct support index or -1
+    const uint8_t *near;       // per site: its reverse stream reads a support site
+    const int *near_ids;       // the marked sites
+    int nnear;
     const void *g;             // taped post-stream populations (S)
     const double *Fm;          // taped marker forces (3 per marker)
+    const void *Fs;            // taped force at the distinct support sites (R, D x nu)
     const void *lam_in;        // adjoint of the post-collision f (R)
     void *lam_out;             // adjoint of the pre-stream f (R)
     void *lamg, *lamF;         // R scratch
@@ -116,18 +134,11 @@ __device__ __forceinline__ void adj_collide_at(const AdjArgs &a, int id, const t
     }
     if (P::shifted) rho += R(a.rho0);
     // the force field of the step: zero after the reset, the spread marker
-    // forces at support sites
+    // forces (taped) at support sites
     R F[3] = {R(0), R(0), R(0)};
     const int su = a.site_u[id];
-    if (su >= 0) {
-        double fs[3] = {0.0, 0.0, 0.0};
-        for (int q = a.uoff[su]; q < a.uoff[su + 1]; ++q) {
-            const int s = a.uref[q];
-            const int m = a.smarker[s];
-            for (int d = 0; d < D; ++d) fs[d] -= a.mdelta[s] * a.Fm[3 * m + d] * a.w[m];
-        }
-        for (int d = 0; d < D; ++d) F[d] = R(fs[d]);
-    }
+    if (su >= 0)
+        for (int d = 0; d < D; ++d) F[d] = static_cast<const R *>(a.Fs)[(size_t)d * a.nu + su];
     R u[3] = {R(0), R(0), R(0)};
     u[0] = (j[0] + R(0.5) * F[0] + (a.quirk ? R(0.5) * F[2] : R(0))) / rho;
     u[1] = (j[1] + R(0.5) * F[1]) / rho;
@@ -301,15 +312,6 @@ __global__ void k_adj_support(AdjArgs a) {
     if (u < a.nu) adj_support<Q, P>(a, u);
 }
 
-// Both IBM reverse passes in one block, for bodies small enough that one
-// block covers them, parallel over supports: the delta-weighted lam_F of
-// every support (shared memory), the per-marker sums in support order (the
-// same sums as adj_marker), then the per-support delta sensitivities and the
-// per-site gathers.  Block barriers order the phases.
-constexpr int kIbmBlock = 512;
-constexpr int kIbmBlockMaxMarkers = 4 * kIbmBlock;
-constexpr size_t kIbmBlockMaxSmem = 160 * 1024;
-
 // Density and momentum at a support site in the policy's arithmetic (the
 // FP32 path sums its shifted populations in FP32).
 template <int Q, class P>
@@ -334,52 +336,128 @@ __device__ __forceinline__ void support_moments_r(const AdjArgs &a, int id, doub
     }
 }
 
+// Both IBM reverse passes in one block, for bodies small enough that one
+// block covers them.  Everything the passes read is staged in shared memory
+// first, in one round of independent loads (the per-support lam_F, moments
+// and weights, the per-marker data, the support-site lists and the adjoint
+// at the support sites); then, separated by block barriers: the per-marker
+// sums in support order (as adj_marker), the per-support delta
+// sensitivities, and the per-site gathers in the forward's order (as
+// adj_support), which write the updated adjoint back.
+constexpr int kIbmBlock = 512;
+constexpr size_t kIbmBlockMaxSmem = 160 * 1024;
+
+size_t ibm_block_smem(int nsup, int nm, int nu, int Q, size_t rs) {
+    const size_t dbl = (size_t)nsup * 8 + (size_t)nm * 11;
+    const size_t ints = (size_t)nu + (nu + 1) + 2 * (size_t)nsup + (nm + 1);
+    return dbl * 8 + (size_t)nu * Q * rs + ints * 4;
+}
+
 template <int Q, class P>
 __global__ void __launch_bounds__(kIbmBlock) k_adj_ibm_block(AdjArgs a) {
     using R = typename P::R;
     constexpr int D = Lattice<Q>::D;
-    extern __shared__ double dlf[];  // 3 per support: delta * lam_F at its site
+    extern __shared__ double sm[];
+    const int ns = a.nsup, nm = a.nm, nu = a.nu;
+    double *dlf = sm;               // 3 per support: delta * lam_F at its site
+    double *qs = dlf + 3 * ns;      // 3 per support: 2 area (j - rho V) at its site
+    double *c0 = qs + 3 * ns;       // per support: G_delta so far - w F . lam_F
+    double *cs = c0 + ns;           // per support: 2 area delta
+    double *mu = cs + ns;           // 3 per marker: dJ/dF
+    double *mk = mu + 3 * nm;       // 8 per marker: V, w, F, G_w so far
+    R *lgo = reinterpret_cast<R *>(mk + 8 * nm);                 // Q per support site: lam_g before the pass
+    int *usid = reinterpret_cast<int *>(lgo + (size_t)Q * nu);  // support site, -1 unless fluid
+    int *uoff = usid + nu;
+    int *uref = uoff + nu + 1;
+    int *ms = uref + ns;            // marker of each support
+    int *moff = ms + ns;
     const size_t n = (size_t)a.ncell;
     const R *lF = static_cast<const R *>(a.lamF);
-    for (int s = threadIdx.x; s < a.nsup; s += blockDim.x) {
-        const int id = a.msite[s];
-        const double dl = a.mdelta[s];
-        for (int d = 0; d < 3; ++d) dlf[3 * s + d] = d < D ? dl * double(lF[(size_t)d * n + id]) : 0.0;
+    R *lg = static_cast<R *>(a.lamg);
+    for (int s = threadIdx.x; s < ns; s += blockDim.x) {
+        const int id = a.msite[s], m = a.smarker[s];
+        const double dl = a.mdelta[s], wm = a.w[m], A2 = 2.0 * a.area[m];
+        double rho, j[3];
+        support_moments_r<Q, P>(a, id, rho, j);
+        double c = a.Gd[s];
+        for (int d = 0; d < 3; ++d) {
+            const double l = d < D ? double(lF[(size_t)d * n + id]) : 0.0;
+            dlf[3 * s + d] = dl * l;
+            qs[3 * s + d] = d < D ? A2 * (j[d] - rho * a.vel[3 * m + d]) : 0.0;
+            if (d < D) c -= wm * a.Fm[3 * m + d] * l;
+        }
+        c0[s] = c;
+        cs[s] = A2 * dl;
+        ms[s] = m;
+        uref[s] = a.uref[s];
+    }
+    for (int m = threadIdx.x; m <= nm; m += blockDim.x) {
+        moff[m] = a.moff[m];
+        if (m == nm) continue;
+        for (int d = 0; d < 3; ++d) {
+            mk[8 * m + d] = a.vel[3 * m + d];
+            mk[8 * m + 4 + d] = a.Fm[3 * m + d];
+        }
+        mk[8 * m + 3] = a.w[m];
+        mk[8 * m + 7] = a.Gw[m];
+    }
+    for (int u = threadIdx.x; u <= nu; u += blockDim.x) {
+        uoff[u] = a.uoff[u];
+        if (u == nu) continue;
+        const int id = a.usite[u];
+        const bool fluid = a.typ[id] == LUMA_SITE_FLUID;
+        usid[u] = fluid ? id : -1;
+        if (fluid)
+#pragma unroll
+            for (int v = 0; v < Q; ++v) lgo[(size_t)v * nu + u] = lg[(size_t)v * n + id];
     }
     __syncthreads();
-    for (int m = threadIdx.x; m < a.nm; m += blockDim.x) {
+    for (int m = threadIdx.x; m < nm; m += blockDim.x) {
         const bool inbody = m >= a.body_base && m < a.body_base + a.body_nm;
         double sl[3] = {0, 0, 0};
-        for (int s = a.moff[m]; s < a.moff[m + 1]; ++s)
+        for (int s = moff[m]; s < moff[m + 1]; ++s)
             for (int d = 0; d < D; ++d) sl[d] += dlf[3 * s + d];
-        const double wm = a.w[m];
-        const double *Fm = a.Fm + 3 * m;
-        double mu[3] = {0, 0, 0}, gw = 0.0;
+        const double wm = mk[8 * m + 3];
+        const double *Fm = mk + 8 * m + 4;
+        double mv[3] = {0, 0, 0}, gw = 0.0;
         for (int d = 0; d < D; ++d) {
-            mu[d] = -wm * sl[d];
+            mv[d] = -wm * sl[d];
             gw -= Fm[d] * sl[d];
         }
         if (inbody) {
-            mu[0] += a.invT * wm;
+            mv[0] += a.invT * wm;
             gw += a.invT * Fm[0];
         }
-        a.Gw[m] += gw;
-        for (int d = 0; d < 3; ++d) a.mu[3 * m + d] = mu[d];
+        a.Gw[m] = mk[8 * m + 7] + gw;
+        for (int d = 0; d < 3; ++d) mu[3 * m + d] = mv[d];
     }
     __syncthreads();
-    for (int s = threadIdx.x; s < a.nsup; s += blockDim.x) {
-        const int m = a.smarker[s], id = a.msite[s];
-        const double wm = a.w[m], A2 = 2.0 * a.area[m];
-        const double *Fm = a.Fm + 3 * m;
-        double Vmu = 0.0;
-        for (int d = 0; d < D; ++d) Vmu += a.vel[3 * m + d] * a.mu[3 * m + d];
-        double rho, j[3];
-        support_moments_r<Q, P>(a, id, rho, j);
-        double t = -A2 * rho * Vmu;
-        for (int d = 0; d < D; ++d) t += A2 * a.mu[3 * m + d] * j[d] - wm * Fm[d] * double(lF[(size_t)d * n + id]);
-        a.Gd[s] += t;
+    for (int s = threadIdx.x; s < ns; s += blockDim.x) {
+        const int m = ms[s];
+        double t = c0[s];
+        for (int d = 0; d < D; ++d) t += mu[3 * m + d] * qs[3 * s + d];
+        a.Gd[s] = t;
     }
-    for (int u = threadIdx.x; u < a.nu; u += blockDim.x) adj_support<Q, P>(a, u);
+    for (int u = threadIdx.x; u < nu; u += blockDim.x) {
+        const int id = usid[u];
+        if (id < 0) continue;  // moments of other sites are constants
+        double lj[3] = {0, 0, 0}, lr = 0.0;
+        for (int q = uoff[u]; q < uoff[u + 1]; ++q) {
+            const int s = uref[q];
+            const int m = ms[s];
+            const double c = cs[s];
+            for (int d = 0; d < D; ++d) {
+                lj[d] += c * mu[3 * m + d];
+                lr -= c * mk[8 * m + d] * mu[3 * m + d];
+            }
+        }
+#pragma unroll
+        for (int v = 0; v < Q; ++v) {
+            double c = lr;
+            for (int d = 0; d < D; ++d) c += Lattice<Q>::c(v, d) * lj[d];
+            lg[(size_t)v * n + id] = lgo[(size_t)v * nu + u] + R(c);
+        }
+    }
 }
 
 __device__ __forceinline__ bool pulls(int t) {
@@ -391,15 +469,19 @@ __device__ __forceinline__ bool pulls(int t) {
 // FUSE: the adjoint of the pre-stream populations of step t stays in
 // registers and feeds the reverse collision of step t-1 at the same site
 // (arguments b); otherwise it goes to a.lam_out.
-template <int Q, class P, bool FUSE>
+// SEL: 0 every site, 1 the sites not marked near, 2 the near list.
+template <int Q, class P, bool FUSE, int SEL>
 __global__ void __launch_bounds__(256) k_adj_stream(AdjArgs a, AdjArgs b) {
     using L = Lattice<Q>;
     using R = typename P::R;
     constexpr int D = L::D;
-    const int id = blockIdx.x * blockDim.x + threadIdx.x;
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    int id = x;
+    if (SEL == 1 && id < a.ncell && a.near[id]) id = -1;
+    if (SEL == 2) id = x < a.nnear ? a.near_ids[x] : -1;
     const size_t n = (size_t)a.ncell;
     double gs_local = 0.0;
-    if (id < a.ncell) {
+    if (id >= 0 && id < a.ncell) {
         const int K = a.K, M = a.M, N = a.N;
         const int k = id % K, j = (id / K) % M, i = id / (K * M);
         const R *lg = static_cast<const R *>(a.lamg);
@@ -506,10 +588,14 @@ void free_state(AdjState *st) {
     if (!st) return;
     for (void *p : st->ckpt) cudaFree(p);
     cudaFree(st->fin_f[0]); cudaFree(st->fin_f[1]); cudaFree(st->fin_u); cudaFree(st->fin_rho);
-    cudaFree(st->tape_g); cudaFree(st->tape_Fm); cudaFree(st->site_u); cudaFree(st->drag_terms);
+    cudaFree(st->tape_g); cudaFree(st->tape_Fm); cudaFree(st->tape_Fs); cudaFree(st->site_u); cudaFree(st->drag_terms);
     if (st->seg_fwd) cudaGraphExecDestroy(st->seg_fwd);
     if (st->seg_bwd) cudaGraphExecDestroy(st->seg_bwd);
     if (st->own) cudaStreamDestroy(st->own);
+    if (st->side) cudaStreamDestroy(st->side);
+    if (st->ev_fork) cudaEventDestroy(st->ev_fork);
+    if (st->ev_join) cudaEventDestroy(st->ev_join);
+    cudaFree(st->near); cudaFree(st->near_ids);
     cudaFree(st->lam); cudaFree(st->lamg[0]); cudaFree(st->lamg[1]); cudaFree(st->lamF); cudaFree(st->mu);
     cudaFree(st->Gw); cudaFree(st->Gd); cudaFree(st->w); cudaFree(st->d_J); cudaFree(st->d_gs);
     delete st;
@@ -548,9 +634,13 @@ AdjArgs make_adj_args(luma_gpu_grid *g, AdjState &st, int slot, int gbuf) {
     a.omega = g->d.omega; a.rho0 = g->d.rho_in; a.invT = 1.0 / st.T;
     a.typ = g->typ;
     a.site_u = st.site_u;
+    a.near = st.near;
+    a.near_ids = st.near_ids;
+    a.nnear = st.nnear;
     const size_t rs = rsize(g);
     a.g = static_cast<char *>(st.tape_g) + (size_t)slot * g->n * g->d.Q * rs;
     a.Fm = st.tape_Fm + (size_t)slot * 3 * dv.nm;
+    a.Fs = static_cast<char *>(st.tape_Fs) + (size_t)slot * g->d.dims * dv.nu * rs;
     a.lam_in = st.lam;
     a.lam_out = st.lam;
     a.lamg = st.lamg[gbuf];
@@ -571,20 +661,35 @@ cudaError_t launch_adj_collide(const AdjArgs &a, cudaStream_t s) {
 
 // The reverse IBM pass and the reverse stream of step t (a); with a
 // previous step (b, prev) the reverse collision of step t-1 rides on the
-// reverse stream.
+// reverse stream.  With a near list, the one-block IBM pass runs on the side
+// stream while the sites away from the supports stream back; the near sites
+// follow once both are done (forked and joined by events, so the order holds
+// in a captured graph as in direct launches).
 template <int Q, class P>
-cudaError_t launch_adj_step(const AdjArgs &a, const AdjArgs &b, bool prev, cudaStream_t s) {
-    const size_t smem = (size_t)a.nsup * 3 * sizeof(double);
-    if (a.nm > 0 && a.nm <= kIbmBlockMaxMarkers && smem <= kIbmBlockMaxSmem) {
-        if (smem > 48 * 1024)
-            cudaFuncSetAttribute(k_adj_ibm_block<Q, P>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+cudaError_t launch_adj_step(const AdjArgs &a, const AdjArgs &b, bool prev, cudaStream_t s, const AdjState &st) {
+    const size_t smem = ibm_block_smem(a.nsup, a.nm, a.nu, Q, sizeof(typename P::R));
+    const bool block = a.nm > 0 && smem <= kIbmBlockMaxSmem;
+    if (block && smem > 48 * 1024)
+        cudaFuncSetAttribute(k_adj_ibm_block<Q, P>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    const unsigned grid = (unsigned)((a.ncell + 255) / 256);
+    if (block && prev && st.side && a.near_ids) {
+        if (cudaEventRecord(st.ev_fork, s) != cudaSuccess || cudaStreamWaitEvent(st.side, st.ev_fork, 0) != cudaSuccess)
+            return cudaGetLastError();
+        k_adj_ibm_block<Q, P><<<1, kIbmBlock, smem, st.side>>>(a);
+        if (cudaEventRecord(st.ev_join, st.side) != cudaSuccess) return cudaGetLastError();
+        k_adj_stream<Q, P, true, 1><<<grid, 256, 0, s>>>(a, b);
+        if (cudaStreamWaitEvent(s, st.ev_join, 0) != cudaSuccess) return cudaGetLastError();
+        if (a.nnear > 0) k_adj_stream<Q, P, true, 2><<<(a.nnear + 63) / 64, 64, 0, s>>>(a, b);
+        return cudaGetLastError();
+    }
+    if (block) {
         k_adj_ibm_block<Q, P><<<1, kIbmBlock, smem, s>>>(a);
     } else if (a.nm > 0) {
         k_adj_marker<Q, P><<<(a.nm + 63) / 64, 64, 0, s>>>(a);
         k_adj_support<Q, P><<<(a.nu + 127) / 128, 128, 0, s>>>(a);
     }
-    if (prev) k_adj_stream<Q, P, true><<<(a.ncell + 255) / 256, 256, 0, s>>>(a, b);
-    else k_adj_stream<Q, P, false><<<(a.ncell + 255) / 256, 256, 0, s>>>(a, b);
+    if (prev) k_adj_stream<Q, P, true, 0><<<grid, 256, 0, s>>>(a, b);
+    else k_adj_stream<Q, P, false, 0><<<grid, 256, 0, s>>>(a, b);
     return cudaGetLastError();
 }
 
@@ -760,6 +865,7 @@ void luma_adj_redirect(luma_gpu_grid *g, StepArgs &a) {
     } else if (st.mode == 2) {
         a.fNew = static_cast<char *>(st.tape_g) + (size_t)st.tape_pos * g->n * g->d.Q * rsize(g);
         a.ibm_f_out = st.tape_Fm + (size_t)st.tape_pos * 3 * g->ibm->dev.nm;
+        a.ibm_sf_out = static_cast<char *>(st.tape_Fs) + (size_t)st.tape_pos * g->d.dims * g->ibm->dev.nu * rsize(g);
     }
 }
 
@@ -821,16 +927,37 @@ int run_graph(luma_gpu_grid *g, AdjState &st, cudaGraphExec_t *exec, F &&fn, H &
 
 // Per-site index of the distinct support site (or -1), for the force-field
 // reconstruction in the reverse collide.
-int build_site_map(luma_gpu_grid *g, AdjState &st) {
+int build_site_map(luma_gpu_grid *g, AdjState &st, const std::vector<int> &usite) {
     const IbmDevice &dv = g->ibm->dev;
-    std::vector<int> usite(dv.nu), map(g->n, -1);
-    if (dv.nu && cudaMemcpy(usite.data(), dv.usite, dv.nu * sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess)
-        return luma_set_error(LUMA_E_CUDA, "adjoint: support sites");
+    std::vector<int> map(g->n, -1);
     for (int u = 0; u < dv.nu; ++u) map[usite[u]] = u;
     int rc = dmalloc(&st.site_u, g->n * sizeof(int), st);
     if (rc) return rc;
     if (cudaMemcpy(st.site_u, map.data(), g->n * sizeof(int), cudaMemcpyHostToDevice) != cudaSuccess)
         return luma_set_error(LUMA_E_CUDA, "adjoint: site map upload");
+    // Sites whose reverse stream reads the adjoint at a support site u: the
+    // pull sources u - c_v, u itself (bounce-back, inflow) and the
+    // extrapolate-right sources u - c_v - 2 e_x, periodic like the gathers.
+    const int N = g->d.N, M = g->d.M, K = g->d.K, D = g->d.dims;
+    std::vector<uint8_t> near(g->n, 0);
+    for (int u = 0; u < dv.nu; ++u) {
+        const int id = usite[u];
+        const int k = id % K, j = (id / K) % M, i = id / (K * M);
+        for (int di = -3; di <= 1; ++di)
+            for (int dj = -1; dj <= 1; ++dj)
+                for (int dk = (D == 3 ? -1 : 0); dk <= (D == 3 ? 1 : 0); ++dk) {
+                    const int x = ((i + di) % N + N) % N, y = ((j + dj) % M + M) % M, z = ((k + dk) % K + K) % K;
+                    near[(size_t)z + (size_t)y * K + (size_t)x * K * M] = 1;
+                }
+    }
+    std::vector<int> ids;
+    for (size_t id = 0; id < g->n; ++id)
+        if (near[id]) ids.push_back((int)id);
+    st.nnear = (int)ids.size();
+    if ((rc = dmalloc(&st.near, g->n, st)) || (rc = dmalloc(&st.near_ids, ids.size() * sizeof(int), st))) return rc;
+    if (cudaMemcpy(st.near, near.data(), g->n, cudaMemcpyHostToDevice) != cudaSuccess ||
+        (!ids.empty() && cudaMemcpy(st.near_ids, ids.data(), ids.size() * sizeof(int), cudaMemcpyHostToDevice) != cudaSuccess))
+        return luma_set_error(LUMA_E_CUDA, "adjoint: near-site upload");
     return LUMA_OK;
 }
 
@@ -843,17 +970,54 @@ int luma_gpu_adj_forward(luma_gpu_grid *g, int nsteps, int checkpoint_every, int
         return luma_set_error(LUMA_E_INVALID, "luma_gpu_adj_forward: null pointer or non-positive step counts");
     int rc = check_scope(g, body);
     if (rc) return rc;
-    luma_adj_free(g);
-    AdjState *st = new AdjState();
-    g->adj = st;
-    auto fail = [&](int code) { luma_adj_free(g); return code; };
-    if (cudaStreamCreateWithFlags(&st->own, cudaStreamNonBlocking) != cudaSuccess)
-        return fail(luma_set_error(LUMA_E_CUDA, "adjoint: stream creation failed"));
-    st->body = body;
-    st->T = nsteps;
-    st->K = std::min(checkpoint_every, nsteps);
-    st->nseg = (nsteps + st->K - 1) / st->K;
     const IbmState &ib = *g->ibm;
+    const IbmDevice &dv = ib.dev;
+    std::vector<int> usite(dv.nu);
+    if (dv.nu && cudaMemcpy(usite.data(), dv.usite, dv.nu * sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess)
+        return luma_set_error(LUMA_E_CUDA, "adjoint: support sites");
+    const int K = std::min(checkpoint_every, nsteps);
+    AdjState *st = g->adj;
+    bool reuse = false;
+    if (st && st->T == nsteps && st->K == K && st->body == body && st->usite_host == usite) {
+        std::vector<uintptr_t> sig;
+        luma_tree_signature(g, sig);
+        reuse = sig == st->sig;
+    }
+    auto fail = [&](int code) { luma_adj_free(g); return code; };
+    const size_t rs = rsize(g);
+    const size_t fbytes = g->n * g->d.Q * rs;
+    const size_t ub = g->n * g->d.dims * rs, rb = g->n * rs;
+    if (!reuse) {
+        luma_adj_free(g);
+        st = new AdjState();
+        g->adj = st;
+        if (cudaStreamCreateWithFlags(&st->own, cudaStreamNonBlocking) != cudaSuccess ||
+            cudaStreamCreateWithFlags(&st->side, cudaStreamNonBlocking) != cudaSuccess ||
+            cudaEventCreateWithFlags(&st->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
+            cudaEventCreateWithFlags(&st->ev_join, cudaEventDisableTiming) != cudaSuccess)
+            return fail(luma_set_error(LUMA_E_CUDA, "adjoint: stream creation failed"));
+        st->body = body;
+        st->T = nsteps;
+        st->K = K;
+        st->nseg = (nsteps + K - 1) / K;
+        st->usite_host = usite;
+        if ((rc = dmalloc(&st->w, (size_t)dv.nm * 8, *st)) || (rc = dmalloc(&st->d_J, 8, *st)) ||
+            (rc = dmalloc(&st->d_gs, 8, *st)) || (rc = build_site_map(g, *st, usite)))
+            return fail(rc);
+        int bnm = 0;
+        for (size_t b = 0; b < ib.bodies.size(); ++b)
+            if ((int)b == body) bnm = ib.bodies[b].nm;
+        if ((rc = dmalloc(&st->drag_terms, (size_t)K * std::max(1, bnm) * 8, *st))) return fail(rc);
+        st->ckpt.assign(st->nseg, nullptr);
+        for (int k = 0; k < st->nseg; ++k)
+            if ((rc = dmalloc(&st->ckpt[k], fbytes, *st))) return fail(rc);
+        if ((rc = dmalloc(&st->fin_f[0], fbytes, *st)) || (rc = dmalloc(&st->fin_f[1], fbytes, *st)) ||
+            (rc = dmalloc(&st->fin_u, ub, *st)) || (rc = dmalloc(&st->fin_rho, rb, *st)))
+            return fail(rc);
+        st->graphs = (K % 2) == 0;  // a graph replays a fixed buffer parity
+        luma_tree_signature(g, st->sig);
+    }
+    st->valid = false;
     std::vector<double> w;
     int base = 0, sbase = 0;
     for (size_t b = 0; b < ib.bodies.size(); ++b) {
@@ -867,22 +1031,8 @@ int luma_gpu_adj_forward(luma_gpu_grid *g, int nsteps, int checkpoint_every, int
         base += bd.nm;
         sbase += bd.off.back();
     }
-    const size_t rs = rsize(g);
-    const size_t fbytes = g->n * g->d.Q * rs;
-    if ((rc = dmalloc(&st->w, w.size() * 8, *st)) || (rc = dmalloc(&st->d_J, 8, *st)) ||
-        (rc = dmalloc(&st->d_gs, 8, *st)) || (rc = build_site_map(g, *st)) ||
-        (rc = dmalloc(&st->drag_terms, (size_t)st->K * std::max(1, st->body_nm) * 8, *st)))
-        return fail(rc);
     if (cudaMemcpy(st->w, w.data(), w.size() * 8, cudaMemcpyHostToDevice) != cudaSuccess)
         return fail(luma_set_error(LUMA_E_CUDA, "adjoint: weights upload"));
-    st->ckpt.assign(st->nseg, nullptr);
-    for (int k = 0; k < st->nseg; ++k)
-        if ((rc = dmalloc(&st->ckpt[k], fbytes, *st))) return fail(rc);
-    const size_t ub = g->n * g->d.dims * rs, rb = g->n * rs;
-    if ((rc = dmalloc(&st->fin_f[0], fbytes, *st)) || (rc = dmalloc(&st->fin_f[1], fbytes, *st)) ||
-        (rc = dmalloc(&st->fin_u, ub, *st)) || (rc = dmalloc(&st->fin_rho, rb, *st)))
-        return fail(rc);
-    st->graphs = (st->K % 2) == 0;  // a graph replays a fixed buffer parity
     double h = 0.0;
     {
         OwnStream guard(g, *st);
@@ -942,6 +1092,7 @@ int luma_gpu_adj_backward(luma_gpu_grid *g, double dJ, double *grad_inlet_scale,
     if (!st.tape_g) {
         if ((rc = dmalloc(&st.tape_g, (size_t)st.K * fbytes, st)) ||
             (rc = dmalloc(&st.tape_Fm, (size_t)st.K * 3 * dv.nm * 8, st)) || (rc = dmalloc(&st.lam, fbytes, st)) ||
+            (rc = dmalloc(&st.tape_Fs, (size_t)st.K * D * dv.nu * rs, st)) ||
             (rc = dmalloc(&st.lamg[0], fbytes, st)) || (rc = dmalloc(&st.lamg[1], fbytes, st)) ||
             (rc = dmalloc(&st.lamF, g->n * D * rs, st)) || (rc = dmalloc(&st.mu, 3 * (size_t)dv.nm * 8, st)) ||
             (rc = dmalloc(&st.Gw, (size_t)dv.nm * 8, st)) || (rc = dmalloc(&st.Gd, (size_t)dv.nsup * 8, st)))
@@ -979,7 +1130,7 @@ int luma_gpu_adj_backward(luma_gpu_grid *g, double dJ, double *grad_inlet_scale,
                 const AdjArgs a = make_adj_args(g, st, t, gb);
                 const AdjArgs b = make_adj_args(g, st, t > 0 ? t - 1 : 0, gb ^ 1);
                 e = dispatch(Q, g->d.precision, [&](auto q, auto p) {
-                    return launch_adj_step<decltype(q)::value, decltype(p)>(a, b, t > 0, s);
+                    return launch_adj_step<decltype(q)::value, decltype(p)>(a, b, t > 0, s, st);
                 });
                 gb ^= 1;
             }

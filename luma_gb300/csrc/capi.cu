@@ -541,6 +541,13 @@ void free_grid(luma_gpu_grid *g) {
 
 }  // namespace
 
+// The launch-relevant state of a grid tree (buffers, lists, counts, flags):
+// a graph captured under one signature replays correctly while it holds.
+void luma_tree_signature(const luma_gpu_grid *g, std::vector<uintptr_t> &sig) {
+    sig.clear();
+    tree_signature(g, sig);
+}
+
 extern "C" {
 
 int luma_gpu_abi_version(void) { return LUMA_GPU_ABI_VERSION; }

@@ -57,8 +57,11 @@ struct StepArgs {
     const uint8_t *defer;   // IBM grids: per-site "collide in phase C" flag (null: phase C collides all)
     int macro_out;          // interior sites store u and rho (0: nothing reads them before the next step)
     // recording for the adjoint (null when off): the rigid markers' forces
-    // (3 per marker) and one body's per-marker drag terms F_x w of the step
+    // (3 per marker), the spread force at the distinct support sites (R,
+    // component-major over the supports) and one body's per-marker drag
+    // terms F_x w of the step
     double *ibm_f_out, *ibm_drag_out;
+    void *ibm_sf_out;
     const double *ibm_drag_w;
     int ibm_drag_base, ibm_drag_nm;
     void *u, *rho;          // R*, SoA

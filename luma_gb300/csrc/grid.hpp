@@ -63,6 +63,7 @@ int luma_set_error(int code, const char *fmt, ...);
 // capi.cu
 int luma_update_defer(luma_gpu_grid *g);
 int luma_build_interior(luma_gpu_grid *g);
+void luma_tree_signature(const luma_gpu_grid *g, std::vector<uintptr_t> &sig);
 // ibm.cu
 int luma_ibm_reset_forces(luma_gpu_grid *g, const luma::StepArgs &a);
 int luma_ibm_apply(luma_gpu_grid *g, const luma::StepArgs &a);

@@ -730,6 +730,8 @@ __global__ void k_ibm_spread(StepArgs a, IbmArgs b) {
         for (int d = 0; d < D; ++d) f[d] -= b.mdelta[s] * b.F[3 * m + d] * volWidth * volDepth * b.ds[m];
     }
     for (int d = 0; d < D; ++d) str<P>(const_cast<void *>(a.force), (size_t)d * n + id, typename P::R(f[d]));
+    if (a.ibm_sf_out)
+        for (int d = 0; d < D; ++d) static_cast<typename P::R *>(a.ibm_sf_out)[(size_t)d * b.nu + u] = typename P::R(f[d]);
 }
 
 // ibm_updateMacroscopic (:696-766): the macroscopic step again at every

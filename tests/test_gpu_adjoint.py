@@ -119,6 +119,32 @@ def test_backward_restores_forward_state_and_runs_once(small):
         g.close()
 
 
+def test_repeated_gradient_on_one_grid(small, fp64):
+    """A second forward/backward of the same length on the same grid (state
+    and captured segment graphs kept) from the same initial state gives the
+    same J and gradients; a different length rebuilds the state."""
+    g, l0 = ADJ.make_grid(small, A.PREC_FP64)
+    _, f0, u, rho = ADJ.initial_state(small.defs)
+    force = l0.force_xyz.copy() if l0.force_xyz is not None else None
+    J0, gs0, gx0 = fp64
+    try:
+        for nsteps in (small.nsteps, small.nsteps, 2 * KCK):
+            g.upload(f0, u, rho, force, t=0)
+            J = g.adj_forward(nsteps, small.checkpoint_every, 0)
+            gs, gx = g.adj_backward(1.0)
+            if nsteps == small.nsteps:
+                assert J == J0
+                assert abs(gs - gs0) <= 1e-12 * abs(gs0)
+                assert np.max(np.abs(gx - gx0)) <= 1e-12 * np.max(np.abs(gx0))
+        short = ADJ.DragCase(small.defs, small.markers, 2 * KCK, small.checkpoint_every)
+        Js, gss, gxs = ADJ.drag_and_gradient(short, A.PREC_FP64)
+        assert J == Js
+        assert abs(gs - gss) <= 1e-12 * abs(gss)
+        assert np.max(np.abs(gx - gxs)) <= 1e-12 * np.max(np.abs(gxs))
+    finally:
+        g.close()
+
+
 def test_autograd_function_contract(small, fp64):
     torch = pytest.importorskip("torch")
     fn = ADJ.drag_function()
