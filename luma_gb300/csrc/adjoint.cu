@@ -115,11 +115,27 @@ struct AdjArgs {
     double *mu, *Gw, *Gd, *gs;
 };
 
-// Reverse of macroscopic + forcing + collision at fluid site id, given the
-// adjoint lam' of the collided populations (registers): writes
-// lam_g = d(lam'.f')/dg and lam_F = d(lam'.f')/dF of the site.
+// The taped populations of site id and the step's force there: zero after
+// the reset, the spread marker forces (taped) at support sites.
 template <int Q, class P>
-__device__ __forceinline__ void adj_collide_at(const AdjArgs &a, int id, const typename P::R *lam, typename P::R *lg,
+__device__ __forceinline__ void adj_collide_load(const AdjArgs &a, int id, typename P::R *gv, typename P::R *F) {
+    using R = typename P::R;
+    const size_t n = (size_t)a.ncell;
+#pragma unroll
+    for (int v = 0; v < Q; ++v) gv[v] = ld<P>(a.g, (size_t)v * n + id);
+    F[0] = F[1] = F[2] = R(0);
+    const int su = a.site_u[id];
+    if (su >= 0)
+        for (int d = 0; d < Lattice<Q>::D; ++d) F[d] = static_cast<const R *>(a.Fs)[(size_t)d * a.nu + su];
+}
+
+// Reverse of macroscopic + forcing + collision at fluid site id, given the
+// adjoint lam' of the collided populations, the taped populations gv and
+// the force F (registers): writes lam_g = d(lam'.f')/dg and
+// lam_F = d(lam'.f')/dF of the site.
+template <int Q, class P>
+__device__ __forceinline__ void adj_collide_at(const AdjArgs &a, int id, const typename P::R *lam,
+                                               const typename P::R *gv, const typename P::R *F, typename P::R *lg,
                                                typename P::R *lF) {
     using L = Lattice<Q>;
     using R = typename P::R;
@@ -128,17 +144,10 @@ __device__ __forceinline__ void adj_collide_at(const AdjArgs &a, int id, const t
     R rho = R(0), j[3] = {R(0), R(0), R(0)};
 #pragma unroll
     for (int v = 0; v < Q; ++v) {
-        const R gv = ld<P>(a.g, (size_t)v * n + id);
-        rho += gv;
-        for (int d = 0; d < D; ++d) j[d] += R(L::c(v, d)) * gv;
+        rho += gv[v];
+        for (int d = 0; d < D; ++d) j[d] += R(L::c(v, d)) * gv[v];
     }
     if (P::shifted) rho += R(a.rho0);
-    // the force field of the step: zero after the reset, the spread marker
-    // forces (taped) at support sites
-    R F[3] = {R(0), R(0), R(0)};
-    const int su = a.site_u[id];
-    if (su >= 0)
-        for (int d = 0; d < D; ++d) F[d] = static_cast<const R *>(a.Fs)[(size_t)d * a.nu + su];
     R u[3] = {R(0), R(0), R(0)};
     u[0] = (j[0] + R(0.5) * F[0] + (a.quirk ? R(0.5) * F[2] : R(0))) / rho;
     u[1] = (j[1] + R(0.5) * F[1]) / rho;
@@ -202,10 +211,11 @@ __global__ void __launch_bounds__(128) k_adj_collide(AdjArgs a) {
     }
     const size_t n = (size_t)a.ncell;
     const R *lin = static_cast<const R *>(a.lam_in);
-    R lam[Q];
+    R lam[Q], gv[Q], F[3];
 #pragma unroll
     for (int v = 0; v < Q; ++v) lam[v] = lin[(size_t)v * n + id];
-    adj_collide_at<Q, P>(a, id, lam, lg, lF);
+    adj_collide_load<Q, P>(a, id, gv, F);
+    adj_collide_at<Q, P>(a, id, lam, gv, F, lg, lF);
 }
 
 // Density and momentum at a support site as the IBM interpolation saw them:
@@ -494,6 +504,9 @@ __global__ void __launch_bounds__(256) k_adj_stream(AdjArgs a, AdjArgs b) {
             return z + y * K + x * K * M;
         };
         const int yt = a.typ[id];
+        // the reverse collision's inputs, loaded before the gathers
+        R gv[Q], F[3];
+        if (FUSE && yt == LUMA_SITE_FLUID) adj_collide_load<Q, P>(b, id, gv, F);
         const bool regular_source = yt == LUMA_SITE_FLUID;  // solid, velocity, extrapolate sources are replaced
         const bool extrap_source = i + 2 < N && a.typ[wrapid(i + 2, j, k)] == LUMA_SITE_EXTRAPOLATE_RIGHT;
         R lam[Q];
@@ -534,7 +547,7 @@ __global__ void __launch_bounds__(256) k_adj_stream(AdjArgs a, AdjArgs b) {
         if (FUSE) {
             R *lgb = static_cast<R *>(b.lamg);
             R *lFb = static_cast<R *>(b.lamF);
-            if (yt == LUMA_SITE_FLUID) adj_collide_at<Q, P>(b, id, lam, lgb, lFb);
+            if (yt == LUMA_SITE_FLUID) adj_collide_at<Q, P>(b, id, lam, gv, F, lgb, lFb);
             else adj_collide_zero<Q, P>(b, id, lgb, lFb);
         }
     }
