@@ -1,0 +1,205 @@
+"""Host set-up of BFL (Bouzidi-Firdaouss-Lallemand) bodies: the data the
+device stream needs, built the way the reference's BFLBody builds it.
+
+A BFL body is a set of markers, at most one looked up per lattice voxel.
+The device step reads, per site, the marker whose voxel the site is
+(``Body::getMarkerData``, LUMA ``inc/Body.h:581-614``: the first marker whose
+primary support voxel matches) and, per marker, the link distances
+``Q[v + Q*m]`` (``BFLBody::Q``; -1 where no wall cuts the link).
+
+``circle_body`` follows, for a 2D grid:
+  * the circle prefab ``Body(g, id, centre, radius)`` (``inc/Body.h:197-255``):
+    floor(2 pi r / dh) angles from ``GridUtils::linspace``, the first dropped;
+  * ``Marker`` voxels (``inc/Marker.h:66-95`` through
+    ``GridUtils::getEnclosingVoxel``, ``src/GridUtils.cpp:1630-1718``);
+  * ``BFLBody::initialise`` (``src/BFLBody.cpp:49-142``): eBFL labels, then
+    ``enforceSurfaceClosure`` (``:548-715``), then ``computeQ`` over the eBFL
+    sites in (i, j, k) order (2D overload, ``:412-515``).
+The geometry reader shifts the centre by the solid-wall thickness
+(``src/ObjectManager_ops_io.cpp:585-597``); ``circle_body`` takes the centre
+as written in the geometry file and applies that shift.
+"""
+from __future__ import annotations
+
+import math
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import _abi as A
+from .case import lattice
+
+L_PI = 3.14159265358979323846  # the reference's L_PI (inc/stdafx.h:114)
+
+
+@dataclass
+class BflBody:
+    typ: np.ndarray          # (N*M*K,) int32 site labels with eBFL sites
+    site_marker: np.ndarray  # (N*M*K,) int32, marker of the site's voxel or -1
+    q: np.ndarray            # (nm, Q) link distances, -1 for none
+    positions: np.ndarray    # (nm, 3)
+
+
+def _linspace(lo: float, hi: float, n: int) -> list:
+    n = max(n, 2)
+    spacing = (hi - lo) / float(n - 1)
+    return [lo + spacing * i for i in range(n)]
+
+
+def _vecnorm(v) -> float:
+    s = 0.0
+    for x in v:
+        s += x * x
+    return math.sqrt(s)
+
+
+def circle_body(level0, centre, radius: float) -> BflBody:
+    """A rigid 2D BFL circle on level 0 (reference ``CIRCLE_SPHERE BFL``)."""
+    lv = level0
+    d = lv.defs
+    if d.dims != 2:
+        raise ValueError("circle_body builds the 2D prefab")
+    N, M, K, dh = lv.N, lv.M, lv.K, lv.dh
+    Q = d.Q
+    c = [[int(x) for x in cv] for cv in lattice(d.dims, Q)[0]]
+    wt = lv.wall_thickness
+    shift = [wt[0] if d.walls[0] == A.SOLID else 0.0, wt[2] if d.walls[2] == A.SOLID else 0.0,
+             wt[4] if d.walls[4] == A.SOLID else 0.0]
+    cx, cy, cz = centre[0] + shift[0], centre[1] + shift[1], centre[2] + shift[2]
+    gx0, gy0 = lv.global_edges[0], lv.global_edges[2]
+    typ = lv.typ.reshape(N, M, K).copy()
+    xpos, ypos, zpos = lv.xpos, lv.ypos, lv.zpos
+
+    def voxel(x, y, z):
+        return (int(math.floor((x - gx0) / dh)), int(math.floor((y - gy0) / dh)), 0)
+
+    def off_grid(i, j, k):
+        return i >= N or i < 0 or j >= M or j < 0 or k >= K or k < 0
+
+    pos, supp = [], []
+
+    def add_marker(x, y, z):
+        v = voxel(x, y, z)
+        if off_grid(*v):
+            raise ValueError("BFL marker off the grid")
+        pos.append((x, y, z))
+        supp.append(v)
+
+    def marker_at(x, y, z):
+        v = voxel(x, y, z)
+        if off_grid(*v):
+            return -1
+        for m, s in enumerate(supp):
+            if s == v:
+                return m
+        return -1
+
+    n = int(math.floor(2.0 * L_PI * radius / dh))
+    theta = _linspace(0.0, 2.0 * L_PI - (2.0 * L_PI / float(n)), n)
+    for t in theta[1:]:
+        add_marker(cx + radius * math.cos(t), cy + radius * math.sin(t), cz)
+    for s in supp:
+        typ[s] = A.BFL
+
+    # enforceSurfaceClosure: a diagonal eBFL neighbour without an eBFL site
+    # connecting the two gets a marker at the mean of the projected points
+    # that fall outside eBFL voxels
+    npts = 20
+    m = 0
+    while m < len(pos):
+        for di in (-1, 1):
+            for dj in (-1, 1):
+                dk = 0
+                ni, nj, nk = supp[m][0] + di, supp[m][1] + dj, supp[m][2] + dk
+                if off_grid(ni, nj, nk) or typ[ni, nj, nk] != A.BFL:
+                    continue
+                found = False
+                for ic in range(2):
+                    for jc in range(2):
+                        for kc in range(2):
+                            is_, js, ks = di - ic * di, dj - jc * dj, dk - kc * dk
+                            if (is_, js, ks) == (di, dj, dk) or (is_, js, ks) == (0, 0, 0):
+                                continue
+                            a, b, e = supp[m][0] + is_, supp[m][1] + js, supp[m][2] + ks
+                            if not off_grid(a, b, e) and typ[a, b, e] == A.BFL:
+                                found = True
+                                break
+                        if found:
+                            break
+                    if found:
+                        break
+                if found:
+                    continue
+                start = pos[m]
+                other = pos[marker_at(xpos[ni], ypos[nj], zpos[nk])]
+                ln = (other[0] - start[0], other[1] - start[1], other[2] - start[2])
+                need, count = False, 0
+                av = [0.0, 0.0, 0.0]
+                while not need:
+                    npts *= 2
+                    sp = 1.0 / npts
+                    for p in range(npts + 1):
+                        px = start[0] + p * sp * ln[0]
+                        py = start[1] + p * sp * ln[1]
+                        pz = start[2] + p * sp * ln[2]
+                        vi, vj, vk = voxel(px, py, pz)
+                        if typ[vi, vj, vk] != A.BFL:
+                            if not need:
+                                need = True
+                                av = [px, py, pz]
+                            else:
+                                av = [(av[0] * count + px) / (count + 1), (av[1] * count + py) / (count + 1),
+                                      (av[2] * count + pz) / (count + 1)]
+                            count += 1
+                    if need:
+                        add_marker(av[0], av[1], av[2])
+                        typ[supp[-1]] = A.BFL
+        m += 1
+
+    # computeQ (2D): line-line intersections of each link of an eBFL site
+    # with the segments to its horizontal/vertical eBFL neighbours
+    nm = len(pos)
+    q = np.full(Q * nm, -1.0)
+    for i in range(N):
+        for j in range(M):
+            if typ[i, j, 0] != A.BFL:
+                continue
+            store = marker_at(xpos[i], ypos[j], zpos[0])
+            combo = []
+            for ii in range(i - 1, i + 2):
+                for jj in range(j - 1, j + 2):
+                    if 0 <= ii < N and 0 <= jj < M and (ii == i or jj == j) and not (ii == i and jj == j):
+                        mm = marker_at(xpos[ii], ypos[jj], zpos[0])
+                        if mm >= 0:
+                            combo.append((store, mm))
+            if not combo:
+                continue
+            q0 = pos[store]
+            for first, second in combo:
+                qps = pos[second]
+                p = (xpos[i], ypos[j], pos[first][2])
+                for vel in range(Q - 1):
+                    di_ = (i + c[vel][0] + N) % N
+                    dj_ = (j + c[vel][1] + M) % M
+                    ppr = (xpos[di_], ypos[dj_], pos[first][2])
+                    s1x, s1y = ppr[0] - p[0], ppr[1] - p[1]
+                    s2x, s2y = qps[0] - q0[0], qps[1] - q0[1]
+                    den = -s2x * s1y + s1x * s2y
+                    if den == 0.0:
+                        continue  # parallel: the reference's s and t are inf or nan
+                    s = (-s1y * (p[0] - q0[0]) + s1x * (p[1] - q0[1])) / den
+                    t = (s2x * (p[1] - q0[1]) - s2y * (p[0] - q0[0])) / den
+                    if s >= 0 and s <= 1 and t >= 0 and t <= 1:
+                        ix, iy = p[0] + t * s1x, p[1] + t * s1y
+                        wd = _vecnorm((ix - p[0], iy - p[1], p[2] - p[2])) / \
+                            _vecnorm((ppr[0] - p[0], ppr[1] - p[1], ppr[2] - p[2]))
+                        k = vel + Q * store
+                        if q[k] == -1:
+                            q[k] = np.finfo(np.float64).max
+                        if wd < q[k]:
+                            q[k] = wd
+    site_marker = np.full(N * M * K, -1, dtype=np.int32)
+    for i in range(N):
+        for j in range(M):
+            site_marker[j * K + i * K * M] = marker_at(xpos[i], ypos[j], zpos[0])
+    return BflBody(typ=typ.reshape(-1), site_marker=site_marker, q=q.reshape(nm, Q), positions=np.array(pos))

@@ -91,6 +91,11 @@ struct oracle_grid {
     int has_ibm_bodies, has_flexible_bodies;
     void (*ibm_hook)(oracle_grid *, void *); /* IBM pass (set by the IBM oracle) */
     void *ibm_ctx;
+    /* BFL body 0 (oracle_bfl_set): per site the marker of its voxel (-1),
+     * per marker Q[v + Q*m] and the momentum-exchange force of the step */
+    int *bfl_marker;
+    double *bfl_q, *bfl_force;
+    int bfl_nm;
 };
 
 static char g_err[512];
@@ -214,6 +219,56 @@ static int spec_reflect(oracle_grid *g, int i, int j, int k, int id, int v, int 
     return 0;
 }
 
+/* ---- GridObj::_LBM_applyBFL_opt, :1010-1113 ----
+ * Returns 1 when the link carries the BFL condition (fNew written or, at a
+ * grid-edge stencil, left as it was), 0 for the regular stream, -1 on a
+ * BFL-labelled site without a marker.  The stencil site of the near-wall
+ * branch is built from (i, j, k) itself (:1070-1071), so its interpolation
+ * reduces to f_opp(v) at the site. Momentum exchange as
+ * ObjectManager::computeLiftDrag(v, id, g, markerID) (src/ObjectManager.cpp:
+ * 176-189). */
+static int apply_bfl(oracle_grid *g, int id, int sid, int v, int i, int j, int k) {
+    const int Q = g->Q, N = g->d.N, M = g->d.M, K = g->d.K;
+    double q = -1.0;
+    int current = 1, marker = -1;
+    if (g->typ[id] == LUMA_SITE_BFL) {
+        marker = g->bfl_marker ? g->bfl_marker[id] : -1;
+        if (marker < 0) { set_err("BFL site without a BFL marker"); return -1; }
+        q = g->bfl_q[g->opp[v] + Q * marker];
+    }
+    if (q == -1.0) {
+        const int ms = g->bfl_marker ? g->bfl_marker[sid] : -1;
+        if (ms >= 0) {
+            current = 0;
+            marker = ms;
+            q = g->bfl_q[v + Q * ms];
+        }
+    }
+    if (q == -1.0) return 0;
+    const int vo = g->opp[v];
+    double *fn = &g->fNew[v + (size_t)id * Q];
+    const double fo = g->f[vo + (size_t)id * Q];
+    int contributes = 0;
+    if (current) {
+        const int si = i + g->c[v][0], sj = j + g->c[v][1], sk = k + g->c[v][2];
+        if (si >= 0 && si < N && sj >= 0 && sj < M && sk >= 0 && sk < K) {
+            const size_t stencil = (size_t)k + (size_t)j * K + (size_t)i * K * M;
+            *fn = (1 - 2 * q) * (g->f[vo + stencil * Q] - fo) + fo;
+            contributes = 1;
+        }
+    } else {
+        *fn = (1 - 2 * q) * ((g->f[v + (size_t)id * Q] - fo) / (2 - 2 * q)) + fo;
+        contributes = 1;
+    }
+    if (contributes && g->bfl_force) {
+        const double s = fo + *fn;
+        g->bfl_force[3 * marker + 0] += g->c[vo][0] * s;
+        g->bfl_force[3 * marker + 1] += g->c[vo][1] * s;
+        g->bfl_force[3 * marker + 2] += g->c[vo][2] * s;
+    }
+    return 1;
+}
+
 /* ---- _LBM_stream_opt, :206-297 ---- */
 static int stream_site(oracle_grid *g, int i, int j, int k, int id, int type, int subcycle) {
     const int N = g->d.N, M = g->d.M, K = g->d.K, Q = g->Q;
@@ -224,8 +279,9 @@ static int stream_site(oracle_grid *g, int i, int j, int k, int id, int type, in
         const int sid = sz + sy * K + sx * K * M;
         const int st = g->typ[sid];
         if (type == LUMA_SITE_BFL || st == LUMA_SITE_BFL) {
-            set_err("BFL bodies are outside the GPU path");
-            return -1;
+            const int r = apply_bfl(g, id, sid, v, i, j, k);
+            if (r < 0) return -1;
+            if (r) continue;
         }
         if (type == LUMA_SITE_SLIP) {
             int applied;
@@ -579,6 +635,7 @@ static int loop_is_local(const oracle_grid *g) {
     if (g->d.velocity_ramp > 0.0 && !(g->d.flags & LUMA_FLAG_REGULARISED)) return 0;
     if (g->d.flags & LUMA_FLAG_REGULARISED) return 0;
     if (g->nsub) return 0;
+    if (g->bfl_marker) return 0;  /* marker forces accumulate in site order */
     return 1;
 }
 
@@ -592,6 +649,7 @@ static int multi_opt(oracle_grid *g, int subcycle) {
     const int N = g->d.N, M = g->d.M, K = g->d.K;
     const int reg = (g->d.flags & LUMA_FLAG_REGULARISED) != 0;
     if (ibm && g->has_ibm_bodies) reset_forces(g);
+    if (g->bfl_force) memset(g->bfl_force, 0, sizeof(double) * 3 * (size_t)g->bfl_nm);
     int err = 0;
     const int par = loop_is_local(g);
 #pragma omp parallel for schedule(static) if (par) reduction(| : err)
@@ -686,7 +744,30 @@ void oracle_grid_destroy(oracle_grid *g) {
     free(g->ux_in); free(g->uy_in); free(g->uz_in);
     free(g->f); free(g->fNew); free(g->feq); free(g->force_i);
     free(g->u); free(g->u_n); free(g->force_xyz); free(g->rho);
+    free(g->bfl_marker); free(g->bfl_q); free(g->bfl_force);
     free(g);
+}
+
+/* BFL body 0 of the grid: site_marker[ncell] (Body::getMarkerData of each
+ * site's position, -1 for none) and q[Q * nm] (BFLBody::Q). */
+int oracle_bfl_set(oracle_grid *g, const int *site_marker, int nm, const double *q) {
+    const size_t n = (size_t)g->ncell;
+    for (size_t i = 0; i < n; ++i)
+        if (site_marker[i] < -1 || site_marker[i] >= nm) { set_err("BFL site marker out of range"); return -1; }
+    free(g->bfl_marker); free(g->bfl_q); free(g->bfl_force);
+    g->bfl_marker = (int *)malloc(sizeof(int) * n);
+    memcpy(g->bfl_marker, site_marker, sizeof(int) * n);
+    g->bfl_q = dup_d(q, (size_t)g->Q * nm);
+    g->bfl_force = dup_d(NULL, 3 * (size_t)nm);
+    g->bfl_nm = nm;
+    return 0;
+}
+
+/* Per-marker momentum-exchange force of the latest step (3 per marker). */
+int oracle_bfl_forces(const oracle_grid *g, double *out) {
+    if (!g->bfl_force) { set_err("no BFL body"); return -1; }
+    memcpy(out, g->bfl_force, sizeof(double) * 3 * (size_t)g->bfl_nm);
+    return 0;
 }
 
 /* Upload sets f, fNew and feq to the given populations, as LBM_initGrid

@@ -69,6 +69,8 @@ def lib():
         L.oracle_fem_state.argtypes = [C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_int),
                                        C.POINTER(C.c_int), C.POINTER(C.c_double)]
         L.oracle_momex_force.argtypes = [C.c_void_p, C.POINTER(C.c_double)]
+        L.oracle_bfl_set.argtypes = [C.c_void_p, C.POINTER(C.c_int), C.c_int, C.POINTER(C.c_double)]
+        L.oracle_bfl_forces.argtypes = [C.c_void_p, C.POINTER(C.c_double)]
         _lib = L
     return _lib
 
@@ -116,6 +118,22 @@ class OracleGrid:
         """Momentum-exchange force of the solid sites (computeLiftDrag)."""
         out = np.zeros(3)
         self.L.oracle_momex_force(self.h, A.dptr(out))
+        return out
+
+    def bfl_set(self, site_marker, q) -> None:
+        """BFL body 0: per-site marker of the site's voxel (-1 for none) and
+        the (nm, Q) link distances (-1: no wall on the link)."""
+        sm = np.ascontiguousarray(site_marker, dtype=np.int32)
+        q = np.ascontiguousarray(q, dtype=np.float64)
+        self._bfl_nm = int(q.shape[0])
+        if self.L.oracle_bfl_set(self.h, sm.ctypes.data_as(C.POINTER(C.c_int)), self._bfl_nm, A.dptr(q)):
+            raise RuntimeError(self.L.oracle_last_error().decode())
+
+    def bfl_forces(self) -> np.ndarray:
+        """(nm, 3) momentum-exchange force per BFL marker of the latest step."""
+        out = np.zeros((self._bfl_nm, 3))
+        if self.L.oracle_bfl_forces(self.h, A.dptr(out)):
+            raise RuntimeError(self.L.oracle_last_error().decode())
         return out
 
     def equilibrium(self, u, rho):

@@ -13,10 +13,19 @@
  * Usage:
  *   luma_ref --out DIR --steps N [--dump-every K] [--init-u FILE] [--init-rho FILE]
  *            [--workdir DIR] [--markers FILE] [--drag-out FILE] [--momex-out FILE]
+ *            [--bfl-out FILE] [--bfl-forces FILE]
  *
  * With --momex-out (cases compiled with L_LD_OUT) FILE gets, per step s, the
  * momentum-exchange force ObjectManager::computeLiftDrag accumulated over
  * the solid sites during step s (from the populations before it).
+ *
+ * With --bfl-out FILE gets BFL body 0 as the stream looks it up: its
+ * marker count and Q values (L_NUM_VELS per marker, BFLBody::Q) and, per L0
+ * site in id order, the marker Body::getMarkerData finds for the site's
+ * position (-1 for none).  With --bfl-forces (cases compiled with L_LD_OUT)
+ * FILE gets, per step s and marker m, the momentum-exchange force
+ * ObjectManager::computeLiftDrag(v, id, g, markerID) accumulated on the
+ * marker during step s.
  *
  * With --drag-out nothing is dumped; FILE gets the time average over the N
  * steps of body 0's lattice-unit drag and N.
@@ -182,6 +191,30 @@ static void inject_markers(ObjectManager *om, GridObj *root, const std::string &
 }
 #endif
 
+static void dump_bfl(GridObj *g, const std::string &path) {
+    ObjectManager *om = ObjectManager::getInstance();
+    FILE *fp = std::fopen(path.c_str(), "w");
+    if (om->pBody.empty()) {
+        std::fprintf(fp, "0 %d\n", L_NUM_VELS);
+        std::fclose(fp);
+        return;
+    }
+    BFLBody &b = om->pBody[0];
+    std::fprintf(fp, "%zu %d\n", b.markers.size(), L_NUM_VELS);
+    for (size_t m = 0; m < b.markers.size(); ++m) {
+        for (int v = 0; v < L_NUM_VELS; ++v) std::fprintf(fp, "%.17g ", b.Q[v + L_NUM_VELS * m]);
+        std::fprintf(fp, "\n");
+    }
+    for (int i = 0; i < g->N_lim; ++i)
+        for (int j = 0; j < g->M_lim; ++j)
+            for (int k = 0; k < g->K_lim; ++k) {
+                MarkerData *md = b.getMarkerData(g->XPos[i], g->YPos[j], g->ZPos[k]);
+                std::fprintf(fp, "%d\n", md->isValid() ? md->ID : -1);
+                delete md;
+            }
+    std::fclose(fp);
+}
+
 static void reinit_equilibrium(GridObj *g) {
     const int n = g->N_lim * g->M_lim * g->K_lim;
     for (int id = 0; id < n; ++id)
@@ -191,7 +224,7 @@ static void reinit_equilibrium(GridObj *g) {
 }
 
 int main(int argc, char **argv) {
-    std::string out = ".", init_u, init_rho, workdir, markers, drag_out, momex_out;
+    std::string out = ".", init_u, init_rho, workdir, markers, drag_out, momex_out, bfl_out, bfl_forces;
     int steps = 0, dump_every = 0;
     for (int a = 1; a < argc; ++a) {
         std::string k = argv[a];
@@ -208,6 +241,8 @@ int main(int argc, char **argv) {
         else if (k == "--markers") markers = next();
         else if (k == "--drag-out") drag_out = next();
         else if (k == "--momex-out") momex_out = next();
+        else if (k == "--bfl-out") bfl_out = next();
+        else if (k == "--bfl-forces") bfl_forces = next();
         else { std::fprintf(stderr, "unknown argument %s\n", k.c_str()); return 2; }
     }
     mkdir(out.c_str(), 0755);
@@ -253,6 +288,8 @@ int main(int argc, char **argv) {
     om->ibm_initialise();
 #endif
     (void)om;
+    if (!bfl_out.empty()) dump_bfl(grids, bfl_out);
+    FILE *bf = bfl_forces.empty() ? nullptr : std::fopen(bfl_forces.c_str(), "w");
 
 #ifdef L_LD_OUT
     // Momentum-exchange force of the solid sites of L0, reset every step
@@ -274,12 +311,18 @@ int main(int argc, char **argv) {
             std::fprintf(mf, "%d %.17g %.17g %.17g\n", s, om->bbbForceOnObjectX, om->bbbForceOnObjectY,
                          om->bbbForceOnObjectZ);
 #endif
+        if (bf && !om->pBody.empty())
+            for (size_t m = 0; m < om->pBody[0].markers.size(); ++m) {
+                const BFLMarker &mk = om->pBody[0].markers[m];
+                std::fprintf(bf, "%d %zu %.17g %.17g %.17g\n", s, m, mk.forceX, mk.forceY, mk.forceZ);
+            }
         if (!drag_out.empty()) drag_sum += body_drag();
         else if ((dump_every > 0 && s % dump_every == 0) || s == steps) dump_all(grids, out, s);
     }
 #ifdef L_LD_OUT
     if (mf) std::fclose(mf);
 #endif
+    if (bf) std::fclose(bf);
     if (!drag_out.empty()) {
         FILE *df = std::fopen(drag_out.c_str(), "w");
         std::fprintf(df, "%.17g %d\n", steps > 0 ? drag_sum / steps : 0.0, steps);

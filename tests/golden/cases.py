@@ -83,6 +83,12 @@ CASES = {
         filaments=[dict(start=(0.5, 0.0, 0.0), length=0.4, height=0.02, depth=0.0, angle_v=90.0,
                         nel=10, clamped=True, density=1000.0, E=1.0e8)],
         steps=(2, 30), store_f=(2,)),
+    # D2Q9 channel with a rigid BFL cylinder (the reference's circle prefab,
+    # labelled, closed and given link distances by its BFLBody set-up).
+    "bfl_cyl_d2q9": dict(
+        defs=Definitions(dims=2, resolution=50, timestep=1.0 / 1250.0, bx=2.0, by=1.0, re=100, ux0=1.0,
+                         walls=(V, X, S, S, F, F)),
+        bfl=dict(centre=(0.5, 0.5, 0.0), radius=0.16), steps=(10, 300), store_f=(10,)),
     # D2Q9 BGK-Smagorinsky channel.
     "smag_d2q9": dict(
         defs=Definitions(dims=2, resolution=32, timestep=1.0 / 320.0, bx=2.0, by=1.0, re=2000,
@@ -184,8 +190,13 @@ def write_marker_file(path: str, body_list) -> None:
 
 
 def geometry_config(name: str) -> str:
-    """input/geometry.config text for the case's filaments (reference format)."""
+    """input/geometry.config text for the case's filaments and BFL circle
+    (reference format)."""
     lines = []
+    bfl = CASES[name].get("bfl")
+    if bfl:
+        x, y, z = bfl["centre"]
+        lines.append("CIRCLE_SPHERE BFL 0 0 %r %r %r %r RIGID" % (x, y, z, bfl["radius"]))
     for fl in CASES[name].get("filaments", []):
         x, y, z = fl["start"]
         lines.append("FILAMENT_ARRAY IBM 0 0 1 %r %r %r 0.0 0.0 0.0 %r %r %r %r 0 FLEXIBLE %d %s %r %r" % (

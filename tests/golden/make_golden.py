@@ -64,11 +64,13 @@ def run_case(name: str, ref: str) -> str:
         upath = os.path.join(work, "init_u.bin")
         init["u"].astype(np.float64).tofile(upath)
         args += ["--init-u", upath]
-    if spec.get("filaments"):
+    if spec.get("filaments") or spec.get("bfl"):
         os.makedirs(os.path.join(work, "input"), exist_ok=True)
         with open(os.path.join(work, "input", "geometry.config"), "w") as fp:
             fp.write(CASES.geometry_config(name))
         args += ["--workdir", work]
+    if spec.get("bfl"):
+        args += ["--bfl-out", os.path.join(work, "bfl.txt"), "--bfl-forces", os.path.join(work, "bfl_forces.txt")]
     blist = CASES.bodies(name) or (["filament"] if spec.get("filaments") else [])
     if blist and not spec.get("filaments"):
         mpath = os.path.join(work, "markers.in")
@@ -127,6 +129,17 @@ def run_case(name: str, ref: str) -> str:
             out[f"markers_{s}"] = mk
         sup = np.loadtxt(os.path.join(work, "s0", "supports.txt"), ndmin=2)
         out["supports"] = sup
+    if spec.get("bfl"):
+        with open(os.path.join(work, "bfl.txt")) as fp:
+            lines = fp.read().split("\n")
+        nm, q = (int(x) for x in lines[0].split())
+        out["bfl_q"] = np.array([[float(x) for x in lines[1 + m].split()] for m in range(nm)]).reshape(nm, q)
+        out["bfl_site_marker"] = np.array([int(x) for x in lines[1 + nm:] if x.strip()], dtype=np.int32)
+        bf = np.loadtxt(os.path.join(work, "bfl_forces.txt"), ndmin=2)
+        forces = bf[:, 2:5].reshape(-1, nm, 3)
+        keep = sorted(set(range(1, min(10, len(forces)) + 1)) | set(spec["steps"]))
+        out["bfl_force_steps"] = np.array(keep, dtype=np.int64)
+        out["bfl_forces"] = forces[np.array(keep) - 1]
     with open(os.path.join(work, "timing.txt")) as fp:
         out["ref_timing"] = fp.read()
     np.savez_compressed(os.path.join(HERE, f"{name}.npz"), **out)

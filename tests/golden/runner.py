@@ -7,6 +7,7 @@ import os
 
 import numpy as np
 
+from luma_gb300 import bfl
 from luma_gb300 import case as hostcase
 from tests.golden import cases as CASES
 
@@ -28,6 +29,11 @@ def level0(name: str) -> hostcase.Level0:
     init = CASES.initial_fields(name)
     if init is not None:
         l0.u = init["u"].copy()
+    b = spec.get("bfl")
+    if b:
+        body = bfl.circle_body(l0, b["centre"], b["radius"])
+        l0.typ = body.typ
+        l0.bfl = body
     return l0
 
 
@@ -64,6 +70,9 @@ def build_backend(name: str, make, precision=None):
         grids.append(g)
     for g, lv in zip(grids, levels):
         g.upload(*initial_state(lv), t=0)
+        body = getattr(lv, "bfl", None)
+        if body is not None:
+            g.bfl_set(body.site_marker, body.q)
     return grids, levels
 
 

@@ -146,6 +146,25 @@ def test_oracle_fem_fsi_bit_exact_vs_reference(name):
         assert np.array_equal(mk[:, 6], rm[:, 8]), "epsilon"
 
 
+@pytest.mark.parametrize("name", sorted(n for n in CASES.CASES if CASES.CASES[n].get("bfl")))
+def test_bfl_setup_and_oracle_forces_bit_exact_vs_reference(name):
+    """The host BFL set-up (circle prefab, labels, surface closure, link
+    distances, per-site marker lookup) equals the reference's BFLBody, and the
+    restated BFL stream's per-marker momentum-exchange forces equal the
+    reference's computeLiftDrag(v, id, g, markerID) at every stored step."""
+    fx = R.fixture(name)
+    l0 = R.level0(name)
+    assert np.array_equal(l0.typ, fx["typ"])
+    assert np.array_equal(l0.bfl.site_marker, fx["bfl_site_marker"])
+    assert np.array_equal(l0.bfl.q, fx["bfl_q"])
+    grids, _ = R.build_backend(name, lambda d, p: O.OracleGrid(d, p))
+    done = 0
+    for s, ref in zip(fx["bfl_force_steps"], fx["bfl_forces"]):
+        grids[0].step(int(s) - done)
+        done = int(s)
+        assert np.array_equal(grids[0].bfl_forces(), ref), f"marker forces at step {s}"
+
+
 def test_oracle_momentum_exchange_bit_exact_vs_reference():
     """computeLiftDrag over the solid sites (the Poiseuille channel's walls),
     restated in the oracle: bit-exact with the reference build's force for
