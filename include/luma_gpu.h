@@ -227,6 +227,24 @@ int luma_gpu_ibm_body_force(luma_gpu_grid *grid, int body, double force[3]);
  * host. */
 int luma_gpu_momex_force(luma_gpu_grid *grid, double force[3]);
 
+/* ---- BFL bodies ------------------------------------------------------------ */
+/* Attach BFL body 0 of a grid (ObjectManager::pBody[0], set up by BFLBody:
+ * labels, surface closure and link distances, src/BFLBody.cpp:49-142):
+ * site_marker[N*M*K] is, per site in id order, the marker
+ * Body::getMarkerData finds for the site's position (inc/Body.h:581-614;
+ * -1 for none) and q[Q*nmarkers] is BFLBody::Q (q[v + Q*m]; -1 where no wall
+ * cuts the link).  The grid's stream then applies _LBM_applyBFL_opt
+ * (src/GridObj_ops_lbm_optimised.cpp:1010-1113) on every link it names.
+ * A grid whose labels hold LUMA_SITE_BFL sites refuses to step
+ * (LUMA_E_STATE) until this is called.  Replaces the per-link position
+ * lookups of _LBM_applyBFL_opt. */
+int luma_gpu_bfl_set(luma_gpu_grid *grid, const int32_t *site_marker, int nmarkers, const double *q);
+/* Per-marker momentum-exchange force (forces[3*m + d], FP64, lattice units)
+ * of the latest step: ObjectManager::computeLiftDrag(v, id, g, markerID)
+ * (src/ObjectManager.cpp:176-189) summed in the reference's loop order.
+ * Blocks until the result is on the host. */
+int luma_gpu_bfl_forces(luma_gpu_grid *grid, double *forces);
+
 /* ---- discrete adjoint of the time-averaged drag ------------------------- */
 /* No counterpart in the reference (its objective is the drag that
  * io_writeLiftDrag writes, src/ObjectManager_ops_io.cpp:105-121).

@@ -93,7 +93,6 @@ int build_site_tables(luma_gpu_grid *g, const int32_t *typ, const double *xpos, 
             for (int k = 0; k < K; ++k) {
                 const int id = k + j * K + i * K * M;
                 const int t = typ[id];
-                if (t == LUMA_SITE_BFL) return luma_set_error(LUMA_E_INVALID, "BFL sites are outside the GPU path");
                 // Pulling from an extrapolate-right site reads the population two
                 // sites to its left (:246-251): such sites need i >= 2.
                 if (t == LUMA_SITE_EXTRAPOLATE_RIGHT && i < 2)
@@ -272,6 +271,7 @@ StepArgs make_args(luma_gpu_grid *g, int subcycle) {
     a.f = g->f[g->cur];
     a.fNew = g->f[g->cur ^ 1];
     a.fOut = a.fNew;
+    luma_bfl_args(g, a);
     a.defer = g->fuse ? g->defer : nullptr;
     a.u = g->u; a.rho = g->rho; a.force = g->force;
     a.ux_in = g->uxin; a.uy_in = g->uyin; a.uz_in = g->uzin;
@@ -403,7 +403,7 @@ void tree_signature(const luma_gpu_grid *g, std::vector<uintptr_t> &s) {
     auto P = [&](const void *p) { s.push_back((uintptr_t)p); };
     auto V = [&](long long v) { s.push_back((uintptr_t)v); };
     P(g); P(g->f[0]); P(g->f[1]); P(g->u); P(g->rho); P(g->force); P(g->typ); P(g->wall); P(g->reg); P(g->velu);
-    P(g->uxin); P(g->defer); P(g->defer_ids); P(g->fast); P(g->gen_ids); P(g->adj);
+    P(g->uxin); P(g->defer); P(g->defer_ids); P(g->fast); P(g->gen_ids); P(g->adj); P(g->bfl);
     V(g->cur); V(g->aa_odd); V(g->bulk); V(g->fuse); V(g->ngen); V(g->ndefer); V(g->nreg); V(g->nvelu);
     V(g->d.flags);
     if (g->ibm) {
@@ -519,6 +519,7 @@ void free_grid(luma_gpu_grid *g) {
     free_graph(g);
     luma_ibm_free(g);
     luma_adj_free(g);
+    luma_bfl_free(g);
     cudaFree(g->typ);
     cudaFree(g->f[0]);
     cudaFree(g->f[1]);
@@ -653,6 +654,7 @@ int luma_gpu_grid_create(const luma_grid_desc *desc, luma_gpu_grid *parent, luma
     rc = build_site_tables(g, d.lattyp, d.xpos, d.ypos, d.zpos);
     if (rc) return fail(rc);
     g->htyp.assign(d.lattyp, d.lattyp + g->n);
+    g->nbfl_sites = (size_t)std::count(g->htyp.begin(), g->htyp.end(), (uint8_t)LUMA_SITE_BFL);
     if ((rc = luma_update_defer(g))) return fail(rc);
     if ((rc = luma_build_interior(g))) return fail(rc);
     if (d.xpos) g->hx.assign(d.xpos, d.xpos + d.N);
@@ -792,10 +794,20 @@ int luma_gpu_get_time(const luma_gpu_grid *g, int *t) {
     return LUMA_OK;
 }
 
+static int check_bfl(const luma_gpu_grid *g) {
+    if (g->nbfl_sites && !g->bfl)
+        return luma_set_error(LUMA_E_STATE, "grid L%d has %zu BFL sites and no BFL body (luma_gpu_bfl_set)",
+                              g->d.level, g->nbfl_sites);
+    for (const luma_gpu_grid *c : g->kids)
+        if (int rc = check_bfl(c)) return rc;
+    return LUMA_OK;
+}
+
 int luma_gpu_step(luma_gpu_grid *root, int nsteps) {
     if (!root) return luma_set_error(LUMA_E_INVALID, "null grid");
     if (root->parent) return luma_set_error(LUMA_E_INVALID, "luma_gpu_step takes the level-0 grid");
     if (nsteps < 0) return luma_set_error(LUMA_E_INVALID, "negative step count");
+    if (int rc = check_bfl(root)) return rc;
     if (nsteps >= kGraphMinSteps) {
         // pairs as graph launches; the last step runs directly (it writes u, rho)
         int done = 0;

@@ -62,6 +62,15 @@ struct StepArgs {
     // terms F_x w of the step
     double *ibm_f_out, *ibm_drag_out;
     void *ibm_sf_out;
+    // BFL links (null without a BFL body): per site a record or -1, per
+    // record the linked directions and first link, per link q, kind and the
+    // recorded f_opp + fNew_v of the step
+    const int *bfl_rec;
+    const uint32_t *bfl_mask;
+    const int *bfl_first;
+    const double *bfl_q;
+    const uint8_t *bfl_kind;
+    double *bfl_val;
     const double *ibm_drag_w;
     int ibm_drag_base, ibm_drag_nm;
     void *u, *rho;          // R*, SoA
@@ -93,6 +102,13 @@ struct RegSite {
     int8_t ndir;
     int8_t edges;
 };
+
+// Rounded products and sums the compiler may not fuse into an FMA (where an
+// expression must round as the reference's does).
+__device__ __forceinline__ float mul_rn(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ double mul_rn(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ float add_rn(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ double add_rn(double a, double b) { return __dadd_rn(a, b); }
 
 template <class P>
 __device__ __forceinline__ typename P::R ld(const void *p, size_t idx) {

@@ -14,6 +14,7 @@ namespace luma {
 struct IbmState;
 struct AdjState;
 struct StepGraph;
+struct BflState;
 }
 
 struct luma_gpu_grid;
@@ -55,6 +56,8 @@ struct luma_gpu_grid {
     luma::IbmState *ibm = nullptr;
     luma::AdjState *adj = nullptr;   // discrete-adjoint tape (adjoint.cu)
     luma::StepGraph *graph = nullptr;  // level 0: two steps of the tree as a CUDA graph (capi.cu)
+    luma::BflState *bfl = nullptr;     // BFL link tables (bfl.cu)
+    size_t nbfl_sites = 0;             // eBFL-labelled sites
     std::vector<double> hx, hy, hz;  // site positions (host copy, for IB support search)
 };
 
@@ -72,6 +75,9 @@ void luma_ibm_free(luma_gpu_grid *g);
 int luma_adj_step_hook(luma_gpu_grid *g, const luma::StepArgs &a);
 void luma_adj_redirect(luma_gpu_grid *g, luma::StepArgs &a);
 void luma_adj_free(luma_gpu_grid *g);
+// bfl.cu
+void luma_bfl_free(luma_gpu_grid *g);
+void luma_bfl_args(const luma_gpu_grid *g, luma::StepArgs &a);
 // fem.cu
 int luma_fem_upload(luma_gpu_grid *g);
 int luma_fem_supports(luma_gpu_grid *g);

@@ -67,9 +67,34 @@ __device__ __forceinline__ void stream_site(const StepArgs &a, const int8_t *wal
         const int sid = sz + sy * K + sx * K * M;
         const int stype = a.typ[sid];
         if (type == LUMA_SITE_BFL || stype == LUMA_SITE_BFL) {
-            g_unsupported = 1;
-            fn[v] = R(0);
-            continue;
+            // _LBM_applyBFL_opt (:1010-1113) through the link tables
+            // (kinds in bfl.cu); links without a wall stream as usual
+            if (!a.bfl_rec) {
+                g_unsupported = 1;
+                fn[v] = R(0);
+                continue;
+            }
+            const int r = a.bfl_rec[id];
+            const uint32_t lm = r >= 0 ? a.bfl_mask[r] : 0u;
+            if ((lm >> v) & 1u) {
+                const int l = a.bfl_first[r] + __popc(lm & ((1u << v) - 1u));
+                const int kind = a.bfl_kind[l];
+                const R fo = ld<P>(a.f, (size_t)L::opp(v) * n + id);
+                if (kind == 0) {
+                    fn[v] = fo;
+                } else if (kind == 1) {
+                    fn[v] = ld<P>(a.fNew, (size_t)v * n + id);
+                } else {
+                    const double q = a.bfl_q[l];
+                    const R fv = ld<P>(a.f, (size_t)v * n + id);
+                    fn[v] = add_rn(mul_rn(R(1 - 2 * q), R((fv - fo) / R(2 - 2 * q))), fo);
+                }
+                if (kind != 1) {
+                    const double sh = P::shifted ? L::w(v) * a.rho0 : 0.0;  // w_opp(v) = w_v
+                    a.bfl_val[l] = (double(fo) + sh) + (double(fn[v]) + sh);
+                }
+                continue;
+            }
         }
         if (type == LUMA_SITE_SLIP) {
             // _LBM_applySpecReflect_opt (:527-581): first matching wall wins.

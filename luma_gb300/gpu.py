@@ -61,6 +61,8 @@ def lib() -> C.CDLL:
         L.luma_gpu_adj_backward.argtypes = [vp, C.c_double, dp, dp]
         L.luma_gpu_adj_memory.argtypes = [vp, C.POINTER(C.c_size_t)]
         L.luma_gpu_momex_force.argtypes = [vp, dp]
+        L.luma_gpu_bfl_set.argtypes = [vp, C.POINTER(C.c_int32), C.c_int, dp]
+        L.luma_gpu_bfl_forces.argtypes = [vp, dp]
         if L.luma_gpu_abi_version() != A.ABI_VERSION:
             raise RuntimeError("luma_gb300 library ABI version mismatch")
         _lib = L
@@ -174,6 +176,20 @@ class GpuGrid:
         """Momentum-exchange force of the solid sites (lattice units)."""
         out = np.zeros(3)
         check(self.L.luma_gpu_momex_force(self.h, A.dptr(out)))
+        return out
+
+    def bfl_set(self, site_marker, q) -> None:
+        """BFL body 0: per-site marker of the site's voxel (-1 for none) and
+        the (nmarkers, Q) link distances (-1: no wall on the link)."""
+        sm = np.ascontiguousarray(site_marker, dtype=np.int32)
+        q = np.ascontiguousarray(q, dtype=np.float64)
+        self._bfl_nm = int(q.shape[0])
+        check(self.L.luma_gpu_bfl_set(self.h, sm.ctypes.data_as(C.POINTER(C.c_int32)), self._bfl_nm, A.dptr(q)))
+
+    def bfl_forces(self) -> np.ndarray:
+        """(nmarkers, 3) momentum-exchange force per BFL marker of the latest step."""
+        out = np.zeros((self._bfl_nm, 3))
+        check(self.L.luma_gpu_bfl_forces(self.h, A.dptr(out)))
         return out
 
     # ---- discrete adjoint of the time-averaged drag ----

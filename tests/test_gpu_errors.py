@@ -51,7 +51,13 @@ def test_site_label_refusals():
     typ = l0.typ.copy()
     typ[500] = A.BFL
     l0.typ = typ
-    expect(A.LUMA_E_INVALID, create, l0.desc(), match="BFL")
+    g = create(l0.desc())
+    g.upload(*R.initial_state(l0), t=0)
+    expect(A.LUMA_E_STATE, g.step, 1, match="BFL")   # BFL labels without a BFL body
+    sm = np.full(l0.ncell, -1, dtype=np.int32)
+    expect(A.LUMA_E_INVALID, g.bfl_set, sm, np.full((0, 9), -1.0), match="no marker")
+    sm[500] = 3
+    expect(A.LUMA_E_INVALID, g.bfl_set, sm, np.full((2, 9), -1.0), match="marker 3")
     l0 = channel()
     typ = l0.typ.reshape(l0.N, l0.M, l0.K).copy()
     typ[1, 10, 0] = A.EXTRAPOLATE_RIGHT

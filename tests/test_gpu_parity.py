@@ -276,3 +276,21 @@ def test_momentum_exchange_force(prec):
     got, want = g.momex_force(), o.momex_force()
     assert abs(want[0]) > 1e-3
     assert np.max(np.abs(got - want)) <= tol * np.max(np.abs(want)), (got, want)
+
+
+@pytest.mark.parametrize("split", [False, True], ids=["one_kernel", "split_interior"])
+@pytest.mark.parametrize("prec", [A.PREC_FP64, A.PREC_FP32_SHIFTED])
+def test_bfl_marker_forces(prec, split):
+    """BFL cylinder: per-marker momentum-exchange forces against the
+    reference build's computeLiftDrag(v, id, g, markerID) at every stored
+    step (FP64: within 1e-10 of the largest force; shifted FP32: 1e-4)."""
+    name = "bfl_cyl_d2q9"
+    fx = R.fixture(name)
+    tol = 1e-10 if prec == A.PREC_FP64 else 1e-4
+    gg, _ = R.build_backend(name, make_gpu_split if split else make_gpu, prec)
+    for s, want in zip(fx["bfl_force_steps"], fx["bfl_forces"]):
+        gg[0].step(int(s) - gg[0].t)
+        got = gg[0].bfl_forces()
+        scale = np.max(np.abs(want))
+        assert scale > 0
+        assert np.max(np.abs(got - want)) <= tol * scale, (int(s), np.max(np.abs(got - want)), scale)
