@@ -396,6 +396,73 @@ def run_filaments_workload(args) -> int:
     return 0
 
 
+def run_bfl_workload(args) -> int:
+    """D2Q9 channel 8192x2048 with a BFL cylinder (radius 128 lu): MLUPS,
+    HBM fraction of the whole step, body force, FP32 vs FP64; the oracle
+    (serial on BFL grids) timed on a few steps of the same grid."""
+    from luma_gb300 import _abi as A
+    from luma_gb300 import workloads as WL
+
+    nx = args.size or 8192
+    kw = dict(nx=nx, ny=nx // 4, radius_lu=128.0 * nx / 8192.0)
+    l0, body = WL.bfl_cylinder(**kw)
+    res = {}
+    sampler = ClockSampler(0)
+    sampler.start()
+    time.sleep(0.3)
+    t0 = time.monotonic()
+    for name, prec in (("fp32_shifted", A.PREC_FP32_SHIFTED), ("fp64", A.PREC_FP64)):
+        if args.precision not in ("both", name.split("_")[0]):
+            continue
+        res[name] = WL.run_bfl(prec, args.steps, warmup=args.warmup, l0=l0, body=body)
+    t1 = time.monotonic()
+    clocks = sampler.summary(t0, t1)
+    peaks = read_peaks()
+    head = res.get("fp32_shifted") or res.get("fp64")
+    s = 4 if "fp32_shifted" in res else 8
+    bpl = 2 * 9 * s + 1
+    line = {"metric": "D2Q9 channel with a BFL cylinder: lattice updates per second",
+            "value": round(head["mlups"], 2), "unit": "MLUPS", "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": round(head["ms_per_step"], 4), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32" if s == 4 else "f64", "data": "synthetic",
+            "config": {"workload": f"D2Q9 LBGK {l0.N}x{l0.M}, solid bottom/top, uniform forced-equilibrium inlet "
+                                   f"u=0.04 lu, extrapolate-right outlet, BFL cylinder radius {kw['radius_lu']:g} lu "
+                                   f"(CIRCLE_SPHERE BFL prefab, {head['markers']} markers, {head['links']} wall "
+                                   f"links), Re_D=250", "inputs": "larger than L2"},
+            "roofline": {"bound": "hbm", "bytes_per_lu": bpl,
+                         "achieved": round(head["mlups"] * 1e6 * bpl / 1e9, 1), "peak": peaks["hbm_gbs"],
+                         "unit": "GB/s", "frac": round(head["mlups"] * 1e6 * bpl / 1e9 / peaks["hbm_gbs"], 4),
+                         "note": "whole step (all kernels) against 2*Q*s+1 bytes per lattice update"},
+            "clocks": clocks}
+    for name, r in res.items():
+        line[name] = {"mlups": round(r["mlups"], 2), "ms_per_step": round(r["ms_per_step"], 4),
+                      "body_force": r["force"]}
+    if len(res) == 2:
+        u32, u64 = res["fp32_shifted"]["u"], res["fp64"]["u"]
+        f32, f64 = res["fp32_shifted"]["force"][0], res["fp64"]["force"][0]
+        line["fp32_vs_fp64"] = {"rel_l2_u": float(np.linalg.norm(u32 - u64) / np.linalg.norm(u64)),
+                                "drag_rel": abs(f32 - f64) / abs(f64),
+                                "speedup": round(res["fp32_shifted"]["mlups"] / res["fp64"]["mlups"], 3)}
+    if not args.no_cpu_baseline:
+        from oracle import oracle as O
+        from luma_gb300 import case as hostcase
+        o = O.OracleGrid(l0.desc())
+        o.upload(hostcase.equilibrium(2, 9, l0.rho, l0.u).reshape(-1), l0.u, l0.rho, None, 0)
+        o.bfl_set(body.site_marker, body.q)
+        o.step(1)
+        nst = 2
+        t = time.perf_counter()
+        o.step(nst)
+        dt = time.perf_counter() - t
+        line["cpu_baseline"] = {"value": round(l0.ncell * nst / dt / 1e6, 2), "unit": "MLUPS", "cores": 1,
+                                "kind": "port", "sample": f"{nst} steps of the same grid on the oracle (FP64; "
+                                                          f"serial: BFL marker forces accumulate in site order), "
+                                                          f"{dt:.1f} s"}
+        o.close()
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def run_ours(args, rank: int, world: int, local_rank: int):
     import torch
     from luma_gb300 import _abi as A
@@ -568,10 +635,10 @@ def main(argv=None) -> int:
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--size", type=int, default=None,
                     help="box edge (default 256) or, for --workload sphere, base x extent (default 384)")
-    ap.add_argument("--workload", default="box", choices=["box", "sphere", "cylinder_adjoint", "filaments"],
+    ap.add_argument("--workload", default="box", choices=["box", "sphere", "cylinder_adjoint", "filaments", "bfl"],
                     help="box: the headline 256^3 line (default); sphere: IB sphere with two refinement "
                          "levels; cylinder_adjoint: the drag-gradient workload alone; filaments: D3Q27 KBC with "
-                         "one refinement level and 64 FEM filaments")
+                         "one refinement level and 64 FEM filaments; bfl: D2Q9 channel with a BFL cylinder")
     ap.add_argument("--precision", default="both", choices=["both", "fp32", "fp64"],
                     help="sphere / cylinder_adjoint workloads: which precisions to run")
     ap.add_argument("--cpu-steps", type=int, default=20)
@@ -589,6 +656,8 @@ def main(argv=None) -> int:
         return run_sphere_workload(args) if rank == 0 else 0
     if args.workload == "filaments":
         return run_filaments_workload(args) if rank == 0 else 0
+    if args.workload == "bfl":
+        return run_bfl_workload(args) if rank == 0 else 0
     if args.workload == "cylinder_adjoint":
         if rank == 0:
             prec = {"both": ("fp32_shifted", "fp64"), "fp32": ("fp32_shifted",), "fp64": ("fp64",)}[args.precision]

@@ -53,8 +53,17 @@ def _vecnorm(v) -> float:
     return math.sqrt(s)
 
 
-def circle_body(level0, centre, radius: float) -> BflBody:
-    """A rigid 2D BFL circle on level 0 (reference ``CIRCLE_SPHERE BFL``)."""
+def circle_body(level0, centre, radius: float, reset_projection: bool = False) -> BflBody:
+    """A rigid 2D BFL circle on level 0 (reference ``CIRCLE_SPHERE BFL``).
+
+    The reference's surface closure never resets its projection point count
+    (``num_points_in_projection`` is doubled per projection for the whole
+    body, ``src/BFLBody.cpp:572,654``), so its cost doubles with every
+    closure marker and a circle needing a few dozen of them never finishes
+    setting up.  ``reset_projection`` starts every closure from the initial
+    20 points instead (a circle the reference can set up may then get
+    slightly different closure positions); the default follows the
+    reference."""
     lv = level0
     d = lv.defs
     if d.dims != 2:
@@ -77,11 +86,13 @@ def circle_body(level0, centre, radius: float) -> BflBody:
         return i >= N or i < 0 or j >= M or j < 0 or k >= K or k < 0
 
     pos, supp = [], []
+    voxel_marker = {}  # voxel -> first marker in it (getMarkerData's linear search)
 
     def add_marker(x, y, z):
         v = voxel(x, y, z)
         if off_grid(*v):
             raise ValueError("BFL marker off the grid")
+        voxel_marker.setdefault(v, len(pos))
         pos.append((x, y, z))
         supp.append(v)
 
@@ -89,10 +100,7 @@ def circle_body(level0, centre, radius: float) -> BflBody:
         v = voxel(x, y, z)
         if off_grid(*v):
             return -1
-        for m, s in enumerate(supp):
-            if s == v:
-                return m
-        return -1
+        return voxel_marker.get(v, -1)
 
     n = int(math.floor(2.0 * L_PI * radius / dh))
     theta = _linspace(0.0, 2.0 * L_PI - (2.0 * L_PI / float(n)), n)
@@ -135,6 +143,8 @@ def circle_body(level0, centre, radius: float) -> BflBody:
                 ln = (other[0] - start[0], other[1] - start[1], other[2] - start[2])
                 need, count = False, 0
                 av = [0.0, 0.0, 0.0]
+                if reset_projection:
+                    npts = 20
                 while not need:
                     npts *= 2
                     sp = 1.0 / npts
@@ -160,46 +170,44 @@ def circle_body(level0, centre, radius: float) -> BflBody:
     # with the segments to its horizontal/vertical eBFL neighbours
     nm = len(pos)
     q = np.full(Q * nm, -1.0)
-    for i in range(N):
-        for j in range(M):
-            if typ[i, j, 0] != A.BFL:
-                continue
-            store = marker_at(xpos[i], ypos[j], zpos[0])
-            combo = []
-            for ii in range(i - 1, i + 2):
-                for jj in range(j - 1, j + 2):
-                    if 0 <= ii < N and 0 <= jj < M and (ii == i or jj == j) and not (ii == i and jj == j):
-                        mm = marker_at(xpos[ii], ypos[jj], zpos[0])
-                        if mm >= 0:
-                            combo.append((store, mm))
-            if not combo:
-                continue
-            q0 = pos[store]
-            for first, second in combo:
-                qps = pos[second]
-                p = (xpos[i], ypos[j], pos[first][2])
-                for vel in range(Q - 1):
-                    di_ = (i + c[vel][0] + N) % N
-                    dj_ = (j + c[vel][1] + M) % M
-                    ppr = (xpos[di_], ypos[dj_], pos[first][2])
-                    s1x, s1y = ppr[0] - p[0], ppr[1] - p[1]
-                    s2x, s2y = qps[0] - q0[0], qps[1] - q0[1]
-                    den = -s2x * s1y + s1x * s2y
-                    if den == 0.0:
-                        continue  # parallel: the reference's s and t are inf or nan
-                    s = (-s1y * (p[0] - q0[0]) + s1x * (p[1] - q0[1])) / den
-                    t = (s2x * (p[1] - q0[1]) - s2y * (p[0] - q0[0])) / den
-                    if s >= 0 and s <= 1 and t >= 0 and t <= 1:
-                        ix, iy = p[0] + t * s1x, p[1] + t * s1y
-                        wd = _vecnorm((ix - p[0], iy - p[1], p[2] - p[2])) / \
-                            _vecnorm((ppr[0] - p[0], ppr[1] - p[1], ppr[2] - p[2]))
-                        k = vel + Q * store
-                        if q[k] == -1:
-                            q[k] = np.finfo(np.float64).max
-                        if wd < q[k]:
-                            q[k] = wd
+    for i, j in np.argwhere(typ[:, :, 0] == A.BFL).tolist():  # (i, j) order
+        store = marker_at(xpos[i], ypos[j], zpos[0])
+        combo = []
+        for ii in range(i - 1, i + 2):
+            for jj in range(j - 1, j + 2):
+                if 0 <= ii < N and 0 <= jj < M and (ii == i or jj == j) and not (ii == i and jj == j):
+                    mm = marker_at(xpos[ii], ypos[jj], zpos[0])
+                    if mm >= 0:
+                        combo.append((store, mm))
+        if not combo:
+            continue
+        q0 = pos[store]
+        for first, second in combo:
+            qps = pos[second]
+            p = (xpos[i], ypos[j], pos[first][2])
+            for vel in range(Q - 1):
+                di_ = (i + c[vel][0] + N) % N
+                dj_ = (j + c[vel][1] + M) % M
+                ppr = (xpos[di_], ypos[dj_], pos[first][2])
+                s1x, s1y = ppr[0] - p[0], ppr[1] - p[1]
+                s2x, s2y = qps[0] - q0[0], qps[1] - q0[1]
+                den = -s2x * s1y + s1x * s2y
+                if den == 0.0:
+                    continue  # parallel: the reference's s and t are inf or nan
+                s = (-s1y * (p[0] - q0[0]) + s1x * (p[1] - q0[1])) / den
+                t = (s2x * (p[1] - q0[1]) - s2y * (p[0] - q0[0])) / den
+                if s >= 0 and s <= 1 and t >= 0 and t <= 1:
+                    ix, iy = p[0] + t * s1x, p[1] + t * s1y
+                    wd = _vecnorm((ix - p[0], iy - p[1], p[2] - p[2])) / \
+                        _vecnorm((ppr[0] - p[0], ppr[1] - p[1], ppr[2] - p[2]))
+                    k = vel + Q * store
+                    if q[k] == -1:
+                        q[k] = np.finfo(np.float64).max
+                    if wd < q[k]:
+                        q[k] = wd
+    # a site's position lies in its own voxel: the lookup is the first
+    # marker of the voxel
     site_marker = np.full(N * M * K, -1, dtype=np.int32)
-    for i in range(N):
-        for j in range(M):
-            site_marker[j * K + i * K * M] = marker_at(xpos[i], ypos[j], zpos[0])
+    for (i, j, k), m in voxel_marker.items():
+        site_marker[k + j * K + i * K * M] = m
     return BflBody(typ=typ.reshape(-1), site_marker=site_marker, q=q.reshape(nm, Q), positions=np.array(pos))

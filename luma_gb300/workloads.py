@@ -28,6 +28,16 @@ the filament tips.  The reference cannot run it (its FEM aborts in 3D); the
 structure density is 100x the fluid's, since lighter filaments in the
 reference's 3D coupling diverge within a few dozen steps (oracle, scaled
 copy).
+
+``bfl_cylinder``: D2Q9 BGK channel 8192 x 2048 (solid bottom/top, uniform
+forced-equilibrium inlet u = 0.04 lu and the same initial velocity inside,
+extrapolate-right outlet) with a
+rigid BFL cylinder of radius 128 lu at 1/4 of the length, built as the
+reference's CIRCLE_SPHERE BFL prefab (``bfl.circle_body``, with the closure's
+projection count reset per closure: the reference's own count doubles per
+closure marker and never finishes a circle this size); ``run_bfl``
+steps it and reports MLUPS, the BFL link count and the body's
+momentum-exchange force.
 """
 from __future__ import annotations
 
@@ -208,3 +218,41 @@ def run_filaments(precision: int, steps: int, warmup: int = 2, levels=None, fils
     for g in reversed(grids):
         g.close()
     return out
+
+
+def bfl_cylinder(nx: int = 8192, ny: int = 2048, radius_lu: float = 128.0, u_lu: float = 0.04,
+                 re_d: float = 250.0):
+    """(level0, BflBody) of the BFL channel workload; Re on the diameter."""
+    from . import bfl
+    res = ny // 2                               # the channel is 2 length units high
+    dh = 1.0 / res
+    nu_lu = u_lu * 2.0 * radius_lu / re_d
+    defs = hostcase.Definitions(dims=2, resolution=res, timestep=u_lu * dh, bx=nx / res, by=2.0,
+                                re=u_lu / (nu_lu * dh), ux0=1.0, no_flow=False,
+                                walls=(A.VELOCITY, A.EXTRAPOLATE_RIGHT, A.SOLID, A.SOLID, A.FLUID, A.FLUID))
+    l0 = hostcase.build_level0(defs)
+    body = bfl.circle_body(l0, (0.25 * nx * dh, 1.0 - dh, 0.0), radius_lu * dh, reset_projection=True)
+    l0.typ = body.typ
+    return l0, body
+
+
+def run_bfl(precision: int, steps: int, warmup: int = 5, l0=None, body=None) -> dict:
+    """Steps the BFL workload; returns timing, the body force and the fields."""
+    from .gpu import GpuGrid
+    if l0 is None:
+        l0, body = bfl_cylinder()
+    g = GpuGrid(l0.desc(precision=precision))
+    upload_level(g, l0)
+    g.bfl_set(body.site_marker, body.q)
+    g.step(warmup)
+    g.synchronize()
+    t = time.perf_counter()
+    g.step(steps)
+    g.synchronize()
+    sec = time.perf_counter() - t
+    F = g.bfl_forces().sum(axis=0)
+    st = g.download(f=False)
+    g.close()
+    return {"steps": steps, "warmup": warmup, "seconds": sec, "ms_per_step": sec / steps * 1e3,
+            "mlups": l0.ncell * steps / sec / 1e6, "sites": l0.ncell, "markers": int(len(body.positions)),
+            "links": int((body.q >= 0).sum()), "force": F.tolist(), "u": st["u"], "rho": st["rho"]}
