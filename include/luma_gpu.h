@@ -34,7 +34,7 @@
 extern "C" {
 #endif
 
-#define LUMA_GPU_ABI_VERSION 1
+#define LUMA_GPU_ABI_VERSION 2
 
 /* Status codes. */
 #define LUMA_OK 0
@@ -112,6 +112,11 @@ typedef struct luma_grid_desc {
     const int32_t *lattyp;      /* N*M*K site labels (LUMA_SITE_*) */
     const double *xpos, *ypos, *zpos;    /* XPos[N], YPos[M], ZPos[K] */
     const double *ux_in, *uy_in, *uz_in; /* inlet profile, length M */
+    double reynolds_ramp;       /* L_REYNOLDS_RAMP (dimensionless time); 0 = no ramp.  With a ramp every
+                                   step of the grid first sets omega from Re = re * ramp coefficient of
+                                   (t+1)*dt (GridObj::_LBM_updateReynolds, src/GridObj_ops_lbm_optimised.cpp:
+                                   39-42, 1313-1321) */
+    double re;                  /* L_RE (used by the Reynolds ramp only) */
 } luma_grid_desc;
 
 typedef struct luma_gpu_grid luma_gpu_grid;

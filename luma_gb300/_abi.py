@@ -7,7 +7,7 @@ from __future__ import annotations
 
 import ctypes as C
 
-ABI_VERSION = 1
+ABI_VERSION = 2
 
 LUMA_OK = 0
 LUMA_E_INVALID = -1
@@ -64,6 +64,7 @@ class GridDesc(C.Structure):
         ("lattyp", _ip),
         ("xpos", _dp), ("ypos", _dp), ("zpos", _dp),
         ("ux_in", _dp), ("uy_in", _dp), ("uz_in", _dp),
+        ("reynolds_ramp", C.c_double), ("re", C.c_double),
     ]
 
 

@@ -48,6 +48,7 @@ class Definitions:
     parabolic_inlet: bool = False  # L_PARABOLIC_INLET
     no_flow: bool = True           # L_NO_FLOW
     velocity_ramp: float = 0.0     # L_VELOCITY_RAMP (0 = undefined)
+    reynolds_ramp: float = 0.0     # L_REYNOLDS_RAMP (0 = undefined)
     regularised: bool = False      # L_REGULARISED_BOUNDARIES
     kbc: bool = False              # L_USE_KBC_COLLISION
     smagorinsky: bool = False      # L_USE_BGKSMAG
@@ -142,6 +143,8 @@ class Level0:
             g.coarse_lims[q] = int(self.coarse_lims[q])
         g.rho_in = d.rho_in
         g.velocity_ramp = d.velocity_ramp
+        g.reynolds_ramp = d.reynolds_ramp
+        g.re = float(d.re) if d.re is not None else 0.0
         g.pressure_delta = pd2dlbm(d.pressure_delta, self.dh, self.dt, self.dm)
         g.gravity = self.gravity
         g.gravity_dir = d.gravity_dir

@@ -69,6 +69,19 @@ void host_c(int Q, int v, int c[3]) {
         c[d] = Q == 9 ? Lattice<9>::c(v, d) : (Q == 19 ? Lattice<19>::c(v, d) : Lattice<27>::c(v, d));
 }
 
+// GridObj::_LBM_updateReynolds with GridUtils::getReynoldsRampCoefficient
+// (src/GridObj_ops_lbm_optimised.cpp:39-42, 1313-1321; src/GridUtils.cpp:
+// 1825-1833): omega of the step from Re = L_RE * (1 - cos(pi t / ramp)) at
+// t = (t_grid + 1) dt while t <= ramp (the coefficient reaches 2 at the end
+// of the ramp, then drops to 1), in the reference's operation order.
+void update_reynolds(luma_gpu_grid *g) {
+    luma_grid_desc &d = g->d;
+    const double t = (g->t + 1) * d.dt;
+    const double coeff = t <= d.reynolds_ramp ? 1.0 - std::cos(3.14159265358979323846 * t / d.reynolds_ramp) : 1.0;
+    const double nu = ((1.0 / (d.re * coeff)) * d.dt) / (d.dh * d.dh);
+    d.omega = 1.0 / ((nu / g->cs2) + 0.5);
+}
+
 double ramp(const luma_grid_desc &d, double t) {
     if (d.velocity_ramp > 0.0 && t <= d.velocity_ramp) return (1.0 - std::cos(3.14159265358979323846 * t / d.velocity_ramp)) / 2.0;
     return 1.0;
@@ -313,6 +326,7 @@ bool bulk_eligible(const luma_gpu_grid *g, const int32_t *typ) {
 }
 
 int step_grid(luma_gpu_grid *g, int subcycle, bool write_macro) {
+    if (g->d.reynolds_ramp > 0.0) update_reynolds(g);
     for (luma_gpu_grid *c : g->kids)
         for (int it = 0; it < 2; ++it) {
             int rc = step_grid(c, it, true);
@@ -417,7 +431,8 @@ void tree_signature(const luma_gpu_grid *g, std::vector<uintptr_t> &s) {
 }
 
 bool graph_safe(const luma_gpu_grid *g) {
-    if (g->d.velocity_ramp > 0.0 || g->adj || (g->ibm && g->ibm->has_flexible)) return false;
+    if (g->d.velocity_ramp > 0.0 || g->d.reynolds_ramp > 0.0 || g->adj || (g->ibm && g->ibm->has_flexible))
+        return false;
     for (const luma_gpu_grid *c : g->kids)
         if (!graph_safe(c)) return false;
     return true;
@@ -578,6 +593,9 @@ int luma_gpu_grid_create(const luma_grid_desc *desc, luma_gpu_grid *parent, luma
         return luma_set_error(LUMA_E_INVALID, "Cannot use regularised boundaries with D3Q27");
     if (!(d.omega > 0.0) || (d.omega >= 2.0 && d.collision != LUMA_COLL_BGK_SMAG))
         return luma_set_error(LUMA_E_INVALID, "relaxation frequency omega=%g out of range", d.omega);
+    if (d.reynolds_ramp < 0.0 || (d.reynolds_ramp > 0.0 && !(d.re > 0.0)))
+        return luma_set_error(LUMA_E_INVALID, "a Reynolds ramp needs re > 0 (reynolds_ramp=%g, re=%g)",
+                              d.reynolds_ramp, d.re);
     if (!d.lattyp) return luma_set_error(LUMA_E_INVALID, "lattyp is required");
     if (!d.ux_in || !d.uy_in || !d.uz_in) return luma_set_error(LUMA_E_INVALID, "inlet profile arrays are required");
     if (parent) {

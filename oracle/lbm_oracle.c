@@ -639,8 +639,20 @@ static int loop_is_local(const oracle_grid *g) {
     return 1;
 }
 
+/* ---- GridObj::_LBM_updateReynolds, :1313-1321, with
+ * GridUtils::getReynoldsRampCoefficient (src/GridUtils.cpp:1825-1833), as
+ * LBM_multi_opt calls it first (:39-42) ---- */
+static void update_reynolds(oracle_grid *g) {
+    const double t = (g->t + 1) * g->d.dt;
+    const double coeff = t <= g->d.reynolds_ramp ? 1.0 - cos(L_PI * t / g->d.reynolds_ramp) : 1.0;
+    const double nu = ((1.0 / (g->d.re * coeff)) * g->d.dt) / (g->d.dh * g->d.dh);
+    const double cs = cs_();
+    g->d.omega = 1.0 / ((nu / (cs * cs)) + 0.5);
+}
+
 /* ---- GridObj::LBM_multi_opt, :36-193 ---- */
 static int multi_opt(oracle_grid *g, int subcycle) {
+    if (g->d.reynolds_ramp > 0.0) update_reynolds(g);
     for (int s = 0; s < g->nsub; ++s)
         for (int it = 0; it < 2; ++it)
             if (multi_opt(g->sub[s], it)) return -1;

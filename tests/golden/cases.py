@@ -60,6 +60,13 @@ CASES = {
                          walls=(V, X, S, S, F, F)),
         regions=[((0.5, 0.25, 0.0), (1.0, 0.75, 0.0))],
         steps=(10, 200), store_f=(10,)),
+    # The same channel with a Reynolds-number ramp over 0.1 time units (80
+    # level-0 steps): omega set every step on both levels.
+    "reramp_d2q9": dict(
+        defs=Definitions(dims=2, resolution=40, timestep=1.0 / 800.0, bx=2.0, by=1.0, re=50, ux0=1.0,
+                         reynolds_ramp=0.1, walls=(V, X, S, S, F, F)),
+        regions=[((0.5, 0.25, 0.0), (1.0, 0.75, 0.0))],
+        steps=(10, 60, 200), store_f=(10,)),
     # D3Q19 periodic box with two nested refined regions.
     "refine_d3q19": dict(
         defs=Definitions(dims=3, resolution=32, timestep=1.0 / 512.0, bx=1.0, by=1.0, bz=1.0,
