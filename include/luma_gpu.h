@@ -250,6 +250,31 @@ int luma_gpu_bfl_set(luma_gpu_grid *grid, const int32_t *site_marker, int nmarke
  * Blocks until the result is on the host. */
 int luma_gpu_bfl_forces(luma_gpu_grid *grid, double *forces);
 
+/* ---- output in the reference's formats ------------------------------------ */
+/* GridObj::io_lite(tval, "") (src/GridObj_ops_io.cpp:706-810) for every grid
+ * of the tree: <dir>/io_lite.Lev<l>.Reg<r>.Rnk<rank>.<(int)tval>.dat, doubles
+ * in fixed notation with `precision` digits (L_OUTPUT_PRECISION).  The state
+ * is copied to the host before the call returns; the files are formatted
+ * and written by a host thread while the caller steps on (luma_gpu_io_wait
+ * joins it).  fNew is the state before the latest step, as the reference's
+ * fNew after its swap (on the in-place all-fluid path, f). */
+int luma_gpu_io_lite(luma_gpu_grid *root, const char *dir, double tval, int precision, int rank);
+/* GridObj::io_restart(eWrite) (src/GridObj_ops_io.cpp:406-490) for the tree:
+ * <dir>/restart_LBM_Rnk<rank>.out, level 0 then each sub-grid after its
+ * parent; same snapshot and host-thread scheme as luma_gpu_io_lite. */
+int luma_gpu_io_restart(luma_gpu_grid *root, const char *dir, int rank);
+/* Waits for the tree's pending writers; returns the first error they met. */
+int luma_gpu_io_wait(luma_gpu_grid *root);
+/* The two formats from host arrays in the reference layout (f, fnew: N*M*K*Q;
+ * u: N*M*K*dims; rho: N*M*K), with the labels, positions, dt, dh and omega
+ * of `desc`: the formatting alone, for callers that hold the state.
+ * fnew may be NULL (f is written in its place); `append` adds to an
+ * existing restart file, as the reference's sub-grids do. */
+int luma_io_lite_write(const luma_grid_desc *desc, const double *f, const double *fnew, const double *u,
+                       const double *rho, const char *dir, double tval, int precision, int rank);
+int luma_io_restart_write(const luma_grid_desc *desc, const double *f, const double *u, const double *rho,
+                          const char *path, int append);
+
 /* ---- discrete adjoint of the time-averaged drag ------------------------- */
 /* No counterpart in the reference (its objective is the drag that
  * io_writeLiftDrag writes, src/ObjectManager_ops_io.cpp:105-121).

@@ -535,6 +535,7 @@ void free_grid(luma_gpu_grid *g) {
     luma_ibm_free(g);
     luma_adj_free(g);
     luma_bfl_free(g);
+    luma_io_free(g);
     cudaFree(g->typ);
     cudaFree(g->f[0]);
     cudaFree(g->f[1]);

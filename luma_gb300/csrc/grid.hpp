@@ -15,6 +15,7 @@ struct IbmState;
 struct AdjState;
 struct StepGraph;
 struct BflState;
+struct IoJobs;
 }
 
 struct luma_gpu_grid;
@@ -57,6 +58,7 @@ struct luma_gpu_grid {
     luma::AdjState *adj = nullptr;   // discrete-adjoint tape (adjoint.cu)
     luma::StepGraph *graph = nullptr;  // level 0: two steps of the tree as a CUDA graph (capi.cu)
     luma::BflState *bfl = nullptr;     // BFL link tables (bfl.cu)
+    luma::IoJobs *io = nullptr;        // level 0: pending file writers (io.cu)
     size_t nbfl_sites = 0;             // eBFL-labelled sites
     std::vector<double> hx, hy, hz;  // site positions (host copy, for IB support search)
 };
@@ -78,6 +80,8 @@ void luma_adj_free(luma_gpu_grid *g);
 // bfl.cu
 void luma_bfl_free(luma_gpu_grid *g);
 void luma_bfl_args(const luma_gpu_grid *g, luma::StepArgs &a);
+// io.cu
+void luma_io_free(luma_gpu_grid *g);
 // fem.cu
 int luma_fem_upload(luma_gpu_grid *g);
 int luma_fem_supports(luma_gpu_grid *g);

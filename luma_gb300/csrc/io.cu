@@ -1,0 +1,329 @@
+// Output of grid state in the reference's ASCII formats, fed by device
+// snapshots.
+//
+// GridObj::io_lite (LUMA src/GridObj_ops_io.cpp:706-810): one file per grid,
+// <dir>/io_lite.Lev<l>.Reg<r>.Rnk<rank>.<(int)t>.dat, one line per site in
+// (k, j, i) order (i fastest): rank, label, X, Y, Z, rho, u (a 0.000000
+// z-column in 2D), f[Q], fNew[Q], every value followed by a tab, doubles in
+// fixed notation with the writer's precision (L_OUTPUT_PRECISION).
+//
+// GridObj::io_restart(eWrite) (:406-490): <dir>/restart_LBM_Rnk<rank>.out,
+// level 0 first and every sub-grid appended after its parent (depth first,
+// region order), one line per site in (k, j, i) order: level, region, X, Y,
+// Z, u in dimensionless units (u dh / dt), rho, and per direction the scaled
+// non-equilibrium part ((f - feq) omega) / (feq dt), with feq from the
+// site's rho and u as _LBM_equilibrium_opt (:674-705) evaluates it; values in
+// the stream's default format (6 significant digits).
+//
+// The ostream insertions the reference uses format a double as printf's
+// "%.*f" (fixed) and "%.6g" (default) do, so the writers use those.
+//
+// luma_gpu_io_lite / luma_gpu_io_restart take the snapshot on the calling
+// thread (device -> host, reference layout, FP64) and leave the formatting
+// and the file writes to a host thread: they return once the state is on
+// the host, while the GPU steps on.  luma_gpu_io_wait joins the writers.
+#include <cuda_runtime.h>
+
+#include <cerrno>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <memory>
+#include <mutex>
+#include <string>
+#include <thread>
+#include <vector>
+
+#include "grid.hpp"
+#include "lattice.cuh"
+#include "dispatch.hpp"
+#include "kernels.hpp"
+
+using namespace luma;
+
+namespace luma {
+struct IoJobs {
+    std::vector<std::thread> threads;
+    std::mutex mu;
+    int status = LUMA_OK;
+    std::string message;
+};
+}  // namespace luma
+
+namespace {
+
+// One grid's state in the reference layout with what the writers print.
+struct Snapshot {
+    int level = 0, region = 0, N = 0, M = 0, K = 0, Q = 0, dims = 0;
+    double dt = 0, dh = 0, omega = 0;
+    std::vector<int> typ;
+    std::vector<double> x, y, z, f, fnew, u, rho;
+};
+
+void lattice_c(int Q, int v, int c[3]) {
+    for (int d = 0; d < 3; ++d)
+        c[d] = Q == 9 ? Lattice<9>::c(v, d) : (Q == 19 ? Lattice<19>::c(v, d) : Lattice<27>::c(v, d));
+}
+double lattice_w(int Q, int v) { return Q == 9 ? Lattice<9>::w(v) : (Q == 19 ? Lattice<19>::w(v) : Lattice<27>::w(v)); }
+
+// _LBM_equilibrium_opt with the reference's expression structure (integer
+// lattice products, cs = 1/sqrt(3) squared in place).
+double feq(int Q, int dims, int v, double rho, const double *u) {
+    int c[3];
+    lattice_c(Q, v, c);
+    const double cs = 1.0 / std::sqrt(3.0);
+    double A, B;
+    if (dims == 3) {
+        A = (c[0] * u[0]) + (c[1] * u[1]) + (c[2] * u[2]);
+        B = ((c[0] * c[0]) - (cs * cs)) * (u[0] * u[0]) + ((c[1] * c[1]) - (cs * cs)) * (u[1] * u[1]) +
+            ((c[2] * c[2]) - (cs * cs)) * (u[2] * u[2]) + 2 * c[0] * c[1] * u[0] * u[1] +
+            2 * c[0] * c[2] * u[0] * u[2] + 2 * c[1] * c[2] * u[1] * u[2];
+    } else {
+        A = (c[0] * u[0]) + (c[1] * u[1]);
+        B = ((c[0] * c[0]) - (cs * cs)) * (u[0] * u[0]) + ((c[1] * c[1]) - (cs * cs)) * (u[1] * u[1]) +
+            2 * c[0] * c[1] * u[0] * u[1];
+    }
+    return rho * lattice_w(Q, v) * (1.0 + (A / (cs * cs)) + (B / (2.0 * (cs * cs) * (cs * cs))));
+}
+
+struct Out {
+    FILE *fp;
+    std::string buf;
+    char tmp[64];
+    void d(int v) { buf += std::to_string(v); buf += '\t'; }
+    void fixed(double v, int prec) {
+        std::snprintf(tmp, sizeof tmp, "%.*f", prec, v);
+        buf += tmp;
+        buf += '\t';
+    }
+    void gen(double v) {
+        std::snprintf(tmp, sizeof tmp, "%.6g", v);
+        buf += tmp;
+        buf += '\t';
+    }
+    void raw(const char *s) { buf += s; }
+    bool flush(bool force = false) {
+        if (!force && buf.size() < (1u << 20)) return true;
+        const bool ok = std::fwrite(buf.data(), 1, buf.size(), fp) == buf.size();
+        buf.clear();
+        return ok;
+    }
+};
+
+int write_lite(const Snapshot &s, const std::string &dir, double tval, int prec, int rank) {
+    const std::string path = dir + "/io_lite.Lev" + std::to_string(s.level) + ".Reg" + std::to_string(s.region) +
+                             ".Rnk" + std::to_string(rank) + "." + std::to_string((int)tval) + ".dat";
+    FILE *fp = std::fopen(path.c_str(), "w");
+    if (!fp) return luma_set_error(LUMA_E_INVALID, "io_lite: cannot open %s: %s", path.c_str(), std::strerror(errno));
+    Out o{fp, {}, {}};
+    o.buf.reserve(1u << 21);
+    const char *zero = "0.000000\t";  // std::to_string(0.0)
+    bool ok = true;
+    for (int k = 0; k < s.K && ok; ++k)
+        for (int j = 0; j < s.M && ok; ++j)
+            for (int i = 0; i < s.N && ok; ++i) {
+                const size_t id = (size_t)k + (size_t)j * s.K + (size_t)i * s.K * s.M;
+                o.d(rank);
+                o.d(s.typ[id]);
+                o.fixed(s.x[i], prec);
+                o.fixed(s.y[j], prec);
+                o.fixed(s.z[k], prec);
+                o.fixed(s.rho[id], prec);
+                for (int d = 0; d < s.dims; ++d) o.fixed(s.u[id * s.dims + d], prec);
+                if (s.dims != 3) o.raw(zero);
+                for (int v = 0; v < s.Q; ++v) o.fixed(s.f[v + id * s.Q], prec);
+                for (int v = 0; v < s.Q; ++v) o.fixed(s.fnew[v + id * s.Q], prec);
+                o.raw("\n");
+                ok = o.flush();
+            }
+    ok = ok && o.flush(true);
+    ok = (std::fclose(fp) == 0) && ok;
+    return ok ? LUMA_OK : luma_set_error(LUMA_E_INVALID, "io_lite: write to %s failed", path.c_str());
+}
+
+int write_restart(const Snapshot &s, FILE *fp) {
+    Out o{fp, {}, {}};
+    o.buf.reserve(1u << 21);
+    bool ok = true;
+    for (int k = 0; k < s.K && ok; ++k)
+        for (int j = 0; j < s.M && ok; ++j)
+            for (int i = 0; i < s.N && ok; ++i) {
+                const size_t id = (size_t)k + (size_t)j * s.K + (size_t)i * s.K * s.M;
+                o.d(s.level);
+                o.d(s.region);
+                o.gen(s.x[i]);
+                o.gen(s.y[j]);
+                o.gen(s.z[k]);
+                const double *u = &s.u[id * s.dims];
+                for (int d = 0; d < s.dims; ++d) o.gen((u[d] * s.dh) / s.dt);
+                o.gen(s.rho[id]);
+                for (int v = 0; v < s.Q; ++v) {
+                    const double fe = feq(s.Q, s.dims, v, s.rho[id], u);
+                    o.gen(((s.f[v + id * s.Q] - fe) * s.omega) / (fe * s.dt));
+                }
+                o.raw("\n");
+                ok = o.flush();
+            }
+    ok = ok && o.flush(true);
+    return ok ? LUMA_OK : luma_set_error(LUMA_E_INVALID, "io_restart: write failed");
+}
+
+int from_desc(const luma_grid_desc *d, const double *f, const double *fnew, const double *u, const double *rho,
+              Snapshot &s) {
+    if (!d || !d->lattyp || !d->xpos || !d->ypos || !d->zpos || !f || !u || !rho)
+        return luma_set_error(LUMA_E_INVALID, "writer: descriptor labels/positions and f, u, rho are required");
+    const size_t n = (size_t)d->N * d->M * d->K;
+    s.level = d->level; s.region = d->region; s.N = d->N; s.M = d->M; s.K = d->K; s.Q = d->Q; s.dims = d->dims;
+    s.dt = d->dt; s.dh = d->dh; s.omega = d->omega;
+    s.typ.assign(d->lattyp, d->lattyp + n);
+    s.x.assign(d->xpos, d->xpos + d->N);
+    s.y.assign(d->ypos, d->ypos + d->M);
+    s.z.assign(d->zpos, d->zpos + d->K);
+    s.f.assign(f, f + n * d->Q);
+    s.fnew.assign(fnew ? fnew : f, (fnew ? fnew : f) + n * d->Q);
+    s.u.assign(u, u + n * d->dims);
+    s.rho.assign(rho, rho + n);
+    return LUMA_OK;
+}
+
+// Device -> host snapshot of one grid (reference layout, FP64).  fNew is the
+// other population buffer of the two-buffer path (the state before the
+// latest step, as the reference's fNew holds after its swap); the in-place
+// path keeps one buffer and reports f there.
+int take(luma_gpu_grid *g, Snapshot &s) {
+    const luma_grid_desc &d = g->d;
+    s.level = d.level; s.region = d.region; s.N = d.N; s.M = d.M; s.K = d.K; s.Q = d.Q; s.dims = d.dims;
+    s.dt = d.dt; s.dh = d.dh; s.omega = d.omega;
+    s.typ.assign(g->htyp.begin(), g->htyp.end());
+    if (g->hx.size() != (size_t)d.N || g->hy.size() != (size_t)d.M || g->hz.size() != (size_t)d.K)
+        return luma_set_error(LUMA_E_STATE, "writer: the grid was created without site positions");
+    s.x = g->hx; s.y = g->hy; s.z = g->hz;
+    s.f.resize(g->n * d.Q);
+    s.u.resize(g->n * d.dims);
+    s.rho.resize(g->n);
+    int rc = luma_gpu_download_state(g, s.f.data(), s.u.data(), s.rho.data(), nullptr);
+    if (rc) return rc;
+    if (g->bulk) {
+        s.fnew = s.f;
+        return LUMA_OK;
+    }
+    s.fnew.resize(g->n * d.Q);
+    double *stage = nullptr;
+    cudaStream_t st = g->stream;
+    if (cudaMallocAsync(&stage, g->n * d.Q * sizeof(double), st) != cudaSuccess)
+        return luma_set_error(LUMA_E_NOMEM, "writer: staging allocation failed");
+    cudaError_t e = dispatch(d.Q, d.precision, [&](auto q, auto p) {
+        return launch_pop_out<decltype(q)::value, decltype(p)>(g->f[g->cur ^ 1], stage, d.N, d.M, d.K, kPopPlain,
+                                                              d.rho_in, st);
+    });
+    if (e == cudaSuccess) e = cudaMemcpyAsync(s.fnew.data(), stage, g->n * d.Q * sizeof(double), cudaMemcpyDeviceToHost, st);
+    cudaFreeAsync(stage, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    return e == cudaSuccess ? LUMA_OK : luma_set_error(LUMA_E_CUDA, "writer snapshot: %s", cudaGetErrorString(e));
+}
+
+// The tree in the reference's recursion order (parent, then each sub-grid's
+// subtree in region order).
+int take_tree(luma_gpu_grid *g, std::vector<Snapshot> &out) {
+    out.emplace_back();
+    if (int rc = take(g, out.back())) return rc;
+    for (luma_gpu_grid *c : g->kids)
+        if (int rc = take_tree(c, out)) return rc;
+    return LUMA_OK;
+}
+
+IoJobs &jobs(luma_gpu_grid *root) {
+    if (!root->io) root->io = new IoJobs();
+    return *root->io;
+}
+
+void record(IoJobs &J, int rc) {
+    if (rc == LUMA_OK) return;
+    std::lock_guard<std::mutex> lk(J.mu);
+    if (J.status == LUMA_OK) {
+        J.status = rc;
+        J.message = luma_gpu_last_error_string();
+    }
+}
+
+}  // namespace
+
+void luma_io_free(luma_gpu_grid *g) {
+    if (!g->io) return;
+    for (std::thread &t : g->io->threads)
+        if (t.joinable()) t.join();
+    delete g->io;
+    g->io = nullptr;
+}
+
+extern "C" {
+
+int luma_gpu_io_lite(luma_gpu_grid *root, const char *dir, double tval, int precision, int rank) {
+    if (!root || !dir || precision < 0 || precision > 30)
+        return luma_set_error(LUMA_E_INVALID, "luma_gpu_io_lite: null argument or precision outside 0..30");
+    if (root->parent) return luma_set_error(LUMA_E_INVALID, "luma_gpu_io_lite takes the level-0 grid");
+    auto snaps = std::make_shared<std::vector<Snapshot>>();
+    if (int rc = take_tree(root, *snaps)) return rc;
+    IoJobs &J = jobs(root);
+    const std::string d(dir);
+    J.threads.emplace_back([snaps, d, tval, precision, rank, &J] {
+        for (const Snapshot &s : *snaps) record(J, write_lite(s, d, tval, precision, rank));
+    });
+    return LUMA_OK;
+}
+
+int luma_gpu_io_restart(luma_gpu_grid *root, const char *dir, int rank) {
+    if (!root || !dir) return luma_set_error(LUMA_E_INVALID, "luma_gpu_io_restart: null argument");
+    if (root->parent) return luma_set_error(LUMA_E_INVALID, "luma_gpu_io_restart takes the level-0 grid");
+    auto snaps = std::make_shared<std::vector<Snapshot>>();
+    if (int rc = take_tree(root, *snaps)) return rc;
+    IoJobs &J = jobs(root);
+    const std::string path = std::string(dir) + "/restart_LBM_Rnk" + std::to_string(rank) + ".out";
+    J.threads.emplace_back([snaps, path, &J] {
+        FILE *fp = std::fopen(path.c_str(), "w");
+        if (!fp) {
+            record(J, luma_set_error(LUMA_E_INVALID, "io_restart: cannot open %s", path.c_str()));
+            return;
+        }
+        for (const Snapshot &s : *snaps) record(J, write_restart(s, fp));
+        if (std::fclose(fp) != 0) record(J, luma_set_error(LUMA_E_INVALID, "io_restart: close of %s failed", path.c_str()));
+    });
+    return LUMA_OK;
+}
+
+int luma_gpu_io_wait(luma_gpu_grid *root) {
+    if (!root) return luma_set_error(LUMA_E_INVALID, "null grid");
+    if (!root->io) return LUMA_OK;
+    IoJobs &J = *root->io;
+    for (std::thread &t : J.threads)
+        if (t.joinable()) t.join();
+    J.threads.clear();
+    const int rc = J.status;
+    const std::string msg = J.message;
+    J.status = LUMA_OK;
+    J.message.clear();
+    return rc == LUMA_OK ? LUMA_OK : luma_set_error(rc, "%s", msg.c_str());
+}
+
+int luma_io_lite_write(const luma_grid_desc *desc, const double *f, const double *fnew, const double *u,
+                       const double *rho, const char *dir, double tval, int precision, int rank) {
+    if (!dir || precision < 0 || precision > 30)
+        return luma_set_error(LUMA_E_INVALID, "luma_io_lite_write: null directory or precision outside 0..30");
+    Snapshot s;
+    if (int rc = from_desc(desc, f, fnew, u, rho, s)) return rc;
+    return write_lite(s, dir, tval, precision, rank);
+}
+
+int luma_io_restart_write(const luma_grid_desc *desc, const double *f, const double *u, const double *rho,
+                          const char *path, int append) {
+    if (!path) return luma_set_error(LUMA_E_INVALID, "luma_io_restart_write: null path");
+    Snapshot s;
+    if (int rc = from_desc(desc, f, nullptr, u, rho, s)) return rc;
+    FILE *fp = std::fopen(path, append ? "a" : "w");
+    if (!fp) return luma_set_error(LUMA_E_INVALID, "io_restart: cannot open %s", path);
+    int rc = write_restart(s, fp);
+    if (std::fclose(fp) != 0 && rc == LUMA_OK) rc = luma_set_error(LUMA_E_INVALID, "io_restart: close failed");
+    return rc;
+}
+
+}  // extern "C"

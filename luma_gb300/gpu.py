@@ -63,6 +63,12 @@ def lib() -> C.CDLL:
         L.luma_gpu_momex_force.argtypes = [vp, dp]
         L.luma_gpu_bfl_set.argtypes = [vp, C.POINTER(C.c_int32), C.c_int, dp]
         L.luma_gpu_bfl_forces.argtypes = [vp, dp]
+        L.luma_gpu_io_lite.argtypes = [vp, C.c_char_p, C.c_double, C.c_int, C.c_int]
+        L.luma_gpu_io_restart.argtypes = [vp, C.c_char_p, C.c_int]
+        L.luma_gpu_io_wait.argtypes = [vp]
+        L.luma_io_lite_write.argtypes = [C.POINTER(A.GridDesc), dp, dp, dp, dp, C.c_char_p, C.c_double, C.c_int,
+                                         C.c_int]
+        L.luma_io_restart_write.argtypes = [C.POINTER(A.GridDesc), dp, dp, dp, C.c_char_p, C.c_int]
         if L.luma_gpu_abi_version() != A.ABI_VERSION:
             raise RuntimeError("luma_gb300 library ABI version mismatch")
         _lib = L
@@ -192,6 +198,18 @@ class GpuGrid:
         check(self.L.luma_gpu_bfl_forces(self.h, A.dptr(out)))
         return out
 
+    # ---- output in the reference's formats ----
+    def io_lite(self, directory: str, tval: float, precision: int = 10, rank: int = 0) -> None:
+        """GridObj::io_lite for the tree (files written by a host thread)."""
+        check(self.L.luma_gpu_io_lite(self.h, directory.encode(), float(tval), precision, rank))
+
+    def io_restart(self, directory: str, rank: int = 0) -> None:
+        """GridObj::io_restart(eWrite) for the tree (written by a host thread)."""
+        check(self.L.luma_gpu_io_restart(self.h, directory.encode(), rank))
+
+    def io_wait(self) -> None:
+        check(self.L.luma_gpu_io_wait(self.h))
+
     # ---- discrete adjoint of the time-averaged drag ----
     def adj_forward(self, nsteps: int, checkpoint_every: int, body: int = 0) -> float:
         """Runs nsteps steps, checkpointing every checkpoint_every, and returns
@@ -213,3 +231,16 @@ class GpuGrid:
         b = C.c_size_t()
         check(self.L.luma_gpu_adj_memory(self.h, C.byref(b)))
         return b.value
+
+
+def write_io_lite(desc, f, fnew, u, rho, directory: str, tval: float, precision: int = 10, rank: int = 0) -> None:
+    """The io_lite format from host arrays (reference layout) of one grid."""
+    arr = [np.ascontiguousarray(x, dtype=np.float64) if x is not None else None for x in (f, fnew, u, rho)]
+    check(lib().luma_io_lite_write(C.byref(desc), *(A.dptr(x) for x in arr), directory.encode(), float(tval),
+                                   precision, rank))
+
+
+def write_io_restart(desc, f, u, rho, path: str, append: bool = False) -> None:
+    """The io_restart format from host arrays (reference layout) of one grid."""
+    arr = [np.ascontiguousarray(x, dtype=np.float64) for x in (f, u, rho)]
+    check(lib().luma_io_restart_write(C.byref(desc), *(A.dptr(x) for x in arr), path.encode(), int(append)))

@@ -7,10 +7,11 @@ configuration header pre-included in place of the reference's
 stubs in ``ref_stubs.cpp`` and the driver ``ref_harness.cpp``.  Outputs go to
 ``oracle/_ref/<case>/`` only.
 
-Left out of the build: ``main_lbm.cpp`` (the harness replaces it),
-``GridObj_ops_io.cpp`` (includes ``hdf5.h`` unconditionally, line 28) and the
+Left out of the build: ``main_lbm.cpp`` (the harness replaces it) and the
 ``MpiManager*.cpp`` / ``Mpi_buffer_*.cpp`` sources (MPI calls outside
-``L_BUILD_FOR_MPI`` guards).
+``L_BUILD_FOR_MPI`` guards).  ``GridObj_ops_io.cpp`` includes ``hdf5.h``
+unconditionally; it compiles against the do-nothing ``shim/hdf5.h`` (its
+HDF5 writer is never called) for its ASCII writers.
 
 Usage: ``python oracle/build_ref.py [--ref LUMA_DIR] [case ...]``
 """
@@ -27,7 +28,7 @@ CASES_DIR = os.path.join(HERE, "cases")
 OUT_ROOT = os.path.join(HERE, "_ref")
 DEFAULT_REF = "/root/reference/LUMA"
 
-EXCLUDE_PREFIX = ("main_lbm", "GridObj_ops_io", "MpiManager", "Mpi_buffer")
+EXCLUDE_PREFIX = ("main_lbm", "MpiManager", "Mpi_buffer")
 
 
 def list_cases() -> list[str]:

@@ -760,6 +760,13 @@ void oracle_grid_destroy(oracle_grid *g) {
     free(g);
 }
 
+/* GridObj::fNew between steps (after the swap: the state before the latest
+ * step), reference layout. */
+int oracle_download_fnew(const oracle_grid *g, double *out) {
+    memcpy(out, g->fNew, sizeof(double) * (size_t)g->ncell * g->Q);
+    return 0;
+}
+
 /* BFL body 0 of the grid: site_marker[ncell] (Body::getMarkerData of each
  * site's position, -1 for none) and q[Q * nm] (BFLBody::Q). */
 int oracle_bfl_set(oracle_grid *g, const int *site_marker, int nm, const double *q) {

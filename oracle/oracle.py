@@ -71,6 +71,7 @@ def lib():
         L.oracle_momex_force.argtypes = [C.c_void_p, C.POINTER(C.c_double)]
         L.oracle_bfl_set.argtypes = [C.c_void_p, C.POINTER(C.c_int), C.c_int, C.POINTER(C.c_double)]
         L.oracle_bfl_forces.argtypes = [C.c_void_p, C.POINTER(C.c_double)]
+        L.oracle_download_fnew.argtypes = [C.c_void_p, C.POINTER(C.c_double)]
         _lib = L
     return _lib
 
@@ -118,6 +119,12 @@ class OracleGrid:
         """Momentum-exchange force of the solid sites (computeLiftDrag)."""
         out = np.zeros(3)
         self.L.oracle_momex_force(self.h, A.dptr(out))
+        return out
+
+    def fnew(self) -> np.ndarray:
+        """GridObj::fNew between steps (the state before the latest step)."""
+        out = np.zeros(self.desc.N * self.desc.M * self.desc.K * self.desc.Q)
+        self.L.oracle_download_fnew(self.h, A.dptr(out))
         return out
 
     def bfl_set(self, site_marker, q) -> None:

@@ -13,7 +13,7 @@
  * Usage:
  *   luma_ref --out DIR --steps N [--dump-every K] [--init-u FILE] [--init-rho FILE]
  *            [--workdir DIR] [--markers FILE] [--drag-out FILE] [--momex-out FILE]
- *            [--bfl-out FILE] [--bfl-forces FILE]
+ *            [--bfl-out FILE] [--bfl-forces FILE] [--io-at S]
  *
  * With --momex-out (cases compiled with L_LD_OUT) FILE gets, per step s, the
  * momentum-exchange force ObjectManager::computeLiftDrag accumulated over
@@ -26,6 +26,10 @@
  * FILE gets, per step s and marker m, the momentum-exchange force
  * ObjectManager::computeLiftDrag(v, id, g, markerID) accumulated on the
  * marker during step s.
+ *
+ * With --io-at S the reference's own ASCII writers run after step S:
+ * GridObj::io_lite(S, "") (files io_lite.Lev<l>.Reg<r>.Rnk0.<S>.dat) and
+ * GridObj::io_restart(eWrite) (restart_LBM_Rnk0.out), into DIR.
  *
  * With --drag-out nothing is dumped; FILE gets the time average over the N
  * steps of body 0's lattice-unit drag and N.
@@ -225,7 +229,7 @@ static void reinit_equilibrium(GridObj *g) {
 
 int main(int argc, char **argv) {
     std::string out = ".", init_u, init_rho, workdir, markers, drag_out, momex_out, bfl_out, bfl_forces;
-    int steps = 0, dump_every = 0;
+    int steps = 0, dump_every = 0, io_at = -1;
     for (int a = 1; a < argc; ++a) {
         std::string k = argv[a];
         auto next = [&]() -> std::string {
@@ -243,6 +247,7 @@ int main(int argc, char **argv) {
         else if (k == "--momex-out") momex_out = next();
         else if (k == "--bfl-out") bfl_out = next();
         else if (k == "--bfl-forces") bfl_forces = next();
+        else if (k == "--io-at") io_at = std::atoi(next().c_str());
         else { std::fprintf(stderr, "unknown argument %s\n", k.c_str()); return 2; }
     }
     mkdir(out.c_str(), 0755);
@@ -316,6 +321,15 @@ int main(int argc, char **argv) {
                 const BFLMarker &mk = om->pBody[0].markers[m];
                 std::fprintf(bf, "%d %zu %.17g %.17g %.17g\n", s, m, mk.forceX, mk.forceY, mk.forceZ);
             }
+        if (s == io_at) {
+            // io_lite prefixes "./" to the output path: run it from / so
+            // that the absolute path stays absolute
+            char cwd[4096];
+            if (!getcwd(cwd, sizeof cwd) || chdir("/") != 0) { std::perror("chdir"); return 2; }
+            grids->io_lite(s, "");
+            if (chdir(cwd) != 0) { std::perror("chdir"); return 2; }
+            grids->io_restart(eWrite);
+        }
         if (!drag_out.empty()) drag_sum += body_drag();
         else if ((dump_every > 0 && s % dump_every == 0) || s == steps) dump_all(grids, out, s);
     }
