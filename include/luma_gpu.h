@@ -84,6 +84,10 @@ enum {
                                        relaxes the pre-stream f, :1147,1296) */
 #define LUMA_FLAG_TWO_BUFFER 0x20   /* keep the two-buffer step even where the in-place
                                        (AA-pattern) step applies */
+#define LUMA_FLAG_TIME_AVERAGES 0x80 /* L_COMPUTE_TIME_AVERAGED_QUANTITIES: running means of rho, u_p
+                                        and u_p u_q (p <= q) updated by every macroscopic update
+                                        (_LBM_macro_opt, :895-917); not with regularised BCs or
+                                        flexible bodies (LUMA_E_INVALID) */
 #define LUMA_FLAG_SPLIT_INTERIOR 0x40 /* two-buffer step: run interior fluid sites in their
                                        own kernel at any grid size (by default only grids
                                        of 2^18 sites or more split) */
@@ -155,6 +159,10 @@ int luma_gpu_upload_state(luma_gpu_grid *grid, const double *f, const double *u,
 /* Device -> host, same layout; any pointer may be NULL to skip it. */
 int luma_gpu_download_state(luma_gpu_grid *grid, double *f, double *u, double *rho,
                             double *force_xyz);
+/* Running means of a grid created with LUMA_FLAG_TIME_AVERAGES
+ * (GridObj::rho_timeav, ui_timeav, uiuj_timeav; reference layout: N*M*K,
+ * N*M*K*dims, N*M*K*(3*dims-3) with the (p, q >= p) pairs in order). */
+int luma_gpu_download_time_averages(luma_gpu_grid *grid, double *rho_ta, double *ui_ta, double *uiuj_ta);
 /* Step counter of a grid (GridObj::t). */
 int luma_gpu_get_time(const luma_gpu_grid *grid, int *t);
 

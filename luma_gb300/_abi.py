@@ -36,6 +36,7 @@ FLAG_FIX_MACRO3D = 0x8
 FLAG_FIX_KBC = 0x10
 FLAG_TWO_BUFFER = 0x20
 FLAG_SPLIT_INTERIOR = 0x40
+FLAG_TIME_AVERAGES = 0x80
 
 _dp = C.POINTER(C.c_double)
 _ip = C.POINTER(C.c_int32)

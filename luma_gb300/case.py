@@ -49,6 +49,7 @@ class Definitions:
     no_flow: bool = True           # L_NO_FLOW
     velocity_ramp: float = 0.0     # L_VELOCITY_RAMP (0 = undefined)
     reynolds_ramp: float = 0.0     # L_REYNOLDS_RAMP (0 = undefined)
+    time_averages: bool = False    # L_COMPUTE_TIME_AVERAGED_QUANTITIES
     regularised: bool = False      # L_REGULARISED_BOUNDARIES
     kbc: bool = False              # L_USE_KBC_COLLISION
     smagorinsky: bool = False      # L_USE_BGKSMAG
@@ -119,6 +120,8 @@ class Level0:
             fl |= A.FLAG_IBM
         if d.gravity:
             fl |= A.FLAG_GRAVITY
+        if d.time_averages:
+            fl |= A.FLAG_TIME_AVERAGES
         if fix_macro3d:
             fl |= A.FLAG_FIX_MACRO3D
         if fix_kbc:

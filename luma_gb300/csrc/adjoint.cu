@@ -625,6 +625,7 @@ int check_scope(const luma_gpu_grid *g, int body) {
         return luma_set_error(LUMA_E_INVALID, "adjoint: no regularised BCs or gravity");
     if (d.velocity_ramp > 0.0 || d.reynolds_ramp > 0.0)
         return luma_set_error(LUMA_E_INVALID, "adjoint: no velocity or Reynolds ramp");
+    if (d.flags & LUMA_FLAG_TIME_AVERAGES) return luma_set_error(LUMA_E_INVALID, "adjoint: no time averages");
     if (body < 0 || body >= (int)g->ibm->bodies.size()) return luma_set_error(LUMA_E_INVALID, "adjoint: bad body %d", body);
     std::vector<uint8_t> typ(g->n);
     if (cudaMemcpy(typ.data(), g->typ, g->n, cudaMemcpyDeviceToHost) != cudaSuccess)

@@ -285,6 +285,12 @@ StepArgs make_args(luma_gpu_grid *g, int subcycle) {
     a.fNew = g->f[g->cur ^ 1];
     a.fOut = a.fNew;
     luma_bfl_args(g, a);
+    if (g->tav) {
+        a.tav_rho = g->tav;
+        a.tav_u = g->tav + g->n;
+        a.tav_uu = g->tav + g->n * (1 + d.dims);
+        a.tav_t = g->t;
+    }
     a.defer = g->fuse ? g->defer : nullptr;
     a.u = g->u; a.rho = g->rho; a.force = g->force;
     a.ux_in = g->uxin; a.uy_in = g->uyin; a.uz_in = g->uzin;
@@ -319,7 +325,9 @@ bool bulk_eligible(const luma_gpu_grid *g, const int32_t *typ) {
     if (g->parent || !g->kids.empty()) return false;
     if (d.collision != LUMA_COLL_BGK) return false;
     if (d.N > 65535 || d.M > 65535) return false;  // grid.y / grid.z launch limits
-    if (d.flags & (LUMA_FLAG_IBM | LUMA_FLAG_GRAVITY | LUMA_FLAG_REGULARISED | LUMA_FLAG_TWO_BUFFER)) return false;
+    if (d.flags & (LUMA_FLAG_IBM | LUMA_FLAG_GRAVITY | LUMA_FLAG_REGULARISED | LUMA_FLAG_TWO_BUFFER |
+                   LUMA_FLAG_TIME_AVERAGES))
+        return false;
     for (size_t i = 0; i < g->n; ++i)
         if (typ[i] != LUMA_SITE_FLUID) return false;
     return true;
@@ -431,7 +439,8 @@ void tree_signature(const luma_gpu_grid *g, std::vector<uintptr_t> &s) {
 }
 
 bool graph_safe(const luma_gpu_grid *g) {
-    if (g->d.velocity_ramp > 0.0 || g->d.reynolds_ramp > 0.0 || g->adj || (g->ibm && g->ibm->has_flexible))
+    if (g->d.velocity_ramp > 0.0 || g->d.reynolds_ramp > 0.0 || g->adj || g->tav ||
+        (g->ibm && g->ibm->has_flexible))
         return false;
     for (const luma_gpu_grid *c : g->kids)
         if (!graph_safe(c)) return false;
@@ -549,6 +558,7 @@ void free_grid(luma_gpu_grid *g) {
     cudaFree(g->reg);
     cudaFree(g->velu);
     cudaFree(g->acc);
+    cudaFree(g->tav);
     cudaFree(g->defer);
     cudaFree(g->defer_ids);
     cudaFree(g->fast);
@@ -594,6 +604,9 @@ int luma_gpu_grid_create(const luma_grid_desc *desc, luma_gpu_grid *parent, luma
         return luma_set_error(LUMA_E_INVALID, "Cannot use regularised boundaries with D3Q27");
     if (!(d.omega > 0.0) || (d.omega >= 2.0 && d.collision != LUMA_COLL_BGK_SMAG))
         return luma_set_error(LUMA_E_INVALID, "relaxation frequency omega=%g out of range", d.omega);
+    if ((d.flags & LUMA_FLAG_TIME_AVERAGES) && (d.flags & LUMA_FLAG_REGULARISED))
+        return luma_set_error(LUMA_E_INVALID, "time averages with regularised BCs: the reference's extrapolation "
+                                              "re-runs the macroscopic step at neighbour sites (not reproduced)");
     if (d.reynolds_ramp < 0.0 || (d.reynolds_ramp > 0.0 && !(d.re > 0.0)))
         return luma_set_error(LUMA_E_INVALID, "a Reynolds ramp needs re > 0 (reynolds_ramp=%g, re=%g)",
                               d.reynolds_ramp, d.re);
@@ -670,6 +683,11 @@ int luma_gpu_grid_create(const luma_grid_desc *desc, luma_gpu_grid *parent, luma
     CKF(cudaMemcpy(g->uyin, d.uy_in, d.M * sizeof(double), cudaMemcpyHostToDevice));
     CKF(cudaMemcpy(g->uzin, d.uz_in, d.M * sizeof(double), cudaMemcpyHostToDevice));
     CKF(cudaMalloc(&g->acc, 8 * sizeof(double)));
+    if (d.flags & LUMA_FLAG_TIME_AVERAGES) {
+        const size_t nt = g->n * (size_t)(1 + d.dims + 3 * d.dims - 3);
+        CKF(cudaMalloc(&g->tav, nt * sizeof(double)));
+        CKF(cudaMemset(g->tav, 0, nt * sizeof(double)));
+    }
     rc = build_site_tables(g, d.lattyp, d.xpos, d.ypos, d.zpos);
     if (rc) return fail(rc);
     g->htyp.assign(d.lattyp, d.lattyp + g->n);
@@ -807,18 +825,37 @@ int luma_gpu_download_state(luma_gpu_grid *g, double *f, double *u, double *rho,
     return rc;
 }
 
+int luma_gpu_download_time_averages(luma_gpu_grid *g, double *rho_ta, double *ui_ta, double *uiuj_ta) {
+    if (!g || !rho_ta || !ui_ta || !uiuj_ta) return luma_set_error(LUMA_E_INVALID, "null argument");
+    if (!g->tav) return luma_set_error(LUMA_E_STATE, "grid created without LUMA_FLAG_TIME_AVERAGES");
+    const int D = g->d.dims, npq = 3 * D - 3;
+    const size_t n = g->n;
+    std::vector<double> h(n * (size_t)(1 + D + npq));
+    CK(cudaStreamSynchronize(g->stream));
+    CK(cudaMemcpy(h.data(), g->tav, h.size() * sizeof(double), cudaMemcpyDeviceToHost));
+    for (size_t id = 0; id < n; ++id) {
+        rho_ta[id] = h[id];
+        for (int p = 0; p < D; ++p) ui_ta[p + id * D] = h[(1 + p) * n + id];
+        for (int q = 0; q < npq; ++q) uiuj_ta[q + id * npq] = h[(1 + D + q) * n + id];
+    }
+    return LUMA_OK;
+}
+
 int luma_gpu_get_time(const luma_gpu_grid *g, int *t) {
     if (!g || !t) return luma_set_error(LUMA_E_INVALID, "null argument");
     *t = g->t;
     return LUMA_OK;
 }
 
-static int check_bfl(const luma_gpu_grid *g) {
+static int check_tree(const luma_gpu_grid *g) {
     if (g->nbfl_sites && !g->bfl)
         return luma_set_error(LUMA_E_STATE, "grid L%d has %zu BFL sites and no BFL body (luma_gpu_bfl_set)",
                               g->d.level, g->nbfl_sites);
+    if (g->tav && g->ibm && g->ibm->has_flexible)
+        return luma_set_error(LUMA_E_INVALID, "time averages with flexible bodies: the FSI loop re-runs the "
+                                              "macroscopic step per sub-iteration (not reproduced)");
     for (const luma_gpu_grid *c : g->kids)
-        if (int rc = check_bfl(c)) return rc;
+        if (int rc = check_tree(c)) return rc;
     return LUMA_OK;
 }
 
@@ -826,7 +863,7 @@ int luma_gpu_step(luma_gpu_grid *root, int nsteps) {
     if (!root) return luma_set_error(LUMA_E_INVALID, "null grid");
     if (root->parent) return luma_set_error(LUMA_E_INVALID, "luma_gpu_step takes the level-0 grid");
     if (nsteps < 0) return luma_set_error(LUMA_E_INVALID, "negative step count");
-    if (int rc = check_bfl(root)) return rc;
+    if (int rc = check_tree(root)) return rc;
     if (nsteps >= kGraphMinSteps) {
         // pairs as graph launches; the last step runs directly (it writes u, rho)
         int done = 0;

@@ -71,6 +71,10 @@ struct StepArgs {
     const double *bfl_q;
     const uint8_t *bfl_kind;
     double *bfl_val;
+    // running means (LUMA_FLAG_TIME_AVERAGES; null otherwise): rho, u_p and
+    // u_p u_q (p <= q), SoA, FP64; tav_t = the grid's completed steps
+    double *tav_rho, *tav_u, *tav_uu;
+    int tav_t;
     const double *ibm_drag_w;
     int ibm_drag_base, ibm_drag_nm;
     void *u, *rho;          // R*, SoA

@@ -176,7 +176,8 @@ __device__ __forceinline__ void stream_site(const StepArgs &a, const int8_t *wal
 template <int Q, class P, bool STORE = true>
 __device__ __forceinline__ void macro_site(const StepArgs &a, int i, int j, int k, int id, int type,
                                            const typename P::R *fn, typename P::R &rho, typename P::R &drho,
-                                           typename P::R &ux, typename P::R &uy, typename P::R &uz) {
+                                           typename P::R &ux, typename P::R &uy, typename P::R &uz,
+                                           int tav_reps = 1) {
     using L = Lattice<Q>;
     using R = typename P::R;
     constexpr int D = L::D;
@@ -223,6 +224,25 @@ __device__ __forceinline__ void macro_site(const StepArgs &a, int i, int j, int 
         ux = ldr<P>(a.u, id);
         uy = ldr<P>(a.u, n + id);
         uz = D == 3 ? ldr<P>(a.u, 2 * n + id) : R(0);
+    }
+    // time-averaged quantities (:895-917), tav_reps times (an IB support
+    // site is re-macroed once per marker it supports)
+    if (a.tav_rho) {
+        const double t = (double)a.tav_t, t1 = (double)(a.tav_t + 1);
+        const double uu[3] = {double(ux), double(uy), double(uz)};
+        for (int rep = 0; rep < tav_reps; ++rep) {
+            a.tav_rho[id] = __ddiv_rn(__dadd_rn(__dmul_rn(a.tav_rho[id], t), double(rho)), t1);
+            int pq = 0;
+            for (int p = 0; p < D; ++p) {
+                double *up = a.tav_u + (size_t)p * n + id;
+                *up = __ddiv_rn(__dadd_rn(__dmul_rn(*up, t), uu[p]), t1);
+                for (int q = p; q < D; ++q) {
+                    double *w = a.tav_uu + (size_t)pq * n + id;
+                    *w = __ddiv_rn(__dadd_rn(__dmul_rn(*w, t), __dmul_rn(uu[p], uu[q])), t1);
+                    ++pq;
+                }
+            }
+        }
     }
     if (type == LUMA_SITE_TL_TO_FINER) {
         const int s = child_at<Q>(a, i, j, k);
@@ -774,7 +794,9 @@ __global__ void k_ibm_remacro(StepArgs a, IbmArgs b) {
 #pragma unroll
     for (int v = 0; v < Q; ++v) fn[v] = ld<P>(a.fNew, (size_t)v * n + id);
     R rho, drho, ux, uy, uz;
-    macro_site<Q, P>(a, i, j, k, id, type, fn, rho, drho, ux, uy, uz);
+    // ibm_updateMacroscopic (:696-766) re-runs the macroscopic step once per
+    // (marker, support) pair: the running means see each repetition
+    macro_site<Q, P>(a, i, j, k, id, type, fn, rho, drho, ux, uy, uz, b.uoff[u + 1] - b.uoff[u]);
 }
 
 // _LBM_resetForces (:1327-1337): zero the force field, or, under gravity,

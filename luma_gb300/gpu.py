@@ -61,6 +61,7 @@ def lib() -> C.CDLL:
         L.luma_gpu_adj_backward.argtypes = [vp, C.c_double, dp, dp]
         L.luma_gpu_adj_memory.argtypes = [vp, C.POINTER(C.c_size_t)]
         L.luma_gpu_momex_force.argtypes = [vp, dp]
+        L.luma_gpu_download_time_averages.argtypes = [vp, dp, dp, dp]
         L.luma_gpu_bfl_set.argtypes = [vp, C.POINTER(C.c_int32), C.c_int, dp]
         L.luma_gpu_bfl_forces.argtypes = [vp, dp]
         L.luma_gpu_io_lite.argtypes = [vp, C.c_char_p, C.c_double, C.c_int, C.c_int]
@@ -177,6 +178,14 @@ class GpuGrid:
                                                int(clamped), density, E, dm, fsi_vel_scale, C.byref(idx)))
         self._nm = getattr(self, "_nm", []) + [int(math.floor(length / self.desc.dh)) + 1]
         return idx.value
+
+    def time_averages(self) -> dict:
+        """Running means (reference layout): rho (n), u (n*D), uu (n*(3D-3))."""
+        d = self.desc
+        n = d.N * d.M * d.K
+        out = {"rho": np.zeros(n), "u": np.zeros(n * d.dims), "uu": np.zeros(n * (3 * d.dims - 3))}
+        check(self.L.luma_gpu_download_time_averages(self.h, A.dptr(out["rho"]), A.dptr(out["u"]), A.dptr(out["uu"])))
+        return out
 
     def momex_force(self) -> np.ndarray:
         """Momentum-exchange force of the solid sites (lattice units)."""

@@ -96,6 +96,8 @@ struct oracle_grid {
     int *bfl_marker;
     double *bfl_q, *bfl_force;
     int bfl_nm;
+    /* running means (LUMA_FLAG_TIME_AVERAGES), reference layout */
+    double *rho_ta, *ui_ta, *uiuj_ta;
 };
 
 static char g_err[512];
@@ -341,7 +343,7 @@ static void macro_site(oracle_grid *g, int i, int j, int k, int id, int type) {
     }
     if (type == LUMA_SITE_TL_TO_FINER) {
         oracle_grid *cg = sub_grid_at(g, i, j, k);
-        if (!cg) return;
+        if (!cg) goto averages;
         const int cM = cg->d.M, cK = cg->d.K;
         const int ci = 2 * (i - cg->d.coarse_lims[0] + 1) - 2;
         const int cj = 2 * (j - cg->d.coarse_lims[2] + 1) - 2;
@@ -353,6 +355,29 @@ static void macro_site(oracle_grid *g, int i, int j, int k, int id, int type) {
                     for (int dd = 0; dd < D; ++dd) cg->u[dd + cid * D] = g->u[dd + (size_t)id * D];
                     cg->rho[cid] = g->rho[id];
                 }
+    }
+averages:
+    /* time-averaged quantities, :895-917: the mean over t completed steps
+     * becomes the mean over t + 1 with the current value */
+    if (g->rho_ta) {
+        const double t = (double)g->t, t1 = (double)(g->t + 1);
+        const double *u = g->u + (size_t)id * D;
+        double ta = g->rho_ta[id] * t;
+        ta += g->rho[id];
+        g->rho_ta[id] = ta / t1;
+        const int npq = 3 * D - 3;
+        int pq = 0;
+        for (int p = 0; p < D; ++p) {
+            ta = g->ui_ta[p + (size_t)id * D] * t;
+            ta += u[p];
+            g->ui_ta[p + (size_t)id * D] = ta / t1;
+            for (int q = p; q < D; ++q) {
+                ta = g->uiuj_ta[pq + (size_t)id * npq] * t;
+                ta += (u[p] * u[q]);
+                g->uiuj_ta[pq + (size_t)id * npq] = ta / t1;
+                pq++;
+            }
+        }
     }
 }
 
@@ -738,6 +763,11 @@ oracle_grid *oracle_grid_create(const luma_grid_desc *d, oracle_grid *parent) {
     g->u_n = dup_d(NULL, n * g->D);
     g->force_xyz = dup_d(NULL, n * g->D);
     g->rho = dup_d(NULL, n);
+    if (d->flags & LUMA_FLAG_TIME_AVERAGES) {
+        g->rho_ta = dup_d(NULL, n);
+        g->ui_ta = dup_d(NULL, n * g->D);
+        g->uiuj_ta = dup_d(NULL, n * (3 * g->D - 3));
+    }
     g->d.lattyp = NULL;
     g->d.xpos = g->d.ypos = g->d.zpos = NULL;
     g->d.ux_in = g->d.uy_in = g->d.uz_in = NULL;
@@ -757,7 +787,18 @@ void oracle_grid_destroy(oracle_grid *g) {
     free(g->f); free(g->fNew); free(g->feq); free(g->force_i);
     free(g->u); free(g->u_n); free(g->force_xyz); free(g->rho);
     free(g->bfl_marker); free(g->bfl_q); free(g->bfl_force);
+    free(g->rho_ta); free(g->ui_ta); free(g->uiuj_ta);
     free(g);
+}
+
+/* Running means of rho, u_p and u_p u_q (p <= q), reference layout. */
+int oracle_download_time_averages(const oracle_grid *g, double *rho_ta, double *ui_ta, double *uiuj_ta) {
+    if (!g->rho_ta) { set_err("grid keeps no time averages"); return -1; }
+    const size_t n = (size_t)g->ncell;
+    memcpy(rho_ta, g->rho_ta, sizeof(double) * n);
+    memcpy(ui_ta, g->ui_ta, sizeof(double) * n * g->D);
+    memcpy(uiuj_ta, g->uiuj_ta, sizeof(double) * n * (3 * g->D - 3));
+    return 0;
 }
 
 /* GridObj::fNew between steps (after the swap: the state before the latest

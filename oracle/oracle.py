@@ -72,6 +72,7 @@ def lib():
         L.oracle_bfl_set.argtypes = [C.c_void_p, C.POINTER(C.c_int), C.c_int, C.POINTER(C.c_double)]
         L.oracle_bfl_forces.argtypes = [C.c_void_p, C.POINTER(C.c_double)]
         L.oracle_download_fnew.argtypes = [C.c_void_p, C.POINTER(C.c_double)]
+        L.oracle_download_time_averages.argtypes = [C.c_void_p] + [C.POINTER(C.c_double)] * 3
         _lib = L
     return _lib
 
@@ -119,6 +120,15 @@ class OracleGrid:
         """Momentum-exchange force of the solid sites (computeLiftDrag)."""
         out = np.zeros(3)
         self.L.oracle_momex_force(self.h, A.dptr(out))
+        return out
+
+    def time_averages(self) -> dict:
+        """Running means (reference layout): rho (n), u (n*D), uu (n*(3D-3))."""
+        d = self.desc
+        n = d.N * d.M * d.K
+        out = {"rho": np.zeros(n), "u": np.zeros(n * d.dims), "uu": np.zeros(n * (3 * d.dims - 3))}
+        if self.L.oracle_download_time_averages(self.h, A.dptr(out["rho"]), A.dptr(out["u"]), A.dptr(out["uu"])):
+            raise RuntimeError(self.L.oracle_last_error().decode())
         return out
 
     def fnew(self) -> np.ndarray:

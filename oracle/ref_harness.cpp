@@ -36,7 +36,8 @@
  *
  * Output, per dump step s and grid (level l, region r):
  *   DIR/s<s>/L<l>R<r>_meta.txt   key value lines (sizes, omega, dt, dh, t, limits)
- *   DIR/s<s>/L<l>R<r>_<name>.bin f, u, rho, typ (int32), force (if allocated)
+ *   DIR/s<s>/L<l>R<r>_<name>.bin f, u, rho, typ (int32), force (if allocated),
+ *                                rho_ta, ui_ta, uiuj_ta (time-averaging builds)
  * and, if IBM bodies exist, DIR/s<s>/markers.txt.
  */
 #include <sys/stat.h>
@@ -98,6 +99,11 @@ static void dump_grid(GridObj *g, const std::string &dir) {
     write_raw(p + "zpos.bin", g->ZPos.data(), g->ZPos.size() * sizeof(double));
     if (!g->force_xyz.empty())
         write_raw(p + "force.bin", g->force_xyz.data(), g->force_xyz.size() * sizeof(double));
+#ifdef L_COMPUTE_TIME_AVERAGED_QUANTITIES
+    write_raw(p + "rho_ta.bin", g->rho_timeav.data(), g->rho_timeav.size() * sizeof(double));
+    write_raw(p + "ui_ta.bin", g->ui_timeav.data(), g->ui_timeav.size() * sizeof(double));
+    write_raw(p + "uiuj_ta.bin", g->uiuj_timeav.data(), g->uiuj_timeav.size() * sizeof(double));
+#endif
     for (GridObj *sg : g->subGrid) dump_grid(sg, dir);
 }
 

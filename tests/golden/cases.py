@@ -96,6 +96,17 @@ CASES = {
         defs=Definitions(dims=2, resolution=50, timestep=1.0 / 1250.0, bx=2.0, by=1.0, re=100, ux0=1.0,
                          walls=(V, X, S, S, F, F)),
         bfl=dict(centre=(0.5, 0.5, 0.0), radius=0.16), steps=(10, 300), store_f=(10,)),
+    # Time-averaged quantities: the refined channel (both levels) and the IB
+    # cylinder (support sites re-macroed once per marker they support).
+    "tavg_refine_d2q9": dict(
+        defs=Definitions(dims=2, resolution=40, timestep=1.0 / 800.0, bx=2.0, by=1.0, re=50, ux0=1.0,
+                         time_averages=True, walls=(V, X, S, S, F, F)),
+        regions=[((0.5, 0.25, 0.0), (1.0, 0.75, 0.0))],
+        steps=(10, 100), store_f=(), store_tav=True),
+    "tavg_ibm_cyl_d2q9": dict(
+        defs=Definitions(dims=2, resolution=32, timestep=1.0 / 800.0, bx=5.0, by=2.0, re=160, ux0=1.0,
+                         ibm=True, time_averages=True, walls=(V, X, S, S, F, F)),
+        bodies="cylinder", steps=(5, 100), store_f=(), store_tav=True),
     # D2Q9 BGK-Smagorinsky channel.
     "smag_d2q9": dict(
         defs=Definitions(dims=2, resolution=32, timestep=1.0 / 320.0, bx=2.0, by=1.0, re=2000,

@@ -47,7 +47,7 @@ def read_grid(d: str, lev: int = 0, reg: int = 0) -> dict:
             if len(meta[k]) == 1:
                 meta[k] = meta[k][0]
     out = {"meta": meta}
-    for name in ("f", "u", "rho", "uxin", "xpos", "ypos", "zpos", "force"):
+    for name in ("f", "u", "rho", "uxin", "xpos", "ypos", "zpos", "force", "rho_ta", "ui_ta", "uiuj_ta"):
         if os.path.exists(p + name + ".bin"):
             out[name] = np.fromfile(p + name + ".bin", dtype=np.float64)
     out["typ"] = np.fromfile(p + "typ.bin", dtype=np.int32)
@@ -109,6 +109,11 @@ def run_case(name: str, ref: str) -> str:
         if spec.get("store_fields", True):
             out[f"u_{s}"] = gs["u"]
             out[f"rho_{s}"] = gs["rho"]
+        if spec.get("store_tav"):
+            for t in ("rho_ta", "ui_ta", "uiuj_ta"):
+                out[f"{t}_{s}"] = gs[t]
+                for (lev, reg) in levels[1:]:
+                    out[f"L{lev}R{reg}_{t}_{s}"] = read_grid(os.path.join(work, f"s{s}"), lev, reg)[t]
         out[f"u_sha_{s}"] = sha(gs["u"])
         out[f"rho_sha_{s}"] = sha(gs["rho"])
         out[f"f_sha_{s}"] = sha(gs["f"])

@@ -165,6 +165,31 @@ def test_bfl_setup_and_oracle_forces_bit_exact_vs_reference(name):
         assert np.array_equal(grids[0].bfl_forces(), ref), f"marker forces at step {s}"
 
 
+@pytest.mark.parametrize("name", sorted(n for n in CASES.CASES if CASES.CASES[n].get("store_tav")))
+def test_oracle_time_averages_bit_exact_vs_reference(name):
+    """Running means of rho, u_p and u_p u_q (_LBM_macro_opt :895-917; IB
+    support sites re-averaged once per marker by ibm_updateMacroscopic) equal
+    the reference's on every grid at every stored step."""
+    spec = CASES.CASES[name]
+    fx = R.fixture(name)
+    grids, levels = R.build_backend(name, lambda d, p: O.OracleGrid(d, p))
+    if spec.get("bodies"):
+        ibm = O.OracleIBM()
+        for lev, reg, pos in CASES.bodies(name):
+            ibm.add_body(grids[lev], pos)
+        ibm.initialise()
+    done = 0
+    for s in spec["steps"]:
+        grids[0].step(s - done)
+        done = s
+        for g, lv in zip(grids, levels):
+            pre = "" if R.grid_key(lv) == "L0R0" else R.grid_key(lv) + "_"
+            ta = g.time_averages()
+            assert np.array_equal(ta["rho"], fx[f"{pre}rho_ta_{s}"]), (pre, s)
+            assert np.array_equal(ta["u"], fx[f"{pre}ui_ta_{s}"]), (pre, s)
+            assert np.array_equal(ta["uu"], fx[f"{pre}uiuj_ta_{s}"]), (pre, s)
+
+
 def test_oracle_momentum_exchange_bit_exact_vs_reference():
     """computeLiftDrag over the solid sites (the Poiseuille channel's walls),
     restated in the oracle: bit-exact with the reference build's force for
