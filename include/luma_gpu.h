@@ -276,10 +276,13 @@ int luma_gpu_io_wait(luma_gpu_grid *root);
 /* The two formats from host arrays in the reference layout (f, fnew: N*M*K*Q;
  * u: N*M*K*dims; rho: N*M*K), with the labels, positions, dt, dh and omega
  * of `desc`: the formatting alone, for callers that hold the state.
- * fnew may be NULL (f is written in its place); `append` adds to an
- * existing restart file, as the reference's sub-grids do. */
+ * fnew may be NULL (f is written in its place); the three time averages
+ * (layout of luma_gpu_download_time_averages) are all NULL or all given and
+ * then add the columns the reference writes when it keeps them; `append`
+ * adds to an existing restart file, as the reference's sub-grids do. */
 int luma_io_lite_write(const luma_grid_desc *desc, const double *f, const double *fnew, const double *u,
-                       const double *rho, const char *dir, double tval, int precision, int rank);
+                       const double *rho, const double *rho_ta, const double *ui_ta, const double *uiuj_ta,
+                       const char *dir, double tval, int precision, int rank);
 int luma_io_restart_write(const luma_grid_desc *desc, const double *f, const double *u, const double *rho,
                           const char *path, int append);
 

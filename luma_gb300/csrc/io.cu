@@ -58,6 +58,7 @@ struct Snapshot {
     double dt = 0, dh = 0, omega = 0;
     std::vector<int> typ;
     std::vector<double> x, y, z, f, fnew, u, rho;
+    std::vector<double> rho_ta, ui_ta, uiuj_ta;  // empty without time averages
 };
 
 void lattice_c(int Q, int v, int c[3]) {
@@ -133,6 +134,25 @@ int write_lite(const Snapshot &s, const std::string &dir, double tval, int prec,
                 if (s.dims != 3) o.raw(zero);
                 for (int v = 0; v < s.Q; ++v) o.fixed(s.f[v + id * s.Q], prec);
                 for (int v = 0; v < s.Q; ++v) o.fixed(s.fnew[v + id * s.Q], prec);
+                if (!s.rho_ta.empty()) {
+                    // the time-averaged columns (:764-791): rho, u (a zero
+                    // z-column in 2D), then the u u products padded to six
+                    const int npq = 3 * s.dims - 3;
+                    const double *uu = &s.uiuj_ta[id * npq];
+                    o.fixed(s.rho_ta[id], prec);
+                    for (int d = 0; d < s.dims; ++d) o.fixed(s.ui_ta[id * s.dims + d], prec);
+                    if (s.dims != 3) o.raw(zero);
+                    o.fixed(uu[0], prec);
+                    o.fixed(uu[1], prec);
+                    if (s.dims == 3) {
+                        for (int q = 2; q < 6; ++q) o.fixed(uu[q], prec);
+                    } else {
+                        o.raw(zero);
+                        o.fixed(uu[2], prec);
+                        o.raw(zero);
+                        o.raw(zero);
+                    }
+                }
                 o.raw("\n");
                 ok = o.flush();
             }
@@ -186,6 +206,16 @@ int from_desc(const luma_grid_desc *d, const double *f, const double *fnew, cons
     return LUMA_OK;
 }
 
+int set_averages(Snapshot &s, const double *rho_ta, const double *ui_ta, const double *uiuj_ta) {
+    if (!rho_ta && !ui_ta && !uiuj_ta) return LUMA_OK;
+    if (!rho_ta || !ui_ta || !uiuj_ta) return luma_set_error(LUMA_E_INVALID, "writer: give all three time averages");
+    const size_t n = (size_t)s.N * s.M * s.K;
+    s.rho_ta.assign(rho_ta, rho_ta + n);
+    s.ui_ta.assign(ui_ta, ui_ta + n * s.dims);
+    s.uiuj_ta.assign(uiuj_ta, uiuj_ta + n * (3 * s.dims - 3));
+    return LUMA_OK;
+}
+
 // Device -> host snapshot of one grid (reference layout, FP64).  fNew is the
 // other population buffer of the two-buffer path (the state before the
 // latest step, as the reference's fNew holds after its swap); the in-place
@@ -203,6 +233,12 @@ int take(luma_gpu_grid *g, Snapshot &s) {
     s.rho.resize(g->n);
     int rc = luma_gpu_download_state(g, s.f.data(), s.u.data(), s.rho.data(), nullptr);
     if (rc) return rc;
+    if (g->tav) {
+        s.rho_ta.resize(g->n);
+        s.ui_ta.resize(g->n * d.dims);
+        s.uiuj_ta.resize(g->n * (3 * d.dims - 3));
+        if ((rc = luma_gpu_download_time_averages(g, s.rho_ta.data(), s.ui_ta.data(), s.uiuj_ta.data()))) return rc;
+    }
     if (g->bulk) {
         s.fnew = s.f;
         return LUMA_OK;
@@ -306,11 +342,13 @@ int luma_gpu_io_wait(luma_gpu_grid *root) {
 }
 
 int luma_io_lite_write(const luma_grid_desc *desc, const double *f, const double *fnew, const double *u,
-                       const double *rho, const char *dir, double tval, int precision, int rank) {
+                       const double *rho, const double *rho_ta, const double *ui_ta, const double *uiuj_ta,
+                       const char *dir, double tval, int precision, int rank) {
     if (!dir || precision < 0 || precision > 30)
         return luma_set_error(LUMA_E_INVALID, "luma_io_lite_write: null directory or precision outside 0..30");
     Snapshot s;
     if (int rc = from_desc(desc, f, fnew, u, rho, s)) return rc;
+    if (int rc = set_averages(s, rho_ta, ui_ta, uiuj_ta)) return rc;
     return write_lite(s, dir, tval, precision, rank);
 }
 

@@ -67,8 +67,8 @@ def lib() -> C.CDLL:
         L.luma_gpu_io_lite.argtypes = [vp, C.c_char_p, C.c_double, C.c_int, C.c_int]
         L.luma_gpu_io_restart.argtypes = [vp, C.c_char_p, C.c_int]
         L.luma_gpu_io_wait.argtypes = [vp]
-        L.luma_io_lite_write.argtypes = [C.POINTER(A.GridDesc), dp, dp, dp, dp, C.c_char_p, C.c_double, C.c_int,
-                                         C.c_int]
+        L.luma_io_lite_write.argtypes = [C.POINTER(A.GridDesc), dp, dp, dp, dp, dp, dp, dp, C.c_char_p, C.c_double,
+                                         C.c_int, C.c_int]
         L.luma_io_restart_write.argtypes = [C.POINTER(A.GridDesc), dp, dp, dp, C.c_char_p, C.c_int]
         if L.luma_gpu_abi_version() != A.ABI_VERSION:
             raise RuntimeError("luma_gb300 library ABI version mismatch")
@@ -242,9 +242,12 @@ class GpuGrid:
         return b.value
 
 
-def write_io_lite(desc, f, fnew, u, rho, directory: str, tval: float, precision: int = 10, rank: int = 0) -> None:
-    """The io_lite format from host arrays (reference layout) of one grid."""
-    arr = [np.ascontiguousarray(x, dtype=np.float64) if x is not None else None for x in (f, fnew, u, rho)]
+def write_io_lite(desc, f, fnew, u, rho, directory: str, tval: float, precision: int = 10, rank: int = 0,
+                  averages: dict | None = None) -> None:
+    """The io_lite format from host arrays (reference layout) of one grid;
+    `averages` (keys rho, u, uu) adds the time-averaged columns."""
+    tav = (averages["rho"], averages["u"], averages["uu"]) if averages else (None, None, None)
+    arr = [np.ascontiguousarray(x, dtype=np.float64) if x is not None else None for x in (f, fnew, u, rho, *tav)]
     check(lib().luma_io_lite_write(C.byref(desc), *(A.dptr(x) for x in arr), directory.encode(), float(tval),
                                    precision, rank))
 

@@ -17,10 +17,14 @@ from oracle import oracle as O
 from tests.golden import runner as R
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REF = json.load(open(os.path.join(HERE, "golden", "io_refine_d2q9.json")))
+CASES_IO = ("refine_d2q9", "tavg_refine_d2q9")   # the second keeps time averages
 
 
-def oracle_files(tmp_path):
+def ref_of(case):
+    return json.load(open(os.path.join(HERE, "golden", f"io_{case}.json")))
+
+
+def oracle_files(tmp_path, REF):
     from luma_gb300 import gpu as G
     grids, levels = R.build_backend(REF["case"], lambda d, p: O.OracleGrid(d, p))
     grids[0].step(REF["steps"])
@@ -28,13 +32,17 @@ def oracle_files(tmp_path):
     for n, (g, lv) in enumerate(zip(grids, levels)):
         st = g.download()
         desc = lv.desc()
-        G.write_io_lite(desc, st["f"], g.fnew(), st["u"], st["rho"], str(tmp_path), REF["steps"], REF["precision"])
+        tav = g.time_averages() if lv.defs.time_averages else None
+        G.write_io_lite(desc, st["f"], g.fnew(), st["u"], st["rho"], str(tmp_path), REF["steps"], REF["precision"],
+                        averages=tav)
         G.write_io_restart(desc, st["f"], st["u"], st["rho"], restart, append=n > 0)
     return tmp_path
 
 
-def test_writers_reproduce_reference_files(tmp_path):
-    out = oracle_files(tmp_path)
+@pytest.mark.parametrize("case", CASES_IO)
+def test_writers_reproduce_reference_files(tmp_path, case):
+    REF = ref_of(case)
+    out = oracle_files(tmp_path, REF)
     for name, ref in REF["files"].items():
         data = open(os.path.join(out, name), "rb").read()
         assert len(data) == ref["bytes"], name
@@ -47,14 +55,16 @@ def _rows(path):
 
 
 @pytest.mark.gpu
-def test_gpu_snapshot_writers_match_oracle(tmp_path):
+@pytest.mark.parametrize("case", CASES_IO)
+def test_gpu_snapshot_writers_match_oracle(tmp_path, case):
     from luma_gb300 import _abi as A
     from luma_gb300.gpu import GpuGrid
+    REF = ref_of(case)
     ref_dir = tmp_path / "ref"
     gpu_dir = tmp_path / "gpu"
     ref_dir.mkdir()
     gpu_dir.mkdir()
-    oracle_files(ref_dir)
+    oracle_files(ref_dir, REF)
     gg, _ = R.build_backend(REF["case"], lambda d, p: GpuGrid(d, p), A.PREC_FP64)
     gg[0].step(REF["steps"])
     gg[0].io_lite(str(gpu_dir), REF["steps"], REF["precision"])
