@@ -114,7 +114,6 @@ __device__ __forceinline__ unsigned long long mag_bits(double v) {
 
 __device__ void lu_solve_block(double *A, int lda, int off, int n, int *ipiv, double *x) {
 #define AC(r, c) A[(size_t)(off + (c)) * lda + (off + (r))]
-    __shared__ int nnz, nnc;
     __shared__ int nzr[512], nzc[512];
     __shared__ int lim[512];
     __shared__ double xs[512];
@@ -141,23 +140,35 @@ __device__ void lu_solve_block(double *A, int lda, int off, int n, int *ipiv, do
                     AC(k, c) = AC(p, c);
                     AC(p, c) = t;
                 }
-            if (lane == 0) {
-                nnz = 0;
-                nnc = 0;
-            }
             __syncwarp();
+            // rows with a non-zero multiplier and columns with a non-zero
+            // pivot-row entry, listed by warp ballots (every lane keeps the
+            // counts)
             const double inv = 1.0 / AC(k, k);
-            for (int r = k + 1 + lane; r < n; r += 32) {
-                const double m = AC(r, k) * inv;
-                AC(r, k) = m;
-                if (!is_zero(m)) nzr[atomicAdd(&nnz, 1)] = r;
+            const unsigned below = (1u << lane) - 1u;
+            int cr = 0, cc = 0;
+            for (int r0 = k + 1; r0 < n; r0 += 32) {
+                const int r = r0 + lane;
+                bool nz = false;
+                if (r < n) {
+                    const double m = AC(r, k) * inv;
+                    AC(r, k) = m;
+                    nz = !is_zero(m);
+                }
+                const unsigned b = __ballot_sync(0xffffffffu, nz);
+                if (nz) nzr[cr + __popc(b & below)] = r;
+                cr += __popc(b);
             }
-            for (int c = k + 1 + lane; c < n; c += 32)
-                if (!is_zero(AC(k, c))) nzc[atomicAdd(&nnc, 1)] = c;
+            for (int c0 = k + 1; c0 < n; c0 += 32) {
+                const int c = c0 + lane;
+                const bool nz = c < n && !is_zero(AC(k, c));
+                const unsigned b = __ballot_sync(0xffffffffu, nz);
+                if (nz) nzc[cc + __popc(b & below)] = c;
+                cc += __popc(b);
+            }
             __syncwarp();
             // the rank-1 update over (row, column) pairs with a non-zero
             // multiplier and a non-zero pivot-row entry, one pair per lane
-            const int cr = nnz, cc = nnc;
             for (int t = lane; t < cr * cc; t += 32) {
                 const int r = nzr[t % cr], c = nzc[t / cr];
                 AC(r, c) -= AC(r, k) * AC(k, c);
