@@ -1094,6 +1094,18 @@ static void lu_solve_t(int n, const double *a, int lda, const int *ipiv, double 
 #undef A_
 }
 
+/* The dense solver of the epsilon and FEM systems as a test entry: solves
+ * A x = b for a row-major A (destroyed) with b in x, the way
+ * GridUtils::solveLinearSystem (src/GridUtils.cpp:356-395) drives LAPACK
+ * (dgetrf on the transposed view, dgetrs with trans = 'T'). */
+int oracle_lu_solve_rowmajor(int n, double *A, double *x) {
+    int *ipiv = (int *)malloc(sizeof(int) * (size_t)(n > 0 ? n : 1));
+    lu_factor(n, A, n, ipiv);
+    lu_solve_t(n, A, n, ipiv, x);
+    free(ipiv);
+    return 0;
+}
+
 /* ibm_findEpsilon (:773-920) + GridUtils::solveLinearSystem (src/GridUtils.cpp:356-395). */
 static void find_epsilon(ibm_body *b) {
     const int n = b->nm, D = b->owner->D;

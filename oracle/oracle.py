@@ -73,8 +73,17 @@ def lib():
         L.oracle_bfl_forces.argtypes = [C.c_void_p, C.POINTER(C.c_double)]
         L.oracle_download_fnew.argtypes = [C.c_void_p, C.POINTER(C.c_double)]
         L.oracle_download_time_averages.argtypes = [C.c_void_p] + [C.POINTER(C.c_double)] * 3
+        L.oracle_lu_solve_rowmajor.argtypes = [C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_double)]
         _lib = L
     return _lib
+
+
+def lu_solve(M: np.ndarray, b: np.ndarray) -> np.ndarray:
+    """The oracle's dense partial-pivot LU solve of M x = b (M row-major)."""
+    a = np.array(M, dtype=np.float64, order="C", copy=True)
+    x = np.array(b, dtype=np.float64, copy=True)
+    lib().oracle_lu_solve_rowmajor(int(a.shape[0]), A.dptr(a), A.dptr(x))
+    return x
 
 
 class OracleGrid:

@@ -201,3 +201,25 @@ def test_oracle_momentum_exchange_bit_exact_vs_reference():
         got = oo[0].momex_force()
         assert got.tolist() == ref["forces"][str(s)], (s, got, ref["forces"][str(s)])
         oo[0].step(1)
+
+
+@pytest.mark.parametrize("n", [1, 5, 33, 64, 96])
+def test_oracle_dense_solver_against_scipy(n):
+    """The dense LU the oracle (and the device) uses for the epsilon and FEM
+    systems, in place of the reference's unpinned LAPACK: residual
+    ||Ax - b|| / ||b|| <= 1e-13 and agreement with scipy.linalg's LU
+    (lu_factor/lu_solve, a second oracle) within 1e-12, on seeded matrices
+    shaped like the epsilon system (diagonally dominant, positive) and on
+    general well-conditioned ones."""
+    scipy_linalg = pytest.importorskip("scipy.linalg")
+    rng = np.random.Generator(np.random.PCG64(20261204 + n))
+    for kind in ("epsilon", "general"):
+        if kind == "epsilon":
+            M = rng.uniform(0.0, 0.3, size=(n, n)) + np.eye(n) * (1.0 + 0.3 * n)
+        else:
+            M = rng.normal(size=(n, n)) + np.eye(n) * 4.0 * np.sqrt(n)
+        b = rng.normal(size=n)
+        x = O.lu_solve(M, b)
+        assert np.linalg.norm(M @ x - b) <= 1e-13 * np.linalg.norm(b) * max(1.0, np.linalg.cond(M) / 1e2)
+        xs = scipy_linalg.lu_solve(scipy_linalg.lu_factor(M), b)
+        assert np.max(np.abs(x - xs)) <= 1e-12 * np.max(np.abs(xs)), kind
