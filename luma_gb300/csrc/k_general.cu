@@ -18,6 +18,8 @@
 // followed by a swap of the two population buffers (:159).
 #include <cuda_runtime.h>
 
+#include <type_traits>
+
 #include "device.cuh"
 #include "grid.hpp"
 #include "kernels.hpp"
@@ -173,7 +175,9 @@ __device__ __forceinline__ void stream_site(const StepArgs &a, const int8_t *wal
 // _LBM_macro_opt (:800-891): density and velocity of fluid-like sites from
 // the streamed populations, + 0.5*F when forcing; the 3D reference adds the
 // z half-force to x (:833) unless LUMA_FLAG_FIX_MACRO3D.
-template <int Q, class P, bool STORE = true>
+// TAV: the kernel carries the running-mean update (a compile-time choice:
+// the lean interior kernels do without its registers).
+template <int Q, class P, bool STORE = true, bool TAV = true>
 __device__ __forceinline__ void macro_site(const StepArgs &a, int i, int j, int k, int id, int type,
                                            const typename P::R *fn, typename P::R &rho, typename P::R &drho,
                                            typename P::R &ux, typename P::R &uy, typename P::R &uz,
@@ -227,7 +231,7 @@ __device__ __forceinline__ void macro_site(const StepArgs &a, int i, int j, int 
     }
     // time-averaged quantities (:895-917), tav_reps times (an IB support
     // site is re-macroed once per marker it supports)
-    if (a.tav_rho) {
+    if (TAV && a.tav_rho) {
         const double t = (double)a.tav_t, t1 = (double)(a.tav_t + 1);
         const double uu[3] = {double(ux), double(uy), double(uz)};
         for (int rep = 0; rep < tav_reps; ++rep) {
@@ -414,7 +418,7 @@ __device__ __forceinline__ void collide_site(const StepArgs &a, int id, typename
     }
 }
 
-template <int Q, class P>
+template <int Q, class P, bool TAV>
 __device__ __forceinline__ void stream_macro_site(const StepArgs &a, const int8_t *wall, int id) {
     using R = typename P::R;
     const int type = a.typ[id];
@@ -428,7 +432,7 @@ __device__ __forceinline__ void stream_macro_site(const StepArgs &a, const int8_
     R fn[Q];
     stream_site<Q, P>(a, wall, i, j, k, id, type, fn);
     R rho, drho, ux, uy, uz;
-    macro_site<Q, P>(a, i, j, k, id, type, fn, rho, drho, ux, uy, uz);
+    macro_site<Q, P, true, TAV>(a, i, j, k, id, type, fn, rho, drho, ux, uy, uz);
     const size_t n = (size_t)a.ncell;
     if (a.ibm_split && a.defer && !a.defer[id] && type != LUMA_SITE_TL_TO_COARSER) {
         // IBM grid, site outside every support: its force is the reset's zero,
@@ -448,17 +452,17 @@ __device__ __forceinline__ void stream_macro_site(const StepArgs &a, const int8_
     for (int v = 0; v < Q; ++v) st<P>(a.fNew, (size_t)v * n + id, fn[v]);
 }
 
-template <int Q, class P>
+template <int Q, class P, bool TAV>
 __global__ void __launch_bounds__(128) k_stream_macro(StepArgs a, const int8_t *wall) {
     const int id = blockIdx.x * blockDim.x + threadIdx.x;
-    if (id < a.ncell) stream_macro_site<Q, P>(a, wall, id);
+    if (id < a.ncell) stream_macro_site<Q, P, TAV>(a, wall, id);
 }
 
 // The same over the listed sites (those the interior kernel leaves).
-template <int Q, class P>
+template <int Q, class P, bool TAV>
 __global__ void __launch_bounds__(128) k_stream_macro_list(StepArgs a, const int8_t *wall, const int *ids, int nids) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t < nids) stream_macro_site<Q, P>(a, wall, ids[t]);
+    if (t < nids) stream_macro_site<Q, P, TAV>(a, wall, ids[t]);
 }
 
 // Interior fluid sites (every pull source a fluid site, so every direction
@@ -468,7 +472,7 @@ __global__ void __launch_bounds__(128) k_stream_macro_list(StepArgs a, const int
 // split, deferred sites stop after the macroscopic step (phase C collides
 // them); the others carry the reset's zero force, whose Guo term and half
 // force add exact zeros, so their force is not read.
-template <int Q, class P, int COLL>
+template <int Q, class P, int COLL, bool TAV>
 __global__ void __launch_bounds__(128) k_interior(StepArgs a, const uint8_t *fast) {
     using L = Lattice<Q>;
     using R = typename P::R;
@@ -494,8 +498,8 @@ __global__ void __launch_bounds__(128) k_interior(StepArgs a, const uint8_t *fas
     R rho, drho, ux, uy, uz;
     // u and rho go to memory where something reads them later in the step
     // or after it (macro_out) or the IBM pass needs them (deferred sites)
-    if (a.macro_out || deferred) macro_site<Q, P, true>(b, i, j, k, id, LUMA_SITE_FLUID, fn, rho, drho, ux, uy, uz);
-    else macro_site<Q, P, false>(b, i, j, k, id, LUMA_SITE_FLUID, fn, rho, drho, ux, uy, uz);
+    if (a.macro_out || deferred) macro_site<Q, P, true, TAV>(b, i, j, k, id, LUMA_SITE_FLUID, fn, rho, drho, ux, uy, uz);
+    else macro_site<Q, P, false, TAV>(b, i, j, k, id, LUMA_SITE_FLUID, fn, rho, drho, ux, uy, uz);
     if (deferred || (a.ibm_split && a.fOut != a.fNew)) {
 #pragma unroll
         for (int v = 0; v < Q; ++v) st<P>(a.fNew, (size_t)v * n + id, fn[v]);
@@ -898,15 +902,22 @@ template <int Q, class P>
 cudaError_t launch_general_phaseA(const StepArgs &a, const int8_t *wall, const uint8_t *fast, const int *gen_ids,
                                   int ngen, cudaStream_t s) {
     const int bs = 128;
+    const bool tav = a.tav_rho != nullptr;
     if (!fast) {
-        k_stream_macro<Q, P><<<(a.ncell + bs - 1) / bs, bs, 0, s>>>(a, wall);
+        if (tav) k_stream_macro<Q, P, true><<<(a.ncell + bs - 1) / bs, bs, 0, s>>>(a, wall);
+        else k_stream_macro<Q, P, false><<<(a.ncell + bs - 1) / bs, bs, 0, s>>>(a, wall);
         return cudaGetLastError();
     }
     const int nb = (a.ncell + bs - 1) / bs;
-    if (a.collision == LUMA_COLL_KBC) k_interior<Q, P, LUMA_COLL_KBC><<<nb, bs, 0, s>>>(a, fast);
-    else if (a.collision == LUMA_COLL_BGK_SMAG) k_interior<Q, P, LUMA_COLL_BGK_SMAG><<<nb, bs, 0, s>>>(a, fast);
-    else k_interior<Q, P, LUMA_COLL_BGK><<<nb, bs, 0, s>>>(a, fast);
-    if (ngen > 0) k_stream_macro_list<Q, P><<<(ngen + bs - 1) / bs, bs, 0, s>>>(a, wall, gen_ids, ngen);
+    auto interior = [&](auto tv) {
+        constexpr bool T = decltype(tv)::value;
+        if (a.collision == LUMA_COLL_KBC) k_interior<Q, P, LUMA_COLL_KBC, T><<<nb, bs, 0, s>>>(a, fast);
+        else if (a.collision == LUMA_COLL_BGK_SMAG) k_interior<Q, P, LUMA_COLL_BGK_SMAG, T><<<nb, bs, 0, s>>>(a, fast);
+        else k_interior<Q, P, LUMA_COLL_BGK, T><<<nb, bs, 0, s>>>(a, fast);
+        if (ngen > 0) k_stream_macro_list<Q, P, T><<<(ngen + bs - 1) / bs, bs, 0, s>>>(a, wall, gen_ids, ngen);
+    };
+    if (tav) interior(std::true_type{});
+    else interior(std::false_type{});
     return cudaGetLastError();
 }
 template <int Q, class P>
