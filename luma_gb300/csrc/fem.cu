@@ -112,7 +112,13 @@ __device__ __forceinline__ unsigned long long mag_bits(double v) {
     return (unsigned long long)__double_as_longlong(v) & 0x7fffffffffffffffull;
 }
 
-__device__ void lu_solve_block(double *A, int lda, int off, int n, int *ipiv, double *x) {
+// `band`: no entry of the matrix lies more than `band` rows below or
+// columns right of the diagonal (n for a dense matrix).  Partial pivoting
+// keeps the multipliers of column k in rows k+1..k+band and the pivot row's
+// entries in columns up to k+2*band, so the scans stop there; the entries
+// they skip are exact zeros, which the dense elimination would leave as
+// they are.
+__device__ void lu_solve_block(double *A, int lda, int off, int n, int *ipiv, double *x, int band) {
 #define AC(r, c) A[(size_t)(off + (c)) * lda + (off + (r))]
     __shared__ int nzr[512], nzc[512];
     __shared__ int lim[512];
@@ -122,7 +128,8 @@ __device__ void lu_solve_block(double *A, int lda, int off, int n, int *ipiv, do
         for (int k = 0; k < n; ++k) {
             unsigned long long best = 0;
             int p = n;
-            for (int r = k + lane; r < n; r += 32) {
+            const int rend = min(n, k + band + 1), cend = min(n, k + 2 * band + 1);
+            for (int r = k + lane; r < rend; r += 32) {
                 const unsigned long long v = mag_bits(AC(r, k));
                 if (p == n || v > best) { best = v; p = r; }
             }
@@ -147,10 +154,10 @@ __device__ void lu_solve_block(double *A, int lda, int off, int n, int *ipiv, do
             const double inv = 1.0 / AC(k, k);
             const unsigned below = (1u << lane) - 1u;
             int cr = 0, cc = 0;
-            for (int r0 = k + 1; r0 < n; r0 += 32) {
+            for (int r0 = k + 1; r0 < rend; r0 += 32) {
                 const int r = r0 + lane;
                 bool nz = false;
-                if (r < n) {
+                if (r < rend) {
                     const double m = AC(r, k) * inv;
                     AC(r, k) = m;
                     nz = !is_zero(m);
@@ -159,9 +166,9 @@ __device__ void lu_solve_block(double *A, int lda, int off, int n, int *ipiv, do
                 if (nz) nzr[cr + __popc(b & below)] = r;
                 cr += __popc(b);
             }
-            for (int c0 = k + 1; c0 < n; c0 += 32) {
+            for (int c0 = k + 1; c0 < cend; c0 += 32) {
                 const int c = c0 + lane;
-                const bool nz = c < n && !is_zero(AC(k, c));
+                const bool nz = c < cend && !is_zero(AC(k, c));
                 const unsigned b = __ballot_sync(0xffffffffu, nz);
                 if (nz) nzc[cc + __popc(b & below)] = c;
                 cc += __popc(b);
@@ -403,7 +410,8 @@ __global__ void k_fem_dynamic(FemKernelArgs a) {
         }
         for (int i = threadIdx.x; i < nd; i += blockDim.x) a.delU[d0 + i] = a.Fv[d0 + i];
         __syncthreads();
-        lu_solve_block(K, nd, bc, nd - bc, ipiv, a.delU + d0 + bc);
+        // an element couples the 6 DOFs of its two nodes: half-bandwidth 5
+        lu_solve_block(K, nd, bc, nd - bc, ipiv, a.delU + d0 + bc, 5);
         for (int i = threadIdx.x; i < bc; i += blockDim.x) a.delU[d0 + i] = 0.0;
         __syncthreads();
         for (int i = threadIdx.x; i < nd; i += blockDim.x) a.U[d0 + i] = a.U[d0 + i] + a.delU[d0 + i];
@@ -600,7 +608,7 @@ __global__ void k_flex_support(FemKernelArgs a) {
     __shared__ int ipiv[512];
     for (int m = threadIdx.x; m < nmk; m += blockDim.x) x.eps[mk0 + m] = 1.0;
     __syncthreads();
-    lu_solve_block(A, nmk, 0, nmk, ipiv, x.eps + mk0);
+    lu_solve_block(A, nmk, 0, nmk, ipiv, x.eps + mk0, nmk);
 }
 
 // max over flexible markers of |U - U_km1| / (L_UX0 dt/dh)  (ibm_checkVelDiff)
