@@ -6,6 +6,7 @@ import os
 import numpy as np
 import pytest
 
+from luma_gb300 import _abi as A
 from luma_gb300 import case as hostcase
 from oracle import oracle as O
 from tests.golden import cases as CASES
@@ -223,3 +224,26 @@ def test_oracle_dense_solver_against_scipy(n):
         assert np.linalg.norm(M @ x - b) <= 1e-13 * np.linalg.norm(b) * max(1.0, np.linalg.cond(M) / 1e2)
         xs = scipy_linalg.lu_solve(scipy_linalg.lu_factor(M), b)
         assert np.max(np.abs(x - xs)) <= 1e-12 * np.max(np.abs(xs)), kind
+
+
+def test_bfl_builder_large_circle_with_projection_reset():
+    """The circle set-up with the closure's projection count reset per
+    closure (the bench workload's option: the reference's own count doubles
+    per closure marker and never finishes a circle this size): every eBFL
+    site has a marker, every marker's voxel is eBFL, link distances lie in
+    [0, 1] or are -1, and the labelled ring is closed (every eBFL site has
+    an eBFL site among its 4 axis neighbours)."""
+    from luma_gb300 import bfl
+    d = hostcase.Definitions(dims=2, resolution=128, timestep=1.0 / 3200.0, bx=2.0, by=1.0, re=100, ux0=1.0,
+                             walls=(A.VELOCITY, A.EXTRAPOLATE_RIGHT, A.SOLID, A.SOLID, A.FLUID, A.FLUID))
+    l0 = hostcase.build_level0(d)
+    body = bfl.circle_body(l0, (0.5, 0.5, 0.0), 0.25, reset_projection=True)
+    typ = body.typ.reshape(l0.N, l0.M)
+    sm = body.site_marker.reshape(l0.N, l0.M)
+    assert np.array_equal(typ == A.BFL, sm >= 0)
+    q = body.q
+    assert np.all((q == -1.0) | ((q >= 0.0) & (q <= 1.0)))
+    assert (q >= 0).sum() > 0
+    for i, j in np.argwhere(typ == A.BFL):
+        nb = [typ[i + di, j + dj] == A.BFL for di, dj in ((1, 0), (-1, 0), (0, 1), (0, -1))]
+        assert any(nb), (i, j)
