@@ -98,6 +98,16 @@ void luma_bfl_free(luma_gpu_grid *g) {
     g->bfl = nullptr;
 }
 
+// The table pointers a captured step bakes in (a new body allocates new
+// tables, whatever address its state object gets).
+void luma_bfl_signature(const luma_gpu_grid *g, std::vector<uintptr_t> &sig) {
+    const BflState *b = g->bfl;
+    if (!b) return;
+    for (const void *p : {(const void *)b->rec, (const void *)b->mask, (const void *)b->first, (const void *)b->q,
+                          (const void *)b->kind, (const void *)b->val})
+        sig.push_back((uintptr_t)p);
+}
+
 void luma_bfl_args(const luma_gpu_grid *g, StepArgs &a) {
     const BflState *b = g->bfl;
     if (!b) return;

@@ -428,6 +428,7 @@ void tree_signature(const luma_gpu_grid *g, std::vector<uintptr_t> &s) {
     P(g->uxin); P(g->defer); P(g->defer_ids); P(g->fast); P(g->gen_ids); P(g->adj); P(g->bfl);
     V(g->cur); V(g->aa_odd); V(g->bulk); V(g->fuse); V(g->ngen); V(g->ndefer); V(g->nreg); V(g->nvelu);
     V(g->d.flags);
+    luma_bfl_signature(g, s);
     if (g->ibm) {
         const IbmDevice &d = g->ibm->dev;
         P(d.vel); P(d.eps); P(d.ds); P(d.area); P(d.F); P(d.irho); P(d.imom); P(d.moff); P(d.msite);

@@ -81,6 +81,7 @@ void luma_adj_free(luma_gpu_grid *g);
 // bfl.cu
 void luma_bfl_free(luma_gpu_grid *g);
 void luma_bfl_args(const luma_gpu_grid *g, luma::StepArgs &a);
+void luma_bfl_signature(const luma_gpu_grid *g, std::vector<uintptr_t> &sig);
 // io.cu
 void luma_io_free(luma_gpu_grid *g);
 // fem.cu
