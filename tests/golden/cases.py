@@ -25,6 +25,12 @@ CASES = {
                          ux0=1.0, parabolic_inlet=True, regularised=True, velocity_ramp=0.5,
                          walls=(V, P, S, S, F, F)),
         steps=(10, 1000), store_f=(10, 1000)),
+    # D3Q19 regularised inlet (ramped) and pressure outlet meeting solid
+    # walls in edges (extrapolated density).
+    "reg_d3q19": dict(
+        defs=Definitions(dims=3, resolution=12, timestep=1.0 / 300.0, bx=2.0, by=1.0, bz=1.0, re=20,
+                         ux0=1.0, regularised=True, velocity_ramp=0.2, walls=(V, P, S, S, F, F)),
+        steps=(10, 200), store_f=(10,)),
     # D2Q9 forced-equilibrium uniform inlet with a velocity ramp.
     "ramp_d2q9": dict(
         defs=Definitions(dims=2, resolution=24, timestep=1.0 / 480.0, bx=2.0, by=1.0, re=40,
