@@ -1094,6 +1094,45 @@ static void lu_solve_t(int n, const double *a, int lda, const int *ipiv, double 
 #undef A_
 }
 
+/* Test entries for unit known-answer checks: the lattice tables, the
+ * Roma delta kernel (ibm_deltaKernel, src/ObjectManager_ops_ibm.cpp:
+ * 255-272) and the Guo forcing of one site (_LBM_forceGrid_opt, :928-990). */
+int oracle_lattice(int Q, int *c, double *w, int *opp, int *refl) {
+    const int (*cc)[3];
+    const double *ww;
+    const int *oo, *rr;
+    if (Q == 9) { cc = C9; ww = W9; oo = OPP9; rr = &REF9[0][0]; }
+    else if (Q == 19) { cc = C19; ww = W19; oo = OPP19; rr = &REF19[0][0]; }
+    else if (Q == 27) { cc = C27; ww = W27; oo = OPP27; rr = &REF27[0][0]; }
+    else { set_err("unsupported lattice"); return -1; }
+    for (int v = 0; v < Q; ++v) {
+        for (int d = 0; d < 3; ++d) c[3 * v + d] = cc[v][d];
+        w[v] = ww[v];
+        opp[v] = oo[v];
+        for (int p = 0; p < 3; ++p) refl[p * Q + v] = rr[p * Q + v];
+    }
+    return 0;
+}
+
+double oracle_delta(double r, double dilation) { return delta_kernel(r, dilation); }
+
+int oracle_guo(int Q, int dims, double omega, const double *u, const double *F, double *out) {
+    oracle_grid g;
+    memset(&g, 0, sizeof g);
+    g.Q = Q;
+    g.D = dims;
+    if (Q == 9) { g.c = C9; g.w = W9; }
+    else if (Q == 19) { g.c = C19; g.w = W19; }
+    else if (Q == 27) { g.c = C27; g.w = W27; }
+    else { set_err("unsupported lattice"); return -1; }
+    g.d.omega = omega;
+    g.force_i = out;
+    g.u = (double *)u;
+    g.force_xyz = (double *)F;
+    force_grid(&g, 0);
+    return 0;
+}
+
 /* The dense solver of the epsilon and FEM systems as a test entry: solves
  * A x = b for a row-major A (destroyed) with b in x, the way
  * GridUtils::solveLinearSystem (src/GridUtils.cpp:356-395) drives LAPACK

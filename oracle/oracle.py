@@ -74,8 +74,38 @@ def lib():
         L.oracle_download_fnew.argtypes = [C.c_void_p, C.POINTER(C.c_double)]
         L.oracle_download_time_averages.argtypes = [C.c_void_p] + [C.POINTER(C.c_double)] * 3
         L.oracle_lu_solve_rowmajor.argtypes = [C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_double)]
+        L.oracle_lattice.argtypes = [C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_double), C.POINTER(C.c_int),
+                                     C.POINTER(C.c_int)]
+        L.oracle_delta.restype = C.c_double
+        L.oracle_delta.argtypes = [C.c_double, C.c_double]
+        L.oracle_guo.argtypes = [C.c_int, C.c_int, C.c_double] + [C.POINTER(C.c_double)] * 3
         _lib = L
     return _lib
+
+
+def lattice(Q: int) -> dict:
+    """The oracle's lattice tables: c (Q, 3), w (Q,), opp (Q,), refl (3, Q)."""
+    c = np.zeros(3 * Q, dtype=np.int32)
+    w = np.zeros(Q)
+    opp = np.zeros(Q, dtype=np.int32)
+    refl = np.zeros(3 * Q, dtype=np.int32)
+    ip = C.POINTER(C.c_int)
+    if lib().oracle_lattice(Q, c.ctypes.data_as(ip), A.dptr(w), opp.ctypes.data_as(ip), refl.ctypes.data_as(ip)):
+        raise RuntimeError(lib().oracle_last_error().decode())
+    return {"c": c.reshape(Q, 3), "w": w, "opp": opp, "refl": refl.reshape(3, Q)}
+
+
+def delta(r: float, dilation: float = 1.0) -> float:
+    return lib().oracle_delta(float(r), float(dilation))
+
+
+def guo(Q: int, dims: int, omega: float, u, F) -> np.ndarray:
+    """Guo forcing terms F_i of one site with velocity u and force F."""
+    u = np.ascontiguousarray(u, dtype=np.float64)
+    F = np.ascontiguousarray(F, dtype=np.float64)
+    out = np.zeros(Q)
+    lib().oracle_guo(Q, dims, float(omega), A.dptr(u), A.dptr(F), A.dptr(out))
+    return out
 
 
 def lu_solve(M: np.ndarray, b: np.ndarray) -> np.ndarray:

@@ -247,3 +247,57 @@ def test_bfl_builder_large_circle_with_projection_reset():
     for i, j in np.argwhere(typ == A.BFL):
         nb = [typ[i + di, j + dj] == A.BFL for di, dj in ((1, 0), (-1, 0), (0, 1), (0, -1))]
         assert any(nb), (i, j)
+
+
+@pytest.mark.parametrize("Q,dims", [(9, 2), (19, 3), (27, 3)])
+def test_lattice_tables_known_answers(Q, dims):
+    """Lattice tables (src/stdafx.cpp:29-153, src/GridUtils.cpp:31-69):
+    opposites negate c, reflections negate one component, the weights'
+    moments are 1, 0 and cs^2 I (cs^2 = 1/3), and the host set-up's tables
+    are the oracle's."""
+    L = O.lattice(Q)
+    c, w, opp, refl = L["c"], L["w"], L["opp"], L["refl"]
+    for v in range(Q):
+        assert np.array_equal(c[opp[v]], -c[v])
+        for p in range(dims):
+            want = c[v].copy()
+            want[p] = -want[p]
+            assert np.array_equal(c[refl[p, v]], want), (p, v)
+    assert abs(w.sum() - 1.0) <= 1e-15
+    assert np.all(np.abs(w @ c) <= 1e-16)
+    second = np.einsum("v,va,vb->ab", w, c.astype(float), c.astype(float))
+    assert np.allclose(second[:dims, :dims], np.eye(dims) / 3.0, rtol=0, atol=1e-15)
+    hc, hw = hostcase.lattice(dims, Q)
+    assert np.array_equal(np.asarray(hc), c) and np.array_equal(np.asarray(hw), w)
+
+
+def test_delta_kernel_known_answers():
+    """Roma et al. 3-point kernel (ibm_deltaKernel): value 2/3 at 0, support
+    |r| <= 1.5, symmetric, and for any offset the integer shifts sum to 1
+    (partition of unity), have zero first moment and squares summing to 1/2;
+    the dilation scales the argument."""
+    assert O.delta(0.0) == pytest.approx(2.0 / 3.0, abs=1e-16)
+    assert O.delta(1.5) == 0.0 and O.delta(1.6) == 0.0
+    for r in np.linspace(-0.5, 0.5, 101):
+        vals = np.array([O.delta(r - j) for j in range(-3, 4)])
+        shifts = r - np.arange(-3, 4)
+        assert abs(vals.sum() - 1.0) <= 1e-14, r
+        assert abs((shifts * vals).sum()) <= 1e-14, r
+        assert abs((vals ** 2).sum() - 0.5) <= 1e-14, r
+        assert O.delta(r) == O.delta(-r)
+    assert O.delta(0.6, 2.0) == O.delta(0.3, 1.0)
+
+
+@pytest.mark.parametrize("Q,dims", [(9, 2), (19, 3), (27, 3)])
+def test_guo_forcing_moments(Q, dims):
+    """Guo forcing of one site (_LBM_forceGrid_opt): no mass source and a
+    momentum source of (1 - omega/2) F."""
+    rng = np.random.Generator(np.random.PCG64(7 + Q))
+    L = O.lattice(Q)
+    for omega in (0.8, 1.5, 1.9):
+        u = rng.uniform(-0.05, 0.05, size=dims)
+        F = rng.uniform(-1e-3, 1e-3, size=dims)
+        Fi = O.guo(Q, dims, omega, u, F)
+        assert abs(Fi.sum()) <= 1e-18
+        mom = Fi @ L["c"][:, :dims].astype(float)
+        assert np.allclose(mom, (1.0 - 0.5 * omega) * F, rtol=1e-13, atol=1e-19)
