@@ -285,6 +285,15 @@ int luma_io_lite_write(const luma_grid_desc *desc, const double *f, const double
                        const char *dir, double tval, int precision, int rank);
 int luma_io_restart_write(const luma_grid_desc *desc, const double *f, const double *u, const double *rho,
                           const char *path, int append);
+/* GridObj::io_restart(eRead) (src/GridObj_ops_io.cpp:490-580) on host
+ * arrays: descs[0..ngrids) are the tree's grids with level 0 first (labels
+ * not needed; positions, dt, dh, omega, global_edges used), f/u/rho their
+ * reference-layout state, overwritten at every site the file names (then
+ * upload with luma_gpu_upload_state).  As the reference does, each line's
+ * f = feq (1 + dt f_neq / omega) takes feq from level 0's rho and u at the
+ * level-0 index of the line's (i, j, k), and level 0's omega. */
+int luma_io_restart_read(const char *path, int ngrids, const luma_grid_desc *const *descs, double *const *f,
+                         double *const *u, double *const *rho);
 
 /* ---- discrete adjoint of the time-averaged drag ------------------------- */
 /* No counterpart in the reference (its objective is the drag that

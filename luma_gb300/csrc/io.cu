@@ -27,7 +27,9 @@
 #include <cerrno>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
+#include <fstream>
 #include <memory>
 #include <mutex>
 #include <string>
@@ -350,6 +352,70 @@ int luma_io_lite_write(const luma_grid_desc *desc, const double *f, const double
     if (int rc = from_desc(desc, f, fnew, u, rho, s)) return rc;
     if (int rc = set_averages(s, rho_ta, ui_ta, uiuj_ta)) return rc;
     return write_lite(s, dir, tval, precision, rank);
+}
+
+// GridObj::io_restart(eRead) (:490-580) called on level 0: every line of
+// the file sets u (dimensionless -> lattice: u dt / dh), rho and f of the
+// site of its (level, region) grid that encloses its position, with
+// f = feq (1 + dt f_neq / omega).  As the reference does, feq is level 0's
+// equilibrium at the index (k + j K0 + i K0 M0) with level 0's rho and u,
+// and omega is level 0's, whatever grid the line belongs to.  Lines whose
+// position lies outside level 0's domain, or off their grid, are skipped.
+int luma_io_restart_read(const char *path, int ngrids, const luma_grid_desc *const *descs, double *const *f,
+                         double *const *u, double *const *rho) {
+    if (!path || ngrids <= 0 || !descs || !f || !u || !rho)
+        return luma_set_error(LUMA_E_INVALID, "luma_io_restart_read: null argument");
+    for (int g = 0; g < ngrids; ++g)
+        if (!descs[g] || !f[g] || !u[g] || !rho[g] || !descs[g]->xpos || !descs[g]->ypos || !descs[g]->zpos)
+            return luma_set_error(LUMA_E_INVALID, "luma_io_restart_read: grid %d lacks arrays or positions", g);
+    const luma_grid_desc &L0 = *descs[0];
+    if (L0.level != 0) return luma_set_error(LUMA_E_INVALID, "luma_io_restart_read: descs[0] must be level 0");
+    std::ifstream in(path);
+    if (!in.is_open()) return luma_set_error(LUMA_E_INVALID, "io_restart: cannot open %s", path);
+    const int D = L0.dims, Q = L0.Q;
+    const double *E = L0.global_edges;
+    std::string line;
+    while (std::getline(in, line)) {
+        const char *p = line.c_str();
+        char *end;
+        auto num = [&](double &v) -> bool {
+            v = std::strtod(p, &end);
+            if (end == p) return false;
+            p = end;
+            return true;
+        };
+        double lv, rg, x, y, z;
+        if (!num(lv) || !num(rg) || !num(x) || !num(y) || !num(z)) continue;  // blank or short line
+        int gi = -1;
+        for (int g = 0; g < ngrids; ++g)
+            if (descs[g]->level == (int)lv && descs[g]->region == (int)rg) gi = g;
+        if (gi < 0)
+            return luma_set_error(LUMA_E_INVALID, "io_restart: no grid level %d region %d", (int)lv, (int)rg);
+        const luma_grid_desc &G = *descs[gi];
+        // GridUtils::isOnThisRank (serial): inside level 0's edges, then the
+        // enclosing voxel of the line's grid must be on that grid
+        if (!(E[0] <= x && x < E[1] && E[2] <= y && y < E[3] && (D != 3 || (E[4] <= z && z < E[5])))) continue;
+        const double sx = G.level == 0 ? E[0] : G.xpos[0] - 0.5 * G.dh;
+        const double sy = G.level == 0 ? E[2] : G.ypos[0] - 0.5 * G.dh;
+        const double sz = G.level == 0 ? E[4] : G.zpos[0] - 0.5 * G.dh;
+        const int i = (int)std::floor((x - sx) / G.dh), j = (int)std::floor((y - sy) / G.dh);
+        const int k = D == 3 ? (int)std::floor((z - sz) / G.dh) : 0;
+        if (i < 0 || i >= G.N || j < 0 || j >= G.M || k < 0 || k >= G.K) continue;
+        const size_t gid = (size_t)k + (size_t)j * G.K + (size_t)i * G.K * G.M;
+        const size_t id0 = (size_t)k + (size_t)j * L0.K + (size_t)i * L0.K * L0.M;  // level 0's strides
+        double vals[3 + 1 + 27];
+        int nv = 0;
+        for (; nv < D + 1 + Q; ++nv)
+            if (!num(vals[nv])) break;
+        if (nv < D + 1 + Q) return luma_set_error(LUMA_E_INVALID, "io_restart: short line in %s", path);
+        for (int d = 0; d < D; ++d) u[gi][gid * D + d] = (vals[d] * G.dt) / G.dh;
+        rho[gi][gid] = vals[D];
+        for (int v = 0; v < Q; ++v) {
+            const double fe = feq(Q, D, v, rho[0][id0], &u[0][id0 * D]);
+            f[gi][gid * Q + v] = fe * (1 + (G.dt * vals[D + 1 + v]) / L0.omega);
+        }
+    }
+    return LUMA_OK;
 }
 
 int luma_io_restart_write(const luma_grid_desc *desc, const double *f, const double *u, const double *rho,

@@ -70,6 +70,8 @@ def lib() -> C.CDLL:
         L.luma_io_lite_write.argtypes = [C.POINTER(A.GridDesc), dp, dp, dp, dp, dp, dp, dp, C.c_char_p, C.c_double,
                                          C.c_int, C.c_int]
         L.luma_io_restart_write.argtypes = [C.POINTER(A.GridDesc), dp, dp, dp, C.c_char_p, C.c_int]
+        L.luma_io_restart_read.argtypes = [C.c_char_p, C.c_int, C.POINTER(C.POINTER(A.GridDesc)),
+                                           C.POINTER(dp), C.POINTER(dp), C.POINTER(dp)]
         if L.luma_gpu_abi_version() != A.ABI_VERSION:
             raise RuntimeError("luma_gb300 library ABI version mismatch")
         _lib = L
@@ -256,3 +258,18 @@ def write_io_restart(desc, f, u, rho, path: str, append: bool = False) -> None:
     """The io_restart format from host arrays (reference layout) of one grid."""
     arr = [np.ascontiguousarray(x, dtype=np.float64) for x in (f, u, rho)]
     check(lib().luma_io_restart_write(C.byref(desc), *(A.dptr(x) for x in arr), path.encode(), int(append)))
+
+
+def read_io_restart(path: str, descs, states) -> None:
+    """GridObj::io_restart(eRead) into host arrays: descs (level 0 first) and
+    states [{"f", "u", "rho"}] (float64, reference layout), overwritten in
+    place."""
+    n = len(descs)
+    darr = (C.POINTER(A.GridDesc) * n)(*[C.pointer(d) for d in descs])
+    for st in states:
+        for k in ("f", "u", "rho"):
+            assert st[k].dtype == np.float64 and st[k].flags["C_CONTIGUOUS"]
+    fp = (C.POINTER(C.c_double) * n)(*[A.dptr(st["f"]) for st in states])
+    up = (C.POINTER(C.c_double) * n)(*[A.dptr(st["u"]) for st in states])
+    rp = (C.POINTER(C.c_double) * n)(*[A.dptr(st["rho"]) for st in states])
+    check(lib().luma_io_restart_read(path.encode(), n, darr, fp, up, rp))

@@ -13,7 +13,7 @@
  * Usage:
  *   luma_ref --out DIR --steps N [--dump-every K] [--init-u FILE] [--init-rho FILE]
  *            [--workdir DIR] [--markers FILE] [--drag-out FILE] [--momex-out FILE]
- *            [--bfl-out FILE] [--bfl-forces FILE] [--io-at S]
+ *            [--bfl-out FILE] [--bfl-forces FILE] [--io-at S] [--restart-read]
  *
  * With --momex-out (cases compiled with L_LD_OUT) FILE gets, per step s, the
  * momentum-exchange force ObjectManager::computeLiftDrag accumulated over
@@ -30,6 +30,10 @@
  * With --io-at S the reference's own ASCII writers run after step S:
  * GridObj::io_lite(S, "") (files io_lite.Lev<l>.Reg<r>.Rnk0.<S>.dat) and
  * GridObj::io_restart(eWrite) (restart_LBM_Rnk0.out), into DIR.
+ *
+ * With --restart-read the grids are read back from
+ * <workdir>/input/restart_LBM_Rnk0.out by GridObj::io_restart(eRead) before
+ * the first dump.
  *
  * With --drag-out nothing is dumped; FILE gets the time average over the N
  * steps of body 0's lattice-unit drag and N.
@@ -236,6 +240,7 @@ static void reinit_equilibrium(GridObj *g) {
 int main(int argc, char **argv) {
     std::string out = ".", init_u, init_rho, workdir, markers, drag_out, momex_out, bfl_out, bfl_forces;
     int steps = 0, dump_every = 0, io_at = -1;
+    bool restart_read = false;
     for (int a = 1; a < argc; ++a) {
         std::string k = argv[a];
         auto next = [&]() -> std::string {
@@ -254,6 +259,7 @@ int main(int argc, char **argv) {
         else if (k == "--bfl-out") bfl_out = next();
         else if (k == "--bfl-forces") bfl_forces = next();
         else if (k == "--io-at") io_at = std::atoi(next().c_str());
+        else if (k == "--restart-read") restart_read = true;
         else { std::fprintf(stderr, "unknown argument %s\n", k.c_str()); return 2; }
     }
     mkdir(out.c_str(), 0755);
@@ -299,6 +305,7 @@ int main(int argc, char **argv) {
     om->ibm_initialise();
 #endif
     (void)om;
+    if (restart_read) grids->io_restart(eRead);
     if (!bfl_out.empty()) dump_bfl(grids, bfl_out);
     FILE *bf = bfl_forces.empty() ? nullptr : std::fopen(bfl_forces.c_str(), "w");
 

@@ -6,7 +6,10 @@ quantities, whose io_lite lines carry them) with the reference's serial
 build, runs 12 steps and calls
 GridObj::io_lite(12, "") and GridObj::io_restart(eWrite) after the last
 (harness option ``--io-at``).  Stores, per written file, its size and the
-SHA-256 of its bytes (the files themselves are 1.8 MB of text).
+SHA-256 of its bytes (the files themselves are 1.8 MB of text).  Then runs
+the reference's reader, GridObj::io_restart(eRead), on that restart file
+(``--restart-read``) and stores the SHA-256 of every grid's f, u and rho as
+it leaves them.
 
 Output: ``io_<case>.json`` beside this script.
 
@@ -19,9 +22,12 @@ import argparse
 import hashlib
 import json
 import os
+import shutil
 import subprocess
 import sys
 import tempfile
+
+import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(os.path.dirname(HERE))
@@ -45,7 +51,18 @@ def main() -> int:
             if name.startswith(("io_lite.", "restart_LBM_")):
                 data = open(os.path.join(work, name), "rb").read()
                 files[name] = {"bytes": len(data), "sha256": hashlib.sha256(data).hexdigest()}
-        out = {"case": case, "steps": STEPS, "precision": PRECISION, "files": files}
+        back = tempfile.mkdtemp(prefix="io_read_")
+        os.makedirs(os.path.join(back, "input"))
+        shutil.copy(os.path.join(work, "restart_LBM_Rnk0.out"), os.path.join(back, "input"))
+        subprocess.run([exe, "--out", os.path.join(back, "out"), "--steps", "0", "--dump-every", "0",
+                        "--workdir", back, "--restart-read"], check=True)
+        read = {}
+        s0 = os.path.join(back, "out", "s0")
+        for name in sorted(os.listdir(s0)):
+            if name.endswith(("_f.bin", "_u.bin", "_rho.bin")):
+                data = np.fromfile(os.path.join(s0, name), dtype=np.float64)
+                read[name[:-4]] = hashlib.sha256(data.tobytes()).hexdigest()
+        out = {"case": case, "steps": STEPS, "precision": PRECISION, "files": files, "restart_read": read}
         dst = os.path.join(HERE, f"io_{case}.json")
         with open(dst, "w") as fp:
             json.dump(out, fp, indent=1)

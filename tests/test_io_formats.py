@@ -81,3 +81,27 @@ def test_gpu_snapshot_writers_match_oracle(tmp_path, case):
             # significant digits (restart)
             tol = dict(rtol=0.0, atol=2e-10) if name.startswith("io_lite") else dict(rtol=2e-5, atol=1e-9)
             assert np.allclose(np.array(ra[2:-1], float), np.array(rb[2:-1], float), **tol), name
+
+
+@pytest.mark.parametrize("case", CASES_IO)
+def test_restart_reader_matches_reference(tmp_path, case):
+    """The restart file read back (GridObj::io_restart(eRead): f rebuilt as
+    feq (1 + dt f_neq / omega), with feq from level 0's state at the level-0
+    index of every line, level 0's omega) gives every grid the f, u and rho
+    the reference's own reader leaves (SHA-256 of the arrays)."""
+    from luma_gb300 import gpu as G
+    REF = ref_of(case)
+    oracle_files(tmp_path, REF)
+    levels = R.hierarchy(REF["case"])
+    descs = [lv.desc() for lv in levels]
+    states = []
+    for lv in levels:
+        f0, u0, rho0, _ = R.initial_state(lv)
+        states.append({"f": f0.astype(np.float64).copy(), "u": np.ascontiguousarray(u0, dtype=np.float64),
+                       "rho": np.ascontiguousarray(rho0, dtype=np.float64)})
+    G.read_io_restart(os.path.join(tmp_path, "restart_LBM_Rnk0.out"), descs, states)
+    for lv, st in zip(levels, states):
+        key = R.grid_key(lv)
+        for k in ("f", "u", "rho"):
+            got = hashlib.sha256(np.ascontiguousarray(st[k]).tobytes()).hexdigest()
+            assert got == REF["restart_read"][f"{key}_{k}"], (key, k)
