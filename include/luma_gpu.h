@@ -285,6 +285,13 @@ int luma_io_lite_write(const luma_grid_desc *desc, const double *f, const double
                        const char *dir, double tval, int precision, int rank);
 int luma_io_restart_write(const luma_grid_desc *desc, const double *f, const double *u, const double *rho,
                           const char *path, int append);
+/* The IB-body part of the restart (ObjectManager::io_restart(eWrite),
+ * src/ObjectManager_ops_io.cpp:136-190; restart_IBBody_Rnk<rank>.out):
+ * nmarkers[b] markers per body, positions (3 per marker, bodies in order,
+ * e.g. from luma_gpu_ibm_get_markers), flexible[b] non-zero for bodies that
+ * also write their old positions (positions0, same layout). */
+int luma_io_ibbody_restart_write(const char *path, int nbodies, const int *nmarkers, const int *flexible,
+                                 const double *positions, const double *positions0);
 /* GridObj::io_restart(eRead) (src/GridObj_ops_io.cpp:490-580) on host
  * arrays: descs[0..ngrids) are the tree's grids with level 0 first (labels
  * not needed; positions, dt, dh, omega, global_edges used), f/u/rho their

@@ -418,6 +418,43 @@ int luma_io_restart_read(const char *path, int ngrids, const luma_grid_desc *con
     return LUMA_OK;
 }
 
+// ObjectManager::io_restart(eWrite) (src/ObjectManager_ops_io.cpp:136-190):
+// the number of bodies and a newline, then per body a "\t/\t" separator,
+// its marker count, "\t/\t", and per marker x, y, z (and, for a flexible
+// body, the old position) each followed by a tab; no final newline.
+int luma_io_ibbody_restart_write(const char *path, int nbodies, const int *nmarkers, const int *flexible,
+                                 const double *positions, const double *positions0) {
+    if (!path || nbodies < 0 || (nbodies > 0 && (!nmarkers || !positions)))
+        return luma_set_error(LUMA_E_INVALID, "luma_io_ibbody_restart_write: null argument");
+    FILE *fp = std::fopen(path, "w");
+    if (!fp) return luma_set_error(LUMA_E_INVALID, "io_restart: cannot open %s", path);
+    Out o{fp, {}, {}};
+    o.buf += std::to_string(nbodies);
+    o.buf += '\n';
+    size_t m0 = 0;
+    int rc = LUMA_OK;
+    for (int b = 0; b < nbodies && rc == LUMA_OK; ++b) {
+        const bool flex = flexible && flexible[b];
+        if (flex && !positions0) {
+            rc = luma_set_error(LUMA_E_INVALID, "io_restart: flexible body %d needs old positions", b);
+            break;
+        }
+        o.raw("\t/\t");
+        o.buf += std::to_string(nmarkers[b]);
+        o.raw("\t/\t");
+        for (int m = 0; m < nmarkers[b]; ++m) {
+            const size_t g = m0 + (size_t)m;
+            for (int d = 0; d < 3; ++d) o.gen(positions[3 * g + d]);
+            if (flex)
+                for (int d = 0; d < 3; ++d) o.gen(positions0[3 * g + d]);
+        }
+        m0 += (size_t)nmarkers[b];
+    }
+    const bool ok = o.flush(true);
+    if (std::fclose(fp) != 0 || !ok) rc = rc ? rc : luma_set_error(LUMA_E_INVALID, "io_restart: write failed");
+    return rc;
+}
+
 int luma_io_restart_write(const luma_grid_desc *desc, const double *f, const double *u, const double *rho,
                           const char *path, int append) {
     if (!path) return luma_set_error(LUMA_E_INVALID, "luma_io_restart_write: null path");

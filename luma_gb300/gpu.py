@@ -70,6 +70,8 @@ def lib() -> C.CDLL:
         L.luma_io_lite_write.argtypes = [C.POINTER(A.GridDesc), dp, dp, dp, dp, dp, dp, dp, C.c_char_p, C.c_double,
                                          C.c_int, C.c_int]
         L.luma_io_restart_write.argtypes = [C.POINTER(A.GridDesc), dp, dp, dp, C.c_char_p, C.c_int]
+        L.luma_io_ibbody_restart_write.argtypes = [C.c_char_p, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int), dp,
+                                                   dp]
         L.luma_io_restart_read.argtypes = [C.c_char_p, C.c_int, C.POINTER(C.POINTER(A.GridDesc)),
                                            C.POINTER(dp), C.POINTER(dp), C.POINTER(dp)]
         if L.luma_gpu_abi_version() != A.ABI_VERSION:
@@ -273,3 +275,21 @@ def read_io_restart(path: str, descs, states) -> None:
     up = (C.POINTER(C.c_double) * n)(*[A.dptr(st["u"]) for st in states])
     rp = (C.POINTER(C.c_double) * n)(*[A.dptr(st["rho"]) for st in states])
     check(lib().luma_io_restart_read(path.encode(), n, darr, fp, up, rp))
+
+
+def write_io_ibbody_restart(path: str, positions, positions0=None) -> None:
+    """The IB-body restart file: positions (one (n_b, 3) array per body);
+    positions0 (same shapes, or None per body) marks flexible bodies."""
+    nb = len(positions)
+    counts = np.array([len(p) for p in positions], dtype=np.int32)
+    flex = np.array([0 if positions0 is None or positions0[b] is None else 1 for b in range(nb)], dtype=np.int32)
+    pos = np.ascontiguousarray(np.concatenate([np.asarray(p, dtype=np.float64).reshape(-1, 3) for p in positions])
+                               if nb else np.zeros((0, 3)))
+    pos0 = None
+    if flex.any():
+        pos0 = np.ascontiguousarray(np.concatenate([
+            np.asarray(positions0[b] if flex[b] else positions[b], dtype=np.float64).reshape(-1, 3)
+            for b in range(nb)]))
+    ip = C.POINTER(C.c_int)
+    check(lib().luma_io_ibbody_restart_write(path.encode(), nb, counts.ctypes.data_as(ip), flex.ctypes.data_as(ip),
+                                             A.dptr(pos), A.dptr(pos0)))

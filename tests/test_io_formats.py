@@ -17,7 +17,7 @@ from oracle import oracle as O
 from tests.golden import runner as R
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-CASES_IO = ("refine_d2q9", "tavg_refine_d2q9")   # the second keeps time averages
+CASES_IO = ("refine_d2q9", "tavg_refine_d2q9", "ibm_cyl_d2q9")  # time averages; an IB cylinder
 
 
 def ref_of(case):
@@ -26,8 +26,19 @@ def ref_of(case):
 
 def oracle_files(tmp_path, REF):
     from luma_gb300 import gpu as G
+    from tests.golden import cases as CASE_DEFS
     grids, levels = R.build_backend(REF["case"], lambda d, p: O.OracleGrid(d, p))
+    bodies = CASE_DEFS.bodies(REF["case"])
+    if bodies:
+        ibm = O.OracleIBM()
+        for lev, reg, pos in bodies:
+            ibm.add_body(grids[lev], pos)
+        ibm.initialise()
     grids[0].step(REF["steps"])
+    if bodies:
+        mk = [ibm.markers(b) for b in range(len(bodies))]
+        G.write_io_ibbody_restart(os.path.join(tmp_path, "restart_IBBody_Rnk0.out"),
+                                  [m[:, 0:3] for m in mk])
     restart = os.path.join(tmp_path, "restart_LBM_Rnk0.out")
     for n, (g, lv) in enumerate(zip(grids, levels)):
         st = g.download()
@@ -55,7 +66,7 @@ def _rows(path):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("case", CASES_IO)
+@pytest.mark.parametrize("case", CASES_IO[:2])
 def test_gpu_snapshot_writers_match_oracle(tmp_path, case):
     from luma_gb300 import _abi as A
     from luma_gb300.gpu import GpuGrid
