@@ -102,17 +102,15 @@ CASES = {
         defs=Definitions(dims=2, resolution=50, timestep=1.0 / 1250.0, bx=2.0, by=1.0, re=100, ux0=1.0,
                          walls=(V, X, S, S, F, F)),
         bfl=dict(centre=(0.5, 0.5, 0.0), radius=0.16), steps=(10, 300), store_f=(10,)),
-    # D3Q19 channel with a rigid BFL sphere (3D prefab).  The host set-up is
-    # restated for the 2D circle only: this case takes the labels, the
-    # per-site marker lookup and the link distances from the reference's
-    # own BFLBody (stored in the fixture).  The reference diverges once the
+    # D3Q19 channel with a rigid BFL sphere (3D prefab: Fibonacci points,
+    # triangle-based link distances).  The reference diverges once the
     # flow reaches the sphere (step 14: link distances near 1 amplify the
     # source-side interpolation by 1/(2-2q)), so parity is pinned on the
     # steps before that, with the body already loaded.
     "bfl_sphere_d3q19": dict(
         defs=Definitions(dims=3, resolution=20, timestep=1.0 / 500.0, bx=2.0, by=1.0, bz=1.0, re=10, ux0=1.0,
                          walls=(V, X, S, S, F, F)),
-        bfl=dict(centre=(0.6, 0.5, 0.5), radius=0.15, from_reference=True), steps=(11, 13), store_f=(13,)),
+        bfl=dict(centre=(0.6, 0.5, 0.5), radius=0.15), steps=(11, 13), store_f=(13,)),
     # Time-averaged quantities: the refined channel (both levels) and the IB
     # cylinder (support sites re-macroed once per marker they support).
     "tavg_refine_d2q9": dict(

@@ -30,14 +30,9 @@ def level0(name: str) -> hostcase.Level0:
     if init is not None:
         l0.u = init["u"].copy()
     b = spec.get("bfl")
-    if b and b.get("from_reference"):
-        fx = fixture(name)
-        body = bfl.BflBody(typ=fx["typ"].astype(np.int32), site_marker=fx["bfl_site_marker"], q=fx["bfl_q"],
-                           positions=np.zeros((fx["bfl_q"].shape[0], 3)))
-        l0.typ = body.typ
-        l0.bfl = body
-    elif b:
-        body = bfl.circle_body(l0, b["centre"], b["radius"])
+    if b:
+        make = bfl.circle_body if spec["defs"].dims == 2 else bfl.sphere_body
+        body = make(l0, b["centre"], b["radius"])
         l0.typ = body.typ
         l0.bfl = body
     return l0
