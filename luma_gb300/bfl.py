@@ -8,16 +8,17 @@ primary support voxel matches) and, per marker, the link distances
 ``Q[v + Q*m]`` (``BFLBody::Q``; -1 where no wall cuts the link).
 
 ``circle_body`` (2D) and ``sphere_body`` (3D) follow:
-  * the circle prefab ``Body(g, id, centre, radius)`` (``inc/Body.h:197-255``):
-    floor(2 pi r / dh) angles from ``GridUtils::linspace``, the first dropped;
+  * the prefab ``Body(g, id, centre, radius)`` (``inc/Body.h:197-255``): in
+    2D floor(2 pi r / dh) angles from ``GridUtils::linspace``, the first
+    dropped; in 3D floor(4 pi r^2 / dh^2) Fibonacci points;
   * ``Marker`` voxels (``inc/Marker.h:66-95`` through
     ``GridUtils::getEnclosingVoxel``, ``src/GridUtils.cpp:1630-1718``);
   * ``BFLBody::initialise`` (``src/BFLBody.cpp:49-142``): eBFL labels, then
     ``enforceSurfaceClosure`` (``:548-715``), then ``computeQ`` over the eBFL
     sites in (i, j, k) order (2D overload ``:412-515``, 3D ``:244-404``).
 The geometry reader shifts the centre by the solid-wall thickness
-(``src/ObjectManager_ops_io.cpp:585-597``); ``circle_body`` takes the centre
-as written in the geometry file and applies that shift.
+(``src/ObjectManager_ops_io.cpp:585-597``); both take the centre as written
+in the geometry file and apply that shift.
 """
 from __future__ import annotations
 
