@@ -62,6 +62,32 @@ def _vecnorm(v) -> float:
     return math.sqrt(s)
 
 
+def prefab_points(lv, centre, radius: float) -> list:
+    """Marker positions of the circle/sphere prefab (``inc/Body.h:197-255``)
+    for a centre as written in the geometry file (the wall shift applied):
+    in 2D floor(2 pi r / dh) angles from ``GridUtils::linspace``, the first
+    dropped; in 3D floor(4 pi r^2 / dh^2) Fibonacci points."""
+    d = lv.defs
+    wt = lv.wall_thickness
+    cx = centre[0] + (wt[0] if d.walls[0] == A.SOLID else 0.0)
+    cy = centre[1] + (wt[2] if d.walls[2] == A.SOLID else 0.0)
+    cz = centre[2] + (wt[4] if d.walls[4] == A.SOLID else 0.0)
+    if d.dims == 3:
+        n = int(math.floor(4.0 * L_PI * (radius ** 2) / (lv.dh ** 2)))
+        inc = L_PI * (3 - math.sqrt(5))
+        off = 2.0 / float(n)
+        pts = []
+        for k in range(n):
+            y = k * off - 1 + (off / 2)
+            r = math.sqrt(1 - y * y)
+            phi = k * inc
+            pts.append((cx + (math.cos(phi) * r * radius), y * radius + cy, cz + (math.sin(phi) * r * radius)))
+        return pts
+    n = int(math.floor(2.0 * L_PI * radius / lv.dh))
+    theta = _linspace(0.0, 2.0 * L_PI - (2.0 * L_PI / float(n)), n)
+    return [(cx + radius * math.cos(t), cy + radius * math.sin(t), cz) for t in theta[1:]]
+
+
 def circle_body(level0, centre, radius: float, reset_projection: bool = False) -> BflBody:
     """A rigid 2D BFL circle on level 0 (reference ``CIRCLE_SPHERE BFL``).
 
@@ -75,41 +101,18 @@ def circle_body(level0, centre, radius: float, reset_projection: bool = False) -
     reference."""
     if level0.defs.dims != 2:
         raise ValueError("circle_body builds the 2D prefab")
-    cx, cy, cz = _shifted_centre(level0, centre)
-    n = int(math.floor(2.0 * L_PI * radius / level0.dh))
-    theta = _linspace(0.0, 2.0 * L_PI - (2.0 * L_PI / float(n)), n)
-    pts = [(cx + radius * math.cos(t), cy + radius * math.sin(t), cz) for t in theta[1:]]
-    return _build(level0, pts, reset_projection)
+    return _build(level0, prefab_points(level0, centre, radius), reset_projection)
 
 
 def sphere_body(level0, centre, radius: float, reset_projection: bool = False) -> BflBody:
     """A rigid 3D BFL sphere on level 0 (reference ``CIRCLE_SPHERE BFL`` in
-    3D): floor(4 pi r^2 / dh^2) points of the Fibonacci (golden-angle)
-    layout of ``inc/Body.h:212-229``, then the same labelling and closure,
-    and the 3D ``computeQ`` (``src/BFLBody.cpp:244-404``): line-triangle
-    intersections of each even direction's link with every triangle of
-    three markers of the site's 3x3x3 neighbourhood."""
+    3D): the Fibonacci prefab, the same labelling and closure, and the 3D
+    ``computeQ`` (``src/BFLBody.cpp:244-404``): line-triangle intersections
+    of each even direction's link with every triangle of three markers of
+    the site's 3x3x3 neighbourhood."""
     if level0.defs.dims != 3:
         raise ValueError("sphere_body builds the 3D prefab")
-    cx, cy, cz = _shifted_centre(level0, centre)
-    n = int(math.floor(4.0 * L_PI * (radius ** 2) / (level0.dh ** 2)))
-    inc = L_PI * (3 - math.sqrt(5))
-    off = 2.0 / float(n)
-    pts = []
-    for k in range(n):
-        y = k * off - 1 + (off / 2)
-        r = math.sqrt(1 - y * y)
-        phi = k * inc
-        pts.append((cx + (math.cos(phi) * r * radius), y * radius + cy, cz + (math.sin(phi) * r * radius)))
-    return _build(level0, pts, reset_projection)
-
-
-def _shifted_centre(lv, centre):
-    d = lv.defs
-    wt = lv.wall_thickness
-    shift = [wt[0] if d.walls[0] == A.SOLID else 0.0, wt[2] if d.walls[2] == A.SOLID else 0.0,
-             wt[4] if d.walls[4] == A.SOLID else 0.0]
-    return centre[0] + shift[0], centre[1] + shift[1], centre[2] + shift[2]
+    return _build(level0, prefab_points(level0, centre, radius), reset_projection)
 
 
 def _build(lv, points, reset_projection: bool) -> BflBody:

@@ -301,3 +301,46 @@ def test_guo_forcing_moments(Q, dims):
         assert abs(Fi.sum()) <= 1e-18
         mom = Fi @ L["c"][:, :dims].astype(float)
         assert np.allclose(mom, (1.0 - 0.5 * omega) * F, rtol=1e-13, atol=1e-19)
+
+
+def test_geometry_reader_prefabs_match_reference():
+    """The geometry reader restatement (CIRCLE_SPHERE IBM, FILAMENT_ARRAY of
+    flexible filaments) gives the reference reader's bodies: every marker's
+    position, epsilon and ds after initialisation equal the reference's
+    (tests/golden/make_geometry.py)."""
+    import json
+    from luma_gb300 import geometry
+    ref = json.load(open(os.path.join(R.HERE, "geometry_prefab.json")))
+    l0 = R.level0(ref["case"])
+    bodies = geometry.read_geometry(ref["config"], {(0, 0): l0})
+    assert [b["kind"] for b in bodies] == ["ibm", "filament", "filament"]
+    grids, _ = R.build_backend(ref["case"], lambda d, p: O.OracleGrid(d, p))
+    ibm = O.OracleIBM()
+    for b in bodies:
+        if b["kind"] == "ibm":
+            ibm.add_body(grids[0], b["positions"])
+        else:
+            ibm.add_filament(grids[0], **b["args"])
+    ibm.initialise()
+    got = []
+    for ib in range(len(bodies)):
+        mk = ibm.markers(ib)
+        got += [[ib, m, *mk[m, 0:3], mk[m, 6], mk[m, 7]] for m in range(mk.shape[0])]
+    want = ref["markers"]
+    assert len(got) == len(want)
+    for g, w in zip(got, want):
+        assert g[:2] == w[:2] and all(float(a) == float(b) for a, b in zip(g[2:], w[2:])), (g, w)
+
+
+def test_geometry_reader_bfl_entries():
+    """CIRCLE_SPHERE BFL entries build the BFL bodies of the BFL cases
+    (the set-up pinned to the reference's BFLBody above)."""
+    from luma_gb300 import geometry
+    for name in ("bfl_cyl_d2q9", "bfl_sphere_d3q19"):
+        l0 = R.level0(name)
+        fx = R.fixture(name)
+        base = hostcase.build_level0(CASES.CASES[name]["defs"])
+        (b,) = geometry.read_geometry(CASES.geometry_config(name), {(0, 0): base})
+        assert b["kind"] == "bfl"
+        assert np.array_equal(b["body"].typ, fx["typ"]) and np.array_equal(b["body"].q, fx["bfl_q"])
+        assert np.array_equal(b["body"].site_marker, l0.bfl.site_marker)
