@@ -303,24 +303,35 @@ def test_guo_forcing_moments(Q, dims):
         assert np.allclose(mom, (1.0 - 0.5 * omega) * F, rtol=1e-13, atol=1e-19)
 
 
-def test_geometry_reader_prefabs_match_reference():
-    """The geometry reader restatement (CIRCLE_SPHERE IBM, FILAMENT_ARRAY of
-    flexible filaments) gives the reference reader's bodies: every marker's
-    position, epsilon and ds after initialisation equal the reference's
-    (tests/golden/make_geometry.py)."""
+GEOM_DEFS = {
+    "geom_d3q19": dict(dims=3, resolution=20, timestep=1.0 / 500.0, bx=2.0, by=1.0, bz=1.0, re=100, ux0=1.0,
+                       ibm=True, walls=(A.VELOCITY, A.EXTRAPOLATE_RIGHT, A.SOLID, A.SOLID, A.FLUID, A.FLUID)),
+}
+
+
+@pytest.mark.parametrize("run", [0, 1], ids=["2d", "3d"])
+def test_geometry_reader_prefabs_match_reference(run):
+    """The geometry reader restatement (circle/sphere, square/cube, plate,
+    rigid and flexible filament arrays) gives the reference reader's IB
+    bodies: every marker's position, epsilon and ds after initialisation
+    equal the reference's (tests/golden/make_geometry.py)."""
     import json
     from luma_gb300 import geometry
-    ref = json.load(open(os.path.join(R.HERE, "geometry_prefab.json")))
-    l0 = R.level0(ref["case"])
+    ref = json.load(open(os.path.join(R.HERE, "geometry_prefab.json")))["runs"][run]
+    name = ref["case"]
+    if name in CASES.CASES:
+        l0 = R.level0(name)
+    else:
+        l0 = hostcase.build_level0(hostcase.Definitions(**GEOM_DEFS[name]))
     bodies = geometry.read_geometry(ref["config"], {(0, 0): l0})
-    assert [b["kind"] for b in bodies] == ["ibm", "filament", "filament"]
-    grids, _ = R.build_backend(ref["case"], lambda d, p: O.OracleGrid(d, p))
+    g = O.OracleGrid(l0.desc())
+    g.upload(*R.initial_state(l0), t=0)
     ibm = O.OracleIBM()
     for b in bodies:
         if b["kind"] == "ibm":
-            ibm.add_body(grids[0], b["positions"])
+            ibm.add_body(g, b["positions"])
         else:
-            ibm.add_filament(grids[0], **b["args"])
+            ibm.add_filament(g, **b["args"])
     ibm.initialise()
     got = []
     for ib in range(len(bodies)):
@@ -328,8 +339,8 @@ def test_geometry_reader_prefabs_match_reference():
         got += [[ib, m, *mk[m, 0:3], mk[m, 6], mk[m, 7]] for m in range(mk.shape[0])]
     want = ref["markers"]
     assert len(got) == len(want)
-    for g, w in zip(got, want):
-        assert g[:2] == w[:2] and all(float(a) == float(b) for a, b in zip(g[2:], w[2:])), (g, w)
+    for gr, w in zip(got, want):
+        assert gr[:2] == w[:2] and all(float(a) == float(b) for a, b in zip(gr[2:], w[2:])), (gr, w)
 
 
 def test_geometry_reader_bfl_entries():
