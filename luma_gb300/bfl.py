@@ -115,15 +115,18 @@ def sphere_body(level0, centre, radius: float, reset_projection: bool = False) -
     return _build(level0, prefab_points(level0, centre, radius), reset_projection)
 
 
-def _build(lv, points, reset_projection: bool) -> BflBody:
-    """Markers at `points` (in order), then BFLBody::initialise: labels,
-    enforceSurfaceClosure, computeQ, and the per-site marker lookup."""
+def _build(lv, points, reset_projection: bool, voxels=None) -> BflBody:
+    """Markers at `points` (in order; `voxels`, when given, are their
+    primary support voxels, else the voxels enclosing the points), then
+    BFLBody::initialise: labels, enforceSurfaceClosure, computeQ, and the
+    per-site marker lookup."""
     d = lv.defs
     D = d.dims
     N, M, K, dh = lv.N, lv.M, lv.K, lv.dh
     Q = d.Q
     c = [[int(x) for x in cv] for cv in lattice(D, Q)[0]]
-    gx0, gy0, gz0 = lv.global_edges[0], lv.global_edges[2], lv.global_edges[4]
+    e = lv.edges if lv.edges is not None else lv.global_edges  # the grid's own edges
+    gx0, gy0, gz0 = e[0], e[2], e[4]
     typ = lv.typ.reshape(N, M, K).copy()
     xpos, ypos, zpos = lv.xpos, lv.ypos, lv.zpos
 
@@ -151,8 +154,14 @@ def _build(lv, points, reset_projection: bool) -> BflBody:
             return -1
         return voxel_marker.get(v, -1)
 
-    for p in points:
+    for n_, p in enumerate(points):
         add_marker(*p)
+        if voxels is not None and tuple(voxels[n_]) != supp[-1]:
+            v = tuple(voxels[n_])
+            if voxel_marker.get(supp[-1]) == len(pos) - 1:
+                del voxel_marker[supp[-1]]
+            voxel_marker.setdefault(v, len(pos) - 1)
+            supp[-1] = v
     for s in supp:
         typ[s] = A.BFL
 

@@ -20,9 +20,19 @@ parses the same text for:
 * ``PLATE IBM|BFL lev reg x y z length width angle_x angle_y angle_z
   RIGID|MOVABLE`` (3D, :711-790) at ``plate_points``.
 
-All shift positions by the solid-wall thickness as the reader does (left,
-bottom, front walls).  The reader skips '#' lines only at the top of the
-file; so does this.  FROM_FILE point clouds raise ``NotImplementedError``.
+* ``FROM_FILE BBB|BFL|IBM file lev reg START|CENTRE x START|CENTRE y
+  START|CENTRE z length X|Y|Z RIGID|MOVABLE CLAMPED|SUPPORTED`` (:360-452
+  with ``io_readInCloud``, :812-1058): the point cloud scaled to `length`
+  along the direction and placed at the reference position, kept where it
+  lies on the grid; BBB labels the fluid sites enclosing the points solid
+  (``addBouncebackObject``, src/ObjectManager.cpp:304-338: u set to 0 with
+  the 3D quirk that sets u_x twice and leaves u_z, rho to L_RHOIN); BFL and
+  IBM bodies take the voxel-grid filter's markers (``Body::buildFromCloud``
+  / ``passToVoxelFilter``, inc/Body.h:622-790).
+
+The prefab entries shift positions by the solid-wall thickness as the
+reader does (left, bottom, front walls); FROM_FILE does not.  The reader
+skips '#' lines only at the top of the file; so does this.
 """
 from __future__ import annotations
 
@@ -122,6 +132,135 @@ def plate_points(lv, centre, length: float, width: float, angles) -> list:
     return pts
 
 
+L_SMALL_NUMBER = 1e-8
+
+
+def _cround(v: float) -> float:
+    """std::round: halves away from zero."""
+    r = math.floor(abs(v))
+    if abs(v) - r >= 0.5:
+        r += 1
+    return math.copysign(r, v)
+
+
+def read_cloud(text: str, dims: int) -> list:
+    """Points of a cloud file as io_readInCloud reads them: one "x y z" line
+    each (z forced to 0 in 2D); a line without values (the empty line after
+    a final newline) repeats the previous point, as the reader's stream
+    extraction leaves its variables unchanged."""
+    pts = []
+    x = y = z = None
+    for line in text.split("\n"):
+        vals = line.split()
+        if len(vals) > 0:
+            x = float(vals[0])
+        if len(vals) > 1:
+            y = float(vals[1])
+        if len(vals) > 2:
+            z = float(vals[2])
+        if x is None or y is None or (dims == 3 and z is None):
+            # the reference would store uninitialised values here
+            raise ValueError("cloud file: a point before any complete coordinates")
+        pts.append((x, y, z if dims == 3 else 0.0))
+    return pts
+
+
+def place_cloud(lv, pts, refs, length: float, direction: str) -> list:
+    """Scale and shift a cloud as io_readInCloud does (:850-1000) and keep
+    the points that lie on the grid; `refs` = ((centre?, value) per axis)."""
+    D = lv.defs.dims
+    dcell = lv.dh
+    ref = [_cround(r / dcell) * dcell for _, r in refs]
+    blen = _cround(length / dcell) * dcell
+    axes = [[p[a] for p in pts] for a in range(3)]
+    ai = "XYZ".index(direction)
+    scale = (blen - 2 * L_SMALL_NUMBER * dcell) / abs(max(axes[ai]) - min(axes[ai]))
+    shift = [0.0, 0.0, 0.0]
+    for a in range(3):
+        lo, hi = min(axes[a]), max(axes[a])
+        if refs[a][0]:
+            ref[a] += (dcell / 2.0)
+            dist = scale * abs(hi - lo)
+            dist = _cround(dist / dcell) * dcell
+            start = ref[a] - (dist / 2.0)
+            shift[a] = start - scale * lo
+        else:
+            shift[a] = (ref[a] + L_SMALL_NUMBER * dcell) - scale * lo
+    E = lv.global_edges
+    out = []
+    for p in pts:
+        x = p[0] * scale
+        x += shift[0]
+        y = p[1] * scale
+        y += shift[1]
+        z = p[2]
+        if D == 3:
+            z = z * scale
+            z += shift[2]
+        v = _voxel(lv, x, y, z)
+        inside = E[0] <= x < E[1] and E[2] <= y < E[3] and (D != 3 or E[4] <= z < E[5])
+        if inside and v is not None:
+            out.append((x, y, z))
+    return out
+
+
+def _voxel(lv, x, y, z):
+    """GridUtils::getEnclosingVoxel on the grid's own edges, None off the
+    grid (isOffGrid)."""
+    D = lv.defs.dims
+    e = lv.edges if lv.edges is not None else lv.global_edges
+    v = (int(math.floor((x - e[0]) / lv.dh)), int(math.floor((y - e[2]) / lv.dh)),
+         int(math.floor((z - e[4]) / lv.dh)) if D == 3 else 0)
+    if not (0 <= v[0] < lv.N and 0 <= v[1] < lv.M and 0 <= v[2] < lv.K):
+        return None
+    return v
+
+
+def voxel_filter(lv, pts) -> tuple:
+    """Body::buildFromCloud: one marker per voxel at the running mean of the
+    points that fall in it, in the reference's order (the current marker's
+    voxel window first, then any earlier marker's voxel, else a new
+    marker).  Returns (positions, voxels, first points): a marker's primary
+    support voxel and IBMarker::position0 stay those of the point that made
+    it."""
+    pos, vox, count, made = [], [], [], []
+    first = {}
+    half = lv.dh / 2.0
+    E = lv.global_edges
+    D = lv.defs.dims
+
+    def add(i, p):
+        v = _voxel(lv, *p)
+        made.append(i)
+        pos.append(list(p))
+        vox.append(v)
+        count.append(1)
+        first.setdefault(v, len(pos) - 1)
+
+    def mean(m, p):
+        count[m] += 1
+        c = count[m]
+        for a in range(3):
+            pos[m][a] = ((pos[m][a] * (c - 1)) + p[a]) / c
+
+    add(0, pts[0])
+    cur = 0
+    for i, p in enumerate(pts[1:], 1):
+        vx, vy, vz = lv.xpos[vox[cur][0]], lv.ypos[vox[cur][1]], lv.zpos[vox[cur][2]]
+        if (vx - half <= p[0] < vx + half) and (vy - half <= p[1] < vy + half) and (vz - half <= p[2] < vz + half):
+            mean(cur, p)
+            continue
+        inside = E[0] <= p[0] < E[1] and E[2] <= p[1] < E[3] and (D != 3 or E[4] <= p[2] < E[5])
+        v = _voxel(lv, *p) if inside else None
+        if v is not None and v in first:
+            cur = first[v]
+            mean(cur, p)
+            continue
+        cur = len(count)
+        add(i, p)
+    return [tuple(q) for q in pos], vox, [tuple(pts[i]) for i in made]
+
+
 def _rigid(btype, move, lev, reg, lv, pts) -> dict:
     if btype == "IBM":
         if move == "FLEXIBLE":
@@ -133,16 +272,18 @@ def _rigid(btype, move, lev, reg, lv, pts) -> dict:
     raise NotImplementedError(f"boundary type {btype}")
 
 
-def read_geometry(text: str, levels: dict, dm=None, ux0: float | None = None) -> list:
+def read_geometry(text: str, levels: dict, dm=None, ux0: float | None = None, clouds: dict | None = None) -> list:
     """Bodies of a geometry.config text.
 
     ``levels`` maps (level, region) to the grid's host description
     (``case.Level0`` or a sub-grid); ``dm(lv)`` gives a grid's
     ``GridObj::dm`` for filaments (default (L_PHYSICAL_RHO / L_RHOIN) dh^3).
+    ``clouds`` maps a FROM_FILE entry's file name to the file's text.
     Returns dicts with ``kind`` "ibm" (``positions``, ``movable``), "bfl"
-    (``body``, a ``bfl.BflBody``) or "filament" (the keyword arguments of
-    ``GpuGrid.ibm_add_filament``), each with ``level`` and ``region``, in
-    the reader's body order."""
+    (``body``, a ``bfl.BflBody``), "filament" (the keyword arguments of
+    ``GpuGrid.ibm_add_filament``) or "bbb" (``sites`` to label, see
+    ``apply_bbb``), each with ``level`` and ``region``, in the reader's body
+    order."""
     lines = text.split("\n")
     while lines and lines[0].startswith("#"):
         lines = lines[1:]
@@ -230,6 +371,62 @@ def read_geometry(text: str, levels: dict, dm=None, ux0: float | None = None) ->
                                          clamped=bc == "CLAMPED", density=float(rho), E=float(E),
                                          dm=(dm or default_dm)(lv), fsi_vel_scale=u0 * lv.dt / lv.dh)})
             del ah  # the planar beam has no horizontal angle
+        elif case == "FROM_FILE":
+            (btype, fname, lev, reg, xrt, xr, yrt, yr, zrt, zr, length, direction, move, bc) = take(14)
+            if int(lev) < 0:
+                raise NotImplementedError("FROM_FILE bodies spanning levels (level -1)")
+            if btype not in ("BBB", "BFL", "IBM"):
+                raise ValueError(f"FROM_FILE: unknown boundary type {btype}")
+            if direction not in ("X", "Y", "Z"):
+                raise ValueError(f"FROM_FILE: unknown scale direction {direction}")
+            lv = grid(lev, reg)
+            if clouds is None or fname not in clouds:
+                raise ValueError(f"geometry config: no cloud text for {fname}")
+            for rt in (xrt, yrt, zrt):
+                if rt not in ("START", "CENTRE"):
+                    raise ValueError(f"Unknown reference type {rt}")
+            pts = place_cloud(lv, read_cloud(clouds[fname], lv.defs.dims),
+                              ((xrt == "CENTRE", float(xr)), (yrt == "CENTRE", float(yr)), (zrt == "CENTRE", float(zr))),
+                              float(length), direction)
+            if not pts:
+                continue  # nothing of the body on the grid
+            if btype == "BBB":
+                out.append({"kind": "bbb", "level": int(lev), "region": int(reg),
+                            "sites": [_voxel(lv, *q) for q in pts]})
+                continue
+            if btype == "IBM" and move == "FLEXIBLE":
+                raise NotImplementedError("flexible bodies other than filaments")
+            mk, vox, p0 = voxel_filter(lv, pts)
+            if btype == "IBM":
+                out.append({"kind": "ibm", "level": int(lev), "region": int(reg),
+                            "movable": move == "MOVABLE", "positions": mk, "positions0": p0})
+            else:
+                out.append({"kind": "bfl", "level": int(lev), "region": int(reg),
+                            "body": _bfl._build(lv, mk, False, voxels=vox)})
         else:
             raise NotImplementedError(f"geometry entry {case}")
     return out
+
+
+def apply_bbb(lv, entry) -> None:
+    """Label a BBB entry's sites solid on a host grid description as
+    addBouncebackObject does: fluid sites only; u set to 0 (in 3D u_x twice,
+    u_z kept) and rho to L_RHOIN.  The reference has set the populations
+    from u and rho when it built the grid, before it reads the geometry:
+    take them from the description before labelling to match."""
+    N, M, K = lv.N, lv.M, lv.K
+    D = lv.defs.dims
+    typ = lv.typ.reshape(N, M, K).copy()
+    u = lv.u.reshape(N, M, K, D).copy()
+    rho = lv.rho.reshape(N, M, K).copy()
+    for (i, j, k) in entry["sites"]:
+        if typ[i, j, k] == A.FLUID:
+            typ[i, j, k] = A.SOLID
+            u[i, j, k, 0] = 0.0
+            u[i, j, k, 1] = 0.0
+            if D == 3:
+                u[i, j, k, 0] = 0.0
+            rho[i, j, k] = lv.defs.rho_in
+    lv.typ = typ.reshape(-1)
+    lv.u = u.reshape(-1)
+    lv.rho = rho.reshape(-1)

@@ -11,6 +11,13 @@ ds after ibm_initialise:
 
 Output: ``geometry_prefab.json`` beside this script.
 
+FROM_FILE point clouds (seeded synthetic clouds written here): for each run
+of ``CLOUD_RUNS`` the cloud files go to the run's ``input/`` folder and
+``geometry_cloud.npz`` stores the cloud texts, the config, the level-0
+labels, velocity and density after the reader (BBB labelling), the IB
+markers (as above) and, for BFL runs, the body's Q table and per-site marker
+lookup (``--bfl-out``).
+
 Usage (needs the reference checkout; not run on the GPU machine):
     python tests/golden/make_geometry.py [--ref /root/reference/LUMA]
 """
@@ -46,10 +53,105 @@ RUNS = {
 }
 
 
+def _cloud_texts() -> dict:
+    """Seeded clouds: a 2D cambered ellipse (700 points, final newline: the
+    reader repeats the last point), a filled 2D disc, a 2D bar, a 3D
+    ellipsoid surface (1500 points) and a filled 3D box with one line of
+    two values (the reader keeps the previous z)."""
+    rs = np.random.RandomState(7)
+    t = np.linspace(0.0, 2.0 * np.pi, 700, endpoint=False)
+    ell = np.stack([np.cos(t), 0.35 * np.sin(t) + 0.05 * np.sin(2 * t)], 1) + rs.uniform(-1e-3, 1e-3, (700, 2))
+    xs, ys = np.meshgrid(np.linspace(-1, 1, 41), np.linspace(-1, 1, 41))
+    keep = xs ** 2 + ys ** 2 <= 1.0
+    disc = np.stack([xs[keep], ys[keep]], 1)
+    bar = np.stack([np.linspace(0.0, 5.0, 200), 0.02 * np.sin(np.linspace(0.0, 9.0, 200))], 1)
+    n = 1500
+    k = np.arange(n) + 0.5
+    phi = np.arccos(1.0 - 2.0 * k / n)
+    th = np.pi * (1.0 + 5.0 ** 0.5) * k
+    sph = np.stack([2.0 * np.cos(th) * np.sin(phi), np.sin(th) * np.sin(phi), 0.8 * np.cos(phi)], 1)
+    sph += rs.uniform(-1e-3, 1e-3, sph.shape)
+    g = np.linspace(0.0, 1.0, 9)
+    box = np.stack(np.meshgrid(g, 0.5 * g, 0.7 * g, indexing="ij"), -1).reshape(-1, 3)
+    lines = ["%.6f %.6f %.6f" % tuple(p) for p in box]
+    lines[300] = "%.6f %.6f" % tuple(box[300, :2])
+    return {
+        "ellipse.txt": "".join("%.6f %.6f\n" % tuple(p) for p in ell),
+        "disc.txt": "\n".join("%.6f %.6f" % tuple(p) for p in disc),
+        "bar.txt": "\n".join("%.6f %.6f" % tuple(p) for p in bar) + "\n",
+        "ellipsoid.txt": "\n".join("%.6f %.6f %.6f" % tuple(p) for p in sph),
+        "box.txt": "\n".join(lines) + "\n",
+    }
+
+
+CLOUD_RUNS = {
+    "ibm_bbb_2d": ("fem_filament_d2q9",
+                   "FROM_FILE IBM ellipse.txt 0 0 CENTRE 0.6 CENTRE 0.5 START 0.0 0.4 X RIGID CLAMPED\n"
+                   "FROM_FILE BBB disc.txt 0 0 START 1.3 CENTRE 0.5 START 0.0 0.2 Y RIGID CLAMPED\n"
+                   "FROM_FILE BBB bar.txt 0 0 START 1.7 START 0.9 START 0.0 0.5 X RIGID CLAMPED\n"),
+    "bfl_2d": ("bfl_cyl_d2q9",
+               "FROM_FILE BFL ellipse.txt 0 0 CENTRE 0.7 CENTRE 0.5 START 0.0 0.3 X RIGID CLAMPED\n"),
+    "ibm_bbb_3d": ("geom_d3q19",
+                   "FROM_FILE IBM ellipsoid.txt 0 0 CENTRE 0.5 CENTRE 0.5 CENTRE 0.5 0.4 X RIGID CLAMPED\n"
+                   "FROM_FILE BBB box.txt 0 0 START 1.2 START 0.1 CENTRE 0.5 0.2 Z RIGID CLAMPED\n"),
+    "bfl_3d": ("bfl_sphere_d3q19",
+               "FROM_FILE BFL ellipsoid.txt 0 0 CENTRE 0.6 CENTRE 0.5 CENTRE 0.5 0.4 X RIGID CLAMPED\n"),
+}
+
+
+def _level0(path: str):
+    out = {}
+    for k, dt in (("typ", np.int32), ("u", np.float64), ("rho", np.float64)):
+        out[k] = np.fromfile(path + k + ".bin", dtype=dt)
+    return out
+
+
+def make_clouds(ref: str) -> str:
+    clouds = _cloud_texts()
+    store = {}
+    for run, (case, config) in CLOUD_RUNS.items():
+        exe = build_ref.build_case(case, ref)
+        work = tempfile.mkdtemp(prefix="cloud_")
+        os.makedirs(os.path.join(work, "input"))
+        with open(os.path.join(work, "input", "geometry.config"), "w") as fp:
+            fp.write(config)
+        for fname, text in clouds.items():
+            with open(os.path.join(work, "input", fname), "w") as fp:
+                fp.write(text)
+        bfl = os.path.join(work, "bfl.txt")
+        subprocess.run([exe, "--out", os.path.join(work, "out"), "--steps", "0", "--dump-every", "0",
+                        "--workdir", work, "--bfl-out", bfl], check=True, timeout=600)
+        s0 = os.path.join(work, "out", "s0", "L0R0_")
+        lv = _level0(s0)
+        store[run + "/case"] = np.array(case)
+        store[run + "/config"] = np.array(config)
+        for k, v in lv.items():
+            store[run + "/" + k] = v
+        mk_path = os.path.join(work, "out", "s0", "markers.txt")
+        if os.path.exists(mk_path):
+            mk = np.loadtxt(mk_path, ndmin=2)
+            store[run + "/markers"] = np.array([[r[0], r[1], *r[2:5], r[8], r[9]] for r in mk], dtype=np.float64)
+        lines = open(bfl).read().split("\n")
+        nm, q = (int(x) for x in lines[0].split())
+        if nm:
+            store[run + "/bfl_q"] = np.array([[float(x) for x in lines[1 + m].split()] for m in range(nm)])
+            store[run + "/bfl_marker"] = np.array([int(x) for x in lines[1 + nm:] if x.strip()], dtype=np.int32)
+        print(run, case, "markers" if os.path.exists(mk_path) else "", nm)
+    for fname, text in clouds.items():
+        store["cloud/" + fname] = np.array(text)
+    dst = os.path.join(HERE, "geometry_cloud.npz")
+    np.savez_compressed(dst, **store)
+    return dst
+
+
 def main() -> int:
     ap = argparse.ArgumentParser(description=__doc__)
     ap.add_argument("--ref", default=build_ref.DEFAULT_REF)
+    ap.add_argument("--clouds-only", action="store_true")
     a = ap.parse_args()
+    if a.clouds_only:
+        print(make_clouds(a.ref))
+        return 0
     runs = []
     for case, config in RUNS.items():
         exe = build_ref.build_case(case, a.ref)
@@ -68,6 +170,7 @@ def main() -> int:
     with open(dst, "w") as fp:
         json.dump({"runs": runs}, fp, indent=0)
     print(dst)
+    print(make_clouds(a.ref))
     return 0
 
 

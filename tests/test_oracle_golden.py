@@ -355,3 +355,57 @@ def test_geometry_reader_bfl_entries():
         assert b["kind"] == "bfl"
         assert np.array_equal(b["body"].typ, fx["typ"]) and np.array_equal(b["body"].q, fx["bfl_q"])
         assert np.array_equal(b["body"].site_marker, l0.bfl.site_marker)
+
+
+@pytest.mark.parametrize("run", ["ibm_bbb_2d", "bfl_2d", "ibm_bbb_3d", "bfl_3d"])
+def test_geometry_reader_clouds_match_reference(run):
+    """FROM_FILE point clouds (IBM, BFL, BBB; seeded clouds partly off the
+    grid, CENTRE and START references) give the reference reader's labels,
+    velocity and density, IB markers (position, epsilon, ds after
+    initialisation) and BFL Q table and site lookup
+    (tests/golden/make_geometry.py)."""
+    from luma_gb300 import geometry
+    z = np.load(os.path.join(R.HERE, "geometry_cloud.npz"))
+    clouds = {k.split("/", 1)[1]: str(z[k]) for k in z.files if k.startswith("cloud/")}
+    name, config = str(z[run + "/case"]), str(z[run + "/config"])
+    defs = CASES.CASES[name]["defs"] if name in CASES.CASES else hostcase.Definitions(**GEOM_DEFS[name])
+    l0 = hostcase.build_level0(defs)
+    bodies = geometry.read_geometry(config, {(0, 0): l0}, clouds=clouds)
+    for b in bodies:
+        if b["kind"] == "bbb":
+            geometry.apply_bbb(l0, b)
+    typ = l0.typ
+    for b in bodies:
+        if b["kind"] == "bfl":
+            typ = b["body"].typ.reshape(-1)
+            assert np.array_equal(b["body"].q, z[run + "/bfl_q"])
+            assert np.array_equal(b["body"].site_marker, z[run + "/bfl_marker"])
+    assert np.array_equal(typ, z[run + "/typ"])
+    assert np.array_equal(l0.u, z[run + "/u"]) and np.array_equal(l0.rho, z[run + "/rho"])
+    ibs = [b for b in bodies if b["kind"] == "ibm"]
+    assert bool(ibs) == (run + "/markers" in z.files)
+    if ibs:
+        g = O.OracleGrid(l0.desc())
+        g.upload(*R.initial_state(l0), t=0)
+        ibm = O.OracleIBM()
+        for b in ibs:
+            ibm.add_body(g, b["positions"])
+        ibm.initialise()
+        got = []
+        for ib in range(len(ibs)):
+            mk = ibm.markers(ib)
+            got += [[ib, m, *mk[m, 0:3], mk[m, 6], mk[m, 7]] for m in range(mk.shape[0])]
+        assert np.array_equal(np.array(got), z[run + "/markers"])
+
+
+def test_cloud_reader_quirks():
+    """io_readInCloud's stream reading: a line without values (the one after
+    a final newline) repeats the previous point, a missing z keeps the
+    previous z; std::round rounds halves away from zero."""
+    from luma_gb300 import geometry
+    pts = geometry.read_cloud("1 2 3\n4 5\n", 3)
+    assert pts == [(1.0, 2.0, 3.0), (4.0, 5.0, 3.0), (4.0, 5.0, 3.0)]
+    assert geometry.read_cloud("1 2 3\n4 5", 2) == [(1.0, 2.0, 0.0), (4.0, 5.0, 0.0)]
+    with pytest.raises(ValueError):
+        geometry.read_cloud("\n1 2 3", 3)
+    assert [geometry._cround(v) for v in (0.5, 1.5, 2.5, -0.5, -2.5, 2.4999)] == [1, 2, 3, -1, -3, 2]
