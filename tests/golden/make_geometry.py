@@ -7,14 +7,17 @@ ds after ibm_initialise:
   circle, a FILAMENT_ARRAY of two flexible filaments (CONFORMING elements),
   a rotated square and a rigid filament;
 * ``oracle/cases/geom_d3q19.h`` (3D): a sphere, a rotated cube, a plate and
-  two rigid filaments.
+  two rigid filaments;
+* ``oracle/cases/geom_refine_d2q9.h`` (2D, one refined region) for the
+  point clouds placed on level 1.
 
 Output: ``geometry_prefab.json`` beside this script.
 
 FROM_FILE point clouds (seeded synthetic clouds written here): for each run
 of ``CLOUD_RUNS`` the cloud files go to the run's ``input/`` folder and
 ``geometry_cloud.npz`` stores the cloud texts, the config, the level-0
-labels, velocity and density after the reader (BBB labelling), the IB
+labels, velocity and density of every grid after the reader (BBB
+labelling; one run puts clouds on a refined level), the IB
 markers (as above) and, for BFL runs, the body's Q table and per-site marker
 lookup (``--bfl-out``).
 
@@ -96,6 +99,11 @@ CLOUD_RUNS = {
                    "FROM_FILE BBB box.txt 0 0 START 1.2 START 0.1 CENTRE 0.5 0.2 Z RIGID CLAMPED\n"),
     "bfl_3d": ("bfl_sphere_d3q19",
                "FROM_FILE BFL ellipsoid.txt 0 0 CENTRE 0.6 CENTRE 0.5 CENTRE 0.5 0.4 X RIGID CLAMPED\n"),
+    "levels_2d": ("geom_refine_d2q9",
+                  "FROM_FILE IBM ellipse.txt 1 0 CENTRE 0.7 CENTRE 0.55 START 0.0 0.15 X RIGID CLAMPED\n"
+                  "FROM_FILE BBB disc.txt 1 0 CENTRE 0.9 CENTRE 0.4 START 0.0 0.08 X RIGID CLAMPED\n"
+                      "FROM_FILE BBB bar.txt 1 0 START 0.6 START 0.3 START 0.0 0.5 X RIGID CLAMPED\n"
+                      "FROM_FILE BBB disc.txt 0 0 START 1.4 CENTRE 0.5 START 0.0 0.15 Y RIGID CLAMPED\n"),
 }
 
 
@@ -121,12 +129,13 @@ def make_clouds(ref: str) -> str:
         bfl = os.path.join(work, "bfl.txt")
         subprocess.run([exe, "--out", os.path.join(work, "out"), "--steps", "0", "--dump-every", "0",
                         "--workdir", work, "--bfl-out", bfl], check=True, timeout=600)
-        s0 = os.path.join(work, "out", "s0", "L0R0_")
-        lv = _level0(s0)
         store[run + "/case"] = np.array(case)
         store[run + "/config"] = np.array(config)
-        for k, v in lv.items():
-            store[run + "/" + k] = v
+        for meta in sorted(os.listdir(os.path.join(work, "out", "s0"))):
+            if meta.endswith("_meta.txt"):
+                key = meta[:-len("_meta.txt")]
+                for k, v in _level0(os.path.join(work, "out", "s0", key + "_")).items():
+                    store[run + "/" + key + "/" + k] = v
         mk_path = os.path.join(work, "out", "s0", "markers.txt")
         if os.path.exists(mk_path):
             mk = np.loadtxt(mk_path, ndmin=2)

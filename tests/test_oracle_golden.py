@@ -306,7 +306,11 @@ def test_guo_forcing_moments(Q, dims):
 GEOM_DEFS = {
     "geom_d3q19": dict(dims=3, resolution=20, timestep=1.0 / 500.0, bx=2.0, by=1.0, bz=1.0, re=100, ux0=1.0,
                        ibm=True, walls=(A.VELOCITY, A.EXTRAPOLATE_RIGHT, A.SOLID, A.SOLID, A.FLUID, A.FLUID)),
+    "geom_refine_d2q9": dict(dims=2, resolution=40, timestep=1.0 / 800.0, bx=2.0, by=1.0, re=50, ux0=1.0,
+                             no_flow=False, ibm=True,
+                             walls=(A.VELOCITY, A.EXTRAPOLATE_RIGHT, A.SOLID, A.SOLID, A.FLUID, A.FLUID)),
 }
+GEOM_REGIONS = {"geom_refine_d2q9": [((0.5, 0.25, 0.0), (1.0, 0.75, 0.0))]}
 
 
 @pytest.mark.parametrize("run", [0, 1], ids=["2d", "3d"])
@@ -357,39 +361,51 @@ def test_geometry_reader_bfl_entries():
         assert np.array_equal(b["body"].site_marker, l0.bfl.site_marker)
 
 
-@pytest.mark.parametrize("run", ["ibm_bbb_2d", "bfl_2d", "ibm_bbb_3d", "bfl_3d"])
+@pytest.mark.parametrize("run", ["ibm_bbb_2d", "bfl_2d", "ibm_bbb_3d", "bfl_3d", "levels_2d"])
 def test_geometry_reader_clouds_match_reference(run):
     """FROM_FILE point clouds (IBM, BFL, BBB; seeded clouds partly off the
-    grid, CENTRE and START references) give the reference reader's labels,
-    velocity and density, IB markers (position, epsilon, ds after
-    initialisation) and BFL Q table and site lookup
-    (tests/golden/make_geometry.py)."""
+    grid, CENTRE and START references, on level 0 and on a refined level)
+    give the reference reader's labels, velocity and density on every grid,
+    IB markers (position, epsilon, ds after initialisation) and BFL Q table
+    and site lookup (tests/golden/make_geometry.py)."""
     from luma_gb300 import geometry
     z = np.load(os.path.join(R.HERE, "geometry_cloud.npz"))
     clouds = {k.split("/", 1)[1]: str(z[k]) for k in z.files if k.startswith("cloud/")}
     name, config = str(z[run + "/case"]), str(z[run + "/config"])
-    defs = CASES.CASES[name]["defs"] if name in CASES.CASES else hostcase.Definitions(**GEOM_DEFS[name])
-    l0 = hostcase.build_level0(defs)
-    bodies = geometry.read_geometry(config, {(0, 0): l0}, clouds=clouds)
+    if name in CASES.CASES:
+        grids = [hostcase.build_level0(CASES.CASES[name]["defs"])]
+    else:
+        grids = [hostcase.build_level0(hostcase.Definitions(**GEOM_DEFS[name]))]
+    for r in GEOM_REGIONS.get(name, []):
+        grids.append(hostcase.build_subgrid(grids[-1], r[0], r[1]))
+    levels = {(g.level, g.region): g for g in grids}
+    states = [R.initial_state(g) for g in grids]  # the populations predate the reader
+    bodies = geometry.read_geometry(config, levels, clouds=clouds)
     for b in bodies:
         if b["kind"] == "bbb":
-            geometry.apply_bbb(l0, b)
-    typ = l0.typ
+            geometry.apply_bbb(levels[(b["level"], b["region"])], b)
+    typ = {k: g.typ for k, g in levels.items()}
     for b in bodies:
         if b["kind"] == "bfl":
-            typ = b["body"].typ.reshape(-1)
+            typ[(b["level"], b["region"])] = b["body"].typ.reshape(-1)
             assert np.array_equal(b["body"].q, z[run + "/bfl_q"])
             assert np.array_equal(b["body"].site_marker, z[run + "/bfl_marker"])
-    assert np.array_equal(typ, z[run + "/typ"])
-    assert np.array_equal(l0.u, z[run + "/u"]) and np.array_equal(l0.rho, z[run + "/rho"])
+    keys = sorted({k.split("/")[1] for k in z.files if k.startswith(run + "/L")})
+    assert keys == sorted(f"L{lv}R{rg}" for lv, rg in levels)
+    for (lv, rg), g in levels.items():
+        key = f"{run}/L{lv}R{rg}/"
+        assert np.array_equal(typ[(lv, rg)], z[key + "typ"]), (lv, rg)
+        assert np.array_equal(g.u, z[key + "u"]) and np.array_equal(g.rho, z[key + "rho"]), (lv, rg)
     ibs = [b for b in bodies if b["kind"] == "ibm"]
     assert bool(ibs) == (run + "/markers" in z.files)
     if ibs:
-        g = O.OracleGrid(l0.desc())
-        g.upload(*R.initial_state(l0), t=0)
+        og = {}
+        for g, st in zip(grids, states):
+            og[(g.level, g.region)] = O.OracleGrid(g.desc(), og.get((g.level - 1, 0)))
+            og[(g.level, g.region)].upload(*st, t=0)
         ibm = O.OracleIBM()
         for b in ibs:
-            ibm.add_body(g, b["positions"])
+            ibm.add_body(og[(b["level"], b["region"])], b["positions"])
         ibm.initialise()
         got = []
         for ib in range(len(ibs)):
