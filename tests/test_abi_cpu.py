@@ -14,9 +14,19 @@ HEADER = os.path.join(ROOT, "include", "luma_gpu.h")
 LIB = os.path.join(ROOT, "luma_gb300", "_build", "libluma_gpu.so")
 
 
+def declarations():
+    """(name, [parameter declarations]) of every function the header
+    declares."""
+    src = re.sub(r"/\*.*?\*/", "", open(HEADER).read(), flags=re.S)
+    out = []
+    for m in re.finditer(r"^\s*(?:int|const char \*)\s*(luma_\w+)\s*\(([^)]*)\)\s*;", src, re.M):
+        params = [p.strip() for p in m.group(2).split(",") if p.strip() and p.strip() != "void"]
+        out.append((m.group(1), params))
+    return out
+
+
 def declared_functions():
-    src = open(HEADER).read()
-    return sorted(set(re.findall(r"^\s*(?:int|const char \*)\s*(luma_gpu_\w+)\s*\(", src, re.M)))
+    return sorted({name for name, _ in declarations()})
 
 
 @pytest.fixture(scope="module")
@@ -39,6 +49,46 @@ def test_header_declares_entry_points():
 def test_library_exports_every_declared_symbol(lib):
     for name in declared_functions():
         assert hasattr(lib, name), name
+
+
+def _ctype(param: str):
+    if "*" in param or "[" in param:
+        return C.c_void_p
+    if param.startswith("double"):
+        return C.c_double
+    if param.startswith("size_t"):
+        return C.c_size_t
+    if param.startswith("int64_t"):
+        return C.c_int64
+    assert param.startswith("int"), param
+    return C.c_int
+
+
+# entry points for which every argument zero or null is a valid call
+NULL_OK = {"luma_gpu_grid_destroy", "luma_gpu_abi_version", "luma_gpu_last_error_string"}
+
+
+def test_every_entry_point_refuses_null_arguments(lib):
+    """With every pointer null and every number zero, each entry point
+    returns an error status (no CUDA call happens first, so this runs on a
+    host without a GPU) and sets a message; destroying a null grid is a
+    no-op."""
+    lib.luma_gpu_last_error_string.restype = C.c_char_p
+    names = []
+    for name, params in declarations():
+        if name in NULL_OK:
+            continue
+        fn = getattr(lib, name)
+        fn.restype = C.c_int
+        fn.argtypes = [_ctype(p) for p in params]
+        args = [None if t is C.c_void_p else 0 for t in fn.argtypes]
+        rc = fn(*args)
+        assert rc in (A.LUMA_E_INVALID, A.LUMA_E_STATE), (name, rc)
+        assert lib.luma_gpu_last_error_string(), name
+        names.append(name)
+    assert len(names) >= 28
+    lib.luma_gpu_grid_destroy.argtypes = [C.c_void_p]
+    assert lib.luma_gpu_grid_destroy(None) == A.LUMA_OK
 
 
 def test_abi_version_and_error_string(lib):
