@@ -99,8 +99,9 @@ def test_abi_version_and_error_string(lib):
 
 
 def test_invalid_descriptor_rejected_without_gpu(lib):
-    """Descriptor validation runs before any CUDA call: a wrong ABI version
-    and an unsupported lattice come back as LUMA_E_INVALID."""
+    """Descriptor validation runs before any CUDA call: a wrong ABI version,
+    an unsupported lattice, 3D KBC off D3Q27, more sites than 32-bit ids
+    address and empty or 2D-with-depth grids come back as LUMA_E_INVALID."""
     lib.luma_gpu_grid_create.argtypes = [C.POINTER(A.GridDesc), C.c_void_p, C.POINTER(C.c_void_p)]
     lib.luma_gpu_last_error_string.restype = C.c_char_p
     d = A.GridDesc()
@@ -117,6 +118,16 @@ def test_invalid_descriptor_rejected_without_gpu(lib):
     d.omega = 1.5
     assert lib.luma_gpu_grid_create(C.byref(d), None, C.byref(h)) == A.LUMA_E_INVALID
     assert b"D3Q27" in lib.luma_gpu_last_error_string()
+    # site ids are 32-bit: at most 2^31-1 sites per grid (1291^3 is above)
+    d.N = d.M = d.K = 1291
+    assert lib.luma_gpu_grid_create(C.byref(d), None, C.byref(h)) == A.LUMA_E_INVALID
+    assert b"2^31-1" in lib.luma_gpu_last_error_string()
+    d.N, d.M, d.K = 0, 4, 4
+    assert lib.luma_gpu_grid_create(C.byref(d), None, C.byref(h)) == A.LUMA_E_INVALID
+    assert b"bad grid size" in lib.luma_gpu_last_error_string()
+    d.dims, d.Q, d.N, d.M, d.K = 2, 9, 4, 4, 2  # 2D grids have K = 1
+    assert lib.luma_gpu_grid_create(C.byref(d), None, C.byref(h)) == A.LUMA_E_INVALID
+    assert not h.value
 
 
 def test_desc_struct_size_matches_header():
