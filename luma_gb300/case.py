@@ -20,6 +20,7 @@ bit-identical to those the reference computes.
 from __future__ import annotations
 
 import math
+import re
 from dataclasses import dataclass, field
 
 import numpy as np
@@ -223,6 +224,90 @@ def _initial_velocity(defs: Definitions, typ: np.ndarray, prof: np.ndarray) -> n
     u[use] = prof_b[use]
     u[typ == A.SOLID] = 0.0
     return u
+
+
+_NUMBER = re.compile(r"[+-]?(?:\d+\.?\d*|\.\d+)?(?:[eE][+-]?\d*)?")
+
+
+class _StreamReader:
+    """Formatted extraction of doubles from one std::istringstream that is
+    refilled line by line with str() + seekg(0), as
+    GridUtils::readVelocityFromFile does: seekg clears only end-of-file, so
+    once an extraction has failed every later one fails too and leaves the
+    variable as it was; an extraction that finds no whitespace-delimited
+    remainder fails without touching the variable; one that finds
+    characters that do not form a number stores 0 and fails."""
+
+    def __init__(self):
+        self.failed = False
+        self.line = ""
+        self.pos = 0
+        self.tmp = None
+
+    def reset(self, line: str) -> None:
+        self.line, self.pos = line, 0
+
+    def extract(self) -> float | None:
+        if self.failed:
+            return self.tmp
+        while self.pos < len(self.line) and self.line[self.pos].isspace():
+            self.pos += 1
+        if self.pos >= len(self.line):
+            self.failed = True
+            return self.tmp
+        m = _NUMBER.match(self.line, self.pos)
+        text = m.group(0)
+        mant = re.match(r"[+-]?(\d+\.?\d*|\.\d+)", text)
+        exp = text[mant.end():] if mant else ""
+        if not mant or (exp and not re.fullmatch(r"[eE][+-]?\d+", exp)):
+            self.pos = m.end()
+            self.failed = True
+            self.tmp = 0.0
+            return self.tmp
+        self.pos = m.end()
+        self.tmp = float(text)
+        return self.tmp
+
+
+def initial_velocity_from_file(text: str, l0: "Level0") -> np.ndarray:
+    """Level-0 velocity under L_INIT_VELOCITY_FROM_FILE (LBM_initVelocity,
+    src/GridObj_init_grids.cpp:42-78, with GridUtils::readVelocityFromFile,
+    src/GridUtils.cpp:1467-1524) from the text of
+    ``input/initial_velocity.in``: one point "x y z ux uy uz" per line in
+    dimensionless units, read with the stream semantics of ``_StreamReader``
+    (the empty line after a final newline adds a point repeating the last
+    value read); the first N*M*K points in file order are applied, each to
+    the site enclosing its position (points off the grid are skipped, later
+    points overwrite earlier ones), as u * dt / dh; every other site keeps
+    u = 0 (no profile, no zeroing of solid sites).  Fewer points than sites
+    raise ValueError, as the reference stops there."""
+    rd = _StreamReader()
+    cols = [[] for _ in range(6)]
+    lines = text.split("\n")
+    for line in lines:
+        rd.reset(line)
+        for c in cols:
+            c.append(rd.extract())
+    n = l0.N * l0.M * l0.K
+    if len(cols[0]) < n:
+        raise ValueError(f"initial velocity file has {len(cols[0])} points for {n} sites")
+    if any(v is None for c in cols for v in c[:n]):
+        raise ValueError("initial velocity file: a value read before any number (uninitialised in the reference)")
+    D = l0.defs.dims
+    E = l0.global_edges
+    u = np.zeros((l0.N, l0.M, l0.K, D))
+    for p in range(n):
+        x, y, z = cols[0][p], cols[1][p], cols[2][p]
+        if not (E[0] <= x < E[1] and E[2] <= y < E[3] and (D != 3 or E[4] <= z < E[5])):
+            continue
+        i = int(math.floor((x - E[0]) / l0.dh))
+        j = int(math.floor((y - E[2]) / l0.dh))
+        k = int(math.floor((z - E[4]) / l0.dh)) if D == 3 else 0
+        if not (0 <= i < l0.N and 0 <= j < l0.M and 0 <= k < l0.K):
+            continue
+        for d in range(D):
+            u[i, j, k, d] = (cols[3 + d][p] * l0.dt) / l0.dh
+    return u.reshape(-1)
 
 
 def build_level0(defs: Definitions) -> Level0:

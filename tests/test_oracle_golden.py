@@ -425,3 +425,47 @@ def test_cloud_reader_quirks():
     with pytest.raises(ValueError):
         geometry.read_cloud("\n1 2 3", 3)
     assert [geometry._cround(v) for v in (0.5, 1.5, 2.5, -0.5, -2.5, 2.4999)] == [1, 2, 3, -1, -3, 2]
+
+
+INITVEL_DEFS = {
+    "initvel_d2q9": dict(dims=2, resolution=20, timestep=1.0 / 400.0, bx=2.0, by=1.0, re=50, ux0=1.0,
+                         no_flow=False,
+                         walls=(A.VELOCITY, A.EXTRAPOLATE_RIGHT, A.SOLID, A.SOLID, A.FLUID, A.FLUID)),
+    "initvel_d3q19": dict(dims=3, resolution=4, timestep=1.0 / 80.0, bx=3.0, by=2.0, bz=1.5, re=10, ux0=0.0,
+                          no_flow=False),
+}
+
+
+@pytest.mark.parametrize("name", sorted(INITVEL_DEFS))
+def test_initial_velocity_file_matches_reference(name):
+    """L_INIT_VELOCITY_FROM_FILE: the level-0 velocity and populations the
+    reference starts from, for shuffled seeded files with duplicates, points
+    off the grid, more points than sites and (3D) a short line that freezes
+    every later value (tests/golden/make_initvel.py)."""
+    z = np.load(os.path.join(R.HERE, "initial_velocity.npz"))
+    d = hostcase.Definitions(**INITVEL_DEFS[name])
+    l0 = hostcase.build_level0(d)
+    u = hostcase.initial_velocity_from_file(str(z[name + "/text"]), l0)
+    assert np.array_equal(u, z[name + "/u"])
+    f = hostcase.equilibrium(d.dims, d.Q, l0.rho, u).reshape(-1)
+    assert np.array_equal(f, z[name + "/f"])
+    with pytest.raises(ValueError):
+        hostcase.initial_velocity_from_file("\n".join(str(z[name + "/text"]).split("\n")[:100]), l0)
+
+
+def test_velocity_stream_reader_semantics():
+    """The stream rules the initial-velocity reader relies on: a missing
+    value keeps the variable, a non-number stores 0, and after either every
+    later extraction fails."""
+    rd = hostcase._StreamReader()
+    rd.reset("1.5 2e1 -.25")
+    assert [rd.extract() for _ in range(3)] == [1.5, 20.0, -0.25]
+    assert rd.extract() == -0.25 and rd.failed
+    rd.reset("7 8 9")
+    assert rd.extract() == -0.25
+    rd = hostcase._StreamReader()
+    rd.reset("3 abc 4")
+    assert [rd.extract(), rd.extract(), rd.extract()] == [3.0, 0.0, 0.0]
+    rd = hostcase._StreamReader()
+    rd.reset("1e+ 5")
+    assert rd.extract() == 0.0 and rd.failed
