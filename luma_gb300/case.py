@@ -47,6 +47,7 @@ class Definitions:
     uz0: float = 0.0               # L_UZ0
     rho_in: float = 1.0            # L_RHOIN
     parabolic_inlet: bool = False  # L_PARABOLIC_INLET
+    inlet_profile: str | None = None  # L_USE_INLET_PROFILE: text of input/inlet_profile.in
     no_flow: bool = True           # L_NO_FLOW
     velocity_ramp: float = 0.0     # L_VELOCITY_RAMP (0 = undefined)
     reynolds_ramp: float = 0.0     # L_REYNOLDS_RAMP (0 = undefined)
@@ -310,6 +311,52 @@ def initial_velocity_from_file(text: str, l0: "Level0") -> np.ndarray:
     return u.reshape(-1)
 
 
+def inlet_profile_from_file(text: str, ypos: np.ndarray) -> tuple:
+    """L_USE_INLET_PROFILE (_LBM_initGetInletProfileFromFile,
+    src/GridObj_init_grids.cpp:1234-1314): the points of
+    ``input/inlet_profile.in`` ("x y z ux uy uz" lines, read as
+    ``initial_velocity_from_file`` reads, so a final newline appends a point
+    whose every value is the last one read), taken in file order for each
+    site row y: below the first point, linear extrapolation from the first
+    two; above the last, from the last two; between two consecutive points,
+    linear interpolation; on a point, its values.  The values are used as
+    they are (lattice units); a row no rule reaches keeps 0."""
+    rd = _StreamReader()
+    cols = [[] for _ in range(6)]
+    for line in text.split("\n"):
+        rd.reset(line)
+        for c in cols:
+            c.append(rd.extract())
+    if any(v is None for c in cols for v in c):
+        raise ValueError("inlet profile file: a value read before any number (uninitialised in the reference)")
+    yb, ub = cols[1], cols[3:6]
+    if len(yb) < 2:
+        raise ValueError("inlet profile file: the rules need at least two points")
+    M = ypos.size
+    out = [np.zeros(M), np.zeros(M), np.zeros(M)]
+    last = len(yb) - 1
+    for j in range(M):
+        y = float(ypos[j])
+        for i in range(len(yb)):
+            if i == 0 and yb[i] > y:
+                for o, u in zip(out, ub):
+                    o[j] = -(u[i + 1] - u[i]) + u[i]
+                break
+            if i == last and yb[i] < y:
+                for o, u in zip(out, ub):
+                    o[j] = (u[i] - u[i - 1]) + u[i]
+                break
+            if yb[i] < y and yb[i + 1] > y:
+                for o, u in zip(out, ub):
+                    o[j] = ((u[i + 1] - u[i]) / (yb[i + 1] - yb[i])) * (y - yb[i]) + u[i]
+                break
+            if yb[i] == y:
+                for o, u in zip(out, ub):
+                    o[j] = u[i]
+                break
+    return tuple(out)
+
+
 def build_level0(defs: Definitions) -> Level0:
     N, M, K = defs.sizes()
     dh = 1.0 / float(defs.resolution)
@@ -347,7 +394,9 @@ def build_level0(defs: Definitions) -> Level0:
             label((slice(None), slice(j, j + 1), slice(None)), top)
 
     # Inlet profile.
-    if defs.parabolic_inlet:
+    if defs.inlet_profile is not None:
+        ux_in, uy_in, uz_in = inlet_profile_from_file(defs.inlet_profile, ypos)
+    elif defs.parabolic_inlet:
         b = edges[3] - wt[3]
         p = (b + wt[2]) / 2.0
         q = b - p
@@ -384,6 +433,8 @@ def build_level0(defs: Definitions) -> Level0:
 def _inlet_profile(defs: Definitions, ypos: np.ndarray, dt: float, dh: float, edges0) -> tuple:
     """_LBM_initSetInletProfile (src/GridObj_init_grids.cpp:1322-1360) on any grid."""
     M = ypos.size
+    if defs.inlet_profile is not None:
+        return inlet_profile_from_file(defs.inlet_profile, ypos)
     if defs.parabolic_inlet:
         wt_top = defs.wall_cells[3] / float(defs.resolution)
         wt_bot = defs.wall_cells[2] / float(defs.resolution)

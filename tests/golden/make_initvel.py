@@ -1,5 +1,6 @@
 """The reference's initial-velocity reader (L_INIT_VELOCITY_FROM_FILE) on
-seeded velocity files, as level-0 velocity and populations.
+seeded velocity files, as level-0 velocity and populations; and its
+inlet-profile reader (L_USE_INLET_PROFILE) on a refined channel.
 
 Builds ``oracle/cases/initvel_d2q9.h`` (2D channel 40 x 20) and
 ``initvel_d3q19.h`` (periodic 12 x 8 x 6) with the reference's serial
@@ -10,6 +11,10 @@ points off the grid, shuffled, with a final newline; the 2D file's
 ordering leaves some sites unset (only the first N*M*K points count) and
 the 3D file has a short line among the last points that count (every later
 value repeats the last one read).
+
+``oracle/cases/inletfile_refine_d2q9.h`` (80 x 40 channel with a refined
+region) reads ``input/inlet_profile.in`` (five points, a final newline);
+stored: the text and every grid's inlet profile, velocity and populations.
 
 Output: ``initial_velocity.npz`` beside this script.
 
@@ -54,6 +59,13 @@ def velocity_text(case: str, seed: int) -> str:
     return "\n".join(lines) + "\n"
 
 
+PROFILE_TEXT = ("0.0 0.1 0.0 0.020 0.001 0.3\n"
+                "0.0 0.3 0.0 0.045 -0.002 0.1\n"
+                "0.0 0.5125 0.0 0.050 0.000 0.2\n"
+                "0.0 0.7 0.0 0.040 0.003 0.4\n"
+                "0.0 0.85 0.0 0.025 0.001 0.6\n")
+
+
 def main() -> int:
     ap = argparse.ArgumentParser(description=__doc__)
     ap.add_argument("--ref", default=build_ref.DEFAULT_REF)
@@ -73,6 +85,20 @@ def main() -> int:
         store[case + "/u"] = np.fromfile(s0 + "u.bin", dtype=np.float64)
         store[case + "/f"] = np.fromfile(s0 + "f.bin", dtype=np.float64)
         print(case, len(text.splitlines()), "lines")
+    case = "inletfile_refine_d2q9"
+    exe = build_ref.build_case(case, a.ref)
+    work = tempfile.mkdtemp(prefix="inletfile_")
+    os.makedirs(os.path.join(work, "input"))
+    with open(os.path.join(work, "input", "inlet_profile.in"), "w") as fp:
+        fp.write(PROFILE_TEXT)
+    subprocess.run([exe, "--out", os.path.join(work, "out"), "--steps", "0", "--dump-every", "0",
+                    "--workdir", work], check=True, timeout=300)
+    store[case + "/text"] = np.array(PROFILE_TEXT)
+    for key in ("L0R0", "L1R0"):
+        s0 = os.path.join(work, "out", "s0", key + "_")
+        for name in ("uxin", "u", "f"):
+            store[f"{case}/{key}/{name}"] = np.fromfile(s0 + name + ".bin", dtype=np.float64)
+    print(case)
     dst = os.path.join(HERE, "initial_velocity.npz")
     np.savez_compressed(dst, **store)
     print(dst)

@@ -469,3 +469,24 @@ def test_velocity_stream_reader_semantics():
     rd = hostcase._StreamReader()
     rd.reset("1e+ 5")
     assert rd.extract() == 0.0 and rd.failed
+
+
+def test_inlet_profile_file_matches_reference():
+    """L_USE_INLET_PROFILE on a refined channel: every grid's inlet profile,
+    initial velocity and populations equal the reference's, including the
+    point a final newline appends (its y is the last value read), which
+    sets the top rows by extrapolation (tests/golden/make_initvel.py)."""
+    z = np.load(os.path.join(R.HERE, "initial_velocity.npz"))
+    case = "inletfile_refine_d2q9"
+    d = hostcase.Definitions(dims=2, resolution=40, timestep=1.0 / 800.0, bx=2.0, by=1.0, re=50, ux0=1.0,
+                             no_flow=False, inlet_profile=str(z[case + "/text"]),
+                             walls=(A.VELOCITY, A.EXTRAPOLATE_RIGHT, A.SOLID, A.SOLID, A.FLUID, A.FLUID))
+    g0 = hostcase.build_level0(d)
+    g1 = hostcase.build_subgrid(g0, (0.5, 0.25, 0.0), (1.0, 0.75, 0.0))
+    for g, key in ((g0, "L0R0"), (g1, "L1R0")):
+        assert np.array_equal(g.ux_in, z[f"{case}/{key}/uxin"]), key
+        assert np.array_equal(g.u, z[f"{case}/{key}/u"]), key
+        f = hostcase.equilibrium(2, 9, g.rho, g.u).reshape(-1)
+        assert np.array_equal(f, z[f"{case}/{key}/f"]), key
+    with pytest.raises(ValueError):
+        hostcase.inlet_profile_from_file("0 0.5 0 0.1 0 0", g0.ypos)
