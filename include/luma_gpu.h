@@ -88,6 +88,9 @@ enum {
                                         and u_p u_q (p <= q) updated by every macroscopic update
                                         (_LBM_macro_opt, :895-917); not with regularised BCs or
                                         flexible bodies (LUMA_E_INVALID) */
+#define LUMA_FLAG_UNIVERSAL_EPSILON 0x100 /* L_UNIVERSAL_EPSILON_CALC: one epsilon system over all IB
+                                              bodies of the grid's level (rigid bodies, one region per
+                                              level) */
 #define LUMA_FLAG_SPLIT_INTERIOR 0x40 /* two-buffer step: run interior fluid sites in their
                                        own kernel at any grid size (by default only grids
                                        of 2^18 sites or more split) */
@@ -193,6 +196,17 @@ int luma_gpu_reduce_fields_noalloc(const uint8_t *typ, const double *rho, const 
                                    int dims, void *cuda_stream, luma_reduction *out);
 
 /* ---- immersed-boundary bodies (grids created with LUMA_FLAG_IBM) -------- */
+/* Host-only: the set-up luma_gpu_ibm_initialise runs for rigid bodies on one
+ * grid (support search, marker spacing ds, epsilon system; the reference's
+ * ObjectManager::ibm_initialise, src/ObjectManager_ops_ibm.cpp:190-246),
+ * for `nbodies` bodies of nmarkers[b] markers at positions[3*m + d]
+ * (bodies concatenated), on the grid `desc` describes (sizes, dh, level,
+ * site positions and global_edges read).  universal != 0 solves one
+ * epsilon system over all the bodies (L_UNIVERSAL_EPSILON_CALC, :773-920
+ * with :1067-1142).  Writes eps, ds and (if not NULL) each marker's
+ * support count, per marker.  No device call. */
+int luma_ibm_setup_host(const luma_grid_desc *desc, int nbodies, const int *nmarkers, const double *positions,
+                        int universal, double *eps, double *ds, int *nsupports);
 /* Adds a rigid body of `nmarkers` Lagrangian markers to the grid that owns
  * it: positions[3*m + d] in the reference's length units, optional marker
  * velocities (lattice units, NULL = stationary).  Replaces the body

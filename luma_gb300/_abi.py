@@ -37,6 +37,7 @@ FLAG_FIX_KBC = 0x10
 FLAG_TWO_BUFFER = 0x20
 FLAG_SPLIT_INTERIOR = 0x40
 FLAG_TIME_AVERAGES = 0x80
+FLAG_UNIVERSAL_EPSILON = 0x100
 
 _dp = C.POINTER(C.c_double)
 _ip = C.POINTER(C.c_int32)

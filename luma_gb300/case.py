@@ -57,6 +57,7 @@ class Definitions:
     smagorinsky: bool = False      # L_USE_BGKSMAG
     csmag: float = 0.3             # L_CSMAG
     ibm: bool = False              # L_IBM_ON
+    universal_epsilon: bool = False  # L_UNIVERSAL_EPSILON_CALC
     gravity: bool = False          # L_GRAVITY_ON
     gravity_force: float = 0.0     # L_GRAVITY_FORCE
     gravity_dir: int = 0           # L_GRAVITY_DIRECTION
@@ -124,6 +125,8 @@ class Level0:
             fl |= A.FLAG_GRAVITY
         if d.time_averages:
             fl |= A.FLAG_TIME_AVERAGES
+        if d.universal_epsilon:
+            fl |= A.FLAG_UNIVERSAL_EPSILON
         if fix_macro3d:
             fl |= A.FLAG_FIX_MACRO3D
         if fix_kbc:

@@ -36,23 +36,38 @@ const luma_gpu_grid *root_of(const luma_gpu_grid *g) {
     return g;
 }
 
-double grid_start(const luma_gpu_grid *g, int axis) {
-    const std::vector<double> &p = axis == 0 ? g->hx : (axis == 1 ? g->hy : g->hz);
-    return g->d.level == 0 ? 0.0 : p[0] - g->d.dh / 2.0;
+// What the rigid-body set-up reads of a grid: sizes, spacing, site
+// positions and the level-0 edges.  Built from a device grid or, for the
+// host-only entry point, from a grid descriptor.
+struct GridView {
+    int dims, N, M, K, level;
+    double dh;
+    const double *x, *y, *z;  // site positions
+    const double *E;          // level-0 global edges
+};
+
+GridView view_of(const luma_gpu_grid *g) {
+    return GridView{g->d.dims, g->d.N, g->d.M, g->d.K, g->d.level, g->d.dh,
+                    g->hx.data(), g->hy.data(), g->hz.data(), root_of(g)->d.global_edges};
 }
 
-void support_delta(const luma_gpu_grid *g, const IbmBody &b, int m, const double est[3], double *out) {
-    const double dh = g->d.dh;
+double grid_start(const GridView &g, int axis) {
+    const double *p = axis == 0 ? g.x : (axis == 1 ? g.y : g.z);
+    return g.level == 0 ? 0.0 : p[0] - g.dh / 2.0;
+}
+
+void support_delta(const GridView &g, const IbmBody &b, int m, const double est[3], double *out) {
+    const double dh = g.dh;
     const double *x = &b.pos[3 * m];
     double v = delta_kernel((est[0] - x[0]) / dh, b.dil[m]) * delta_kernel((est[1] - x[1]) / dh, b.dil[m]);
-    if (g->d.dims == 3) v = v * delta_kernel((est[2] - x[2]) / dh, b.dil[m]);
+    if (g.dims == 3) v = v * delta_kernel((est[2] - x[2]) / dh, b.dil[m]);
     *out = v;
 }
 
-int find_support(const luma_gpu_grid *g, IbmBody &b) {
-    const int D = g->d.dims;
-    const double dh = g->d.dh;
-    const double *E = root_of(g)->d.global_edges;
+int find_support(const GridView &g, IbmBody &b) {
+    const int D = g.dims;
+    const double dh = g.dh;
+    const double *E = g.E;
     b.off.assign(b.nm + 1, 0);
     b.si.clear(); b.sj.clear(); b.sk.clear();
     b.sx.clear(); b.sy.clear(); b.sz.clear(); b.delta.clear();
@@ -69,9 +84,9 @@ int find_support(const luma_gpu_grid *g, IbmBody &b) {
         const int in = (int)std::floor((x[0] - grid_start(g, 0)) / dh);
         const int jn = (int)std::floor((x[1] - grid_start(g, 1)) / dh);
         const int kn = D == 3 ? (int)std::floor((x[2] - grid_start(g, 2)) / dh) : 0;
-        if (in < 0 || jn < 0 || kn < 0 || in >= g->d.N || jn >= g->d.M || kn >= g->d.K)
+        if (in < 0 || jn < 0 || kn < 0 || in >= g.N || jn >= g.M || kn >= g.K)
             return luma_set_error(LUMA_E_DOMAIN, "IB marker %d is no longer inside its grid", m);
-        const double near[3] = {g->hx[in], g->hy[jn], D == 3 ? g->hz[kn] : 0.0};
+        const double near[3] = {g.x[in], g.y[jn], D == 3 ? g.z[kn] : 0.0};
         push(in, jn, kn, near, m);
         for (int i = in - 5; i <= in + 5; i++)
             for (int j = jn - 5; j <= jn + 5; j++)
@@ -84,7 +99,7 @@ int find_support(const luma_gpu_grid *g, IbmBody &b) {
                     const bool in_domain = !(est[0] < E[0] || est[0] > E[1] || est[1] < E[2] || est[1] > E[3] ||
                                              (D == 3 && (est[2] < E[4] || est[2] > E[5])));
                     if (in_cage && in_domain && (i != in || j != jn || (D == 3 && k != kn))) {
-                        if (i < 0 || j < 0 || k < 0 || i >= g->d.N || j >= g->d.M || k >= g->d.K)
+                        if (i < 0 || j < 0 || k < 0 || i >= g.N || j >= g.M || k >= g.K)
                             return luma_set_error(LUMA_E_DOMAIN, "IB marker %d has supports off its grid", m);
                         push(i, j, k, est, m);
                     }
@@ -94,8 +109,8 @@ int find_support(const luma_gpu_grid *g, IbmBody &b) {
     return LUMA_OK;
 }
 
-void compute_ds(const luma_gpu_grid *g, IbmBody &b) {
-    const double dh = g->d.dh;
+void compute_ds(const GridView &g, IbmBody &b) {
+    const double dh = g.dh;
     for (int m = 0; m < b.nm; ++m) {
         double ds = 10.0;
         for (int n = 0; n < b.nm; ++n) {
@@ -143,26 +158,58 @@ void lu_solve_transposed(int n, std::vector<double> &a, std::vector<double> &x) 
 #undef A_
 }
 
-void find_epsilon(const luma_gpu_grid *g, IbmBody &b) {
-    const int n = b.nm, D = g->d.dims;
-    const double dh = g->d.dh;
+// One epsilon system over the markers of `set`, concatenated in order:
+// a single body as ibm_findEpsilon builds it, or every body of a level as
+// one system under L_UNIVERSAL_EPSILON_CALC (ibm_universalEpsilonGather /
+// Scatter, :1067-1142), which couples bodies whose supports overlap.
+void find_epsilon_set(const GridView &g, const std::vector<IbmBody *> &set) {
+    const int D = g.dims;
+    const double dh = g.dh;
+    std::vector<std::pair<IbmBody *, int>> mk;  // global marker -> (body, marker)
+    for (IbmBody *b : set)
+        for (int m = 0; m < b->nm; ++m) mk.emplace_back(b, m);
+    const int n = (int)mk.size();
+    if (n == 0) return;
     std::vector<double> A((size_t)n * n, 0.0);  // row-major A[I][J]
 #pragma omp parallel for schedule(dynamic, 16) if (n > 256)
-    for (int I = 0; I < n; ++I)
+    for (int I = 0; I < n; ++I) {
+        const IbmBody &bi = *mk[I].first;
+        const int mi = mk[I].second;
         for (int J = 0; J < n; ++J) {
+            const IbmBody &bj = *mk[J].first;
+            const int mj = mk[J].second;
             double aij = 0.0;
-            for (int s = b.off[I]; s < b.off[I + 1]; ++s) {
-                const double dI = b.delta[s];
-                double dJ = delta_kernel((b.pos[3 * J + 0] - b.sx[s]) / dh, b.dil[J]) *
-                            delta_kernel((b.pos[3 * J + 1] - b.sy[s]) / dh, b.dil[J]);
-                if (D == 3) dJ = dJ * delta_kernel((b.pos[3 * J + 2] - b.sz[s]) / dh, b.dil[J]);
-                aij += dI * dJ * b.area[I];
+            for (int s = bi.off[mi]; s < bi.off[mi + 1]; ++s) {
+                const double dI = bi.delta[s];
+                double dJ = delta_kernel((bj.pos[3 * mj + 0] - bi.sx[s]) / dh, bj.dil[mj]) *
+                            delta_kernel((bj.pos[3 * mj + 1] - bi.sy[s]) / dh, bj.dil[mj]);
+                if (D == 3) dJ = dJ * delta_kernel((bj.pos[3 * mj + 2] - bi.sz[s]) / dh, bj.dil[mj]);
+                aij += dI * dJ * bi.area[mi];
             }
-            A[(size_t)I * n + J] = aij * b.ds[J];
+            A[(size_t)I * n + J] = aij * bj.ds[mj];
         }
+    }
     std::vector<double> x(n, 1.0);
     lu_solve_transposed(n, A, x);
-    for (int m = 0; m < n; ++m) b.eps[m] = x[m];
+    for (int I = 0; I < n; ++I) mk[I].first->eps[mk[I].second] = x[I];
+}
+
+// Supports, spacing and epsilon of rigid bodies on one grid, in the order
+// ObjectManager::ibm_initialise runs them (:190-246).
+int setup_bodies(const GridView &v, std::vector<IbmBody> &bodies, bool universal) {
+    for (IbmBody &b : bodies) {
+        int rc = find_support(v, b);
+        if (rc) return rc;
+    }
+    for (IbmBody &b : bodies) compute_ds(v, b);
+    if (universal) {
+        std::vector<IbmBody *> all;
+        for (IbmBody &b : bodies) all.push_back(&b);
+        find_epsilon_set(v, all);
+    } else {
+        for (IbmBody &b : bodies) find_epsilon_set(v, {&b});
+    }
+    return LUMA_OK;
 }
 
 template <class T>
@@ -258,16 +305,26 @@ IbmArgs make_ibm_args(const luma_gpu_grid *g) {
     return b;
 }
 
+int grids_on_level(const luma_gpu_grid *g, int level) {
+    if (g->d.level == level) return 1;
+    int n = 0;
+    for (const luma_gpu_grid *c : g->kids) n += grids_on_level(c, level);
+    return n;
+}
+
 int init_tree(luma_gpu_grid *g) {
     if (g->ibm && g->ibm->has_bodies) {
         IbmState &st = *g->ibm;
-        for (IbmBody &b : st.bodies) {
-            int rc = find_support(g, b);
-            if (rc) return rc;
-        }
-        for (IbmBody &b : st.bodies) compute_ds(g, b);
-        for (IbmBody &b : st.bodies) find_epsilon(g, b);
-        int rc = upload_bodies(g);
+        const bool universal = (g->d.flags & LUMA_FLAG_UNIVERSAL_EPSILON) != 0;
+        if (universal && st.has_flexible)
+            return luma_set_error(LUMA_E_INVALID, "universal epsilon with flexible bodies: the reference re-solves "
+                                                  "the coupled system every sub-iteration (not reproduced)");
+        if (universal && grids_on_level(root_of(g), g->d.level) > 1)
+            return luma_set_error(LUMA_E_INVALID, "universal epsilon couples the bodies of a level: one region "
+                                                  "per level only");
+        int rc = setup_bodies(view_of(g), st.bodies, universal);
+        if (rc) return rc;
+        rc = upload_bodies(g);
         if (rc) return rc;
         if (st.has_flexible) {
             if ((rc = luma_fem_upload(g))) return rc;
@@ -345,6 +402,42 @@ void luma_ibm_free(luma_gpu_grid *g) {
 }
 
 extern "C" {
+
+int luma_ibm_setup_host(const luma_grid_desc *desc, int nbodies, const int *nmarkers, const double *positions,
+                        int universal, double *eps, double *ds, int *nsupports) {
+    if (!desc || nbodies <= 0 || !nmarkers || !positions || !eps || !ds)
+        return luma_set_error(LUMA_E_INVALID, "luma_ibm_setup_host: null argument or no bodies");
+    const luma_grid_desc &d = *desc;
+    if (!((d.dims == 2 && d.K == 1) || d.dims == 3) || d.N <= 0 || d.M <= 0 || d.K <= 0 || !(d.dh > 0.0))
+        return luma_set_error(LUMA_E_INVALID, "luma_ibm_setup_host: bad grid size or spacing");
+    if (!d.xpos || !d.ypos || !d.zpos)
+        return luma_set_error(LUMA_E_INVALID, "luma_ibm_setup_host: the grid's site positions are required");
+    const GridView v{d.dims, d.N, d.M, d.K, d.level, d.dh, d.xpos, d.ypos, d.zpos, d.global_edges};
+    std::vector<IbmBody> bodies(nbodies);
+    size_t off = 0;
+    for (int ib = 0; ib < nbodies; ++ib) {
+        if (nmarkers[ib] <= 0) return luma_set_error(LUMA_E_INVALID, "luma_ibm_setup_host: body %d has no markers", ib);
+        IbmBody &b = bodies[ib];
+        b.nm = nmarkers[ib];
+        b.pos.assign(positions + 3 * off, positions + 3 * (off + b.nm));
+        b.eps.assign(b.nm, 0.0);
+        b.ds.assign(b.nm, 1.0);
+        b.dil.assign(b.nm, 1.0);
+        b.area.assign(b.nm, 1.0);
+        off += b.nm;
+    }
+    if (int rc = setup_bodies(v, bodies, universal != 0)) return rc;
+    off = 0;
+    for (const IbmBody &b : bodies) {
+        for (int m = 0; m < b.nm; ++m) {
+            eps[off + m] = b.eps[m];
+            ds[off + m] = b.ds[m];
+            if (nsupports) nsupports[off + m] = b.off[m + 1] - b.off[m];
+        }
+        off += b.nm;
+    }
+    return LUMA_OK;
+}
 
 int luma_gpu_ibm_add_body(luma_gpu_grid *g, int nmarkers, const double *positions, const double *velocities,
                           int *body_index) {

@@ -1145,23 +1145,37 @@ int oracle_lu_solve_rowmajor(int n, double *A, double *x) {
     return 0;
 }
 
-/* ibm_findEpsilon (:773-920) + GridUtils::solveLinearSystem (src/GridUtils.cpp:356-395). */
-static void find_epsilon(ibm_body *b) {
-    const int n = b->nm, D = b->owner->D;
-    const double dh = b->owner->d.dh;
+/* ibm_findEpsilon (:773-920) + GridUtils::solveLinearSystem
+ * (src/GridUtils.cpp:356-395) over the markers of `set` concatenated in
+ * order: one body, or under L_UNIVERSAL_EPSILON_CALC every body of a level
+ * (ibm_universalEpsilonGather/Scatter, :1067-1142). */
+static void find_epsilon_set(ibm_body *const *set, int nset) {
+    int n = 0;
+    for (int b = 0; b < nset; ++b) n += set[b]->nm;
+    if (n == 0) return;
+    const int D = set[0]->owner->D;
+    const double dh = set[0]->owner->d.dh;
+    int *mb = (int *)malloc(sizeof(int) * n), *mm = (int *)malloc(sizeof(int) * n);
+    for (int b = 0, I = 0; b < nset; ++b)
+        for (int m = 0; m < set[b]->nm; ++m, ++I) { mb[I] = b; mm[I] = m; }
     double *A = (double *)calloc((size_t)n * n, sizeof(double));  /* row-major A[I][J] */
-    for (int I = 0; I < n; ++I)
+    for (int I = 0; I < n; ++I) {
+        const ibm_body *bi = set[mb[I]];
+        const int i = mm[I];
         for (int J = 0; J < n; ++J) {
+            const ibm_body *bj = set[mb[J]];
+            const int j = mm[J];
             double aij = 0.0;
-            for (int s = b->off[I]; s < b->off[I + 1]; ++s) {
-                const double dI = b->delta[s];
-                double dJ = delta_kernel((b->pos[3 * J + 0] - b->sx[s]) / dh, b->dil[J]) *
-                            delta_kernel((b->pos[3 * J + 1] - b->sy[s]) / dh, b->dil[J]);
-                if (D == 3) dJ = dJ * delta_kernel((b->pos[3 * J + 2] - b->sz[s]) / dh, b->dil[J]);
-                aij += dI * dJ * b->area[I];
+            for (int s = bi->off[i]; s < bi->off[i + 1]; ++s) {
+                const double dI = bi->delta[s];
+                double dJ = delta_kernel((bj->pos[3 * j + 0] - bi->sx[s]) / dh, bj->dil[j]) *
+                            delta_kernel((bj->pos[3 * j + 1] - bi->sy[s]) / dh, bj->dil[j]);
+                if (D == 3) dJ = dJ * delta_kernel((bj->pos[3 * j + 2] - bi->sz[s]) / dh, bj->dil[j]);
+                aij += dI * dJ * bi->area[i];
             }
-            A[(size_t)I * n + J] = aij * b->ds[J];
+            A[(size_t)I * n + J] = aij * bj->ds[j];
         }
+    }
     /* The row-major copy read column-major is A^T; the transposed solve
      * then solves A x = 1. */
     int *ipiv = (int *)malloc(sizeof(int) * n);
@@ -1169,9 +1183,16 @@ static void find_epsilon(ibm_body *b) {
     for (int i = 0; i < n; ++i) x[i] = 1.0;
     lu_factor(n, A, n, ipiv);
     lu_solve_t(n, A, n, ipiv, x);
-    for (int m = 0; m < n; ++m) b->eps[m] = x[m];
-    free(A); free(ipiv); free(x);
+    for (int I = 0; I < n; ++I) set[mb[I]]->eps[mm[I]] = x[I];
+    free(A); free(ipiv); free(x); free(mb); free(mm);
 }
+
+static void find_epsilon(ibm_body *b) { find_epsilon_set(&b, 1); }
+
+static int g_universal_eps = 0;
+
+/* L_UNIVERSAL_EPSILON_CALC on (1) or off (0) for the next initialisation. */
+void oracle_ibm_set_universal(int on) { g_universal_eps = on != 0; }
 
 static void fem_move_bodies(oracle_grid *g, ibm_ctx *c);
 static void fem_free_all(void);
@@ -1287,7 +1308,24 @@ int oracle_ibm_initialise(void) {
     for (int ib = 0; ib < g_ibm->nb; ++ib)
         if (find_support(g_ibm, &g_ibm->b[ib])) return -1;
     for (int ib = 0; ib < g_ibm->nb; ++ib) compute_ds(&g_ibm->b[ib]);
-    for (int ib = 0; ib < g_ibm->nb; ++ib) find_epsilon(&g_ibm->b[ib]);
+    if (!g_universal_eps) {
+        for (int ib = 0; ib < g_ibm->nb; ++ib) find_epsilon(&g_ibm->b[ib]);
+        return 0;
+    }
+    for (int ib = 0; ib < g_ibm->nb; ++ib)
+        if (grid_has_flexible(g_ibm->b[ib].owner)) {
+            set_err("universal epsilon with flexible bodies is not reproduced");
+            return -1;
+        }
+    /* one system per level over its bodies in body order */
+    ibm_body **set = (ibm_body **)malloc(sizeof(ibm_body *) * (g_ibm->nb > 0 ? g_ibm->nb : 1));
+    for (int lev = 0; lev < 16; ++lev) {
+        int ns = 0;
+        for (int ib = 0; ib < g_ibm->nb; ++ib)
+            if (g_ibm->b[ib].owner->d.level == lev) set[ns++] = &g_ibm->b[ib];
+        if (ns) find_epsilon_set(set, ns);
+    }
+    free(set);
     return 0;
 }
 

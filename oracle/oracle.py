@@ -60,6 +60,7 @@ def lib():
         L.oracle_last_error.restype = C.c_char_p
         L.oracle_ibm_add_body.argtypes = [C.c_void_p, C.c_int, C.POINTER(C.c_double)]
         L.oracle_ibm_initialise.argtypes = []
+        L.oracle_ibm_set_universal.argtypes = [C.c_int]
         L.oracle_ibm_markers.argtypes = [C.c_int, C.POINTER(C.c_double)]
         L.oracle_ibm_supports.argtypes = [C.c_int, C.POINTER(C.c_double), C.c_int]
         L.oracle_ibm_reset.argtypes = []
@@ -227,7 +228,9 @@ class OracleIBM:
         self.nm.append(pos.shape[0])
         return ib
 
-    def initialise(self):
+    def initialise(self, universal: bool = False):
+        """ibm_initialise; `universal` = L_UNIVERSAL_EPSILON_CALC."""
+        self.L.oracle_ibm_set_universal(1 if universal else 0)
         if self.L.oracle_ibm_initialise() != 0:
             raise RuntimeError(self.L.oracle_last_error().decode())
 

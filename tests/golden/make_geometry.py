@@ -8,6 +8,8 @@ ds after ibm_initialise:
   a rotated square and a rigid filament;
 * ``oracle/cases/geom_d3q19.h`` (3D): a sphere, a rotated cube, a plate and
   two rigid filaments;
+* ``oracle/cases/ibm_universal_d2q9.h`` (2D, L_UNIVERSAL_EPSILON_CALC): two
+  circles whose supports overlap and a square;
 * ``oracle/cases/geom_refine_d2q9.h`` (2D, one refined region) for the
   point clouds placed on level 1.
 
@@ -53,6 +55,10 @@ RUNS = {
                    "PLATE IBM 0 0 1.4 0.5 0.5 0.3 0.2 10.0 20.0 30.0 RIGID\n"
                    "FILAMENT_ARRAY IBM 0 0 2 1.75 0.0 0.3 0.0 0.0 0.3 0.4 0.05 0.05 70.0 25.0 MOVABLE "
                    "CONFORMING CLAMPED 1000.0 100000000.0\n"),
+    "ibm_universal_d2q9": ("# two circles whose supports overlap and a square, one epsilon system\n"
+                           "CIRCLE_SPHERE IBM 0 0 0.9 0.5 0.0 0.1 RIGID\n"
+                           "CIRCLE_SPHERE IBM 0 0 1.135 0.5 0.0 0.1 RIGID\n"
+                           "SQUARE_CUBE IBM 0 0 1.6 0.45 0.0 0.15 0.1 0.0 20.0 0.0 RIGID\n"),
 }
 
 

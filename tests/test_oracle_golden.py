@@ -490,3 +490,57 @@ def test_inlet_profile_file_matches_reference():
         assert np.array_equal(f, z[f"{case}/{key}/f"]), key
     with pytest.raises(ValueError):
         hostcase.inlet_profile_from_file("0 0.5 0 0.1 0 0", g0.ypos)
+
+
+def test_universal_epsilon_matches_reference():
+    """L_UNIVERSAL_EPSILON_CALC: one epsilon system over two circles whose
+    supports overlap and a square.  The oracle and the library's host set-up
+    (luma_ibm_setup_host, what luma_gpu_ibm_initialise runs for rigid bodies)
+    give the reference's epsilon and ds bit for bit; per-body systems do not
+    (tests/golden/make_geometry.py, oracle/cases/ibm_universal_d2q9.h)."""
+    import ctypes as C
+    import json
+    from luma_gb300 import geometry
+    ref = json.load(open(os.path.join(R.HERE, "geometry_prefab.json")))["runs"][2]
+    assert ref["case"] == "ibm_universal_d2q9"
+    defs = hostcase.Definitions(dims=2, resolution=40, timestep=1.0 / 1000.0, bx=2.0, by=1.0, re=100, ux0=1.0,
+                                ibm=True, universal_epsilon=True,
+                                walls=(A.VELOCITY, A.EXTRAPOLATE_RIGHT, A.SOLID, A.SOLID, A.FLUID, A.FLUID))
+    l0 = hostcase.build_level0(defs)
+    assert l0.desc().flags & A.FLAG_UNIVERSAL_EPSILON
+    bodies = geometry.read_geometry(ref["config"], {(0, 0): l0})
+    want = np.array(ref["markers"])
+    for universal in (True, False):
+        g = O.OracleGrid(l0.desc())
+        g.upload(*R.initial_state(l0), t=0)
+        ibm = O.OracleIBM()
+        for b in bodies:
+            ibm.add_body(g, b["positions"])
+        ibm.initialise(universal=universal)
+        got = np.array([[ib, m, *mk[m, 0:3], mk[m, 6], mk[m, 7]]
+                        for ib in range(len(bodies)) for mk in [ibm.markers(ib)] for m in range(mk.shape[0])])
+        assert np.array_equal(got, want) == universal
+    lib_path = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "luma_gb300", "_build",
+                            "libluma_gpu.so")
+    if not os.path.exists(lib_path):
+        from luma_gb300 import build
+        build.build()
+    try:
+        lib = C.CDLL(lib_path)
+    except OSError as e:
+        pytest.skip(f"cannot load CUDA library here: {e}")
+    dp = C.POINTER(C.c_double)
+    lib.luma_ibm_setup_host.argtypes = [C.POINTER(A.GridDesc), C.c_int, C.POINTER(C.c_int), dp, C.c_int, dp, dp,
+                                        C.POINTER(C.c_int)]
+    d = l0.desc()
+    nm = np.array([len(b["positions"]) for b in bodies], dtype=np.int32)
+    pos = np.ascontiguousarray(np.concatenate([np.asarray(b["positions"], float).reshape(-1, 3) for b in bodies]))
+    for universal in (1, 0):
+        eps, ds = np.zeros(nm.sum()), np.zeros(nm.sum())
+        ns = np.zeros(nm.sum(), dtype=np.int32)
+        assert lib.luma_ibm_setup_host(C.byref(d), len(nm), nm.ctypes.data_as(C.POINTER(C.c_int)),
+                                       pos.ctypes.data_as(dp), universal, eps.ctypes.data_as(dp),
+                                       ds.ctypes.data_as(dp), ns.ctypes.data_as(C.POINTER(C.c_int))) == 0
+        assert np.array_equal(ds, want[:, 6])
+        assert np.array_equal(eps, want[:, 5]) == bool(universal)
+        assert ns.min() >= 4
