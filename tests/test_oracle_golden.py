@@ -510,6 +510,7 @@ def test_universal_epsilon_matches_reference():
     assert l0.desc().flags & A.FLAG_UNIVERSAL_EPSILON
     bodies = geometry.read_geometry(ref["config"], {(0, 0): l0})
     want = np.array(ref["markers"])
+    oracle_eps = {}
     for universal in (True, False):
         g = O.OracleGrid(l0.desc())
         g.upload(*R.initial_state(l0), t=0)
@@ -520,6 +521,7 @@ def test_universal_epsilon_matches_reference():
         got = np.array([[ib, m, *mk[m, 0:3], mk[m, 6], mk[m, 7]]
                         for ib in range(len(bodies)) for mk in [ibm.markers(ib)] for m in range(mk.shape[0])])
         assert np.array_equal(got, want) == universal
+        oracle_eps[universal] = got[:, 5]
     lib_path = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "luma_gb300", "_build",
                             "libluma_gpu.so")
     if not os.path.exists(lib_path):
@@ -543,4 +545,5 @@ def test_universal_epsilon_matches_reference():
                                        ds.ctypes.data_as(dp), ns.ctypes.data_as(C.POINTER(C.c_int))) == 0
         assert np.array_equal(ds, want[:, 6])
         assert np.array_equal(eps, want[:, 5]) == bool(universal)
+        assert np.array_equal(eps, oracle_eps[bool(universal)])
         assert ns.min() >= 4
