@@ -546,4 +546,25 @@ def test_universal_epsilon_matches_reference():
         assert np.array_equal(ds, want[:, 6])
         assert np.array_equal(eps, want[:, 5]) == bool(universal)
         assert np.array_equal(eps, oracle_eps[bool(universal)])
+
+
+def test_universal_epsilon_refused_with_flexible_bodies():
+    """With a flexible filament on the grid the reference re-solves the
+    coupled system every FSI sub-iteration; the oracle refuses the universal
+    mode there instead of solving something else."""
+    import json
+    from luma_gb300 import geometry
+    ref = json.load(open(os.path.join(R.HERE, "geometry_prefab.json")))["runs"][0]
+    l0 = R.level0(ref["case"])
+    bodies = geometry.read_geometry(ref["config"], {(0, 0): l0})
+    g = O.OracleGrid(l0.desc())
+    g.upload(*R.initial_state(l0), t=0)
+    ibm = O.OracleIBM()
+    for b in bodies:
+        if b["kind"] == "ibm":
+            ibm.add_body(g, b["positions"])
+        else:
+            ibm.add_filament(g, **b["args"])
+    with pytest.raises(RuntimeError, match="flexible"):
+        ibm.initialise(universal=True)
         assert ns.min() >= 4
