@@ -451,6 +451,15 @@ def _inlet_profile(defs: Definitions, ypos: np.ndarray, dt: float, dh: float, ed
             np.full(M, (defs.uz0 * dt) / dh))
 
 
+def cround(v: float) -> float:
+    """std::round: halves away from zero (Python's round takes them to the
+    even neighbour)."""
+    r = math.floor(abs(v))
+    if abs(v) - r >= 0.5:
+        r += 1
+    return math.copysign(r, v)
+
+
 def build_subgrid(parent: "Level0", start: tuple, end: tuple, region: int = 0,
                   coarse_dh_for_edges: float | None = None) -> "Level0":
     """One embedded refined grid (factor 2) inside `parent`, mirroring the
@@ -473,8 +482,8 @@ def build_subgrid(parent: "Level0", start: tuple, end: tuple, region: int = 0,
         if a_ == 2 and D == 2:
             edges += [0.0, 0.0]
             continue
-        lo = round(start[a_] / rdh) * rdh
-        hi = round(end[a_] / rdh) * rdh
+        lo = cround(start[a_] / rdh) * rdh
+        hi = cround(end[a_] / rdh) * rdh
         edges += [lo, hi]
     pstart = [parent.edges[0], parent.edges[2], parent.edges[4]]
     ppos = [parent.xpos, parent.ypos, parent.zpos]

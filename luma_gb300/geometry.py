@@ -40,6 +40,7 @@ import math
 
 from . import _abi as A
 from . import bfl as _bfl
+from . import case as _case
 
 
 def _shift(lv) -> tuple:
@@ -135,12 +136,7 @@ def plate_points(lv, centre, length: float, width: float, angles) -> list:
 L_SMALL_NUMBER = 1e-8
 
 
-def _cround(v: float) -> float:
-    """std::round: halves away from zero."""
-    r = math.floor(abs(v))
-    if abs(v) - r >= 0.5:
-        r += 1
-    return math.copysign(r, v)
+_cround = _case.cround  # std::round
 
 
 def read_cloud(text: str, dims: int) -> list:

@@ -16,6 +16,10 @@ value repeats the last one read).
 region) reads ``input/inlet_profile.in`` (five points, a final newline);
 stored: the text and every grid's inlet profile, velocity and populations.
 
+``oracle/cases/refine_halfcell_d2q9.h`` (16 x 8 channel whose refined
+region's limits fall on half coarse cells): every grid's labels and site
+positions, which pin the std::round of the sub-grid edges.
+
 Output: ``initial_velocity.npz`` beside this script.
 
 Usage (needs the reference checkout; not run on the GPU machine):
@@ -97,6 +101,17 @@ def main() -> int:
     for key in ("L0R0", "L1R0"):
         s0 = os.path.join(work, "out", "s0", key + "_")
         for name in ("uxin", "u", "f"):
+            store[f"{case}/{key}/{name}"] = np.fromfile(s0 + name + ".bin", dtype=np.float64)
+    print(case)
+    case = "refine_halfcell_d2q9"
+    exe = build_ref.build_case(case, a.ref)
+    work = tempfile.mkdtemp(prefix="halfcell_")
+    subprocess.run([exe, "--out", os.path.join(work, "out"), "--steps", "0", "--dump-every", "0"], check=True,
+                   timeout=300)
+    for key in ("L0R0", "L1R0"):
+        s0 = os.path.join(work, "out", "s0", key + "_")
+        store[f"{case}/{key}/typ"] = np.fromfile(s0 + "typ.bin", dtype=np.int32)
+        for name in ("xpos", "ypos"):
             store[f"{case}/{key}/{name}"] = np.fromfile(s0 + name + ".bin", dtype=np.float64)
     print(case)
     dst = os.path.join(HERE, "initial_velocity.npz")

@@ -568,3 +568,22 @@ def test_universal_epsilon_refused_with_flexible_bodies():
     with pytest.raises(RuntimeError, match="flexible"):
         ibm.initialise(universal=True)
         assert ns.min() >= 4
+
+
+def test_subgrid_edges_round_half_away_from_zero():
+    """Refined-region limits on half coarse cells: the edges follow
+    std::round (halves away from zero), so the refined grid's size, site
+    positions and both grids' labels equal the reference's
+    (oracle/cases/refine_halfcell_d2q9.h, tests/golden/make_initvel.py);
+    round-half-to-even would give a 12 x 8 grid shifted by a coarse cell."""
+    z = np.load(os.path.join(R.HERE, "initial_velocity.npz"))
+    d = hostcase.Definitions(dims=2, resolution=4, timestep=1.0 / 80.0, bx=4.0, by=2.0, re=50, ux0=1.0,
+                             walls=(A.VELOCITY, A.EXTRAPOLATE_RIGHT, A.SOLID, A.SOLID, A.FLUID, A.FLUID))
+    g0 = hostcase.build_level0(d)
+    g1 = hostcase.build_subgrid(g0, (0.625, 0.375, 0.0), (2.125, 1.625, 0.0))
+    case = "refine_halfcell_d2q9"
+    for g, key in ((g0, "L0R0"), (g1, "L1R0")):
+        assert np.array_equal(g.typ, z[f"{case}/{key}/typ"]), key
+        assert np.array_equal(g.xpos, z[f"{case}/{key}/xpos"]), key
+        assert np.array_equal(g.ypos, z[f"{case}/{key}/ypos"]), key
+    assert (g1.N, g1.M) == (12, 10)
