@@ -143,3 +143,11 @@ def test_desc_struct_size_matches_header():
         out = subprocess.run([exe], capture_output=True, text=True, check=True).stdout.split()
     assert int(out[0]) == C.sizeof(A.GridDesc)
     assert int(out[1]) == C.sizeof(A.Reduction)
+
+
+def test_integration_guide_maps_every_entry_point():
+    """Every function the header declares has a row in the integration
+    guide's table of the reference interfaces they replace."""
+    guide = open(os.path.join(ROOT, "INTEGRATION.md")).read()
+    missing = [n for n in declared_functions() if f"`{n}`" not in guide]
+    assert not missing, missing
