@@ -22,6 +22,12 @@ LIB = os.path.join(BUILD, "libluma_gpu.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 # Units whose FP64 operation sequence must be the reference's (no FMA contraction).
 FMAD_OFF = {"fem.cu"}
+# Units compiled once per variant (object suffix, defines): the general-path
+# kernels instantiate per lattice and precision, six objects in parallel.
+VARIANTS = {
+    "k_general.cu": [(f"q{q}_{p}", [f"-DLUMA_GEN_Q={q}", f"-DLUMA_GEN_FP64={1 if p == 'fp64' else 0}"])
+                     for q in (9, 19, 27) for p in ("fp64", "fp32")],
+}
 
 
 def nvcc() -> str:
@@ -48,12 +54,19 @@ def build(force: bool = False, debug: bool = False, jobs: int | None = None, ver
     cc = nvcc()
     flags = _flags(debug)
 
-    def compile_one(src: str):
-        obj = os.path.join(BUILD, os.path.basename(src)[:-3] + ".o")
+    jobs_list = []
+    for src in units:
+        base = os.path.basename(src)
+        for suffix, defs in VARIANTS.get(base, [("", [])]):
+            obj = os.path.join(BUILD, base[:-3] + (f"_{suffix}" if suffix else "") + ".o")
+            jobs_list.append((src, obj, defs))
+
+    def compile_one(job):
+        src, obj, defs = job
         if not force and os.path.exists(obj) and os.path.getmtime(obj) >= max(os.path.getmtime(src), newest_hdr):
             return obj, None
         extra = ["-fmad=false"] if os.path.basename(src) in FMAD_OFF else []
-        cmd = [cc, *flags, *extra, "-c", src, "-o", obj]
+        cmd = [cc, *flags, *extra, *defs, "-c", src, "-o", obj]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             return obj, " ".join(cmd) + "\n" + r.stdout[-3000:] + r.stderr[-6000:]
@@ -61,8 +74,8 @@ def build(force: bool = False, debug: bool = False, jobs: int | None = None, ver
             print(r.stderr, file=sys.stderr)
         return obj, None
 
-    with cf.ThreadPoolExecutor(max_workers=jobs or min(len(units), os.cpu_count() or 4)) as ex:
-        res = list(ex.map(compile_one, units))
+    with cf.ThreadPoolExecutor(max_workers=jobs or min(len(jobs_list), os.cpu_count() or 4)) as ex:
+        res = list(ex.map(compile_one, jobs_list))
     errs = [e for _, e in res if e]
     if errs:
         raise RuntimeError("luma_gb300 CUDA build failed:\n" + "\n".join(errs))

@@ -303,6 +303,7 @@ StepArgs make_args(luma_gpu_grid *g, int subcycle) {
     a.forcing = (d.flags & (LUMA_FLAG_IBM | LUMA_FLAG_GRAVITY)) != 0;
     a.ibm_split = (d.flags & LUMA_FLAG_IBM) != 0;
     a.level = d.level;
+    a.unsupported = g->unsup;
     if (g->parent) {
         a.parent_f = g->parent->f[g->parent->cur];
         a.pN = g->parent->d.N; a.pM = g->parent->d.M; a.pK = g->parent->d.K;
@@ -559,6 +560,7 @@ void free_grid(luma_gpu_grid *g) {
     cudaFree(g->reg);
     cudaFree(g->velu);
     cudaFree(g->acc);
+    cudaFree(g->unsup);
     cudaFree(g->tav);
     cudaFree(g->defer);
     cudaFree(g->defer_ids);
@@ -684,6 +686,8 @@ int luma_gpu_grid_create(const luma_grid_desc *desc, luma_gpu_grid *parent, luma
     CKF(cudaMemcpy(g->uyin, d.uy_in, d.M * sizeof(double), cudaMemcpyHostToDevice));
     CKF(cudaMemcpy(g->uzin, d.uz_in, d.M * sizeof(double), cudaMemcpyHostToDevice));
     CKF(cudaMalloc(&g->acc, 8 * sizeof(double)));
+    CKF(cudaMalloc(&g->unsup, sizeof(int)));
+    CKF(cudaMemset(g->unsup, 0, sizeof(int)));
     if (d.flags & LUMA_FLAG_TIME_AVERAGES) {
         const size_t nt = g->n * (size_t)(1 + d.dims + 3 * d.dims - 3);
         CKF(cudaMalloc(&g->tav, nt * sizeof(double)));
@@ -879,11 +883,29 @@ int luma_gpu_step(luma_gpu_grid *root, int nsteps) {
     return LUMA_OK;
 }
 
+// Reads and clears the unsupported-site flag of every grid of a tree; the
+// first grid (parent before its sub-grids) with a code set is reported.
+static int take_unsupported(luma_gpu_grid *g, int *code, int *level, int *region) {
+    int h = 0;
+    CK(cudaMemcpyAsync(&h, g->unsup, sizeof(int), cudaMemcpyDeviceToHost, g->stream));
+    CK(cudaStreamSynchronize(g->stream));
+    if (h) {
+        CK(cudaMemsetAsync(g->unsup, 0, sizeof(int), g->stream));
+        if (!*code) { *code = h; *level = g->d.level; *region = g->d.region; }
+    }
+    for (luma_gpu_grid *c : g->kids)
+        if (int rc = take_unsupported(c, code, level, region)) return rc;
+    return LUMA_OK;
+}
+
 int luma_gpu_synchronize(luma_gpu_grid *root) {
     if (!root) return luma_set_error(LUMA_E_INVALID, "null grid");
     CK(cudaStreamSynchronize(root->stream));
-    if (int u = read_unsupported_flag(root->stream))
-        return luma_set_error(LUMA_E_INVALID, "a site needed an operation outside the GPU path (code %d)", u);
+    int code = 0, level = 0, region = 0;
+    if (int rc = take_unsupported(root, &code, &level, &region)) return rc;
+    if (code)
+        return luma_set_error(LUMA_E_INVALID, "grid L%d R%d: a site needed an operation outside the GPU path (code %d)",
+                              level, region, code);
     return LUMA_OK;
 }
 

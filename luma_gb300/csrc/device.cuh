@@ -95,6 +95,9 @@ struct StepArgs {
     int level;
     int nchild;
     ChildView child[kMaxChildren];
+    // this grid's device flag: a site that needs an operation outside the
+    // GPU path writes a non-zero code (read and cleared by luma_gpu_synchronize)
+    int *unsupported;
 };
 
 // Per regularised site: inward normal, normal direction and edge count from

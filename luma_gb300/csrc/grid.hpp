@@ -35,6 +35,7 @@ struct luma_gpu_grid {
     int2 *velu = nullptr;       // (velocity site, row of last writer) under a ramp
     int nvelu = 0;
     double *acc = nullptr;      // reduction accumulators
+    int *unsup = nullptr;       // device flag: non-zero when a site needed an operation outside the GPU path
     double *tav = nullptr;      // running means (rho, u_p, u_p u_q; SoA, FP64) or null
     int t = 0;
     bool bulk = false;          // in-place AA path

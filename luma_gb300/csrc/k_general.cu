@@ -28,8 +28,6 @@ namespace luma {
 
 namespace {
 
-__device__ int g_unsupported;  // set when a site needs a feature outside the GPU path
-
 template <int Q>
 __device__ __forceinline__ int child_at(const StepArgs &a, int i, int j, int k) {
     constexpr int D = Lattice<Q>::D;
@@ -72,7 +70,7 @@ __device__ __forceinline__ void stream_site(const StepArgs &a, const int8_t *wal
             // _LBM_applyBFL_opt (:1010-1113) through the link tables
             // (kinds in bfl.cu); links without a wall stream as usual
             if (!a.bfl_rec) {
-                g_unsupported = 1;
+                *a.unsupported = 1;
                 fn[v] = R(0);
                 continue;
             }
@@ -146,7 +144,7 @@ __device__ __forceinline__ void stream_site(const StepArgs &a, const int8_t *wal
             // _LBM_coalesce_opt (:591-636) with GridUtils::getFineIndices.
             const int s = child_at<Q>(a, i, j, k);
             if (s < 0) {
-                g_unsupported = 2;
+                *a.unsupported = 2;
                 fn[v] = R(0);
                 continue;
             }
@@ -945,36 +943,32 @@ cudaError_t launch_general_phaseC(const StepArgs &a, const int *ids, int nids, c
     return cudaGetLastError();
 }
 
-int read_unsupported_flag(cudaStream_t s) {
-    int h = 0;
-    cudaMemcpyFromSymbolAsync(&h, g_unsupported, sizeof(int), 0, cudaMemcpyDeviceToHost, s);
-    cudaStreamSynchronize(s);
-    return h;
-}
-
 #define LUMA_INST(Q, P)                                                                                        \
     template cudaError_t launch_general_phaseA<Q, P>(const StepArgs &, const int8_t *, const uint8_t *, const int *, \
                                                      int, cudaStream_t);                                       \
     template cudaError_t launch_general_phaseB<Q, P>(const StepArgs &, const int8_t *, const RegSite *, int,   \
                                                      cudaStream_t);                                            \
     template cudaError_t launch_general_phaseC<Q, P>(const StepArgs &, const int *, int, cudaStream_t);
-LUMA_INST(9, P64)
-LUMA_INST(19, P64)
-LUMA_INST(27, P64)
-LUMA_INST(9, P32)
-LUMA_INST(19, P32)
-LUMA_INST(27, P32)
 #define LUMA_INST_IBM(Q, P) \
     template cudaError_t launch_ibm_pass<Q, P>(const StepArgs &, const IbmArgs &, const FlexArgs &, cudaStream_t);
-LUMA_INST_IBM(9, P64)
-LUMA_INST_IBM(19, P64)
-LUMA_INST_IBM(27, P64)
-LUMA_INST_IBM(9, P32)
-LUMA_INST_IBM(19, P32)
-LUMA_INST_IBM(27, P32)
-template cudaError_t launch_reset_forces<P64>(const StepArgs &, int, double, int, double, cudaStream_t);
-template cudaError_t launch_reset_forces<P32>(const StepArgs &, int, double, int, double, cudaStream_t);
-template cudaError_t launch_velocity_u<P64>(const StepArgs &, int, const int2 *, int, cudaStream_t);
-template cudaError_t launch_velocity_u<P32>(const StepArgs &, int, const int2 *, int, cudaStream_t);
+
+// This unit is compiled once per (lattice, precision) pair, with
+// -DLUMA_GEN_Q=<9|19|27> -DLUMA_GEN_FP64=<0|1> (luma_gb300/build.py), so
+// the six sets of instantiations build in parallel; the lattice-free
+// launchers come with the D2Q9 objects.
+#if !defined(LUMA_GEN_Q) || !defined(LUMA_GEN_FP64)
+#error "k_general.cu is compiled per lattice and precision: define LUMA_GEN_Q and LUMA_GEN_FP64"
+#endif
+#if LUMA_GEN_FP64
+#define LUMA_GEN_P P64
+#else
+#define LUMA_GEN_P P32
+#endif
+LUMA_INST(LUMA_GEN_Q, LUMA_GEN_P)
+LUMA_INST_IBM(LUMA_GEN_Q, LUMA_GEN_P)
+#if LUMA_GEN_Q == 9
+template cudaError_t launch_reset_forces<LUMA_GEN_P>(const StepArgs &, int, double, int, double, cudaStream_t);
+template cudaError_t launch_velocity_u<LUMA_GEN_P>(const StepArgs &, int, const int2 *, int, cudaStream_t);
+#endif
 
 }  // namespace luma

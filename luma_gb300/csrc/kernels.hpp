@@ -18,7 +18,6 @@ template <class P>
 cudaError_t launch_velocity_u(const StepArgs &a, int dims, const int2 *sites, int nsites, cudaStream_t s);
 template <int Q, class P>
 cudaError_t launch_general_phaseC(const StepArgs &a, const int *ids, int nids, cudaStream_t s);
-int read_unsupported_flag(cudaStream_t s);
 struct IbmArgs;
 struct FlexArgs;
 template <int Q, class P>

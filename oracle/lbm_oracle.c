@@ -98,6 +98,9 @@ struct oracle_grid {
     int bfl_nm;
     /* running means (LUMA_FLAG_TIME_AVERAGES), reference layout */
     double *rho_ta, *ui_ta, *uiuj_ta;
+    /* KBC grids: the stabiliser gamma of each site's latest collision
+     * (NaN where no collision ran yet); a record for tests, not an input */
+    double *kbc_gamma;
 };
 
 static char g_err[512];
@@ -631,6 +634,7 @@ static void collide_kbc(oracle_grid *g, int id) {
     double gamma;
     if (bot == 0.0) gamma = 2.0;
     else gamma = beta_m1 - (2.0 - beta_m1) * (top / bot);
+    if (g->kbc_gamma) g->kbc_gamma[id] = gamma;
     double *fn = g->fNew + (size_t)id * Q;
     for (int v = 0; v < Q; v++) {
         const double base = src[v + (size_t)id * Q] - (1.0 / beta_m1) * (2.0 * ds[v] + gamma * dh[v]);
@@ -768,6 +772,10 @@ oracle_grid *oracle_grid_create(const luma_grid_desc *d, oracle_grid *parent) {
         g->ui_ta = dup_d(NULL, n * g->D);
         g->uiuj_ta = dup_d(NULL, n * (3 * g->D - 3));
     }
+    if (d->collision == LUMA_COLL_KBC) {
+        g->kbc_gamma = dup_d(NULL, n);
+        for (size_t i = 0; i < n; ++i) g->kbc_gamma[i] = NAN;
+    }
     g->d.lattyp = NULL;
     g->d.xpos = g->d.ypos = g->d.zpos = NULL;
     g->d.ux_in = g->d.uy_in = g->d.uz_in = NULL;
@@ -788,6 +796,7 @@ void oracle_grid_destroy(oracle_grid *g) {
     free(g->u); free(g->u_n); free(g->force_xyz); free(g->rho);
     free(g->bfl_marker); free(g->bfl_q); free(g->bfl_force);
     free(g->rho_ta); free(g->ui_ta); free(g->uiuj_ta);
+    free(g->kbc_gamma);
     free(g);
 }
 
@@ -798,6 +807,15 @@ int oracle_download_time_averages(const oracle_grid *g, double *rho_ta, double *
     memcpy(rho_ta, g->rho_ta, sizeof(double) * n);
     memcpy(ui_ta, g->ui_ta, sizeof(double) * n * g->D);
     memcpy(uiuj_ta, g->uiuj_ta, sizeof(double) * n * (3 * g->D - 3));
+    return 0;
+}
+
+/* KBC grids: the stabiliser gamma = 2/omega - (2 - 2/omega) <ds|dh>/<dh|dh>
+ * (2 where <dh|dh> = 0) of each site's latest collision, NaN where none ran
+ * (_LBM_kbcCollide_opt, src/GridObj_ops_lbm_optimised.cpp:1287-1289). */
+int oracle_kbc_gamma(const oracle_grid *g, double *out) {
+    if (!g->kbc_gamma) { set_err("not a KBC grid"); return -1; }
+    memcpy(out, g->kbc_gamma, sizeof(double) * (size_t)g->ncell);
     return 0;
 }
 

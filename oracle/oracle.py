@@ -74,6 +74,7 @@ def lib():
         L.oracle_bfl_forces.argtypes = [C.c_void_p, C.POINTER(C.c_double)]
         L.oracle_download_fnew.argtypes = [C.c_void_p, C.POINTER(C.c_double)]
         L.oracle_download_time_averages.argtypes = [C.c_void_p] + [C.POINTER(C.c_double)] * 3
+        L.oracle_kbc_gamma.argtypes = [C.c_void_p, C.POINTER(C.c_double)]
         L.oracle_lu_solve_rowmajor.argtypes = [C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_double)]
         L.oracle_lattice.argtypes = [C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_double), C.POINTER(C.c_int),
                                      C.POINTER(C.c_int)]
@@ -160,6 +161,14 @@ class OracleGrid:
         """Momentum-exchange force of the solid sites (computeLiftDrag)."""
         out = np.zeros(3)
         self.L.oracle_momex_force(self.h, A.dptr(out))
+        return out
+
+    def kbc_gamma(self) -> np.ndarray:
+        """The KBC stabiliser gamma of each site's latest collision (NaN
+        where none ran)."""
+        out = np.empty(self.n)
+        if self.L.oracle_kbc_gamma(self.h, A.dptr(out)):
+            raise RuntimeError(self.L.oracle_last_error().decode())
         return out
 
     def time_averages(self) -> dict:

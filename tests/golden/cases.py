@@ -89,6 +89,16 @@ CASES = {
         defs=Definitions(dims=3, resolution=16, timestep=1.0 / 400.0, bx=3.0, by=1.5, bz=1.5, re=40, ux0=1.0,
                          ibm=True, walls=(V, X, S, S, F, F)),
         bodies="sphere", steps=(5, 50), store_f=()),
+    # Scaled copy of the refined-sphere workload: D3Q19 channel 48 x 24 x 24
+    # with two nested refined regions centred on a rigid IBM sphere that
+    # lives on level 1 (diameter 12 level-1 lu, 314 Fibonacci markers); the
+    # level-2 box sits inside the sphere, clear of the supports.  Uniform
+    # start at the inlet velocity (0.04 lu).
+    "ibm_sphere_refine_d3q19": dict(
+        defs=Definitions(dims=3, resolution=8, timestep=0.005, bx=6.0, by=3.0, bz=3.0, re=20, ux0=1.0,
+                         no_flow=False, ibm=True, walls=(V, X, F, F, F, F)),
+        regions=[((0.75, 0.75, 0.75), (2.25, 2.25, 2.25)), ((1.375, 1.375, 1.375), (1.625, 1.625, 1.625))],
+        bodies="sphere_l1", steps=(4, 20), store_f=()),
     # D2Q9 channel with a flexible FEM filament (FSI sub-iterations).
     "fem_filament_d2q9": dict(
         defs=Definitions(dims=2, resolution=40, timestep=1.0 / 1000.0, bx=2.0, by=1.0, re=100, ux0=1.0,
@@ -210,6 +220,8 @@ def bodies(name: str):
     if kind == "sphere":
         n = int(math.floor(4.0 * math.pi * 0.25 ** 2 / dh ** 2))
         return [(0, 0, fibonacci_sphere(1.0, 0.75, 0.75, 0.25, n))]
+    if kind == "sphere_l1":
+        return [(1, 0, fibonacci_sphere(1.5, 1.5, 1.5, 0.375, 314))]
     return []
 
 

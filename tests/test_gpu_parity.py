@@ -137,12 +137,13 @@ def test_ibm_matches_oracle(name, prec, split):
     gg, levels = R.build_backend(name, make_gpu_split if split else make_gpu, prec)
     oo, _ = R.build_backend(name, make_oracle)
     oibm = O.OracleIBM()
+    blev = CASES.bodies(name)[0][0]     # the grid that owns the body (level 1 on the refined sphere)
     for lev, reg, pos in CASES.bodies(name):
         gg[lev].ibm_add_body(pos)
         oibm.add_body(oo[lev], pos)
     gg[0].ibm_initialise()
     oibm.initialise()
-    gm, om = gg[0].ibm_markers(0), oibm.markers(0)
+    gm, om = gg[blev].ibm_markers(0), oibm.markers(0)
     assert np.array_equal(gm[:, 6:9], om[:, 6:9])
     assert np.array_equal(gm[:, 6], fx["markers_0"][:, 8])
     done = 0
@@ -151,19 +152,25 @@ def test_ibm_matches_oracle(name, prec, split):
         gg[0].step(s - done)
         oo[0].step(s - done)
         done = s
-        gs, os_ = gg[0].download(), oo[0].download()
-        gm, om = gg[0].ibm_markers(0), oibm.markers(0)
+        gm, om = gg[blev].ibm_markers(0), oibm.markers(0)
         ef = rel_l2(gm[:, 3:3 + D], om[:, 3:3 + D])
-        eu = rel_l2(gs["u"], os_["u"])
+        for g, o, lv in zip(gg, oo, levels):
+            gs, os_ = g.download(), o.download()
+            eu = rel_l2(gs["u"], os_["u"])
+            key = R.grid_key(lv)
+            if prec == A.PREC_FP64:
+                assert eu <= 1e-10 and rel_l2(gs["f"], os_["f"]) <= 1e-10, (name, key, s, eu)
+                u_ref = R.fields_at(fx, key, s, name)[0]
+                assert rel_l2(gs["u"], u_ref) <= 1e-10, (name, key, s)
+            else:
+                assert eu <= 2e-4, (name, key, s, eu)
         if prec == A.PREC_FP64:
-            assert eu <= 1e-10 and rel_l2(gs["f"], os_["f"]) <= 1e-10, (name, s, eu)
             assert ef <= 1e-9, (name, s, ef)
-            assert rel_l2(gs["u"], fx[f"u_{s}"]) <= 1e-10
+            assert rel_l2(gm[:, 3:3 + D], fx[f"markers_{s}"][:, 5:5 + D]) <= 1e-9, (name, s)
         else:
-            assert eu <= 2e-4, (name, s, eu)
             assert ef <= 1e-3, (name, s, ef)
-    tot = gg[0].ibm_body_force(0)
-    mk = gg[0].ibm_markers(0)
+    tot = gg[blev].ibm_body_force(0)
+    mk = gg[blev].ibm_markers(0)
     vd = mk[:, 7] if D == 3 else 1.0
     ref = (mk[:, 3:3 + D] * (mk[:, 6] * vd * mk[:, 7])[:, None]).sum(axis=0)
     assert np.allclose(tot[:D], ref, rtol=1e-12, atol=0)

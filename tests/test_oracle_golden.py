@@ -115,6 +115,11 @@ def test_oracle_ibm_bit_exact_vs_reference(name):
         st = grids[0].download()
         assert np.array_equal(st["u"], fx[f"u_{s}"]) and np.array_equal(st["rho"], fx[f"rho_{s}"])
         assert R.sha(st["f"]) == str(fx[f"f_sha_{s}"])
+        for g, lv in zip(grids[1:], levels[1:]):   # refined levels (bodies on a sub-grid)
+            key = R.grid_key(lv)
+            st = g.download()
+            _, _, u_sha, rho_sha, f_sha = R.fields_at(fx, key, s, name)
+            assert (R.sha(st["u"]), R.sha(st["rho"]), R.sha(st["f"])) == (u_sha, rho_sha, f_sha), (key, s)
         mk = ibm.markers(0)
         assert np.array_equal(mk[:, 3:3 + D], fx[f"markers_{s}"][:, 5:5 + D]), f"marker force at step {s}"
 
