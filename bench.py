@@ -12,9 +12,16 @@ state, the K steps, and download of u and rho, all inside the timed region.
 Multi-GPU: every rank runs an independent replica of the box (the path has no
 data exchange on one grid per GPU); value = sum over ranks.
 
+The FP32-vs-FP64 accuracy leg runs both paths to t = 10^4 (the stated
+accuracy target's step count) whatever ``--steps`` is, outside the timed
+regions.
+
 ``--impl reference`` times the reference's CPU implementation of the path
-(the oracle restatement of GridObj::LBM_multi_opt, OpenMP over all host
-threads) on a bounded slab of the same workload.
+(the oracle restatement of GridObj::LBM_multi_opt, bit-exact with the
+reference's own serial build, OpenMP over all host threads) on the same
+256^3 box, one full-box LBM step per bench step, plus a 1-thread figure.
+The same CPU leg gives the ``cpu_baseline`` of the GPU line and, from its
+state, the FP64 GPU path's parity at full size.
 """
 from __future__ import annotations
 
@@ -43,6 +50,9 @@ FP64_FLOP_PER_LU_D3Q19 = 231
 FP64_NOMINAL_TFLOPS = 1.25
 U0 = 0.02
 NOISE = 1e-4
+ACCURACY_STEPS = 10000      # step count of the FP32-vs-FP64 accuracy target
+# a CPU sample (warm-up + timed steps) is kept under this many seconds
+CPU_SAMPLE_BUDGET_S = 150.0
 
 
 def workload_level0(n: int, nz: int | None = None):
@@ -136,6 +146,25 @@ def read_peaks() -> dict:
     return {"hbm_gbs": 6800.0, "source": "fallback"}
 
 
+def cpu_model() -> str:
+    """The host CPU's model name (lscpu, else /proc/cpuinfo), or ''."""
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.strip().lower().startswith("model name"):
+                return line.split(":", 1)[1].strip()
+    except (OSError, subprocess.SubprocessError):
+        pass
+    try:
+        with open("/proc/cpuinfo") as fp:
+            for line in fp:
+                if line.lower().startswith("model name"):
+                    return line.split(":", 1)[1].strip()
+    except OSError:
+        pass
+    return ""
+
+
 def read_profile_traffic(name: str):
     """Per-launch DRAM bytes from a committed ncu summary (profiles/<name>.txt,
     line 'dram_bytes_per_launch <bytes>'), or None."""
@@ -152,26 +181,59 @@ def read_profile_traffic(name: str):
     return None
 
 
-def cpu_oracle_mlups(n: int, nz: int, steps: int, warmup: int, threads: int | None, min_seconds: float = 0.0):
-    """Time the oracle (OpenMP) on an n x n x nz slab: `steps` steps, or more
-    in chunks until at least `min_seconds` of CPU work has been timed."""
-    from oracle import oracle as O
-    l0 = workload_level0(n, nz)
-    f0 = equilibrium_f(l0)
-    g = O.OracleGrid(l0.desc())
-    used = O.set_threads(threads or os.cpu_count() or 1)
-    g.upload(f0, l0.u, l0.rho, None, 0)
-    if warmup:
-        g.step(warmup)
-    done = 0
-    t0 = time.perf_counter()
-    g.step(steps)
-    done += steps
-    while time.perf_counter() - t0 < min_seconds:
-        g.step(steps)
-        done += steps
-    dt = time.perf_counter() - t0
-    return l0.ncell * done / dt / 1e6, used, dt, done
+class CpuBox:
+    """The oracle (the reference's algorithm, FP64, bit-exact with its serial
+    build) on the n x n x nz Taylor-Green box, for the CPU baseline."""
+
+    def __init__(self, n: int, nz: int):
+        from oracle import oracle as O
+        self.O = O
+        self.l0 = workload_level0(n, nz)
+        self.g = O.OracleGrid(self.l0.desc())
+        self.g.upload(equilibrium_f(self.l0), self.l0.u, self.l0.rho, None, 0)
+        self.t = 0
+
+    def time(self, steps: int, warmup: int, threads: int) -> dict:
+        """Warm-up steps, then `steps` timed steps (wall clock) on `threads`
+        host threads; the state carries on from the previous call."""
+        used = self.O.set_threads(threads)
+        if warmup:
+            self.g.step(warmup)
+        t0 = time.perf_counter()
+        self.g.step(steps)
+        dt = time.perf_counter() - t0
+        self.t += warmup + steps
+        return {"mlups": self.l0.ncell * steps / dt / 1e6, "threads": used, "seconds": dt, "steps": steps,
+                "warmup": warmup}
+
+    def close(self):
+        self.g.close()
+
+
+def cpu_baseline_full_box(n: int, steps_all: int = 4, steps_one: int = 3):
+    """CPU baseline on the same n^3 box: all host threads (1 warm-up +
+    steps_all timed), then 1 thread (1 warm-up + steps_one timed), fewer when
+    a step would not fit the sample budget.  Returns (record, CpuBox at
+    t = 1 + steps_all with the all-thread state saved as 'state')."""
+    box = CpuBox(n, n)
+    nth = os.cpu_count() or 1
+    allt = box.time(steps_all, 1, nth)
+    state = box.g.download()
+    t_all = box.t
+    est_one = allt["seconds"] / allt["steps"] * allt["threads"] * 1.3   # a 1-thread step, roughly
+    k1 = max(1, min(steps_one, int(CPU_SAMPLE_BUDGET_S / max(est_one, 1e-3)) - 1))
+    one = box.time(k1, 1, 1)
+    box.O.set_threads(nth)
+    rec = {"value": round(allt["mlups"], 3), "unit": "MLUPS", "cores": allt["threads"], "kind": "port",
+           "same_config": True, "nproc": nth, "cpu_model": cpu_model(),
+           "sample": f"{allt['steps']} LBM steps of the full {n}^3 box after 1 warm-up step, all "
+                     f"{allt['threads']} host threads (oracle restatement of GridObj::LBM_multi_opt, FP64, "
+                     f"bit-exact with the reference's serial build; OpenMP over the site loop), "
+                     f"{allt['seconds']:.2f} s",
+           "one_thread": {"value": round(one["mlups"], 3), "unit": "MLUPS", "cores": 1,
+                          "sample": f"{one['steps']} LBM steps of the same box after 1 warm-up step, 1 thread, "
+                                    f"{one['seconds']:.2f} s"}}
+    return rec, box, state, t_all
 
 
 def max_over_ranks(x: float, dist=None, device=None) -> float:
@@ -192,21 +254,45 @@ def replica_mlups(world: int, sites_per_rank: int, steps: int, seconds: float) -
 
 
 def run_reference(args, rank: int, world: int):
+    """The reference's CPU path on the host cores: one LBM step of the full
+    256^3 box per bench step on all host threads (a z-slab of the box per
+    bench step only when K full-box steps would not fit the sample budget),
+    then a 1-thread figure on the same box."""
     if rank != 0:
         return 0
-    nz = 16
-    mlups, used, dt, _ = cpu_oracle_mlups(SIZE, nz, args.steps, args.warmup, None)
-    sample = (f"one LBM step of a {SIZE}x{SIZE}x{nz} periodic slab of the Taylor-Green box per bench step "
-              f"(oracle restatement of GridObj::LBM_multi_opt, FP64, OpenMP)")
+    n = args.size or SIZE
+    nth = os.cpu_count() or 1
+    probe = CpuBox(n, n)
+    est = probe.time(1, 0, nth)["seconds"]          # one full-box step
+    nz = n
+    if est * (args.steps + args.warmup) > CPU_SAMPLE_BUDGET_S:
+        nz = max(8, int(n * CPU_SAMPLE_BUDGET_S / (est * (args.steps + args.warmup))) // 8 * 8)
+    box = probe if nz == n else CpuBox(n, nz)
+    if box is not probe:
+        probe.close()
+    allt = box.time(args.steps, args.warmup, nth)
+    k1 = max(1, min(3, int(CPU_SAMPLE_BUDGET_S / max(est * nth * 1.3 * nz / n, 1e-3)) - 1))
+    one = box.time(k1, 1, 1)
+    box.close()
+    mlups = allt["mlups"]
+    what = f"the full {n}^3 box" if nz == n else f"a {n}x{n}x{nz} slab of the {n}^3 box"
     line = {
         "metric": METRIC, "value": round(mlups, 3), "unit": "MLUPS", "n_gpus": world, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": round(dt / args.steps * 1e3, 4), "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "warmup": args.warmup, "ms_per_step": round(allt["seconds"] / args.steps * 1e3, 4),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "impl": "reference",
-        "config": {"workload": f"D3Q19 LBGK periodic {SIZE}x{SIZE}x{nz} slab, tau={TAU}, TGV u0={U0} + noise {NOISE}",
-                   "precision": "fp64", "host_threads": used},
-        "cpu_baseline": {"value": round(mlups, 3), "unit": "MLUPS", "cores": used, "kind": "port",
-                         "sample": sample},
+        "config": {"workload": f"D3Q19 LBGK periodic {n}^3 Taylor-Green u0={U0} + U(-{NOISE},{NOISE}) noise "
+                               f"(seed 20261203), tau={TAU}",
+                   "precision": "fp64 (the reference's arithmetic)", "host_threads": allt["threads"],
+                   "same_config": nz == n},
+        "cpu_baseline": {"value": round(mlups, 3), "unit": "MLUPS", "cores": allt["threads"], "kind": "port",
+                         "same_config": nz == n, "nproc": nth, "cpu_model": cpu_model(),
+                         "sample": f"one LBM step of {what} per bench step, {args.steps} timed after "
+                                   f"{args.warmup} warm-up (oracle restatement of GridObj::LBM_multi_opt, FP64, "
+                                   f"bit-exact with the reference's serial build; OpenMP over the site loop)",
+                         "one_thread": {"value": round(one["mlups"], 3), "unit": "MLUPS", "cores": 1,
+                                        "sample": f"{one['steps']} LBM steps of {what} after 1 warm-up step, "
+                                                  f"1 thread, {one['seconds']:.2f} s"}},
         "e2e": {"value": round(mlups, 3), "unit": "MLUPS", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -536,14 +622,19 @@ def run_ours(args, rank: int, world: int, local_rank: int):
     sampler.stop()
     sec64 = max_over_ranks_(sec64)
     mlups64 = replica_mlups(world, ncell, K64, sec64)
-    # accuracy at equal step counts: bring both to t = W + K
-    g64.step(K - K64)
+    # accuracy at equal step counts, outside the timed regions: both paths
+    # to t = 10^4 (or W + K when the timed run went further)
+    t_acc = max(ACCURACY_STEPS, W + K)
+    g32.step(t_acc - g32.t)
+    g64.step(t_acc - g64.t)
+    g32.synchronize()
     g64.synchronize()
     s32 = g32.download(f=False)
     s64 = g64.download(f=False)
     eu = float(np.linalg.norm(s32["u"] - s64["u"]) / np.linalg.norm(s64["u"]))
     er = float(np.linalg.norm(s32["rho"] - s64["rho"]) / np.linalg.norm(s64["rho"]))
     red64 = g64.reduce()
+    red32 = g32.reduce()
     g64.close()
 
     # ---- e2e through the C ABI with host buffers (pinned) ----
@@ -582,11 +673,23 @@ def run_ours(args, rank: int, world: int, local_rank: int):
     adjoint = measure_adjoint() if rank == 0 and not args.no_adjoint else None
 
     cpu = None
-    if rank == 0 and not args.no_cpu_baseline:
-        mlc, used, dtc, nst = cpu_oracle_mlups(SIZE, 16, args.cpu_steps, 1, None, min_seconds=10.0)
-        cpu = {"value": round(mlc, 3), "unit": "MLUPS", "cores": used, "kind": "port",
-               "sample": f"{nst} LBM steps of a {SIZE}x{SIZE}x16 periodic slab of the same box "
-                         f"(oracle restatement, FP64, OpenMP), {dtc:.1f} s"}
+    parity = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        cpu, box, ostate, t_o = cpu_baseline_full_box(n, steps_all=args.cpu_steps)
+        # the FP64 GPU path at full size against the CPU leg's own state (the
+        # oracle after the same steps from the same initial state)
+        gp = GpuGrid(l0.desc(precision=A.PREC_FP64))
+        gp.set_stream(stream.cuda_stream)
+        gp.upload(f0, l0.u, l0.rho, None, 0)
+        gp.step(t_o)
+        gs = gp.download()
+        gp.close()
+        box.close()
+        rl = lambda a, b: float(np.linalg.norm(a - b) / np.linalg.norm(b))  # noqa: E731
+        parity = {"after_steps": t_o, "rel_l2_u": rl(gs["u"], ostate["u"]), "rel_l2_rho": rl(gs["rho"], ostate["rho"]),
+                  "rel_l2_f": rl(gs["f"], ostate["f"]), "bound": 1e-10,
+                  "what": f"GPU FP64 path vs the oracle (the reference's arithmetic) on the full {n}^3 box"}
+        del gs, ostate
 
     if rank == 0:
         line = {
@@ -606,6 +709,9 @@ def run_ours(args, rank: int, world: int, local_rank: int):
             "gpu_launches": K,
             "roofline": {"bound": "hbm", "achieved": round(ach32, 1), "peak": peaks["hbm_gbs"], "unit": "GB/s",
                          "frac": round(ach32 / peaks["hbm_gbs"], 4), "traffic": traffic,
+                         "traffic_source": ("profiles/k_aa_d3q19_fp32_256.txt: dram__bytes_read.sum + "
+                                            "dram__bytes_write.sum of one launch of this kernel on this workload "
+                                            "(ncu, 1 pass), not measured in this run") if traffic else None,
                          "peak_source": peaks["source"], "kernel": "k_aa<19,P32>",
                          "bytes_per_launch": bytes32},
             "fp64": {"value": round(mlups64, 2), "unit": "MLUPS", "steps": K64,
@@ -617,7 +723,10 @@ def run_ours(args, rank: int, world: int, local_rank: int):
                                                    FP64_NOMINAL_TFLOPS, 3),
                      "bound": "FP64 pipe (231 FP64 FLOP per update, counted with ncu)"},
             "fp32_vs_fp64": {"speedup": round(mlups32 / mlups64, 3), "rel_l2_u": eu, "rel_l2_rho": er,
-                             "after_steps": W + K, "fp64_mass": red64["mass"]},
+                             "after_steps": t_acc, "bound_rel_l2_u": 1e-5, "fp64_mass": red64["mass"],
+                             "fp32_mass": red32["mass"],
+                             "what": "both paths from the same initial state to t = after_steps (untimed)"},
+            "fp64_parity_full_size": parity,
             "cpu_baseline": cpu,
             "adjoint": adjoint,
         }
@@ -641,7 +750,7 @@ def main(argv=None) -> int:
                          "one refinement level and 64 FEM filaments; bfl: D2Q9 channel with a BFL cylinder")
     ap.add_argument("--precision", default="both", choices=["both", "fp32", "fp64"],
                     help="sphere / cylinder_adjoint workloads: which precisions to run")
-    ap.add_argument("--cpu-steps", type=int, default=20)
+    ap.add_argument("--cpu-steps", type=int, default=4, help="timed all-thread steps of the CPU baseline")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint workload measurement")
     args = ap.parse_args(argv)

@@ -11,7 +11,7 @@
  * whose state is the GridObj members f, fNew, u, rho, force_xyz, LatTyp,
  * omega, dt, dh, ux_in/uy_in/uz_in, CoarseLims and the sub-grid tree
  * (LUMA inc/GridObj.h:54-127).  A host shim compiled into those member
- * functions forwards to the entry points below (see INTEGRATION.md).
+ * functions forwards to the entry points below.
  *
  * Conventions
  *  - Every entry point returns an int status: LUMA_OK (0) or a negative
@@ -138,6 +138,9 @@ typedef struct luma_reduction {
 } luma_reduction;
 
 /* ---- version / errors -------------------------------------------------- */
+/* No counterpart in the reference: its failures go through L_ERROR
+ * (inc/stdafx.h:127-149), which logs and exits; here the ABI version and
+ * the calling thread's last error message. */
 int luma_gpu_abi_version(void);
 const char *luma_gpu_last_error_string(void);
 
@@ -147,51 +150,66 @@ const char *luma_gpu_last_error_string(void);
  * one grid; `parent` is NULL for level 0, else the parent's handle (the new
  * grid becomes its next sub-grid, in region order). */
 int luma_gpu_grid_create(const luma_grid_desc *desc, luma_gpu_grid *parent, luma_gpu_grid **out);
-/* Destroys a grid and its sub-grids. */
+/* Destroys a grid and its sub-grids: GridObj::~GridObj
+ * (src/GridObj.cpp:39) over the tree, as `delete Grids` (src/main_lbm.cpp:667). */
 int luma_gpu_grid_destroy(luma_gpu_grid *grid);
-/* Selects the CUDA stream (a cudaStream_t, may be NULL for the legacy
- * stream) used by every subsequent call on this grid tree. */
+/* No counterpart in the reference (its step runs on the calling host
+ * thread).  Selects the CUDA stream (a cudaStream_t, may be NULL for the
+ * legacy stream) used by every subsequent call on this grid tree. */
 int luma_gpu_set_stream(luma_gpu_grid *root, void *cuda_stream);
 
 /* ---- state transfer ------------------------------------------------------ */
-/* Host -> device: f (N*M*K*Q), u (N*M*K*dims), rho (N*M*K); force_xyz may be
+/* The state the reference keeps in GridObj::f, u, rho, force_xyz
+ * (inc/GridObj.h:54-127).
+ * Host -> device: f (N*M*K*Q), u (N*M*K*dims), rho (N*M*K); force_xyz may be
  * NULL and is ignored on grids without IBM or gravity forcing.  Arrays in the reference layout (post-collision f, as GridObj::f
  * holds between time steps).  Sets the grid's step counter to t. */
 int luma_gpu_upload_state(luma_gpu_grid *grid, const double *f, const double *u,
                           const double *rho, const double *force_xyz, int t);
-/* Device -> host, same layout; any pointer may be NULL to skip it. */
+/* Device -> host into the GridObj members' layout (inc/GridObj.h:54-127);
+ * any pointer may be NULL to skip it. */
 int luma_gpu_download_state(luma_gpu_grid *grid, double *f, double *u, double *rho,
                             double *force_xyz);
 /* Running means of a grid created with LUMA_FLAG_TIME_AVERAGES
- * (GridObj::rho_timeav, ui_timeav, uiuj_timeav; reference layout: N*M*K,
+ * (GridObj::rho_timeav, ui_timeav, uiuj_timeav, inc/GridObj.h:93-95;
+ * reference layout: N*M*K,
  * N*M*K*dims, N*M*K*(3*dims-3) with the (p, q >= p) pairs in order). */
 int luma_gpu_download_time_averages(luma_gpu_grid *grid, double *rho_ta, double *ui_ta, double *uiuj_ta);
-/* Step counter of a grid (GridObj::t). */
+/* Step counter of a grid (GridObj::t, inc/GridObj.h:111). */
 int luma_gpu_get_time(const luma_gpu_grid *grid, int *t);
 
 /* ---- the time step ------------------------------------------------------ */
-/* Runs `nsteps` calls of GridObj::LBM_multi_opt() on the root grid: each
+/* Runs `nsteps` calls of GridObj::LBM_multi_opt()
+ * (src/GridObj_ops_lbm_optimised.cpp:36-193, as src/main_lbm.cpp:441 calls it) on the root grid: each
  * recursively advances every sub-grid two sub-steps, then this grid one
  * step (explode/coalesce, IBM pass and collision included).  Asynchronous
  * on the grid's stream. */
 int luma_gpu_step(luma_gpu_grid *root, int nsteps);
-/* Blocks until all work queued on the grid's stream has finished. */
+/* No counterpart in the reference (its step is synchronous).  Blocks until
+ * all work queued on the grid's stream has finished; reports a site that
+ * needed an operation outside the GPU path (the first grid of the tree
+ * with one) and clears that record. */
 int luma_gpu_synchronize(luma_gpu_grid *root);
 
 /* ---- reductions / watchdog ----------------------------------------------- */
+/* No counterpart in the reference (it keeps no running sums).  FP64 sums
+ * over the grid's fluid-updated sites (see luma_reduction), deterministic:
+ * the same state gives the same bits.  Blocks until the result is on the
+ * host. */
 int luma_gpu_reduce(luma_gpu_grid *grid, luma_reduction *out);
 
 /* No counterpart in the reference.  The FP64 reduction of luma_gpu_reduce
- * for callers that cannot allocate device memory — code running inside a
- * CUDA-graph stream capture, hosts that give the GPU's memory to a fixed
- * pool at start-up, real-time loops — over SoA device arrays they own:
- * typ[n] site labels (uint8, LUMA_SITE_*), rho[n], u[d*n + id] (FP64).
- * It allocates nothing: its scratch is a fixed 64 KiB device array held by
- * every GPU that loads the library.  At most 16,777,216 sites (larger n is
- * rejected with LUMA_E_INVALID).  The first call on a device sets up that
- * device's scratch address, so make it before any stream capture.  Calls
- * share the scratch: calls whose kernels overlap on the GPU race.
- * Blocks until the result is on the host. */
+ * for callers that cannot allocate device memory — hosts that give the
+ * GPU's memory to a fixed pool at start-up and forbid later allocations,
+ * real-time loops that cannot afford an allocation's latency or failure —
+ * over SoA device arrays they own: typ[n] site labels (uint8, LUMA_SITE_*),
+ * rho[n], u[d*n + id] (FP64).  It allocates nothing: its scratch is a fixed
+ * 64 KiB device array held by every GPU that loads the library.  At most
+ * 16,777,216 sites (larger n is rejected with LUMA_E_INVALID).  The first
+ * call on a device sets up that device's scratch address, so make it before
+ * any stream capture; the address is cached for the process, so the call is
+ * not valid after cudaDeviceReset.  Calls share the scratch: calls whose
+ * kernels overlap on the GPU race.  Blocks until the result is on the host. */
 int luma_gpu_reduce_fields_noalloc(const uint8_t *typ, const double *rho, const double *u, int64_t n,
                                    int dims, void *cuda_stream, luma_reduction *out);
 
@@ -236,7 +254,8 @@ int luma_gpu_ibm_initialise(luma_gpu_grid *root);
 int luma_gpu_ibm_add_filament(luma_gpu_grid *grid, const double start[3], double length, double height,
                               double depth, double angle_v, int nel, int clamped, double density,
                               double youngs_modulus, double dm, double fsi_vel_scale, int *body_index);
-/* Per-marker state, 9 doubles per marker: x y z Fx Fy Fz epsilon ds nsupport
+/* IBMarker state (inc/IBMarker.h:33-74) of one body of the grid,
+ * 9 doubles per marker: x y z Fx Fy Fz epsilon ds nsupport
  * (F = the last IBM force of ibm_computeForce, lattice units). */
 int luma_gpu_ibm_get_markers(luma_gpu_grid *grid, int body, double *out);
 /* FP64 sum over a body's markers of F*epsilon*ds (*ds in 3D): the force the
@@ -285,9 +304,11 @@ int luma_gpu_io_lite(luma_gpu_grid *root, const char *dir, double tval, int prec
  * <dir>/restart_LBM_Rnk<rank>.out, level 0 then each sub-grid after its
  * parent; same snapshot and host-thread scheme as luma_gpu_io_lite. */
 int luma_gpu_io_restart(luma_gpu_grid *root, const char *dir, int rank);
-/* Waits for the tree's pending writers; returns the first error they met. */
+/* No counterpart in the reference (its writers are synchronous).  Waits
+ * for the tree's pending writers; returns the first error they met. */
 int luma_gpu_io_wait(luma_gpu_grid *root);
-/* The two formats from host arrays in the reference layout (f, fnew: N*M*K*Q;
+/* GridObj::io_lite and io_restart(eWrite) (src/GridObj_ops_io.cpp:406-490,
+ * 706-810), the two formats from host arrays in the reference layout (f, fnew: N*M*K*Q;
  * u: N*M*K*dims; rho: N*M*K), with the labels, positions, dt, dh and omega
  * of `desc`: the formatting alone, for callers that hold the state.
  * fnew may be NULL (f is written in its place); the three time averages
@@ -326,14 +347,15 @@ int luma_io_restart_read(const char *path, int ngrids, const luma_grid_desc *con
  * bodies; site types fluid, solid, velocity, extrapolate-right; no
  * regularised BCs, gravity or ramp (LUMA_E_INVALID otherwise). */
 int luma_gpu_adj_forward(luma_gpu_grid *grid, int nsteps, int checkpoint_every, int body, double *J);
-/* Backward: once per forward.  Recomputes each checkpoint segment, runs the
+/* No counterpart in the reference.  Backward: once per forward.  Recomputes each checkpoint segment, runs the
  * reverse steps and returns dJ * dJ/ds for the scale s of the velocity of
  * every velocity site (u = s * u_uploaded, at s = 1) and dJ * dJ/dX for the
  * body's marker positions (dims doubles per marker, reference length
  * units; through the supports' delta values, epsilon and ds).  Either
  * output may be NULL.  The grid is left in the state after the forward. */
 int luma_gpu_adj_backward(luma_gpu_grid *grid, double dJ, double *grad_inlet_scale, double *grad_markers);
-/* Device bytes held by the checkpoints and the tape of the last forward. */
+/* No counterpart in the reference.  Device bytes held by the checkpoints
+ * and the tape of the last forward. */
 int luma_gpu_adj_memory(const luma_gpu_grid *grid, size_t *bytes);
 
 #ifdef __cplusplus

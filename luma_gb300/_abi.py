@@ -1,4 +1,4 @@
-"""ctypes mirror of ``include/luma_gpu.h`` (ABI version 1).
+"""ctypes mirror of ``include/luma_gpu.h`` (the ABI version is ``ABI_VERSION`` below).
 
 The structure layouts here must match the header field for field; a CPU
 test checks the sizes against the compiled library's own view.

@@ -685,7 +685,7 @@ int luma_gpu_grid_create(const luma_grid_desc *desc, luma_gpu_grid *parent, luma
     CKF(cudaMemcpy(g->uxin, d.ux_in, d.M * sizeof(double), cudaMemcpyHostToDevice));
     CKF(cudaMemcpy(g->uyin, d.uy_in, d.M * sizeof(double), cudaMemcpyHostToDevice));
     CKF(cudaMemcpy(g->uzin, d.uz_in, d.M * sizeof(double), cudaMemcpyHostToDevice));
-    CKF(cudaMalloc(&g->acc, 8 * sizeof(double)));
+    CKF(cudaMalloc(&g->acc, (size_t)(kReduceBlocks + 1) * 8 * sizeof(double)));
     CKF(cudaMalloc(&g->unsup, sizeof(int)));
     CKF(cudaMemset(g->unsup, 0, sizeof(int)));
     if (d.flags & LUMA_FLAG_TIME_AVERAGES) {
@@ -922,7 +922,7 @@ int luma_gpu_reduce(luma_gpu_grid *g, luma_reduction *out) {
     out->momentum[1] = h[2];
     out->momentum[2] = h[3];
     out->kinetic_energy = h[4];
-    memcpy(&out->max_speed, &h[5], sizeof(double));
+    out->max_speed = h[5];
     out->nonfinite = (int64_t)h[6];
     return LUMA_OK;
 }

@@ -79,11 +79,16 @@ __device__ __forceinline__ double warp_max(double v) {
 
 // Sums over the sites the macroscopic step updates (fluid, BFL, slip and
 // transition-to-finer), accumulated in FP64: mass, momentum, kinetic energy;
-// max |u| and a count of non-finite values.
+// max |u| and a count of non-finite values.  Deterministic: each of the
+// kReduceBlocks blocks sums a fixed set of sites (grid stride) in a fixed
+// order and writes its partials to its own slot; k_reduce_fold then adds the
+// slots in block order.  The same state gives the same bits on every run.
 template <class P>
-__global__ void k_reduce(const uint8_t *__restrict__ typ, const typename P::R *__restrict__ rho,
-                         const typename P::R *__restrict__ u, size_t n, int dims, double *acc) {
-    double m = 0, mx = 0, my = 0, mz = 0, ke = 0, umax = 0, bad = 0;
+__global__ void __launch_bounds__(256) k_reduce(const uint8_t *__restrict__ typ, const typename P::R *__restrict__ rho,
+                                                const typename P::R *__restrict__ u, size_t n, int dims,
+                                                double *partials) {
+    __shared__ double sh[8][8];
+    double v[8] = {0, 0, 0, 0, 0, 0, 0, 0};
     for (size_t id = (size_t)blockIdx.x * blockDim.x + threadIdx.x; id < n; id += (size_t)gridDim.x * blockDim.x) {
         const int t = typ[id];
         if (!(t == LUMA_SITE_FLUID || t == LUMA_SITE_BFL || t == LUMA_SITE_SLIP || t == LUMA_SITE_TL_TO_FINER))
@@ -91,33 +96,41 @@ __global__ void k_reduce(const uint8_t *__restrict__ typ, const typename P::R *_
         const double r = double(rho[id]);
         const double ux = double(u[id]), uy = double(u[n + id]), uz = dims == 3 ? double(u[2 * n + id]) : 0.0;
         if (!isfinite(r) || !isfinite(ux) || !isfinite(uy) || !isfinite(uz)) {
-            bad += 1.0;
+            v[6] += 1.0;
             continue;
         }
-        m += r;
-        mx += r * ux;
-        my += r * uy;
-        mz += r * uz;
+        v[0] += r;
+        v[1] += r * ux;
+        v[2] += r * uy;
+        v[3] += r * uz;
         const double q = ux * ux + uy * uy + uz * uz;
-        ke += 0.5 * r * q;
-        umax = fmax(umax, sqrt(q));
+        v[4] += 0.5 * r * q;
+        v[5] = fmax(v[5], sqrt(q));
     }
-    m = warp_sum(m);
-    mx = warp_sum(mx);
-    my = warp_sum(my);
-    mz = warp_sum(mz);
-    ke = warp_sum(ke);
-    bad = warp_sum(bad);
-    umax = warp_max(umax);
-    if ((threadIdx.x & 31) == 0) {
-        atomicAdd(acc + 0, m);
-        atomicAdd(acc + 1, mx);
-        atomicAdd(acc + 2, my);
-        atomicAdd(acc + 3, mz);
-        atomicAdd(acc + 4, ke);
-        atomicMax(reinterpret_cast<unsigned long long *>(acc + 5), (unsigned long long)__double_as_longlong(umax));
-        atomicAdd(acc + 6, bad);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+        const double w = k == 5 ? warp_max(v[k]) : warp_sum(v[k]);
+        if (lane == 0) sh[warp][k] = w;
     }
+    __syncthreads();
+    if (threadIdx.x < 8) {
+        const int k = threadIdx.x;
+        double acc = sh[0][k];
+        for (int w = 1; w < (int)(blockDim.x >> 5); ++w) acc = k == 5 ? fmax(acc, sh[w][k]) : acc + sh[w][k];
+        partials[(size_t)blockIdx.x * 8 + k] = acc;
+    }
+}
+
+__global__ void k_reduce_fold(const double *__restrict__ partials, int nblocks, double *out) {
+    const int k = threadIdx.x;
+    if (k >= 8) return;
+    double acc = partials[k];
+    for (int b = 1; b < nblocks; ++b) {
+        const double x = partials[(size_t)b * 8 + k];
+        acc = k == 5 ? fmax(acc, x) : acc + x;
+    }
+    out[k] = acc;
 }
 
 }  // namespace
@@ -151,9 +164,12 @@ cudaError_t launch_vec_out(const void *soa, double *aos, size_t n, int dims, cud
 template <class P>
 cudaError_t launch_reduce(const uint8_t *typ, const void *rho, const void *u, size_t n, int dims, double *acc,
                           cudaStream_t s) {
-    cudaMemsetAsync(acc, 0, 7 * sizeof(double), s);
-    k_reduce<P><<<152 * 4, 256, 0, s>>>(typ, static_cast<const typename P::R *>(rho),
-                                         static_cast<const typename P::R *>(u), n, dims, acc);
+    double *partials = acc + 8;
+    k_reduce<P><<<kReduceBlocks, 256, 0, s>>>(typ, static_cast<const typename P::R *>(rho),
+                                               static_cast<const typename P::R *>(u), n, dims, partials);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    k_reduce_fold<<<1, 32, 0, s>>>(partials, kReduceBlocks, acc);
     return cudaGetLastError();
 }
 

@@ -43,9 +43,12 @@ template <class P>
 cudaError_t launch_vec_in(const double *aos, void *soa, size_t n, int dims, cudaStream_t s);
 template <class P>
 cudaError_t launch_vec_out(const void *soa, double *aos, size_t n, int dims, cudaStream_t s);
+// Blocks of the FP64 field reduction; its device buffer holds
+// (kReduceBlocks + 1) * 8 doubles: the result (mass, mx, my, mz, ke, max|u|,
+// nonfinite, spare) followed by one slot of partials per block.
+constexpr int kReduceBlocks = 152 * 4;
 template <class P>
-cudaError_t launch_reduce(const uint8_t *typ, const void *rho, const void *u, size_t n, int dims,
-                          double *acc /* device: mass, mx, my, mz, ke, maxspeed(bits), nonfinite */,
+cudaError_t launch_reduce(const uint8_t *typ, const void *rho, const void *u, size_t n, int dims, double *acc,
                           cudaStream_t s);
 
 }  // namespace luma

@@ -1,13 +1,13 @@
 // Field reductions for callers that cannot allocate device memory.
 //
 // Some callers of this library cannot call cudaMalloc or let a library do it
-// for them: code running while a stream is being captured into a CUDA graph
-// (allocation is not a capturable operation), hosts that hand the GPU's
-// memory to a fixed-size pool at start-up and forbid later allocations, and
-// real-time loops where an allocation's latency or failure is not
+// for them: hosts that hand the GPU's memory to a fixed-size pool at
+// start-up and forbid any later allocation, and real-time loops where an
+// allocation's latency, or its failure under memory pressure, is not
 // acceptable.  luma_gpu_reduce_fields_noalloc gives them the FP64 mass /
 // momentum / energy reduction of luma_gpu_reduce over device arrays they
-// already own, using only the fixed scratch array below.
+// already own, using only the fixed scratch array below.  The call blocks
+// until the result is on the host.
 //
 // Scratch: one file-scope __device__ array of (kBlocks + 1) * 8 doubles
 // (64 KiB + 64 B).  Every GPU that loads this library holds it until the
@@ -21,7 +21,9 @@
 // address: the device address is obtained once per device with
 // cudaGetSymbolAddress, with that device current, and passed to the
 // kernels.  The first call on each device performs that set-up, so make the
-// first call on a device before starting any stream capture.
+// first call on a device before starting any stream capture.  The address
+// is cached for the life of the process: after cudaDeviceReset the cached
+// address is stale and the call must not be used again in that process.
 #include <cuda_runtime.h>
 
 #include <cstdint>
@@ -139,13 +141,20 @@ extern "C" int luma_gpu_reduce_fields_noalloc(const uint8_t *typ, const double *
     double *scratch = nullptr;
     int rc = scratch_address(&scratch);
     if (rc) return rc;
+    // an error left pending by an earlier, unrelated call belongs to that
+    // call's owner: report it without clearing it and launch nothing
+    cudaError_t e = cudaPeekAtLastError();
+    if (e != cudaSuccess)
+        return luma_set_error(LUMA_E_CUDA, "a CUDA error was pending before the reduction: %s", cudaGetErrorString(e));
     cudaStream_t s = static_cast<cudaStream_t>(cuda_stream);
     const int64_t chunk = (int64_t)kThreads * kItemsPerThread;
     const int nblocks = (int)((n + chunk - 1) / chunk);
     k_partials<<<nblocks, kThreads, 0, s>>>(typ, rho, u, n, dims, chunk, scratch);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return luma_set_error(LUMA_E_CUDA, "k_partials launch: %s", cudaGetErrorString(e));
     k_fold<<<1, 32, 0, s>>>(nblocks, scratch);
-    cudaError_t e = cudaGetLastError();
-    if (e != cudaSuccess) return luma_set_error(LUMA_E_CUDA, "reduction launch: %s", cudaGetErrorString(e));
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return luma_set_error(LUMA_E_CUDA, "k_fold launch: %s", cudaGetErrorString(e));
     double h[kValues];
     e = cudaMemcpyAsync(h, scratch + kBlocks * kValues, sizeof h, cudaMemcpyDeviceToHost, s);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s);

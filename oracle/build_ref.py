@@ -13,7 +13,8 @@ Left out of the build: ``main_lbm.cpp`` (the harness replaces it) and the
 unconditionally; it compiles against the do-nothing ``shim/hdf5.h`` (its
 HDF5 writer is never called) for its ASCII writers.
 
-Usage: ``python oracle/build_ref.py [--ref LUMA_DIR] [case ...]``
+Usage: ``python oracle/build_ref.py [--ref LUMA_DIR] [case ...]`` (default
+``$LUMA_REFERENCE_DIR``).
 """
 from __future__ import annotations
 
@@ -26,7 +27,11 @@ import sys
 HERE = os.path.dirname(os.path.abspath(__file__))
 CASES_DIR = os.path.join(HERE, "cases")
 OUT_ROOT = os.path.join(HERE, "_ref")
-DEFAULT_REF = "/root/reference/LUMA"
+# The reference checkout's LUMA directory: $LUMA_REFERENCE_DIR, else the place
+# this recipe's build container holds it.  Only this recipe and the fixture
+# scripts under tests/golden/ read the reference; nothing at run time does.
+REF_ENV = "LUMA_REFERENCE_DIR"
+DEFAULT_REF = os.environ.get(REF_ENV) or "/root/reference/LUMA"
 
 EXCLUDE_PREFIX = ("main_lbm", "MpiManager", "Mpi_buffer")
 

@@ -14,7 +14,7 @@ The runs are independent processes, spread over the host cores.
 Output: ``adjoint_fd_cyl400.json`` beside this script.
 
 Usage (needs the reference checkout; not run on the GPU machine):
-    python tests/golden/make_adjoint_fd.py [--ref /root/reference/LUMA] [--steps 4000]
+    python tests/golden/make_adjoint_fd.py [--ref LUMA_DIR]  (default: $LUMA_REFERENCE_DIR, see oracle/build_ref.py) [--steps 4000]
 """
 from __future__ import annotations
 

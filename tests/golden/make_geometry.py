@@ -24,7 +24,7 @@ markers (as above) and, for BFL runs, the body's Q table and per-site marker
 lookup (``--bfl-out``).
 
 Usage (needs the reference checkout; not run on the GPU machine):
-    python tests/golden/make_geometry.py [--ref /root/reference/LUMA]
+    python tests/golden/make_geometry.py [--ref LUMA_DIR]  (default: $LUMA_REFERENCE_DIR, see oracle/build_ref.py)
 """
 from __future__ import annotations
 

@@ -12,7 +12,7 @@ holds for the current algorithm: the t=0 D2Q9 equilibrium row of
 ``cases/testsuite/base/case000/io_lite.Lev0.Reg0.Rnk0.0.dat``.
 
 Usage (needs the reference checkout; not run on the GPU machine):
-    python tests/golden/make_golden.py [--ref /root/reference/LUMA] [case ...]
+    python tests/golden/make_golden.py [--ref LUMA_DIR]  (default: $LUMA_REFERENCE_DIR, see oracle/build_ref.py) [case ...]
 """
 from __future__ import annotations
 

@@ -23,7 +23,7 @@ positions, which pin the std::round of the sub-grid edges.
 Output: ``initial_velocity.npz`` beside this script.
 
 Usage (needs the reference checkout; not run on the GPU machine):
-    python tests/golden/make_initvel.py [--ref /root/reference/LUMA]
+    python tests/golden/make_initvel.py [--ref LUMA_DIR]  (default: $LUMA_REFERENCE_DIR, see oracle/build_ref.py)
 """
 from __future__ import annotations
 

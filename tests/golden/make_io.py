@@ -15,7 +15,7 @@ it leaves them.
 Output: ``io_<case>.json`` beside this script.
 
 Usage (needs the reference checkout; not run on the GPU machine):
-    python tests/golden/make_io.py [--ref /root/reference/LUMA]
+    python tests/golden/make_io.py [--ref LUMA_DIR]  (default: $LUMA_REFERENCE_DIR, see oracle/build_ref.py)
 """
 from __future__ import annotations
 

@@ -9,7 +9,7 @@ over the solid sites during step s, from the populations before it.
 Output: ``momex_d2q9.json`` beside this script.
 
 Usage (needs the reference checkout; not run on the GPU machine):
-    python tests/golden/make_momex.py [--ref /root/reference/LUMA] [--steps 300]
+    python tests/golden/make_momex.py [--ref LUMA_DIR]  (default: $LUMA_REFERENCE_DIR, see oracle/build_ref.py) [--steps 300]
 """
 from __future__ import annotations
 

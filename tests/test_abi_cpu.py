@@ -145,9 +145,20 @@ def test_desc_struct_size_matches_header():
     assert int(out[1]) == C.sizeof(A.Reduction)
 
 
-def test_integration_guide_maps_every_entry_point():
-    """Every function the header declares has a row in the integration
-    guide's table of the reference interfaces they replace."""
-    guide = open(os.path.join(ROOT, "INTEGRATION.md")).read()
-    missing = [n for n in declared_functions() if f"`{n}`" not in guide]
+def test_every_entry_point_cites_what_it_replaces():
+    """The comment that documents each declared function (the nearest
+    block comment above it, which a group of functions may share) names the
+    reference interface the entry point replaces by file (src/... or
+    inc/...), or states that it has no counterpart in the reference."""
+    src = open(HEADER).read()
+    cite = re.compile(r"\b(?:src|inc)/\w+\.(?:cpp|h)|no counterpart in the reference", re.I)
+    missing = []
+    for name in declared_functions():
+        m = re.search(r"^\s*(?:int|const char \*)\s*" + name + r"\s*\(", src, re.M)
+        assert m, name
+        comments = list(re.finditer(r"/\*.*?\*/", src[:m.start()], re.S))
+        # skip section rulers ("/* ---- name ---- */") to the comment that documents the call
+        doc = next((c.group(0) for c in reversed(comments) if not re.match(r"/\* -{3,}", c.group(0))), "")
+        if not cite.search(doc):
+            missing.append(name)
     assert not missing, missing

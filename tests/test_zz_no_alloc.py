@@ -1,11 +1,12 @@
 """The no-allocation reduction entry point, through the C ABI.
 
 luma_gpu_reduce_fields_noalloc serves callers that cannot allocate device
-memory (code inside a CUDA-graph stream capture, hosts with a fixed
-pre-allocated memory pool, real-time loops).  It must give the same FP64
-sums as luma_gpu_reduce on the same fields — here within the FP64 parity
-tolerance of these tests (relative 1e-10) — on two calls in a row, because
-both calls share the entry point's fixed scratch array; and it must refuse a
+memory (hosts that give the GPU's memory to a fixed pool at start-up,
+real-time loops that cannot afford an allocation).  It must give the same
+FP64 sums as luma_gpu_reduce on the same fields — here within the FP64
+parity tolerance of these tests (relative 1e-10) — on two calls in a row,
+because both calls share the entry point's fixed scratch array; the second
+call must leave the device's free memory unchanged; and it must refuse a
 size beyond its stated maximum with a clear error.
 
 This file is collected last so that a stop-at-first-failure run has already
@@ -63,11 +64,15 @@ def test_noalloc_reduction_matches_reduce(name):
     rho = torch.from_numpy(st["rho"]).to(dev)
     u = torch.from_numpy(np.ascontiguousarray(st["u"].reshape(n, D).T)).to(dev)  # SoA u[d][id]
     stream = torch.cuda.current_stream(dev)
-    for _ in range(2):  # two calls in a row share the scratch array
+    torch.cuda.synchronize(dev)
+    for call in range(2):  # two calls in a row share the scratch array
+        free0 = torch.cuda.mem_get_info(dev)[0]
         out = A.Reduction()
         check(L.luma_gpu_reduce_fields_noalloc(typ.data_ptr(), rho.data_ptr(), u.data_ptr(), n, D,
                                                stream.cuda_stream, C.byref(out)))
         _close(out, ref, n)
+        if call == 1:   # the first call may load the module's code; the second allocates nothing
+            assert torch.cuda.mem_get_info(dev)[0] == free0
     g.close()
 
 
