@@ -187,8 +187,9 @@ int luma_gpu_get_time(const luma_gpu_grid *grid, int *t);
 int luma_gpu_step(luma_gpu_grid *root, int nsteps);
 /* No counterpart in the reference (its step is synchronous).  Blocks until
  * all work queued on the grid's stream has finished; reports a site that
- * needed an operation outside the GPU path (the first grid of the tree
- * with one) and clears that record. */
+ * needed an operation outside the GPU path (LUMA_E_INVALID) or a filament
+ * marker that left its grid during the steps (LUMA_E_DOMAIN), for the first
+ * grid of the tree with one, and clears that record. */
 int luma_gpu_synchronize(luma_gpu_grid *root);
 
 /* ---- reductions / watchdog ----------------------------------------------- */

@@ -334,15 +334,54 @@ bool bulk_eligible(const luma_gpu_grid *g, const int32_t *typ) {
     return true;
 }
 
+void set_tree_stream(luma_gpu_grid *g, cudaStream_t s) {
+    g->stream = s;
+    for (luma_gpu_grid *c : g->kids) set_tree_stream(c, s);
+}
+
+// A grid with sub-grids whose interior sites run in their own kernel: those
+// sites read and write nothing the sub-grids' steps touch (the sub-grids
+// read this grid's pre-step populations for explode; coalesce and the
+// transition sites are in the list kernel), so the interior kernel runs
+// beside the sub-grids' two sub-steps, which go to a high-priority stream;
+// the list kernel and everything after it wait for both.
+bool overlap_kids(const luma_gpu_grid *g) {
+    return !g->kids.empty() && g->fast && !g->bulk && !g->adj && g->kid_stream && g->ev_fork && g->ev_join;
+}
+
 int step_grid(luma_gpu_grid *g, int subcycle, bool write_macro) {
     if (g->d.reynolds_ramp > 0.0) update_reynolds(g);
-    for (luma_gpu_grid *c : g->kids)
-        for (int it = 0; it < 2; ++it) {
-            int rc = step_grid(c, it, true);
-            if (rc) return rc;
-        }
     const luma_grid_desc &d = g->d;
     cudaStream_t s = g->stream;
+    const bool overlap = overlap_kids(g);
+    if (overlap) {
+        StepArgs ai = make_args(g, subcycle);
+        ai.macro_out = write_macro || (d.flags & (LUMA_FLAG_GRAVITY | LUMA_FLAG_REGULARISED)) ? 1 : 0;
+        if (g->ibm && g->ibm->has_bodies) {
+            int rc = luma_ibm_reset_forces(g, ai);
+            if (rc) return rc;
+        }
+        CK(cudaEventRecord(g->ev_fork, s));
+        CK(dispatch(d.Q, d.precision, [&](auto q, auto p) {
+            return launch_general_phaseA<decltype(q)::value, decltype(p)>(ai, g->wall, g->fast, g->gen_ids, g->ngen, s,
+                                                                          kPhaseAInterior);
+        }));
+        CK(cudaStreamWaitEvent(g->kid_stream, g->ev_fork, 0));
+        for (luma_gpu_grid *c : g->kids) set_tree_stream(c, g->kid_stream);
+        int rc = LUMA_OK;
+        for (luma_gpu_grid *c : g->kids)
+            for (int it = 0; it < 2 && rc == LUMA_OK; ++it) rc = step_grid(c, it, true);
+        for (luma_gpu_grid *c : g->kids) set_tree_stream(c, s);
+        if (rc) return rc;
+        CK(cudaEventRecord(g->ev_join, g->kid_stream));
+        CK(cudaStreamWaitEvent(s, g->ev_join, 0));
+    } else {
+        for (luma_gpu_grid *c : g->kids)
+            for (int it = 0; it < 2; ++it) {
+                int rc = step_grid(c, it, true);
+                if (rc) return rc;
+            }
+    }
     if (g->bulk) {
         CK(dispatch(d.Q, d.precision, [&](auto q, auto p) {
             return launch_aa<decltype(q)::value, decltype(p)>(g->f[0], g->u, g->rho, d.N, d.M, d.K, d.omega,
@@ -359,12 +398,13 @@ int step_grid(luma_gpu_grid *g, int subcycle, bool write_macro) {
     // step that follows recomputes them before any use.
     a.macro_out = write_macro || (d.flags & (LUMA_FLAG_GRAVITY | LUMA_FLAG_REGULARISED)) ? 1 : 0;
     if (g->adj) luma_adj_redirect(g, a);
-    if (g->ibm && g->ibm->has_bodies) {
+    if (g->ibm && g->ibm->has_bodies && !overlap) {
         int rc = luma_ibm_reset_forces(g, a);
         if (rc) return rc;
     }
     CK(dispatch(d.Q, d.precision, [&](auto q, auto p) {
-        return launch_general_phaseA<decltype(q)::value, decltype(p)>(a, g->wall, g->fast, g->gen_ids, g->ngen, s);
+        return launch_general_phaseA<decltype(q)::value, decltype(p)>(a, g->wall, g->fast, g->gen_ids, g->ngen, s,
+                                                                      overlap ? kPhaseAList : kPhaseAAll);
     }));
     if (g->nreg)
         CK(dispatch(d.Q, d.precision, [&](auto q, auto p) {
@@ -405,9 +445,9 @@ int step_grid(luma_gpu_grid *g, int subcycle, bool write_macro) {
 // so one graph serves every pair.  The signature below lists what a capture
 // bakes in (device pointers, parities, sizes, paths); any change recaptures.
 // Not used when a step carries host logic between its kernels (velocity
-// ramp: arguments change every step; moving bodies: the FSI loop reads a
-// residual on the host; a recorded adjoint), or while the caller's stream is
-// itself being captured.
+// ramp: arguments change every step; a recorded adjoint), or while the
+// caller's stream is itself being captured.  Moving bodies are captured:
+// their FSI loop runs its test on the device.
 
 namespace luma {
 struct StepGraph {
@@ -420,7 +460,7 @@ struct StepGraph {
 
 namespace {
 
-constexpr int kGraphMinSteps = 8;
+constexpr int kGraphMinSteps = 4;
 
 void tree_signature(const luma_gpu_grid *g, std::vector<uintptr_t> &s) {
     auto P = [&](const void *p) { s.push_back((uintptr_t)p); };
@@ -435,23 +475,19 @@ void tree_signature(const luma_gpu_grid *g, std::vector<uintptr_t> &s) {
         P(d.vel); P(d.eps); P(d.ds); P(d.area); P(d.F); P(d.irho); P(d.imom); P(d.moff); P(d.msite);
         P(d.smarker); P(d.mdelta); P(d.usite); P(d.uoff); P(d.uref);
         V(d.nm); V(d.nsup); V(d.nu); V(g->ibm->has_bodies); V(g->ibm->ready); V(g->ibm->has_flexible);
+        const FemDevice &fe = g->ibm->fem;
+        P(fe.U); P(fe.M); P(fe.K); P(fe.fsi_state); P(fe.flex.pos); P(fe.flex.supp); P(g->ibm->u_n);
+        V(fe.nfil); V(fe.k_in_smem); V(fe.eps_in_smem);
     }
     V((long long)g->kids.size());
     for (const luma_gpu_grid *c : g->kids) tree_signature(c, s);
 }
 
 bool graph_safe(const luma_gpu_grid *g) {
-    if (g->d.velocity_ramp > 0.0 || g->d.reynolds_ramp > 0.0 || g->adj || g->tav ||
-        (g->ibm && g->ibm->has_flexible))
-        return false;
+    if (g->d.velocity_ramp > 0.0 || g->d.reynolds_ramp > 0.0 || g->adj || g->tav) return false;
     for (const luma_gpu_grid *c : g->kids)
         if (!graph_safe(c)) return false;
     return true;
-}
-
-void tree_stream(luma_gpu_grid *g, cudaStream_t s) {
-    g->stream = s;
-    for (luma_gpu_grid *c : g->kids) tree_stream(c, s);
 }
 
 void save_clocks(const luma_gpu_grid *g, std::vector<int> &v) {
@@ -505,7 +541,7 @@ int run_step_pairs(luma_gpu_grid *root, int pairs, int *done) {
         std::vector<int> clocks;
         save_clocks(root, clocks);
         const cudaStream_t user = root->stream;
-        tree_stream(root, G.cap);
+        set_tree_stream(root, G.cap);
         int rc = LUMA_OK;
         cudaGraph_t graph = nullptr;
         if (cudaStreamBeginCapture(G.cap, cudaStreamCaptureModeThreadLocal) == cudaSuccess) {
@@ -515,7 +551,7 @@ int run_step_pairs(luma_gpu_grid *root, int pairs, int *done) {
         } else {
             rc = LUMA_E_CUDA;
         }
-        tree_stream(root, user);
+        set_tree_stream(root, user);
         if (rc == LUMA_OK && graph && cudaGraphInstantiate(&G.exec, graph, 0) != cudaSuccess) rc = LUMA_E_CUDA;
         if (graph) cudaGraphDestroy(graph);
         if (rc != LUMA_OK) {
@@ -566,6 +602,9 @@ void free_grid(luma_gpu_grid *g) {
     cudaFree(g->defer_ids);
     cudaFree(g->fast);
     cudaFree(g->gen_ids);
+    if (g->kid_stream) cudaStreamDestroy(g->kid_stream);
+    if (g->ev_fork) cudaEventDestroy(g->ev_fork);
+    if (g->ev_join) cudaEventDestroy(g->ev_join);
     delete g;
 }
 
@@ -706,6 +745,16 @@ int luma_gpu_grid_create(const luma_grid_desc *desc, luma_gpu_grid *parent, luma
     g->d.xpos = g->d.ypos = g->d.zpos = nullptr;
     g->d.ux_in = g->d.uy_in = g->d.uz_in = nullptr;
     if (parent) {
+        if (!parent->kid_stream) {
+            // the parent's sub-grids step on a stream of the highest priority
+            // beside its interior kernel (step_grid); without it they step in line
+            int least = 0, greatest = 0;
+            cudaDeviceGetStreamPriorityRange(&least, &greatest);
+            if (cudaStreamCreateWithPriority(&parent->kid_stream, cudaStreamNonBlocking, greatest) != cudaSuccess ||
+                cudaEventCreateWithFlags(&parent->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
+                cudaEventCreateWithFlags(&parent->ev_join, cudaEventDisableTiming) != cudaSuccess)
+                cudaGetLastError();
+        }
         parent->kids.push_back(g);
         if (parent->bulk) {
             // A grid with sub-grids takes the general path; it holds no state yet.
@@ -737,14 +786,9 @@ int luma_gpu_grid_destroy(luma_gpu_grid *g) {
     return LUMA_OK;
 }
 
-static void set_stream_rec(luma_gpu_grid *g, cudaStream_t s) {
-    g->stream = s;
-    for (luma_gpu_grid *c : g->kids) set_stream_rec(c, s);
-}
-
 int luma_gpu_set_stream(luma_gpu_grid *root, void *cuda_stream) {
     if (!root) return luma_set_error(LUMA_E_INVALID, "null grid");
-    set_stream_rec(root, static_cast<cudaStream_t>(cuda_stream));
+    set_tree_stream(root, static_cast<cudaStream_t>(cuda_stream));
     return LUMA_OK;
 }
 
@@ -893,6 +937,8 @@ static int take_unsupported(luma_gpu_grid *g, int *code, int *level, int *region
         CK(cudaMemsetAsync(g->unsup, 0, sizeof(int), g->stream));
         if (!*code) { *code = h; *level = g->d.level; *region = g->d.region; }
     }
+    if (g->ibm && g->ibm->has_flexible && g->ibm->ready)
+        if (int rc = luma_fem_take_error(g)) return rc;
     for (luma_gpu_grid *c : g->kids)
         if (int rc = take_unsupported(c, code, level, region)) return rc;
     return LUMA_OK;

@@ -98,6 +98,9 @@ struct StepArgs {
     // this grid's device flag: a site that needs an operation outside the
     // GPU path writes a non-zero code (read and cleared by luma_gpu_synchronize)
     int *unsupported;
+    // FSI sub-iterations: the reset-forces and IBM kernels return at once
+    // while *skip is non-zero (the loop has converged); null outside the loop
+    const int *skip;
 };
 
 // Per regularised site: inward normal, normal direction and edge count from

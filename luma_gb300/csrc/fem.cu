@@ -51,7 +51,9 @@ struct FemKernelArgs {
     const int *parent_el;
     const double *parent_zeta, *mpos0;
     int *it;
-    double *res, *fsi_res;
+    double *res, *fsi_res;      // per filament NR residual; FSI residual: [0] running max, [1] last
+    int *fsi_state;             // FSI loop of the step: [0] converged, [1] sub-iterations run
+    const int *skip;            // while *skip (the loop converged) the kernels return at once; may be null
     double dt, dh;
     FlexArgs flex;
     // grid for the support search
@@ -225,6 +227,145 @@ __device__ void lu_solve_block(double *A, int lda, int off, int n, int *ipiv, do
 #undef AC
 }
 
+// Partial-pivot LU and transposed solve of a banded matrix, the active
+// window in registers.  Same contract and the same arithmetic as
+// lu_solve_block (every matrix and solution element sees the dense serial
+// algorithm's operations in its order; exact no-ops are skipped), for a
+// matrix with no entry more than BL rows below or columns right of the
+// diagonal.  Partial pivoting then confines step k to rows k..k+BL and
+// columns k..k+2BL: lane j of warp 0 owns the column k + ((j - k) mod W) of
+// the window and holds its rows k..k+BL in registers, so a step is one
+// pivot search in registers, a broadcast of the pivot row and of the BL
+// multipliers, and a register update per lane; the finished row of U and
+// column of L go to memory and the next row of the input comes in.  Row
+// swaps reach the finished columns of L in memory (the dense algorithm
+// swaps whole rows), and `drift` bounds how far below its diagonal an L
+// entry can land through them, which bounds the backward solve.
+template <int BL>
+__device__ void band_lu_solve(double *A, int lda, int off, int n, int *ipiv, double *x) {
+#define AC(r, c) A[(size_t)(off + (c)) * lda + (off + (r))]
+    constexpr int BU = 2 * BL;        // upper bandwidth of U
+    constexpr int W = 16;             // lanes that own window columns
+    static_assert(BU + 1 <= W, "window wider than the lanes that hold it");
+    __shared__ double xs[512];
+    __shared__ int drift_s;
+    const int lane = threadIdx.x;
+    if (threadIdx.x < 32) {
+        int drift = BL;
+        double v[BL + 1];
+        int col = lane;                               // this lane's column at k = 0
+#pragma unroll
+        for (int i = 0; i <= BL; ++i) v[i] = (lane < W && i < n && col < n) ? AC(i, col) : 0.0;
+        for (int k = 0; k < n; ++k) {
+            const int lk = k % W;
+            // pivot search in column k (lane lk): first row of largest magnitude
+            int imax = 0;
+            {
+                unsigned long long best = mag_bits(v[0]);
+#pragma unroll
+                for (int i = 1; i <= BL; ++i)
+                    if (k + i < n && mag_bits(v[i]) > best) { best = mag_bits(v[i]); imax = i; }
+            }
+            imax = __shfl_sync(0xffffffffu, imax, lk);
+            double pv = 0.0;
+#pragma unroll
+            for (int i = 0; i <= BL; ++i)
+                if (i == imax) pv = v[i];
+            const bool live = !is_zero(__shfl_sync(0xffffffffu, pv, lk));
+            const int p = k + imax;
+            if (lane == 0) ipiv[k] = p + 1;
+            if (live && imax != 0) {
+                // swap rows k and p: the window in registers, the finished L
+                // columns in memory
+#pragma unroll
+                for (int i = 1; i <= BL; ++i)
+                    if (i == imax) { const double t = v[0]; v[0] = v[i]; v[i] = t; }
+                for (int c = lane; c < k; c += 32) {
+                    const double t = AC(k, c);
+                    AC(k, c) = AC(p, c);
+                    AC(p, c) = t;
+                }
+                drift += imax;
+            }
+            // multipliers of column k (lane lk), broadcast to the window
+            double m[BL];
+            if (lane == lk && live) {
+                const double inv = 1.0 / v[0];
+#pragma unroll
+                for (int i = 1; i <= BL; ++i)
+                    if (k + i < n) v[i] = v[i] * inv;
+            }
+#pragma unroll
+            for (int i = 1; i <= BL; ++i) m[i - 1] = __shfl_sync(0xffffffffu, v[i], lk);
+            // finished row k of U and column k of L to memory; rank-1 update
+            if (lane < W && col < n && col <= k + BU) {
+                AC(k, col) = v[0];
+                if (lane == lk) {
+#pragma unroll
+                    for (int i = 1; i <= BL; ++i)
+                        if (k + i < n) AC(k + i, k) = v[i];
+                } else if (live && !is_zero(v[0])) {
+#pragma unroll
+                    for (int i = 1; i <= BL; ++i)
+                        if (!is_zero(m[i - 1])) v[i] = v[i] - m[i - 1] * v[0];
+                }
+            }
+            // slide the window down a row; lane lk takes column k + W
+            if (lane == lk) {
+                col = k + W;
+#pragma unroll
+                for (int i = 0; i <= BL; ++i) v[i] = 0.0;
+            } else {
+#pragma unroll
+                for (int i = 0; i < BL; ++i) v[i] = v[i + 1];
+            }
+            const int nr = k + 1 + BL;
+            v[BL] = (lane < W && nr < n && col < n) ? AC(nr, col) : 0.0;
+        }
+        __syncwarp();
+        // forward: U^T y = b, one pending row per lane; row r subtracts its
+        // terms as the y_c arrive, in ascending c (the serial order)
+        double s = (lane < W && lane < n) ? x[lane] : 0.0;
+        for (int c = 0; c < n; ++c) {
+            const int lc = c % W;
+            const int r = c + ((lane - c % W + W) % W);  // this lane's pending row
+            double y = 0.0;
+            if (lane == lc) y = s / AC(c, c);
+            y = __shfl_sync(0xffffffffu, y, lc);
+            if (lane == lc) {
+                xs[c] = y;
+                s = c + W < n ? x[c + W] : 0.0;
+            } else if (lane < W && r < n && r <= c + BU) {
+                const double u = AC(c, r);
+                if (!is_zero(u)) s -= u * y;
+            }
+        }
+        if (lane == 0) drift_s = drift;
+        __syncwarp();
+        // backward: L^T z = y, terms in ascending c, nearest first
+        if (lane == 0) {
+            const int reach = drift < n ? drift : n;
+            for (int r = n - 1; r >= 0; --r) {
+                double t = xs[r];
+                const int cend = r + reach < n - 1 ? r + reach : n - 1;
+                for (int c = r + 1; c <= cend; ++c) {
+                    const double l = AC(c, r);
+                    if (!is_zero(l)) t -= l * xs[c];
+                }
+                xs[r] = t;
+            }
+            for (int k = n - 1; k >= 0; --k) {
+                const int q = ipiv[k] - 1;
+                if (q != k) { const double t = xs[k]; xs[k] = xs[q]; xs[q] = t; }
+            }
+        }
+        __syncwarp();
+        for (int r = lane; r < n; r += 32) x[r] = xs[r];
+    }
+    __syncthreads();
+#undef AC
+}
+
 // Element matrices of FEMElement::forceVector/massMatrix/stiffMatrix
 // (:273-302, :178-213, :218-268), in global coordinates.
 __device__ void element_matrices(const FemKernelArgs &a, int f, int e) {
@@ -334,7 +475,7 @@ __device__ double load_entry(const FemKernelArgs &a, int f, int d, double forceS
 
 __global__ void k_fem_dynamic(FemKernelArgs a) {
     const int f = blockIdx.x;
-    if (f >= a.nfil) return;
+    if (f >= a.nfil || (a.skip && *a.skip)) return;
     const int d0 = a.dof_off[f], nd = a.dof_off[f + 1] - d0;
     const int e0 = a.el_off[f], ne = a.el_off[f + 1] - e0;
     const int mk0 = a.mk_off[f], nmk = a.mk_off[f + 1] - mk0;
@@ -411,7 +552,7 @@ __global__ void k_fem_dynamic(FemKernelArgs a) {
         for (int i = threadIdx.x; i < nd; i += blockDim.x) a.delU[d0 + i] = a.Fv[d0 + i];
         __syncthreads();
         // an element couples the 6 DOFs of its two nodes: half-bandwidth 5
-        lu_solve_block(K, nd, bc, nd - bc, ipiv, a.delU + d0 + bc, 5);
+        band_lu_solve<5>(K, nd, bc, nd - bc, ipiv, a.delU + d0 + bc);
         for (int i = threadIdx.x; i < bc; i += blockDim.x) a.delU[d0 + i] = 0.0;
         __syncthreads();
         for (int i = threadIdx.x; i < nd; i += blockDim.x) a.U[d0 + i] = a.U[d0 + i] + a.delU[d0 + i];
@@ -490,7 +631,7 @@ __device__ double delta_kernel_d(double radius, double dilation) {
 // ibm_computeDs, ibm_findEpsilon for a moving body).
 __global__ void k_flex_support(FemKernelArgs a) {
     const int f = blockIdx.x;
-    if (f >= a.nfil) return;
+    if (f >= a.nfil || (a.skip && *a.skip)) return;
     const int mk0 = a.mk_off[f], nmk = a.mk_off[f + 1] - mk0;
     const int D = a.dims;
     const double dh = a.dh;
@@ -606,15 +747,26 @@ __global__ void k_flex_support(FemKernelArgs a) {
         A[(size_t)I * nmk + J] = aij * x.ds[gJ];
     }
     __shared__ int ipiv[512];
+    __shared__ int band;
+    if (threadIdx.x == 0) band = 0;
     for (int m = threadIdx.x; m < nmk; m += blockDim.x) x.eps[mk0 + m] = 1.0;
     __syncthreads();
-    lu_solve_block(A, nmk, 0, nmk, ipiv, x.eps + mk0, nmk);
+    // markers share support nodes only within a few dh of each other: along
+    // a filament the system is banded, and the band solver applies when its
+    // band holds every non-zero (else the dense one; the same arithmetic)
+    for (int q = threadIdx.x; q < nmk * nmk; q += blockDim.x) {
+        const int off = q / nmk - q % nmk;
+        if (!is_zero(A[q])) atomicMax(&band, off < 0 ? -off : off);
+    }
+    __syncthreads();
+    if (band <= 5) band_lu_solve<5>(A, nmk, 0, nmk, ipiv, x.eps + mk0);
+    else lu_solve_block(A, nmk, 0, nmk, ipiv, x.eps + mk0, nmk);
 }
 
 // max over flexible markers of |U - U_km1| / (L_UX0 dt/dh)  (ibm_checkVelDiff)
 __global__ void k_fsi_residual(FemKernelArgs a) {
     const int f = blockIdx.x;
-    if (f >= a.nfil) return;
+    if (f >= a.nfil || (a.skip && *a.skip)) return;
     const int mk0 = a.mk_off[f], nmk = a.mk_off[f + 1] - mk0;
     for (int m = threadIdx.x; m < nmk; m += blockDim.x) {
         const int g = mk0 + m;
@@ -626,6 +778,35 @@ __global__ void k_fsi_residual(FemKernelArgs a) {
         const double v = fabs(sqrt(r) / a.velscale[f]);
         atomicMax(reinterpret_cast<unsigned long long *>(a.fsi_res), (unsigned long long)__double_as_longlong(v));
     }
+}
+
+// The FSI sub-iterations of a step (ibm_subIterate, src/ObjectManager_ops_ibm.cpp:
+// 111-185) run without the host: all ten are enqueued, and after each one
+// k_fsi_decide applies the loop test (another iteration while the residual
+// is above 1e-4); once it fails, every kernel of the later iterations
+// returns at once.  Nothing waits on the flag.
+__global__ void k_fsi_begin(int *state, double *res) {
+    state[0] = 0;
+    state[1] = 0;
+    res[0] = 0.0;
+}
+__global__ void k_fsi_decide(int *state, double *res) {
+    if (state[0]) return;
+    state[1] += 1;
+    res[1] = res[0];
+    res[0] = 0.0;
+    if (!(res[1] > 1e-4)) state[0] = 1;
+}
+// u <- u_n (the velocity at the start of the step) for the next
+// sub-iteration, unless the loop has converged; 4-byte words, 16 at a time.
+__global__ void k_restore_u(const int *skip, uint32_t *__restrict__ dst, const uint32_t *__restrict__ src,
+                            size_t words) {
+    if (*skip) return;
+    const size_t nv = words / 4;
+    const size_t stride = (size_t)gridDim.x * blockDim.x;
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < nv; i += stride)
+        reinterpret_cast<uint4 *>(dst)[i] = reinterpret_cast<const uint4 *>(src)[i];
+    for (size_t i = 4 * nv + (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < words; i += stride) dst[i] = src[i];
 }
 
 __global__ void k_fem_commit(FemKernelArgs a, int ndof_total) {
@@ -650,7 +831,7 @@ FemKernelArgs make_fem_args(luma_gpu_grid *g) {
     a.R = d.R; a.Fv = d.Fv; a.delU = d.delU;
     a.M = d.M; a.K = d.K; a.epsA = d.epsA;
     a.parent_el = d.parent_el; a.parent_zeta = d.parent_zeta; a.mpos0 = d.mpos0;
-    a.it = d.it; a.res = d.res; a.fsi_res = d.fsi_res;
+    a.it = d.it; a.res = d.res; a.fsi_res = d.fsi_res; a.fsi_state = d.fsi_state;
     a.dt = g->d.dt; a.dh = g->d.dh;
     a.flex = d.flex;
     a.N = g->d.N; a.M_ = g->d.M; a.K_ = g->d.K; a.dims = g->d.dims; a.level = g->d.level;
@@ -746,7 +927,8 @@ int luma_fem_upload(luma_gpu_grid *g) {
         (rc = zeros(&d.R, ndof)) || (rc = zeros(&d.Fv, ndof)) || (rc = zeros(&d.delU, ndof)) ||
         (rc = zeros(&d.M, (size_t)d.nfil * maxdof * maxdof)) || (rc = zeros(&d.K, (size_t)d.nfil * maxdof * maxdof)) ||
         (rc = zeros(&d.epsA, (size_t)d.nfil * maxmk * maxmk)) || (rc = zeros(&d.it, d.nfil)) ||
-        (rc = zeros(&d.res, d.nfil)) || (rc = zeros(&d.fsi_res, 1)))
+        (rc = zeros(&d.res, d.nfil)) || (rc = zeros(&d.fsi_res, 2)) ||
+        (rc = zeros(&d.fsi_state, 2)))
         return rc;
     FlexArgs &x = d.flex;
     x.nm = nmk;
@@ -766,6 +948,13 @@ int luma_fem_upload(luma_gpu_grid *g) {
         (rc = up(&sc.hz, g->hz)) || (rc = zeros(&sc.error, 1)))
         return rc;
     g_scratch.push_back({g, sc});
+    // a filament's stiffness and epsilon matrices in shared memory when they fit
+    const size_t kb = (size_t)maxdof * maxdof * sizeof(double), eb = (size_t)maxmk * maxmk * sizeof(double);
+    d.k_in_smem = kb <= kFemSmemMax &&
+                  cudaFuncSetAttribute(k_fem_dynamic, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kb) == cudaSuccess;
+    d.eps_in_smem = eb <= kFemSmemMax &&
+                    cudaFuncSetAttribute(k_flex_support, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)eb) == cudaSuccess;
+    cudaGetLastError();
     st.u_n = nullptr;
     const size_t rs = g->d.precision == LUMA_PREC_FP64 ? 8 : 4;
     if (cudaMalloc(&st.u_n, g->n * g->d.dims * rs) != cudaSuccess)
@@ -790,12 +979,12 @@ static FemKernelArgs full_args(luma_gpu_grid *g) {
 }
 
 // Supports/ds/epsilon of the filaments' markers (initialise and after FEM).
-int luma_fem_supports(luma_gpu_grid *g) {
+int luma_fem_supports(luma_gpu_grid *g, const int *skip) {
     FemKernelArgs a = full_args(g);
+    a.skip = skip;
+    const FemDevice &d = g->ibm->fem;
+    a.eps_in_smem = d.eps_in_smem;
     const size_t eb = (size_t)a.maxmk * a.maxmk * sizeof(double);
-    a.eps_in_smem = eb <= kFemSmemMax &&
-                    cudaFuncSetAttribute(k_flex_support, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)eb) == cudaSuccess;
-    if (!a.eps_in_smem) cudaGetLastError();
     k_flex_support<<<a.nfil, 128, a.eps_in_smem ? eb : 0, g->stream>>>(a);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return luma_set_error(LUMA_E_CUDA, "flex support: %s", cudaGetErrorString(e));
@@ -803,30 +992,61 @@ int luma_fem_supports(luma_gpu_grid *g) {
 }
 
 // ObjectManager::ibm_moveBodies (:61-104) for the filaments of a grid.
-int luma_fem_move_bodies(luma_gpu_grid *g) {
+int luma_fem_move_bodies(luma_gpu_grid *g, const int *skip) {
     FemKernelArgs a = full_args(g);
-    // the stiffness matrix of a filament in shared memory when it fits
+    a.skip = skip;
+    a.k_in_smem = g->ibm->fem.k_in_smem;
     const size_t kb = (size_t)a.maxdof * a.maxdof * sizeof(double);
-    a.k_in_smem = kb <= kFemSmemMax &&
-                  cudaFuncSetAttribute(k_fem_dynamic, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kb) == cudaSuccess;
-    if (!a.k_in_smem) cudaGetLastError();
     k_fem_dynamic<<<a.nfil, 128, a.k_in_smem ? kb : 0, g->stream>>>(a);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return luma_set_error(LUMA_E_CUDA, "FEM: %s", cudaGetErrorString(e));
-    return luma_fem_supports(g);
+    return luma_fem_supports(g, skip);
 }
 
-int luma_fem_residual(luma_gpu_grid *g, double *res) {
-    FemKernelArgs a = full_args(g);
-    cudaMemsetAsync(a.fsi_res, 0, sizeof(double), g->stream);
-    k_fsi_residual<<<a.nfil, 128, 0, g->stream>>>(a);
-    int err = 0;
-    cudaMemcpyAsync(res, a.fsi_res, sizeof(double), cudaMemcpyDeviceToHost, g->stream);
-    cudaMemcpyAsync(&err, a.error, sizeof(int), cudaMemcpyDeviceToHost, g->stream);
-    cudaError_t e = cudaStreamSynchronize(g->stream);
-    if (e != cudaSuccess) return luma_set_error(LUMA_E_CUDA, "FSI residual: %s", cudaGetErrorString(e));
-    if (err) return luma_set_error(LUMA_E_DOMAIN, "a filament marker left its grid (code %d)", err);
+const int *luma_fem_fsi_flag(luma_gpu_grid *g) { return g->ibm->fem.fsi_state; }
+
+int luma_fem_fsi_begin(luma_gpu_grid *g) {
+    FemDevice &d = g->ibm->fem;
+    k_fsi_begin<<<1, 1, 0, g->stream>>>(d.fsi_state, d.fsi_res);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return luma_set_error(LUMA_E_CUDA, "FSI begin: %s", cudaGetErrorString(e));
     return LUMA_OK;
+}
+
+int luma_fem_restore_u(luma_gpu_grid *g) {
+    const size_t bytes = g->n * g->d.dims * (g->d.precision == LUMA_PREC_FP64 ? 8 : 4);
+    k_restore_u<<<152 * 4, 256, 0, g->stream>>>(g->ibm->fem.fsi_state, static_cast<uint32_t *>(g->u),
+                                                 reinterpret_cast<const uint32_t *>(g->ibm->u_n), bytes / 4);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return luma_set_error(LUMA_E_CUDA, "FSI u restore: %s", cudaGetErrorString(e));
+    return LUMA_OK;
+}
+
+// The loop test of one sub-iteration (ibm_checkVelDiff, :988-1032, then
+// the while condition of ibm_subIterate), on the device.
+int luma_fem_fsi_check(luma_gpu_grid *g) {
+    FemKernelArgs a = full_args(g);
+    a.skip = a.fsi_state;
+    k_fsi_residual<<<a.nfil, 128, 0, g->stream>>>(a);
+    k_fsi_decide<<<1, 1, 0, g->stream>>>(a.fsi_state, a.fsi_res);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return luma_set_error(LUMA_E_CUDA, "FSI residual: %s", cudaGetErrorString(e));
+    return LUMA_OK;
+}
+
+// A filament marker that left its grid (or overflowed its support slots)
+// since the last check: reads and clears the record (blocks on the stream).
+int luma_fem_take_error(luma_gpu_grid *g) {
+    FemScratch *sc = scratch_of(g);
+    if (!sc) return LUMA_OK;
+    int err = 0;
+    cudaError_t e = cudaMemcpyAsync(&err, sc->error, sizeof(int), cudaMemcpyDeviceToHost, g->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(g->stream);
+    if (e != cudaSuccess) return luma_set_error(LUMA_E_CUDA, "FEM error read: %s", cudaGetErrorString(e));
+    if (!err) return LUMA_OK;
+    cudaMemsetAsync(sc->error, 0, sizeof(int), g->stream);
+    return luma_set_error(LUMA_E_DOMAIN, "grid L%d R%d: a filament marker left its grid (code %d)", g->d.level,
+                          g->d.region, err);
 }
 
 int luma_fem_commit(luma_gpu_grid *g) {
@@ -854,7 +1074,7 @@ void luma_fem_free(luma_gpu_grid *g) {
     void *ptrs[] = {d.node_off, d.el_off, d.dof_off, d.mk_off, d.bc, d.dm, d.velscale, d.pos0, d.ang0, d.len0,
                     d.area, d.I, d.E, d.rho, d.child_off, d.child_node, d.child_z1, d.child_z2, d.U, d.U_n, d.Ud,
                     d.Ud_n, d.Udd, d.Udd_n, d.R, d.Fv, d.delU, d.M, d.K, d.epsA, d.parent_el, d.parent_zeta,
-                    d.mpos0, d.it, d.res, d.fsi_res, d.flex.pos, d.flex.vel, d.flex.vel_km1, d.flex.F, d.flex.eps,
+                    d.mpos0, d.it, d.res, d.fsi_res, d.fsi_state, d.flex.pos, d.flex.vel, d.flex.vel_km1, d.flex.F, d.flex.eps,
                     d.flex.ds, d.flex.irho, d.flex.imom, d.flex.nsupp, d.flex.supp, d.flex.delta, d.flex.sx,
                     d.flex.sy, d.flex.sz, g->ibm->u_n};
     for (void *p : ptrs) cudaFree(p);

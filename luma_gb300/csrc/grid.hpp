@@ -56,6 +56,10 @@ struct luma_gpu_grid {
     luma_gpu_grid *parent = nullptr;
     std::vector<luma_gpu_grid *> kids;
     cudaStream_t stream = nullptr;
+    // grids with sub-grids: the sub-grids' steps run on kid_stream (high
+    // priority) beside this grid's interior kernel; fork/join events
+    cudaStream_t kid_stream = nullptr;
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     luma::IbmState *ibm = nullptr;
     luma::AdjState *adj = nullptr;   // discrete-adjoint tape (adjoint.cu)
     luma::StepGraph *graph = nullptr;  // level 0: two steps of the tree as a CUDA graph (capi.cu)
@@ -87,9 +91,13 @@ void luma_bfl_signature(const luma_gpu_grid *g, std::vector<uintptr_t> &sig);
 void luma_io_free(luma_gpu_grid *g);
 // fem.cu
 int luma_fem_upload(luma_gpu_grid *g);
-int luma_fem_supports(luma_gpu_grid *g);
-int luma_fem_move_bodies(luma_gpu_grid *g);
-int luma_fem_residual(luma_gpu_grid *g, double *res);
+int luma_fem_supports(luma_gpu_grid *g, const int *skip);
+int luma_fem_move_bodies(luma_gpu_grid *g, const int *skip);
+const int *luma_fem_fsi_flag(luma_gpu_grid *g);
+int luma_fem_fsi_begin(luma_gpu_grid *g);
+int luma_fem_restore_u(luma_gpu_grid *g);
+int luma_fem_fsi_check(luma_gpu_grid *g);
+int luma_fem_take_error(luma_gpu_grid *g);
 int luma_fem_commit(luma_gpu_grid *g);
 void luma_fem_free(luma_gpu_grid *g);
 
@@ -151,7 +159,9 @@ struct FemDevice {
     double *parent_zeta = nullptr, *mpos0 = nullptr;
     // outputs
     int *it = nullptr;
-    double *res = nullptr, *fsi_res = nullptr;
+    double *res = nullptr, *fsi_res = nullptr;  // FSI residual: [0] running max, [1] last
+    int *fsi_state = nullptr;                   // FSI loop of the step: [0] converged, [1] iterations
+    int k_in_smem = 0, eps_in_smem = 0;         // the filament matrices fit in shared memory
     // flexible IB marker arrays
     FlexArgs flex{};
 };
@@ -177,8 +187,6 @@ struct IbmState {
     std::vector<int> flex_body;      // IB body index of each filament
     FemDevice fem;
     double *u_n = nullptr;           // start-of-step velocity (R*), for FSI resets
-    int fsi_iterations = 0;
-    double fsi_residual = 0;
 };
 
 // Marker-side arguments of the IBM kernels.

@@ -328,7 +328,8 @@ int init_tree(luma_gpu_grid *g) {
         if (rc) return rc;
         if (st.has_flexible) {
             if ((rc = luma_fem_upload(g))) return rc;
-            if ((rc = luma_fem_supports(g))) return rc;
+            if ((rc = luma_fem_supports(g, nullptr))) return rc;
+            if ((rc = luma_fem_take_error(g))) return rc;
         }
         st.ready = true;
         if ((rc = luma_update_defer(g))) return rc;
@@ -367,7 +368,11 @@ static int ibm_pass(luma_gpu_grid *g, const StepArgs &a) {
 // and the FSI sub-iterations (:111-185): u_n, the start-of-step velocity,
 // was saved by the caller's first loop; each sub-iteration restores it,
 // resets the forces, re-runs the pass and the FEM, and checks the marker
-// velocity change against 1e-4 (at most 10 iterations).
+// velocity change against 1e-4 (at most 10 iterations).  All ten
+// sub-iterations are enqueued; the device-side loop test makes the ones
+// after convergence return at once, so the host never waits in the loop.
+constexpr int kFsiMaxIterations = 10;
+
 int luma_ibm_apply(luma_gpu_grid *g, const StepArgs &a) {
     IbmState &st = *g->ibm;
     if (!st.ready) return luma_set_error(LUMA_E_STATE, "luma_gpu_ibm_initialise was not called");
@@ -377,20 +382,17 @@ int luma_ibm_apply(luma_gpu_grid *g, const StepArgs &a) {
         return luma_set_error(LUMA_E_CUDA, "u_n copy failed");
     if ((rc = ibm_pass(g, a))) return rc;
     if (!st.has_flexible) return LUMA_OK;
-    if ((rc = luma_fem_move_bodies(g))) return rc;
-    double res = 0.0;
-    int it = 0;
-    do {
-        if (cudaMemcpyAsync(g->u, st.u_n, ubytes, cudaMemcpyDeviceToDevice, g->stream) != cudaSuccess)
-            return luma_set_error(LUMA_E_CUDA, "u reset failed");
-        if ((rc = luma_ibm_reset_forces(g, a))) return rc;
-        if ((rc = ibm_pass(g, a))) return rc;
-        if ((rc = luma_fem_move_bodies(g))) return rc;
-        if ((rc = luma_fem_residual(g, &res))) return rc;
-        it++;
-    } while (res > 1e-4 && it < 10);
-    st.fsi_iterations = it;
-    st.fsi_residual = res;
+    if ((rc = luma_fem_move_bodies(g, nullptr))) return rc;
+    if ((rc = luma_fem_fsi_begin(g))) return rc;
+    StepArgs b = a;
+    b.skip = luma_fem_fsi_flag(g);
+    for (int it = 0; it < kFsiMaxIterations; ++it) {
+        if ((rc = luma_fem_restore_u(g))) return rc;
+        if ((rc = luma_ibm_reset_forces(g, b))) return rc;
+        if ((rc = ibm_pass(g, b))) return rc;
+        if ((rc = luma_fem_move_bodies(g, b.skip))) return rc;
+        if ((rc = luma_fem_fsi_check(g))) return rc;
+    }
     return luma_fem_commit(g);
 }
 

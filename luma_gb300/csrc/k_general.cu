@@ -733,6 +733,7 @@ __global__ void __launch_bounds__(128) k_force_collide_list(StepArgs a, const in
 // marker, FP64 marker arithmetic in the reference's order.
 template <int Q, class P>
 __global__ void k_ibm_interp_force(StepArgs a, IbmArgs b) {
+    if (a.skip && *a.skip) return;  // a converged FSI loop: later sub-iterations do nothing
     constexpr int D = Lattice<Q>::D;
     const int m = blockIdx.x * blockDim.x + threadIdx.x;
     if (m >= b.nm) return;
@@ -762,6 +763,7 @@ __global__ void k_ibm_interp_force(StepArgs a, IbmArgs b) {
 // (body, marker, support) order, so no atomics and a deterministic sum.
 template <int Q, class P>
 __global__ void k_ibm_spread(StepArgs a, IbmArgs b) {
+    if (a.skip && *a.skip) return;  // a converged FSI loop: later sub-iterations do nothing
     constexpr int D = Lattice<Q>::D;
     const int u = blockIdx.x * blockDim.x + threadIdx.x;
     if (u >= b.nu) return;
@@ -785,6 +787,7 @@ __global__ void k_ibm_spread(StepArgs a, IbmArgs b) {
 // support site, now with the spread force.
 template <int Q, class P>
 __global__ void k_ibm_remacro(StepArgs a, IbmArgs b) {
+    if (a.skip && *a.skip) return;  // a converged FSI loop: later sub-iterations do nothing
     using R = typename P::R;
     const int u = blockIdx.x * blockDim.x + threadIdx.x;
     if (u >= b.nu) return;
@@ -806,6 +809,7 @@ __global__ void k_ibm_remacro(StepArgs a, IbmArgs b) {
 // components keep their values, as in the reference).
 template <class P>
 __global__ void k_reset_forces(StepArgs a, int dims, double gravity, int gdir, double rr) {
+    if (a.skip && *a.skip) return;  // a converged FSI loop: later sub-iterations do nothing
     const size_t id = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (id >= (size_t)a.ncell) return;
     const size_t n = (size_t)a.ncell;
@@ -821,6 +825,7 @@ __global__ void k_reset_forces(StepArgs a, int dims, double gravity, int gdir, d
 
 template <int Q, class P>
 __global__ void k_flex_interp_force(StepArgs a, FlexArgs f) {
+    if (a.skip && *a.skip) return;  // a converged FSI loop: later sub-iterations do nothing
     constexpr int D = Lattice<Q>::D;
     const int m = blockIdx.x * blockDim.x + threadIdx.x;
     if (m >= f.nm) return;
@@ -845,6 +850,7 @@ __global__ void k_flex_interp_force(StepArgs a, FlexArgs f) {
 // reference's serial loop at the level of FP64 rounding).
 template <int Q, class P>
 __global__ void k_flex_spread(StepArgs a, FlexArgs f) {
+    if (a.skip && *a.skip) return;  // a converged FSI loop: later sub-iterations do nothing
     constexpr int D = Lattice<Q>::D;
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     const int m = t / kFlexMaxSupp, s = t % kFlexMaxSupp;
@@ -861,6 +867,7 @@ __global__ void k_flex_spread(StepArgs a, FlexArgs f) {
 
 template <int Q, class P>
 __global__ void k_flex_remacro(StepArgs a, FlexArgs f) {
+    if (a.skip && *a.skip) return;  // a converged FSI loop: later sub-iterations do nothing
     using R = typename P::R;
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     const int m = t / kFlexMaxSupp, s = t % kFlexMaxSupp;
@@ -898,7 +905,7 @@ cudaError_t launch_reset_forces(const StepArgs &a, int dims, double gravity, int
 
 template <int Q, class P>
 cudaError_t launch_general_phaseA(const StepArgs &a, const int8_t *wall, const uint8_t *fast, const int *gen_ids,
-                                  int ngen, cudaStream_t s) {
+                                  int ngen, cudaStream_t s, int part) {
     const int bs = 128;
     const bool tav = a.tav_rho != nullptr;
     if (!fast) {
@@ -909,10 +916,13 @@ cudaError_t launch_general_phaseA(const StepArgs &a, const int8_t *wall, const u
     const int nb = (a.ncell + bs - 1) / bs;
     auto interior = [&](auto tv) {
         constexpr bool T = decltype(tv)::value;
-        if (a.collision == LUMA_COLL_KBC) k_interior<Q, P, LUMA_COLL_KBC, T><<<nb, bs, 0, s>>>(a, fast);
-        else if (a.collision == LUMA_COLL_BGK_SMAG) k_interior<Q, P, LUMA_COLL_BGK_SMAG, T><<<nb, bs, 0, s>>>(a, fast);
-        else k_interior<Q, P, LUMA_COLL_BGK, T><<<nb, bs, 0, s>>>(a, fast);
-        if (ngen > 0) k_stream_macro_list<Q, P, T><<<(ngen + bs - 1) / bs, bs, 0, s>>>(a, wall, gen_ids, ngen);
+        if (part != kPhaseAList) {
+            if (a.collision == LUMA_COLL_KBC) k_interior<Q, P, LUMA_COLL_KBC, T><<<nb, bs, 0, s>>>(a, fast);
+            else if (a.collision == LUMA_COLL_BGK_SMAG) k_interior<Q, P, LUMA_COLL_BGK_SMAG, T><<<nb, bs, 0, s>>>(a, fast);
+            else k_interior<Q, P, LUMA_COLL_BGK, T><<<nb, bs, 0, s>>>(a, fast);
+        }
+        if (part != kPhaseAInterior && ngen > 0)
+            k_stream_macro_list<Q, P, T><<<(ngen + bs - 1) / bs, bs, 0, s>>>(a, wall, gen_ids, ngen);
     };
     if (tav) interior(std::true_type{});
     else interior(std::false_type{});
@@ -945,7 +955,7 @@ cudaError_t launch_general_phaseC(const StepArgs &a, const int *ids, int nids, c
 
 #define LUMA_INST(Q, P)                                                                                        \
     template cudaError_t launch_general_phaseA<Q, P>(const StepArgs &, const int8_t *, const uint8_t *, const int *, \
-                                                     int, cudaStream_t);                                       \
+                                                     int, cudaStream_t, int);                                  \
     template cudaError_t launch_general_phaseB<Q, P>(const StepArgs &, const int8_t *, const RegSite *, int,   \
                                                      cudaStream_t);                                            \
     template cudaError_t launch_general_phaseC<Q, P>(const StepArgs &, const int *, int, cudaStream_t);

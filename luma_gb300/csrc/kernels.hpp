@@ -8,9 +8,12 @@
 namespace luma {
 
 // k_general.cu
+// Phase A of a split grid launches the interior kernel and the list kernel
+// of the other streamed sites; `part` selects both or one of them.
+enum { kPhaseAAll = 0, kPhaseAInterior = 1, kPhaseAList = 2 };
 template <int Q, class P>
 cudaError_t launch_general_phaseA(const StepArgs &a, const int8_t *wall, const uint8_t *fast, const int *gen_ids,
-                                  int ngen, cudaStream_t s);
+                                  int ngen, cudaStream_t s, int part = kPhaseAAll);
 template <int Q, class P>
 cudaError_t launch_general_phaseB(const StepArgs &a, const int8_t *wall, const RegSite *sites, int nsites,
                                   cudaStream_t s);
