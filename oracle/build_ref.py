@@ -45,22 +45,39 @@ def _compile(args):
     src, obj, flags = args
     if os.path.exists(obj) and os.path.getmtime(obj) >= os.path.getmtime(src):
         return None
-    cmd = ["g++", *flags, "-c", src, "-o", obj]
+    cmd = ["gcc" if src.endswith(".c") else "g++", *flags, "-c", src, "-o", obj]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         return f"{' '.join(cmd)}\n{r.stderr[-4000:]}"
     return None
 
 
-def build_case(case: str, ref: str = DEFAULT_REF, jobs: int | None = None) -> str:
-    """Build ``oracle/_ref/<case>/luma_ref``; return the binary path."""
+ROOT = os.path.dirname(HERE)
+SHIM_DIR = os.path.join(ROOT, "luma_gb300", "shim")
+GPU_LIB_DIR = os.path.join(ROOT, "luma_gb300", "_build")
+SHIM_BACKENDS = ("oracle", "gpu")
+
+
+def build_case(case: str, ref: str = DEFAULT_REF, jobs: int | None = None, shim: str | None = None) -> str:
+    """Build ``oracle/_ref/<case>/luma_ref``; return the binary path.
+
+    With ``shim`` the harness is built with the LUMA-side shim
+    (``luma_gb300/shim/gridobj_gpu.cpp``, compiled against the reference's
+    own headers) into ``oracle/_ref/<case>_shim_<shim>/``: ``"gpu"`` links
+    ``libluma_gpu.so`` (the drop-in as a maintainer builds it), ``"oracle"``
+    links the shim's ABI calls to the oracle (``abi_on_oracle.c``) so the
+    shim runs on the host."""
     src_dir = os.path.join(ref, "src")
-    out = os.path.join(OUT_ROOT, case)
+    out = os.path.join(OUT_ROOT, case if shim is None else f"{case}_shim_{shim}")
     os.makedirs(out, exist_ok=True)
     header = os.path.join(CASES_DIR, case + ".h")
     flags = ["-O2", "-std=c++11", "-w", "-ffp-contract=off",
              "-I", os.path.join(HERE, "shim"), "-I", CASES_DIR, "-I", src_dir,
              "-include", header, "-include", os.path.join(HERE, "ref_prefix.h")]
+    if shim is not None:
+        if shim not in SHIM_BACKENDS:
+            raise ValueError(f"shim backend {shim!r} not in {SHIM_BACKENDS}")
+        flags = flags + ["-DLUMA_HARNESS_SHIM", "-I", SHIM_DIR, "-I", os.path.join(ref, "inc")]
     units = []
     for f in sorted(os.listdir(src_dir)):
         if not f.endswith(".cpp") or f.startswith(EXCLUDE_PREFIX):
@@ -68,10 +85,20 @@ def build_case(case: str, ref: str = DEFAULT_REF, jobs: int | None = None) -> st
         units.append((os.path.join(src_dir, f), os.path.join(out, f[:-4] + ".o"), flags))
     for f in ("ref_stubs.cpp", "ref_harness.cpp"):
         units.append((os.path.join(HERE, f), os.path.join(out, f[:-4] + ".o"), flags))
+    extra_deps = []
+    if shim is not None:
+        units.append((os.path.join(SHIM_DIR, "gridobj_gpu.cpp"), os.path.join(out, "gridobj_gpu.o"), flags))
+        extra_deps = [os.path.join(SHIM_DIR, "gridobj_gpu.cpp"), os.path.join(SHIM_DIR, "gridobj_gpu.h"),
+                      os.path.join(ROOT, "include", "luma_gpu.h")]
+        if shim == "oracle":
+            cflags = ["-O2", "-std=c11", "-w", "-ffp-contract=off", "-fopenmp"]
+            for f in ("abi_on_oracle.c", "lbm_oracle.c"):
+                units.append((os.path.join(HERE, f), os.path.join(out, f[:-2] + ".o"), cflags))
+                extra_deps.append(os.path.join(HERE, f))
     # A changed case header or harness invalidates every object of the case.
     stamp = os.path.join(out, ".stamp")
     deps = [header, os.path.join(CASES_DIR, "luma_case_tail.h"), os.path.join(HERE, "ref_prefix.h"),
-            os.path.join(HERE, "ref_stubs.cpp"), os.path.join(HERE, "ref_harness.cpp")]
+            os.path.join(HERE, "ref_stubs.cpp"), os.path.join(HERE, "ref_harness.cpp"), *extra_deps]
     newest = max(os.path.getmtime(d) for d in deps)
     if not os.path.exists(stamp) or os.path.getmtime(stamp) < newest:
         for _, obj, _ in units:
@@ -82,7 +109,12 @@ def build_case(case: str, ref: str = DEFAULT_REF, jobs: int | None = None) -> st
     if errs:
         raise RuntimeError("oracle reference build failed:\n" + "\n".join(errs))
     exe = os.path.join(out, "luma_ref")
-    r = subprocess.run(["g++", "-o", exe, *[u[1] for u in units]], capture_output=True, text=True)
+    libs = []
+    if shim == "oracle":
+        libs = ["-fopenmp", "-lm"]
+    elif shim == "gpu":
+        libs = ["-L", GPU_LIB_DIR, "-lluma_gpu", f"-Wl,-rpath,{GPU_LIB_DIR}"]
+    r = subprocess.run(["g++", "-o", exe, *[u[1] for u in units], *libs], capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError("oracle reference link failed:\n" + r.stderr[-4000:])
     with open(stamp, "w") as fp:

@@ -38,6 +38,12 @@
  * With --drag-out nothing is dumped; FILE gets the time average over the N
  * steps of body 0's lattice-unit drag and N.
  *
+ * Builds with the LUMA-side shim (LUMA_HARNESS_SHIM, luma_gb300/shim/)
+ * take --gpu-shim PREC: after the initialisation the shim builds the
+ * device twin of the grid tree (LUMA_PREC_* PREC) and hands over the IB
+ * bodies, each step is the shim's LBM_multi_opt, and every dump first
+ * brings the state back into the GridObj tree through the shim.
+ *
  * Output, per dump step s and grid (level l, region r):
  *   DIR/s<s>/L<l>R<r>_meta.txt   key value lines (sizes, omega, dt, dh, t, limits)
  *   DIR/s<s>/L<l>R<r>_<name>.bin f, u, rho, typ (int32), force (if allocated),
@@ -59,6 +65,10 @@
 #include "../inc/GridManager.h"
 #include "../inc/ObjectManager.h"
 #include "../inc/IBBody.h"
+#ifdef LUMA_HARNESS_SHIM
+#include "../include/luma_gpu.h"
+#include "gridobj_gpu.h"
+#endif
 
 static void write_raw(const std::string &path, const void *data, size_t bytes) {
     FILE *fp = std::fopen(path.c_str(), "wb");
@@ -241,6 +251,7 @@ int main(int argc, char **argv) {
     std::string out = ".", init_u, init_rho, workdir, markers, drag_out, momex_out, bfl_out, bfl_forces;
     int steps = 0, dump_every = 0, io_at = -1;
     bool restart_read = false;
+    int shim_prec = -1;
     for (int a = 1; a < argc; ++a) {
         std::string k = argv[a];
         auto next = [&]() -> std::string {
@@ -260,6 +271,7 @@ int main(int argc, char **argv) {
         else if (k == "--bfl-forces") bfl_forces = next();
         else if (k == "--io-at") io_at = std::atoi(next().c_str());
         else if (k == "--restart-read") restart_read = true;
+        else if (k == "--gpu-shim") shim_prec = std::atoi(next().c_str());
         else { std::fprintf(stderr, "unknown argument %s\n", k.c_str()); return 2; }
     }
     mkdir(out.c_str(), 0755);
@@ -319,11 +331,27 @@ int main(int argc, char **argv) {
         om->bbbOnGridReg = 0;
     }
 #endif
+#ifdef LUMA_HARNESS_SHIM
+    if (shim_prec >= 0 && LumaGpuShim::create(grids, shim_prec) != 0) {
+        std::fprintf(stderr, "shim create failed: %s\n", luma_gpu_last_error_string());
+        return 3;
+    }
+    auto step_once = [&]() {
+        if (shim_prec < 0) { grids->LBM_multi_opt(); return; }
+        if (LumaGpuShim::step(grids, 1) != 0 || LumaGpuShim::sync_to_host(grids) != 0) {
+            std::fprintf(stderr, "shim step failed: %s\n", luma_gpu_last_error_string());
+            std::exit(3);
+        }
+    };
+#else
+    if (shim_prec >= 0) { std::fprintf(stderr, "--gpu-shim needs a build with the shim\n"); return 2; }
+    auto step_once = [&]() { grids->LBM_multi_opt(); };
+#endif
     if (drag_out.empty()) dump_all(grids, out, 0);
     double drag_sum = 0.0;
     auto t0 = std::chrono::steady_clock::now();
     for (int s = 1; s <= steps; ++s) {
-        grids->LBM_multi_opt();
+        step_once();
 #ifdef L_LD_OUT
         if (mf)
             std::fprintf(mf, "%d %.17g %.17g %.17g\n", s, om->bbbForceOnObjectX, om->bbbForceOnObjectY,
