@@ -655,15 +655,30 @@ def run_ours(args, rank: int, world: int, local_rank: int):
     check(L.luma_gpu_step(C.c_void_p(g32.h), K))
     check(L.luma_gpu_download_state(C.c_void_p(g32.h), None, ptr(out_u), ptr(out_r), None))
     barrier()
-    t_e0 = time.perf_counter()
-    check(L.luma_gpu_upload_state(C.c_void_p(g32.h), ptr(hf), ptr(hu), ptr(hr), None, 0))
-    check(L.luma_gpu_step(C.c_void_p(g32.h), K))
-    check(L.luma_gpu_download_state(C.c_void_p(g32.h), None, ptr(out_u), ptr(out_r), None))
-    barrier()
-    sec_e2e = max_over_ranks_(time.perf_counter() - t_e0)
+    runs = []
+    for _ in range(3):   # the whole-call time varies with the host link; the median is reported
+        t_e0 = time.perf_counter()
+        check(L.luma_gpu_upload_state(C.c_void_p(g32.h), ptr(hf), ptr(hu), ptr(hr), None, 0))
+        check(L.luma_gpu_step(C.c_void_p(g32.h), K))
+        check(L.luma_gpu_download_state(C.c_void_p(g32.h), None, ptr(out_u), ptr(out_r), None))
+        barrier()
+        runs.append(max_over_ranks_(time.perf_counter() - t_e0))
+    sec_e2e = sorted(runs)[1]
     e2e = replica_mlups(world, ncell, K, sec_e2e)
     h2d = (f0.nbytes + l0.u.nbytes + l0.rho.nbytes) / K
     d2h = (out_u.numel() + out_r.numel()) * 8 / K
+    # one more call, its phases timed apart (each call blocks or is followed by a sync)
+    t_a = time.perf_counter()
+    check(L.luma_gpu_upload_state(C.c_void_p(g32.h), ptr(hf), ptr(hu), ptr(hr), None, 0))
+    t_b = time.perf_counter()
+    check(L.luma_gpu_step(C.c_void_p(g32.h), K))
+    check(L.luma_gpu_synchronize(C.c_void_p(g32.h)))
+    t_c = time.perf_counter()
+    check(L.luma_gpu_download_state(C.c_void_p(g32.h), None, ptr(out_u), ptr(out_r), None))
+    t_d = time.perf_counter()
+    e2e_phases = {"upload_s": round(t_b - t_a, 5), "steps_s": round(t_c - t_b, 5), "download_s": round(t_d - t_c, 5),
+                  "upload_gbs": round((f0.nbytes + l0.u.nbytes + l0.rho.nbytes) / (t_b - t_a) / 1e9, 1),
+                  "download_gbs": round((out_u.numel() + out_r.numel()) * 8 / (t_d - t_c) / 1e9, 1)}
     g32.close()
 
     # ---- roofline ----
@@ -707,8 +722,10 @@ def run_ours(args, rank: int, world: int, local_rank: int):
             "clocks": sampler_summary,
             "e2e": {"value": round(e2e, 2), "unit": "MLUPS", "h2d_bytes_per_step": int(h2d),
                     "d2h_bytes_per_step": int(d2h),
-                    "note": "C ABI with pinned host buffers: upload of FP64 reference-layout state, K steps, "
-                            "download of u and rho"},
+                    "note": "C ABI with pinned host buffers (read and written in place by the layout "
+                            "conversions): upload of FP64 reference-layout state, K steps, download of u and "
+                            "rho; median of 3 timed calls",
+                    "calls_s": [round(x, 5) for x in runs], "phases": e2e_phases},
             "gpu_launches": K,
             "roofline": {"bound": "hbm", "achieved": round(ach32, 1), "peak": peaks["hbm_gbs"], "unit": "GB/s",
                          "frac": round(ach32 / peaks["hbm_gbs"], 4), "traffic": traffic,

@@ -21,7 +21,7 @@ BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD, "libluma_gpu.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 # Units whose FP64 operation sequence must be the reference's (no FMA contraction).
-FMAD_OFF = {"fem.cu"}
+FMAD_OFF = {"fem.cu", "epsilon.cu"}
 # Units compiled once per variant (object suffix, defines): the general-path
 # kernels instantiate per lattice and precision, six objects in parallel.
 VARIANTS = {

@@ -552,7 +552,11 @@ int run_step_pairs(luma_gpu_grid *root, int pairs, int *done) {
             rc = LUMA_E_CUDA;
         }
         set_tree_stream(root, user);
-        if (rc == LUMA_OK && graph && cudaGraphInstantiate(&G.exec, graph, 0) != cudaSuccess) rc = LUMA_E_CUDA;
+        // node priorities as captured: the sub-grids' chain (high-priority
+        // stream) is scheduled ahead of the parent's interior blocks
+        if (rc == LUMA_OK && graph &&
+            cudaGraphInstantiate(&G.exec, graph, cudaGraphInstantiateFlagUseNodePriority) != cudaSuccess)
+            rc = LUMA_E_CUDA;
         if (graph) cudaGraphDestroy(graph);
         if (rc != LUMA_OK) {
             // nothing ran: put the host-side clocks back and step directly
@@ -792,42 +796,94 @@ int luma_gpu_set_stream(luma_gpu_grid *root, void *cuda_stream) {
     return LUMA_OK;
 }
 
+}  // extern "C"
+
+namespace {
+
+// The device address of a host array the GPU can reach in place (pinned,
+// mapped host memory), or null: the layout conversions read and write such
+// arrays directly; anything else goes through a device staging buffer.
+template <class T>
+T *device_view(T *h) {
+    if (!h) return nullptr;
+    cudaPointerAttributes at;
+    if (cudaPointerGetAttributes(&at, h) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    return at.type == cudaMemoryTypeHost && at.devicePointer ? static_cast<T *>(at.devicePointer) : nullptr;
+}
+
+// A device staging buffer for the host arrays of one transfer, allocated on
+// first need on the stream and freed with it.
+struct Stage {
+    double *p = nullptr;
+    size_t n = 0;
+    cudaStream_t s;
+    explicit Stage(size_t count, cudaStream_t st) : n(count), s(st) {}
+    cudaError_t get(double **out) {
+        if (!p) {
+            cudaError_t e = cudaMallocAsync(&p, n * sizeof(double), s);
+            if (e != cudaSuccess) return e;
+        }
+        *out = p;
+        return cudaSuccess;
+    }
+    ~Stage() {
+        if (p) cudaFreeAsync(p, s);
+    }
+};
+
+}  // namespace
+
+extern "C" {
+
 int luma_gpu_upload_state(luma_gpu_grid *g, const double *f, const double *u, const double *rho,
                           const double *force_xyz, int t) {
     if (!g) return luma_set_error(LUMA_E_INVALID, "null grid");
     const luma_grid_desc &d = g->d;
     cudaStream_t s = g->stream;
     const size_t rs = real_size(g);
-    double *stage = nullptr;
-    const size_t maxd = g->n * (size_t)(d.Q > d.dims ? d.Q : d.dims);
-    CK(cudaMallocAsync(&stage, maxd * sizeof(double), s));
     int rc = LUMA_OK;
-    auto run = [&]() -> int {
-        if (f) {
-            CK(cudaMemcpyAsync(stage, f, g->n * d.Q * sizeof(double), cudaMemcpyHostToDevice, s));
-            const int layout = g->bulk ? kPopAAE : kPopPlain;
-            CK(dispatch(d.Q, d.precision, [&](auto q, auto p) {
-                return launch_pop_in<decltype(q)::value, decltype(p)>(stage, g->f[0], d.N, d.M, d.K, layout, d.rho_in, s);
-            }));
-            if (!g->bulk) CK(cudaMemcpyAsync(g->f[1], g->f[0], g->n * d.Q * rs, cudaMemcpyDeviceToDevice, s));
-            g->cur = 0;
-            g->aa_odd = 0;
-        }
-        auto vec_in = [&](const double *h, void *dst, int dims) -> int {
-            CK(cudaMemcpyAsync(stage, h, g->n * dims * sizeof(double), cudaMemcpyHostToDevice, s));
-            if (d.precision == LUMA_PREC_FP64) CK(launch_vec_in<P64>(stage, dst, g->n, dims, s));
-            else CK(launch_vec_in<P32>(stage, dst, g->n, dims, s));
+    {
+        Stage stage(g->n * (size_t)(d.Q > d.dims ? d.Q : d.dims), s);
+        // the array as the conversion reads it: in place, or copied to the stage
+        auto source = [&](const double *h, size_t count, const double **out) -> int {
+            if ((*out = device_view(h))) return LUMA_OK;
+            double *st = nullptr;
+            CK(stage.get(&st));
+            CK(cudaMemcpyAsync(st, h, count * sizeof(double), cudaMemcpyHostToDevice, s));
+            *out = st;
             return LUMA_OK;
         };
-        if (u && (rc = vec_in(u, g->u, d.dims))) return rc;
-        if (rho && (rc = vec_in(rho, g->rho, 1))) return rc;
-        // force_xyz is ignored on grids without a force field (the reference
-        // allocates it only under L_IBM_ON or L_GRAVITY_ON).
-        if (force_xyz && g->force && (rc = vec_in(force_xyz, g->force, d.dims))) return rc;
-        return LUMA_OK;
-    };
-    rc = run();
-    cudaFreeAsync(stage, s);
+        auto run = [&]() -> int {
+            if (f) {
+                const double *src = nullptr;
+                if (int r = source(f, g->n * d.Q, &src)) return r;
+                const int layout = g->bulk ? kPopAAE : kPopPlain;
+                CK(dispatch(d.Q, d.precision, [&](auto q, auto p) {
+                    return launch_pop_in<decltype(q)::value, decltype(p)>(src, g->f[0], d.N, d.M, d.K, layout, d.rho_in, s);
+                }));
+                if (!g->bulk) CK(cudaMemcpyAsync(g->f[1], g->f[0], g->n * d.Q * rs, cudaMemcpyDeviceToDevice, s));
+                g->cur = 0;
+                g->aa_odd = 0;
+            }
+            auto vec_in = [&](const double *h, void *dst, int dims) -> int {
+                const double *src = nullptr;
+                if (int r = source(h, g->n * dims, &src)) return r;
+                if (d.precision == LUMA_PREC_FP64) CK(launch_vec_in<P64>(src, dst, g->n, dims, s));
+                else CK(launch_vec_in<P32>(src, dst, g->n, dims, s));
+                return LUMA_OK;
+            };
+            if (u && (rc = vec_in(u, g->u, d.dims))) return rc;
+            if (rho && (rc = vec_in(rho, g->rho, 1))) return rc;
+            // force_xyz is ignored on grids without a force field (the reference
+            // allocates it only under L_IBM_ON or L_GRAVITY_ON).
+            if (force_xyz && g->force && (rc = vec_in(force_xyz, g->force, d.dims))) return rc;
+            return LUMA_OK;
+        };
+        rc = run();
+    }
     CK(cudaStreamSynchronize(s));
     if (rc) return rc;
     g->t = t;
@@ -839,37 +895,50 @@ int luma_gpu_download_state(luma_gpu_grid *g, double *f, double *u, double *rho,
     if (!g) return luma_set_error(LUMA_E_INVALID, "null grid");
     const luma_grid_desc &d = g->d;
     cudaStream_t s = g->stream;
-    double *stage = nullptr;
-    const size_t maxd = g->n * (size_t)(d.Q > d.dims ? d.Q : d.dims);
-    CK(cudaMallocAsync(&stage, maxd * sizeof(double), s));
     int rc = LUMA_OK;
-    auto run = [&]() -> int {
-        if (f) {
-            const int layout = g->bulk ? (g->aa_odd ? kPopAAO : kPopAAE) : kPopPlain;
-            const void *src = g->bulk ? g->f[0] : g->f[g->cur];
-            CK(dispatch(d.Q, d.precision, [&](auto q, auto p) {
-                return launch_pop_out<decltype(q)::value, decltype(p)>(src, stage, d.N, d.M, d.K, layout, d.rho_in, s);
-            }));
-            CK(cudaMemcpyAsync(f, stage, g->n * d.Q * sizeof(double), cudaMemcpyDeviceToHost, s));
-            CK(cudaStreamSynchronize(s));
-        }
-        auto vec_out = [&](const void *src, double *h, int dims) -> int {
-            if (d.precision == LUMA_PREC_FP64) CK(launch_vec_out<P64>(src, stage, g->n, dims, s));
-            else CK(launch_vec_out<P32>(src, stage, g->n, dims, s));
-            CK(cudaMemcpyAsync(h, stage, g->n * dims * sizeof(double), cudaMemcpyDeviceToHost, s));
-            CK(cudaStreamSynchronize(s));
+    {
+        Stage stage(g->n * (size_t)(d.Q > d.dims ? d.Q : d.dims), s);
+        // the conversion writes a mapped host array in place, else the stage,
+        // which is then copied out
+        auto target = [&](double *h, double **out) -> int {
+            if ((*out = device_view(h))) return LUMA_OK;
+            CK(stage.get(out));
             return LUMA_OK;
         };
-        if (u && (rc = vec_out(g->u, u, d.dims))) return rc;
-        if (rho && (rc = vec_out(g->rho, rho, 1))) return rc;
-        if (force_xyz) {
-            if (!g->force) memset(force_xyz, 0, g->n * d.dims * sizeof(double));
-            else if ((rc = vec_out(g->force, force_xyz, d.dims))) return rc;
-        }
-        return LUMA_OK;
-    };
-    rc = run();
-    cudaFreeAsync(stage, s);
+        auto finish = [&](double *h, const double *dst, size_t count) -> int {
+            if (dst != device_view(h))
+                CK(cudaMemcpyAsync(h, dst, count * sizeof(double), cudaMemcpyDeviceToHost, s));
+            CK(cudaStreamSynchronize(s));   // the stage is reused by the next array
+            return LUMA_OK;
+        };
+        auto run = [&]() -> int {
+            if (f) {
+                double *dst = nullptr;
+                if (int r = target(f, &dst)) return r;
+                const int layout = g->bulk ? (g->aa_odd ? kPopAAO : kPopAAE) : kPopPlain;
+                const void *src = g->bulk ? g->f[0] : g->f[g->cur];
+                CK(dispatch(d.Q, d.precision, [&](auto q, auto p) {
+                    return launch_pop_out<decltype(q)::value, decltype(p)>(src, dst, d.N, d.M, d.K, layout, d.rho_in, s);
+                }));
+                if (int r = finish(f, dst, g->n * d.Q)) return r;
+            }
+            auto vec_out = [&](const void *src, double *h, int dims) -> int {
+                double *dst = nullptr;
+                if (int r = target(h, &dst)) return r;
+                if (d.precision == LUMA_PREC_FP64) CK(launch_vec_out<P64>(src, dst, g->n, dims, s));
+                else CK(launch_vec_out<P32>(src, dst, g->n, dims, s));
+                return finish(h, dst, g->n * dims);
+            };
+            if (u && (rc = vec_out(g->u, u, d.dims))) return rc;
+            if (rho && (rc = vec_out(g->rho, rho, 1))) return rc;
+            if (force_xyz) {
+                if (!g->force) memset(force_xyz, 0, g->n * d.dims * sizeof(double));
+                else if ((rc = vec_out(g->force, force_xyz, d.dims))) return rc;
+            }
+            return LUMA_OK;
+        };
+        rc = run();
+    }
     CK(cudaStreamSynchronize(s));
     return rc;
 }

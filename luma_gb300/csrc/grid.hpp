@@ -89,6 +89,8 @@ void luma_bfl_args(const luma_gpu_grid *g, luma::StepArgs &a);
 void luma_bfl_signature(const luma_gpu_grid *g, std::vector<uintptr_t> &sig);
 // io.cu
 void luma_io_free(luma_gpu_grid *g);
+// epsilon.cu
+int luma_eps_solve_device(int n, int band, const std::vector<double> &a, std::vector<double> &x, cudaStream_t s);
 // fem.cu
 int luma_fem_upload(luma_gpu_grid *g);
 int luma_fem_supports(luma_gpu_grid *g, const int *skip);

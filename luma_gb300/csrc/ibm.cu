@@ -111,6 +111,7 @@ int find_support(const GridView &g, IbmBody &b) {
 
 void compute_ds(const GridView &g, IbmBody &b) {
     const double dh = g.dh;
+#pragma omp parallel for schedule(static) if (b.nm > 512)
     for (int m = 0; m < b.nm; ++m) {
         double ds = 10.0;
         for (int n = 0; n < b.nm; ++n) {
@@ -162,22 +163,32 @@ void lu_solve_transposed(int n, std::vector<double> &a, std::vector<double> &x) 
 // a single body as ibm_findEpsilon builds it, or every body of a level as
 // one system under L_UNIVERSAL_EPSILON_CALC (ibm_universalEpsilonGather /
 // Scatter, :1067-1142), which couples bodies whose supports overlap.
-void find_epsilon_set(const GridView &g, const std::vector<IbmBody *> &set) {
+// Entry (I, J) sums over I's supports the kernel of J at the support; a
+// pair of markers further apart on an axis than their two kernel reaches
+// (1.5 dilations each) has only exact-zero terms, so the entry stays +0
+// without evaluating them.  With a stream the LU and the solve run on the
+// device (the same arithmetic); the host-only set-up solves on the host.
+int find_epsilon_set(const GridView &g, const std::vector<IbmBody *> &set, cudaStream_t *device) {
     const int D = g.dims;
     const double dh = g.dh;
     std::vector<std::pair<IbmBody *, int>> mk;  // global marker -> (body, marker)
     for (IbmBody *b : set)
         for (int m = 0; m < b->nm; ++m) mk.emplace_back(b, m);
     const int n = (int)mk.size();
-    if (n == 0) return;
+    if (n == 0) return LUMA_OK;
     std::vector<double> A((size_t)n * n, 0.0);  // row-major A[I][J]
-#pragma omp parallel for schedule(dynamic, 16) if (n > 256)
+    int band = 0;
+#pragma omp parallel for schedule(dynamic, 16) reduction(max : band) if (n > 256)
     for (int I = 0; I < n; ++I) {
         const IbmBody &bi = *mk[I].first;
         const int mi = mk[I].second;
         for (int J = 0; J < n; ++J) {
             const IbmBody &bj = *mk[J].first;
             const int mj = mk[J].second;
+            const double reach = (1.5 * (bi.dil[mi] + bj.dil[mj]) + 1e-6) * dh;
+            bool near = true;
+            for (int d = 0; d < D; ++d) near = near && std::fabs(bi.pos[3 * mi + d] - bj.pos[3 * mj + d]) <= reach;
+            if (!near) continue;
             double aij = 0.0;
             for (int s = bi.off[mi]; s < bi.off[mi + 1]; ++s) {
                 const double dI = bi.delta[s];
@@ -187,16 +198,24 @@ void find_epsilon_set(const GridView &g, const std::vector<IbmBody *> &set) {
                 aij += dI * dJ * bi.area[mi];
             }
             A[(size_t)I * n + J] = aij * bj.ds[mj];
+            if (A[(size_t)I * n + J] != 0.0) band = std::max(band, I > J ? I - J : J - I);
         }
     }
     std::vector<double> x(n, 1.0);
-    lu_solve_transposed(n, A, x);
+    int rc = device ? luma_eps_solve_device(n, band, A, x, *device) : LUMA_E_INVALID;
+    if (rc == LUMA_E_INVALID) {   // host-only set-up, or a band too wide for the device solve
+        std::fill(x.begin(), x.end(), 1.0);
+        lu_solve_transposed(n, A, x);
+    } else if (rc) {
+        return rc;
+    }
     for (int I = 0; I < n; ++I) mk[I].first->eps[mk[I].second] = x[I];
+    return LUMA_OK;
 }
 
 // Supports, spacing and epsilon of rigid bodies on one grid, in the order
 // ObjectManager::ibm_initialise runs them (:190-246).
-int setup_bodies(const GridView &v, std::vector<IbmBody> &bodies, bool universal) {
+int setup_bodies(const GridView &v, std::vector<IbmBody> &bodies, bool universal, cudaStream_t *device) {
     for (IbmBody &b : bodies) {
         int rc = find_support(v, b);
         if (rc) return rc;
@@ -205,10 +224,10 @@ int setup_bodies(const GridView &v, std::vector<IbmBody> &bodies, bool universal
     if (universal) {
         std::vector<IbmBody *> all;
         for (IbmBody &b : bodies) all.push_back(&b);
-        find_epsilon_set(v, all);
-    } else {
-        for (IbmBody &b : bodies) find_epsilon_set(v, {&b});
+        return find_epsilon_set(v, all, device);
     }
+    for (IbmBody &b : bodies)
+        if (int rc = find_epsilon_set(v, {&b}, device)) return rc;
     return LUMA_OK;
 }
 
@@ -322,7 +341,7 @@ int init_tree(luma_gpu_grid *g) {
         if (universal && grids_on_level(root_of(g), g->d.level) > 1)
             return luma_set_error(LUMA_E_INVALID, "universal epsilon couples the bodies of a level: one region "
                                                   "per level only");
-        int rc = setup_bodies(view_of(g), st.bodies, universal);
+        int rc = setup_bodies(view_of(g), st.bodies, universal, &g->stream);
         if (rc) return rc;
         rc = upload_bodies(g);
         if (rc) return rc;
@@ -428,7 +447,7 @@ int luma_ibm_setup_host(const luma_grid_desc *desc, int nbodies, const int *nmar
         b.area.assign(b.nm, 1.0);
         off += b.nm;
     }
-    if (int rc = setup_bodies(v, bodies, universal != 0)) return rc;
+    if (int rc = setup_bodies(v, bodies, universal != 0, nullptr)) return rc;
     off = 0;
     for (const IbmBody &b : bodies) {
         for (int m = 0; m < b.nm; ++m) {

@@ -729,24 +729,40 @@ __global__ void __launch_bounds__(128) k_force_collide_list(StepArgs a, const in
 
 // ---- immersed boundary pass (ObjectManager::ibm_apply, src/ObjectManager_ops_ibm.cpp:33-54) ----
 
-// ibm_interpolate (:498-591) + ibm_computeForce (:598-614), one thread per
-// marker, FP64 marker arithmetic in the reference's order.
+// ibm_interpolate (:498-591) + ibm_computeForce (:598-614), one warp per
+// marker: the lanes gather the marker's supports in parallel, then every
+// lane adds the terms in support order with the reference's rounding (each
+// term rs*dl*A and rs*u*dl*A rounded, then added; no fused multiply-add),
+// so the sums are the reference's FP64 sums.
 template <int Q, class P>
 __global__ void k_ibm_interp_force(StepArgs a, IbmArgs b) {
     if (a.skip && *a.skip) return;  // a converged FSI loop: later sub-iterations do nothing
     constexpr int D = Lattice<Q>::D;
-    const int m = blockIdx.x * blockDim.x + threadIdx.x;
-    if (m >= b.nm) return;
+    const int lane = threadIdx.x & 31;
+    const int m = (int)(((size_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+    if (m >= b.nm) return;                              // whole warps leave together
     const size_t n = (size_t)a.ncell;
     double r = 0.0, mom[3] = {0.0, 0.0, 0.0};
     const double A = b.area[m];
-    for (int s = b.moff[m]; s < b.moff[m + 1]; ++s) {
-        const int id = b.msite[s];
-        const double rs = double(ldr<P>(a.rho, id));
-        const double dl = b.mdelta[s];
-        r += rs * dl * A;
-        for (int d = 0; d < D; ++d) mom[d] += rs * double(ldr<P>(a.u, (size_t)d * n + id)) * dl * A;
+    const int s0 = b.moff[m], s1 = b.moff[m + 1];
+    for (int base = s0; base < s1; base += 32) {
+        const int s = base + lane;
+        double pr = 0.0, pm[3] = {0.0, 0.0, 0.0};
+        if (s < s1) {
+            const int id = b.msite[s];
+            const double rs = double(ldr<P>(a.rho, id));
+            const double dl = b.mdelta[s];
+            pr = __dmul_rn(__dmul_rn(rs, dl), A);
+            for (int d = 0; d < D; ++d)
+                pm[d] = __dmul_rn(__dmul_rn(__dmul_rn(rs, double(ldr<P>(a.u, (size_t)d * n + id))), dl), A);
+        }
+        const int cnt = s1 - base < 32 ? s1 - base : 32;
+        for (int t = 0; t < cnt; ++t) {
+            r = __dadd_rn(r, __shfl_sync(0xffffffffu, pr, t));
+            for (int d = 0; d < D; ++d) mom[d] = __dadd_rn(mom[d], __shfl_sync(0xffffffffu, pm[d], t));
+        }
     }
+    if (lane != 0) return;
     b.irho[m] = r;
     for (int d = 0; d < D; ++d) {
         b.imom[3 * m + d] = mom[d];
@@ -889,7 +905,7 @@ __global__ void k_flex_remacro(StepArgs a, FlexArgs f) {
 template <int Q, class P>
 cudaError_t launch_ibm_pass(const StepArgs &a, const IbmArgs &b, const FlexArgs &f, cudaStream_t s) {
     const int nt = f.nm * kFlexMaxSupp;
-    if (b.nm > 0) k_ibm_interp_force<Q, P><<<(b.nm + 127) / 128, 128, 0, s>>>(a, b);
+    if (b.nm > 0) k_ibm_interp_force<Q, P><<<(unsigned)(((size_t)b.nm * 32 + 127) / 128), 128, 0, s>>>(a, b);
     if (f.nm > 0) k_flex_interp_force<Q, P><<<(f.nm + 127) / 128, 128, 0, s>>>(a, f);
     if (b.nm > 0) k_ibm_spread<Q, P><<<(b.nu + 127) / 128, 128, 0, s>>>(a, b);
     if (f.nm > 0) k_flex_spread<Q, P><<<(nt + 127) / 128, 128, 0, s>>>(a, f);

@@ -332,3 +332,32 @@ def test_time_averages_match_oracle(name, prec):
             assert rel_l2(a["rho"], b["rho"]) <= tol[0], (R.grid_key(lv), s)
             assert rel_l2(a["u"], b["u"]) <= tol[1], (R.grid_key(lv), s)
             assert rel_l2(a["uu"], b["uu"]) <= tol[1], (R.grid_key(lv), s)
+
+
+@pytest.mark.parametrize("prec", [A.PREC_FP64, A.PREC_FP32_SHIFTED])
+def test_pinned_host_arrays_transfer_in_place(prec):
+    """Pinned host arrays are read and written in place by the layout
+    conversions (no staging copy): the state they carry up and back equals
+    the staged transfer of the same values in ordinary host memory."""
+    import ctypes as C
+    import torch
+    from luma_gb300.gpu import check, lib
+    L = lib()
+    lv = R.level0("refine_d2q9")
+    f0, u0, r0, _ = R.initial_state(lv)
+    ga, gb = gpu_grid(lv.desc(precision=prec)), gpu_grid(lv.desc(precision=prec))
+    ga.upload(f0, u0, r0, None, 0)
+    pin = {k: torch.from_numpy(v.copy()).pin_memory() for k, v in (("f", f0), ("u", u0), ("rho", r0))}
+    dp = C.POINTER(C.c_double)
+    ptr = lambda t: C.cast(t.data_ptr(), dp)  # noqa: E731
+    check(L.luma_gpu_upload_state(C.c_void_p(gb.h), ptr(pin["f"]), ptr(pin["u"]), ptr(pin["rho"]), None, 0))
+    for g in (ga, gb):
+        g.step(7)
+        g.synchronize()
+    want = ga.download()
+    out = {k: torch.empty(v.size, dtype=torch.float64).pin_memory() for k, v in want.items() if k != "force"}
+    check(L.luma_gpu_download_state(C.c_void_p(gb.h), ptr(out["f"]), ptr(out["u"]), ptr(out["rho"]), None))
+    for k in ("f", "u", "rho"):
+        assert np.array_equal(out[k].numpy(), want[k]), k
+    ga.close()
+    gb.close()

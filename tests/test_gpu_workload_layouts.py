@@ -168,3 +168,48 @@ def test_refined_kbc_filaments_fp32_tips_close_to_fp64():
     for g, o in zip(gg, oo):
         gs, os_ = g.download(), o.download()
         assert rel_l2(gs["u"], os_["u"]) <= 2e-4
+
+
+@pytest.mark.parametrize("prec", [A.PREC_FP64, A.PREC_FP32_SHIFTED], ids=["fp64", "fp32s"])
+def test_refined_sphere_at_split_size_matches_oracle(prec):
+    """The refined-sphere workload scaled to a level-0 grid of 351,232 sites:
+    at this size level 0 runs its interior sites in their own kernel, beside
+    the level-1 and level-2 sub-steps (the body on level 1), as the full
+    workload does.  Every grid against the oracle after 2, 6 and 10 steps:
+    FP64 rel L2 of f, u, rho <= 1e-10, marker forces <= 1e-9; shifted FP32
+    rel L2(u) <= 2e-4."""
+    from luma_gb300.gpu import GpuGrid
+    nx = 112
+    sc = nx / 384.0
+    levels, markers = W.sphere_refined(nx=nx, ny=nx // 2, nz=nx // 2, diameter_lu=24.0 * sc,
+                                       n_markers=int(round(5000 * sc * sc)), l1_half=max(6, int(round(24 * sc))),
+                                       l2_half=max(1, int(round(4 * sc))))
+    assert levels[0].ncell >= 1 << 18
+    gg, oo = [], []
+    for lv in levels:
+        gg.append(GpuGrid(lv.desc(precision=prec), gg[-1] if gg else None))
+        oo.append(O.OracleGrid(lv.desc(), oo[-1] if oo else None))
+    for g, o, lv in zip(gg, oo, levels):
+        W.upload_level(g, lv)
+        W.upload_level(o, lv)
+    oibm = O.OracleIBM()
+    gg[W.BODY_LEVEL].ibm_add_body(markers)
+    oibm.add_body(oo[W.BODY_LEVEL], markers)
+    gg[0].ibm_initialise()
+    oibm.initialise()
+    done = 0
+    for s in (2, 6, 10):
+        gg[0].step(s - done)
+        oo[0].step(s - done)
+        done = s
+        for g, o, lv in zip(gg, oo, levels):
+            gs, os_ = g.download(), o.download()
+            eu = rel_l2(gs["u"], os_["u"])
+            if prec == A.PREC_FP64:
+                ef = rel_l2(gs["f"], os_["f"])
+                assert eu <= 1e-10 and ef <= 1e-10, (R.grid_key(lv), s, eu, ef)
+            else:
+                assert eu <= 2e-4, (R.grid_key(lv), s, eu)
+        gm, om = gg[W.BODY_LEVEL].ibm_markers(0), oibm.markers(0)
+        ef = rel_l2(gm[:, 3:6], om[:, 3:6])
+        assert ef <= (1e-9 if prec == A.PREC_FP64 else 1e-3), (s, ef)
