@@ -192,6 +192,25 @@ int luma_gpu_step(luma_gpu_grid *root, int nsteps);
  * grid of the tree with one, and clears that record. */
 int luma_gpu_synchronize(luma_gpu_grid *root);
 
+/* ---- decomposed grids: halo planes ----------------------------------------- */
+/* A grid cut into slabs along x, one per GPU (or several on one), each slab
+ * a grid of its own with one ghost x-plane on each side that holds a copy of
+ * the neighbouring slab's edge plane.  After every step each slab exports
+ * its first and last real planes and imports its neighbours' into its
+ * ghost planes: the exchange MpiManager::mpi_communicate performs with
+ * mpi_buffer_pack / mpi_buffer_unpack after every step of a grid
+ * (src/MpiManager.cpp:631-820, src/Mpi_buffer_pack.cpp,
+ * src/Mpi_buffer_unpk.cpp; called from src/GridObj_ops_lbm_optimised.cpp:189).
+ * The planes are the grid's current populations, all Q directions, in the
+ * device's storage (FP64, or shifted FP32), direction-major: direction v's
+ * nplanes*M*K values, then v+1's.  `buf` is device memory of this or a peer
+ * GPU, or pinned host memory.  Stream-ordered on the grid's stream.  Grids
+ * created with LUMA_FLAG_TWO_BUFFER only (the in-place step keeps two
+ * storage layouts); LUMA_E_INVALID otherwise or for planes off the grid. */
+int luma_gpu_planes_bytes(const luma_gpu_grid *grid, int nplanes, size_t *bytes);
+int luma_gpu_planes_export(luma_gpu_grid *grid, int i0, int nplanes, void *buf);
+int luma_gpu_planes_import(luma_gpu_grid *grid, int i0, int nplanes, const void *buf);
+
 /* ---- reductions / watchdog ----------------------------------------------- */
 /* No counterpart in the reference (it keeps no running sums).  FP64 sums
  * over the grid's fluid-updated sites (see luma_reduction), deterministic:

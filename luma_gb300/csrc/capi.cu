@@ -1013,6 +1013,40 @@ static int take_unsupported(luma_gpu_grid *g, int *code, int *level, int *region
     return LUMA_OK;
 }
 
+static int check_planes(const luma_gpu_grid *g, int i0, int nplanes, const void *buf) {
+    if (!g || !buf) return luma_set_error(LUMA_E_INVALID, "null argument");
+    if (g->bulk || !g->f[1]) return luma_set_error(LUMA_E_INVALID, "halo planes need a two-buffer grid (LUMA_FLAG_TWO_BUFFER)");
+    if (nplanes <= 0 || i0 < 0 || i0 + nplanes > g->d.N)
+        return luma_set_error(LUMA_E_INVALID, "planes %d..%d off the grid's %d x-planes", i0, i0 + nplanes - 1, g->d.N);
+    return LUMA_OK;
+}
+
+int luma_gpu_planes_bytes(const luma_gpu_grid *g, int nplanes, size_t *bytes) {
+    if (!g || !bytes || nplanes < 0) return luma_set_error(LUMA_E_INVALID, "bad argument");
+    *bytes = (size_t)nplanes * g->d.M * g->d.K * g->d.Q * real_size(g);
+    return LUMA_OK;
+}
+
+// Direction v's planes i0..i0+np-1 are one contiguous run of the SoA
+// buffer (sites are x-major), so a transfer is one strided 2D copy of Q rows.
+int luma_gpu_planes_export(luma_gpu_grid *g, int i0, int nplanes, void *buf) {
+    if (int rc = check_planes(g, i0, nplanes, buf)) return rc;
+    const size_t rs = real_size(g), plane = (size_t)g->d.M * g->d.K;
+    const char *src = static_cast<const char *>(g->f[g->cur]) + i0 * plane * rs;
+    CK(cudaMemcpy2DAsync(buf, nplanes * plane * rs, src, g->n * rs, nplanes * plane * rs, g->d.Q, cudaMemcpyDefault,
+                         g->stream));
+    return LUMA_OK;
+}
+
+int luma_gpu_planes_import(luma_gpu_grid *g, int i0, int nplanes, const void *buf) {
+    if (int rc = check_planes(g, i0, nplanes, buf)) return rc;
+    const size_t rs = real_size(g), plane = (size_t)g->d.M * g->d.K;
+    char *dst = static_cast<char *>(g->f[g->cur]) + i0 * plane * rs;
+    CK(cudaMemcpy2DAsync(dst, g->n * rs, buf, nplanes * plane * rs, nplanes * plane * rs, g->d.Q, cudaMemcpyDefault,
+                         g->stream));
+    return LUMA_OK;
+}
+
 int luma_gpu_synchronize(luma_gpu_grid *root) {
     if (!root) return luma_set_error(LUMA_E_INVALID, "null grid");
     CK(cudaStreamSynchronize(root->stream));

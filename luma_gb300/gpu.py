@@ -50,6 +50,9 @@ def lib() -> C.CDLL:
         L.luma_gpu_step.argtypes = [vp, C.c_int]
         L.luma_gpu_synchronize.argtypes = [vp]
         L.luma_gpu_reduce.argtypes = [vp, C.POINTER(A.Reduction)]
+        L.luma_gpu_planes_bytes.argtypes = [vp, C.c_int, C.POINTER(C.c_size_t)]
+        L.luma_gpu_planes_export.argtypes = [vp, C.c_int, C.c_int, vp]
+        L.luma_gpu_planes_import.argtypes = [vp, C.c_int, C.c_int, vp]
         L.luma_gpu_ibm_add_body.argtypes = [vp, C.c_int, dp, dp, C.POINTER(C.c_int)]
         L.luma_gpu_ibm_initialise.argtypes = [vp]
         L.luma_gpu_ibm_get_markers.argtypes = [vp, C.c_int, dp]
@@ -112,6 +115,19 @@ class GpuGrid:
             self.close()
         except Exception:
             pass
+
+    def planes_bytes(self, nplanes: int) -> int:
+        v = C.c_size_t()
+        check(self.L.luma_gpu_planes_bytes(self.h, nplanes, C.byref(v)))
+        return v.value
+
+    def planes_export(self, i0: int, nplanes: int, buf_ptr: int) -> None:
+        """Current populations of x-planes i0.. (device storage, direction-major)
+        into `buf_ptr` (device or pinned host address), on the grid's stream."""
+        check(self.L.luma_gpu_planes_export(self.h, i0, nplanes, buf_ptr))
+
+    def planes_import(self, i0: int, nplanes: int, buf_ptr: int) -> None:
+        check(self.L.luma_gpu_planes_import(self.h, i0, nplanes, buf_ptr))
 
     def set_stream(self, stream_ptr: int | None):
         check(self.L.luma_gpu_set_stream(self.h, stream_ptr))
