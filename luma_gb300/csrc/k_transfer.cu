@@ -10,16 +10,30 @@ namespace luma {
 
 namespace {
 
+// The interleaved host arrays are read and written one block of kTile sites
+// at a time through shared memory: the block's Q*kTile (or dims*kTile)
+// consecutive values move with consecutive threads on consecutive
+// addresses, which matters most when the array is host memory the kernel
+// reaches in place (a site-per-thread access would touch a new 32-byte
+// sector per thread for each value).  The conversion of each value is the
+// same expression as before.
+constexpr int kTile = 128;
+
 template <int Q, class P>
-__global__ void k_pop_in(const double *__restrict__ aos, typename P::S *__restrict__ soa, int N, int M, int K,
-                         int layout, double rho0) {
+__global__ void __launch_bounds__(kTile) k_pop_in(const double *__restrict__ aos, typename P::S *__restrict__ soa,
+                                                  int N, int M, int K, int layout, double rho0) {
     using L = Lattice<Q>;
+    __shared__ double tile[kTile * Q];
     const size_t n = (size_t)N * M * K;
-    const size_t id = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (id >= n) return;
+    const size_t base = (size_t)blockIdx.x * kTile;
+    const int nsite = n - base < (size_t)kTile ? (int)(n - base) : kTile;
+    for (int t = threadIdx.x; t < nsite * Q; t += kTile) tile[t] = aos[base * Q + t];
+    __syncthreads();
+    if ((int)threadIdx.x >= nsite) return;
+    const size_t id = base + threadIdx.x;
 #pragma unroll
     for (int v = 0; v < Q; ++v) {
-        double f = aos[(size_t)v + id * Q];
+        double f = tile[threadIdx.x * Q + v];
         if (P::shifted) f -= L::w(v) * rho0;
         const int slot = layout == kPopAAE ? L::opp(v) : v;
         soa[(size_t)slot * n + id] = typename P::S(f);
@@ -27,45 +41,64 @@ __global__ void k_pop_in(const double *__restrict__ aos, typename P::S *__restri
 }
 
 template <int Q, class P>
-__global__ void k_pop_out(const typename P::S *__restrict__ soa, double *__restrict__ aos, int N, int M, int K,
-                          int layout, double rho0) {
+__global__ void __launch_bounds__(kTile) k_pop_out(const typename P::S *__restrict__ soa, double *__restrict__ aos,
+                                                   int N, int M, int K, int layout, double rho0) {
     using L = Lattice<Q>;
+    __shared__ double tile[kTile * Q];
     const size_t n = (size_t)N * M * K;
-    const size_t id = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (id >= n) return;
-    const int k = (int)(id % K), j = (int)((id / K) % M), i = (int)(id / ((size_t)K * M));
+    const size_t base = (size_t)blockIdx.x * kTile;
+    const int nsite = n - base < (size_t)kTile ? (int)(n - base) : kTile;
+    if ((int)threadIdx.x < nsite) {
+        const size_t id = base + threadIdx.x;
+        const int k = (int)(id % K), j = (int)((id / K) % M), i = (int)(id / ((size_t)K * M));
 #pragma unroll
-    for (int v = 0; v < Q; ++v) {
-        size_t src;
-        if (layout == kPopAAE) {
-            src = (size_t)L::opp(v) * n + id;
-        } else if (layout == kPopAAO) {
-            int x = i + L::c(v, 0), y = j + L::c(v, 1), z = k + L::c(v, 2);
-            x = (x + N) % N;
-            y = (y + M) % M;
-            z = (z + K) % K;
-            src = (size_t)v * n + (size_t)z + (size_t)K * ((size_t)y + (size_t)M * x);
-        } else {
-            src = (size_t)v * n + id;
+        for (int v = 0; v < Q; ++v) {
+            size_t src;
+            if (layout == kPopAAE) {
+                src = (size_t)L::opp(v) * n + id;
+            } else if (layout == kPopAAO) {
+                int x = i + L::c(v, 0), y = j + L::c(v, 1), z = k + L::c(v, 2);
+                x = (x + N) % N;
+                y = (y + M) % M;
+                z = (z + K) % K;
+                src = (size_t)v * n + (size_t)z + (size_t)K * ((size_t)y + (size_t)M * x);
+            } else {
+                src = (size_t)v * n + id;
+            }
+            double f = double(soa[src]);
+            if (P::shifted) f += L::w(v) * rho0;
+            tile[threadIdx.x * Q + v] = f;
         }
-        double f = double(soa[src]);
-        if (P::shifted) f += L::w(v) * rho0;
-        aos[(size_t)v + id * Q] = f;
     }
+    __syncthreads();
+    for (int t = threadIdx.x; t < nsite * Q; t += kTile) aos[base * Q + t] = tile[t];
 }
 
 template <class P>
-__global__ void k_vec_in(const double *__restrict__ aos, typename P::R *__restrict__ soa, size_t n, int dims) {
-    const size_t id = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (id >= n) return;
-    for (int d = 0; d < dims; ++d) soa[(size_t)d * n + id] = typename P::R(aos[(size_t)d + id * dims]);
+__global__ void __launch_bounds__(kTile) k_vec_in(const double *__restrict__ aos, typename P::R *__restrict__ soa,
+                                                  size_t n, int dims) {
+    __shared__ double tile[kTile * 3];
+    const size_t base = (size_t)blockIdx.x * kTile;
+    const int nsite = n - base < (size_t)kTile ? (int)(n - base) : kTile;
+    for (int t = threadIdx.x; t < nsite * dims; t += kTile) tile[t] = aos[base * dims + t];
+    __syncthreads();
+    if ((int)threadIdx.x >= nsite) return;
+    const size_t id = base + threadIdx.x;
+    for (int d = 0; d < dims; ++d) soa[(size_t)d * n + id] = typename P::R(tile[threadIdx.x * dims + d]);
 }
 
 template <class P>
-__global__ void k_vec_out(const typename P::R *__restrict__ soa, double *__restrict__ aos, size_t n, int dims) {
-    const size_t id = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (id >= n) return;
-    for (int d = 0; d < dims; ++d) aos[(size_t)d + id * dims] = double(soa[(size_t)d * n + id]);
+__global__ void __launch_bounds__(kTile) k_vec_out(const typename P::R *__restrict__ soa, double *__restrict__ aos,
+                                                   size_t n, int dims) {
+    __shared__ double tile[kTile * 3];
+    const size_t base = (size_t)blockIdx.x * kTile;
+    const int nsite = n - base < (size_t)kTile ? (int)(n - base) : kTile;
+    if ((int)threadIdx.x < nsite) {
+        const size_t id = base + threadIdx.x;
+        for (int d = 0; d < dims; ++d) tile[threadIdx.x * dims + d] = double(soa[(size_t)d * n + id]);
+    }
+    __syncthreads();
+    for (int t = threadIdx.x; t < nsite * dims; t += kTile) aos[base * dims + t] = tile[t];
 }
 
 __device__ __forceinline__ double warp_sum(double v) {
@@ -139,26 +172,27 @@ template <int Q, class P>
 cudaError_t launch_pop_in(const double *aos, void *soa, int N, int M, int K, int layout, double rho0,
                           cudaStream_t s) {
     const size_t n = (size_t)N * M * K;
-    k_pop_in<Q, P><<<(unsigned)((n + 255) / 256), 256, 0, s>>>(aos, static_cast<typename P::S *>(soa), N, M, K,
-                                                               layout, rho0);
+    k_pop_in<Q, P><<<(unsigned)((n + kTile - 1) / kTile), kTile, 0, s>>>(aos, static_cast<typename P::S *>(soa), N,
+                                                                          M, K, layout, rho0);
     return cudaGetLastError();
 }
 template <int Q, class P>
 cudaError_t launch_pop_out(const void *soa, double *aos, int N, int M, int K, int layout, double rho0,
                            cudaStream_t s) {
     const size_t n = (size_t)N * M * K;
-    k_pop_out<Q, P><<<(unsigned)((n + 255) / 256), 256, 0, s>>>(static_cast<const typename P::S *>(soa), aos, N,
-                                                                M, K, layout, rho0);
+    k_pop_out<Q, P><<<(unsigned)((n + kTile - 1) / kTile), kTile, 0, s>>>(static_cast<const typename P::S *>(soa),
+                                                                           aos, N, M, K, layout, rho0);
     return cudaGetLastError();
 }
 template <class P>
 cudaError_t launch_vec_in(const double *aos, void *soa, size_t n, int dims, cudaStream_t s) {
-    k_vec_in<P><<<(unsigned)((n + 255) / 256), 256, 0, s>>>(aos, static_cast<typename P::R *>(soa), n, dims);
+    k_vec_in<P><<<(unsigned)((n + kTile - 1) / kTile), kTile, 0, s>>>(aos, static_cast<typename P::R *>(soa), n, dims);
     return cudaGetLastError();
 }
 template <class P>
 cudaError_t launch_vec_out(const void *soa, double *aos, size_t n, int dims, cudaStream_t s) {
-    k_vec_out<P><<<(unsigned)((n + 255) / 256), 256, 0, s>>>(static_cast<const typename P::R *>(soa), aos, n, dims);
+    k_vec_out<P><<<(unsigned)((n + kTile - 1) / kTile), kTile, 0, s>>>(static_cast<const typename P::R *>(soa), aos, n,
+                                                                       dims);
     return cudaGetLastError();
 }
 template <class P>
