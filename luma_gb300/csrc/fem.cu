@@ -193,22 +193,45 @@ __device__ void lu_solve_block(double *A, int lda, int off, int n, int *ipiv, do
             __syncwarp();
         }
         for (int r = lane; r < n; r += 32) xs[r] = x[r];
-        // forward sums start at the first non-zero of each row's range
-        for (int r = lane; r < n; r += 32) {
-            int c = 0;
-            while (c < r && is_zero(AC(c, r))) ++c;
-            lim[r] = c;
-        }
-        __syncwarp();
-        if (lane == 0)
-            for (int r = 0; r < n; ++r) {
-                double s = xs[r];
-                for (int c = lim[r]; c < r; ++c) {
-                    const double v = AC(c, r);
-                    if (!is_zero(v)) s -= v * xs[c];
+        if (2 * band < 32) {
+            // forward U^T y = x with U's rows reaching 2*band right of the
+            // diagonal: each lane keeps one pending row and subtracts a term
+            // as soon as its unknown is known, in ascending order (the serial
+            // order), so a row costs one division and one multiply-subtract
+            // of the whole warp instead of a serial sum on one lane
+            double s = lane < n ? xs[lane] : 0.0;
+            int row = lane;
+            for (int c = 0; c < n; ++c) {
+                double y = 0.0;
+                if (row == c) y = s / AC(c, c);
+                y = __shfl_sync(0xffffffffu, y, c & 31);
+                if (row == c) {
+                    xs[c] = y;
+                    row += 32;
+                    s = row < n ? xs[row] : 0.0;
+                } else if (row < n && row <= c + 2 * band) {
+                    const double v = AC(c, row);
+                    if (!is_zero(v)) s -= v * y;
                 }
-                xs[r] = s / AC(r, r);
             }
+        } else {
+            // forward sums start at the first non-zero of each row's range
+            for (int r = lane; r < n; r += 32) {
+                int c = 0;
+                while (c < r && is_zero(AC(c, r))) ++c;
+                lim[r] = c;
+            }
+            __syncwarp();
+            if (lane == 0)
+                for (int r = 0; r < n; ++r) {
+                    double s = xs[r];
+                    for (int c = lim[r]; c < r; ++c) {
+                        const double v = AC(c, r);
+                        if (!is_zero(v)) s -= v * xs[c];
+                    }
+                    xs[r] = s / AC(r, r);
+                }
+        }
         __syncwarp();
         // backward sums end at the last non-zero
         for (int r = lane; r < n; r += 32) {
@@ -227,145 +250,6 @@ __device__ void lu_solve_block(double *A, int lda, int off, int n, int *ipiv, do
                 xs[r] = s;
             }
             for (int k = n - 1; k >= 0; --k) { const int p = ipiv[k] - 1; if (p != k) { const double t = xs[k]; xs[k] = xs[p]; xs[p] = t; } }
-        }
-        __syncwarp();
-        for (int r = lane; r < n; r += 32) x[r] = xs[r];
-    }
-    __syncthreads();
-#undef AC
-}
-
-// Partial-pivot LU and transposed solve of a banded matrix, the active
-// window in registers.  Same contract and the same arithmetic as
-// lu_solve_block (every matrix and solution element sees the dense serial
-// algorithm's operations in its order; exact no-ops are skipped), for a
-// matrix with no entry more than BL rows below or columns right of the
-// diagonal.  Partial pivoting then confines step k to rows k..k+BL and
-// columns k..k+2BL: lane j of warp 0 owns the column k + ((j - k) mod W) of
-// the window and holds its rows k..k+BL in registers, so a step is one
-// pivot search in registers, a broadcast of the pivot row and of the BL
-// multipliers, and a register update per lane; the finished row of U and
-// column of L go to memory and the next row of the input comes in.  Row
-// swaps reach the finished columns of L in memory (the dense algorithm
-// swaps whole rows), and `drift` bounds how far below its diagonal an L
-// entry can land through them, which bounds the backward solve.
-template <int BL>
-__device__ void band_lu_solve(double *A, int lda, int off, int n, int *ipiv, double *x) {
-#define AC(r, c) A[(size_t)(off + (c)) * lda + (off + (r))]
-    constexpr int BU = 2 * BL;        // upper bandwidth of U
-    constexpr int W = 16;             // lanes that own window columns
-    static_assert(BU + 1 <= W, "window wider than the lanes that hold it");
-    __shared__ double xs[512];
-    __shared__ int drift_s;
-    const int lane = threadIdx.x;
-    if (threadIdx.x < 32) {
-        int drift = BL;
-        double v[BL + 1];
-        int col = lane;                               // this lane's column at k = 0
-#pragma unroll
-        for (int i = 0; i <= BL; ++i) v[i] = (lane < W && i < n && col < n) ? AC(i, col) : 0.0;
-        for (int k = 0; k < n; ++k) {
-            const int lk = k % W;
-            // pivot search in column k (lane lk): first row of largest magnitude
-            int imax = 0;
-            {
-                unsigned long long best = mag_bits(v[0]);
-#pragma unroll
-                for (int i = 1; i <= BL; ++i)
-                    if (k + i < n && mag_bits(v[i]) > best) { best = mag_bits(v[i]); imax = i; }
-            }
-            imax = __shfl_sync(0xffffffffu, imax, lk);
-            double pv = 0.0;
-#pragma unroll
-            for (int i = 0; i <= BL; ++i)
-                if (i == imax) pv = v[i];
-            const bool live = !is_zero(__shfl_sync(0xffffffffu, pv, lk));
-            const int p = k + imax;
-            if (lane == 0) ipiv[k] = p + 1;
-            if (live && imax != 0) {
-                // swap rows k and p: the window in registers, the finished L
-                // columns in memory
-#pragma unroll
-                for (int i = 1; i <= BL; ++i)
-                    if (i == imax) { const double t = v[0]; v[0] = v[i]; v[i] = t; }
-                for (int c = lane; c < k; c += 32) {
-                    const double t = AC(k, c);
-                    AC(k, c) = AC(p, c);
-                    AC(p, c) = t;
-                }
-                drift += imax;
-            }
-            // multipliers of column k (lane lk), broadcast to the window
-            double m[BL];
-            if (lane == lk && live) {
-                const double inv = 1.0 / v[0];
-#pragma unroll
-                for (int i = 1; i <= BL; ++i)
-                    if (k + i < n) v[i] = v[i] * inv;
-            }
-#pragma unroll
-            for (int i = 1; i <= BL; ++i) m[i - 1] = __shfl_sync(0xffffffffu, v[i], lk);
-            // finished row k of U and column k of L to memory; rank-1 update
-            if (lane < W && col < n && col <= k + BU) {
-                AC(k, col) = v[0];
-                if (lane == lk) {
-#pragma unroll
-                    for (int i = 1; i <= BL; ++i)
-                        if (k + i < n) AC(k + i, k) = v[i];
-                } else if (live && !is_zero(v[0])) {
-#pragma unroll
-                    for (int i = 1; i <= BL; ++i)
-                        if (!is_zero(m[i - 1])) v[i] = v[i] - m[i - 1] * v[0];
-                }
-            }
-            // slide the window down a row; lane lk takes column k + W
-            if (lane == lk) {
-                col = k + W;
-#pragma unroll
-                for (int i = 0; i <= BL; ++i) v[i] = 0.0;
-            } else {
-#pragma unroll
-                for (int i = 0; i < BL; ++i) v[i] = v[i + 1];
-            }
-            const int nr = k + 1 + BL;
-            v[BL] = (lane < W && nr < n && col < n) ? AC(nr, col) : 0.0;
-        }
-        __syncwarp();
-        // forward: U^T y = b, one pending row per lane; row r subtracts its
-        // terms as the y_c arrive, in ascending c (the serial order)
-        double s = (lane < W && lane < n) ? x[lane] : 0.0;
-        for (int c = 0; c < n; ++c) {
-            const int lc = c % W;
-            const int r = c + ((lane - c % W + W) % W);  // this lane's pending row
-            double y = 0.0;
-            if (lane == lc) y = s / AC(c, c);
-            y = __shfl_sync(0xffffffffu, y, lc);
-            if (lane == lc) {
-                xs[c] = y;
-                s = c + W < n ? x[c + W] : 0.0;
-            } else if (lane < W && r < n && r <= c + BU) {
-                const double u = AC(c, r);
-                if (!is_zero(u)) s -= u * y;
-            }
-        }
-        if (lane == 0) drift_s = drift;
-        __syncwarp();
-        // backward: L^T z = y, terms in ascending c, nearest first
-        if (lane == 0) {
-            const int reach = drift < n ? drift : n;
-            for (int r = n - 1; r >= 0; --r) {
-                double t = xs[r];
-                const int cend = r + reach < n - 1 ? r + reach : n - 1;
-                for (int c = r + 1; c <= cend; ++c) {
-                    const double l = AC(c, r);
-                    if (!is_zero(l)) t -= l * xs[c];
-                }
-                xs[r] = t;
-            }
-            for (int k = n - 1; k >= 0; --k) {
-                const int q = ipiv[k] - 1;
-                if (q != k) { const double t = xs[k]; xs[k] = xs[q]; xs[q] = t; }
-            }
         }
         __syncwarp();
         for (int r = lane; r < n; r += 32) x[r] = xs[r];
@@ -560,7 +444,7 @@ __global__ void k_fem_dynamic(FemKernelArgs a) {
         for (int i = threadIdx.x; i < nd; i += blockDim.x) a.delU[d0 + i] = a.Fv[d0 + i];
         __syncthreads();
         // an element couples the 6 DOFs of its two nodes: half-bandwidth 5
-        band_lu_solve<5>(K, nd, bc, nd - bc, ipiv, a.delU + d0 + bc);
+        lu_solve_block(K, nd, bc, nd - bc, ipiv, a.delU + d0 + bc, 5);
         for (int i = threadIdx.x; i < bc; i += blockDim.x) a.delU[d0 + i] = 0.0;
         __syncthreads();
         for (int i = threadIdx.x; i < nd; i += blockDim.x) a.U[d0 + i] = a.U[d0 + i] + a.delU[d0 + i];
@@ -760,15 +644,13 @@ __global__ void k_flex_support(FemKernelArgs a) {
     for (int m = threadIdx.x; m < nmk; m += blockDim.x) x.eps[mk0 + m] = 1.0;
     __syncthreads();
     // markers share support nodes only within a few dh of each other: along
-    // a filament the system is banded, and the band solver applies when its
-    // band holds every non-zero (else the dense one; the same arithmetic)
+    // a filament the system is banded, which bounds the solver's scans
     for (int q = threadIdx.x; q < nmk * nmk; q += blockDim.x) {
         const int off = q / nmk - q % nmk;
         if (!is_zero(A[q])) atomicMax(&band, off < 0 ? -off : off);
     }
     __syncthreads();
-    if (band <= 5) band_lu_solve<5>(A, nmk, 0, nmk, ipiv, x.eps + mk0);
-    else lu_solve_block(A, nmk, 0, nmk, ipiv, x.eps + mk0, nmk);
+    lu_solve_block(A, nmk, 0, nmk, ipiv, x.eps + mk0, band < nmk ? band : nmk);
 }
 
 // max over flexible markers of |U - U_km1| / (L_UX0 dt/dh)  (ibm_checkVelDiff)
