@@ -408,6 +408,16 @@ def run_sphere_workload(args) -> int:
                        "sites_per_level": head["sites"], "lattice_updates_per_base_step":
                            head["lattice_updates_per_step"]},
             "clocks": clocks}
+    # every level carries a force field (IB grids): 2*Q*s populations + the
+    # label byte + dims*s force bytes per lattice update, the step as a whole
+    peaks = read_peaks()
+    s_b = 4 if "fp32_shifted" in res else 8
+    bpl = 2 * 19 * s_b + 1 + 3 * s_b
+    line["roofline"] = {"bound": "hbm", "bytes_per_lu": bpl, "achieved": round(head["mlups"] * 1e6 * bpl / 1e9, 1),
+                        "peak": peaks["hbm_gbs"], "unit": "GB/s",
+                        "frac": round(head["mlups"] * 1e6 * bpl / 1e9 / peaks["hbm_gbs"], 4),
+                        "note": "whole step (all kernels) against 2*Q*s+1+3*s bytes per lattice update, fine "
+                                "levels counted 2^level times per base step"}
     for name, r in res.items():
         line[name] = {"mlups": round(r["mlups"], 2), "ms_per_step": round(r["ms_per_step"], 4), "cd": r["cd"],
                       "force": r["force"], "ibm_init_s": round(r["ibm_init_s"], 3)}

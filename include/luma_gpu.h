@@ -93,7 +93,7 @@ enum {
                                               level) */
 #define LUMA_FLAG_SPLIT_INTERIOR 0x40 /* two-buffer step: run interior fluid sites in their
                                        own kernel at any grid size (by default only grids
-                                       of 2^18 sites or more split) */
+                                       of 2^14 sites or more split) */
 
 /* Description of one grid (one level/region of the hierarchy).  Mirrors the
  * GridObj members it is filled from; arrays are read during create only. */

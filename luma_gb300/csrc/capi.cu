@@ -230,8 +230,11 @@ int luma_update_defer(luma_gpu_grid *g) {
 // sites whose every pull source, wrapped periodically, is a fluid site) and
 // the full site logic (the rest, less the sites the stream skips).  Grids
 // below kInteriorMinSites keep the single full-logic launch: there the step
-// is bound by launch latency, not by the full kernel's register budget.
-constexpr size_t kInteriorMinSites = 1u << 18;
+// is bound by launch latency.  Above it the full-logic kernel, latency bound
+// per site (a label branch per pulled direction, 110 registers), is slower
+// than the interior kernel plus a list of the other sites (a 110,592-site
+// level: 33 us per launch at 121 GB/s in one kernel).
+constexpr size_t kInteriorMinSites = 1u << 14;
 
 int luma_build_interior(luma_gpu_grid *g) {
     cudaFree(g->fast);
