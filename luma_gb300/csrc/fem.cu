@@ -74,14 +74,6 @@ __device__ __forceinline__ void Tmat(double ang, double T[6][6]) {
     T[2][2] = T[5][5] = 1.0;
 }
 
-// First work item of this thread when items are dealt to the warps in
-// turn (item i goes to warp i % W, W the block's warps), stepping by the
-// block size: a warp's FP64 instruction costs the same with one active
-// lane as with 32, so per-item FP64 work is spread over all the warps.
-__device__ __forceinline__ int spread_first() {
-    return (int)((threadIdx.x & 31) * (blockDim.x >> 5) + (threadIdx.x >> 5));
-}
-
 // FEMBody::updateFEMValues (:297-325) for filament f.
 __device__ void update_values(const FemKernelArgs &a, int f) {
     const int n0 = a.node_off[f], nn = a.node_off[f + 1] - n0;
@@ -93,7 +85,7 @@ __device__ void update_values(const FemKernelArgs &a, int f) {
         a.nang[n0 + n] = a.ang0[n0 + n] + a.U[d0 + n * 3 + 2];
     }
     __syncthreads();
-    for (int e = spread_first(); e < ne; e += blockDim.x) {
+    for (int e = threadIdx.x; e < ne; e += blockDim.x) {
         double v[3];
         for (int d = 0; d < 3; ++d) v[d] = a.npos[3 * (n0 + e + 1) + d] - a.npos[3 * (n0 + e) + d];
         a.elang[e0 + e] = atan2(v[1], v[0]);
@@ -387,13 +379,13 @@ __global__ void k_fem_dynamic(FemKernelArgs a) {
     __syncthreads();
     update_values(a, f);
     const double forceScale = a.dm[f] / (Dt * Dt);
-    for (int d = spread_first(); d < nd; d += blockDim.x) a.R[d0 + d] = load_entry(a, f, d, forceScale);
+    for (int d = threadIdx.x; d < nd; d += blockDim.x) a.R[d0 + d] = load_entry(a, f, d, forceScale);
     __syncthreads();
     const double a0 = 1.0 / (kNbAlpha * (Dt * Dt)), a2 = 1.0 / (kNbAlpha * Dt), a3 = 1.0 / (2.0 * kNbAlpha) - 1.0;
     int it = 0;
     double res = 0.0;
     do {
-        for (int e = spread_first(); e < ne; e += blockDim.x) element_matrices(a, f, e);
+        for (int e = threadIdx.x; e < ne; e += blockDim.x) element_matrices(a, f, e);
         for (int q = threadIdx.x; q < nd * nd; q += blockDim.x) {
             M[q] = 0.0;
             K[q] = 0.0;
@@ -474,7 +466,7 @@ __global__ void k_fem_dynamic(FemKernelArgs a) {
     }
     __syncthreads();
     // FEMBody::updateIBMarkers (:329-370)
-    for (int m = spread_first(); m < nmk; m += blockDim.x) {
+    for (int m = threadIdx.x; m < nmk; m += blockDim.x) {
         const int e = a.parent_el[mk0 + m];
         const int ge = e0 + e;
         const double z = a.parent_zeta[mk0 + m];
@@ -528,7 +520,7 @@ __global__ void k_flex_support(FemKernelArgs a) {
     const int D = a.dims;
     const double dh = a.dh;
     const FlexArgs &x = a.flex;
-    for (int m = spread_first(); m < nmk; m += blockDim.x) {
+    for (int m = threadIdx.x; m < nmk; m += blockDim.x) {
         const int g = mk0 + m;
         const double *p = &x.pos[3 * g];
         const int in = (int)floor((p[0] - a.gstart[0]) / dh);
@@ -586,7 +578,7 @@ __global__ void k_flex_support(FemKernelArgs a) {
         x.nsupp[g] = ns;
     }
     __syncthreads();
-    for (int m = spread_first(); m < nmk; m += blockDim.x) {
+    for (int m = threadIdx.x; m < nmk; m += blockDim.x) {
         const int g = mk0 + m;
         double ds = 10.0;
         for (int q = 0; q < nmk; ++q) {
