@@ -99,13 +99,14 @@ __device__ void update_values(const FemKernelArgs &a, int f) {
 // Partial-pivot LU of the n x n block whose column-major element (r, c)
 // is A[(off + c) * lda + (off + r)] (a row-major matrix read column-major,
 // as GridUtils::solveLinearSystem hands it to dgetrf_), then the transposed
-// solve for x (length n), n <= 512.  Every element sees the operations of
-// the dense serial algorithm in the same order; the ones that are exact
-// no-ops (a zero multiplier, a zero matrix entry in the triangular sums) are
-// skipped, which is what makes the banded beam and epsilon systems cheap.
-// One warp does the work (lanes over rows / columns, warp barriers only);
-// the pivot is the first row of largest magnitude (ties to the lower row).
-// Called by the whole block; returns after a block barrier.
+// solve for x (length n), n <= 512 (dgetrs_ with trans = 'T': U^T y = x,
+// then L^T z = y, then the row interchanges in reverse).  Every element sees
+// the operations of the dense serial algorithm in the same order; the ones
+// that are exact no-ops (a zero multiplier, a zero matrix entry in the
+// triangular sums, a swap of two zeros) are skipped, which is what makes the
+// banded beam and epsilon systems cheap.  One warp does the work (warp
+// barriers only); the pivot is the first row of largest magnitude (ties to
+// the lower row).  Called by the whole block; returns after a block barrier.
 // Zero tests and magnitude order on the bit patterns (integer pipe): +-0
 // are the only doubles whose bits shifted left by one are 0, and |x| of
 // non-NaN doubles orders like its bits read as unsigned.
@@ -113,206 +114,405 @@ __device__ __forceinline__ bool is_zero(double v) { return (__double_as_longlong
 __device__ __forceinline__ unsigned long long mag_bits(double v) {
     return (unsigned long long)__double_as_longlong(v) & 0x7fffffffffffffffull;
 }
+// Position of the set bit of `mask` with `nth` set bits below it (mask has
+// more than nth set bits).
+__device__ __forceinline__ int nth_bit(unsigned mask, int nth) {
+    for (int i = 0; i < nth; ++i) mask &= mask - 1;
+    return __ffs(mask) - 1;
+}
+__device__ __forceinline__ int exponent_of(double v) { return (int)((__double_as_longlong(v) >> 52) & 0x7ff) - 1023; }
+
+// RN(a / b) from y = RN(1 / b) with multiplications and FMAs only.
+// q0 = RN(a y) lies within 1.5 ulp of a / b; one correction
+// q1 = RN(q0 + RN(a - b q0) y) brings it within one ulp (the remainder and
+// the reciprocal's error enter only at about 2^-52 ulp), and a second
+// correction with the exact FMA remainder a - b q1 rounds to the correctly
+// rounded quotient by Markstein's theorem (P. Markstein, "Computation of
+// elementary functions on the IBM RISC System/6000 processor", IBM J. Res.
+// Dev. 34(1):111-119, 1990: a faithful quotient plus the remainder times
+// the correctly rounded reciprocal, rounded once).  Zeros, non-finite
+// values and magnitudes beyond 2^+-400 (where a remainder could leave the
+// normal range) take the division itself.  Five dependent FP64 operations
+// instead of a division's longer sequence on the solve's critical path.
+__device__ __forceinline__ double quotient(double a, double b, double y) {
+    const int ea = exponent_of(a), eb = exponent_of(b);
+    if (ea < -400 || ea > 400 || eb < -400 || eb > 400) return a / b;
+    const double q0 = __dmul_rn(a, y);
+    const double q1 = __fma_rn(__fma_rn(-q0, b, a), y, q0);
+    return __fma_rn(__fma_rn(-q1, b, a), y, q1);
+}
+
+#define AC(r, c) A[(size_t)(off + (c)) * lda + (off + (r))]
 
 // `band`: no entry of the matrix lies more than `band` rows below or
 // columns right of the diagonal (n for a dense matrix).  Partial pivoting
 // keeps the multipliers of column k in rows k+1..k+band and the pivot row's
-// entries in columns up to k+2*band, so the scans stop there; the entries
-// they skip are exact zeros, which the dense elimination would leave as
-// they are.
+// entries in columns up to k+2*band (a row at position r >= k holds
+// original entries up to column r+band and fill from earlier steps j up to
+// j+2*band), so the scans stop there; the entries they skip are exact
+// zeros, which the dense elimination would leave as they are.
+
+// The banded case (band <= NB, NB = 7 or 15), one warp.  GB300 gives an
+// FP64 instruction of a warp 64 cycles of its sub-partition however many
+// lanes are active, so a step issues as few as it can, each dense: the
+// pivot's reciprocal, one multiply for all the multipliers (lane i: row
+// k+1+i), and the rank-1 update over the (row, column) pairs of non-zero
+// multiplier and pivot-row entry, 32 pairs per multiply-subtract.  The pivot
+// search is integer work on every lane (the candidates' magnitude bits);
+// the row interchange moves the rows' entries left of the window's right
+// end (further right both rows hold zeros).  lim[c] bounds the last row
+// holding a non-zero of L's column c (set by the multipliers, raised when
+// an interchange moves a non-zero down), so the backward solve needs no
+// scan.
+template <int NB>
+__device__ __forceinline__ void lu_solve_banded(double *A, int lda, int off, int n, int *ipiv, double *x, int band,
+                                                int *lim, double *xs, double *rd) {
+    const unsigned full = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    for (int r = lane; r < n; r += 32) lim[r] = r;
+    __syncwarp();
+    for (int k = 0; k < n; ++k) {
+        const int nr = min(n, k + band + 1) - k - 1;  // window rows below the diagonal
+        const int cend = min(n, k + 2 * band + 1);
+        double cv[NB + 1];
+#pragma unroll
+        for (int i = 0; i <= NB; ++i) cv[i] = i <= nr ? AC(k + i, k) : 0.0;
+        int pi = 0;
+        unsigned long long best = mag_bits(cv[0]);
+#pragma unroll
+        for (int i = 1; i <= NB; ++i) {
+            const unsigned long long v = mag_bits(cv[i]);
+            if (i <= nr && v > best) {
+                best = v;
+                pi = i;
+            }
+        }
+        const int p = k + pi;
+        if (lane == 0) ipiv[k] = p + 1;
+        if (best == 0) continue;  // a zero column: no interchange, no elimination
+        double pv = cv[0], mine = 0.0;
+#pragma unroll
+        for (int i = 1; i <= NB; ++i) {
+            if (pi == i) pv = cv[i];
+            if (lane == i - 1) mine = pi == i ? cv[0] : cv[i];  // row k+1+lane after the interchange
+        }
+        if (pi) {
+            __syncwarp();  // every lane's candidate reads before the interchange writes
+            for (int c = lane; c < cend; c += 32) {
+                const double t = AC(k, c);
+                AC(k, c) = AC(p, c);
+                AC(p, c) = t;
+                if (c < k && !is_zero(t) && p > lim[c]) lim[c] = p;
+            }
+            __syncwarp();
+        }
+        const double inv = 1.0 / pv;
+        const double m = mine * inv;
+        const bool mrow = lane < nr && !is_zero(m);
+        if (lane < nr) AC(k + 1 + lane, k) = m;
+        const int c = k + 1 + lane;
+        const bool mcol = c < cend && !is_zero(AC(k, c));
+        const unsigned rmask = __ballot_sync(full, mrow), cmask = __ballot_sync(full, mcol);
+        if (lane == 0 && rmask) lim[k] = k + 32 - __clz(rmask);
+        __syncwarp();
+        const int nrl = __popc(rmask), npairs = nrl * __popc(cmask);
+        for (int t = lane; t < npairs; t += 32) {
+            const int ci = t / nrl, ri = t - ci * nrl;
+            const int rr = k + 1 + nth_bit(rmask, ri), cc = k + 1 + nth_bit(cmask, ci);
+            AC(rr, cc) -= AC(rr, k) * AC(k, cc);
+        }
+        __syncwarp();
+    }
+    // forward U^T y = x: U's rows reach 2*band right of the diagonal, so each
+    // lane keeps one pending row and subtracts a term as soon as its unknown
+    // is known, in ascending order (the serial order); the divisions use the
+    // diagonal's reciprocals, all formed at once beforehand
+    for (int r = lane; r < n; r += 32) {
+        xs[r] = x[r];
+        rd[r] = 1.0 / AC(r, r);
+    }
+    __syncwarp();
+    double s = lane < n ? xs[lane] : 0.0;
+    int row = lane;
+    for (int c = 0; c < n; ++c) {
+        const double dc = AC(c, c), rc = rd[c];
+        const double v = row < n ? AC(c, row) : 0.0;
+        double y = 0.0;
+        if (row == c) y = quotient(s, dc, rc);
+        y = __shfl_sync(full, y, c & 31);
+        if (row == c) {
+            xs[c] = y;
+            row += 32;
+            s = row < n ? xs[row] : 0.0;
+        } else if (row < n && row <= c + 2 * band && !is_zero(v)) {
+            s -= v * y;
+        }
+    }
+    __syncwarp();
+    // backward L^T z = y, rows from the last: z_r = y_r - sum over c = r+1..lim[r]
+    // of L(c, r) z_c, in ascending c.  Every lane carries the running sum;
+    // lane j holds z_{r+1+j} (a window shifted by one lane per row) and forms
+    // its product off the critical path; the sum takes the non-zero terms in
+    // order, the first one from z_{r+1} itself.  A row's entries are loaded
+    // while the row before it is summed.
+    double zw = 0.0, zr = 0.0;
+    int tn = lim[n - 1] - (n - 1);
+    double yn = xs[n - 1];
+    double Ln = 0.0;
+    for (int r = n - 1; r >= 0; --r) {
+        const int t = tn;
+        const double yr = yn, L = Ln;
+        if (r > 0) {
+            tn = lim[r - 1] - (r - 1);
+            yn = xs[r - 1];
+            Ln = lane < tn ? AC(r + lane, r - 1) : 0.0;
+        }
+        zw = __shfl_up_sync(full, zw, 1);
+        double zn;
+        if (t <= 32) {
+            const unsigned nzm = __ballot_sync(full, !is_zero(L));
+            const double L0 = __shfl_sync(full, L, 0);
+            const double prod = L * zw;
+            double acc = yr;
+            if (nzm & 1u) acc -= L0 * zr;
+            for (unsigned b = nzm & ~1u; b; b &= b - 1) acc -= __shfl_sync(full, prod, __ffs(b) - 1);
+            zn = acc;
+        } else {
+            // long columns (interchanges carried L far down): the plain sum
+            double acc = yr;
+            for (int cc = r + 1; cc <= lim[r]; ++cc) {
+                const double v = AC(cc, r);
+                if (!is_zero(v)) acc -= v * xs[cc];
+            }
+            zn = acc;
+        }
+        if (lane == 0) {
+            zw = zr;  // z_{r+1} enters the window for the next row's shift
+            if (r + 1 < n) xs[r + 1] = zr;
+        }
+        zr = zn;
+        if (r > 0 && tn > 32) {
+            if (lane == 0) xs[r] = zr;
+            __syncwarp();
+        }
+    }
+    if (lane == 0) {
+        xs[0] = zr;
+        for (int k = n - 1; k >= 0; --k) {
+            const int p = ipiv[k] - 1;
+            if (p != k) {
+                const double t = xs[k];
+                xs[k] = xs[p];
+                xs[p] = t;
+            }
+        }
+    }
+    __syncwarp();
+    for (int r = lane; r < n; r += 32) x[r] = xs[r];
+}
+
+// The general case, one warp: lanes over rows / columns, the rank-1 update
+// over (row, column) pairs of non-zero multiplier and pivot-row entry.
+__device__ void lu_solve_dense(double *A, int lda, int off, int n, int *ipiv, double *x, int band, int *nzr,
+                               int *nzc, int *lim, double *xs) {
+    const int lane = threadIdx.x & 31;
+    for (int k = 0; k < n; ++k) {
+        unsigned long long best = 0;
+        int p = n;
+        const int rend = min(n, k + band + 1), cend = min(n, k + 2 * band + 1);
+        for (int r = k + lane; r < rend; r += 32) {
+            const unsigned long long v = mag_bits(AC(r, k));
+            if (p == n || v > best) { best = v; p = r; }
+        }
+        for (int o = 16; o > 0; o >>= 1) {
+            const unsigned long long ob = __shfl_xor_sync(0xffffffffu, best, o);
+            const int op = __shfl_xor_sync(0xffffffffu, p, o);
+            if (op < n && (p == n || ob > best || (ob == best && op < p))) { best = ob; p = op; }
+        }
+        if (lane == 0) ipiv[k] = p + 1;
+        if (is_zero(AC(p, k))) continue;  // same value on every lane
+        __syncwarp();
+        if (p != k)
+            for (int c = lane; c < n; c += 32) {
+                const double t = AC(k, c);
+                AC(k, c) = AC(p, c);
+                AC(p, c) = t;
+            }
+        __syncwarp();
+        // rows with a non-zero multiplier and columns with a non-zero
+        // pivot-row entry, listed by warp ballots (every lane keeps the
+        // counts)
+        const double inv = 1.0 / AC(k, k);
+        const unsigned below = (1u << lane) - 1u;
+        int cr = 0, cc = 0;
+        for (int r0 = k + 1; r0 < rend; r0 += 32) {
+            const int r = r0 + lane;
+            bool nz = false;
+            if (r < rend) {
+                const double m = AC(r, k) * inv;
+                AC(r, k) = m;
+                nz = !is_zero(m);
+            }
+            const unsigned b = __ballot_sync(0xffffffffu, nz);
+            if (nz) nzr[cr + __popc(b & below)] = r;
+            cr += __popc(b);
+        }
+        for (int c0 = k + 1; c0 < cend; c0 += 32) {
+            const int c = c0 + lane;
+            const bool nz = c < cend && !is_zero(AC(k, c));
+            const unsigned b = __ballot_sync(0xffffffffu, nz);
+            if (nz) nzc[cc + __popc(b & below)] = c;
+            cc += __popc(b);
+        }
+        __syncwarp();
+        for (int t = lane; t < cr * cc; t += 32) {
+            const int r = nzr[t % cr], c = nzc[t / cr];
+            AC(r, c) -= AC(r, k) * AC(k, c);
+        }
+        __syncwarp();
+    }
+    for (int r = lane; r < n; r += 32) xs[r] = x[r];
+    // forward sums start at the first non-zero of each row's range
+    for (int r = lane; r < n; r += 32) {
+        int c = 0;
+        while (c < r && is_zero(AC(c, r))) ++c;
+        lim[r] = c;
+    }
+    __syncwarp();
+    if (lane == 0)
+        for (int r = 0; r < n; ++r) {
+            double s = xs[r];
+            for (int c = lim[r]; c < r; ++c) {
+                const double v = AC(c, r);
+                if (!is_zero(v)) s -= v * xs[c];
+            }
+            xs[r] = s / AC(r, r);
+        }
+    __syncwarp();
+    // backward sums end at the last non-zero
+    for (int r = lane; r < n; r += 32) {
+        int c = n - 1;
+        while (c > r && is_zero(AC(c, r))) --c;
+        lim[r] = c;
+    }
+    __syncwarp();
+    if (lane == 0) {
+        for (int r = n - 1; r >= 0; --r) {
+            double s = xs[r];
+            for (int c = r + 1; c <= lim[r]; ++c) {
+                const double v = AC(c, r);
+                if (!is_zero(v)) s -= v * xs[c];
+            }
+            xs[r] = s;
+        }
+        for (int k = n - 1; k >= 0; --k) { const int p = ipiv[k] - 1; if (p != k) { const double t = xs[k]; xs[k] = xs[p]; xs[p] = t; } }
+    }
+    __syncwarp();
+    for (int r = lane; r < n; r += 32) x[r] = xs[r];
+}
+
+#undef AC
+
 __device__ void lu_solve_block(double *A, int lda, int off, int n, int *ipiv, double *x, int band) {
-#define AC(r, c) A[(size_t)(off + (c)) * lda + (off + (r))]
     __shared__ int nzr[512], nzc[512];
     __shared__ int lim[512];
-    __shared__ double xs[512];
+    __shared__ double xs[512], rd[512];
     if (threadIdx.x < 32) {
-        const int lane = threadIdx.x;
-        for (int k = 0; k < n; ++k) {
-            unsigned long long best = 0;
-            int p = n;
-            const int rend = min(n, k + band + 1), cend = min(n, k + 2 * band + 1);
-            for (int r = k + lane; r < rend; r += 32) {
-                const unsigned long long v = mag_bits(AC(r, k));
-                if (p == n || v > best) { best = v; p = r; }
-            }
-            for (int o = 16; o > 0; o >>= 1) {
-                const unsigned long long ob = __shfl_xor_sync(0xffffffffu, best, o);
-                const int op = __shfl_xor_sync(0xffffffffu, p, o);
-                if (op < n && (p == n || ob > best || (ob == best && op < p))) { best = ob; p = op; }
-            }
-            if (lane == 0) ipiv[k] = p + 1;
-            if (is_zero(AC(p, k))) continue;  // same value on every lane
-            __syncwarp();
-            if (p != k)
-                for (int c = lane; c < n; c += 32) {
-                    const double t = AC(k, c);
-                    AC(k, c) = AC(p, c);
-                    AC(p, c) = t;
-                }
-            __syncwarp();
-            // rows with a non-zero multiplier and columns with a non-zero
-            // pivot-row entry, listed by warp ballots (every lane keeps the
-            // counts)
-            const double inv = 1.0 / AC(k, k);
-            const unsigned below = (1u << lane) - 1u;
-            int cr = 0, cc = 0;
-            for (int r0 = k + 1; r0 < rend; r0 += 32) {
-                const int r = r0 + lane;
-                bool nz = false;
-                if (r < rend) {
-                    const double m = AC(r, k) * inv;
-                    AC(r, k) = m;
-                    nz = !is_zero(m);
-                }
-                const unsigned b = __ballot_sync(0xffffffffu, nz);
-                if (nz) nzr[cr + __popc(b & below)] = r;
-                cr += __popc(b);
-            }
-            for (int c0 = k + 1; c0 < cend; c0 += 32) {
-                const int c = c0 + lane;
-                const bool nz = c < cend && !is_zero(AC(k, c));
-                const unsigned b = __ballot_sync(0xffffffffu, nz);
-                if (nz) nzc[cc + __popc(b & below)] = c;
-                cc += __popc(b);
-            }
-            __syncwarp();
-            // the rank-1 update over (row, column) pairs with a non-zero
-            // multiplier and a non-zero pivot-row entry, one pair per lane
-            for (int t = lane; t < cr * cc; t += 32) {
-                const int r = nzr[t % cr], c = nzc[t / cr];
-                AC(r, c) -= AC(r, k) * AC(k, c);
-            }
-            __syncwarp();
-        }
-        for (int r = lane; r < n; r += 32) xs[r] = x[r];
-        if (2 * band < 32) {
-            // forward U^T y = x with U's rows reaching 2*band right of the
-            // diagonal: each lane keeps one pending row and subtracts a term
-            // as soon as its unknown is known, in ascending order (the serial
-            // order), so a row costs one division and one multiply-subtract
-            // of the whole warp instead of a serial sum on one lane
-            double s = lane < n ? xs[lane] : 0.0;
-            int row = lane;
-            for (int c = 0; c < n; ++c) {
-                double y = 0.0;
-                if (row == c) y = s / AC(c, c);
-                y = __shfl_sync(0xffffffffu, y, c & 31);
-                if (row == c) {
-                    xs[c] = y;
-                    row += 32;
-                    s = row < n ? xs[row] : 0.0;
-                } else if (row < n && row <= c + 2 * band) {
-                    const double v = AC(c, row);
-                    if (!is_zero(v)) s -= v * y;
-                }
-            }
-        } else {
-            // forward sums start at the first non-zero of each row's range
-            for (int r = lane; r < n; r += 32) {
-                int c = 0;
-                while (c < r && is_zero(AC(c, r))) ++c;
-                lim[r] = c;
-            }
-            __syncwarp();
-            if (lane == 0)
-                for (int r = 0; r < n; ++r) {
-                    double s = xs[r];
-                    for (int c = lim[r]; c < r; ++c) {
-                        const double v = AC(c, r);
-                        if (!is_zero(v)) s -= v * xs[c];
-                    }
-                    xs[r] = s / AC(r, r);
-                }
-        }
-        __syncwarp();
-        // backward sums end at the last non-zero
-        for (int r = lane; r < n; r += 32) {
-            int c = n - 1;
-            while (c > r && is_zero(AC(c, r))) --c;
-            lim[r] = c;
-        }
-        __syncwarp();
-        if (lane == 0) {
-            for (int r = n - 1; r >= 0; --r) {
-                double s = xs[r];
-                for (int c = r + 1; c <= lim[r]; ++c) {
-                    const double v = AC(c, r);
-                    if (!is_zero(v)) s -= v * xs[c];
-                }
-                xs[r] = s;
-            }
-            for (int k = n - 1; k >= 0; --k) { const int p = ipiv[k] - 1; if (p != k) { const double t = xs[k]; xs[k] = xs[p]; xs[p] = t; } }
-        }
-        __syncwarp();
-        for (int r = lane; r < n; r += 32) x[r] = xs[r];
+        if (band <= 7) lu_solve_banded<7>(A, lda, off, n, ipiv, x, band, lim, xs, rd);
+        else if (band <= 15) lu_solve_banded<15>(A, lda, off, n, ipiv, x, band, lim, xs, rd);
+        else lu_solve_dense(A, lda, off, n, ipiv, x, band, nzr, nzc, lim, xs);
     }
     __syncthreads();
-#undef AC
+}
+
+// 0.0 + v: v itself, except that -0 becomes +0 (integer work).
+__device__ __forceinline__ double plus_zero(double v) {
+    const long long b = __double_as_longlong(v);
+    return __longlong_as_double(b == (long long)0x8000000000000000ull ? 0ll : b);
+}
+
+// sum over k = 0..5, from +0, of T[k][r] * g(k) in ascending k.  T (Tmat)
+// is block diagonal: rotation blocks {0,1} and {3,4}, ones at 2 and 5.  A
+// term with one of its zeros is an exact zero, and adding an exact zero to
+// the running sum (which starts at +0 and so is never -0) leaves it as it
+// is; a term with one of its ones is g(k) itself.  So the sum is the first
+// block term (+0 + it) plus the second, or g(r) with -0 made +0.
+template <class G>
+__device__ __forceinline__ double tsum(const double T[6][6], int r, G g) {
+    if (r == 2 || r == 5) return plus_zero(g(r));
+    const int k1 = r < 2 ? 0 : 3;
+    return plus_zero(T[k1][r] * g(k1)) + T[k1 + 1][r] * g(k1 + 1);
 }
 
 // Element matrices of FEMElement::forceVector/massMatrix/stiffMatrix
-// (:273-302, :178-213, :218-268), in global coordinates.
-__device__ void element_matrices(const FemKernelArgs &a, int f, int e) {
+// (:273-302, :178-213, :218-268), in global coordinates.  Four threads per
+// element, `part` 0 and 1 forming rows 0-2 and 3-5 of the mass matrix
+// T^T M T (part 0 also the force vector T^T F), parts 2 and 3 those of the
+// stiffness matrix (a row of T^T X T needs only the same row of T^T X).
+// The caller gives a warp one part, so the FP64 work of a warp does not
+// diverge.
+template <int PART>
+__device__ __forceinline__ void element_matrices(const FemKernelArgs &a, int f, int e) {
     const int e0 = a.el_off[f], n0 = a.node_off[f];
     const int ge = e0 + e;
-    const double ang = a.elang[ge], L = a.ellen[ge], L0 = a.len0[ge];
+    const double ang = a.elang[ge], L0 = a.len0[ge];
     const double EE = a.E[ge], A = a.area[ge], I = a.I[ge];
-    const double a1 = a.nang[n0 + e], a2 = a.nang[n0 + e + 1];
-    const double u = (L * L - L0 * L0) / (L + L0);
-    const double t1 = atan2(cos(ang) * sin(a1) - sin(ang) * cos(a1), cos(ang) * cos(a1) + sin(ang) * sin(a1));
-    const double t2 = atan2(cos(ang) * sin(a2) - sin(ang) * cos(a2), cos(ang) * cos(a2) + sin(ang) * sin(a2));
-    const double F0 = (EE * A / L0) * u;
-    const double M1 = (2 * EE * I / L0) * (2.0 * t1 + t2);
-    const double M2 = (2 * EE * I / L0) * (t1 + 2.0 * t2);
-    double F[6] = {-F0, (1.0 / L0) * (M1 + M2), M1, F0, -(1.0 / L0) * (M1 + M2), M2};
     double T[6][6];
     Tmat(ang, T);
-    // internal force in global coordinates, T^T F (the assembly's product)
-    for (int i = 0; i < 6; ++i) {
-        double fg = 0.0;
-        for (int c = 0; c < 6; ++c) fg += T[c][i] * F[c];
-        a.elF[6 * ge + i] = fg;
+    double F[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+    if (PART != 1) {
+        const double L = a.ellen[ge];
+        const double a1 = a.nang[n0 + e], a2 = a.nang[n0 + e + 1];
+        const double u = (L * L - L0 * L0) / (L + L0);
+        const double t1 = atan2(cos(ang) * sin(a1) - sin(ang) * cos(a1), cos(ang) * cos(a1) + sin(ang) * sin(a1));
+        const double t2 = atan2(cos(ang) * sin(a2) - sin(ang) * cos(a2), cos(ang) * cos(a2) + sin(ang) * sin(a2));
+        const double F0 = (EE * A / L0) * u;
+        const double M1 = (2 * EE * I / L0) * (2.0 * t1 + t2);
+        const double M2 = (2 * EE * I / L0) * (t1 + 2.0 * t2);
+        F[0] = -F0; F[1] = (1.0 / L0) * (M1 + M2); F[2] = M1; F[3] = F0; F[4] = -(1.0 / L0) * (M1 + M2); F[5] = M2;
     }
-    // mass
-    double Ml[6][6] = {};
-    const double C1 = a.rho[ge] * A * L0 / 420.0;
-    Ml[0][0] = C1 * 140.0; Ml[0][3] = C1 * 70.0; Ml[1][1] = C1 * 156.0; Ml[1][2] = C1 * 22.0 * L0;
-    Ml[1][4] = C1 * 54; Ml[1][5] = C1 * (-13.0 * L0); Ml[2][2] = C1 * 4.0 * (L0 * L0); Ml[2][4] = C1 * 13.0 * L0;
-    Ml[2][5] = C1 * (-3.0 * (L0 * L0)); Ml[3][3] = C1 * 140.0; Ml[4][4] = C1 * 156.0; Ml[4][5] = C1 * (-22.0 * L0);
-    Ml[5][5] = C1 * 4.0 * (L0 * L0);
+    if (PART == 0)
+        // internal force in global coordinates, T^T F (the assembly's product)
+#pragma unroll
+        for (int i = 0; i < 6; ++i) a.elF[6 * ge + i] = tsum(T, i, [&](int c) { return F[c]; });
+    double X[6][6] = {};
+    if (PART < 2) {
+        // mass
+        const double C1 = a.rho[ge] * A * L0 / 420.0;
+        X[0][0] = C1 * 140.0; X[0][3] = C1 * 70.0; X[1][1] = C1 * 156.0; X[1][2] = C1 * 22.0 * L0;
+        X[1][4] = C1 * 54; X[1][5] = C1 * (-13.0 * L0); X[2][2] = C1 * 4.0 * (L0 * L0); X[2][4] = C1 * 13.0 * L0;
+        X[2][5] = C1 * (-3.0 * (L0 * L0)); X[3][3] = C1 * 140.0; X[4][4] = C1 * 156.0; X[4][5] = C1 * (-22.0 * L0);
+        X[5][5] = C1 * 4.0 * (L0 * L0);
+    } else {
+        // stiffness (linear + geometric)
+        X[0][0] = EE * A / L0; X[0][3] = -EE * A / L0;
+        X[1][1] = 12.0 * EE * I / (L0 * L0 * L0); X[1][2] = 6.0 * EE * I / (L0 * L0);
+        X[1][4] = -12.0 * EE * I / (L0 * L0 * L0); X[1][5] = 6.0 * EE * I / (L0 * L0);
+        X[2][2] = 4.0 * EE * I / L0; X[2][4] = -6.0 * EE * I / (L0 * L0); X[2][5] = 2.0 * EE * I / L0;
+        X[3][3] = EE * A / L0; X[4][4] = 12.0 * EE * I / (L0 * L0 * L0); X[4][5] = -6.0 * EE * I / (L0 * L0);
+        X[5][5] = 4.0 * EE * I / L0;
+    }
+#pragma unroll
     for (int i = 1; i < 6; i++)
-        for (int j = 0; j < i; j++) Ml[i][j] = Ml[j][i];
-    // stiffness (linear + geometric)
-    double Kl[6][6] = {};
-    Kl[0][0] = EE * A / L0; Kl[0][3] = -EE * A / L0;
-    Kl[1][1] = 12.0 * EE * I / (L0 * L0 * L0); Kl[1][2] = 6.0 * EE * I / (L0 * L0);
-    Kl[1][4] = -12.0 * EE * I / (L0 * L0 * L0); Kl[1][5] = 6.0 * EE * I / (L0 * L0);
-    Kl[2][2] = 4.0 * EE * I / L0; Kl[2][4] = -6.0 * EE * I / (L0 * L0); Kl[2][5] = 2.0 * EE * I / L0;
-    Kl[3][3] = EE * A / L0; Kl[4][4] = 12.0 * EE * I / (L0 * L0 * L0); Kl[4][5] = -6.0 * EE * I / (L0 * L0);
-    Kl[5][5] = 4.0 * EE * I / L0;
-    for (int i = 1; i < 6; i++)
-        for (int j = 0; j < i; j++) Kl[i][j] = Kl[j][i];
-    const double Fa = -F[0], V0 = F[4];
-    Kl[0][1] += -V0 / L0; Kl[0][4] += V0 / L0; Kl[1][0] += -V0 / L0; Kl[1][1] += Fa / L0;
-    Kl[1][3] += V0 / L0; Kl[1][4] += -Fa / L0; Kl[3][1] += V0 / L0; Kl[3][4] += -V0 / L0;
-    Kl[4][0] += V0 / L0; Kl[4][1] += -Fa / L0; Kl[4][3] += -V0 / L0; Kl[4][4] += Fa / L0;
-    // T^T X T with the reference's k-ordered products
-    for (int which = 0; which < 2; ++which) {
-        double (*X)[6] = which == 0 ? Ml : Kl;
-        double P[6][6];
-        for (int r = 0; r < 6; ++r)
-            for (int c = 0; c < 6; ++c) {
-                double s = 0.0;
-                for (int k = 0; k < 6; ++k) s += T[k][r] * X[k][c];
-                P[r][c] = s;
-            }
-        double *out = which == 0 ? a.elM + 36 * (size_t)ge : a.elK + 36 * (size_t)ge;
-        for (int r = 0; r < 6; ++r)
-            for (int c = 0; c < 6; ++c) {
-                double s = 0.0;
-                for (int k = 0; k < 6; ++k) s += P[r][k] * T[k][c];
-                out[6 * r + c] = s;
-            }
+#pragma unroll
+        for (int j = 0; j < i; j++) X[i][j] = X[j][i];
+    if (PART >= 2) {
+        const double Fa = -F[0], V0 = F[4];
+        X[0][1] += -V0 / L0; X[0][4] += V0 / L0; X[1][0] += -V0 / L0; X[1][1] += Fa / L0;
+        X[1][3] += V0 / L0; X[1][4] += -Fa / L0; X[3][1] += V0 / L0; X[3][4] += -V0 / L0;
+        X[4][0] += V0 / L0; X[4][1] += -Fa / L0; X[4][3] += -V0 / L0; X[4][4] += Fa / L0;
+    }
+    // rows r0..r0+2 of T^T X T with the reference's k-ordered products
+    constexpr int r0 = 3 * (PART & 1);
+    double *out = (PART < 2 ? a.elM : a.elK) + 36 * (size_t)ge;
+#pragma unroll
+    for (int rr = 0; rr < 3; ++rr) {
+        const int r = r0 + rr;
+        double P[6];
+#pragma unroll
+        for (int c = 0; c < 6; ++c) P[c] = tsum(T, r, [&](int k) { return X[k][c]; });
+#pragma unroll
+        for (int c = 0; c < 6; ++c) out[6 * r + c] = tsum(T, c, [&](int k) { return P[k]; });
     }
 }
 
@@ -369,6 +569,7 @@ __global__ void k_fem_dynamic(FemKernelArgs a) {
     double *K = a.k_in_smem ? fem_smem : a.K + (size_t)f * a.maxdof * a.maxdof;
     double *Meff = a.tmp + 2 * (size_t)d0, *MF = a.tmp + 2 * (size_t)d0 + nd;
     __shared__ int ipiv[512];
+    __shared__ double sq[512];
     __shared__ int go;
     const double Dt = a.dt;
     for (int i = threadIdx.x; i < nd; i += blockDim.x) {
@@ -385,7 +586,13 @@ __global__ void k_fem_dynamic(FemKernelArgs a) {
     int it = 0;
     double res = 0.0;
     do {
-        for (int e = threadIdx.x; e < ne; e += blockDim.x) element_matrices(a, f, e);
+        for (int t = threadIdx.x; t < 4 * ne; t += blockDim.x) {
+            const int part = t / ne, e = t - part * ne;
+            if (part == 0) element_matrices<0>(a, f, e);
+            else if (part == 1) element_matrices<1>(a, f, e);
+            else if (part == 2) element_matrices<2>(a, f, e);
+            else element_matrices<3>(a, f, e);
+        }
         for (int q = threadIdx.x; q < nd * nd; q += blockDim.x) {
             M[q] = 0.0;
             K[q] = 0.0;
@@ -439,12 +646,18 @@ __global__ void k_fem_dynamic(FemKernelArgs a) {
         lu_solve_block(K, nd, bc, nd - bc, ipiv, a.delU + d0 + bc, 5);
         for (int i = threadIdx.x; i < bc; i += blockDim.x) a.delU[d0 + i] = 0.0;
         __syncthreads();
-        for (int i = threadIdx.x; i < nd; i += blockDim.x) a.U[d0 + i] = a.U[d0 + i] + a.delU[d0 + i];
+        // the squares of the residual's sum formed densely beforehand; one
+        // thread adds them in order
+        for (int i = threadIdx.x; i < nd; i += blockDim.x) {
+            const double du = a.delU[d0 + i];
+            a.U[d0 + i] = a.U[d0 + i] + du;
+            sq[i] = du * du;
+        }
         __syncthreads();
         update_values(a, f);
         if (threadIdx.x == 0) {
             double dp = 0.0;
-            for (int i = 0; i < nd; i++) dp += a.delU[d0 + i] * a.delU[d0 + i];
+            for (int i = 0; i < nd; i++) dp += sq[i];
             const double L = a.len0[e0] * ne;
             res = sqrt(dp / (double)nd) / L;
             go = (res > 1e-10 && it + 1 < 20) ? 1 : 0;
@@ -513,6 +726,23 @@ __device__ double delta_kernel_d(double radius, double dilation) {
 
 // Supports, ds and epsilon of one filament's markers (ibm_findSupport,
 // ibm_computeDs, ibm_findEpsilon for a moving body).
+//
+// A marker's supports are the nodes of its cage: per axis the five
+// candidate coordinates around its near node (offsets -2..2), each with the
+// cage test |X - x|/dh < 1.5, the domain test and its kernel value; a
+// support node's coordinates, tests and delta are combinations of these.
+// So the kernel first forms every marker's cage record (x.cage: the 15
+// coordinates and 15 kernel values; x.cagei: the near node and the test
+// bits), one thread per (marker, axis, offset); then lists each marker's
+// supports in the reference's order (the near node, then the cage nodes in
+// (i, j, k) order); then forms ds over marker pairs; then each epsilon entry
+// (I, J) evaluates J's kernel at I's candidate coordinates and sums
+// delta_I * phi_J over I's supports in the same order.  Every value is the
+// same expression on the same operands as node by node.
+constexpr int kEpsChunk = 2048;  // epsilon entries tested per round
+
+__device__ __forceinline__ bool cage_ok(unsigned fl, int d, int o) { return ((fl >> (5 * d + o)) & 1u) != 0; }
+
 __global__ void k_flex_support(FemKernelArgs a) {
     const int f = blockIdx.x;
     if (f >= a.nfil || (a.skip && *a.skip)) return;
@@ -520,41 +750,52 @@ __global__ void k_flex_support(FemKernelArgs a) {
     const int D = a.dims;
     const double dh = a.dh;
     const FlexArgs &x = a.flex;
+    // near node per (marker, axis); the test bits start clear, ds at 10
+    for (int q = threadIdx.x; q < 3 * nmk; q += blockDim.x) {
+        const int m = q / 3, d = q % 3, g = mk0 + m;
+        x.cagei[4 * g + d] = d < D ? (int)floor((x.pos[3 * g + d] - a.gstart[d]) / dh) : 0;
+        if (d == 0) {
+            x.cagei[4 * g + 3] = 0;
+            x.ds[g] = 10.0;
+        }
+    }
+    __syncthreads();
+    // cage record per (marker, axis, offset)
+    for (int q = threadIdx.x; q < 15 * nmk; q += blockDim.x) {
+        const int m = q / 15, w = q % 15, d = w / 5, o = w % 5, g = mk0 + m;
+        const int *ni = &x.cagei[4 * g];
+        if (ni[0] < 0 || ni[1] < 0 || ni[2] < 0 || ni[0] >= a.N || ni[1] >= a.M_ || ni[2] >= a.K_) continue;
+        const bool act = d < D;
+        const double *h = d == 0 ? a.hx : d == 1 ? a.hy : a.hz;
+        const double nearp = act ? h[ni[d]] : 0.0;
+        const double p = x.pos[3 * g + d];
+        const double e = act ? nearp + (o - 2) * dh : nearp;
+        const bool cage = !act || fabs(p - e) / dh < 1.5;
+        const bool dom = !act || !(e < a.edges[2 * d] || e > a.edges[2 * d + 1]);
+        x.cage[32 * (size_t)g + w] = e;
+        x.cage[32 * (size_t)g + 15 + w] = act ? delta_kernel_d((e - p) / dh, 1.0) : 1.0;
+        if (cage && dom) atomicOr(&x.cagei[4 * g + 3], 1 << w);
+    }
+    __syncthreads();
+    // support lists
     for (int m = threadIdx.x; m < nmk; m += blockDim.x) {
         const int g = mk0 + m;
-        const double *p = &x.pos[3 * g];
-        const int in = (int)floor((p[0] - a.gstart[0]) / dh);
-        const int jn = (int)floor((p[1] - a.gstart[1]) / dh);
-        const int kn = D == 3 ? (int)floor((p[2] - a.gstart[2]) / dh) : 0;
-        int ns = 0;
+        const int in = x.cagei[4 * g], jn = x.cagei[4 * g + 1], kn = x.cagei[4 * g + 2];
+        const unsigned fl = (unsigned)x.cagei[4 * g + 3];
         if (in < 0 || jn < 0 || kn < 0 || in >= a.N || jn >= a.M_ || kn >= a.K_) {
             atomicExch(a.error, 1);
             x.nsupp[g] = 0;
             continue;
         }
-        const double nearp[3] = {a.hx[in], a.hy[jn], D == 3 ? a.hz[kn] : 0.0};
-        // Per axis, the five candidate node coordinates around the near node
-        // (offsets -2..2), their cage and domain tests and their kernel
-        // values: every support's test and delta is a combination of these,
-        // evaluated with the same expressions as node by node.
-        double ec[3][5], ph[3][5];
-        bool cage[3][5], dom[3][5];
-        for (int d = 0; d < 3; ++d)
-            for (int o = 0; o < 5; ++o) {
-                const bool act = d < D;
-                const double e = act ? nearp[d] + (o - 2) * dh : nearp[d];
-                ec[d][o] = e;
-                cage[d][o] = !act || fabs(p[d] - e) / dh < 1.5;
-                dom[d][o] = !act || !(e < a.edges[2 * d] || e > a.edges[2 * d + 1]);
-                ph[d][o] = act ? delta_kernel_d((e - p[d]) / dh, 1.0) : 1.0;
-            }
+        const double *rec = &x.cage[32 * (size_t)g];
+        int ns = 0;
         auto add = [&](int i, int j, int k, int oi, int oj, int ok) {
             if (ns >= kFlexMaxSupp) { atomicExch(a.error, 2); return; }
             const int s = g * kFlexMaxSupp + ns;
             x.supp[s] = k + j * a.K_ + i * a.K_ * a.M_;
-            x.sx[s] = ec[0][oi]; x.sy[s] = ec[1][oj]; x.sz[s] = ec[2][ok];
-            double v = ph[0][oi] * ph[1][oj];
-            if (D == 3) v = v * ph[2][ok];
+            x.sx[s] = rec[oi]; x.sy[s] = rec[5 + oj]; x.sz[s] = rec[10 + ok];
+            double v = rec[15 + oi] * rec[20 + oj];
+            if (D == 3) v = v * rec[25 + ok];
             x.delta[s] = v;
             ++ns;
         };
@@ -566,8 +807,7 @@ __global__ void k_flex_support(FemKernelArgs a) {
             for (int oj = 0; oj < 5; oj++)
                 for (int ok = (D == 3 ? 0 : 2); ok <= (D == 3 ? 4 : 2); ok++) {
                     const int i = in + oi - 2, j = jn + oj - 2, k = kn + ok - 2;
-                    if (cage[0][oi] && cage[1][oj] && cage[2][ok] && dom[0][oi] && dom[1][oj] && dom[2][ok] &&
-                        (oi != 2 || oj != 2 || ok != 2)) {
+                    if (cage_ok(fl, 0, oi) && cage_ok(fl, 1, oj) && cage_ok(fl, 2, ok) && (oi != 2 || oj != 2 || ok != 2)) {
                         if (i < 0 || j < 0 || k < 0 || i >= a.N || j >= a.M_ || k >= a.K_) {
                             atomicExch(a.error, 1);
                             continue;
@@ -577,58 +817,89 @@ __global__ void k_flex_support(FemKernelArgs a) {
                 }
         x.nsupp[g] = ns;
     }
-    __syncthreads();
-    for (int m = threadIdx.x; m < nmk; m += blockDim.x) {
-        const int g = mk0 + m;
-        double ds = 10.0;
-        for (int q = 0; q < nmk; ++q) {
-            if (q == m) continue;
-            double r = 0.0;
-            for (int d = 0; d < 3; ++d) {
-                const double v = x.pos[3 * g + d] - x.pos[3 * (mk0 + q) + d];
-                r += v * v;
-            }
-            const double dist = sqrt(r) / dh;
-            if (dist < ds) ds = dist;
+    // ds: the smallest distance to another marker of the filament, in dh
+    // (10 when none is nearer); a minimum of non-negative doubles is the
+    // minimum of their bit patterns
+    for (int q = threadIdx.x; q < nmk * nmk; q += blockDim.x) {
+        const int m = q / nmk, o = q % nmk;
+        if (m == o) continue;
+        const int g = mk0 + m, h = mk0 + o;
+        double r = 0.0;
+        for (int d = 0; d < 3; ++d) {
+            const double v = x.pos[3 * g + d] - x.pos[3 * h + d];
+            r += v * v;
         }
-        x.ds[g] = ds;
+        const double dist = sqrt(r) / dh;
+        if (dist < 10.0)
+            atomicMin(reinterpret_cast<unsigned long long *>(&x.ds[g]), (unsigned long long)__double_as_longlong(dist));
     }
     __syncthreads();
     extern __shared__ double flex_smem[];
     double *A = a.eps_in_smem ? flex_smem : a.epsA + (size_t)f * a.maxmk * a.maxmk;
-    for (int q = threadIdx.x; q < nmk * nmk; q += blockDim.x) {
-        const int I = q / nmk, J = q % nmk;
-        const int gI = mk0 + I, gJ = mk0 + J;
-        double aij = 0.0;
-        // markers more than 3 dh apart on an axis share no support node: every
-        // term is an exact zero and the entry stays +0
-        bool near = true;
-        for (int d = 0; d < D; ++d) near = near && fabs(x.pos[3 * gI + d] - x.pos[3 * gJ + d]) <= 3.01 * dh;
-        // I's support nodes take a few coordinates per axis: the kernel of J
-        // at each distinct coordinate is evaluated once and reused (the same
-        // expression on the same operands, so the same value)
-        double cv[3][6], fv[3][6];
-        int nc[3] = {0, 0, 0};
-        const double XJ[3] = {x.pos[3 * gJ + 0], x.pos[3 * gJ + 1], x.pos[3 * gJ + 2]};
-        auto phi_at = [&](int d, double v) -> double {
-            const long long b = __double_as_longlong(v);
-            for (int t = 0; t < nc[d]; ++t)
-                if (__double_as_longlong(cv[d][t]) == b) return fv[d][t];
-            const double r = delta_kernel_d((XJ[d] - v) / dh, 1.0);
-            if (nc[d] < 6) {
-                cv[d][nc[d]] = v;
-                fv[d][nc[d]] = r;
-                ++nc[d];
-            }
-            return r;
-        };
-        for (int s = 0; near && s < x.nsupp[gI]; ++s) {
-            const int si = gI * kFlexMaxSupp + s;
-            double dJ = phi_at(0, x.sx[si]) * phi_at(1, x.sy[si]);
-            if (D == 3) dJ = dJ * phi_at(2, x.sz[si]);
-            aij += x.delta[si] * dJ * 1.0;
+    // Entries in chunks: each thread tests its share of a chunk, writes the
+    // entries of markers more than 3 dh apart on an axis (they share no
+    // support node: every term is an exact zero and the entry stays +0)
+    // and lists the others, which are then evaluated one per lane, densely.
+    __shared__ int near_list[kEpsChunk];
+    __shared__ int near_count;
+    for (int q0 = 0; q0 < nmk * nmk; q0 += kEpsChunk) {
+        if (threadIdx.x == 0) near_count = 0;
+        __syncthreads();
+        for (int q = q0 + threadIdx.x; q < min(nmk * nmk, q0 + kEpsChunk); q += blockDim.x) {
+            const int I = q / nmk, J = q % nmk;
+            const int gI = mk0 + I, gJ = mk0 + J;
+            bool near = x.nsupp[gI] > 0;
+            for (int d = 0; d < D; ++d) near = near && fabs(x.pos[3 * gI + d] - x.pos[3 * gJ + d]) <= 3.01 * dh;
+            if (near) near_list[atomicAdd(&near_count, 1)] = q;
+            else A[(size_t)I * nmk + J] = 0.0 * x.ds[gJ];
         }
-        A[(size_t)I * nmk + J] = aij * x.ds[gJ];
+        __syncthreads();
+        for (int t = threadIdx.x; t < near_count; t += blockDim.x) {
+            const int q = near_list[t];
+            const int I = q / nmk, J = q % nmk;
+            const int gI = mk0 + I, gJ = mk0 + J;
+            double aij = 0.0;
+            const double *rec = &x.cage[32 * (size_t)gI];
+            const unsigned fl = (unsigned)x.cagei[4 * gI + 3];
+            const int ni[3] = {x.cagei[4 * gI], x.cagei[4 * gI + 1], x.cagei[4 * gI + 2]};
+            double ph[15], fj[15];
+#pragma unroll
+            for (int w = 0; w < 15; ++w) ph[w] = rec[15 + w];
+            // J's kernel at I's candidate coordinates (those a support uses)
+#pragma unroll
+            for (int w = 0; w < 15; ++w) {
+                const int d = w / 5;
+                fj[w] = 0.0;
+                if (d < D && (w % 5 == 2 || cage_ok(fl, d, w % 5)))
+                    fj[w] = delta_kernel_d((x.pos[3 * gJ + d] - rec[w]) / dh, 1.0);
+            }
+            int ns = 0;
+            auto term = [&](int oi, int oj, int ok) {
+                if (ns >= kFlexMaxSupp) return;
+                double dl = ph[oi] * ph[5 + oj];
+                if (D == 3) dl = dl * ph[10 + ok];
+                double dJ = fj[oi] * fj[5 + oj];
+                if (D == 3) dJ = dJ * fj[10 + ok];
+                aij += dl * dJ * 1.0;
+                ++ns;
+            };
+            term(2, 2, 2);
+#pragma unroll
+            for (int oi = 0; oi < 5; oi++)
+#pragma unroll
+                for (int oj = 0; oj < 5; oj++)
+#pragma unroll
+                    for (int ok = 0; ok < 5; ok++) {
+                        if (D != 3 && ok != 2) continue;
+                        const int i = ni[0] + oi - 2, j = ni[1] + oj - 2, k = ni[2] + ok - 2;
+                        if (cage_ok(fl, 0, oi) && cage_ok(fl, 1, oj) && cage_ok(fl, 2, ok) &&
+                            (oi != 2 || oj != 2 || ok != 2) && !(i < 0 || j < 0 || k < 0 || i >= a.N ||
+                                                                 j >= a.M_ || k >= a.K_))
+                            term(oi, oj, ok);
+                    }
+            A[(size_t)I * nmk + J] = aij * x.ds[gJ];
+        }
+        __syncthreads();
     }
     __shared__ int ipiv[512];
     __shared__ int band;
@@ -820,7 +1091,8 @@ int luma_fem_upload(luma_gpu_grid *g) {
         (rc = zeros(&x.irho, nmk)) || (rc = zeros(&x.imom, 3 * (size_t)nmk)) || (rc = zeros(&x.nsupp, nmk)) ||
         (rc = zeros(&x.supp, (size_t)nmk * kFlexMaxSupp)) || (rc = zeros(&x.delta, (size_t)nmk * kFlexMaxSupp)) ||
         (rc = zeros(&x.sx, (size_t)nmk * kFlexMaxSupp)) || (rc = zeros(&x.sy, (size_t)nmk * kFlexMaxSupp)) ||
-        (rc = zeros(&x.sz, (size_t)nmk * kFlexMaxSupp)))
+        (rc = zeros(&x.sz, (size_t)nmk * kFlexMaxSupp)) || (rc = zeros(&x.cage, 32 * (size_t)nmk)) ||
+        (rc = zeros(&x.cagei, 4 * (size_t)nmk)))
         return rc;
     FemScratch sc;
     if ((rc = zeros(&sc.elF, 6 * (size_t)nel)) || (rc = zeros(&sc.elM, 36 * (size_t)nel)) ||
@@ -867,7 +1139,7 @@ int luma_fem_supports(luma_gpu_grid *g, const int *skip) {
     const FemDevice &d = g->ibm->fem;
     a.eps_in_smem = d.eps_in_smem;
     const size_t eb = (size_t)a.maxmk * a.maxmk * sizeof(double);
-    k_flex_support<<<a.nfil, 128, a.eps_in_smem ? eb : 0, g->stream>>>(a);
+    k_flex_support<<<a.nfil, 256, a.eps_in_smem ? eb : 0, g->stream>>>(a);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return luma_set_error(LUMA_E_CUDA, "flex support: %s", cudaGetErrorString(e));
     return LUMA_OK;
@@ -958,7 +1230,7 @@ void luma_fem_free(luma_gpu_grid *g) {
                     d.Ud_n, d.Udd, d.Udd_n, d.R, d.Fv, d.delU, d.M, d.K, d.epsA, d.parent_el, d.parent_zeta,
                     d.mpos0, d.it, d.res, d.fsi_res, d.fsi_state, d.flex.pos, d.flex.vel, d.flex.vel_km1, d.flex.F, d.flex.eps,
                     d.flex.ds, d.flex.irho, d.flex.imom, d.flex.nsupp, d.flex.supp, d.flex.delta, d.flex.sx,
-                    d.flex.sy, d.flex.sz, g->ibm->u_n};
+                    d.flex.sy, d.flex.sz, d.flex.cage, d.flex.cagei, g->ibm->u_n};
     for (void *p : ptrs) cudaFree(p);
     d = FemDevice();
     g->ibm->u_n = nullptr;

@@ -138,6 +138,8 @@ struct FlexArgs {
     double *pos, *vel, *vel_km1, *F, *eps, *ds, *irho, *imom;  // per marker (3 for pos/vel/F/imom)
     int *nsupp, *supp;          // supp[m*kFlexMaxSupp + s] = site id
     double *delta, *sx, *sy, *sz;
+    double *cage;               // per marker: 15 candidate coordinates, 15 kernel values (axis-major, offsets -2..2)
+    int *cagei;                 // per marker: near node (3), cage-and-domain test bits (bit 5*axis + offset)
 };
 
 struct FemDevice {

@@ -56,16 +56,25 @@ __device__ __forceinline__ void stream_site(const StepArgs &a, const int8_t *wal
         nv1 = wall[4 * (size_t)id + 1];
         nv2 = wall[4 * (size_t)id + 2];
     }
+    // every source site's label first (independent loads, all in flight at
+    // once), then the per-direction rules, whose loads do not wait on each
+    // other either
+    int sidv[Q], stv[Q];
 #pragma unroll
     for (int v = 0; v < Q; ++v) {
-        const int cx = L::c(v, 0), cy = L::c(v, 1), cz = L::c(v, 2);
-        int sx = i - cx, sy = j - cy, sz = k - cz;
+        int sx = i - L::c(v, 0), sy = j - L::c(v, 1), sz = k - L::c(v, 2);
         sx = sx < 0 ? sx + N : (sx >= N ? sx - N : sx);
         sy = sy < 0 ? sy + M : (sy >= M ? sy - M : sy);
         if (D == 3) sz = sz < 0 ? sz + K : (sz >= K ? sz - K : sz);
         else sz = 0;
-        const int sid = sz + sy * K + sx * K * M;
-        const int stype = a.typ[sid];
+        sidv[v] = sz + sy * K + sx * K * M;
+        stv[v] = a.typ[sidv[v]];
+    }
+#pragma unroll
+    for (int v = 0; v < Q; ++v) {
+        const int cx = L::c(v, 0), cy = L::c(v, 1), cz = L::c(v, 2);
+        const int sid = sidv[v];
+        const int stype = stv[v];
         if (type == LUMA_SITE_BFL || stype == LUMA_SITE_BFL) {
             // _LBM_applyBFL_opt (:1010-1113) through the link tables
             // (kinds in bfl.cu); links without a wall stream as usual
@@ -131,7 +140,10 @@ __device__ __forceinline__ void stream_site(const StepArgs &a, const int8_t *wal
             fn[v] = feq_s<Q, P>(v, rs, rs - R(a.rho0), ux, uy, uz, R(a.cs2));
         } else if (a.parent_f && stype == LUMA_SITE_TL_TO_COARSER && a.subcycle == 0) {
             // _LBM_explode_opt (:646-663) with GridUtils::getCoarseIndices.
-            int fx = sx, fy = sy, fz = sz;
+            int fx = i - cx, fy = j - cy, fz = D == 3 ? k - cz : 0;
+            fx = fx < 0 ? fx + N : (fx >= N ? fx - N : fx);
+            fy = fy < 0 ? fy + M : (fy >= M ? fy - M : fy);
+            if (D == 3) fz = fz < 0 ? fz + K : (fz >= K ? fz - K : fz);
             if (fx % 2 != 0) fx -= 1;
             if (fy % 2 != 0) fy -= 1;
             if (fz % 2 != 0) fz -= 1;
@@ -729,44 +741,71 @@ __global__ void __launch_bounds__(128) k_force_collide_list(StepArgs a, const in
 
 // ---- immersed boundary pass (ObjectManager::ibm_apply, src/ObjectManager_ops_ibm.cpp:33-54) ----
 
-// ibm_interpolate (:498-591) + ibm_computeForce (:598-614), one warp per
-// marker: the lanes gather the marker's supports in parallel, then every
-// lane adds the terms in support order with the reference's rounding (each
-// term rs*dl*A and rs*u*dl*A rounded, then added; no fused multiply-add),
-// so the sums are the reference's FP64 sums.
+// ibm_interpolate (:498-591) + ibm_computeForce (:598-614) for 32 markers
+// per block.  GB300 runs an FP64 instruction of a warp in 64 cycles of its
+// SM sub-partition whatever the number of active lanes, so the kernel keeps
+// every FP64 instruction dense: each warp forms the products of 8 markers
+// with its lanes over a marker's supports (each term rs*dl*A and rs*u*dl*A
+// rounded as the reference rounds it, no fused multiply-add) and parks them
+// in shared memory; then warp q sums quantity q (rho, then each momentum
+// component) for the 32 markers, lane = marker, in support order, so the
+// sums are the reference's FP64 sums.  Supports beyond 32 per marker come
+// in further rounds of the same two phases.
+constexpr int kInterpMarkers = 32;
+
 template <int Q, class P>
-__global__ void k_ibm_interp_force(StepArgs a, IbmArgs b) {
+__global__ void __launch_bounds__(128) k_ibm_interp_force(StepArgs a, IbmArgs b) {
     if (a.skip && *a.skip) return;  // a converged FSI loop: later sub-iterations do nothing
     constexpr int D = Lattice<Q>::D;
-    const int lane = threadIdx.x & 31;
-    const int m = (int)(((size_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5);
-    if (m >= b.nm) return;                              // whole warps leave together
+    __shared__ double prod[kInterpMarkers][32][4];
+    __shared__ double sums[4][kInterpMarkers];
+    __shared__ int rounds;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int m0 = blockIdx.x * kInterpMarkers;
     const size_t n = (size_t)a.ncell;
-    double r = 0.0, mom[3] = {0.0, 0.0, 0.0};
-    const double A = b.area[m];
-    const int s0 = b.moff[m], s1 = b.moff[m + 1];
-    for (int base = s0; base < s1; base += 32) {
-        const int s = base + lane;
-        double pr = 0.0, pm[3] = {0.0, 0.0, 0.0};
-        if (s < s1) {
-            const int id = b.msite[s];
-            const double rs = double(ldr<P>(a.rho, id));
-            const double dl = b.mdelta[s];
-            pr = __dmul_rn(__dmul_rn(rs, dl), A);
-            for (int d = 0; d < D; ++d)
-                pm[d] = __dmul_rn(__dmul_rn(__dmul_rn(rs, double(ldr<P>(a.u, (size_t)d * n + id))), dl), A);
-        }
-        const int cnt = s1 - base < 32 ? s1 - base : 32;
-        for (int t = 0; t < cnt; ++t) {
-            r = __dadd_rn(r, __shfl_sync(0xffffffffu, pr, t));
-            for (int d = 0; d < D; ++d) mom[d] = __dadd_rn(mom[d], __shfl_sync(0xffffffffu, pm[d], t));
-        }
+    if (threadIdx.x < 32) {
+        const int m = m0 + lane;
+        const int cnt = m < b.nm ? b.moff[m + 1] - b.moff[m] : 0;
+        int mx = cnt;
+        for (int o = 16; o > 0; o >>= 1) mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+        if (lane == 0) rounds = (mx + 31) / 32;
     }
-    if (lane != 0) return;
-    b.irho[m] = r;
+    __syncthreads();
+    double acc = 0.0;  // quantity w of marker m0 + lane
+    for (int r = 0; r < rounds; ++r) {
+#pragma unroll 2
+        for (int i = 0; i < kInterpMarkers / 4; ++i) {
+            const int ml = (kInterpMarkers / 4) * w + i, m = m0 + ml;
+            if (m >= b.nm) break;
+            const int s = b.moff[m] + 32 * r + lane;
+            if (s < b.moff[m + 1]) {
+                const int id = b.msite[s];
+                const double rs = double(ldr<P>(a.rho, id));
+                const double dl = b.mdelta[s];
+                const double A = b.area[m];
+                prod[ml][lane][0] = __dmul_rn(__dmul_rn(rs, dl), A);
+                for (int d = 0; d < D; ++d)
+                    prod[ml][lane][1 + d] = __dmul_rn(__dmul_rn(__dmul_rn(rs, double(ldr<P>(a.u, (size_t)d * n + id))), dl), A);
+            }
+        }
+        __syncthreads();
+        const int m = m0 + lane;
+        if (w <= D && m < b.nm) {
+            const int cnt = b.moff[m + 1] - b.moff[m] - 32 * r;
+            for (int t = 0; t < (cnt < 32 ? cnt : 32); ++t) acc = __dadd_rn(acc, prod[lane][t][w]);
+        }
+        __syncthreads();
+    }
+    if (w <= D) sums[w][lane] = acc;
+    __syncthreads();
+    const int m = m0 + lane;
+    if (w != 0 || m >= b.nm) return;
+    const double rsum = sums[0][lane];
+    b.irho[m] = rsum;
     for (int d = 0; d < D; ++d) {
-        b.imom[3 * m + d] = mom[d];
-        b.F[3 * m + d] = 2.0 * (mom[d] - r * b.vel[3 * m + d]) / 1.0;
+        const double mom = sums[1 + d][lane];
+        b.imom[3 * m + d] = mom;
+        b.F[3 * m + d] = 2.0 * (mom - rsum * b.vel[3 * m + d]) / 1.0;
     }
     if (a.ibm_f_out)
         for (int d = 0; d < 3; ++d) a.ibm_f_out[3 * m + d] = b.F[3 * m + d];
@@ -905,7 +944,7 @@ __global__ void k_flex_remacro(StepArgs a, FlexArgs f) {
 template <int Q, class P>
 cudaError_t launch_ibm_pass(const StepArgs &a, const IbmArgs &b, const FlexArgs &f, cudaStream_t s) {
     const int nt = f.nm * kFlexMaxSupp;
-    if (b.nm > 0) k_ibm_interp_force<Q, P><<<(unsigned)(((size_t)b.nm * 32 + 127) / 128), 128, 0, s>>>(a, b);
+    if (b.nm > 0) k_ibm_interp_force<Q, P><<<(b.nm + kInterpMarkers - 1) / kInterpMarkers, 128, 0, s>>>(a, b);
     if (f.nm > 0) k_flex_interp_force<Q, P><<<(f.nm + 127) / 128, 128, 0, s>>>(a, f);
     if (b.nm > 0) k_ibm_spread<Q, P><<<(b.nu + 127) / 128, 128, 0, s>>>(a, b);
     if (f.nm > 0) k_flex_spread<Q, P><<<(nt + 127) / 128, 128, 0, s>>>(a, f);
