@@ -242,6 +242,7 @@ int luma_build_interior(luma_gpu_grid *g) {
     g->fast = nullptr;
     g->gen_ids = nullptr;
     g->ngen = 0;
+    g->ngen_early = 0;
     if (g->bulk || (g->n < kInteriorMinSites && !(g->d.flags & LUMA_FLAG_SPLIT_INTERIOR))) return LUMA_OK;
     const luma_grid_desc &d = g->d;
     const int N = d.N, M = d.M, K = d.K, Q = d.Q;
@@ -249,7 +250,7 @@ int luma_build_interior(luma_gpu_grid *g) {
     std::vector<int> cs(3 * Q);
     for (int v = 0; v < Q; ++v) host_c(Q, v, &cs[3 * v]);
     std::vector<uint8_t> fast(g->n, 0);
-    std::vector<int> gen;
+    std::vector<int> gen, late;
     const uint8_t *t = g->htyp.data();
     for (int i = 0; i < N; ++i)
         for (int j = 0; j < M; ++j)
@@ -266,8 +267,14 @@ int luma_build_interior(luma_gpu_grid *g) {
                     plain = t[z + y * K + x * K * M] == LUMA_SITE_FLUID;
                 }
                 if (plain) fast[id] = 1;
+                else if (ty == LUMA_SITE_TL_TO_FINER) late.push_back(id);
                 else gen.push_back(id);
             }
+    // the transition sites to finer grids last: only they read the
+    // sub-grids' results (coalesce) or write their macroscopic fields, so the
+    // rest of the list can run beside the sub-grids' steps
+    g->ngen_early = (int)gen.size();
+    gen.insert(gen.end(), late.begin(), late.end());
     CK(cudaMalloc(&g->fast, g->n));
     CK(cudaMemcpy(g->fast, fast.data(), g->n, cudaMemcpyHostToDevice));
     CK(cudaMalloc(&g->gen_ids, std::max<size_t>(1, gen.size()) * sizeof(int)));
@@ -298,6 +305,7 @@ StepArgs make_args(luma_gpu_grid *g, int subcycle) {
     a.u = g->u; a.rho = g->rho; a.force = g->force;
     a.ux_in = g->uxin; a.uy_in = g->uyin; a.uz_in = g->uzin;
     a.omega = d.omega; a.rho0 = d.rho_in; a.cs2 = g->cs2; a.csmag = d.csmag;
+    a.omegaf = (float)a.omega; a.rho0f = (float)a.rho0; a.cs2f = (float)a.cs2; a.csmag2f = (float)(a.csmag * a.csmag);
     a.pdelta = d.pressure_delta;
     a.has_ramp = d.velocity_ramp > 0.0;
     a.ramp_stream = ramp(d, g->t * d.dt);
@@ -357,6 +365,13 @@ int step_grid(luma_gpu_grid *g, int subcycle, bool write_macro) {
     const luma_grid_desc &d = g->d;
     cudaStream_t s = g->stream;
     const bool overlap = overlap_kids(g);
+    // On an IBM grid without bodies of its own, the deferred sites (solid,
+    // refined, velocity) are collided from values nothing else in the step
+    // writes (their streamed populations are left as they are, the force is
+    // the reset's zero, no phase B or velocity update runs): that collision
+    // runs beside the sub-grids instead of after them.
+    const bool early_c = overlap && (d.flags & LUMA_FLAG_IBM) && g->fuse && !(g->ibm && g->ibm->has_bodies) &&
+                         g->nreg == 0 && g->nvelu == 0 && !g->adj;
     if (overlap) {
         StepArgs ai = make_args(g, subcycle);
         ai.macro_out = write_macro || (d.flags & (LUMA_FLAG_GRAVITY | LUMA_FLAG_REGULARISED)) ? 1 : 0;
@@ -369,6 +384,15 @@ int step_grid(luma_gpu_grid *g, int subcycle, bool write_macro) {
             return launch_general_phaseA<decltype(q)::value, decltype(p)>(ai, g->wall, g->fast, g->gen_ids, g->ngen, s,
                                                                           kPhaseAInterior);
         }));
+        if (early_c)
+            CK(dispatch(d.Q, d.precision, [&](auto q, auto p) {
+                return launch_general_phaseC<decltype(q)::value, decltype(p)>(ai, g->defer_ids, g->ndefer, s);
+            }));
+        if (g->ngen_early > 0)
+            CK(dispatch(d.Q, d.precision, [&](auto q, auto p) {
+                return launch_general_phaseA<decltype(q)::value, decltype(p)>(ai, g->wall, g->fast, g->gen_ids,
+                                                                              g->ngen_early, s, kPhaseAList);
+            }));
         CK(cudaStreamWaitEvent(g->kid_stream, g->ev_fork, 0));
         for (luma_gpu_grid *c : g->kids) set_tree_stream(c, g->kid_stream);
         int rc = LUMA_OK;
@@ -405,8 +429,10 @@ int step_grid(luma_gpu_grid *g, int subcycle, bool write_macro) {
         int rc = luma_ibm_reset_forces(g, a);
         if (rc) return rc;
     }
+    const int list0 = overlap ? g->ngen_early : 0;  // the rest of the list ran beside the sub-grids
     CK(dispatch(d.Q, d.precision, [&](auto q, auto p) {
-        return launch_general_phaseA<decltype(q)::value, decltype(p)>(a, g->wall, g->fast, g->gen_ids, g->ngen, s,
+        return launch_general_phaseA<decltype(q)::value, decltype(p)>(a, g->wall, g->fast, g->gen_ids + list0,
+                                                                      g->ngen - list0, s,
                                                                       overlap ? kPhaseAList : kPhaseAAll);
     }));
     if (g->nreg)
@@ -426,10 +452,11 @@ int step_grid(luma_gpu_grid *g, int subcycle, bool write_macro) {
             int rc = luma_adj_step_hook(g, a);
             if (rc) return rc;
         }
-        CK(dispatch(d.Q, d.precision, [&](auto q, auto p) {
-            return launch_general_phaseC<decltype(q)::value, decltype(p)>(a, g->fuse ? g->defer_ids : nullptr,
-                                                                          g->ndefer, s);
-        }));
+        if (!early_c)
+            CK(dispatch(d.Q, d.precision, [&](auto q, auto p) {
+                return launch_general_phaseC<decltype(q)::value, decltype(p)>(a, g->fuse ? g->defer_ids : nullptr,
+                                                                              g->ndefer, s);
+            }));
     }
     g->cur ^= 1;
     ++g->t;
@@ -470,7 +497,8 @@ void tree_signature(const luma_gpu_grid *g, std::vector<uintptr_t> &s) {
     auto V = [&](long long v) { s.push_back((uintptr_t)v); };
     P(g); P(g->f[0]); P(g->f[1]); P(g->u); P(g->rho); P(g->force); P(g->typ); P(g->wall); P(g->reg); P(g->velu);
     P(g->uxin); P(g->defer); P(g->defer_ids); P(g->fast); P(g->gen_ids); P(g->adj); P(g->bfl);
-    V(g->cur); V(g->aa_odd); V(g->bulk); V(g->fuse); V(g->ngen); V(g->ndefer); V(g->nreg); V(g->nvelu);
+    V(g->cur); V(g->aa_odd); V(g->bulk); V(g->fuse); V(g->ngen); V(g->ngen_early); V(g->ndefer); V(g->nreg);
+    V(g->nvelu);
     V(g->d.flags);
     luma_bfl_signature(g, s);
     if (g->ibm) {

@@ -81,6 +81,10 @@ struct StepArgs {
     const void *force;      // R*, SoA force_xyz (null when no forcing)
     const double *ux_in, *uy_in, *uz_in;
     double omega, rho0, cs2, csmag;
+    // the same rounded to FP32 on the host (csmag2f = (float)(csmag * csmag)):
+    // FP32 kernels take these instead of converting per thread, since a
+    // conversion from FP64 occupies the FP64 unit
+    float omegaf, rho0f, cs2f, csmag2f;
     double pdelta;          // GridUnits::pd2dlbm(L_PRESSURE_DELTA)
     double ramp_stream;     // velocity-ramp coefficient at t*dt (0 => no ramp write)
     double ramp_reg;        // ramp coefficient at (t+1)*dt (regularised BCs)
@@ -102,6 +106,24 @@ struct StepArgs {
     // while *skip is non-zero (the loop has converged); null outside the loop
     const int *skip;
 };
+
+// The step's constants in the kernel's arithmetic type.
+template <class P>
+__device__ __forceinline__ typename P::R omega_of(const StepArgs &a) {
+    if constexpr (sizeof(typename P::R) == 4) return a.omegaf; else return a.omega;
+}
+template <class P>
+__device__ __forceinline__ typename P::R rho0_of(const StepArgs &a) {
+    if constexpr (sizeof(typename P::R) == 4) return a.rho0f; else return a.rho0;
+}
+template <class P>
+__device__ __forceinline__ typename P::R cs2_of(const StepArgs &a) {
+    if constexpr (sizeof(typename P::R) == 4) return a.cs2f; else return a.cs2;
+}
+template <class P>
+__device__ __forceinline__ typename P::R csmag2_of(const StepArgs &a) {
+    if constexpr (sizeof(typename P::R) == 4) return a.csmag2f; else return a.csmag * a.csmag;
+}
 
 // Per regularised site: inward normal, normal direction and edge count from
 // GridUtils::isWithinDomainWall (src/GridUtils.cpp:1369-1430), computed on

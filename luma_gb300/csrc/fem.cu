@@ -51,6 +51,13 @@ struct FemKernelArgs {
     const int *parent_el;
     const double *parent_zeta, *mpos0;
     int *it;
+    // first Newton iteration of a step (the state is the step's start in every
+    // FSI sub-iteration): factored matrix, pivots, L extents, internal force
+    // and mass term, kept by the step's first FEM call (cache_mode 1) and
+    // reused by its later ones (cache_mode 2)
+    double *Kc, *Fc, *MFc;
+    int *ipc, *limc;
+    int cache_mode;
     double *res, *fsi_res;      // per filament NR residual; FSI residual: [0] running max, [1] last
     int *fsi_state;             // FSI loop of the step: [0] converged, [1] sub-iterations run
     const int *skip;            // while *skip (the loop converged) the kernels return at once; may be null
@@ -142,7 +149,8 @@ __device__ __forceinline__ double quotient(double a, double b, double y) {
     return __fma_rn(__fma_rn(-q1, b, a), y, q1);
 }
 
-#define AC(r, c) A[(size_t)(off + (c)) * lda + (off + (r))]
+// (32-bit index arithmetic: lda and n are at most 512)
+#define AC(r, c) A[(off + (c)) * lda + (off + (r))]
 
 // `band`: no entry of the matrix lies more than `band` rows below or
 // columns right of the diagonal (n for a dense matrix).  Partial pivoting
@@ -165,8 +173,7 @@ __device__ __forceinline__ double quotient(double a, double b, double y) {
 // an interchange moves a non-zero down), so the backward solve needs no
 // scan.
 template <int NB>
-__device__ __forceinline__ void lu_solve_banded(double *A, int lda, int off, int n, int *ipiv, double *x, int band,
-                                                int *lim, double *xs, double *rd) {
+__device__ __forceinline__ void lu_factor_banded(double *A, int lda, int off, int n, int *ipiv, int band, int *lim) {
     const unsigned full = 0xffffffffu;
     const int lane = threadIdx.x & 31;
     for (int r = lane; r < n; r += 32) lim[r] = r;
@@ -174,14 +181,15 @@ __device__ __forceinline__ void lu_solve_banded(double *A, int lda, int off, int
     for (int k = 0; k < n; ++k) {
         const int nr = min(n, k + band + 1) - k - 1;  // window rows below the diagonal
         const int cend = min(n, k + 2 * band + 1);
-        double cv[NB + 1];
+        // the candidates as bit patterns (integer registers and selects)
+        long long cv[NB + 1];
 #pragma unroll
-        for (int i = 0; i <= NB; ++i) cv[i] = i <= nr ? AC(k + i, k) : 0.0;
+        for (int i = 0; i <= NB; ++i) cv[i] = i <= nr ? __double_as_longlong(AC(k + i, k)) : 0ll;
         int pi = 0;
-        unsigned long long best = mag_bits(cv[0]);
+        unsigned long long best = (unsigned long long)cv[0] & 0x7fffffffffffffffull;
 #pragma unroll
         for (int i = 1; i <= NB; ++i) {
-            const unsigned long long v = mag_bits(cv[i]);
+            const unsigned long long v = (unsigned long long)cv[i] & 0x7fffffffffffffffull;
             if (i <= nr && v > best) {
                 best = v;
                 pi = i;
@@ -190,12 +198,13 @@ __device__ __forceinline__ void lu_solve_banded(double *A, int lda, int off, int
         const int p = k + pi;
         if (lane == 0) ipiv[k] = p + 1;
         if (best == 0) continue;  // a zero column: no interchange, no elimination
-        double pv = cv[0], mine = 0.0;
+        long long pvb = cv[0], mineb = 0;
 #pragma unroll
         for (int i = 1; i <= NB; ++i) {
-            if (pi == i) pv = cv[i];
-            if (lane == i - 1) mine = pi == i ? cv[0] : cv[i];  // row k+1+lane after the interchange
+            if (pi == i) pvb = cv[i];
+            if (lane == i - 1) mineb = pi == i ? cv[0] : cv[i];  // row k+1+lane after the interchange
         }
+        const double pv = __longlong_as_double(pvb), mine = __longlong_as_double(mineb);
         if (pi) {
             __syncwarp();  // every lane's candidate reads before the interchange writes
             for (int c = lane; c < cend; c += 32) {
@@ -223,6 +232,14 @@ __device__ __forceinline__ void lu_solve_banded(double *A, int lda, int off, int
         }
         __syncwarp();
     }
+}
+
+// The transposed solve with the factors of lu_factor_banded (lim included),
+// one warp.
+__device__ __forceinline__ void lu_solve_factored(const double *A, int lda, int off, int n, const int *ipiv, double *x,
+                                                  int band, const int *lim, double *xs, double *rd) {
+    const unsigned full = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
     // forward U^T y = x: U's rows reach 2*band right of the diagonal, so each
     // lane keeps one pending row and subtracts a term as soon as its unknown
     // is known, in ascending order (the serial order); the divisions use the
@@ -418,9 +435,13 @@ __device__ void lu_solve_block(double *A, int lda, int off, int n, int *ipiv, do
     __shared__ int lim[512];
     __shared__ double xs[512], rd[512];
     if (threadIdx.x < 32) {
-        if (band <= 7) lu_solve_banded<7>(A, lda, off, n, ipiv, x, band, lim, xs, rd);
-        else if (band <= 15) lu_solve_banded<15>(A, lda, off, n, ipiv, x, band, lim, xs, rd);
-        else lu_solve_dense(A, lda, off, n, ipiv, x, band, nzr, nzc, lim, xs);
+        if (band <= 15) {
+            if (band <= 7) lu_factor_banded<7>(A, lda, off, n, ipiv, band, lim);
+            else lu_factor_banded<15>(A, lda, off, n, ipiv, band, lim);
+            lu_solve_factored(A, lda, off, n, ipiv, x, band, lim, xs, rd);
+        } else {
+            lu_solve_dense(A, lda, off, n, ipiv, x, band, nzr, nzc, lim, xs);
+        }
     }
     __syncthreads();
 }
@@ -568,10 +589,12 @@ __global__ void k_fem_dynamic(FemKernelArgs a) {
     double *M = a.M + (size_t)f * a.maxdof * a.maxdof;
     double *K = a.k_in_smem ? fem_smem : a.K + (size_t)f * a.maxdof * a.maxdof;
     double *Meff = a.tmp + 2 * (size_t)d0, *MF = a.tmp + 2 * (size_t)d0 + nd;
-    __shared__ int ipiv[512];
-    __shared__ double sq[512];
+    __shared__ int ipiv[512], lim[512];
+    __shared__ double sq[512], xs[512], rd[512];
     __shared__ int go;
     const double Dt = a.dt;
+    double *Kc = a.Kc + (size_t)f * a.maxdof * a.maxdof;
+    int *ipc = a.ipc + (size_t)f * a.maxdof, *limc = a.limc + (size_t)f * a.maxdof;
     for (int i = threadIdx.x; i < nd; i += blockDim.x) {
         a.U[d0 + i] = a.U_n[d0 + i];
         a.Ud[d0 + i] = a.Ud_n[d0 + i];
@@ -586,6 +609,23 @@ __global__ void k_fem_dynamic(FemKernelArgs a) {
     int it = 0;
     double res = 0.0;
     do {
+        if (it == 0 && a.cache_mode == 2) {
+            // the step's first Newton iteration again: its factors, internal
+            // force and mass term from the step's first call, this call's load
+            for (int q = threadIdx.x; q < nd * nd; q += blockDim.x) K[q] = Kc[q];
+            for (int i = threadIdx.x; i < nd - bc; i += blockDim.x) {
+                ipiv[i] = ipc[i];
+                lim[i] = limc[i];
+            }
+            for (int i = threadIdx.x; i < nd; i += blockDim.x) {
+                const double v = a.R[d0 + i] - a.Fc[d0 + i] + a.MFc[d0 + i];
+                a.Fv[d0 + i] = v;
+                a.delU[d0 + i] = v;
+            }
+            __syncthreads();
+            if (threadIdx.x < 32) lu_solve_factored(K, nd, bc, nd - bc, ipiv, a.delU + d0 + bc, 5, lim, xs, rd);
+            __syncthreads();
+        } else {
         for (int t = threadIdx.x; t < 4 * ne; t += blockDim.x) {
             const int part = t / ne, e = t - part * ne;
             if (part == 0) element_matrices<0>(a, f, e);
@@ -634,7 +674,14 @@ __global__ void k_fem_dynamic(FemKernelArgs a) {
             MF[i] = s;
         }
         __syncthreads();
-        for (int i = threadIdx.x; i < nd; i += blockDim.x) a.Fv[d0 + i] = a.R[d0 + i] - a.Fv[d0 + i] + MF[i];
+        const bool keep = it == 0 && a.cache_mode == 1;
+        for (int i = threadIdx.x; i < nd; i += blockDim.x) {
+            if (keep) {
+                a.Fc[d0 + i] = a.Fv[d0 + i];
+                a.MFc[d0 + i] = MF[i];
+            }
+            a.Fv[d0 + i] = a.R[d0 + i] - a.Fv[d0 + i] + MF[i];
+        }
         for (int t = threadIdx.x; t < nd * 9; t += blockDim.x) {
             const int i = t / 9, j = 3 * (i / 3) - 3 + t % 9;
             if (j < 0 || j >= nd) continue;
@@ -643,7 +690,19 @@ __global__ void k_fem_dynamic(FemKernelArgs a) {
         for (int i = threadIdx.x; i < nd; i += blockDim.x) a.delU[d0 + i] = a.Fv[d0 + i];
         __syncthreads();
         // an element couples the 6 DOFs of its two nodes: half-bandwidth 5
-        lu_solve_block(K, nd, bc, nd - bc, ipiv, a.delU + d0 + bc, 5);
+        if (threadIdx.x < 32) {
+            lu_factor_banded<7>(K, nd, bc, nd - bc, ipiv, 5, lim);
+            lu_solve_factored(K, nd, bc, nd - bc, ipiv, a.delU + d0 + bc, 5, lim, xs, rd);
+        }
+        __syncthreads();
+        if (keep) {
+            for (int q = threadIdx.x; q < nd * nd; q += blockDim.x) Kc[q] = K[q];
+            for (int i = threadIdx.x; i < nd - bc; i += blockDim.x) {
+                ipc[i] = ipiv[i];
+                limc[i] = lim[i];
+            }
+        }
+        }
         for (int i = threadIdx.x; i < bc; i += blockDim.x) a.delU[d0 + i] = 0.0;
         __syncthreads();
         // the squares of the residual's sum formed densely beforehand; one
@@ -985,6 +1044,7 @@ FemKernelArgs make_fem_args(luma_gpu_grid *g) {
     a.M = d.M; a.K = d.K; a.epsA = d.epsA;
     a.parent_el = d.parent_el; a.parent_zeta = d.parent_zeta; a.mpos0 = d.mpos0;
     a.it = d.it; a.res = d.res; a.fsi_res = d.fsi_res; a.fsi_state = d.fsi_state;
+    a.Kc = d.Kc; a.Fc = d.Fc; a.MFc = d.MFc; a.ipc = d.ipc; a.limc = d.limc;
     a.dt = g->d.dt; a.dh = g->d.dh;
     a.flex = d.flex;
     a.N = g->d.N; a.M_ = g->d.M; a.K_ = g->d.K; a.dims = g->d.dims; a.level = g->d.level;
@@ -1081,7 +1141,9 @@ int luma_fem_upload(luma_gpu_grid *g) {
         (rc = zeros(&d.M, (size_t)d.nfil * maxdof * maxdof)) || (rc = zeros(&d.K, (size_t)d.nfil * maxdof * maxdof)) ||
         (rc = zeros(&d.epsA, (size_t)d.nfil * maxmk * maxmk)) || (rc = zeros(&d.it, d.nfil)) ||
         (rc = zeros(&d.res, d.nfil)) || (rc = zeros(&d.fsi_res, 2)) ||
-        (rc = zeros(&d.fsi_state, 2)))
+        (rc = zeros(&d.fsi_state, 2)) || (rc = zeros(&d.Kc, (size_t)d.nfil * maxdof * maxdof)) ||
+        (rc = zeros(&d.Fc, ndof)) || (rc = zeros(&d.MFc, ndof)) || (rc = zeros(&d.ipc, (size_t)d.nfil * maxdof)) ||
+        (rc = zeros(&d.limc, (size_t)d.nfil * maxdof)))
         return rc;
     FlexArgs &x = d.flex;
     x.nm = nmk;
@@ -1146,9 +1208,12 @@ int luma_fem_supports(luma_gpu_grid *g, const int *skip) {
 }
 
 // ObjectManager::ibm_moveBodies (:61-104) for the filaments of a grid.
-int luma_fem_move_bodies(luma_gpu_grid *g, const int *skip) {
+// `first`: the step's first FEM call (it keeps its first Newton iteration's
+// factors); later calls of the step reuse them.
+int luma_fem_move_bodies(luma_gpu_grid *g, const int *skip, bool first) {
     FemKernelArgs a = full_args(g);
     a.skip = skip;
+    a.cache_mode = first ? 1 : 2;
     a.k_in_smem = g->ibm->fem.k_in_smem;
     const size_t kb = (size_t)a.maxdof * a.maxdof * sizeof(double);
     k_fem_dynamic<<<a.nfil, 128, a.k_in_smem ? kb : 0, g->stream>>>(a);
@@ -1228,7 +1293,7 @@ void luma_fem_free(luma_gpu_grid *g) {
     void *ptrs[] = {d.node_off, d.el_off, d.dof_off, d.mk_off, d.bc, d.dm, d.velscale, d.pos0, d.ang0, d.len0,
                     d.area, d.I, d.E, d.rho, d.child_off, d.child_node, d.child_z1, d.child_z2, d.U, d.U_n, d.Ud,
                     d.Ud_n, d.Udd, d.Udd_n, d.R, d.Fv, d.delU, d.M, d.K, d.epsA, d.parent_el, d.parent_zeta,
-                    d.mpos0, d.it, d.res, d.fsi_res, d.fsi_state, d.flex.pos, d.flex.vel, d.flex.vel_km1, d.flex.F, d.flex.eps,
+                    d.mpos0, d.it, d.res, d.fsi_res, d.fsi_state, d.Kc, d.Fc, d.MFc, d.ipc, d.limc, d.flex.pos, d.flex.vel, d.flex.vel_km1, d.flex.F, d.flex.eps,
                     d.flex.ds, d.flex.irho, d.flex.imom, d.flex.nsupp, d.flex.supp, d.flex.delta, d.flex.sx,
                     d.flex.sy, d.flex.sz, d.flex.cage, d.flex.cagei, g->ibm->u_n};
     for (void *p : ptrs) cudaFree(p);

@@ -53,6 +53,7 @@ struct luma_gpu_grid {
     uint8_t *fast = nullptr;
     int *gen_ids = nullptr;
     int ngen = 0;
+    int ngen_early = 0;         // gen_ids[0, ngen_early): sites other than transition sites to finer grids
     luma_gpu_grid *parent = nullptr;
     std::vector<luma_gpu_grid *> kids;
     cudaStream_t stream = nullptr;
@@ -94,7 +95,7 @@ int luma_eps_solve_device(int n, int band, const std::vector<double> &a, std::ve
 // fem.cu
 int luma_fem_upload(luma_gpu_grid *g);
 int luma_fem_supports(luma_gpu_grid *g, const int *skip);
-int luma_fem_move_bodies(luma_gpu_grid *g, const int *skip);
+int luma_fem_move_bodies(luma_gpu_grid *g, const int *skip, bool first);
 const int *luma_fem_fsi_flag(luma_gpu_grid *g);
 int luma_fem_fsi_begin(luma_gpu_grid *g);
 int luma_fem_restore_u(luma_gpu_grid *g);
@@ -158,6 +159,10 @@ struct FemDevice {
     double *R = nullptr, *Fv = nullptr, *delU = nullptr;
     // scratch: dense M, K per filament (maxdof^2 each), element matrices
     double *M = nullptr, *K = nullptr, *epsA = nullptr;
+    // the step's first Newton iteration: factors, pivots, L extents (per
+    // filament maxdof^2 / maxdof), internal force and mass term (per DOF)
+    double *Kc = nullptr, *Fc = nullptr, *MFc = nullptr;
+    int *ipc = nullptr, *limc = nullptr;
     // markers
     int *parent_el = nullptr;
     double *parent_zeta = nullptr, *mpos0 = nullptr;

@@ -401,7 +401,7 @@ int luma_ibm_apply(luma_gpu_grid *g, const StepArgs &a) {
         return luma_set_error(LUMA_E_CUDA, "u_n copy failed");
     if ((rc = ibm_pass(g, a))) return rc;
     if (!st.has_flexible) return LUMA_OK;
-    if ((rc = luma_fem_move_bodies(g, nullptr))) return rc;
+    if ((rc = luma_fem_move_bodies(g, nullptr, true))) return rc;
     if ((rc = luma_fem_fsi_begin(g))) return rc;
     StepArgs b = a;
     b.skip = luma_fem_fsi_flag(g);
@@ -409,7 +409,7 @@ int luma_ibm_apply(luma_gpu_grid *g, const StepArgs &a) {
         if ((rc = luma_fem_restore_u(g))) return rc;
         if ((rc = luma_ibm_reset_forces(g, b))) return rc;
         if ((rc = ibm_pass(g, b))) return rc;
-        if ((rc = luma_fem_move_bodies(g, b.skip))) return rc;
+        if ((rc = luma_fem_move_bodies(g, b.skip, false))) return rc;
         if ((rc = luma_fem_fsi_check(g))) return rc;
     }
     return luma_fem_commit(g);

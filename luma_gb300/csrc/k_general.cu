@@ -39,147 +39,156 @@ __device__ __forceinline__ int child_at(const StepArgs &a, int i, int j, int k) 
     return -1;
 }
 
-// _LBM_stream_opt (:206-297) for one site; fills fn[] with the streamed
-// populations in the stored representation.
-template <int Q, class P>
-__device__ __forceinline__ void stream_site(const StepArgs &a, const int8_t *wall, int i, int j, int k, int id,
-                                            int type, typename P::R *fn) {
+// The direction tables in constant memory, for code that picks the
+// direction at run time (one thread per population); fully unrolled loops
+// use Lattice<Q>'s constexpr accessors, which fold to immediates.
+template <int Q>
+struct DirTable {
+    int c[Q][3];
+    int opp[Q];
+    int refl[3][Q];
+};
+template <int Q>
+constexpr DirTable<Q> dir_table() {
+    DirTable<Q> t{};
+    for (int v = 0; v < Q; ++v) {
+        for (int d = 0; d < 3; ++d) t.c[v][d] = Lattice<Q>::c(v, d);
+        t.opp[v] = Lattice<Q>::opp(v);
+        for (int p = 0; p < 3; ++p) t.refl[p][v] = Lattice<Q>::reflect(p, v);
+    }
+    return t;
+}
+__constant__ DirTable<LUMA_GEN_Q> kDirs = dir_table<LUMA_GEN_Q>();
+
+template <int Q, bool RT>
+__device__ __forceinline__ int dir_c(int v, int d) {
+    static_assert(!RT || Q == LUMA_GEN_Q, "run-time direction tables exist for this unit's lattice only");
+    if constexpr (RT) return kDirs.c[v][d];
+    else return Lattice<Q>::c(v, d);
+}
+template <int Q, bool RT>
+__device__ __forceinline__ int dir_opp(int v) {
+    if constexpr (RT) return kDirs.opp[v];
+    else return Lattice<Q>::opp(v);
+}
+template <int Q, bool RT>
+__device__ __forceinline__ int dir_reflect(int plane, int v) {
+    if constexpr (RT) return kDirs.refl[plane][v];
+    else return Lattice<Q>::reflect(plane, v);
+}
+
+// _LBM_stream_opt (:206-297) for one direction v of one site: the streamed
+// population in the stored representation.  RT: v is a run-time value.
+template <int Q, class P, bool RT>
+__device__ __forceinline__ typename P::R stream_dir(const StepArgs &a, const int8_t *wall, int i, int j, int k,
+                                                    int id, int type, int v) {
     using L = Lattice<Q>;
     using R = typename P::R;
     constexpr int D = L::D;
     const int N = a.N, M = a.M, K = a.K;
     const size_t n = (size_t)a.ncell;
-    int slip_plane_mask = 0;  // for slip sites: bit v set when direction v is reflected, plane in nibble
-    int8_t nv0 = 0, nv1 = 0, nv2 = 0;
-    if (type == LUMA_SITE_SLIP) {
-        nv0 = wall[4 * (size_t)id + 0];
-        nv1 = wall[4 * (size_t)id + 1];
-        nv2 = wall[4 * (size_t)id + 2];
-    }
-    // every source site's label first (independent loads, all in flight at
-    // once), then the per-direction rules, whose loads do not wait on each
-    // other either
-    int sidv[Q], stv[Q];
-#pragma unroll
-    for (int v = 0; v < Q; ++v) {
-        int sx = i - L::c(v, 0), sy = j - L::c(v, 1), sz = k - L::c(v, 2);
-        sx = sx < 0 ? sx + N : (sx >= N ? sx - N : sx);
-        sy = sy < 0 ? sy + M : (sy >= M ? sy - M : sy);
-        if (D == 3) sz = sz < 0 ? sz + K : (sz >= K ? sz - K : sz);
-        else sz = 0;
-        sidv[v] = sz + sy * K + sx * K * M;
-        stv[v] = a.typ[sidv[v]];
-    }
-#pragma unroll
-    for (int v = 0; v < Q; ++v) {
-        const int cx = L::c(v, 0), cy = L::c(v, 1), cz = L::c(v, 2);
-        const int sid = sidv[v];
-        const int stype = stv[v];
-        if (type == LUMA_SITE_BFL || stype == LUMA_SITE_BFL) {
-            // _LBM_applyBFL_opt (:1010-1113) through the link tables
-            // (kinds in bfl.cu); links without a wall stream as usual
-            if (!a.bfl_rec) {
-                *a.unsupported = 1;
-                fn[v] = R(0);
-                continue;
-            }
-            const int r = a.bfl_rec[id];
-            const uint32_t lm = r >= 0 ? a.bfl_mask[r] : 0u;
-            if ((lm >> v) & 1u) {
-                const int l = a.bfl_first[r] + __popc(lm & ((1u << v) - 1u));
-                const int kind = a.bfl_kind[l];
-                const R fo = ld<P>(a.f, (size_t)L::opp(v) * n + id);
-                if (kind == 0) {
-                    fn[v] = fo;
-                } else if (kind == 1) {
-                    fn[v] = ld<P>(a.fNew, (size_t)v * n + id);
-                } else {
-                    const double q = a.bfl_q[l];
-                    const R fv = ld<P>(a.f, (size_t)v * n + id);
-                    fn[v] = add_rn(mul_rn(R(1 - 2 * q), R((fv - fo) / R(2 - 2 * q))), fo);
-                }
-                if (kind != 1) {
-                    const double sh = P::shifted ? L::w(v) * a.rho0 : 0.0;  // w_opp(v) = w_v
-                    a.bfl_val[l] = (double(fo) + sh) + (double(fn[v]) + sh);
-                }
-                continue;
-            }
+    const int cx = dir_c<Q, RT>(v, 0), cy = dir_c<Q, RT>(v, 1), cz = dir_c<Q, RT>(v, 2);
+    int sx = i - cx, sy = j - cy, sz = k - cz;
+    sx = sx < 0 ? sx + N : (sx >= N ? sx - N : sx);
+    sy = sy < 0 ? sy + M : (sy >= M ? sy - M : sy);
+    if (D == 3) sz = sz < 0 ? sz + K : (sz >= K ? sz - K : sz);
+    else sz = 0;
+    const int sid = sz + sy * K + sx * K * M;
+    const int stype = a.typ[sid];
+    if (type == LUMA_SITE_BFL || stype == LUMA_SITE_BFL) {
+        // _LBM_applyBFL_opt (:1010-1113) through the link tables
+        // (kinds in bfl.cu); links without a wall stream as usual
+        if (!a.bfl_rec) {
+            *a.unsupported = 1;
+            return R(0);
         }
-        if (type == LUMA_SITE_SLIP) {
-            // _LBM_applySpecReflect_opt (:527-581): first matching wall wins.
-            int plane = -1;
-            if (nv0 == 1 && cx == 1) plane = 0;
-            else if (nv0 == -1 && cx == -1) plane = 0;
-            else if (nv1 == 1 && cy == 1) plane = 1;
-            else if (nv1 == -1 && cy == -1) plane = 1;
-            else if (nv2 == 1 && cz == 1) plane = 2;
-            else if (nv2 == -1 && cz == -1) plane = 2;
-            if (plane >= 0) {
-                int rv = plane == 0 ? L::reflect(0, v) : (plane == 1 ? L::reflect(1, v) : L::reflect(2, v));
-                fn[v] = ld<P>(a.f, (size_t)rv * n + id);
-                slip_plane_mask |= 1;
-                continue;
-            }
-        }
-        if (stype == LUMA_SITE_SOLID) {
-            fn[v] = ld<P>(a.f, (size_t)L::opp(v) * n + id);
-        } else if (stype == LUMA_SITE_EXTRAPOLATE_RIGHT) {
-            fn[v] = ld<P>(a.f, (size_t)v * n + (sid - 2 * (K * M)));
-        } else if (stype == LUMA_SITE_VELOCITY && !(a.flags & LUMA_FLAG_REGULARISED)) {
-            const R rs = ldr<P>(a.rho, sid);
-            R ux, uy, uz = R(0);
-            if (a.has_ramp) {
-                ux = R(a.ux_in[j] * a.ramp_stream);
-                uy = R(a.uy_in[j] * a.ramp_stream);
-                if (D == 3) uz = R(a.uz_in[j] * a.ramp_stream);
+        const int r = a.bfl_rec[id];
+        const uint32_t lm = r >= 0 ? a.bfl_mask[r] : 0u;
+        if ((lm >> v) & 1u) {
+            const int l = a.bfl_first[r] + __popc(lm & ((1u << v) - 1u));
+            const int kind = a.bfl_kind[l];
+            const R fo = ld<P>(a.f, (size_t)dir_opp<Q, RT>(v) * n + id);
+            R out;
+            if (kind == 0) {
+                out = fo;
+            } else if (kind == 1) {
+                out = ld<P>(a.fNew, (size_t)v * n + id);
             } else {
-                ux = ldr<P>(a.u, sid);
-                uy = ldr<P>(a.u, n + sid);
-                if (D == 3) uz = ldr<P>(a.u, 2 * n + sid);
+                const double q = a.bfl_q[l];
+                const R fv = ld<P>(a.f, (size_t)v * n + id);
+                out = add_rn(mul_rn(R(1 - 2 * q), R((fv - fo) / R(2 - 2 * q))), fo);
             }
-            fn[v] = feq_s<Q, P>(v, rs, rs - R(a.rho0), ux, uy, uz, R(a.cs2));
-        } else if (a.parent_f && stype == LUMA_SITE_TL_TO_COARSER && a.subcycle == 0) {
-            // _LBM_explode_opt (:646-663) with GridUtils::getCoarseIndices.
-            int fx = i - cx, fy = j - cy, fz = D == 3 ? k - cz : 0;
-            fx = fx < 0 ? fx + N : (fx >= N ? fx - N : fx);
-            fy = fy < 0 ? fy + M : (fy >= M ? fy - M : fy);
-            if (D == 3) fz = fz < 0 ? fz + K : (fz >= K ? fz - K : fz);
-            if (fx % 2 != 0) fx -= 1;
-            if (fy % 2 != 0) fy -= 1;
-            if (fz % 2 != 0) fz -= 1;
-            const int pi = fx / 2 + a.lims[0];
-            const int pj = fy / 2 + a.lims[2];
-            const int pk = D == 3 ? fz / 2 + a.lims[4] : 0;
-            const size_t pn = (size_t)a.pN * a.pM * a.pK;
-            fn[v] = ld<P>(a.parent_f, (size_t)v * pn + pk + (size_t)pj * a.pK + (size_t)pi * a.pK * a.pM);
-        } else if (a.nchild && stype == LUMA_SITE_REFINED && type == LUMA_SITE_TL_TO_FINER) {
-            // _LBM_coalesce_opt (:591-636) with GridUtils::getFineIndices.
-            const int s = child_at<Q>(a, i, j, k);
-            if (s < 0) {
-                *a.unsupported = 2;
-                fn[v] = R(0);
-                continue;
+            if (kind != 1) {
+                const double sh = P::shifted ? L::w(v) * a.rho0 : 0.0;  // w_opp(v) = w_v
+                a.bfl_val[l] = (double(fo) + sh) + (double(out) + sh);
             }
-            const ChildView &cg = a.child[s];
-            const int ci = 2 * (i - cg.lims[0] + 1) - 2;
-            const int cj = 2 * (j - cg.lims[2] + 1) - 2;
-            const int ck = D == 3 ? 2 * (k - cg.lims[4] + 1) - 2 : 0;
-            const size_t cn = (size_t)cg.N * cg.M * cg.K;
-            R acc = R(0);
-#pragma unroll
-            for (int ii = 0; ii < 2; ++ii)
-#pragma unroll
-                for (int jj = 0; jj < 2; ++jj)
-#pragma unroll
-                    for (int kk = 0; kk < (D == 3 ? 2 : 1); ++kk)
-                        acc += ld<P>(cg.f, (size_t)v * cn + (ck + kk) + (size_t)(cj + jj) * cg.K +
-                                               (size_t)(ci + ii) * cg.K * cg.M);
-            fn[v] = acc / (D == 3 ? R(8) : R(4));
-        } else {
-            fn[v] = ld<P>(a.f, (size_t)v * n + sid);
+            return out;
         }
     }
-    (void)slip_plane_mask;
+    if (type == LUMA_SITE_SLIP) {
+        // _LBM_applySpecReflect_opt (:527-581): first matching wall wins.
+        const int8_t nv0 = wall[4 * (size_t)id + 0], nv1 = wall[4 * (size_t)id + 1], nv2 = wall[4 * (size_t)id + 2];
+        int plane = -1;
+        if (nv0 == 1 && cx == 1) plane = 0;
+        else if (nv0 == -1 && cx == -1) plane = 0;
+        else if (nv1 == 1 && cy == 1) plane = 1;
+        else if (nv1 == -1 && cy == -1) plane = 1;
+        else if (nv2 == 1 && cz == 1) plane = 2;
+        else if (nv2 == -1 && cz == -1) plane = 2;
+        if (plane >= 0) return ld<P>(a.f, (size_t)dir_reflect<Q, RT>(plane, v) * n + id);
+    }
+    if (stype == LUMA_SITE_SOLID) return ld<P>(a.f, (size_t)dir_opp<Q, RT>(v) * n + id);
+    if (stype == LUMA_SITE_EXTRAPOLATE_RIGHT) return ld<P>(a.f, (size_t)v * n + (sid - 2 * (K * M)));
+    if (stype == LUMA_SITE_VELOCITY && !(a.flags & LUMA_FLAG_REGULARISED)) {
+        const R rs = ldr<P>(a.rho, sid);
+        R ux, uy, uz = R(0);
+        if (a.has_ramp) {
+            ux = R(a.ux_in[j] * a.ramp_stream);
+            uy = R(a.uy_in[j] * a.ramp_stream);
+            if (D == 3) uz = R(a.uz_in[j] * a.ramp_stream);
+        } else {
+            ux = ldr<P>(a.u, sid);
+            uy = ldr<P>(a.u, n + sid);
+            if (D == 3) uz = ldr<P>(a.u, 2 * n + sid);
+        }
+        return feq_s<Q, P>(v, rs, rs - rho0_of<P>(a), ux, uy, uz, cs2_of<P>(a));
+    }
+    if (a.parent_f && stype == LUMA_SITE_TL_TO_COARSER && a.subcycle == 0) {
+        // _LBM_explode_opt (:646-663) with GridUtils::getCoarseIndices.
+        int fx = sx, fy = sy, fz = sz;
+        if (fx % 2 != 0) fx -= 1;
+        if (fy % 2 != 0) fy -= 1;
+        if (fz % 2 != 0) fz -= 1;
+        const int pi = fx / 2 + a.lims[0];
+        const int pj = fy / 2 + a.lims[2];
+        const int pk = D == 3 ? fz / 2 + a.lims[4] : 0;
+        const size_t pn = (size_t)a.pN * a.pM * a.pK;
+        return ld<P>(a.parent_f, (size_t)v * pn + pk + (size_t)pj * a.pK + (size_t)pi * a.pK * a.pM);
+    }
+    if (a.nchild && stype == LUMA_SITE_REFINED && type == LUMA_SITE_TL_TO_FINER) {
+        // _LBM_coalesce_opt (:591-636) with GridUtils::getFineIndices.
+        const int s = child_at<Q>(a, i, j, k);
+        if (s < 0) {
+            *a.unsupported = 2;
+            return R(0);
+        }
+        const ChildView &cg = a.child[s];
+        const int ci = 2 * (i - cg.lims[0] + 1) - 2;
+        const int cj = 2 * (j - cg.lims[2] + 1) - 2;
+        const int ck = D == 3 ? 2 * (k - cg.lims[4] + 1) - 2 : 0;
+        const size_t cn = (size_t)cg.N * cg.M * cg.K;
+        R acc = R(0);
+#pragma unroll
+        for (int ii = 0; ii < 2; ++ii)
+#pragma unroll
+            for (int jj = 0; jj < 2; ++jj)
+#pragma unroll
+                for (int kk = 0; kk < (D == 3 ? 2 : 1); ++kk)
+                    acc += ld<P>(cg.f, (size_t)v * cn + (ck + kk) + (size_t)(cj + jj) * cg.K +
+                                           (size_t)(ci + ii) * cg.K * cg.M);
+        return acc / (D == 3 ? R(8) : R(4));
+    }
+    return ld<P>(a.f, (size_t)v * n + sid);
 }
 
 // _LBM_macro_opt (:800-891): density and velocity of fluid-like sites from
@@ -218,10 +227,10 @@ __device__ __forceinline__ void macro_site(const StepArgs &a, int i, int j, int 
         }
         if (P::shifted) {
             drho = r;
-            rho = R(a.rho0) + r;
+            rho = rho0_of<P>(a) + r;
         } else {
             rho = r;
-            drho = r - R(a.rho0);
+            drho = r - rho0_of<P>(a);
         }
         ux = mx / rho;
         uy = my / rho;
@@ -234,7 +243,7 @@ __device__ __forceinline__ void macro_site(const StepArgs &a, int i, int j, int 
         }
     } else {
         rho = ldr<P>(a.rho, id);
-        drho = rho - R(a.rho0);
+        drho = rho - rho0_of<P>(a);
         ux = ldr<P>(a.u, id);
         uy = ldr<P>(a.u, n + id);
         uz = D == 3 ? ldr<P>(a.u, 2 * n + id) : R(0);
@@ -289,7 +298,7 @@ __device__ __forceinline__ typename P::R smag_omega(const StepArgs &a, const typ
     R S00 = 0, S01 = 0, S02 = 0, S11 = 0, S12 = 0, S22 = 0;
 #pragma unroll
     for (int v = 0; v < Q; ++v) {
-        const R fneq = fn[v] - feq_s<Q, P>(v, rho, drho, ux, uy, uz, R(a.cs2));
+        const R fneq = fn[v] - feq_s<Q, P>(v, rho, drho, ux, uy, uz, cs2_of<P>(a));
         S00 += R(L::c(v, 0) * L::c(v, 0)) * fneq;
         S01 += R(L::c(v, 0) * L::c(v, 1)) * fneq;
         S11 += R(L::c(v, 1) * L::c(v, 1)) * fneq;
@@ -303,10 +312,10 @@ __device__ __forceinline__ typename P::R smag_omega(const StepArgs &a, const typ
     const R r1 = S01 * S01 + S11 * S11 + S12 * S12;
     const R r2 = S02 * S02 + S12 * S12 + S22 * S22;
     const R Qs = sqrt(R(2) * (r0 + r1 + r2));
-    const R tau = R(1) / R(a.omega);
-    const R cs2 = R(a.cs2);
-    const R tau_t = R(0.5) * (sqrt(tau * tau + R(2) * R(1.4142135623730950488016887242097) * R(a.csmag * a.csmag) *
-                                                   R(a.rho0) * cs2 * cs2 * Qs) - tau);
+    const R tau = R(1) / omega_of<P>(a);
+    const R cs2 = cs2_of<P>(a);
+    const R tau_t = R(0.5) * (sqrt(tau * tau + R(2) * R(1.4142135623730950488016887242097) * csmag2_of<P>(a) *
+                                                   rho0_of<P>(a) * cs2 * cs2 * Qs) - tau);
     return R(1) / (tau + tau_t);
 }
 
@@ -322,7 +331,7 @@ __device__ __forceinline__ void collide_site(const StepArgs &a, int id, typename
     using R = typename P::R;
     constexpr int D = L::D;
     const size_t n = (size_t)a.ncell;
-    const R cs2 = R(a.cs2);
+    const R cs2 = cs2_of<P>(a);
     R Fx = R(0), Fy = R(0), Fz = R(0);
     if (a.forcing) {
         Fx = ldr<P>(a.force, id);
@@ -331,11 +340,11 @@ __device__ __forceinline__ void collide_site(const StepArgs &a, int id, typename
     }
     const int coll = COLL >= 0 ? COLL : a.collision;
     if (coll != LUMA_COLL_KBC) {
-        const R om = coll == LUMA_COLL_BGK_SMAG ? smag_omega<Q, P>(a, fn, rho, drho, ux, uy, uz) : R(a.omega);
+        const R om = coll == LUMA_COLL_BGK_SMAG ? smag_omega<Q, P>(a, fn, rho, drho, ux, uy, uz) : omega_of<P>(a);
 #pragma unroll
         for (int v = 0; v < Q; ++v) {
             const R eq = feq_s<Q, P>(v, rho, drho, ux, uy, uz, cs2);
-            if (a.forcing) fn[v] = fn[v] + (om * (eq - fn[v]) + guo<Q, R>(v, R(a.omega), cs2, ux, uy, uz, Fx, Fy, Fz));
+            if (a.forcing) fn[v] = fn[v] + (om * (eq - fn[v]) + guo<Q, R>(v, omega_of<P>(a), cs2, ux, uy, uz, Fx, Fy, Fz));
             else fn[v] = fn[v] + om * (eq - fn[v]);
         }
         return;
@@ -413,34 +422,78 @@ __device__ __forceinline__ void collide_site(const StepArgs &a, int id, typename
         }
         ds[v] = s;
         const R dh = fneq[v] - s;
-        const R feq_true = P::shifted ? fe[v] + R(L::w(v)) * R(a.rho0) : fe[v];
+        const R feq_true = P::shifted ? fe[v] + R(L::w(v)) * rho0_of<P>(a) : fe[v];
         top += s * dh / feq_true;
         bot += dh * dh / feq_true;
     }
-    const R beta_m1 = R(2) / R(a.omega);
+    const R beta_m1 = R(2) / omega_of<P>(a);
     const R gamma = bot == R(0) ? R(2) : beta_m1 - (R(2) - beta_m1) * (top / bot);
     const R inv_b = R(1) / beta_m1;
 #pragma unroll
     for (int v = 0; v < Q; ++v) {
         const R dh = fneq[v] - ds[v];
         const R base = src[v] - inv_b * (R(2) * ds[v] + gamma * dh);
-        fn[v] = a.forcing ? base + guo<Q, R>(v, R(a.omega), cs2, ux, uy, uz, Fx, Fy, Fz) : base;
+        fn[v] = a.forcing ? base + guo<Q, R>(v, omega_of<P>(a), cs2, ux, uy, uz, Fx, Fy, Fz) : base;
     }
 }
 
-template <int Q, class P, bool TAV>
-__device__ __forceinline__ void stream_macro_site(const StepArgs &a, const int8_t *wall, int id) {
+// _LBM_stream_opt for one listed site, with most directions plain pulls:
+// the sources' labels first (all loads in flight), a bit per direction whose
+// rule is not a plain pull (every direction of a slip or BFL site), plain
+// pulls for the others, and the full rule (one run-time-indexed copy of the
+// code) for the flagged ones.  The values are those of stream_site.
+template <int Q, class P>
+__device__ __forceinline__ void stream_site_split(const StepArgs &a, const int8_t *wall, int i, int j, int k, int id,
+                                                  int type, typename P::R *fn) {
+    using L = Lattice<Q>;
     using R = typename P::R;
-    const int type = a.typ[id];
+    constexpr int D = L::D;
+    const int N = a.N, M = a.M, K = a.K;
+    const size_t n = (size_t)a.ncell;
     const bool reg = (a.flags & LUMA_FLAG_REGULARISED) != 0;
-    if (type == LUMA_SITE_REFINED || type == LUMA_SITE_SOLID || type == LUMA_SITE_VELOCITY ||
-        (reg && type == LUMA_SITE_PRESSURE))
-        return;  // velocity/pressure sites of regularised grids are phase B
-    const int k = id % a.K;
-    const int j = (id / a.K) % a.M;
-    const int i = id / (a.K * a.M);
-    R fn[Q];
-    stream_site<Q, P>(a, wall, i, j, k, id, type, fn);
+    const bool explode = a.parent_f && a.subcycle == 0;
+    const bool coalesce = a.nchild && type == LUMA_SITE_TL_TO_FINER;
+    unsigned special = (type == LUMA_SITE_SLIP || type == LUMA_SITE_BFL) ? 0xffffffffu : 0u;
+    int sidv[Q];
+#pragma unroll
+    for (int v = 0; v < Q; ++v) {
+        int sx = i - L::c(v, 0), sy = j - L::c(v, 1), sz = k - L::c(v, 2);
+        sx = sx < 0 ? sx + N : (sx >= N ? sx - N : sx);
+        sy = sy < 0 ? sy + M : (sy >= M ? sy - M : sy);
+        if (D == 3) sz = sz < 0 ? sz + K : (sz >= K ? sz - K : sz);
+        else sz = 0;
+        sidv[v] = sz + sy * K + sx * K * M;
+        const int st = a.typ[sidv[v]];
+        const bool sp = st == LUMA_SITE_SOLID || st == LUMA_SITE_EXTRAPOLATE_RIGHT || st == LUMA_SITE_BFL ||
+                        (st == LUMA_SITE_VELOCITY && !reg) || (explode && st == LUMA_SITE_TL_TO_COARSER) ||
+                        (coalesce && st == LUMA_SITE_REFINED);
+        if (sp) special |= 1u << v;
+    }
+#pragma unroll
+    for (int v = 0; v < Q; ++v) fn[v] = ((special >> v) & 1u) ? R(0) : ld<P>(a.f, (size_t)v * n + sidv[v]);
+    for (unsigned b = special & ((Q == 32 ? 0u : (1u << Q)) - 1u); b; b &= b - 1) {
+        const int v = __ffs(b) - 1;
+        const R val = stream_dir<Q, P, true>(a, wall, i, j, k, id, type, v);
+#pragma unroll
+        for (int w = 0; w < Q; ++w)
+            if (w == v) fn[w] = val;
+    }
+}
+
+// Sites phase A leaves alone: velocity/pressure sites of regularised grids
+// are phase B's.
+__device__ __forceinline__ bool phaseA_skips(const StepArgs &a, int type) {
+    const bool reg = (a.flags & LUMA_FLAG_REGULARISED) != 0;
+    return type == LUMA_SITE_REFINED || type == LUMA_SITE_SOLID || type == LUMA_SITE_VELOCITY ||
+           (reg && type == LUMA_SITE_PRESSURE);
+}
+
+// Phase A after the stream: macroscopic step, collision where it belongs
+// to phase A, stores.
+template <int Q, class P, bool TAV, int COLL = -1>
+__device__ __forceinline__ void finish_site(const StepArgs &a, int i, int j, int k, int id, int type,
+                                            typename P::R *fn) {
+    using R = typename P::R;
     R rho, drho, ux, uy, uz;
     macro_site<Q, P, true, TAV>(a, i, j, k, id, type, fn, rho, drho, ux, uy, uz);
     const size_t n = (size_t)a.ncell;
@@ -452,14 +505,27 @@ __device__ __forceinline__ void stream_macro_site(const StepArgs &a, const int8_
 #pragma unroll
             for (int v = 0; v < Q; ++v) st<P>(a.fNew, (size_t)v * n + id, fn[v]);
         }
-        collide_site<Q, P>(a, id, fn, rho, drho, ux, uy, uz);
+        collide_site<Q, P, COLL>(a, id, fn, rho, drho, ux, uy, uz);
 #pragma unroll
         for (int v = 0; v < Q; ++v) st<P>(a.fOut, (size_t)v * n + id, fn[v]);
         return;
     }
-    if (!a.ibm_split && type != LUMA_SITE_TL_TO_COARSER) collide_site<Q, P>(a, id, fn, rho, drho, ux, uy, uz);
+    if (!a.ibm_split && type != LUMA_SITE_TL_TO_COARSER) collide_site<Q, P, COLL>(a, id, fn, rho, drho, ux, uy, uz);
 #pragma unroll
     for (int v = 0; v < Q; ++v) st<P>(a.fNew, (size_t)v * n + id, fn[v]);
+}
+
+template <int Q, class P, bool TAV>
+__device__ __forceinline__ void stream_macro_site(const StepArgs &a, const int8_t *wall, int id) {
+    using R = typename P::R;
+    const int type = a.typ[id];
+    if (phaseA_skips(a, type)) return;
+    const int k = id % a.K;
+    const int j = (id / a.K) % a.M;
+    const int i = id / (a.K * a.M);
+    R fn[Q];
+    stream_site_split<Q, P>(a, wall, i, j, k, id, type, fn);
+    finish_site<Q, P, TAV>(a, i, j, k, id, type, fn);
 }
 
 template <int Q, class P, bool TAV>
@@ -468,11 +534,22 @@ __global__ void __launch_bounds__(128) k_stream_macro(StepArgs a, const int8_t *
     if (id < a.ncell) stream_macro_site<Q, P, TAV>(a, wall, id);
 }
 
-// The same over the listed sites (those the interior kernel leaves).
-template <int Q, class P, bool TAV>
+// The same over the listed sites (those the interior kernel leaves), one
+// thread per site, the collision operator fixed at compile time and the
+// stream split into plain pulls and flagged rules (short code: the
+// full-logic kernel's instruction fetch, not its loads, bounded it).
+template <int Q, class P, int COLL, bool TAV>
 __global__ void __launch_bounds__(128) k_stream_macro_list(StepArgs a, const int8_t *wall, const int *ids, int nids) {
+    using R = typename P::R;
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t < nids) stream_macro_site<Q, P, TAV>(a, wall, ids[t]);
+    if (t >= nids) return;
+    const int id = ids[t];
+    const int type = a.typ[id];
+    if (phaseA_skips(a, type)) return;
+    const int k = id % a.K, j = (id / a.K) % a.M, i = id / (a.K * a.M);
+    R fn[Q];
+    stream_site_split<Q, P>(a, wall, i, j, k, id, type, fn);
+    finish_site<Q, P, TAV, COLL>(a, i, j, k, id, type, fn);
 }
 
 // Interior fluid sites (every pull source a fluid site, so every direction
@@ -520,7 +597,7 @@ __global__ void __launch_bounds__(128) k_interior(StepArgs a, const uint8_t *fas
         // 1.5) instead of the reference's divisions by cs^2: FP64 division
         // is the costliest operation of the step on this part, and the
         // results differ from the reference's expression by rounding only.
-        const R om = R(a.omega);
+        const R om = omega_of<P>(a);
         const R usq15 = R(1.5) * (ux * ux + uy * uy + uz * uz);
         R Fx = R(0), Fy = R(0), Fz = R(0);
         if (b.forcing) {
@@ -567,13 +644,13 @@ __global__ void __launch_bounds__(128) k_regularised(StepArgs a, const int8_t *w
     const int id = rs.id, i = rs.i, j = rs.j, k = rs.k;
     const int type = a.typ[id];
     const size_t n = (size_t)a.ncell;
-    const R cs2 = R(a.cs2);
+    const R cs2 = cs2_of<P>(a);
     R fn[Q];
-    stream_site<Q, P>(a, wall, i, j, k, id, type, fn);
+    stream_site_split<Q, P>(a, wall, i, j, k, id, type, fn);
     R vel[3] = {R(a.ux_in[j] * a.ramp_reg), R(a.uy_in[j] * a.ramp_reg), R(a.uz_in[j] * a.ramp_reg)};
     const int nd = rs.ndir;
     const int nv[3] = {rs.nvec[0], rs.nvec[1], rs.nvec[2]};
-    R dens = R(a.rho0) + R(a.pdelta);
+    R dens = rho0_of<P>(a) + R(a.pdelta);
     R drho;
     if (rs.edges > 1) {
         // First-order extrapolation of rho along the inward normal.
@@ -582,7 +659,7 @@ __global__ void __launch_bounds__(128) k_regularised(StepArgs a, const int8_t *w
         const int id1 = k1 + j1 * a.K + i1 * a.K * a.M;
         const int id2 = k2 + j2 * a.K + i2 * a.K * a.M;
         dens = R(2) * ldr<P>(a.rho, id1) - ldr<P>(a.rho, id2);
-        drho = dens - R(a.rho0);
+        drho = dens - rho0_of<P>(a);
     } else {
         R fp = R(0), f0 = R(0);
         R wp = R(0), w0 = R(0);
@@ -617,8 +694,8 @@ __global__ void __launch_bounds__(128) k_regularised(StepArgs a, const int8_t *w
                 R nvel = vel[nd];
                 if (nv[nd] == -1) nvel *= R(-1);
                 // dens = (rho0 + X)/(1 - un)  =>  dens - rho0 = (X + rho0*un)/(1 - un)
-                drho = (X + R(a.rho0) * nvel) / (R(1) - nvel);
-                dens = R(a.rho0) + drho;
+                drho = (X + rho0_of<P>(a) * nvel) / (R(1) - nvel);
+                dens = rho0_of<P>(a) + drho;
             }
         } else if (type == LUMA_SITE_PRESSURE) {
             for (int d = 0; d < D; d++)
@@ -636,7 +713,7 @@ __global__ void __launch_bounds__(128) k_regularised(StepArgs a, const int8_t *w
             if (nv[nd] == -1) nvel *= R(-1);
             dens = (R(1) / (R(1) - nvel)) * (R(2) * fp + f0);
         }
-        if (!P::shifted) drho = dens - R(a.rho0);
+        if (!P::shifted) drho = dens - rho0_of<P>(a);
     }
     const R ux = vel[0], uy = vel[1], uz = D == 3 ? vel[2] : R(0);
     str<P>(a.rho, id, dens);
@@ -721,7 +798,7 @@ __device__ __forceinline__ void force_collide_site(const StepArgs &a, int id) {
     const R uz = D == 3 ? ldr<P>(a.u, 2 * n + id) : R(0);
     StepArgs b = a;
     if (type == LUMA_SITE_SOLID) b.forcing = 0;  // solid sites are collided without the Guo term
-    collide_site<Q, P>(b, id, fn, rho, rho - R(a.rho0), ux, uy, uz);
+    collide_site<Q, P>(b, id, fn, rho, rho - rho0_of<P>(a), ux, uy, uz);
 #pragma unroll
     for (int v = 0; v < Q; ++v) st<P>(a.fOut, (size_t)v * n + id, fn[v]);
 }
@@ -976,8 +1053,13 @@ cudaError_t launch_general_phaseA(const StepArgs &a, const int8_t *wall, const u
             else if (a.collision == LUMA_COLL_BGK_SMAG) k_interior<Q, P, LUMA_COLL_BGK_SMAG, T><<<nb, bs, 0, s>>>(a, fast);
             else k_interior<Q, P, LUMA_COLL_BGK, T><<<nb, bs, 0, s>>>(a, fast);
         }
-        if (part != kPhaseAInterior && ngen > 0)
-            k_stream_macro_list<Q, P, T><<<(ngen + bs - 1) / bs, bs, 0, s>>>(a, wall, gen_ids, ngen);
+        if (part != kPhaseAInterior && ngen > 0) {
+            const int lb = (ngen + bs - 1) / bs;
+            if (a.collision == LUMA_COLL_KBC) k_stream_macro_list<Q, P, LUMA_COLL_KBC, T><<<lb, bs, 0, s>>>(a, wall, gen_ids, ngen);
+            else if (a.collision == LUMA_COLL_BGK_SMAG)
+                k_stream_macro_list<Q, P, LUMA_COLL_BGK_SMAG, T><<<lb, bs, 0, s>>>(a, wall, gen_ids, ngen);
+            else k_stream_macro_list<Q, P, LUMA_COLL_BGK, T><<<lb, bs, 0, s>>>(a, wall, gen_ids, ngen);
+        }
     };
     if (tav) interior(std::true_type{});
     else interior(std::false_type{});
