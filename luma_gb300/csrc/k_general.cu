@@ -32,11 +32,43 @@ template <int Q>
 __device__ __forceinline__ int child_at(const StepArgs &a, int i, int j, int k) {
     constexpr int D = Lattice<Q>::D;
     if (a.level > 0) return a.nchild ? 0 : -1;
-    for (int s = 0; s < a.nchild; ++s) {
+    int found = -1;
+    // unrolled over the argument array (a run-time index would copy it to
+    // local memory); the first child holding the site wins
+#pragma unroll
+    for (int s = kMaxChildren - 1; s >= 0; --s) {
         const int *L = a.child[s].lims;
-        if (i >= L[0] && i <= L[1] && j >= L[2] && j <= L[3] && (D == 2 || (k >= L[4] && k <= L[5]))) return s;
+        if (s < a.nchild && i >= L[0] && i <= L[1] && j >= L[2] && j <= L[3] && (D == 2 || (k >= L[4] && k <= L[5])))
+            found = s;
     }
-    return -1;
+    return found;
+}
+
+// The 2^d fine sites under coarse site (i, j, k) in its child grid
+// (GridUtils::getFineIndices): the child's populations, their per-direction
+// stride, the first site and the steps along j and i.  False when no child
+// holds the site.
+template <int Q>
+__device__ __forceinline__ bool coalesce_base(const StepArgs &a, int i, int j, int k, const void *&cf, size_t &cn,
+                                              size_t &c0, size_t &cdj, size_t &cdi) {
+    constexpr int D = Lattice<Q>::D;
+    const int cs = child_at<Q>(a, i, j, k);
+    bool ok = false;
+#pragma unroll
+    for (int q = 0; q < kMaxChildren; ++q)
+        if (q == cs) {
+            const ChildView &cg = a.child[q];
+            const int ci = 2 * (i - cg.lims[0] + 1) - 2;
+            const int cj = 2 * (j - cg.lims[2] + 1) - 2;
+            const int ck = D == 3 ? 2 * (k - cg.lims[4] + 1) - 2 : 0;
+            cf = cg.f;
+            cn = (size_t)cg.N * cg.M * cg.K;
+            c0 = (size_t)ck + (size_t)cj * cg.K + (size_t)ci * cg.K * cg.M;
+            cdj = cg.K;
+            cdi = (size_t)cg.K * cg.M;
+            ok = true;
+        }
+    return ok;
 }
 
 // The direction tables in constant memory, for code that picks the
@@ -75,6 +107,28 @@ template <int Q, bool RT>
 __device__ __forceinline__ int dir_reflect(int plane, int v) {
     if constexpr (RT) return kDirs.refl[plane][v];
     else return Lattice<Q>::reflect(plane, v);
+}
+
+// The pull from a forced-equilibrium velocity site (_LBM_stream_opt's
+// velocity branch): the equilibrium of the source's rho and u (the inlet
+// profile times the ramp while a ramp runs).
+template <int Q, class P>
+__device__ __forceinline__ typename P::R velocity_pull(const StepArgs &a, int j, int sid, int v) {
+    using R = typename P::R;
+    constexpr int D = Lattice<Q>::D;
+    const size_t n = (size_t)a.ncell;
+    const R rs = ldr<P>(a.rho, sid);
+    R ux, uy, uz = R(0);
+    if (a.has_ramp) {
+        ux = R(a.ux_in[j] * a.ramp_stream);
+        uy = R(a.uy_in[j] * a.ramp_stream);
+        if (D == 3) uz = R(a.uz_in[j] * a.ramp_stream);
+    } else {
+        ux = ldr<P>(a.u, sid);
+        uy = ldr<P>(a.u, n + sid);
+        if (D == 3) uz = ldr<P>(a.u, 2 * n + sid);
+    }
+    return feq_s<Q, P>(v, rs, rs - rho0_of<P>(a), ux, uy, uz, cs2_of<P>(a));
 }
 
 // _LBM_stream_opt (:206-297) for one direction v of one site: the streamed
@@ -139,20 +193,7 @@ __device__ __forceinline__ typename P::R stream_dir(const StepArgs &a, const int
     }
     if (stype == LUMA_SITE_SOLID) return ld<P>(a.f, (size_t)dir_opp<Q, RT>(v) * n + id);
     if (stype == LUMA_SITE_EXTRAPOLATE_RIGHT) return ld<P>(a.f, (size_t)v * n + (sid - 2 * (K * M)));
-    if (stype == LUMA_SITE_VELOCITY && !(a.flags & LUMA_FLAG_REGULARISED)) {
-        const R rs = ldr<P>(a.rho, sid);
-        R ux, uy, uz = R(0);
-        if (a.has_ramp) {
-            ux = R(a.ux_in[j] * a.ramp_stream);
-            uy = R(a.uy_in[j] * a.ramp_stream);
-            if (D == 3) uz = R(a.uz_in[j] * a.ramp_stream);
-        } else {
-            ux = ldr<P>(a.u, sid);
-            uy = ldr<P>(a.u, n + sid);
-            if (D == 3) uz = ldr<P>(a.u, 2 * n + sid);
-        }
-        return feq_s<Q, P>(v, rs, rs - rho0_of<P>(a), ux, uy, uz, cs2_of<P>(a));
-    }
+    if (stype == LUMA_SITE_VELOCITY && !(a.flags & LUMA_FLAG_REGULARISED)) return velocity_pull<Q, P>(a, j, sid, v);
     if (a.parent_f && stype == LUMA_SITE_TL_TO_COARSER && a.subcycle == 0) {
         // _LBM_explode_opt (:646-663) with GridUtils::getCoarseIndices.
         int fx = sx, fy = sy, fz = sz;
@@ -167,16 +208,12 @@ __device__ __forceinline__ typename P::R stream_dir(const StepArgs &a, const int
     }
     if (a.nchild && stype == LUMA_SITE_REFINED && type == LUMA_SITE_TL_TO_FINER) {
         // _LBM_coalesce_opt (:591-636) with GridUtils::getFineIndices.
-        const int s = child_at<Q>(a, i, j, k);
-        if (s < 0) {
+        const void *cf;
+        size_t cn, c0, cdj, cdi;
+        if (!coalesce_base<Q>(a, i, j, k, cf, cn, c0, cdj, cdi)) {
             *a.unsupported = 2;
             return R(0);
         }
-        const ChildView &cg = a.child[s];
-        const int ci = 2 * (i - cg.lims[0] + 1) - 2;
-        const int cj = 2 * (j - cg.lims[2] + 1) - 2;
-        const int ck = D == 3 ? 2 * (k - cg.lims[4] + 1) - 2 : 0;
-        const size_t cn = (size_t)cg.N * cg.M * cg.K;
         R acc = R(0);
 #pragma unroll
         for (int ii = 0; ii < 2; ++ii)
@@ -184,8 +221,7 @@ __device__ __forceinline__ typename P::R stream_dir(const StepArgs &a, const int
             for (int jj = 0; jj < 2; ++jj)
 #pragma unroll
                 for (int kk = 0; kk < (D == 3 ? 2 : 1); ++kk)
-                    acc += ld<P>(cg.f, (size_t)v * cn + (ck + kk) + (size_t)(cj + jj) * cg.K +
-                                           (size_t)(ci + ii) * cg.K * cg.M);
+                    acc += ld<P>(cf, (size_t)v * cn + c0 + (size_t)kk + jj * cdj + ii * cdi);
         return acc / (D == 3 ? R(8) : R(4));
     }
     return ld<P>(a.f, (size_t)v * n + sid);
@@ -269,8 +305,10 @@ __device__ __forceinline__ void macro_site(const StepArgs &a, int i, int j, int 
     }
     if (type == LUMA_SITE_TL_TO_FINER) {
         const int s = child_at<Q>(a, i, j, k);
-        if (s < 0) return;
-        const ChildView &cg = a.child[s];
+#pragma unroll
+        for (int q = 0; q < kMaxChildren; ++q) {
+        if (q != s) continue;  // the child by unrolled selection (no local copy of the argument array)
+        const ChildView &cg = a.child[q];
         const int ci = 2 * (i - cg.lims[0] + 1) - 2;
         const int cj = 2 * (j - cg.lims[2] + 1) - 2;
         const int ck = D == 3 ? 2 * (k - cg.lims[4] + 1) - 2 : 0;
@@ -284,6 +322,7 @@ __device__ __forceinline__ void macro_site(const StepArgs &a, int i, int j, int 
                     if (D == 3) str<P>(cg.u, 2 * cn + cid, uz);
                     str<P>(cg.rho, cid, rho);
                 }
+        }
     }
 }
 
@@ -437,11 +476,13 @@ __device__ __forceinline__ void collide_site(const StepArgs &a, int id, typename
     }
 }
 
-// _LBM_stream_opt for one listed site, with most directions plain pulls:
-// the sources' labels first (all loads in flight), a bit per direction whose
-// rule is not a plain pull (every direction of a slip or BFL site), plain
-// pulls for the others, and the full rule (one run-time-indexed copy of the
-// code) for the flagged ones.  The values are those of stream_site.
+// _LBM_stream_opt for one listed site.  Per direction (compile-time
+// constants) the source's label picks the source: a plain pull, the
+// bounce-back of a solid source, the extrapolation two planes back, the
+// parent's population at the coarse site (explode), or the equilibrium of
+// a velocity source; the rules that need more (coalesce, slip and BFL
+// sites) take the full rule, one run-time-indexed copy of the code.  The
+// values are those of stream_dir.
 template <int Q, class P>
 __device__ __forceinline__ void stream_site_split(const StepArgs &a, const int8_t *wall, int i, int j, int k, int id,
                                                   int type, typename P::R *fn) {
@@ -453,8 +494,15 @@ __device__ __forceinline__ void stream_site_split(const StepArgs &a, const int8_
     const bool reg = (a.flags & LUMA_FLAG_REGULARISED) != 0;
     const bool explode = a.parent_f && a.subcycle == 0;
     const bool coalesce = a.nchild && type == LUMA_SITE_TL_TO_FINER;
-    unsigned special = (type == LUMA_SITE_SLIP || type == LUMA_SITE_BFL) ? 0xffffffffu : 0u;
-    int sidv[Q];
+    const bool generic = type == LUMA_SITE_SLIP || type == LUMA_SITE_BFL;
+    const size_t pn = explode ? (size_t)a.pN * a.pM * a.pK : 0;
+    unsigned special = generic ? 0xffffffffu : 0u;
+    // coalesce (_LBM_coalesce_opt, :591-636, GridUtils::getFineIndices):
+    // every direction averages the child's populations at the same 2^d fine
+    // sites, so they are found once
+    const void *cf = nullptr;
+    size_t cn = 0, c0 = 0, cdi = 0, cdj = 0;
+    if (coalesce && !generic && !coalesce_base<Q>(a, i, j, k, cf, cn, c0, cdj, cdi)) cf = nullptr;
 #pragma unroll
     for (int v = 0; v < Q; ++v) {
         int sx = i - L::c(v, 0), sy = j - L::c(v, 1), sz = k - L::c(v, 2);
@@ -462,15 +510,40 @@ __device__ __forceinline__ void stream_site_split(const StepArgs &a, const int8_
         sy = sy < 0 ? sy + M : (sy >= M ? sy - M : sy);
         if (D == 3) sz = sz < 0 ? sz + K : (sz >= K ? sz - K : sz);
         else sz = 0;
-        sidv[v] = sz + sy * K + sx * K * M;
-        const int st = a.typ[sidv[v]];
-        const bool sp = st == LUMA_SITE_SOLID || st == LUMA_SITE_EXTRAPOLATE_RIGHT || st == LUMA_SITE_BFL ||
-                        (st == LUMA_SITE_VELOCITY && !reg) || (explode && st == LUMA_SITE_TL_TO_COARSER) ||
-                        (coalesce && st == LUMA_SITE_REFINED);
-        if (sp) special |= 1u << v;
-    }
+        const int sid = sz + sy * K + sx * K * M;
+        const int st = a.typ[sid];
+        if (generic || st == LUMA_SITE_BFL || (coalesce && st == LUMA_SITE_REFINED && !cf)) {
+            special |= 1u << v;
+            fn[v] = R(0);
+        } else if (coalesce && st == LUMA_SITE_REFINED) {
+            R acc = R(0);
 #pragma unroll
-    for (int v = 0; v < Q; ++v) fn[v] = ((special >> v) & 1u) ? R(0) : ld<P>(a.f, (size_t)v * n + sidv[v]);
+            for (int ii = 0; ii < 2; ++ii)
+#pragma unroll
+                for (int jj = 0; jj < 2; ++jj)
+#pragma unroll
+                    for (int kk = 0; kk < (D == 3 ? 2 : 1); ++kk)
+                        acc += ld<P>(cf, (size_t)v * cn + c0 + (size_t)kk + jj * cdj + ii * cdi);
+            fn[v] = acc / (D == 3 ? R(8) : R(4));
+        } else if (st == LUMA_SITE_VELOCITY && !reg) {
+            fn[v] = velocity_pull<Q, P>(a, j, sid, v);
+        } else {
+            const void *src = a.f;
+            size_t q = (size_t)v * n + sid;
+            if (st == LUMA_SITE_SOLID) {
+                q = (size_t)L::opp(v) * n + id;
+            } else if (st == LUMA_SITE_EXTRAPOLATE_RIGHT) {
+                q = (size_t)v * n + (sid - 2 * (K * M));
+            } else if (explode && st == LUMA_SITE_TL_TO_COARSER) {
+                // GridUtils::getCoarseIndices on the wrapped source (even index down)
+                const int pi = (sx >> 1) + a.lims[0], pj = (sy >> 1) + a.lims[2];
+                const int pk = D == 3 ? (sz >> 1) + a.lims[4] : 0;
+                src = a.parent_f;
+                q = (size_t)v * pn + pk + (size_t)pj * a.pK + (size_t)pi * a.pK * a.pM;
+            }
+            fn[v] = ld<P>(src, q);
+        }
+    }
     for (unsigned b = special & ((Q == 32 ? 0u : (1u << Q)) - 1u); b; b &= b - 1) {
         const int v = __ffs(b) - 1;
         const R val = stream_dir<Q, P, true>(a, wall, i, j, k, id, type, v);
@@ -1054,11 +1127,16 @@ cudaError_t launch_general_phaseA(const StepArgs &a, const int8_t *wall, const u
             else k_interior<Q, P, LUMA_COLL_BGK, T><<<nb, bs, 0, s>>>(a, fast);
         }
         if (part != kPhaseAInterior && ngen > 0) {
-            const int lb = (ngen + bs - 1) / bs;
-            if (a.collision == LUMA_COLL_KBC) k_stream_macro_list<Q, P, LUMA_COLL_KBC, T><<<lb, bs, 0, s>>>(a, wall, gen_ids, ngen);
+            // a list shorter than one 128-thread block per SM goes in 32-thread
+            // blocks: its sites' scattered loads (coalesce: 2^d per direction)
+            // then spread over every SM instead of queueing on a few
+            const int lbs = ngen < kSMs * bs ? 32 : bs;
+            const int lb = (ngen + lbs - 1) / lbs;
+            if (a.collision == LUMA_COLL_KBC)
+                k_stream_macro_list<Q, P, LUMA_COLL_KBC, T><<<lb, lbs, 0, s>>>(a, wall, gen_ids, ngen);
             else if (a.collision == LUMA_COLL_BGK_SMAG)
-                k_stream_macro_list<Q, P, LUMA_COLL_BGK_SMAG, T><<<lb, bs, 0, s>>>(a, wall, gen_ids, ngen);
-            else k_stream_macro_list<Q, P, LUMA_COLL_BGK, T><<<lb, bs, 0, s>>>(a, wall, gen_ids, ngen);
+                k_stream_macro_list<Q, P, LUMA_COLL_BGK_SMAG, T><<<lb, lbs, 0, s>>>(a, wall, gen_ids, ngen);
+            else k_stream_macro_list<Q, P, LUMA_COLL_BGK, T><<<lb, lbs, 0, s>>>(a, wall, gen_ids, ngen);
         }
     };
     if (tav) interior(std::true_type{});

@@ -49,7 +49,8 @@ cudaError_t launch_vec_out(const void *soa, double *aos, size_t n, int dims, cud
 // Blocks of the FP64 field reduction; its device buffer holds
 // (kReduceBlocks + 1) * 8 doubles: the result (mass, mx, my, mz, ke, max|u|,
 // nonfinite, spare) followed by one slot of partials per block.
-constexpr int kReduceBlocks = 152 * 4;
+constexpr int kSMs = 152;  // streaming multiprocessors of a GB300
+constexpr int kReduceBlocks = kSMs * 4;
 template <class P>
 cudaError_t launch_reduce(const uint8_t *typ, const void *rho, const void *u, size_t n, int dims, double *acc,
                           cudaStream_t s);
