@@ -433,7 +433,7 @@ int step_grid(luma_gpu_grid *g, int subcycle, bool write_macro) {
     CK(dispatch(d.Q, d.precision, [&](auto q, auto p) {
         return launch_general_phaseA<decltype(q)::value, decltype(p)>(a, g->wall, g->fast, g->gen_ids + list0,
                                                                       g->ngen - list0, s,
-                                                                      overlap ? kPhaseAList : kPhaseAAll);
+                                                                      overlap ? kPhaseALate : kPhaseAAll);
     }));
     if (g->nreg)
         CK(dispatch(d.Q, d.precision, [&](auto q, auto p) {

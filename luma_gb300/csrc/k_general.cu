@@ -503,6 +503,9 @@ __device__ __forceinline__ void stream_site_split(const StepArgs &a, const int8_
     const void *cf = nullptr;
     size_t cn = 0, c0 = 0, cdi = 0, cdj = 0;
     if (coalesce && !generic && !coalesce_base<Q>(a, i, j, k, cf, cn, c0, cdj, cdi)) cf = nullptr;
+    // every source's label first, with no branch between the loads: a
+    // branch on a label right after its load would serialise the Q loads
+    int sidv[Q], stv[Q];
 #pragma unroll
     for (int v = 0; v < Q; ++v) {
         int sx = i - L::c(v, 0), sy = j - L::c(v, 1), sz = k - L::c(v, 2);
@@ -510,8 +513,12 @@ __device__ __forceinline__ void stream_site_split(const StepArgs &a, const int8_
         sy = sy < 0 ? sy + M : (sy >= M ? sy - M : sy);
         if (D == 3) sz = sz < 0 ? sz + K : (sz >= K ? sz - K : sz);
         else sz = 0;
-        const int sid = sz + sy * K + sx * K * M;
-        const int st = a.typ[sid];
+        sidv[v] = sz + sy * K + sx * K * M;
+        stv[v] = a.typ[sidv[v]];
+    }
+#pragma unroll
+    for (int v = 0; v < Q; ++v) {
+        const int sid = sidv[v], st = stv[v];
         if (generic || st == LUMA_SITE_BFL || (coalesce && st == LUMA_SITE_REFINED && !cf)) {
             special |= 1u << v;
             fn[v] = R(0);
@@ -536,6 +543,10 @@ __device__ __forceinline__ void stream_site_split(const StepArgs &a, const int8_
                 q = (size_t)v * n + (sid - 2 * (K * M));
             } else if (explode && st == LUMA_SITE_TL_TO_COARSER) {
                 // GridUtils::getCoarseIndices on the wrapped source (even index down)
+                int sx = i - L::c(v, 0), sy = j - L::c(v, 1), sz = D == 3 ? k - L::c(v, 2) : 0;
+                sx = sx < 0 ? sx + N : (sx >= N ? sx - N : sx);
+                sy = sy < 0 ? sy + M : (sy >= M ? sy - M : sy);
+                if (D == 3) sz = sz < 0 ? sz + K : (sz >= K ? sz - K : sz);
                 const int pi = (sx >> 1) + a.lims[0], pj = (sy >> 1) + a.lims[2];
                 const int pk = D == 3 ? (sz >> 1) + a.lims[4] : 0;
                 src = a.parent_f;
@@ -622,6 +633,44 @@ __global__ void __launch_bounds__(128) k_stream_macro_list(StepArgs a, const int
     const int k = id % a.K, j = (id / a.K) % a.M, i = id / (a.K * a.M);
     R fn[Q];
     stream_site_split<Q, P>(a, wall, i, j, k, id, type, fn);
+    finish_site<Q, P, TAV, COLL>(a, i, j, k, id, type, fn);
+}
+
+// The same for a short list of coalescing sites (transition sites to finer
+// grids, after the sub-grids' steps), direction-parallel: a block takes
+// 128/Q sites, one thread per (site, direction) streams one population into
+// shared memory (a coalesce's 2^d loads per thread, every direction's in
+// flight at once), then one thread per site finishes it.
+template <int Q>
+constexpr int late_sites() { return 128 / Q; }
+
+template <int Q, class P, int COLL, bool TAV>
+__global__ void __launch_bounds__(128) k_stream_macro_late(StepArgs a, const int8_t *wall, const int *ids, int nids) {
+    using R = typename P::R;
+    constexpr int S = late_sites<Q>();
+    __shared__ R fs[S * Q];
+    const int t = threadIdx.x;
+    const int s = t / Q, v = t - s * Q;
+    const int idx = blockIdx.x * S + s;
+    if (s < S && idx < nids) {
+        const int id = ids[idx];
+        const int type = a.typ[id];
+        if (!phaseA_skips(a, type)) {
+            const int k = id % a.K, j = (id / a.K) % a.M, i = id / (a.K * a.M);
+            fs[t] = stream_dir<Q, P, true>(a, wall, i, j, k, id, type, v);
+        }
+    }
+    __syncthreads();
+    if (t >= S) return;
+    const int idx2 = blockIdx.x * S + t;
+    if (idx2 >= nids) return;
+    const int id = ids[idx2];
+    const int type = a.typ[id];
+    if (phaseA_skips(a, type)) return;
+    const int k = id % a.K, j = (id / a.K) % a.M, i = id / (a.K * a.M);
+    R fn[Q];
+#pragma unroll
+    for (int w = 0; w < Q; ++w) fn[w] = fs[t * Q + w];
     finish_site<Q, P, TAV, COLL>(a, i, j, k, id, type, fn);
 }
 
@@ -1121,10 +1170,21 @@ cudaError_t launch_general_phaseA(const StepArgs &a, const int8_t *wall, const u
     const int nb = (a.ncell + bs - 1) / bs;
     auto interior = [&](auto tv) {
         constexpr bool T = decltype(tv)::value;
-        if (part != kPhaseAList) {
+        if (part != kPhaseAList && part != kPhaseALate) {
             if (a.collision == LUMA_COLL_KBC) k_interior<Q, P, LUMA_COLL_KBC, T><<<nb, bs, 0, s>>>(a, fast);
             else if (a.collision == LUMA_COLL_BGK_SMAG) k_interior<Q, P, LUMA_COLL_BGK_SMAG, T><<<nb, bs, 0, s>>>(a, fast);
             else k_interior<Q, P, LUMA_COLL_BGK, T><<<nb, bs, 0, s>>>(a, fast);
+        }
+        if (part == kPhaseALate) {
+            if (ngen > 0) {
+                const int lb = (ngen + late_sites<Q>() - 1) / late_sites<Q>();
+                if (a.collision == LUMA_COLL_KBC)
+                    k_stream_macro_late<Q, P, LUMA_COLL_KBC, T><<<lb, bs, 0, s>>>(a, wall, gen_ids, ngen);
+                else if (a.collision == LUMA_COLL_BGK_SMAG)
+                    k_stream_macro_late<Q, P, LUMA_COLL_BGK_SMAG, T><<<lb, bs, 0, s>>>(a, wall, gen_ids, ngen);
+                else k_stream_macro_late<Q, P, LUMA_COLL_BGK, T><<<lb, bs, 0, s>>>(a, wall, gen_ids, ngen);
+            }
+            return;
         }
         if (part != kPhaseAInterior && ngen > 0) {
             // a list shorter than one 128-thread block per SM goes in 32-thread

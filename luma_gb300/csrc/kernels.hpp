@@ -10,7 +10,9 @@ namespace luma {
 // k_general.cu
 // Phase A of a split grid launches the interior kernel and the list kernel
 // of the other streamed sites; `part` selects both or one of them.
-enum { kPhaseAAll = 0, kPhaseAInterior = 1, kPhaseAList = 2 };
+// kPhaseALate: a list of transition sites to finer grids (coalesce), run
+// one thread per (site, direction)
+enum { kPhaseAAll = 0, kPhaseAInterior = 1, kPhaseAList = 2, kPhaseALate = 3 };
 template <int Q, class P>
 cudaError_t launch_general_phaseA(const StepArgs &a, const int8_t *wall, const uint8_t *fast, const int *gen_ids,
                                   int ngen, cudaStream_t s, int part = kPhaseAAll);
