@@ -173,9 +173,11 @@ __device__ __forceinline__ double quotient(double a, double b, double y) {
 // an interchange moves a non-zero down), so the backward solve needs no
 // scan.
 template <int NB>
-__device__ __forceinline__ void lu_factor_banded(double *A, int lda, int off, int n, int *ipiv, int band, int *lim) {
+__device__ __forceinline__ void lu_factor_banded(double *A, int lda, int off, int n, int *ipiv, int band, int *lim,
+                                                 int *rl, int *cl) {
     const unsigned full = 0xffffffffu;
     const int lane = threadIdx.x & 31;
+    const unsigned below = (1u << lane) - 1u;
     for (int r = lane; r < n; r += 32) lim[r] = r;
     __syncwarp();
     for (int k = 0; k < n; ++k) {
@@ -206,12 +208,14 @@ __device__ __forceinline__ void lu_factor_banded(double *A, int lda, int off, in
         }
         const double pv = __longlong_as_double(pvb), mine = __longlong_as_double(mineb);
         if (pi) {
+            // the interchange in the window's columns (k .. cend-1); the rows'
+            // L parts (left of k) follow after the factorisation
             __syncwarp();  // every lane's candidate reads before the interchange writes
-            for (int c = lane; c < cend; c += 32) {
+            const int c = k + lane;
+            if (c < cend) {
                 const double t = AC(k, c);
                 AC(k, c) = AC(p, c);
                 AC(p, c) = t;
-                if (c < k && !is_zero(t) && p > lim[c]) lim[c] = p;
             }
             __syncwarp();
         }
@@ -222,16 +226,40 @@ __device__ __forceinline__ void lu_factor_banded(double *A, int lda, int off, in
         const int c = k + 1 + lane;
         const bool mcol = c < cend && !is_zero(AC(k, c));
         const unsigned rmask = __ballot_sync(full, mrow), cmask = __ballot_sync(full, mcol);
+        // the non-zero rows and columns listed in order (ballot prefixes)
+        if (mrow) rl[__popc(rmask & below)] = lane;
+        if (mcol) cl[__popc(cmask & below)] = lane;
         if (lane == 0 && rmask) lim[k] = k + 32 - __clz(rmask);
         __syncwarp();
         const int nrl = __popc(rmask), npairs = nrl * __popc(cmask);
-        for (int t = lane; t < npairs; t += 32) {
-            const int ci = t / nrl, ri = t - ci * nrl;
-            const int rr = k + 1 + nth_bit(rmask, ri), cc = k + 1 + nth_bit(cmask, ci);
-            AC(rr, cc) -= AC(rr, k) * AC(k, cc);
+        if (npairs) {
+            // pair t -> (row t mod nrl, column t div nrl); the quotient as a
+            // multiply-shift, exact for t < 2^20 / nrl^2
+            const unsigned magic = (1048576u + nrl - 1) / nrl;
+            for (int t = lane; t < npairs; t += 32) {
+                const int ci = (int)(((unsigned)t * magic) >> 20), ri = t - ci * nrl;
+                const int rr = k + 1 + rl[ri], cc = k + 1 + cl[ci];
+                AC(rr, cc) -= AC(rr, k) * AC(k, cc);
+            }
         }
         __syncwarp();
     }
+    // the row interchanges in the L part: column c takes, in step order, the
+    // interchanges of the steps after it (nothing above reads these columns)
+    for (int c = lane; c < n; c += 32) {
+        int lc = lim[c];
+        for (int k = c + 1; k < n; ++k) {
+            const int p = ipiv[k] - 1;
+            if (p != k) {
+                const double t = AC(k, c);
+                AC(k, c) = AC(p, c);
+                AC(p, c) = t;
+                if (!is_zero(t) && p > lc) lc = p;
+            }
+        }
+        lim[c] = lc;
+    }
+    __syncwarp();
 }
 
 // The transposed solve with the factors of lu_factor_banded (lim included),
@@ -436,8 +464,8 @@ __device__ void lu_solve_block(double *A, int lda, int off, int n, int *ipiv, do
     __shared__ double xs[512], rd[512];
     if (threadIdx.x < 32) {
         if (band <= 15) {
-            if (band <= 7) lu_factor_banded<7>(A, lda, off, n, ipiv, band, lim);
-            else lu_factor_banded<15>(A, lda, off, n, ipiv, band, lim);
+            if (band <= 7) lu_factor_banded<7>(A, lda, off, n, ipiv, band, lim, nzr, nzc);
+            else lu_factor_banded<15>(A, lda, off, n, ipiv, band, lim, nzr, nzc);
             lu_solve_factored(A, lda, off, n, ipiv, x, band, lim, xs, rd);
         } else {
             lu_solve_dense(A, lda, off, n, ipiv, x, band, nzr, nzc, lim, xs);
@@ -589,7 +617,7 @@ __global__ void k_fem_dynamic(FemKernelArgs a) {
     double *M = a.M + (size_t)f * a.maxdof * a.maxdof;
     double *K = a.k_in_smem ? fem_smem : a.K + (size_t)f * a.maxdof * a.maxdof;
     double *Meff = a.tmp + 2 * (size_t)d0, *MF = a.tmp + 2 * (size_t)d0 + nd;
-    __shared__ int ipiv[512], lim[512];
+    __shared__ int ipiv[512], lim[512], rl[32], cl[32];
     __shared__ double sq[512], xs[512], rd[512];
     __shared__ int go;
     const double Dt = a.dt;
@@ -691,7 +719,7 @@ __global__ void k_fem_dynamic(FemKernelArgs a) {
         __syncthreads();
         // an element couples the 6 DOFs of its two nodes: half-bandwidth 5
         if (threadIdx.x < 32) {
-            lu_factor_banded<7>(K, nd, bc, nd - bc, ipiv, 5, lim);
+            lu_factor_banded<7>(K, nd, bc, nd - bc, ipiv, 5, lim, rl, cl);
             lu_solve_factored(K, nd, bc, nd - bc, ipiv, a.delU + d0 + bc, 5, lim, xs, rd);
         }
         __syncthreads();
