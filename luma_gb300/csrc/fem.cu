@@ -172,9 +172,12 @@ __device__ __forceinline__ double quotient(double a, double b, double y) {
 // holding a non-zero of L's column c (set by the multipliers, raised when
 // an interchange moves a non-zero down), so the backward solve needs no
 // scan.
+// `progress` (may be null): after step k's row interchange, row k of U is
+// final; the step count is published there (shared memory) for a forward
+// solve running beside the factorisation on another warp.
 template <int NB>
 __device__ __forceinline__ void lu_factor_banded(double *A, int lda, int off, int n, int *ipiv, int band, int *lim,
-                                                 int *rl, int *cl) {
+                                                 int *rl, int *cl, volatile int *progress = nullptr) {
     const unsigned full = 0xffffffffu;
     const int lane = threadIdx.x & 31;
     const unsigned below = (1u << lane) - 1u;
@@ -199,7 +202,13 @@ __device__ __forceinline__ void lu_factor_banded(double *A, int lda, int off, in
         }
         const int p = k + pi;
         if (lane == 0) ipiv[k] = p + 1;
-        if (best == 0) continue;  // a zero column: no interchange, no elimination
+        if (best == 0) {  // a zero column: no interchange, no elimination
+            if (progress && lane == 0) {
+                __threadfence_block();
+                *progress = k + 1;
+            }
+            continue;
+        }
         long long pvb = cv[0], mineb = 0;
 #pragma unroll
         for (int i = 1; i <= NB; ++i) {
@@ -218,6 +227,10 @@ __device__ __forceinline__ void lu_factor_banded(double *A, int lda, int off, in
                 AC(p, c) = t;
             }
             __syncwarp();
+        }
+        if (progress && lane == 0) {
+            __threadfence_block();
+            *progress = k + 1;
         }
         const double inv = 1.0 / pv;
         const double m = mine * inv;
@@ -262,25 +275,39 @@ __device__ __forceinline__ void lu_factor_banded(double *A, int lda, int off, in
     __syncwarp();
 }
 
-// The transposed solve with the factors of lu_factor_banded (lim included),
-// one warp.
-__device__ __forceinline__ void lu_solve_factored(const double *A, int lda, int off, int n, const int *ipiv, double *x,
-                                                  int band, const int *lim, double *xs, double *rd) {
+// Iterations a warp waits for the factorisation's next step before it
+// gives up (and records code 3): far beyond any step's duration.
+constexpr int kLuWaitLimit = 1 << 24;
+
+// Forward U^T y = x (into xs), one warp.  U's rows reach 2*band right of the
+// diagonal, so each lane keeps one pending row and subtracts a term as soon
+// as its unknown is known, in ascending order (the serial order); the
+// divisions use the diagonal's reciprocals (all formed at once beforehand,
+// or per column when `progress` is given: then column c waits until the
+// factorisation has published step c, and `err` takes code 3 if a wait
+// runs out).
+__device__ __forceinline__ void lu_forward(const double *A, int lda, int off, int n, const double *x, int band,
+                                           double *xs, double *rd, const volatile int *progress, int *err) {
     const unsigned full = 0xffffffffu;
     const int lane = threadIdx.x & 31;
-    // forward U^T y = x: U's rows reach 2*band right of the diagonal, so each
-    // lane keeps one pending row and subtracts a term as soon as its unknown
-    // is known, in ascending order (the serial order); the divisions use the
-    // diagonal's reciprocals, all formed at once beforehand
     for (int r = lane; r < n; r += 32) {
         xs[r] = x[r];
-        rd[r] = 1.0 / AC(r, r);
+        if (!progress) rd[r] = 1.0 / AC(r, r);
     }
     __syncwarp();
     double s = lane < n ? xs[lane] : 0.0;
     int row = lane;
     for (int c = 0; c < n; ++c) {
-        const double dc = AC(c, c), rc = rd[c];
+        if (progress) {
+            int spins = 0;
+            while (*progress <= c)
+                if (++spins > kLuWaitLimit) {
+                    if (lane == 0 && err) atomicExch(err, 3);
+                    break;
+                }
+            __threadfence_block();
+        }
+        const double dc = AC(c, c), rc = progress ? 1.0 / dc : rd[c];
         const double v = row < n ? AC(c, row) : 0.0;
         double y = 0.0;
         if (row == c) y = quotient(s, dc, rc);
@@ -294,6 +321,14 @@ __device__ __forceinline__ void lu_solve_factored(const double *A, int lda, int 
         }
     }
     __syncwarp();
+}
+
+// Backward L^T z = y (y in xs), the row interchanges in reverse, the result
+// into x; one warp.
+__device__ __forceinline__ void lu_backward(const double *A, int lda, int off, int n, const int *ipiv, double *x,
+                                            const int *lim, double *xs) {
+    const unsigned full = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
     // backward L^T z = y, rows from the last: z_r = y_r - sum over c = r+1..lim[r]
     // of L(c, r) z_c, in ascending c.  Every lane carries the running sum;
     // lane j holds z_{r+1+j} (a window shifted by one lane per row) and forms
@@ -354,6 +389,14 @@ __device__ __forceinline__ void lu_solve_factored(const double *A, int lda, int 
     }
     __syncwarp();
     for (int r = lane; r < n; r += 32) x[r] = xs[r];
+}
+
+// The transposed solve with the factors of lu_factor_banded (lim included),
+// one warp.
+__device__ __forceinline__ void lu_solve_factored(const double *A, int lda, int off, int n, const int *ipiv, double *x,
+                                                  int band, const int *lim, double *xs, double *rd) {
+    lu_forward(A, lda, off, n, x, band, xs, rd, nullptr, nullptr);
+    lu_backward(A, lda, off, n, ipiv, x, lim, xs);
 }
 
 // The general case, one warp: lanes over rows / columns, the rank-1 update
@@ -619,6 +662,7 @@ __global__ void k_fem_dynamic(FemKernelArgs a) {
     double *Meff = a.tmp + 2 * (size_t)d0, *MF = a.tmp + 2 * (size_t)d0 + nd;
     __shared__ int ipiv[512], lim[512], rl[32], cl[32];
     __shared__ double sq[512], xs[512], rd[512];
+    __shared__ volatile int lu_progress;
     __shared__ int go;
     const double Dt = a.dt;
     double *Kc = a.Kc + (size_t)f * a.maxdof * a.maxdof;
@@ -717,11 +761,17 @@ __global__ void k_fem_dynamic(FemKernelArgs a) {
         }
         for (int i = threadIdx.x; i < nd; i += blockDim.x) a.delU[d0 + i] = a.Fv[d0 + i];
         __syncthreads();
-        // an element couples the 6 DOFs of its two nodes: half-bandwidth 5
-        if (threadIdx.x < 32) {
-            lu_factor_banded<7>(K, nd, bc, nd - bc, ipiv, 5, lim, rl, cl);
-            lu_solve_factored(K, nd, bc, nd - bc, ipiv, a.delU + d0 + bc, 5, lim, xs, rd);
-        }
+        // an element couples the 6 DOFs of its two nodes: half-bandwidth 5.
+        // Warp 0 factors; warp 1 (another FP64 unit) runs the forward solve
+        // one column behind it; warp 0 then solves backward.
+        if (threadIdx.x == 0) lu_progress = 0;
+        __syncthreads();
+        if (threadIdx.x < 32)
+            lu_factor_banded<7>(K, nd, bc, nd - bc, ipiv, 5, lim, rl, cl, &lu_progress);
+        else if (threadIdx.x < 64)
+            lu_forward(K, nd, bc, nd - bc, a.delU + d0 + bc, 5, xs, rd, &lu_progress, a.error);
+        __syncthreads();
+        if (threadIdx.x < 32) lu_backward(K, nd, bc, nd - bc, ipiv, a.delU + d0 + bc, lim, xs);
         __syncthreads();
         if (keep) {
             for (int q = threadIdx.x; q < nd * nd; q += blockDim.x) Kc[q] = K[q];
@@ -1292,6 +1342,9 @@ int luma_fem_take_error(luma_gpu_grid *g) {
     if (e != cudaSuccess) return luma_set_error(LUMA_E_CUDA, "FEM error read: %s", cudaGetErrorString(e));
     if (!err) return LUMA_OK;
     cudaMemsetAsync(sc->error, 0, sizeof(int), g->stream);
+    if (err == 3)
+        return luma_set_error(LUMA_E_CUDA, "grid L%d R%d: FEM solve gave up waiting for its factorisation", g->d.level,
+                              g->d.region);
     return luma_set_error(LUMA_E_DOMAIN, "grid L%d R%d: a filament marker left its grid (code %d)", g->d.level,
                           g->d.region, err);
 }
