@@ -177,7 +177,8 @@ __device__ __forceinline__ double quotient(double a, double b, double y) {
 // solve running beside the factorisation on another warp.
 template <int NB>
 __device__ __forceinline__ void lu_factor_banded(double *A, int lda, int off, int n, int *ipiv, int band, int *lim,
-                                                 int *rl, int *cl, volatile int *progress = nullptr) {
+                                                 int *rl, int *cl, volatile int *progress = nullptr,
+                                                 bool l_swaps = true) {
     const unsigned full = 0xffffffffu;
     const int lane = threadIdx.x & 31;
     const unsigned below = (1u << lane) - 1u;
@@ -258,7 +259,9 @@ __device__ __forceinline__ void lu_factor_banded(double *A, int lda, int off, in
         __syncwarp();
     }
     // the row interchanges in the L part: column c takes, in step order, the
-    // interchanges of the steps after it (nothing above reads these columns)
+    // interchanges of the steps after it (nothing above reads these columns);
+    // or lu_l_swaps on another warp, beside the factorisation
+    if (!l_swaps) return;
     for (int c = lane; c < n; c += 32) {
         int lc = lim[c];
         for (int k = c + 1; k < n; ++k) {
@@ -275,9 +278,40 @@ __device__ __forceinline__ void lu_factor_banded(double *A, int lda, int off, in
     __syncwarp();
 }
 
+// The L-part row interchanges of lu_factor_banded on another warp, step by
+// step as the factorisation publishes them: step k's interchange of rows k
+// and p in the columns left of k touches nothing the factorisation still
+// reads (its steps read and write columns >= their own index), and column c
+// of L is complete (its multipliers written at step c) before step k > c is
+// published.  lim of those columns is raised here as in the serial pass.
+__device__ __forceinline__ void lu_l_swaps(double *A, int lda, int off, int n, const volatile int *ipiv, int *lim,
+                                           const volatile int *progress, int *err);
+
 // Iterations a warp waits for the factorisation's next step before it
 // gives up (and records code 3): far beyond any step's duration.
 constexpr int kLuWaitLimit = 1 << 24;
+
+__device__ __forceinline__ void lu_l_swaps(double *A, int lda, int off, int n, const volatile int *ipiv, int *lim,
+                                           const volatile int *progress, int *err) {
+    const int lane = threadIdx.x & 31;
+    for (int k = 1; k < n; ++k) {
+        int spins = 0;
+        while (*progress <= k)
+            if (++spins > kLuWaitLimit) {
+                if (lane == 0 && err) atomicExch(err, 3);
+                break;
+            }
+        __threadfence_block();
+        const int p = ipiv[k] - 1;
+        if (p == k) continue;
+        for (int c = lane; c < k; c += 32) {
+            const double t = AC(k, c);
+            AC(k, c) = AC(p, c);
+            AC(p, c) = t;
+            if (!is_zero(t) && p > lim[c]) lim[c] = p;
+        }
+    }
+}
 
 // Forward U^T y = x (into xs), one warp.  U's rows reach 2*band right of the
 // diagonal, so each lane keeps one pending row and subtracts a term as soon
@@ -767,9 +801,11 @@ __global__ void k_fem_dynamic(FemKernelArgs a) {
         if (threadIdx.x == 0) lu_progress = 0;
         __syncthreads();
         if (threadIdx.x < 32)
-            lu_factor_banded<7>(K, nd, bc, nd - bc, ipiv, 5, lim, rl, cl, &lu_progress);
+            lu_factor_banded<7>(K, nd, bc, nd - bc, ipiv, 5, lim, rl, cl, &lu_progress, false);
         else if (threadIdx.x < 64)
             lu_forward(K, nd, bc, nd - bc, a.delU + d0 + bc, 5, xs, rd, &lu_progress, a.error);
+        else if (threadIdx.x < 96)
+            lu_l_swaps(K, nd, bc, nd - bc, ipiv, lim, &lu_progress, a.error);
         __syncthreads();
         if (threadIdx.x < 32) lu_backward(K, nd, bc, nd - bc, ipiv, a.delU + d0 + bc, lim, xs);
         __syncthreads();

@@ -8,8 +8,13 @@ reader's two overlapping circles and a square on a D2Q9 channel (the case
 whose set-up tests/test_oracle_golden.py pins bit for bit against the
 reference build).  Here the GPU grid created with LUMA_FLAG_UNIVERSAL_EPSILON
 steps against the oracle's universal mode: epsilon, ds and support counts
-equal, then after 40 steps FP64 fields within rel L2 1e-10 and marker forces
+equal, then after 400 steps FP64 fields within rel L2 1e-10 and marker forces
 within 1e-9; shifted FP32 within its bounds (u rel L2 2e-4, forces 1e-3).
+The flow starts uniform: over the first few dozen steps some bodies' marker
+forces are residuals of order 1e-9 (against 1e-6 on the others) whose
+relative value moves by 1e-7 when the initial state moves by 1e-15 in the
+oracle itself; by step 400 every body carries a developed force (3.5e-3 to
+6e-3) and that sensitivity is 2e-13.
 """
 import json
 import os
@@ -63,8 +68,8 @@ def test_universal_epsilon_steps_match_oracle(prec):
     for b in range(len(bodies)):
         gm, om = g.ibm_markers(b), oibm.markers(b)
         assert np.array_equal(gm[:, 6:9], om[:, 6:9]), b   # epsilon, ds, supports
-    g.step(40)
-    o.step(40)
+    g.step(400)
+    o.step(400)
     gs, os_ = g.download(), o.download()
     eu = rel_l2(gs["u"], os_["u"])
     for b in range(len(bodies)):
