@@ -535,11 +535,28 @@ __device__ void lu_solve_dense(double *A, int lda, int off, int n, int *ipiv, do
 
 #undef AC
 
-__device__ void lu_solve_block(double *A, int lda, int off, int n, int *ipiv, double *x, int band) {
+__device__ void lu_solve_block(double *A, int lda, int off, int n, int *ipiv, double *x, int band,
+                               int *err = nullptr) {
     __shared__ int nzr[512], nzc[512];
     __shared__ int lim[512];
     __shared__ double xs[512], rd[512];
-    if (threadIdx.x < 32) {
+    __shared__ volatile int progress;
+    if (band <= 15 && blockDim.x >= 96) {
+        // warp 0 factors, warp 1 runs the forward solve one column behind,
+        // warp 2 applies the L-part interchanges; warp 0 then solves backward
+        if (threadIdx.x == 0) progress = 0;
+        __syncthreads();
+        if (threadIdx.x < 32) {
+            if (band <= 7) lu_factor_banded<7>(A, lda, off, n, ipiv, band, lim, nzr, nzc, &progress, false);
+            else lu_factor_banded<15>(A, lda, off, n, ipiv, band, lim, nzr, nzc, &progress, false);
+        } else if (threadIdx.x < 64) {
+            lu_forward(A, lda, off, n, x, band, xs, rd, &progress, err);
+        } else if (threadIdx.x < 96) {
+            lu_l_swaps(A, lda, off, n, ipiv, lim, &progress, err);
+        }
+        __syncthreads();
+        if (threadIdx.x < 32) lu_backward(A, lda, off, n, ipiv, x, lim, xs);
+    } else if (threadIdx.x < 32) {
         if (band <= 15) {
             if (band <= 7) lu_factor_banded<7>(A, lda, off, n, ipiv, band, lim, nzr, nzc);
             else lu_factor_banded<15>(A, lda, off, n, ipiv, band, lim, nzr, nzc);
@@ -890,12 +907,16 @@ __global__ void k_fem_dynamic(FemKernelArgs a) {
     }
 }
 
-__device__ double delta_kernel_d(double radius, double dilation) {
-    const double mag_r = fabs(radius) / dilation;
+// The Roma kernel at dilation 1 with its two divisions (by 6 and by 3)
+// formed as correctly rounded quotients from the constants' reciprocals
+// (quotient(): the same bits as the division, fewer FP64 operations).
+__device__ __forceinline__ double roma(double radius) {
+    const double mag_r = fabs(radius);  // |r| / 1.0
     if (mag_r > 1.5) return 0.0;
-    if (mag_r > 0.5) return (5.0 - (3.0 * mag_r) - sqrt(-3.0 * ((1.0 - mag_r) * (1.0 - mag_r)) + 1.0)) / 6.0;
-    return (1.0 + sqrt(1.0 - 3.0 * (mag_r * mag_r))) / 3.0;
+    if (mag_r > 0.5) return quotient(5.0 - (3.0 * mag_r) - sqrt(-3.0 * ((1.0 - mag_r) * (1.0 - mag_r)) + 1.0), 6.0, 1.0 / 6.0);
+    return quotient(1.0 + sqrt(1.0 - 3.0 * (mag_r * mag_r)), 3.0, 1.0 / 3.0);
 }
+
 
 // Supports, ds and epsilon of one filament's markers (ibm_findSupport,
 // ibm_computeDs, ibm_findEpsilon for a moving body).
@@ -921,12 +942,12 @@ __global__ void k_flex_support(FemKernelArgs a) {
     if (f >= a.nfil || (a.skip && *a.skip)) return;
     const int mk0 = a.mk_off[f], nmk = a.mk_off[f + 1] - mk0;
     const int D = a.dims;
-    const double dh = a.dh;
+    const double dh = a.dh, rdh = 1.0 / dh;  // divisions by dh as quotient(., dh, rdh)
     const FlexArgs &x = a.flex;
     // near node per (marker, axis); the test bits start clear, ds at 10
     for (int q = threadIdx.x; q < 3 * nmk; q += blockDim.x) {
         const int m = q / 3, d = q % 3, g = mk0 + m;
-        x.cagei[4 * g + d] = d < D ? (int)floor((x.pos[3 * g + d] - a.gstart[d]) / dh) : 0;
+        x.cagei[4 * g + d] = d < D ? (int)floor(quotient(x.pos[3 * g + d] - a.gstart[d], dh, rdh)) : 0;
         if (d == 0) {
             x.cagei[4 * g + 3] = 0;
             x.ds[g] = 10.0;
@@ -943,10 +964,10 @@ __global__ void k_flex_support(FemKernelArgs a) {
         const double nearp = act ? h[ni[d]] : 0.0;
         const double p = x.pos[3 * g + d];
         const double e = act ? nearp + (o - 2) * dh : nearp;
-        const bool cage = !act || fabs(p - e) / dh < 1.5;
+        const bool cage = !act || quotient(fabs(p - e), dh, rdh) < 1.5;
         const bool dom = !act || !(e < a.edges[2 * d] || e > a.edges[2 * d + 1]);
         x.cage[32 * (size_t)g + w] = e;
-        x.cage[32 * (size_t)g + 15 + w] = act ? delta_kernel_d((e - p) / dh, 1.0) : 1.0;
+        x.cage[32 * (size_t)g + 15 + w] = act ? roma(quotient(e - p, dh, rdh)) : 1.0;
         if (cage && dom) atomicOr(&x.cagei[4 * g + 3], 1 << w);
     }
     __syncthreads();
@@ -1002,7 +1023,7 @@ __global__ void k_flex_support(FemKernelArgs a) {
             const double v = x.pos[3 * g + d] - x.pos[3 * h + d];
             r += v * v;
         }
-        const double dist = sqrt(r) / dh;
+        const double dist = quotient(sqrt(r), dh, rdh);
         if (dist < 10.0)
             atomicMin(reinterpret_cast<unsigned long long *>(&x.ds[g]), (unsigned long long)__double_as_longlong(dist));
     }
@@ -1044,7 +1065,7 @@ __global__ void k_flex_support(FemKernelArgs a) {
                 const int d = w / 5;
                 fj[w] = 0.0;
                 if (d < D && (w % 5 == 2 || cage_ok(fl, d, w % 5)))
-                    fj[w] = delta_kernel_d((x.pos[3 * gJ + d] - rec[w]) / dh, 1.0);
+                    fj[w] = roma(quotient(x.pos[3 * gJ + d] - rec[w], dh, rdh));
             }
             int ns = 0;
             auto term = [&](int oi, int oj, int ok) {
@@ -1086,7 +1107,7 @@ __global__ void k_flex_support(FemKernelArgs a) {
         if (!is_zero(A[q])) atomicMax(&band, off < 0 ? -off : off);
     }
     __syncthreads();
-    lu_solve_block(A, nmk, 0, nmk, ipiv, x.eps + mk0, band < nmk ? band : nmk);
+    lu_solve_block(A, nmk, 0, nmk, ipiv, x.eps + mk0, band < nmk ? band : nmk, a.error);
 }
 
 // max over flexible markers of |U - U_km1| / (L_UX0 dt/dh)  (ibm_checkVelDiff)
