@@ -494,7 +494,15 @@ __device__ __forceinline__ void stream_site_split(const StepArgs &a, const int8_
     const bool reg = (a.flags & LUMA_FLAG_REGULARISED) != 0;
     const bool explode = a.parent_f && a.subcycle == 0;
     const bool coalesce = a.nchild && type == LUMA_SITE_TL_TO_FINER;
-    const bool generic = type == LUMA_SITE_SLIP || type == LUMA_SITE_BFL;
+    // slip sites take the full rule in every direction; at BFL sites (or
+    // next to them) only the directions with a BFL link do: the others stream
+    // as usual (stream_dir's BFL branch falls through for them)
+    const bool generic = type == LUMA_SITE_SLIP;
+    uint32_t links = 0xffffffffu;  // without link tables every BFL-touched direction goes to the full rule
+    if (a.bfl_rec) {
+        const int r = a.bfl_rec[id];
+        links = r >= 0 ? a.bfl_mask[r] : 0u;
+    }
     const size_t pn = explode ? (size_t)a.pN * a.pM * a.pK : 0;
     unsigned special = generic ? 0xffffffffu : 0u;
     // coalesce (_LBM_coalesce_opt, :591-636, GridUtils::getFineIndices):
@@ -519,7 +527,8 @@ __device__ __forceinline__ void stream_site_split(const StepArgs &a, const int8_
 #pragma unroll
     for (int v = 0; v < Q; ++v) {
         const int sid = sidv[v], st = stv[v];
-        if (generic || st == LUMA_SITE_BFL || (coalesce && st == LUMA_SITE_REFINED && !cf)) {
+        if (generic || ((type == LUMA_SITE_BFL || st == LUMA_SITE_BFL) && ((links >> v) & 1u)) ||
+            (coalesce && st == LUMA_SITE_REFINED && !cf)) {
             special |= 1u << v;
             fn[v] = R(0);
         } else if (coalesce && st == LUMA_SITE_REFINED) {
