@@ -226,10 +226,11 @@ int luma_gpu_reduce(luma_gpu_grid *grid, luma_reduction *out);
  * rho[n], u[d*n + id] (FP64).  It allocates nothing: its scratch is a fixed
  * 64 KiB device array held by every GPU that loads the library.  At most
  * 16,777,216 sites (larger n is rejected with LUMA_E_INVALID).  The first
- * call on a device sets up that device's scratch address, so make it before
- * any stream capture; the address is cached for the process, so the call is
+ * call on a device sets up that device's scratch address; the address is
+ * cached for the process, so the call is
  * not valid after cudaDeviceReset.  Calls share the scratch: calls whose
- * kernels overlap on the GPU race.  Blocks until the result is on the host. */
+ * kernels overlap on the GPU race.  Blocks until the result is on the host,
+ * so a stream under capture is refused (LUMA_E_INVALID, nothing recorded). */
 int luma_gpu_reduce_fields_noalloc(const uint8_t *typ, const double *rho, const double *u, int64_t n,
                                    int dims, void *cuda_stream, luma_reduction *out);
 

@@ -20,8 +20,8 @@
 // In host code the array's name is only a host-side stand-in, not a device
 // address: the device address is obtained once per device with
 // cudaGetSymbolAddress, with that device current, and passed to the
-// kernels.  The first call on each device performs that set-up, so make the
-// first call on a device before starting any stream capture.  The address
+// kernels.  The first call on each device performs that set-up.  A call on
+// a stream under capture is refused before it does anything.  The address
 // is cached for the life of the process: after cudaDeviceReset the cached
 // address is stale and the call must not be used again in that process.
 #include <cuda_runtime.h>
@@ -138,15 +138,25 @@ extern "C" int luma_gpu_reduce_fields_noalloc(const uint8_t *typ, const double *
                               "luma_gpu_reduce_fields_noalloc handles at most %lld sites (its fixed scratch holds "
                               "%d partial sums of %d sites); got %lld — use luma_gpu_reduce",
                               (long long)kMaxSites, kBlocks, kThreads * kItemsPerThread, (long long)n);
+    cudaStream_t s = static_cast<cudaStream_t>(cuda_stream);
+    // the call ends with a copy to the host and a wait on the stream, and a
+    // capturing stream takes neither: refuse before anything is recorded
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    cudaError_t e = cudaStreamIsCapturing(s, &cap);
+    if (e != cudaSuccess) cudaGetLastError();  // this query's own error, reported below
+    if (e != cudaSuccess || cap != cudaStreamCaptureStatusNone)
+        return luma_set_error(LUMA_E_INVALID,
+                              "luma_gpu_reduce_fields_noalloc cannot run on a stream under capture (it blocks until "
+                              "the sums are on the host)%s%s",
+                              e != cudaSuccess ? ": " : "", e != cudaSuccess ? cudaGetErrorString(e) : "");
     double *scratch = nullptr;
     int rc = scratch_address(&scratch);
     if (rc) return rc;
     // an error left pending by an earlier, unrelated call belongs to that
     // call's owner: report it without clearing it and launch nothing
-    cudaError_t e = cudaPeekAtLastError();
+    e = cudaPeekAtLastError();
     if (e != cudaSuccess)
         return luma_set_error(LUMA_E_CUDA, "a CUDA error was pending before the reduction: %s", cudaGetErrorString(e));
-    cudaStream_t s = static_cast<cudaStream_t>(cuda_stream);
     const int64_t chunk = (int64_t)kThreads * kItemsPerThread;
     const int nblocks = (int)((n + chunk - 1) / chunk);
     k_partials<<<nblocks, kThreads, 0, s>>>(typ, rho, u, n, dims, chunk, scratch);

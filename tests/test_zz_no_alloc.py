@@ -7,7 +7,8 @@ FP64 sums as luma_gpu_reduce on the same fields — here within the FP64
 parity tolerance of these tests (relative 1e-10) — on two calls in a row,
 because both calls share the entry point's fixed scratch array; the second
 call must leave the device's free memory unchanged; and it must refuse a
-size beyond its stated maximum with a clear error.
+size beyond its stated maximum with a clear error, and a stream under
+capture.
 
 This file is collected last so that a stop-at-first-failure run has already
 run every other test; it also passes when run alone in a fresh process.
@@ -88,3 +89,39 @@ def test_noalloc_rejects_sizes_beyond_its_maximum():
     assert rc == A.LUMA_E_INVALID
     msg = L.luma_gpu_last_error_string().decode()
     assert "at most 16777216 sites" in msg
+
+
+def test_noalloc_refuses_a_stream_under_capture():
+    """The call copies its sums to the host and waits on the stream, which a
+    capturing stream cannot do: it is refused with LUMA_E_INVALID before
+    anything is recorded, the capture completes and replays, and the same
+    stream takes the call once the capture has ended."""
+    import torch
+    L = _lib()
+    dev = torch.device("cuda", 0)
+    n = 5000
+    typ = torch.full((n,), 1, dtype=torch.uint8, device=dev)          # LUMA_SITE_FLUID
+    rho = torch.full((n,), 1.25, dtype=torch.float64, device=dev)
+    u = torch.zeros(3 * n, dtype=torch.float64, device=dev)
+    y = torch.zeros(n, dtype=torch.float64, device=dev)
+    s = torch.cuda.Stream(dev)
+    out = A.Reduction()
+    with torch.cuda.stream(s):    # the device's scratch address is looked up outside the capture
+        assert L.luma_gpu_reduce_fields_noalloc(typ.data_ptr(), rho.data_ptr(), u.data_ptr(), n, 3,
+                                                s.cuda_stream, C.byref(out)) == A.LUMA_OK
+    torch.cuda.synchronize(dev)
+    graph = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(graph, stream=s):
+        rc = L.luma_gpu_reduce_fields_noalloc(typ.data_ptr(), rho.data_ptr(), u.data_ptr(), n, 3,
+                                              s.cuda_stream, C.byref(out))
+        y.copy_(rho * 2.0)
+    assert rc == A.LUMA_E_INVALID
+    assert "under capture" in L.luma_gpu_last_error_string().decode()
+    graph.replay()
+    torch.cuda.synchronize(dev)
+    assert float(y.sum()) == 2.5 * n
+    out = A.Reduction()
+    from luma_gb300.gpu import check
+    check(L.luma_gpu_reduce_fields_noalloc(typ.data_ptr(), rho.data_ptr(), u.data_ptr(), n, 3,
+                                           s.cuda_stream, C.byref(out)))
+    assert out.mass == 1.25 * n and out.nonfinite == 0 and out.max_speed == 0.0
