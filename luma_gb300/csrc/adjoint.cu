@@ -853,11 +853,7 @@ void marker_gradient(const luma_gpu_grid *g, const IbmBody &bd, const double *Gd
 
 int luma_adj_step_hook(luma_gpu_grid *g, const StepArgs &a) {
     AdjState &st = *g->adj;
-    cudaStream_t s = g->stream;
-    const IbmDevice &dv = g->ibm->dev;
     (void)a;
-    (void)s;
-    (void)dv;
     // the step's records went where luma_adj_redirect pointed them
     if (st.mode == 1 || st.mode == 2) st.tape_pos++;
     cudaError_t e = cudaGetLastError();

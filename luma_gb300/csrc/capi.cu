@@ -360,6 +360,15 @@ bool overlap_kids(const luma_gpu_grid *g) {
     return !g->kids.empty() && g->fast && !g->bulk && !g->adj && g->kid_stream && g->ev_fork && g->ev_join;
 }
 
+// The interior kernel and the listed sites' kernel read the populations
+// of the last step and write only their own sites (populations, u, rho,
+// time averages), so the list may run on its own stream beside the
+// interior: on the small grids of a refinement tree each is a short,
+// latency-bound launch on the sub-grids' dependency chain.
+bool split_list(const luma_gpu_grid *g) {
+    return g->fast && !g->bulk && !g->adj && g->list_stream && g->ev_lfork && g->ev_ljoin;
+}
+
 int step_grid(luma_gpu_grid *g, int subcycle, bool write_macro) {
     if (g->d.reynolds_ramp > 0.0) update_reynolds(g);
     const luma_grid_desc &d = g->d;
@@ -388,11 +397,17 @@ int step_grid(luma_gpu_grid *g, int subcycle, bool write_macro) {
             CK(dispatch(d.Q, d.precision, [&](auto q, auto p) {
                 return launch_general_phaseC<decltype(q)::value, decltype(p)>(ai, g->defer_ids, g->ndefer, s);
             }));
+        // the early list beside the interior, unless the deferred collision
+        // above (which may touch listed sites) holds the stream's order
+        const bool side = g->ngen_early > 0 && !early_c && split_list(g);
+        if (side) CK(cudaStreamWaitEvent(g->list_stream, g->ev_fork, 0));
         if (g->ngen_early > 0)
             CK(dispatch(d.Q, d.precision, [&](auto q, auto p) {
                 return launch_general_phaseA<decltype(q)::value, decltype(p)>(ai, g->wall, g->fast, g->gen_ids,
-                                                                              g->ngen_early, s, kPhaseAList);
+                                                                              g->ngen_early,
+                                                                              side ? g->list_stream : s, kPhaseAList);
             }));
+        if (side) CK(cudaEventRecord(g->ev_ljoin, g->list_stream));
         CK(cudaStreamWaitEvent(g->kid_stream, g->ev_fork, 0));
         for (luma_gpu_grid *c : g->kids) set_tree_stream(c, g->kid_stream);
         int rc = LUMA_OK;
@@ -402,6 +417,7 @@ int step_grid(luma_gpu_grid *g, int subcycle, bool write_macro) {
         if (rc) return rc;
         CK(cudaEventRecord(g->ev_join, g->kid_stream));
         CK(cudaStreamWaitEvent(s, g->ev_join, 0));
+        if (side) CK(cudaStreamWaitEvent(s, g->ev_ljoin, 0));
     } else {
         for (luma_gpu_grid *c : g->kids)
             for (int it = 0; it < 2; ++it) {
@@ -430,11 +446,26 @@ int step_grid(luma_gpu_grid *g, int subcycle, bool write_macro) {
         if (rc) return rc;
     }
     const int list0 = overlap ? g->ngen_early : 0;  // the rest of the list ran beside the sub-grids
-    CK(dispatch(d.Q, d.precision, [&](auto q, auto p) {
-        return launch_general_phaseA<decltype(q)::value, decltype(p)>(a, g->wall, g->fast, g->gen_ids + list0,
-                                                                      g->ngen - list0, s,
-                                                                      overlap ? kPhaseALate : kPhaseAAll);
-    }));
+    if (!overlap && g->kids.empty() && g->ngen > 0 && split_list(g)) {
+        CK(cudaEventRecord(g->ev_lfork, s));
+        CK(cudaStreamWaitEvent(g->list_stream, g->ev_lfork, 0));
+        CK(dispatch(d.Q, d.precision, [&](auto q, auto p) {
+            return launch_general_phaseA<decltype(q)::value, decltype(p)>(a, g->wall, g->fast, g->gen_ids, g->ngen,
+                                                                          g->list_stream, kPhaseAList);
+        }));
+        CK(dispatch(d.Q, d.precision, [&](auto q, auto p) {
+            return launch_general_phaseA<decltype(q)::value, decltype(p)>(a, g->wall, g->fast, g->gen_ids, g->ngen, s,
+                                                                          kPhaseAInterior);
+        }));
+        CK(cudaEventRecord(g->ev_ljoin, g->list_stream));
+        CK(cudaStreamWaitEvent(s, g->ev_ljoin, 0));
+    } else {
+        CK(dispatch(d.Q, d.precision, [&](auto q, auto p) {
+            return launch_general_phaseA<decltype(q)::value, decltype(p)>(a, g->wall, g->fast, g->gen_ids + list0,
+                                                                          g->ngen - list0, s,
+                                                                          overlap ? kPhaseALate : kPhaseAAll);
+        }));
+    }
     if (g->nreg)
         CK(dispatch(d.Q, d.precision, [&](auto q, auto p) {
             return launch_general_phaseB<decltype(q)::value, decltype(p)>(a, g->wall, g->reg, g->nreg, s);
@@ -640,6 +671,9 @@ void free_grid(luma_gpu_grid *g) {
     if (g->kid_stream) cudaStreamDestroy(g->kid_stream);
     if (g->ev_fork) cudaEventDestroy(g->ev_fork);
     if (g->ev_join) cudaEventDestroy(g->ev_join);
+    if (g->list_stream) cudaStreamDestroy(g->list_stream);
+    if (g->ev_lfork) cudaEventDestroy(g->ev_lfork);
+    if (g->ev_ljoin) cudaEventDestroy(g->ev_ljoin);
     delete g;
 }
 
@@ -779,6 +813,16 @@ int luma_gpu_grid_create(const luma_grid_desc *desc, luma_gpu_grid *parent, luma
     g->d.lattyp = nullptr;
     g->d.xpos = g->d.ypos = g->d.zpos = nullptr;
     g->d.ux_in = g->d.uy_in = g->d.uz_in = nullptr;
+    {
+        // the listed sites' kernel steps beside the interior kernel
+        // (step_grid); without the stream both run in line
+        int least = 0, greatest = 0;
+        cudaDeviceGetStreamPriorityRange(&least, &greatest);
+        if (cudaStreamCreateWithPriority(&g->list_stream, cudaStreamNonBlocking, greatest) != cudaSuccess ||
+            cudaEventCreateWithFlags(&g->ev_lfork, cudaEventDisableTiming) != cudaSuccess ||
+            cudaEventCreateWithFlags(&g->ev_ljoin, cudaEventDisableTiming) != cudaSuccess)
+            cudaGetLastError();
+    }
     if (parent) {
         if (!parent->kid_stream) {
             // the parent's sub-grids step on a stream of the highest priority

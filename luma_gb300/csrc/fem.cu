@@ -122,12 +122,6 @@ __device__ __forceinline__ bool is_zero(double v) { return (__double_as_longlong
 __device__ __forceinline__ unsigned long long mag_bits(double v) {
     return (unsigned long long)__double_as_longlong(v) & 0x7fffffffffffffffull;
 }
-// Position of the set bit of `mask` with `nth` set bits below it (mask has
-// more than nth set bits).
-__device__ __forceinline__ int nth_bit(unsigned mask, int nth) {
-    for (int i = 0; i < nth; ++i) mask &= mask - 1;
-    return __ffs(mask) - 1;
-}
 // (32-bit index arithmetic: lda and n are at most 512)
 #define AC(r, c) A[(off + (c)) * lda + (off + (r))]
 

@@ -61,6 +61,11 @@ struct luma_gpu_grid {
     // priority) beside this grid's interior kernel; fork/join events
     cudaStream_t kid_stream = nullptr;
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+    // the listed sites' kernel runs on list_stream (high priority) beside
+    // the interior kernel: both pull from the same populations and write
+    // only their own sites; fork/join events
+    cudaStream_t list_stream = nullptr;
+    cudaEvent_t ev_lfork = nullptr, ev_ljoin = nullptr;
     luma::IbmState *ibm = nullptr;
     luma::AdjState *adj = nullptr;   // discrete-adjoint tape (adjoint.cu)
     luma::StepGraph *graph = nullptr;  // level 0: two steps of the tree as a CUDA graph (capi.cu)

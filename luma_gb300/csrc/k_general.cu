@@ -421,6 +421,13 @@ __device__ __forceinline__ void collide_site(const StepArgs &a, int id, typename
             M[2] += fneq[v] * R(cy * cy);
         }
     }
+    // FP32 (shifted) path: the divisions by 6 and by the equilibrium as
+    // products with reciprocals (an FP32 division is a multi-instruction
+    // sequence, ~60 per site here); FP64 keeps the reference's divisions.
+    auto sixth = [](R x) -> R {
+        if constexpr (P::shifted) return x * R(1.0 / 6.0);
+        else return x / R(6);
+    };
     R ds[Q];
     R top = R(0), bot = R(0);
 #pragma unroll
@@ -432,11 +439,11 @@ __device__ __forceinline__ void collide_site(const StepArgs &a, int id, typename
                 if (cy == 0) {
                     if (cz == 0) s = (-(M[0] + M[8] + M[12]));
                     else
-                        s = ((-(M[0] - M[12]) - (M[8] - M[12])) / R(6) + (M[0] + M[8] + M[12]) / R(6) -
+                        s = (sixth((-(M[0] - M[12]) - (M[8] - M[12]))) + sixth(M[0] + M[8] + M[12]) -
                              R(cz) * R(0.5) * (M[2] + M[9]));
                 } else {
                     if (cz == 0)
-                        s = ((-(M[0] - M[12]) + R(2) * (M[8] - M[12])) / R(6) + (M[0] + M[8] + M[12]) / R(6) -
+                        s = (sixth((-(M[0] - M[12]) + R(2) * (M[8] - M[12]))) + sixth(M[0] + M[8] + M[12]) -
                              R(cy) * R(0.5) * (M[1] + M[11]));
                     else
                         s = (R(cy * cz) * R(0.25) * M[10] + (R(cz) * R(0.25) * M[9] + R(cy) * R(0.25) * M[11]));
@@ -444,7 +451,7 @@ __device__ __forceinline__ void collide_site(const StepArgs &a, int id, typename
             } else {
                 if (cy == 0) {
                     if (cz == 0)
-                        s = ((R(2) * (M[0] - M[12]) - (M[8] - M[12])) / R(6) + (M[0] + M[8] + M[12]) / R(6) -
+                        s = (sixth((R(2) * (M[0] - M[12]) - (M[8] - M[12]))) + sixth(M[0] + M[8] + M[12]) -
                              R(cx) * R(0.5) * (M[4] + M[7]));
                     else
                         s = (R(cx * cz) * R(0.25) * M[6] + (R(cz) * R(0.25) * M[2] + R(cx) * R(0.25) * M[7]));
@@ -462,8 +469,14 @@ __device__ __forceinline__ void collide_site(const StepArgs &a, int id, typename
         ds[v] = s;
         const R dh = fneq[v] - s;
         const R feq_true = P::shifted ? fe[v] + R(L::w(v)) * rho0_of<P>(a) : fe[v];
-        top += s * dh / feq_true;
-        bot += dh * dh / feq_true;
+        if constexpr (P::shifted) {
+            const R rf = __frcp_rn(feq_true);
+            top += s * dh * rf;
+            bot += dh * dh * rf;
+        } else {
+            top += s * dh / feq_true;
+            bot += dh * dh / feq_true;
+        }
     }
     const R beta_m1 = R(2) / omega_of<P>(a);
     const R gamma = bot == R(0) ? R(2) : beta_m1 - (R(2) - beta_m1) * (top / bot);
