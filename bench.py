@@ -370,6 +370,24 @@ def measure_adjoint(nsteps: int = 4000, precisions=("fp32_shifted", "fp64")) -> 
     return out
 
 
+def trace_path(args, workload: str, prec: str) -> str | None:
+    """Where --trace puts a workload's kernel timeline (a Chrome trace and
+    its text summary beside it, written once the workload has run)."""
+    if not args.trace:
+        return None
+    os.makedirs(args.trace, exist_ok=True)
+    return os.path.join(args.trace, f"{workload}_{prec}_timeline.json")
+
+
+def write_trace_summaries(args, workload: str, names) -> None:
+    from luma_gb300 import timeline
+    for name in names:
+        p = trace_path(args, workload, name)
+        if p and os.path.exists(p):
+            with open(p[:-5] + ".txt", "w") as fh:
+                fh.write(timeline.summarize(p, 4))
+
+
 def run_sphere_workload(args) -> int:
     """D3Q19 flow past an IB sphere with two refinement levels (384x192x192
     base; ``--size`` scales the base x extent and everything with it):
@@ -391,7 +409,7 @@ def run_sphere_workload(args) -> int:
             continue
         levels, markers = WL.sphere_refined(**kw)
         res[name] = WL.run_sphere(prec, args.steps, warmup=args.warmup, levels=levels, markers=markers,
-                                  diameter_lu=kw["diameter_lu"])
+                                  diameter_lu=kw["diameter_lu"], trace=trace_path(args, "sphere", name))
     t1 = time.monotonic()
     clocks = sampler.summary(t0, t1)
     head = res.get("fp32_shifted") or res.get("fp64")
@@ -428,6 +446,7 @@ def run_sphere_workload(args) -> int:
                                 "max_abs_rho_level0": float(np.max(np.abs(r32 - r64))),
                                 "cd_rel": abs(res["fp32_shifted"]["cd"] - res["fp64"]["cd"]) / abs(res["fp64"]["cd"]),
                                 "speedup": round(res["fp32_shifted"]["mlups"] / res["fp64"]["mlups"], 3)}
+    write_trace_summaries(args, "sphere", res)
     print(json.dumps(line), flush=True)
     return 0
 
@@ -452,7 +471,8 @@ def run_filaments_workload(args) -> int:
         if args.precision not in ("both", name.split("_")[0]):
             continue
         levels, fils = WL.kbc_filaments(**kw)
-        res[name] = WL.run_filaments(prec, args.steps, warmup=args.warmup, levels=levels, fils=fils)
+        res[name] = WL.run_filaments(prec, args.steps, warmup=args.warmup, levels=levels, fils=fils,
+                                     trace=trace_path(args, "filaments", name))
     t1 = time.monotonic()
     clocks = sampler.summary(t0, t1)
     peaks = read_peaks()
@@ -488,6 +508,7 @@ def run_filaments_workload(args) -> int:
             "rel_l2_u_level0": float(np.linalg.norm(res["fp32_shifted"]["u0"] - res["fp64"]["u0"]) /
                                      np.linalg.norm(res["fp64"]["u0"])),
             "speedup": round(res["fp32_shifted"]["mlups"] / res["fp64"]["mlups"], 3)}
+    write_trace_summaries(args, "filaments", res)
     print(json.dumps(line), flush=True)
     return 0
 
@@ -783,6 +804,9 @@ def main(argv=None) -> int:
     ap.add_argument("--cpu-steps", type=int, default=4, help="timed all-thread steps of the CPU baseline")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint workload measurement")
+    ap.add_argument("--trace", default=None, metavar="DIR",
+                    help="sphere/filaments: after the measurement, record 4 more steps as a kernel timeline "
+                         "(CUPTI through torch.profiler) into DIR, with a text summary")
     args = ap.parse_args(argv)
     if args.warmup < 5:
         args.warmup = 5     # the headline warm-up captures its step graph in >= 4 steps after one

@@ -393,19 +393,22 @@ int step_grid(luma_gpu_grid *g, int subcycle, bool write_macro) {
             return launch_general_phaseA<decltype(q)::value, decltype(p)>(ai, g->wall, g->fast, g->gen_ids, g->ngen, s,
                                                                           kPhaseAInterior);
         }));
-        if (early_c)
-            CK(dispatch(d.Q, d.precision, [&](auto q, auto p) {
-                return launch_general_phaseC<decltype(q)::value, decltype(p)>(ai, g->defer_ids, g->ndefer, s);
-            }));
-        // the early list beside the interior, unless the deferred collision
-        // above (which may touch listed sites) holds the stream's order
-        const bool side = g->ngen_early > 0 && !early_c && split_list(g);
+        // the early list and the early deferred collision beside the
+        // interior: the list's phase A skips the solid, refined and velocity
+        // sites, which are the deferred sites here, the collision writes only
+        // those sites' new populations, and both only read u and rho at
+        // velocity sites; neither touches the interior sites' outputs
+        const bool side = (g->ngen_early > 0 || early_c) && split_list(g);
+        cudaStream_t ls = side ? g->list_stream : s;
         if (side) CK(cudaStreamWaitEvent(g->list_stream, g->ev_fork, 0));
         if (g->ngen_early > 0)
             CK(dispatch(d.Q, d.precision, [&](auto q, auto p) {
                 return launch_general_phaseA<decltype(q)::value, decltype(p)>(ai, g->wall, g->fast, g->gen_ids,
-                                                                              g->ngen_early,
-                                                                              side ? g->list_stream : s, kPhaseAList);
+                                                                              g->ngen_early, ls, kPhaseAList);
+            }));
+        if (early_c)
+            CK(dispatch(d.Q, d.precision, [&](auto q, auto p) {
+                return launch_general_phaseC<decltype(q)::value, decltype(p)>(ai, g->defer_ids, g->ndefer, ls);
             }));
         if (side) CK(cudaEventRecord(g->ev_ljoin, g->list_stream));
         CK(cudaStreamWaitEvent(g->kid_stream, g->ev_fork, 0));

@@ -95,8 +95,11 @@ def upload_level(g, lv) -> None:
 
 
 def run_sphere(precision: int, steps: int, warmup: int = 5, stream=None, levels=None, markers=None,
-               diameter_lu: float = 24.0, u_lu: float = 0.04, body_level: int = BODY_LEVEL) -> dict:
-    """Steps the sphere workload; returns timing, Cd and the L0 fields."""
+               diameter_lu: float = 24.0, u_lu: float = 0.04, body_level: int = BODY_LEVEL,
+               trace: str | None = None, trace_steps: int = 4) -> dict:
+    """Steps the sphere workload; returns timing, Cd and the L0 fields.
+    With `trace`, `trace_steps` further steps (after everything measured)
+    are recorded as a kernel timeline to that path (luma_gb300.timeline)."""
     from .gpu import GpuGrid
     if levels is None:
         levels, markers = sphere_refined(diameter_lu=diameter_lu, u_lu=u_lu)
@@ -128,6 +131,9 @@ def run_sphere(precision: int, steps: int, warmup: int = 5, stream=None, levels=
            "mlups": lu * steps / sec / 1e6, "lattice_updates_per_step": lu, "cd": cd, "force": F.tolist(),
            "ibm_init_s": t_init, "u0": st["u"], "rho0": st["rho"],
            "sites": [lv.ncell for lv in levels], "markers": int(len(markers))}
+    if trace:
+        from . import timeline
+        timeline.record(grids[0], trace_steps, trace)
     for g in reversed(grids):
         g.close()
     return out
@@ -183,8 +189,10 @@ def kbc_filaments(nx: int = 512, ny: int = 256, nz: int = 256, n_fil: int = 64, 
     return [l0, l1], fils
 
 
-def run_filaments(precision: int, steps: int, warmup: int = 2, levels=None, fils=None, fix_kbc: bool = True) -> dict:
-    """Steps the filament-array workload; returns timing and tip positions."""
+def run_filaments(precision: int, steps: int, warmup: int = 2, levels=None, fils=None, fix_kbc: bool = True,
+                  trace: str | None = None, trace_steps: int = 4) -> dict:
+    """Steps the filament-array workload; returns timing and tip positions.
+    `trace` as for run_sphere."""
     from .gpu import GpuGrid
     if levels is None:
         levels, fils = kbc_filaments()
@@ -215,6 +223,9 @@ def run_filaments(precision: int, steps: int, warmup: int = 2, levels=None, fils
            "mlups": lu * steps / sec / 1e6, "lattice_updates_per_step": lu, "ibm_init_s": t_init,
            "tip0": tip0, "tips": tips, "u0": st["u"], "sites": [lv.ncell for lv in levels],
            "finite": bool(np.isfinite(st["u"]).all())}
+    if trace:
+        from . import timeline
+        timeline.record(grids[0], trace_steps, trace)
     for g in reversed(grids):
         g.close()
     return out
