@@ -183,7 +183,10 @@ int luma_gpu_get_time(const luma_gpu_grid *grid, int *t);
  * (src/GridObj_ops_lbm_optimised.cpp:36-193, as src/main_lbm.cpp:441 calls it) on the root grid: each
  * recursively advances every sub-grid two sub-steps, then this grid one
  * step (explode/coalesce, IBM pass and collision included).  Asynchronous
- * on the grid's stream. */
+ * on the grid's stream.  Inside a step, work forks onto streams the library
+ * owns (each grid's sub-grid stream and listed-site stream, of the highest
+ * priority) and joins back into the grid's stream before the step ends, so
+ * the grid's stream orders everything a step does. */
 int luma_gpu_step(luma_gpu_grid *root, int nsteps);
 /* No counterpart in the reference (its step is synchronous).  Blocks until
  * all work queued on the grid's stream has finished; reports a site that
