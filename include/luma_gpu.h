@@ -326,7 +326,12 @@ int luma_gpu_bfl_forces(luma_gpu_grid *grid, double *forces);
 int luma_gpu_io_lite(luma_gpu_grid *root, const char *dir, double tval, int precision, int rank);
 /* GridObj::io_restart(eWrite) (src/GridObj_ops_io.cpp:406-490) for the tree:
  * <dir>/restart_LBM_Rnk<rank>.out, level 0 then each sub-grid after its
- * parent; same snapshot and host-thread scheme as luma_gpu_io_lite. */
+ * parent; on a tree created with LUMA_FLAG_IBM also, as level 0's call has
+ * the ObjectManager do (ObjectManager::io_restart(eWrite),
+ * src/ObjectManager_ops_io.cpp:136-190), <dir>/restart_IBBody_Rnk<rank>.out
+ * with every IB body of the tree in creation order (a filament's markers
+ * where the FEM has moved them, then their initial positions); same
+ * snapshot and host-thread scheme as luma_gpu_io_lite. */
 int luma_gpu_io_restart(luma_gpu_grid *root, const char *dir, int rank);
 /* No counterpart in the reference (its writers are synchronous).  Waits
  * for the tree's pending writers; returns the first error they met. */

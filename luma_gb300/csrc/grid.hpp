@@ -115,6 +115,7 @@ namespace luma {
 // support lists built by ibm_findSupport (FP64, reference order).
 struct IbmBody {
     int nm = 0;
+    long long seq = 0;          // creation order over the process (the restart file lists bodies in it)
     std::vector<double> pos, vel, eps, ds, dil, area;  // per marker (pos/vel: 3 per marker)
     std::vector<int> off;                               // CSR offsets, nm + 1
     std::vector<int> si, sj, sk;                        // support site indices

@@ -12,6 +12,7 @@
 // atomics) and recomputes the macroscopic values there.
 #include <cuda_runtime.h>
 
+#include <atomic>
 #include <cmath>
 #include <cstring>
 #include <vector>
@@ -468,8 +469,10 @@ int luma_gpu_ibm_add_body(luma_gpu_grid *g, int nmarkers, const double *position
     if (g->hx.empty() || g->hy.empty() || g->hz.empty())
         return luma_set_error(LUMA_E_INVALID, "IB bodies need the grid's site positions");
     if (!g->ibm) g->ibm = new IbmState();
+    static std::atomic<long long> next_seq{0};
     IbmBody b;
     b.nm = nmarkers;
+    b.seq = next_seq++;
     b.pos.assign(positions, positions + 3 * (size_t)nmarkers);
     if (velocities) b.vel.assign(velocities, velocities + 3 * (size_t)nmarkers);
     else b.vel.assign(3 * (size_t)nmarkers, 0.0);

@@ -24,6 +24,7 @@
 // the host, while the GPU steps on.  luma_gpu_io_wait joins the writers.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cerrno>
 #include <cmath>
 #include <cstdio>
@@ -284,6 +285,98 @@ void record(IoJobs &J, int rc) {
     }
 }
 
+// ObjectManager::io_restart(eWrite) (src/ObjectManager_ops_io.cpp:136-190):
+// the number of bodies and a newline, then per body a "\t/\t" separator,
+// its marker count, "\t/\t", and per marker x, y, z (and, for a flexible
+// body, the old position) each followed by a tab; no final newline.
+int write_ibbody(const char *path, int nbodies, const int *nmarkers, const int *flexible, const double *positions,
+                 const double *positions0) {
+    FILE *fp = std::fopen(path, "w");
+    if (!fp) return luma_set_error(LUMA_E_INVALID, "io_restart: cannot open %s", path);
+    Out o{fp, {}, {}};
+    o.buf += std::to_string(nbodies);
+    o.buf += '\n';
+    size_t m0 = 0;
+    int rc = LUMA_OK;
+    for (int b = 0; b < nbodies && rc == LUMA_OK; ++b) {
+        const bool flex = flexible && flexible[b];
+        if (flex && !positions0) {
+            rc = luma_set_error(LUMA_E_INVALID, "io_restart: flexible body %d needs old positions", b);
+            break;
+        }
+        o.raw("\t/\t");
+        o.buf += std::to_string(nmarkers[b]);
+        o.raw("\t/\t");
+        for (int m = 0; m < nmarkers[b]; ++m) {
+            const size_t g = m0 + (size_t)m;
+            for (int d = 0; d < 3; ++d) o.gen(positions[3 * g + d]);
+            if (flex)
+                for (int d = 0; d < 3; ++d) o.gen(positions0[3 * g + d]);
+        }
+        m0 += (size_t)nmarkers[b];
+    }
+    const bool ok = o.flush(true);
+    if (std::fclose(fp) != 0 || !ok) rc = rc ? rc : luma_set_error(LUMA_E_INVALID, "io_restart: write failed");
+    return rc;
+}
+
+// The IB bodies of a tree for the restart file, in the order they were
+// created (ObjectManager's iBody order): each body's current marker
+// positions (a filament's from the device) and, for filaments, the
+// markers' initial positions (IBMarker::position0); rigid bodies' entries
+// of pos0 are zeros the writer does not read.
+struct IbBodies {
+    std::vector<int> nm, flex;
+    std::vector<double> pos, pos0;
+};
+
+int take_ib_bodies(luma_gpu_grid *root, IbBodies &out) {
+    struct Entry {
+        long long seq;
+        int nm, flex;
+        std::vector<double> pos, pos0;
+    };
+    std::vector<Entry> all;
+    std::vector<luma_gpu_grid *> todo{root};
+    while (!todo.empty()) {
+        luma_gpu_grid *g = todo.back();
+        todo.pop_back();
+        for (luma_gpu_grid *c : g->kids) todo.push_back(c);
+        if (!g->ibm) continue;
+        const luma::IbmState &st = *g->ibm;
+        std::vector<int> fidx(st.bodies.size(), -1), fbase(st.bodies.size(), 0);
+        int base = 0;
+        for (size_t k = 0; k < st.flex_body.size(); ++k) {
+            fidx[st.flex_body[k]] = (int)k;
+            fbase[st.flex_body[k]] = base;
+            base += st.flex[k].nm;
+        }
+        for (size_t b = 0; b < st.bodies.size(); ++b) {
+            const luma::IbmBody &bd = st.bodies[b];
+            Entry e{bd.seq, bd.nm, fidx[b] >= 0 ? 1 : 0, bd.pos, std::vector<double>(3 * (size_t)bd.nm, 0.0)};
+            if (e.flex) {
+                e.pos0 = st.flex[fidx[b]].mpos0;
+                if (st.ready) {
+                    cudaError_t err = cudaStreamSynchronize(g->stream);
+                    if (err == cudaSuccess)
+                        err = cudaMemcpy(e.pos.data(), st.fem.flex.pos + 3 * (size_t)fbase[b],
+                                         e.pos.size() * sizeof(double), cudaMemcpyDeviceToHost);
+                    if (err != cudaSuccess)
+                        return luma_set_error(LUMA_E_CUDA, "io_restart: filament markers: %s", cudaGetErrorString(err));
+                }
+            }
+            all.push_back(std::move(e));
+        }
+    }
+    std::sort(all.begin(), all.end(), [](const Entry &a, const Entry &b) { return a.seq < b.seq; });
+    for (const Entry &e : all) {
+        out.nm.push_back(e.nm);
+        out.flex.push_back(e.flex);
+        out.pos.insert(out.pos.end(), e.pos.begin(), e.pos.end());
+        out.pos0.insert(out.pos0.end(), e.pos0.begin(), e.pos0.end());
+    }
+    return LUMA_OK;
+}
 }  // namespace
 
 void luma_io_free(luma_gpu_grid *g) {
@@ -316,8 +409,16 @@ int luma_gpu_io_restart(luma_gpu_grid *root, const char *dir, int rank) {
     auto snaps = std::make_shared<std::vector<Snapshot>>();
     if (int rc = take_tree(root, *snaps)) return rc;
     IoJobs &J = jobs(root);
+    // with IBM on (L_IBM_ON), level 0's GridObj::io_restart also has the
+    // ObjectManager write every IB body (src/GridObj_ops_io.cpp:484-487)
+    std::shared_ptr<IbBodies> ib;
+    if (root->d.flags & LUMA_FLAG_IBM) {
+        ib = std::make_shared<IbBodies>();
+        if (int rc = take_ib_bodies(root, *ib)) return rc;
+    }
     const std::string path = std::string(dir) + "/restart_LBM_Rnk" + std::to_string(rank) + ".out";
-    J.threads.emplace_back([snaps, path, &J] {
+    const std::string ibpath = std::string(dir) + "/restart_IBBody_Rnk" + std::to_string(rank) + ".out";
+    J.threads.emplace_back([snaps, ib, path, ibpath, &J] {
         FILE *fp = std::fopen(path.c_str(), "w");
         if (!fp) {
             record(J, luma_set_error(LUMA_E_INVALID, "io_restart: cannot open %s", path.c_str()));
@@ -325,6 +426,9 @@ int luma_gpu_io_restart(luma_gpu_grid *root, const char *dir, int rank) {
         }
         for (const Snapshot &s : *snaps) record(J, write_restart(s, fp));
         if (std::fclose(fp) != 0) record(J, luma_set_error(LUMA_E_INVALID, "io_restart: close of %s failed", path.c_str()));
+        if (ib)
+            record(J, write_ibbody(ibpath.c_str(), (int)ib->nm.size(), ib->nm.data(), ib->flex.data(),
+                                   ib->pos.data(), ib->pos0.data()));
     });
     return LUMA_OK;
 }
@@ -418,41 +522,11 @@ int luma_io_restart_read(const char *path, int ngrids, const luma_grid_desc *con
     return LUMA_OK;
 }
 
-// ObjectManager::io_restart(eWrite) (src/ObjectManager_ops_io.cpp:136-190):
-// the number of bodies and a newline, then per body a "\t/\t" separator,
-// its marker count, "\t/\t", and per marker x, y, z (and, for a flexible
-// body, the old position) each followed by a tab; no final newline.
 int luma_io_ibbody_restart_write(const char *path, int nbodies, const int *nmarkers, const int *flexible,
                                  const double *positions, const double *positions0) {
     if (!path || nbodies < 0 || (nbodies > 0 && (!nmarkers || !positions)))
         return luma_set_error(LUMA_E_INVALID, "luma_io_ibbody_restart_write: null argument");
-    FILE *fp = std::fopen(path, "w");
-    if (!fp) return luma_set_error(LUMA_E_INVALID, "io_restart: cannot open %s", path);
-    Out o{fp, {}, {}};
-    o.buf += std::to_string(nbodies);
-    o.buf += '\n';
-    size_t m0 = 0;
-    int rc = LUMA_OK;
-    for (int b = 0; b < nbodies && rc == LUMA_OK; ++b) {
-        const bool flex = flexible && flexible[b];
-        if (flex && !positions0) {
-            rc = luma_set_error(LUMA_E_INVALID, "io_restart: flexible body %d needs old positions", b);
-            break;
-        }
-        o.raw("\t/\t");
-        o.buf += std::to_string(nmarkers[b]);
-        o.raw("\t/\t");
-        for (int m = 0; m < nmarkers[b]; ++m) {
-            const size_t g = m0 + (size_t)m;
-            for (int d = 0; d < 3; ++d) o.gen(positions[3 * g + d]);
-            if (flex)
-                for (int d = 0; d < 3; ++d) o.gen(positions0[3 * g + d]);
-        }
-        m0 += (size_t)nmarkers[b];
-    }
-    const bool ok = o.flush(true);
-    if (std::fclose(fp) != 0 || !ok) rc = rc ? rc : luma_set_error(LUMA_E_INVALID, "io_restart: write failed");
-    return rc;
+    return write_ibbody(path, nbodies, nmarkers, flexible, positions, positions0);
 }
 
 int luma_io_restart_write(const luma_grid_desc *desc, const double *f, const double *u, const double *rho,

@@ -4,7 +4,9 @@ CPU: the library's writers fed with the oracle's state (bit-exact with the
 reference) reproduce the files the reference's own writers produced on the
 same case byte for byte (SHA-256, tests/golden/make_io.py).
 GPU: the asynchronous snapshot writers on the device state (FP64) give the
-same layout, and values within one unit of the last printed digit.
+same layout, and values within one unit of the last printed digit; the
+IB-body restart file byte for byte (rigid bodies) or equal to the host
+writer's on the device's marker positions (a filament).
 """
 import hashlib
 import json
@@ -66,10 +68,14 @@ def _rows(path):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("case", CASES_IO[:2])
+@pytest.mark.parametrize("case", CASES_IO)
 def test_gpu_snapshot_writers_match_oracle(tmp_path, case):
+    """The same files from the device state; with IB bodies the restart also
+    writes restart_IBBody (rigid markers keep their positions, so that file
+    is the reference's byte for byte)."""
     from luma_gb300 import _abi as A
     from luma_gb300.gpu import GpuGrid
+    from tests.golden import cases as CASE_DEFS
     REF = ref_of(case)
     ref_dir = tmp_path / "ref"
     gpu_dir = tmp_path / "gpu"
@@ -77,12 +83,21 @@ def test_gpu_snapshot_writers_match_oracle(tmp_path, case):
     gpu_dir.mkdir()
     oracle_files(ref_dir, REF)
     gg, _ = R.build_backend(REF["case"], lambda d, p: GpuGrid(d, p), A.PREC_FP64)
+    bodies = CASE_DEFS.bodies(REF["case"])
+    for lev, reg, pos in bodies:
+        gg[lev].ibm_add_body(pos)
+    if bodies:
+        gg[0].ibm_initialise()
     gg[0].step(REF["steps"])
     gg[0].io_lite(str(gpu_dir), REF["steps"], REF["precision"])
     gg[0].io_restart(str(gpu_dir))
     gg[0].step(3)          # the GPU steps on while the host thread writes
     gg[0].io_wait()
     for name in REF["files"]:
+        if name.startswith("restart_IBBody"):
+            data = open(gpu_dir / name, "rb").read()
+            assert hashlib.sha256(data).hexdigest() == REF["files"][name]["sha256"], name
+            continue
         a, b = _rows(gpu_dir / name), _rows(ref_dir / name)
         assert len(a) == len(b), name
         for ra, rb in zip(a, b):
@@ -92,6 +107,30 @@ def test_gpu_snapshot_writers_match_oracle(tmp_path, case):
             # significant digits (restart)
             tol = dict(rtol=0.0, atol=2e-10) if name.startswith("io_lite") else dict(rtol=2e-5, atol=1e-9)
             assert np.allclose(np.array(ra[2:-1], float), np.array(rb[2:-1], float), **tol), name
+
+
+@pytest.mark.gpu
+def test_gpu_restart_lists_filament_markers(tmp_path):
+    """A filament's entry in restart_IBBody: the marker positions the FEM has
+    moved on the device, then the markers' initial positions (the
+    reference's IBMarker::position0); the file equals the host writer's on
+    the positions the device reports."""
+    from luma_gb300 import _abi as A
+    from luma_gb300 import gpu as G
+    from luma_gb300.gpu import GpuGrid
+    from tests.golden import cases as CASE_DEFS
+    name = sorted(n for n in CASE_DEFS.CASES if CASE_DEFS.CASES[n].get("filaments"))[0]
+    gg, levels = R.build_backend(name, lambda d, p: GpuGrid(d, p), A.PREC_FP64)
+    idx = R.attach_filaments(name, gg, levels, lambda g, **k: g.ibm_add_filament(**k))
+    gg[0].ibm_initialise()
+    start = [gg[0].ibm_markers(b)[:, 0:3].copy() for b in idx]
+    gg[0].step(20)
+    gg[0].io_restart(str(tmp_path))
+    gg[0].io_wait()
+    now = [gg[0].ibm_markers(b)[:, 0:3] for b in idx]
+    assert any(not np.array_equal(a, b) for a, b in zip(now, start))   # the filament moved
+    G.write_io_ibbody_restart(str(tmp_path / "host.out"), now, start)
+    assert open(tmp_path / "restart_IBBody_Rnk0.out", "rb").read() == open(tmp_path / "host.out", "rb").read()
 
 
 @pytest.mark.parametrize("case", CASES_IO)
