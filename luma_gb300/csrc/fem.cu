@@ -16,6 +16,8 @@
 
 #include <cmath>
 #include <cstring>
+#include <mutex>
+#include <utility>
 #include <vector>
 
 #include "dispatch.hpp"
@@ -39,6 +41,8 @@ constexpr size_t kFemSmemMax = 200 * 1024;
 struct FemKernelArgs {
     int nfil, maxdof, maxmk;
     int k_in_smem;              // K of the filament in dynamic shared memory
+    int lu32;                   // Newton steps solved with FP32 factors of the scaled matrix (shifted-FP32
+                                // grids; the matrix's FP32 copy follows K in dynamic shared memory)
     int eps_in_smem;            // the epsilon matrix of the filament in dynamic shared memory
     const int *node_off, *el_off, *dof_off, *mk_off, *bc;
     const double *dm, *velscale;
@@ -508,6 +512,97 @@ __device__ void lu_solve_dense(double *A, int lda, int off, int n, int *ipiv, do
 
 #undef AC
 
+// ---- FP32 factors for the shifted-FP32 path ----
+// The Newmark matrix K + a0 M of a filament is well conditioned once its
+// rows and columns are scaled by 1/sqrt|diagonal|: condition 7-44 against
+// 1.6e5-3.2e5 unscaled over the filament-array workload's rigidities
+// (EI 1e-3 .. 1e-1, a0 M / K 6e-2 .. 6 on the diagonal).  FP32 factors of
+// the scaled matrix then solve a Newton step to ~1e-6 relative, and the
+// iteration, whose residual and update stay FP64, converges to the same
+// 1e-10 tolerance.  The algorithm is the FP64 path's (the partial-pivot LU
+// and transposed solve of lu_factor / lu_solve_t), in FP32 with FMAs, on
+// one warp: an FP32 operation does not hold a sub-partition the 64 cycles
+// an FP64 one does, so the shuffles and shared-memory round trips of a
+// pivot step set its length.
+#define AF(r, c) A[(c) * lda + (r)]
+
+// A (n x n, column-major, lda) in place; whole-row interchanges; lim[c] =
+// last row of L's column c holding a non-zero.  band as lu_factor_banded's.
+__device__ __forceinline__ void lu32_factor(float *A, int lda, int n, int *ipiv, int band, int *lim) {
+    const unsigned full = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    for (int r = lane; r < n; r += 32) lim[r] = r;
+    __syncwarp();
+    for (int k = 0; k < n; ++k) {
+        const int nr = min(n, k + band + 1) - k;  // candidate rows k .. k+nr-1 (nr <= 32)
+        const int cend = min(n, k + 2 * band + 1);
+        float v = lane < nr ? fabsf(AF(k + lane, k)) : -1.0f;
+        int idx = lane;
+        for (int o = 16; o > 0; o >>= 1) {  // the largest magnitude, the first row on ties
+            const float ov = __shfl_xor_sync(full, v, o);
+            const int oi = __shfl_xor_sync(full, idx, o);
+            if (ov > v || (ov == v && oi < idx)) {
+                v = ov;
+                idx = oi;
+            }
+        }
+        const int p = k + idx;
+        if (lane == 0) ipiv[k] = p + 1;
+        if (!(v > 0.0f)) continue;  // a zero column: no interchange, no elimination
+        if (p != k) {
+            __syncwarp();
+            for (int c = lane; c < cend; c += 32) {
+                const float t = AF(k, c);
+                AF(k, c) = AF(p, c);
+                AF(p, c) = t;
+                if (c < k && t != 0.0f && p > lim[c]) lim[c] = p;
+            }
+            __syncwarp();
+        }
+        const float inv = 1.0f / AF(k, k);
+        float m = 0.0f;
+        if (lane >= 1 && lane < nr) {
+            m = AF(k + lane, k) * inv;
+            AF(k + lane, k) = m;
+        }
+        const unsigned nzm = __ballot_sync(full, m != 0.0f);
+        if (lane == 0 && nzm) lim[k] = k + 31 - __clz(nzm);
+        __syncwarp();
+        const int nrows = nr - 1, ncols = cend - k - 1;
+        for (int t = lane; t < nrows * ncols; t += 32) {
+            const int j = t / nrows, i = t - j * nrows;
+            const int r = k + 1 + i, c = k + 1 + j;
+            AF(r, c) = fmaf(-AF(r, k), AF(k, c), AF(r, c));
+        }
+        __syncwarp();
+    }
+}
+
+// A^T x = b with the factors of lu32_factor (b in x), one thread.
+__device__ __forceinline__ void lu32_solve_t(const float *A, int lda, int n, const int *ipiv, int band,
+                                             const int *lim, float *x) {
+    for (int r = 0; r < n; ++r) {
+        float s = x[r];
+        for (int c = r - 2 * band < 0 ? 0 : r - 2 * band; c < r; ++c) s = fmaf(-AF(c, r), x[c], s);
+        x[r] = s / AF(r, r);
+    }
+    for (int r = n - 1; r >= 0; --r) {
+        float s = x[r];
+        for (int c = r + 1; c <= lim[r]; ++c) s = fmaf(-AF(c, r), x[c], s);
+        x[r] = s;
+    }
+    for (int k = n - 1; k >= 0; --k) {
+        const int p = ipiv[k] - 1;
+        if (p != k) {
+            const float t = x[k];
+            x[k] = x[p];
+            x[p] = t;
+        }
+    }
+}
+
+#undef AF
+
 __device__ void lu_solve_block(double *A, int lda, int off, int n, int *ipiv, double *x, int band,
                                int *err = nullptr) {
     __shared__ int nzr[512], nzc[512];
@@ -686,8 +781,11 @@ __global__ void k_fem_dynamic(FemKernelArgs a) {
     double *Meff = a.tmp + 2 * (size_t)d0, *MF = a.tmp + 2 * (size_t)d0 + nd;
     __shared__ int ipiv[512], lim[512], rl[32], cl[32];
     __shared__ double sq[512], xs[512], rd[512];
+    __shared__ float sdf[512], yf[512];  // FP32 factors: the scale and the solve's vector
     __shared__ volatile int lu_progress;
     __shared__ int go;
+    const int n32 = nd - bc;
+    float *Kf = reinterpret_cast<float *>(fem_smem + (size_t)a.maxdof * a.maxdof);  // lu32 only
     const double Dt = a.dt;
     double *Kc = a.Kc + (size_t)f * a.maxdof * a.maxdof;
     int *ipc = a.ipc + (size_t)f * a.maxdof, *limc = a.limc + (size_t)f * a.maxdof;
@@ -705,7 +803,28 @@ __global__ void k_fem_dynamic(FemKernelArgs a) {
     int it = 0;
     double res = 0.0;
     do {
-        if (it == 0 && a.cache_mode == 2) {
+        if (it == 0 && a.cache_mode == 2 && a.lu32) {
+            // as below, with the FP32 factors and the scale kept after them
+            const float *Kcf = reinterpret_cast<const float *>(Kc);
+            for (int q = threadIdx.x; q < n32 * n32; q += blockDim.x) Kf[q] = Kcf[q];
+            for (int i = threadIdx.x; i < n32; i += blockDim.x) {
+                sdf[i] = Kcf[(size_t)n32 * n32 + i];
+                ipiv[i] = ipc[i];
+                lim[i] = limc[i];
+            }
+            for (int i = threadIdx.x; i < nd; i += blockDim.x) {
+                const double v = a.R[d0 + i] - a.Fc[d0 + i] + a.MFc[d0 + i];
+                a.Fv[d0 + i] = v;
+                a.delU[d0 + i] = v;
+            }
+            __syncthreads();
+            for (int i = threadIdx.x; i < n32; i += blockDim.x) yf[i] = (float)(sdf[i] * a.delU[d0 + bc + i]);
+            __syncthreads();
+            if (threadIdx.x == 0) lu32_solve_t(Kf, n32, n32, ipiv, 5, lim, yf);
+            __syncthreads();
+            for (int i = threadIdx.x; i < n32; i += blockDim.x) a.delU[d0 + bc + i] = (double)sdf[i] * (double)yf[i];
+            __syncthreads();
+        } else if (it == 0 && a.cache_mode == 2) {
             // the step's first Newton iteration again: its factors, internal
             // force and mass term from the step's first call, this call's load
             for (int q = threadIdx.x; q < nd * nd; q += blockDim.x) K[q] = Kc[q];
@@ -785,6 +904,39 @@ __global__ void k_fem_dynamic(FemKernelArgs a) {
         }
         for (int i = threadIdx.x; i < nd; i += blockDim.x) a.delU[d0 + i] = a.Fv[d0 + i];
         __syncthreads();
+        if (a.lu32) {
+            // scale rows and columns by 1/sqrt|K_ii| (the diagonal holds
+            // a0 M_ii > 0), factor and solve in FP32 (the column-major view
+            // of K, transposed solve, as below), unscale the update
+            for (int i = threadIdx.x; i < n32; i += blockDim.x) {
+                const double kii = fabs(K[(size_t)(bc + i) * nd + bc + i]);
+                sdf[i] = kii > 0.0 ? (float)(1.0 / sqrt(kii)) : 1.0f;
+            }
+            __syncthreads();
+            for (int q = threadIdx.x; q < n32 * n32; q += blockDim.x) {
+                const int c = q / n32, r = q - c * n32;  // Kf(r, c) = s_r K[bc+c][bc+r] s_c
+                const double v = K[(size_t)(bc + c) * nd + bc + r];
+                Kf[q] = v == 0.0 ? 0.0f : (float)((double)sdf[r] * v * (double)sdf[c]);
+            }
+            for (int i = threadIdx.x; i < n32; i += blockDim.x) yf[i] = (float)(sdf[i] * a.delU[d0 + bc + i]);
+            __syncthreads();
+            if (threadIdx.x < 32) {
+                lu32_factor(Kf, n32, n32, ipiv, 5, lim);
+                if (threadIdx.x == 0) lu32_solve_t(Kf, n32, n32, ipiv, 5, lim, yf);
+            }
+            __syncthreads();
+            for (int i = threadIdx.x; i < n32; i += blockDim.x) a.delU[d0 + bc + i] = (double)sdf[i] * (double)yf[i];
+            if (keep) {
+                float *Kcf = reinterpret_cast<float *>(Kc);
+                for (int q = threadIdx.x; q < n32 * n32; q += blockDim.x) Kcf[q] = Kf[q];
+                for (int i = threadIdx.x; i < n32; i += blockDim.x) {
+                    Kcf[(size_t)n32 * n32 + i] = sdf[i];
+                    ipc[i] = ipiv[i];
+                    limc[i] = lim[i];
+                }
+            }
+            __syncthreads();
+        } else {
         // an element couples the 6 DOFs of its two nodes: half-bandwidth 5.
         // Warp 0 factors; warp 1 (another FP64 unit) runs the forward solve
         // one column behind it; warp 0 then solves backward.
@@ -805,6 +957,7 @@ __global__ void k_fem_dynamic(FemKernelArgs a) {
                 ipc[i] = ipiv[i];
                 limc[i] = lim[i];
             }
+        }
         }
         }
         for (int i = threadIdx.x; i < bc; i += blockDim.x) a.delU[d0 + i] = 0.0;
@@ -1193,6 +1346,26 @@ static int zeros(T **dst, size_t n) {
 }
 
 // Upload every filament of the grid (called once by luma_gpu_ibm_initialise).
+// A kernel's dynamic shared-memory limit is process-wide: grids set up
+// later with smaller matrices must not lower it under earlier ones, so it
+// only ever rises (per kernel, under a lock).
+static bool raise_smem_limit(const void *kernel, size_t bytes) {
+    static std::mutex mu;
+    static std::vector<std::pair<const void *, size_t>> set;
+    std::lock_guard<std::mutex> lock(mu);
+    for (auto &e : set)
+        if (e.first == kernel) {
+            if (bytes <= e.second) return true;
+            if (cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes) != cudaSuccess)
+                return false;
+            e.second = bytes;
+            return true;
+        }
+    if (cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes) != cudaSuccess) return false;
+    set.emplace_back(kernel, bytes);
+    return true;
+}
+
 int luma_fem_upload(luma_gpu_grid *g) {
     IbmState &st = *g->ibm;
     FemDevice &d = st.fem;
@@ -1272,12 +1445,14 @@ int luma_fem_upload(luma_gpu_grid *g) {
         (rc = up(&sc.hz, g->hz)) || (rc = zeros(&sc.error, 1)))
         return rc;
     g_scratch.push_back({g, sc});
-    // a filament's stiffness and epsilon matrices in shared memory when they fit
+    // a filament's stiffness and epsilon matrices in shared memory when they
+    // fit; on shifted-FP32 grids the stiffness matrix's FP32 copy after it
     const size_t kb = (size_t)maxdof * maxdof * sizeof(double), eb = (size_t)maxmk * maxmk * sizeof(double);
-    d.k_in_smem = kb <= kFemSmemMax &&
-                  cudaFuncSetAttribute(k_fem_dynamic, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kb) == cudaSuccess;
-    d.eps_in_smem = eb <= kFemSmemMax &&
-                    cudaFuncSetAttribute(k_flex_support, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)eb) == cudaSuccess;
+    const size_t kb32 = kb + (size_t)maxdof * maxdof * sizeof(float);
+    d.lu32 = g->d.precision == LUMA_PREC_FP32_SHIFTED && kb32 <= kFemSmemMax &&
+             raise_smem_limit(reinterpret_cast<const void *>(k_fem_dynamic), kb32);
+    d.k_in_smem = d.lu32 || (kb <= kFemSmemMax && raise_smem_limit(reinterpret_cast<const void *>(k_fem_dynamic), kb));
+    d.eps_in_smem = eb <= kFemSmemMax && raise_smem_limit(reinterpret_cast<const void *>(k_flex_support), eb);
     cudaGetLastError();
     st.u_n = nullptr;
     const size_t rs = g->d.precision == LUMA_PREC_FP64 ? 8 : 4;
@@ -1323,7 +1498,8 @@ int luma_fem_move_bodies(luma_gpu_grid *g, const int *skip, bool first) {
     a.skip = skip;
     a.cache_mode = first ? 1 : 2;
     a.k_in_smem = g->ibm->fem.k_in_smem;
-    const size_t kb = (size_t)a.maxdof * a.maxdof * sizeof(double);
+    a.lu32 = g->ibm->fem.lu32;
+    const size_t kb = (size_t)a.maxdof * a.maxdof * (a.lu32 ? sizeof(double) + sizeof(float) : sizeof(double));
     k_fem_dynamic<<<a.nfil, 128, a.k_in_smem ? kb : 0, g->stream>>>(a);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return luma_set_error(LUMA_E_CUDA, "FEM: %s", cudaGetErrorString(e));

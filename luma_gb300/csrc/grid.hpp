@@ -177,6 +177,7 @@ struct FemDevice {
     double *res = nullptr, *fsi_res = nullptr;  // FSI residual: [0] running max, [1] last
     int *fsi_state = nullptr;                   // FSI loop of the step: [0] converged, [1] iterations
     int k_in_smem = 0, eps_in_smem = 0;         // the filament matrices fit in shared memory
+    int lu32 = 0;                               // Newton steps with FP32 factors (shifted-FP32 grids)
     // flexible IB marker arrays
     FlexArgs flex{};
 };
