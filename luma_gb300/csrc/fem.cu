@@ -578,27 +578,47 @@ __device__ __forceinline__ void lu32_factor(float *A, int lda, int n, int *ipiv,
     }
 }
 
-// A^T x = b with the factors of lu32_factor (b in x), one thread.
+// A^T x = b with the factors of lu32_factor (b in x), one warp.  Forward
+// U^T y = b: each lane keeps one pending row (lane, lane + 32, ...) and
+// subtracts a column's term as soon as its unknown is known (U's rows reach
+// 2*band < 32 right of the diagonal); backward L^T z = y and the
+// interchanges on one lane.
 __device__ __forceinline__ void lu32_solve_t(const float *A, int lda, int n, const int *ipiv, int band,
                                              const int *lim, float *x) {
-    for (int r = 0; r < n; ++r) {
-        float s = x[r];
-        for (int c = r - 2 * band < 0 ? 0 : r - 2 * band; c < r; ++c) s = fmaf(-AF(c, r), x[c], s);
-        x[r] = s / AF(r, r);
-    }
-    for (int r = n - 1; r >= 0; --r) {
-        float s = x[r];
-        for (int c = r + 1; c <= lim[r]; ++c) s = fmaf(-AF(c, r), x[c], s);
-        x[r] = s;
-    }
-    for (int k = n - 1; k >= 0; --k) {
-        const int p = ipiv[k] - 1;
-        if (p != k) {
-            const float t = x[k];
-            x[k] = x[p];
-            x[p] = t;
+    const unsigned full = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    float s = lane < n ? x[lane] : 0.0f;
+    int row = lane;
+    for (int c = 0; c < n; ++c) {
+        const float v = row < n ? AF(c, row) : 0.0f;
+        float y = 0.0f;
+        if (row == c) y = s / AF(c, c);
+        y = __shfl_sync(full, y, c & 31);
+        if (row == c) {
+            x[c] = y;
+            row += 32;
+            s = row < n ? x[row] : 0.0f;
+        } else if (row < n && row <= c + 2 * band) {
+            s = fmaf(-v, y, s);
         }
     }
+    __syncwarp();
+    if (lane == 0) {
+        for (int r = n - 1; r >= 0; --r) {
+            float z = x[r];
+            for (int c = r + 1; c <= lim[r]; ++c) z = fmaf(-AF(c, r), x[c], z);
+            x[r] = z;
+        }
+        for (int k = n - 1; k >= 0; --k) {
+            const int p = ipiv[k] - 1;
+            if (p != k) {
+                const float t = x[k];
+                x[k] = x[p];
+                x[p] = t;
+            }
+        }
+    }
+    __syncwarp();
 }
 
 #undef AF
@@ -820,7 +840,7 @@ __global__ void k_fem_dynamic(FemKernelArgs a) {
             __syncthreads();
             for (int i = threadIdx.x; i < n32; i += blockDim.x) yf[i] = (float)(sdf[i] * a.delU[d0 + bc + i]);
             __syncthreads();
-            if (threadIdx.x == 0) lu32_solve_t(Kf, n32, n32, ipiv, 5, lim, yf);
+            if (threadIdx.x < 32) lu32_solve_t(Kf, n32, n32, ipiv, 5, lim, yf);
             __syncthreads();
             for (int i = threadIdx.x; i < n32; i += blockDim.x) a.delU[d0 + bc + i] = (double)sdf[i] * (double)yf[i];
             __syncthreads();
@@ -912,17 +932,21 @@ __global__ void k_fem_dynamic(FemKernelArgs a) {
                 const double kii = fabs(K[(size_t)(bc + i) * nd + bc + i]);
                 sdf[i] = kii > 0.0 ? (float)(1.0 / sqrt(kii)) : 1.0f;
             }
+            for (int q = threadIdx.x; q < n32 * n32; q += blockDim.x) Kf[q] = 0.0f;
             __syncthreads();
-            for (int q = threadIdx.x; q < n32 * n32; q += blockDim.x) {
-                const int c = q / n32, r = q - c * n32;  // Kf(r, c) = s_r K[bc+c][bc+r] s_c
+            // K is zero more than 5 off the diagonal (an element couples
+            // the DOFs of two adjacent nodes): only the band is converted
+            for (int t = threadIdx.x; t < n32 * 11; t += blockDim.x) {
+                const int c = t / 11, r = c - 5 + (t - c * 11);  // Kf(r, c) = s_r K[bc+c][bc+r] s_c
+                if (r < 0 || r >= n32) continue;
                 const double v = K[(size_t)(bc + c) * nd + bc + r];
-                Kf[q] = v == 0.0 ? 0.0f : (float)((double)sdf[r] * v * (double)sdf[c]);
+                Kf[c * n32 + r] = (float)((double)sdf[r] * v * (double)sdf[c]);
             }
             for (int i = threadIdx.x; i < n32; i += blockDim.x) yf[i] = (float)(sdf[i] * a.delU[d0 + bc + i]);
             __syncthreads();
             if (threadIdx.x < 32) {
                 lu32_factor(Kf, n32, n32, ipiv, 5, lim);
-                if (threadIdx.x == 0) lu32_solve_t(Kf, n32, n32, ipiv, 5, lim, yf);
+                lu32_solve_t(Kf, n32, n32, ipiv, 5, lim, yf);
             }
             __syncthreads();
             for (int i = threadIdx.x; i < n32; i += blockDim.x) a.delU[d0 + bc + i] = (double)sdf[i] * (double)yf[i];
