@@ -17,7 +17,6 @@
 #include <cmath>
 #include <cstring>
 #include <mutex>
-#include <utility>
 #include <vector>
 
 #include "dispatch.hpp"
@@ -1370,23 +1369,30 @@ static int zeros(T **dst, size_t n) {
 }
 
 // Upload every filament of the grid (called once by luma_gpu_ibm_initialise).
-// A kernel's dynamic shared-memory limit is process-wide: grids set up
-// later with smaller matrices must not lower it under earlier ones, so it
-// only ever rises (per kernel, under a lock).
+// A kernel's dynamic shared-memory limit holds for every launch on its
+// device: grids set up later with smaller matrices must not lower it under
+// earlier ones, so it only ever rises (per device and kernel, under a lock).
 static bool raise_smem_limit(const void *kernel, size_t bytes) {
+    struct Limit {
+        int dev;
+        const void *kernel;
+        size_t bytes;
+    };
     static std::mutex mu;
-    static std::vector<std::pair<const void *, size_t>> set;
+    static std::vector<Limit> set;
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return false;
     std::lock_guard<std::mutex> lock(mu);
-    for (auto &e : set)
-        if (e.first == kernel) {
-            if (bytes <= e.second) return true;
+    for (Limit &e : set)
+        if (e.dev == dev && e.kernel == kernel) {
+            if (bytes <= e.bytes) return true;
             if (cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes) != cudaSuccess)
                 return false;
-            e.second = bytes;
+            e.bytes = bytes;
             return true;
         }
     if (cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes) != cudaSuccess) return false;
-    set.emplace_back(kernel, bytes);
+    set.push_back({dev, kernel, bytes});
     return true;
 }
 
